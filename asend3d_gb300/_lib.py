@@ -1,0 +1,95 @@
+"""ctypes binding of ``libasend_gpu.so`` (the C ABI in ``include/asend_gpu.h``).
+
+The library is built in-tree by ``asend3d_gb300.build``.  Loading fails loudly
+when it is missing: there is no CPU fallback for the solve path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libasend_gpu.so"
+
+c_int = C.c_int32
+c_dbl = C.c_double
+P_int = C.POINTER(C.c_int32)
+P_i64 = C.POINTER(C.c_int64)
+P_dbl = C.POINTER(C.c_double)
+
+ASEND_OK, ASEND_MAX_ITER, ASEND_NONFINITE, ASEND_FALLBACK = 0, 1, 2, 3
+ASEND_EINVAL, ASEND_ECUDA, ASEND_ESTATE = -1, -2, -3
+METHOD_FP64, METHOD_MIXED = 0, 1
+PC_JACOBI, PC_BLOCK, PC_LEARNED = 0, 1, 2
+OBJ_DISPLACEMENT, OBJ_COMPLIANCE = 0, 1
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("method", c_int), ("precond", c_int), ("rel_tol", c_dbl), ("max_iter", c_int),
+                ("graph_iters", c_int), ("warm_start", c_int), ("replace_every", c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", c_int), ("status", c_int), ("replacements", c_int), ("n_rhs", c_int),
+                ("rel_residual", c_dbl), ("ms_assemble", c_dbl), ("ms_solve", c_dbl),
+                ("ms_adjoint", c_dbl), ("penalty_scale", c_dbl)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# (name, restype, argtypes) for every symbol declared in include/asend_gpu.h
+SIGNATURES = [
+    ("asend_create", C.c_void_p, [c_int]),
+    ("asend_destroy", None, [C.c_void_p]),
+    ("asend_last_error", C.c_char_p, [C.c_void_p]),
+    ("asend_version", C.c_char_p, []),
+    ("asend_set_mesh", c_int, [C.c_void_p, c_int, c_int, P_dbl, c_int, P_int, P_dbl, P_dbl, P_dbl, P_dbl]),
+    ("asend_set_modulus", c_int, [C.c_void_p, P_dbl]),
+    ("asend_add_node_set", c_int, [C.c_void_p, c_int, P_int]),
+    ("asend_add_element_set", c_int, [C.c_void_p, c_int, P_int]),
+    ("asend_add_constraint", c_int, [C.c_void_p, c_int, P_int, P_int, P_dbl, c_dbl]),
+    ("asend_add_nodal_force", c_int, [C.c_void_p, c_int, c_int, P_dbl]),
+    ("asend_add_surface_traction", c_int, [C.c_void_p, c_int, c_int, P_dbl, c_dbl, P_dbl]),
+    ("asend_add_load_vector", c_int, [C.c_void_p, c_int, P_dbl]),
+    ("asend_clear_loads", c_int, [C.c_void_p]),
+    ("asend_n_dof", c_int, [C.c_void_p]),
+    ("asend_n_load_cases", c_int, [C.c_void_p]),
+    ("asend_get_load_vector", c_int, [C.c_void_p, c_int, P_dbl]),
+    ("asend_assemble", c_int, [C.c_void_p, c_int, c_int, c_dbl, c_dbl, c_dbl]),
+    ("asend_get_csr", c_int, [C.c_void_p, c_int, P_i64, P_i64, P_int, P_dbl]),
+    ("asend_get_coloring", c_int, [C.c_void_p, P_int]),
+    ("asend_static_solve", c_int, [C.c_void_p, C.POINTER(SolveOpts), P_dbl, C.POINTER(SolveStats)]),
+    ("asend_static_solve_device", c_int, [C.c_void_p, C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
+    ("asend_get_solution", c_int, [C.c_void_p, c_int, P_dbl]),
+    ("asend_set_objective", c_int, [C.c_void_p, c_int, c_int, c_int, c_dbl]),
+    ("asend_adjoint_gradient", c_int, [C.c_void_p, C.POINTER(SolveOpts), P_dbl, P_dbl, C.POINTER(SolveStats)]),
+    ("asend_add_modulus_design_var", c_int, [C.c_void_p, c_int, c_int, P_dbl]),
+    ("asend_design_var_gradient", c_int, [C.c_void_p, P_dbl, P_dbl]),
+    ("asend_newmark_run", c_int, [C.c_void_p, C.POINTER(SolveOpts), c_int, P_dbl, c_int, P_dbl, P_dbl,
+                                  C.POINTER(SolveStats)]),
+    ("asend_apply_operator", c_int, [C.c_void_p, c_int, P_dbl, P_dbl]),
+    ("asend_time_spmv", c_int, [C.c_void_p, c_int, c_int, P_dbl, P_dbl]),
+    ("asend_kernel_launches", C.c_int64, [C.c_void_p]),
+    ("asend_stream", C.c_void_p, [C.c_void_p]),
+]
+
+_lib = None
+
+
+def load(path: Path | str | None = None) -> C.CDLL:
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+                           "(the solve path has no CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib

@@ -1,0 +1,99 @@
+"""Seeded synthetic workloads with the shapes of the five benchmark cases.
+
+No public dataset is involved; every input is generated here from a seed.
+
+  cantilever_small   20x4x4 hex8 bar 2.0 x 0.4 x 0.4 m, E = 200 GPa, nu = 0.3,
+                     x = 0 face fixed, 1 kN downward load at the free end's
+                     top-centre node, objective = tip u_z, modulus DVs
+                     (80 column groups and 320 per-element).
+  block_large        200x40x40 hex8 (1.01 M DOF), lognormal modulus (median
+                     70 GPa, sigma_log 0.3, correlation 0.1 L), nu = 0.33,
+                     fixed end + distributed end-face traction, compliance.
+  batch_uq           64 blocks, nx in [20,120], ny = nz in [4,16], own field
+                     each, 4 load cases (tip -z, tip +y, torsion couple,
+                     uniform end traction).
+  learned_grid       128x64x64 hex8 (1.6 M DOF), sigma_log 0.5, corr 0.05 L.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .mesh import block_hex8, lognormal_modulus
+from .solver import Problem
+
+BAR = (2.0, 0.4, 0.4)
+
+
+def _fixed_end(p: Problem, mesh):
+    p.add_node_set("xMin", mesh.nodes_in_range(xr=(-1e-9, 1e-9)))
+    p.fix_displacement("xMin")
+
+
+def cantilever_small(nx=20, ny=4, nz=4, E=200e9, nu=0.3, F=-1000.0) -> Problem:
+    m = block_hex8(nx, ny, nz, *BAR)
+    p = Problem(m, np.full(m.n_elems, E), np.full(m.n_elems, nu), np.full(m.n_elems, 7850.0))
+    _fixed_end(p, m)
+    tip = m.node_id(nx, ny // 2, nz)
+    p.add_node_set("tip", [int(tip)])
+    p.add_nodal_force("tip", [0.0, 0.0, F])
+    p.objective = ("displacement", "tip", 3, 1.0)
+    p.add_elem_set("all", np.arange(m.n_elems))
+    # 80 DVs: one per (ix, iy) column of elements over iz; then 320 per element
+    for i in range(nx):
+        for j in range(ny):
+            name = f"col_{i}_{j}"
+            p.add_elem_set(name, m.elem_id(i, j, np.arange(nz)))
+            p.design_vars.append((name, [1.0]))
+    return p
+
+
+def block_large(nx=200, ny=40, nz=40, median=70e9, sigma_log=0.3, corr=0.1, nu=0.33, seed=2024,
+                traction=(0.0, 0.0, -1.0e6)) -> Problem:
+    m = block_hex8(nx, ny, nz, *BAR)
+    E = lognormal_modulus(m, median, sigma_log, corr, seed)
+    p = Problem(m, E, np.full(m.n_elems, nu), np.full(m.n_elems, 2700.0))
+    _fixed_end(p, m)
+    p.add_elem_set("xMaxEls", m.elem_id(nx - 1, *np.meshgrid(np.arange(ny), np.arange(nz), indexing="ij")).ravel())
+    p.add_surface_traction("xMaxEls", (1.0, 0.0, 0.0), traction)
+    p.objective = ("compliance",)
+    return p
+
+
+def batch_instance(k: int, seed: int = 7, median=70e9, sigma_log=0.3, corr=0.1, nu=0.33) -> Problem:
+    """Instance k of the 64-instance sweep with its 4 load cases."""
+    rng = np.random.default_rng([seed, k])
+    nx = int(rng.integers(20, 121))
+    ny = int(rng.integers(4, 17))
+    nz = ny
+    m = block_hex8(nx, ny, nz, *BAR)
+    E = lognormal_modulus(m, median, sigma_log, corr, int(rng.integers(1 << 30)))
+    p = Problem(m, E, np.full(m.n_elems, nu), np.full(m.n_elems, 2700.0))
+    _fixed_end(p, m)
+    end = m.nodes_in_range(xr=(BAR[0] - 1e-9, BAR[0] + 1e-9))
+    p.add_node_set("xMax", end)
+    p.add_node_set("tip", [int(m.node_id(nx, ny // 2, nz))])
+    p.add_nodal_force("tip", [0.0, 0.0, -1000.0], case=0)
+    p.add_nodal_force("tip", [0.0, 1000.0, 0.0], case=1)
+    # torsion couple about the bar axis on the end face: f = T * (-dz, dy) / sum r^2
+    xyz = m.coords[end]
+    dy, dz = xyz[:, 1] - BAR[1] / 2, xyz[:, 2] - BAR[2] / 2
+    r2 = float(np.sum(dy * dy + dz * dz))
+    f = np.zeros(m.n_dof)
+    f[3 * end + 1] = -1000.0 * dz / r2
+    f[3 * end + 2] = 1000.0 * dy / r2
+    p.add_load_vector(f, case=2)
+    p.add_elem_set("xMaxEls", m.elem_id(nx - 1, *np.meshgrid(np.arange(ny), np.arange(nz), indexing="ij")).ravel())
+    p.add_surface_traction("xMaxEls", (1.0, 0.0, 0.0), (1.0e6, 0.0, 0.0), case=3)
+    p.objective = ("compliance",)
+    return p
+
+
+def learned_grid(seed=11, nx=128, ny=64, nz=64, median=70e9, sigma_log=0.5, corr=0.05, nu=0.33) -> Problem:
+    m = block_hex8(nx, ny, nz, *BAR)
+    E = lognormal_modulus(m, median, sigma_log, corr, seed)
+    p = Problem(m, E, np.full(m.n_elems, nu), np.full(m.n_elems, 2700.0))
+    _fixed_end(p, m)
+    p.add_elem_set("xMaxEls", m.elem_id(nx - 1, *np.meshgrid(np.arange(ny), np.arange(nz), indexing="ij")).ravel())
+    p.add_surface_traction("xMaxEls", (1.0, 0.0, 0.0), (0.0, 0.0, -1.0e6))
+    p.objective = ("compliance",)
+    return p

@@ -1,0 +1,845 @@
+// api.cu -- C ABI entry points and the host-side model (C++).
+//
+// The host side restates the reference's model container and input semantics
+// (solverSrc/asend_run_job/src/model_input.rs, model_prep.rs, const_meth.rs,
+// model_analysis.rs load building) and drives the CUDA kernels of
+// k_assemble.cu, k_pcg.cu, k_adjoint.cu and k_newmark.cu.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <numeric>
+
+#include "common.cuh"
+
+using namespace asend;
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+
+int nodes_per_elem(int type) {
+    switch (type) {
+        case 8: return 8;
+        case 4: return 4;
+        default: return 0;
+    }
+}
+
+template <typename F>
+int guarded(asend_ctx* ctx, F&& fn) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c) return ASEND_EINVAL;
+    try {
+        c->err.clear();
+        return fn(*c);
+    } catch (const InputError& e) {
+        c->err = e.msg;
+        return ASEND_EINVAL;
+    } catch (const CudaError& e) {
+        c->err = e.msg;
+        return ASEND_ECUDA;
+    } catch (const std::exception& e) {
+        c->err = e.what();
+        return ASEND_ECUDA;
+    }
+}
+
+void require(bool ok, const char* msg) {
+    if (!ok) throw InputError(msg);
+}
+
+// Hex8 / tet4 face tables (local node lists, element_meth.rs:525-591 and
+// :460-490) used by the surface-traction load builder.
+const int kHexFaces[6][4] = {{3, 2, 1, 0}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                             {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+const int kTetFaces[4][3] = {{0, 2, 1}, {0, 1, 3}, {1, 2, 3}, {0, 3, 2}};
+
+// Consistent unit-density mass image of a face traction, restricted to the
+// face nodes and rescaled to area*|t| (element_equations.rs:1970-2043).  For
+// the trilinear hex / linear tet the restriction of N_a N_b over the element
+// is evaluated with the element's own Gauss rule on the host.
+void face_load(const Ctx& c, int e, const int* ln, int fnn, const double* trac, double* el_ld) {
+    const int nn = c.nn, tot = 3 * nn;
+    double xyz[24];
+    for (int a = 0; a < nn; ++a)
+        for (int j = 0; j < 3; ++j) xyz[3 * a + j] = c.xyz[3 * (size_t)c.conn[(size_t)e * nn + a] + j];
+    // Gauss data
+    const double g = 0.5773502691896257;
+    double pts[8][3];
+    double wts[8];
+    int np;
+    if (c.type == 8) {
+        np = 8;
+        int k = 0;
+        for (int zc = 0; zc < 2; ++zc)
+            for (int yc = 0; yc < 2; ++yc)
+                for (int xc = 0; xc < 2; ++xc) {
+                    pts[k][0] = xc ? g : -g;
+                    pts[k][1] = yc ? g : -g;
+                    pts[k][2] = zc ? g : -g;
+                    wts[k] = 1.0;
+                    ++k;
+                }
+    } else {
+        np = 1;
+        pts[0][0] = pts[0][1] = pts[0][2] = 0.25;
+        wts[0] = 1.0 / 6.0;
+    }
+    double acc[24] = {0};
+    for (int q = 0; q < fnn; ++q)
+        for (int i = 0; i < 3; ++i) acc[3 * ln[q] + i] = trac[i];
+    double ld[24] = {0};
+    for (int p = 0; p < np; ++p) {
+        double N[8], dN[8][3];
+        const double* s = pts[p];
+        if (c.type == 8) {
+            const double sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                     {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+            for (int a = 0; a < 8; ++a) {
+                const double f0 = 1 + sg[a][0] * s[0], f1 = 1 + sg[a][1] * s[1], f2 = 1 + sg[a][2] * s[2];
+                N[a] = 0.125 * f0 * f1 * f2;
+                dN[a][0] = 0.125 * sg[a][0] * f1 * f2;
+                dN[a][1] = 0.125 * sg[a][1] * f0 * f2;
+                dN[a][2] = 0.125 * sg[a][2] * f0 * f1;
+            }
+        } else {
+            N[0] = 1 - s[0] - s[1] - s[2]; N[1] = s[0]; N[2] = s[1]; N[3] = s[2];
+            const double d[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+            std::memcpy(dN, d, sizeof(d));
+        }
+        double J[3][3] = {{0}};
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                for (int a = 0; a < nn; ++a) J[i][j] += xyz[3 * a + i] * dN[a][j];
+        const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                           J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        const double w = det * wts[p];
+        for (int i = 0; i < tot; ++i) {
+            double a = 0;
+            for (int b = 0; b < nn; ++b) a += N[i / 3] * N[b] * acc[3 * b + i % 3];
+            ld[i] += a * w;
+        }
+    }
+    double tf[3] = {0, 0, 0};
+    for (int i = 0; i < tot; ++i) {
+        bool in_face = false;
+        for (int q = 0; q < fnn; ++q) in_face |= (ln[q] == i / 3);
+        el_ld[i] = in_face ? ld[i] : 0.0;
+        tf[i % 3] += el_ld[i];
+    }
+    // area and scale
+    double v1[3], v2[3], nr[3];
+    for (int i = 0; i < 3; ++i) {
+        if (fnn == 4) {
+            v1[i] = xyz[3 * ln[2] + i] - xyz[3 * ln[0] + i];
+            v2[i] = xyz[3 * ln[3] + i] - xyz[3 * ln[1] + i];
+        } else {
+            v1[i] = xyz[3 * ln[1] + i] - xyz[3 * ln[0] + i];
+            v2[i] = xyz[3 * ln[2] + i] - xyz[3 * ln[0] + i];
+        }
+    }
+    nr[0] = v1[1] * v2[2] - v1[2] * v2[1];
+    nr[1] = v1[2] * v2[0] - v1[0] * v2[2];
+    nr[2] = v1[0] * v2[1] - v1[1] * v2[0];
+    const double area = 0.5 * std::sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
+    const double vmag = std::sqrt(tf[0] * tf[0] + tf[1] * tf[1] + tf[2] * tf[2]);
+    const double imag = std::sqrt(trac[0] * trac[0] + trac[1] * trac[1] + trac[2] * trac[2]);
+    const double scale = area * imag / vmag;
+    for (int i = 0; i < tot; ++i) el_ld[i] *= scale;
+}
+
+void ensure_case(Ctx& c, int rhs) {
+    require(rhs >= 0 && rhs < 4096, "load case index out of range");
+    require(c.n_dof > 0, "set the mesh before adding loads");
+    while ((int)c.loads.size() <= rhs) c.loads.emplace_back(c.n_dof, 0.0);
+}
+
+}  // namespace
+
+namespace asend {
+
+// Pattern: node adjacency from elements plus constraint couplings; sliced
+// block-ELL layout; element slot map; greedy element colouring; penalty
+// entry list.
+void build_pattern(Ctx& c) {
+    const int N = c.n_nodes, nn = c.nn, b = c.dpn, b2 = b * b;
+    std::vector<std::vector<int32_t>> adj(N);
+    for (int e = 0; e < c.n_el; ++e)
+        for (int a = 0; a < nn; ++a)
+            for (int q = 0; q < nn; ++q) adj[c.conn[(size_t)e * nn + a]].push_back(c.conn[(size_t)e * nn + q]);
+    const int nrow_c = (int)c.c_rhs.size();
+    for (int r = 0; r < nrow_c; ++r)
+        for (int k = c.c_ptr[r]; k < c.c_ptr[r + 1]; ++k)
+            for (int k2 = c.c_ptr[r]; k2 < c.c_ptr[r + 1]; ++k2)
+                adj[c.c_dof[k] / b].push_back(c.c_dof[k2] / b);
+    for (int i = 0; i < N; ++i) {
+        auto& v = adj[i];
+        if (v.empty()) v.push_back(i);  // isolated node keeps a diagonal block
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        require(v.size() <= 255, "a node has more than 255 neighbouring nodes");
+    }
+    Sbell& A = c.A;
+    A.b = b;
+    A.n_rows = N;
+    A.n_slices = (N + kSlice - 1) / kSlice;
+    A.h_slice_off.assign(A.n_slices + 1, 0);
+    A.h_row_len.assign(N, 0);
+    A.h_diag.assign(N, 0);
+    for (int s = 0; s < A.n_slices; ++s) {
+        size_t w = 0;
+        for (int r = s * kSlice; r < std::min(N, (s + 1) * kSlice); ++r) w = std::max(w, adj[r].size());
+        A.h_slice_off[s + 1] = A.h_slice_off[s] + (int64_t)w;
+    }
+    A.n_groups = A.h_slice_off[A.n_slices];
+    A.h_col.assign((size_t)A.n_groups * kSlice, 0);
+    for (int r = 0; r < N; ++r) {
+        const int s = r / kSlice, lane = r % kSlice;
+        const int64_t w = A.h_slice_off[s + 1] - A.h_slice_off[s];
+        A.h_row_len[r] = (uint8_t)adj[r].size();
+        for (int64_t j = 0; j < w; ++j) {
+            const int col = (j < (int64_t)adj[r].size()) ? adj[r][j] : r;
+            A.h_col[(size_t)(A.h_slice_off[s] + j) * kSlice + lane] = col;
+            if (j < (int64_t)adj[r].size() && adj[r][j] == r) A.h_diag[r] = (uint8_t)j;
+        }
+    }
+    auto pos = [&](int row, int col) -> int {
+        const auto& v = adj[row];
+        auto it = std::lower_bound(v.begin(), v.end(), col);
+        return (int)(it - v.begin());
+    };
+    // element slot map
+    std::vector<int32_t> slot_map((size_t)c.n_el * nn * nn);
+    for (int e = 0; e < c.n_el; ++e)
+        for (int a = 0; a < nn; ++a) {
+            const int ra = c.conn[(size_t)e * nn + a];
+            for (int q = 0; q < nn; ++q) {
+                const int cb = c.conn[(size_t)e * nn + q];
+                slot_map[((size_t)e * nn + a) * nn + q] = (int32_t)A.slot(ra, pos(ra, cb));
+            }
+        }
+    // penalty entries: value index of (dof_i, dof_j) for every term pair
+    std::vector<int64_t> pen_idx;
+    std::vector<double> pen_coef;
+    for (int r = 0; r < nrow_c; ++r)
+        for (int k = c.c_ptr[r]; k < c.c_ptr[r + 1]; ++k)
+            for (int k2 = c.c_ptr[r]; k2 < c.c_ptr[r + 1]; ++k2) {
+                const int di = c.c_dof[k], dj = c.c_dof[k2];
+                const int ni = di / b, ai = di % b, nj = dj / b, aj = dj % b;
+                const int64_t slot = A.slot(ni, pos(ni, nj));
+                const int64_t g = slot / kSlice, lane = slot % kSlice;
+                pen_idx.push_back((g * b2 + ai * b + aj) * kSlice + lane);
+                pen_coef.push_back(c.c_coef[k] * c.c_coef[k2]);
+            }
+    // greedy colouring with per-node colour masks
+    std::vector<uint64_t> mask(N, 0);
+    c.colour_of.assign(c.n_el, 0);
+    int n_col = 0;
+    for (int e = 0; e < c.n_el; ++e) {
+        uint64_t used = 0;
+        for (int a = 0; a < nn; ++a) used |= mask[c.conn[(size_t)e * nn + a]];
+        require(~used != 0, "element colouring needs more than 64 colours");
+        int col = 0;
+        while (used & (1ull << col)) ++col;
+        c.colour_of[e] = col;
+        n_col = std::max(n_col, col + 1);
+        for (int a = 0; a < nn; ++a) mask[c.conn[(size_t)e * nn + a]] |= (1ull << col);
+    }
+    c.colour_ptr.assign(n_col + 1, 0);
+    for (int e = 0; e < c.n_el; ++e) c.colour_ptr[c.colour_of[e] + 1]++;
+    for (int k = 0; k < n_col; ++k) c.colour_ptr[k + 1] += c.colour_ptr[k];
+    c.colour_elems.assign(c.n_el, 0);
+    {
+        std::vector<int32_t> fill(c.colour_ptr.begin(), c.colour_ptr.end() - 1);
+        for (int e = 0; e < c.n_el; ++e) c.colour_elems[fill[c.colour_of[e]]++] = e;
+    }
+    // uploads
+    cudaStream_t s = c.stream;
+    A.slice_off.upload(A.h_slice_off, s);
+    A.col.upload(A.h_col, s);
+    A.row_len.upload(A.h_row_len, s);
+    A.diag.upload(A.h_diag, s);
+    c.d_slot_map.upload(slot_map, s);
+    c.d_colour_elems.upload(c.colour_elems, s);
+    c.d_pen_idx.upload(pen_idx, s);
+    c.d_pen_coef.upload(pen_coef, s);
+    ASEND_CUDA(cudaStreamSynchronize(s));
+    c.pattern_ready = true;
+}
+
+// Load vectors incl. the penalty right-hand side -sf C^T (C*0 - q) = sf C^T q
+// (const_meth.rs:105-119 at u = 0) to the device.
+void upload_rhs(Ctx& c) {
+    const int nr = std::max<int>(1, (int)c.loads.size());
+    if (c.loads.empty()) c.loads.emplace_back(c.n_dof, 0.0);
+    std::vector<double> f((size_t)nr * c.n_dof);
+    for (int r = 0; r < nr; ++r) {
+        double* fr = &f[(size_t)r * c.n_dof];
+        std::copy(c.loads[r].begin(), c.loads[r].end(), fr);
+        const int nrow_c = (int)c.c_rhs.size();
+        for (int q = 0; q < nrow_c; ++q) {
+            const double qq = c.sf * c.c_rhs[q];
+            for (int k = c.c_ptr[q]; k < c.c_ptr[q + 1]; ++k) fr[c.c_dof[k]] += c.c_coef[k] * qq;
+        }
+    }
+    c.nrhs = nr;
+    c.d_f.upload(f, c.stream);
+}
+
+}  // namespace asend
+
+extern "C" {
+
+const char* asend_version(void) {
+    return "asend_gpu 0.1 (sm_103a; sliced block-ELL; mixed FP32/FP64 PCG)";
+}
+
+asend_ctx* asend_create(int32_t device) {
+    Ctx* c = new Ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return nullptr;
+    }
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
+    if (cudaMallocHost(&c->h_sc, sizeof(PcgScalars) * 64) != cudaSuccess) {
+        delete c;
+        return nullptr;
+    }
+    return reinterpret_cast<asend_ctx*>(c);
+}
+
+void asend_destroy(asend_ctx* ctx) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->h_sc) cudaFreeHost(c->h_sc);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* asend_last_error(const asend_ctx* ctx) {
+    const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
+    return c ? c->err.c_str() : "null context";
+}
+
+void* asend_stream(const asend_ctx* ctx) {
+    const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
+    return c ? reinterpret_cast<void*>(c->stream) : nullptr;
+}
+
+int64_t asend_kernel_launches(const asend_ctx* ctx) {
+    const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
+    return c ? c->launches : -1;
+}
+
+int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const double* coords,
+                   int32_t n_elems, const int32_t* conn, const double* E, const double* nu,
+                   const double* rho, const double* thickness) {
+    return guarded(ctx, [&](Ctx& c) {
+        const int nn = nodes_per_elem(elem_type);
+        require(nn > 0, "unsupported element type (supported: 8 hex8, 4 tet4)");
+        require(n_nodes > 0 && n_elems > 0 && coords && conn && E && nu, "empty or null mesh input");
+        for (int64_t k = 0; k < (int64_t)n_elems * nn; ++k)
+            require(conn[k] >= 0 && conn[k] < n_nodes, "connectivity refers to a node out of range");
+        for (int e = 0; e < n_elems; ++e) {
+            require(std::isfinite(E[e]) && E[e] > 0.0, "element modulus must be positive and finite");
+            require(nu[e] > -1.0 && nu[e] < 0.5, "Poisson ratio out of range (-1, 0.5)");
+        }
+        ASEND_CUDA(cudaSetDevice(c.device));
+        c.type = elem_type;
+        c.nn = nn;
+        c.dpn = 3;
+        c.nip = (elem_type == 8) ? 8 : 1;
+        c.n_nodes = n_nodes;
+        c.n_el = n_elems;
+        c.n_dof = n_nodes * c.dpn;
+        c.xyz.assign(coords, coords + (size_t)3 * n_nodes);
+        c.conn.assign(conn, conn + (size_t)n_elems * nn);
+        c.E.assign(E, E + n_elems);
+        c.nu.assign(nu, nu + n_elems);
+        c.rho.assign(n_elems, 0.0);
+        if (rho) c.rho.assign(rho, rho + n_elems);
+        c.thk.clear();
+        if (thickness) c.thk.assign(thickness, thickness + n_elems);
+        c.node_sets.clear();
+        c.elem_sets.clear();
+        c.c_ptr.assign(1, 0);
+        c.c_dof.clear();
+        c.c_coef.clear();
+        c.c_rhs.clear();
+        c.loads.clear();
+        c.dv_ptr.assign(1, 0);
+        c.dv_el.clear();
+        c.dv_coef.clear();
+        c.pattern_ready = c.assembled = c.solved = false;
+        c.d_xyz.upload(c.xyz, c.stream);
+        c.d_conn.upload(c.conn, c.stream);
+        c.d_E.upload(c.E, c.stream);
+        c.d_nu.upload(c.nu, c.stream);
+        c.d_rho.upload(c.rho, c.stream);
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        return ASEND_OK;
+    });
+}
+
+int asend_set_modulus(asend_ctx* ctx, const double* E) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.n_el > 0 && E, "set the mesh first");
+        for (int e = 0; e < c.n_el; ++e)
+            require(std::isfinite(E[e]) && E[e] > 0.0, "element modulus must be positive and finite");
+        c.E.assign(E, E + c.n_el);
+        c.d_E.upload(c.E, c.stream);
+        c.assembled = c.solved = false;
+        return ASEND_OK;
+    });
+}
+
+int asend_add_node_set(asend_ctx* ctx, int32_t n, const int32_t* nodes) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(n >= 1 && nodes, "empty node set");
+        for (int i = 0; i < n; ++i) require(nodes[i] >= 0 && nodes[i] < c.n_nodes, "node set entry out of range");
+        c.node_sets.emplace_back(nodes, nodes + n);
+        return (int)c.node_sets.size() - 1;
+    });
+}
+
+int asend_add_element_set(asend_ctx* ctx, int32_t n, const int32_t* elems) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(n >= 1 && elems, "empty element set");
+        for (int i = 0; i < n; ++i) require(elems[i] >= 0 && elems[i] < c.n_el, "element set entry out of range");
+        c.elem_sets.emplace_back(elems, elems + n);
+        return (int)c.elem_sets.size() - 1;
+    });
+}
+
+// const_meth.rs:30-90 (Constraint::build_mat): the row count is the largest
+// term-set size; a term over a one-node set adds that DOF to every row, a term
+// over an n-node set adds its k-th node to row k.
+int asend_add_constraint(asend_ctx* ctx, int32_t n_terms, const int32_t* node_set,
+                         const int32_t* comp, const double* coef, double rhs) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(n_terms >= 1 && node_set && comp && coef, "constraint needs at least one term");
+        size_t rows = 1;
+        for (int t = 0; t < n_terms; ++t) {
+            require(node_set[t] >= 0 && node_set[t] < (int)c.node_sets.size(), "unknown node set");
+            require(comp[t] >= 1 && comp[t] <= c.dpn, "constraint component out of range");
+            rows = std::max(rows, c.node_sets[node_set[t]].size());
+        }
+        for (int t = 0; t < n_terms; ++t) {
+            const size_t len = c.node_sets[node_set[t]].size();
+            require(len == 1 || len == rows, "constraint term sets of mismatched size");
+        }
+        for (size_t r = 0; r < rows; ++r) {
+            for (int t = 0; t < n_terms; ++t) {
+                const auto& set = c.node_sets[node_set[t]];
+                const int nd = (set.size() == 1) ? set[0] : set[r];
+                c.c_dof.push_back(nd * c.dpn + comp[t] - 1);
+                c.c_coef.push_back(coef[t]);
+            }
+            c.c_ptr.push_back((int32_t)c.c_dof.size());
+            c.c_rhs.push_back(rhs);
+        }
+        c.pattern_ready = c.assembled = c.solved = false;
+        return ASEND_OK;
+    });
+}
+
+// build_elastic_app_load nodalForce branch (model_analysis.rs:37-46).
+int asend_add_nodal_force(asend_ctx* ctx, int32_t rhs, int32_t node_set, const double* load6) {
+    return guarded(ctx, [&](Ctx& c) {
+        ensure_case(c, rhs);
+        require(node_set >= 0 && node_set < (int)c.node_sets.size() && load6, "unknown node set");
+        for (int nd : c.node_sets[node_set])
+            for (int k = 0; k < c.dpn; ++k) c.loads[rhs][(size_t)nd * c.dpn + k] += load6[k];
+        return ASEND_OK;
+    });
+}
+
+// surfaceTraction (element_equations.rs:1970-2043); surface faces are faces
+// owned by one element only (model_prep.rs:510-554).
+int asend_add_surface_traction(asend_ctx* ctx, int32_t rhs, int32_t elem_set, const double* norm_dir,
+                               double norm_tol_deg, const double* traction) {
+    return guarded(ctx, [&](Ctx& c) {
+        ensure_case(c, rhs);
+        require(elem_set >= 0 && elem_set < (int)c.elem_sets.size() && norm_dir && traction, "unknown element set");
+        const int nf = (c.type == 8) ? 6 : 4, fnn = (c.type == 8) ? 4 : 3;
+        auto face_nodes = [&](int fi) -> const int* { return c.type == 8 ? kHexFaces[fi] : kTetFaces[fi]; };
+        auto key = [&](int e, int fi) {
+            std::array<int32_t, 4> k{-1, -1, -1, -1};
+            const int* ln = face_nodes(fi);
+            for (int q = 0; q < fnn; ++q) k[q] = c.conn[(size_t)e * c.nn + ln[q]];
+            for (int i = 1; i < fnn; ++i)
+                for (int j = i; j > 0 && k[j - 1] > k[j]; --j) std::swap(k[j - 1], k[j]);
+            return k;
+        };
+        std::vector<std::array<int32_t, 4>> all;
+        all.reserve((size_t)c.n_el * nf);
+        for (int e = 0; e < c.n_el; ++e)
+            for (int fi = 0; fi < nf; ++fi) all.push_back(key(e, fi));
+        std::sort(all.begin(), all.end());
+        const double cos_tol = std::cos(kPi / 180.0 * norm_tol_deg);
+        double el_ld[24], keep[24];
+        for (int e : c.elem_sets[elem_set]) {
+            bool any = false;
+            for (int fi = 0; fi < nf; ++fi) {
+                const auto k = key(e, fi);
+                auto rg = std::equal_range(all.begin(), all.end(), k);
+                if (rg.second - rg.first != 1) continue;
+                const int* ln = face_nodes(fi);
+                double v1[3], v2[3], nr[3];
+                for (int i = 0; i < 3; ++i) {
+                    const double* x0 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[0]]];
+                    const double* x1 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[1]]];
+                    const double* x2 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[2]]];
+                    if (fnn == 4) {
+                        const double* x3 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[3]]];
+                        v1[i] = x2[i] - x0[i];
+                        v2[i] = x3[i] - x1[i];
+                    } else {
+                        v1[i] = x1[i] - x0[i];
+                        v2[i] = x2[i] - x0[i];
+                    }
+                }
+                nr[0] = v1[1] * v2[2] - v1[2] * v2[1];
+                nr[1] = v1[2] * v2[0] - v1[0] * v2[2];
+                nr[2] = v1[0] * v2[1] - v1[1] * v2[0];
+                const double l = std::sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
+                const double dp = (norm_dir[0] * nr[0] + norm_dir[1] * nr[1] + norm_dir[2] * nr[2]) / l;
+                if (!(dp > cos_tol)) continue;
+                face_load(c, e, ln, fnn, traction, el_ld);
+                std::copy(el_ld, el_ld + 3 * c.nn, keep);  // last loaded face survives
+                any = true;
+            }
+            if (any)
+                for (int i = 0; i < 3 * c.nn; ++i)
+                    c.loads[rhs][(size_t)c.conn[(size_t)e * c.nn + i / 3] * 3 + i % 3] += keep[i];
+        }
+        return ASEND_OK;
+    });
+}
+
+int asend_add_load_vector(asend_ctx* ctx, int32_t rhs, const double* f) {
+    return guarded(ctx, [&](Ctx& c) {
+        ensure_case(c, rhs);
+        require(f != nullptr, "null load vector");
+        for (int i = 0; i < c.n_dof; ++i) c.loads[rhs][i] += f[i];
+        return ASEND_OK;
+    });
+}
+
+int asend_clear_loads(asend_ctx* ctx) {
+    return guarded(ctx, [&](Ctx& c) {
+        c.loads.clear();
+        c.solved = false;
+        return ASEND_OK;
+    });
+}
+
+int asend_n_dof(const asend_ctx* ctx) {
+    const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
+    return c ? c->n_dof : ASEND_EINVAL;
+}
+int asend_n_load_cases(const asend_ctx* ctx) {
+    const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
+    return c ? (int)c->loads.size() : ASEND_EINVAL;
+}
+
+int asend_get_load_vector(asend_ctx* ctx, int32_t rhs, double* f_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(rhs >= 0 && rhs < (int)c.loads.size() && f_out, "bad load case");
+        std::copy(c.loads[rhs].begin(), c.loads[rhs].end(), f_out);
+        if (c.assembled) {
+            const int nrow_c = (int)c.c_rhs.size();
+            for (int q = 0; q < nrow_c; ++q)
+                for (int k = c.c_ptr[q]; k < c.c_ptr[q + 1]; ++k) f_out[c.c_dof[k]] += c.c_coef[k] * c.sf * c.c_rhs[q];
+        }
+        return ASEND_OK;
+    });
+}
+
+int asend_assemble(asend_ctx* ctx, int32_t precision, int32_t dynamic, double dt, double beta,
+                   double gamma) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.n_el > 0, "set the mesh first");
+        require(precision == 32 || precision == 64, "precision must be 32 or 64");
+        if (dynamic) {
+            require(dt > 0.0 && beta != gamma, "Newmark needs dt > 0 and beta != gamma");
+            for (double r : c.rho) require(r > 0.0, "dynamic assembly needs positive densities");
+        }
+        ASEND_CUDA(cudaSetDevice(c.device));
+        c.dynamic = dynamic != 0;
+        c.dt = dt;
+        c.beta = beta;
+        c.gamma = gamma;
+        c.cM = c.dynamic ? -1.0 / (dt * dt * (beta - gamma)) : 0.0;
+        if (!c.pattern_ready) build_pattern(c);
+        assemble_operator(c, precision);
+        c.assembled = true;
+        c.solved = false;
+        return ASEND_OK;
+    });
+}
+
+int asend_get_coloring(asend_ctx* ctx, int32_t* colour_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.pattern_ready, "assemble first");
+        if (colour_out) std::copy(c.colour_of.begin(), c.colour_of.end(), colour_out);
+        return (int)c.colour_ptr.size() - 1;
+    });
+}
+
+// Scalar CSR view (sorted columns) of the assembled operator; which 0 = the
+// operator with penalty, 1 = the mass matrix, 2 = the operator without the
+// penalty terms.
+int asend_get_csr(asend_ctx* ctx, int32_t which, int64_t* nnz_out, int64_t* row_ptr, int32_t* col,
+                  double* val) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.assembled, "assemble first");
+        require(which >= 0 && which <= 2, "which must be 0, 1 or 2");
+        require(which != 1 || c.dynamic, "no mass matrix (static assembly)");
+        const Sbell& A = c.A;
+        const int b = A.b, b2 = b * b;
+        const int64_t nnz = A.nnz_scalar();
+        if (nnz_out) *nnz_out = nnz;
+        if (!row_ptr && !col && !val) return ASEND_OK;
+        std::vector<double> h;
+        if (val) {
+            const DArr<double>& src = (which == 1) ? A.m64 : A.v64;
+            h.resize(src.n);
+            ASEND_CUDA(cudaMemcpyAsync(h.data(), src.p, src.n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            ASEND_CUDA(cudaStreamSynchronize(c.stream));
+            if (which == 2) {
+                std::vector<int64_t> pi(c.d_pen_idx.n);
+                std::vector<double> pc(c.d_pen_coef.n);
+                ASEND_CUDA(cudaMemcpy(pi.data(), c.d_pen_idx.p, pi.size() * sizeof(int64_t), cudaMemcpyDeviceToHost));
+                ASEND_CUDA(cudaMemcpy(pc.data(), c.d_pen_coef.p, pc.size() * sizeof(double), cudaMemcpyDeviceToHost));
+                for (size_t k = 0; k < pi.size(); ++k) h[pi[k]] -= c.sf * pc[k];
+            }
+        }
+        int64_t k = 0;
+        if (row_ptr) row_ptr[0] = 0;
+        for (int r = 0; r < A.n_rows; ++r) {
+            const int s = r / kSlice, lane = r % kSlice;
+            for (int a = 0; a < b; ++a) {
+                for (int j = 0; j < A.h_row_len[r]; ++j) {
+                    const int64_t g = A.h_slice_off[s] + j;
+                    const int cn = A.h_col[(size_t)g * kSlice + lane];
+                    for (int cc = 0; cc < b; ++cc) {
+                        if (col) col[k] = cn * b + cc;
+                        if (val) val[k] = h[(size_t)(g * b2 + a * b + cc) * kSlice + lane];
+                        ++k;
+                    }
+                }
+                if (row_ptr) row_ptr[r * b + a + 1] = k;
+            }
+        }
+        return ASEND_OK;
+    });
+}
+
+int asend_apply_operator(asend_ctx* ctx, int32_t precision, const double* x, double* y) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.assembled, "assemble first");
+        require(x && y, "null vector");
+        DArr<double> dx, dy;
+        dx.upload(x, c.n_dof, c.stream);
+        dy.alloc(c.n_dof);
+        apply_operator_device(c, precision, dx.p, dy.p);
+        ASEND_CUDA(cudaMemcpyAsync(y, dy.p, c.n_dof * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        return ASEND_OK;
+    });
+}
+
+int asend_time_spmv(asend_ctx* ctx, int32_t precision, int32_t n_launch, double* ms_per_launch,
+                    double* bytes_per_launch) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.assembled, "assemble first");
+        require(n_launch > 0, "n_launch must be positive");
+        double bytes = 0.0;
+        const double ms = time_spmv(c, precision, n_launch, &bytes);
+        if (ms_per_launch) *ms_per_launch = ms;
+        if (bytes_per_launch) *bytes_per_launch = bytes;
+        return ASEND_OK;
+    });
+}
+
+int asend_static_solve_device(asend_ctx* ctx, const asend_solve_opts* opts, asend_solve_stats* stats) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(opts != nullptr, "null options");
+        require(c.assembled, "assemble first");
+        upload_rhs(c);
+        c.d_x.alloc((size_t)c.nrhs * c.n_dof);
+        const int rc = pcg_solve(c, *opts, stats, false, c.d_f.p, c.d_x.p, c.nrhs);
+        c.solved = true;
+        return rc;
+    });
+}
+
+int asend_static_solve(asend_ctx* ctx, const asend_solve_opts* opts, double* u_io, asend_solve_stats* stats) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(opts != nullptr && u_io != nullptr, "null argument");
+        require(c.assembled, "assemble first");
+        upload_rhs(c);
+        const size_t n = (size_t)c.nrhs * c.n_dof;
+        if (opts->warm_start) c.d_x.upload(u_io, n, c.stream);
+        else c.d_x.alloc(n);
+        const int rc = pcg_solve(c, *opts, stats, opts->warm_start != 0, c.d_f.p, c.d_x.p, c.nrhs);
+        c.solved = true;
+        ASEND_CUDA(cudaMemcpyAsync(u_io, c.d_x.p, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        return rc;
+    });
+}
+
+int asend_get_solution(asend_ctx* ctx, int32_t rhs, double* u_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.solved, "no solution available");
+        require(rhs >= 0 && rhs < c.nrhs && u_out, "bad load case");
+        ASEND_CUDA(cudaMemcpyAsync(u_out, c.d_x.p + (size_t)rhs * c.n_dof, c.n_dof * sizeof(double),
+                                   cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        return ASEND_OK;
+    });
+}
+
+int asend_set_objective(asend_ctx* ctx, int32_t kind, int32_t node_set, int32_t comp, double coef) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(kind == ASEND_OBJ_DISPLACEMENT || kind == ASEND_OBJ_COMPLIANCE, "unknown objective kind");
+        if (kind == ASEND_OBJ_DISPLACEMENT) {
+            require(node_set >= 0 && node_set < (int)c.node_sets.size(), "unknown node set");
+            require(comp >= 1 && comp <= c.dpn, "objective component out of range");
+        }
+        c.obj_kind = kind;
+        c.obj_set = node_set;
+        c.obj_comp = comp;
+        c.obj_coef = coef;
+        return ASEND_OK;
+    });
+}
+
+// Static adjoint gradient w.r.t. per-element modulus (get_obj_gradient static
+// branch, model_analysis.rs:1632-1704; solve_for_adjoint :1065-1126).
+int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double* L_out, double* dLdE_out,
+                           asend_solve_stats* stats) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(opts != nullptr, "null options");
+        require(c.solved, "run a static solve before the adjoint gradient");
+        const size_t n = c.n_dof;
+        c.d_gE.alloc(c.n_el);
+        DArr<double> part, scal;
+        part.alloc(256);
+        scal.alloc(1);
+        double L = 0.0;
+        int rc = ASEND_OK;
+        asend_solve_stats ast{};
+        float ms_solve = 0.f;
+        ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
+        if (c.obj_kind == ASEND_OBJ_COMPLIANCE) {
+            // L = sum_r b_r^T u_r, self-adjoint: lambda_r = u_r
+            for (int r = 0; r < c.nrhs; ++r) {
+                device_dot(c, n, c.d_f.p + r * n, c.d_x.p + r * n, scal.p, part.p);
+                double v = 0.0;
+                ASEND_CUDA(cudaMemcpyAsync(&v, scal.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+                ASEND_CUDA(cudaStreamSynchronize(c.stream));
+                L += v;
+                adjoint_contract(c, c.d_x.p + r * n, c.d_x.p + r * n, c.d_gE.p, r > 0);
+            }
+        } else {
+            // L = coef * sum_r sum_{node in set} u_r[node, comp]  ('powerNorm', exponent 1)
+            const auto& set = c.node_sets[c.obj_set];
+            std::vector<double> dldu(n, 0.0);
+            for (int nd : set) dldu[(size_t)nd * c.dpn + c.obj_comp - 1] += c.obj_coef;
+            DArr<double> d_dldu, d_usum;
+            d_dldu.upload(dldu, c.stream);
+            d_usum.alloc(n);
+            d_usum.zero(c.stream);
+            for (int r = 0; r < c.nrhs; ++r) {
+                device_dot(c, n, d_dldu.p, c.d_x.p + r * n, scal.p, part.p);
+                double v = 0.0;
+                ASEND_CUDA(cudaMemcpyAsync(&v, scal.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+                ASEND_CUDA(cudaStreamSynchronize(c.stream));
+                L += v;
+                device_axpy(c, n, 1.0, c.d_x.p + r * n, d_usum.p);
+            }
+            c.d_lam.alloc(n);
+            rc = pcg_solve(c, *opts, &ast, false, d_dldu.p, c.d_lam.p, 1);
+            ms_solve = (float)ast.ms_solve;
+            cudaEvent_t e0, e1;
+            ASEND_CUDA(cudaEventCreate(&e0));
+            ASEND_CUDA(cudaEventCreate(&e1));
+            ASEND_CUDA(cudaEventRecord(e0, c.stream));
+            adjoint_contract(c, c.d_lam.p, d_usum.p, c.d_gE.p, false);
+            ASEND_CUDA(cudaEventRecord(e1, c.stream));
+            ASEND_CUDA(cudaEventSynchronize(e1));
+            float mc = 0.f;
+            ASEND_CUDA(cudaEventElapsedTime(&mc, e0, e1));
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            ast.ms_adjoint = mc;
+        }
+        ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
+        if (dLdE_out)
+            ASEND_CUDA(cudaMemcpyAsync(dLdE_out, c.d_gE.p, sizeof(double) * c.n_el, cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        float ms = 0.f;
+        ASEND_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+        if (L_out) *L_out = L;
+        if (stats) {
+            *stats = ast;
+            stats->ms_solve = ms_solve;
+            stats->ms_adjoint = (c.obj_kind == ASEND_OBJ_COMPLIANCE) ? ms : ast.ms_adjoint;
+            stats->penalty_scale = c.sf;
+        }
+        return rc;
+    });
+}
+
+int asend_newmark_run(asend_ctx* ctx, const asend_solve_opts* opts, int32_t n_steps, const double* amp,
+                      int32_t probe_dof, double* probe_hist, double* u_final, asend_solve_stats* stats) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(opts && amp && n_steps > 0, "bad Newmark arguments");
+        require(c.assembled && c.dynamic, "assemble with dynamic=1 first");
+        require(probe_dof < c.n_dof, "probe DOF out of range");
+        return newmark_run(c, *opts, n_steps, amp, probe_dof, probe_hist, u_final, stats);
+    });
+}
+
+int asend_add_modulus_design_var(asend_ctx* ctx, int32_t elem_set, int32_t n_coef, const double* coefs) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(elem_set >= 0 && elem_set < (int)c.elem_sets.size(), "unknown element set");
+        const auto& set = c.elem_sets[elem_set];
+        require(n_coef <= 1 || (size_t)n_coef == set.size(),
+                "coefficient list does not match the length of the element set");
+        for (size_t k = 0; k < set.size(); ++k) {
+            c.dv_el.push_back(set[k]);
+            c.dv_coef.push_back(n_coef == 0 ? 1.0 : (n_coef == 1 ? coefs[0] : coefs[k]));
+        }
+        c.dv_ptr.push_back((int32_t)c.dv_el.size());
+        return (int)c.dv_ptr.size() - 2;
+    });
+}
+
+int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(dLdE && dLdD_out, "null argument");
+        const int ndv = (int)c.dv_ptr.size() - 1;
+        for (int i = 0; i < ndv; ++i) {
+            double s = 0.0;
+            for (int k = c.dv_ptr[i]; k < c.dv_ptr[i + 1]; ++k) s += c.dv_coef[k] * dLdE[c.dv_el[k]];
+            dLdD_out[i] = s;
+        }
+        return ndv;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,206 @@
+// common.cuh -- shared device helpers and the library context.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/asend_gpu.h"
+
+#define ASEND_CUDA(call)                                                        \
+    do {                                                                        \
+        cudaError_t e__ = (call);                                               \
+        if (e__ != cudaSuccess) {                                               \
+            throw asend::CudaError(std::string(#call) + ": " + cudaGetErrorString(e__)); \
+        }                                                                       \
+    } while (0)
+
+namespace asend {
+
+struct CudaError {
+    std::string msg;
+    explicit CudaError(std::string m) : msg(std::move(m)) {}
+};
+struct InputError {
+    std::string msg;
+    explicit InputError(std::string m) : msg(std::move(m)) {}
+};
+
+// Device array owned by the context.
+template <typename T>
+struct DArr {
+    T* p = nullptr;
+    size_t n = 0;
+    DArr() = default;
+    DArr(const DArr&) = delete;
+    DArr& operator=(const DArr&) = delete;
+    ~DArr() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count) {
+        if (count == n && p) return;
+        release();
+        if (count == 0) return;
+        ASEND_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        n = count;
+    }
+    void upload(const T* h, size_t count, cudaStream_t s) {
+        alloc(count);
+        if (count) ASEND_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void upload(const std::vector<T>& h, cudaStream_t s) { upload(h.data(), h.size(), s); }
+    void zero(cudaStream_t s) {
+        if (n) ASEND_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+};
+
+constexpr int kSlice = 32;  // rows per slice of the sliced block-ELL matrix
+
+// Sliced block-ELL ("SBELL") matrix over node rows with b x b blocks.
+// Block column group g = slice_off[row/32] + j holds, for the 32 rows of the
+// slice, column node col[g*32 + lane] and values
+// vals[(g*b*b + v)*32 + lane], v = a*b + c (row component a, column comp c).
+// Rows shorter than the slice width are padded (never read: row_len).
+struct Sbell {
+    int b = 3, n_rows = 0, n_slices = 0;
+    int64_t n_groups = 0;  // total block-column groups (slots = 32 * n_groups)
+    std::vector<int64_t> h_slice_off;
+    std::vector<int32_t> h_col;
+    std::vector<uint8_t> h_row_len, h_diag;
+    DArr<int64_t> slice_off;
+    DArr<int32_t> col;
+    DArr<uint8_t> row_len, diag;
+    DArr<double> v64, m64;  // operator values (K [+cM M] + penalty), mass values
+    DArr<float> v32;
+    int64_t nnz_scalar() const {  // stored scalar entries excluding padding
+        int64_t s = 0;
+        for (int r = 0; r < n_rows; ++r) s += (int64_t)h_row_len[r];
+        return s * b * b;
+    }
+    int64_t slot(int row, int j) const {
+        return (h_slice_off[row / kSlice] + j) * kSlice + (row % kSlice);
+    }
+};
+
+struct PcgScalars {
+    double rz, rz_new, pAp, rr, bb, alpha, beta, target_rr, rr_last_true;
+    int32_t iter, done, status, since_replace;
+    uint32_t ticket_a, ticket_b, ticket_c, pad;
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int64_t launches = 0;
+
+    // ---- mesh (host)
+    int type = 0, nn = 0, dpn = 3, nip = 0;
+    int n_nodes = 0, n_el = 0, n_dof = 0;
+    std::vector<double> xyz, E, nu, rho, thk;
+    std::vector<int32_t> conn;
+    std::vector<std::vector<int32_t>> node_sets, elem_sets;
+    // constraint rows (natural DOF numbering)
+    std::vector<int32_t> c_ptr{0}, c_dof;
+    std::vector<double> c_coef, c_rhs;
+    // load cases (FP64 host, natural numbering, without penalty rhs)
+    std::vector<std::vector<double>> loads;
+    // objective + design variables
+    int obj_kind = ASEND_OBJ_COMPLIANCE, obj_set = -1, obj_comp = 1;
+    double obj_coef = 1.0;
+    std::vector<int32_t> dv_ptr{0}, dv_el;
+    std::vector<double> dv_coef;
+
+    // ---- device mesh
+    DArr<double> d_xyz, d_E, d_nu, d_rho, d_thk;
+    DArr<int32_t> d_conn;
+    bool pattern_ready = false, assembled = false, dynamic = false;
+    double dt = 0, beta = 0.25, gamma = 0.5, cM = 0;
+    double sf = 0;
+    int assembled_precision = 64;
+    float last_assemble_ms = 0.f;
+
+    // ---- pattern / assembly
+    Sbell A;
+    DArr<int32_t> d_slot_map;  // [n_el * nn * nn] slot of block (a, b)
+    std::vector<int32_t> colour_of, colour_ptr, colour_elems;
+    DArr<int32_t> d_colour_elems;
+    DArr<int64_t> d_pen_idx;   // value indices receiving penalty terms
+    DArr<double> d_pen_coef;   // coef_i * coef_j per penalty entry
+    DArr<double> d_max_partial;
+
+    // ---- solver state (nrhs * n_dof each)
+    int nrhs = 0;
+    DArr<double> d_f, d_x, d_r;        // rhs incl. penalty, solution, residual
+    DArr<float> d_p32, d_ap32;         // mixed: padded direction, A p
+    DArr<double> d_p64, d_ap64;        // fp64: padded direction, A p
+    DArr<double> d_dinv;               // point Jacobi inverse diagonal (n_dof)
+    DArr<float> d_binv;                // nodal block inverse (n_nodes * b*b)
+    DArr<double> d_partials;           // block partial sums
+    DArr<PcgScalars> d_sc;
+    PcgScalars* h_sc = nullptr;        // pinned mirror
+    bool solved = false;
+    int last_method = ASEND_METHOD_MIXED;
+
+    // adjoint
+    DArr<double> d_lam, d_gE;
+
+    // timing
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    // graphs
+    cudaGraphExec_t graph = nullptr;
+    int graph_key[6] = {-1, -1, -1, -1, -1, -1};
+};
+
+// ---- device reductions -----------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide sum of K values per thread (K small); result valid in thread 0.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K], double* smem /* [32*K] */) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) smem[warp * K + k] = v[k];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double t = (lane < nw) ? smem[lane * K + k] : 0.0;
+            v[k] = warp_sum(t);
+        }
+    }
+}
+
+// host-side helpers implemented in the .cu files
+void assemble_operator(Ctx& c, int precision);
+void build_pattern(Ctx& c);
+void apply_operator_device(Ctx& c, int precision, const double* d_x, double* d_y);
+double time_spmv(Ctx& c, int precision, int n_launch, double* bytes);
+int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f,
+              double* d_x, int nrhs);
+void device_dot(Ctx& c, size_t n, const double* a, const double* b, double* d_out, double* d_part);
+void device_axpy(Ctx& c, size_t n, double alpha, const double* x, double* y);
+void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g, bool accumulate);
+int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* amp, int probe,
+                double* probe_hist, double* u_final, asend_solve_stats* st);
+void upload_rhs(Ctx& c);
+
+}  // namespace asend

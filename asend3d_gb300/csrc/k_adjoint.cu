@@ -1,0 +1,186 @@
+// k_adjoint.cu -- K4: per-element adjoint modulus-sensitivity contraction.
+//
+// Reference: Model::get_obj_gradient static branch
+// (solverSrc/asend_run_job/src/model_analysis.rs:1632-1704): for every design
+// variable i, d_relasticd_d(i) (:1379-1457) re-integrates the elements that
+// depend on D_i with forward-mode dual numbers and the gradient gets
+// dL/dD_i -= sum_dof lambda * dR/dD_i (:1692-1700).  That loop is
+// O(n_dv * (n_dof + n_el)).  For a modulus DV on element e only that element's
+// internal force R_e = K_e u_e depends on it, and with C linear in E at fixed
+// nu, dR_e/dE_e = (K_e / E_e) u_e, so all n_el sensitivities come from one
+// O(n_el) pass:
+//     g_e = -(1/E_e) sum_gp w detJ  eps(a_e)^T C eps(b_e)
+// with (a, b) = (lambda, u).  Strains use the reference's Voigt order and
+// engineering shear (element_soln_fields.rs:1345-1461).
+//
+// GB300 design: one thread per element, 8 Gauss points unrolled, node data
+// gathered once into registers; displacements are made element-relative in
+// FP64 (rigid translation removed) before forming gradients.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace asend {
+namespace {
+
+template <int NN>
+__global__ void __launch_bounds__(128)
+k_adjoint_modulus(int n_el, const int32_t* __restrict__ conn, const double* __restrict__ xyz,
+                  const double* __restrict__ E, const double* __restrict__ nu,
+                  const double* __restrict__ av, const double* __restrict__ bv, double* __restrict__ g,
+                  int accumulate) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_el) return;
+    double x[NN][3], ua[NN][3], ub[NN][3];
+    int nd[NN];
+#pragma unroll
+    for (int a = 0; a < NN; ++a) nd[a] = conn[(size_t)e * NN + a];
+#pragma unroll
+    for (int a = 0; a < NN; ++a)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            x[a][j] = xyz[3 * (size_t)nd[a] + j] - xyz[3 * (size_t)nd[0] + j];
+            ua[a][j] = av[3 * (size_t)nd[a] + j];
+            ub[a][j] = bv[3 * (size_t)nd[a] + j];
+        }
+#pragma unroll
+    for (int a = NN - 1; a >= 0; --a)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            ua[a][j] -= ua[0][j];
+            ub[a][j] -= ub[0][j];
+        }
+    const double ne = nu[e];
+    const double lam = ne / ((1.0 + ne) * (1.0 - 2.0 * ne));  // C / E
+    const double mu = 1.0 / (2.0 * (1.0 + ne));
+    const double gq = 0.5773502691896257;
+    constexpr int NIP = (NN == 8) ? 8 : 1;
+    double acc = 0.0;
+#pragma unroll
+    for (int gp = 0; gp < NIP; ++gp) {
+        double dn[NN][3];
+        double wt;
+        if constexpr (NN == 8) {
+            const double s0 = (gp & 1) ? gq : -gq, s1 = (gp & 2) ? gq : -gq, s2 = (gp & 4) ? gq : -gq;
+            const double sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                     {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+#pragma unroll
+            for (int a = 0; a < 8; ++a) {
+                const double f0 = 1 + sg[a][0] * s0, f1 = 1 + sg[a][1] * s1, f2 = 1 + sg[a][2] * s2;
+                dn[a][0] = 0.125 * sg[a][0] * f1 * f2;
+                dn[a][1] = 0.125 * sg[a][1] * f0 * f2;
+                dn[a][2] = 0.125 * sg[a][2] * f0 * f1;
+            }
+            wt = 1.0;
+        } else {
+            const double d[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) dn[a][j] = d[a][j];
+            wt = 1.0 / 6.0;
+        }
+        double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+        for (int a = 0; a < NN; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) J[i][j] += x[a][i] * dn[a][j];
+        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        const double id = 1.0 / det;
+        double Ji[3][3];
+        Ji[0][0] = c00 * id;
+        Ji[1][0] = c01 * id;
+        Ji[2][0] = c02 * id;
+        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+        // displacement gradients H[i][j] = du_i/dx_j
+        double Ha[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Hb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+        for (int a = 1; a < NN; ++a) {
+            double gx[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) gx[j] = dn[a][0] * Ji[0][j] + dn[a][1] * Ji[1][j] + dn[a][2] * Ji[2][j];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    Ha[i][j] += ua[a][i] * gx[j];
+                    Hb[i][j] += ub[a][i] * gx[j];
+                }
+        }
+        // Voigt strains (11,22,33,12,13,23), engineering shear
+        const double ea[6] = {Ha[0][0], Ha[1][1], Ha[2][2], Ha[0][1] + Ha[1][0], Ha[0][2] + Ha[2][0], Ha[1][2] + Ha[2][1]};
+        const double eb[6] = {Hb[0][0], Hb[1][1], Hb[2][2], Hb[0][1] + Hb[1][0], Hb[0][2] + Hb[2][0], Hb[1][2] + Hb[2][1]};
+        const double trb = eb[0] + eb[1] + eb[2];
+        double s = 0.0;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) s += ea[i] * (lam * trb + 2.0 * mu * eb[i]);
+#pragma unroll
+        for (int i = 3; i < 6; ++i) s += ea[i] * (mu * eb[i]);
+        acc += s * det * wt;
+    }
+    const double v = -acc;  // (1/E) dK/d? folded: C/E used above
+    if (accumulate) g[e] += v;
+    else g[e] = v;
+    (void)E;
+}
+
+__global__ void k_dot_partial(size_t n, const double* __restrict__ a, const double* __restrict__ b,
+                              double* __restrict__ part) {
+    __shared__ double sm[32];
+    double v[1] = {0.0};
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        v[0] += a[i] * b[i];
+    block_sum<1>(v, sm);
+    if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+__global__ void k_dot_final(int nb, const double* __restrict__ part, double* __restrict__ out) {
+    __shared__ double sm[32];
+    double v[1] = {0.0};
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) v[0] += part[i];
+    block_sum<1>(v, sm);
+    if (threadIdx.x == 0) *out = v[0];
+}
+__global__ void k_axpy(size_t n, double alpha, const double* __restrict__ x, double* __restrict__ y) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        y[i] += alpha * x[i];
+}
+
+}  // namespace
+
+// Deterministic FP64 dot product (fixed two-stage order) into *d_out.
+void device_dot(Ctx& c, size_t n, const double* a, const double* b, double* d_out, double* d_part) {
+    constexpr int nb = 256;
+    k_dot_partial<<<nb, 256, 0, c.stream>>>(n, a, b, d_part);
+    k_dot_final<<<1, 256, 0, c.stream>>>(nb, d_part, d_out);
+    ASEND_CUDA(cudaGetLastError());
+    c.launches += 2;
+}
+void device_axpy(Ctx& c, size_t n, double alpha, const double* x, double* y) {
+    k_axpy<<<(int)std::min<size_t>((n + 255) / 256, 2432), 256, 0, c.stream>>>(n, alpha, x, y);
+    ASEND_CUDA(cudaGetLastError());
+    ++c.launches;
+}
+
+void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g, bool accumulate) {
+    const int blocks = (c.n_el + 127) / 128;
+    if (c.nn == 8)
+        k_adjoint_modulus<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, d_a, d_b, d_g,
+                                                            accumulate ? 1 : 0);
+    else
+        k_adjoint_modulus<4><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, d_a, d_b, d_g,
+                                                            accumulate ? 1 : 0);
+    ASEND_CUDA(cudaGetLastError());
+    ++c.launches;
+}
+
+}  // namespace asend

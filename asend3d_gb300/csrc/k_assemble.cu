@@ -1,0 +1,319 @@
+// k_assemble.cu -- K1 element integration fused with K2 coloured scatter.
+//
+// Reference path (solverSrc/asend_run_job/src/):
+//   per-element K_e: element_equations.rs:206-418 (get_ruk_dfd0, Gauss loop
+//   K += B^T C B detJ w), shape functions element_soln_fields.rs:120-229,
+//   Jacobian / dN/dx element_soln_fields.rs:383-463, solid C
+//   element_properties.rs:648-764, consistent mass element_equations.rs:583-609,
+//   Newmark mass term element_equations.rs:977-988, scatter to the global
+//   matrix element_equations.rs:1040-1059 (SparseMat::add_entry,
+//   list_ent_meth.rs:6-18), penalty scale model_analysis.rs:255-259 and the
+//   penalty operator const_meth.rs:92-103.
+//
+// GB300 design: a CTA integrates EB elements; each thread owns one node pair
+// (a <= b) of one element and forms the 3x3 block
+//     K_ab = lambda S + mu S^T + mu tr(S) I,   S = sum_gp w detJ g_a g_b^T
+// (the isotropic B^T C B product in closed form), then scatters K_ab and its
+// transpose into the sliced block-ELL values through a precomputed slot map.
+// Elements of one colour share no node, so the scatter needs no atomics and
+// the summation order is fixed (deterministic).
+#include "common.cuh"
+
+namespace asend {
+namespace {
+
+// Reference-element tables (filled once from the host).
+__constant__ double c_hex_dn[8][8][3];  // [gp][node][ds_j]
+__constant__ double c_hex_n[8][8];      // [gp][node]
+__constant__ int c_hex_pair[36][2];
+__constant__ int c_tet_pair[10][2];
+bool g_tables_ready = false;
+
+void init_tables() {
+    if (g_tables_ready) return;
+    const double g = 0.5773502691896257;
+    const double sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                             {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+    double dn[8][8][3], nv[8][8];
+    int k = 0;
+    for (int zc = 0; zc < 2; ++zc)
+        for (int yc = 0; yc < 2; ++yc)
+            for (int xc = 0; xc < 2; ++xc) {
+                const double s[3] = {xc ? g : -g, yc ? g : -g, zc ? g : -g};
+                for (int a = 0; a < 8; ++a) {
+                    const double f0 = 1 + sg[a][0] * s[0], f1 = 1 + sg[a][1] * s[1], f2 = 1 + sg[a][2] * s[2];
+                    nv[k][a] = 0.125 * f0 * f1 * f2;
+                    dn[k][a][0] = 0.125 * sg[a][0] * f1 * f2;
+                    dn[k][a][1] = 0.125 * sg[a][1] * f0 * f2;
+                    dn[k][a][2] = 0.125 * sg[a][2] * f0 * f1;
+                }
+                ++k;
+            }
+    int hp[36][2], tp[10][2];
+    k = 0;
+    for (int a = 0; a < 8; ++a)
+        for (int b = a; b < 8; ++b) { hp[k][0] = a; hp[k][1] = b; ++k; }
+    k = 0;
+    for (int a = 0; a < 4; ++a)
+        for (int b = a; b < 4; ++b) { tp[k][0] = a; tp[k][1] = b; ++k; }
+    ASEND_CUDA(cudaMemcpyToSymbol(c_hex_dn, dn, sizeof(dn)));
+    ASEND_CUDA(cudaMemcpyToSymbol(c_hex_n, nv, sizeof(nv)));
+    ASEND_CUDA(cudaMemcpyToSymbol(c_hex_pair, hp, sizeof(hp)));
+    ASEND_CUDA(cudaMemcpyToSymbol(c_tet_pair, tp, sizeof(tp)));
+    g_tables_ready = true;
+}
+
+template <int NN>
+struct ElemTraits;
+template <>
+struct ElemTraits<8> {
+    static constexpr int NIP = 8, NP = 36, EB = 8;
+};
+template <>
+struct ElemTraits<4> {
+    static constexpr int NIP = 1, NP = 10, EB = 32;
+};
+
+template <int NN, typename T>
+__device__ __forceinline__ void shape_ref(int gp, int a, T& n, T (&dn)[3]) {
+    if constexpr (NN == 8) {
+        n = (T)c_hex_n[gp][a];
+        dn[0] = (T)c_hex_dn[gp][a][0];
+        dn[1] = (T)c_hex_dn[gp][a][1];
+        dn[2] = (T)c_hex_dn[gp][a][2];
+    } else {
+        n = (T)0.25;
+        dn[0] = (a == 1) ? (T)1 : (a == 0 ? (T)-1 : (T)0);
+        dn[1] = (a == 2) ? (T)1 : (a == 0 ? (T)-1 : (T)0);
+        dn[2] = (a == 3) ? (T)1 : (a == 0 ? (T)-1 : (T)0);
+    }
+}
+
+// One CTA = EB elements of one colour; thread = (element, node pair).
+template <int NN, typename T>
+__global__ void __launch_bounds__(ElemTraits<NN>::EB * ElemTraits<NN>::NP)
+assemble_colour_kernel(int n_el, const int32_t* __restrict__ el_list, const int32_t* __restrict__ conn,
+                       const double* __restrict__ xyz, const double* __restrict__ E,
+                       const double* __restrict__ nu, const double* __restrict__ rho,
+                       const int32_t* __restrict__ slot_map, T* __restrict__ vals,
+                       double* __restrict__ mvals, double cM) {
+    constexpr int NIP = ElemTraits<NN>::NIP, NP = ElemTraits<NN>::NP, EB = ElemTraits<NN>::EB;
+    __shared__ T s_x[EB][NN][3];
+    __shared__ T s_g[EB][NIP][NN][3];
+    __shared__ T s_w[EB][NIP];
+    __shared__ int s_el[EB];
+    const int tid = threadIdx.x;
+    const int base = blockIdx.x * EB;
+    if (tid < EB) s_el[tid] = (base + tid < n_el) ? el_list[base + tid] : -1;
+    __syncthreads();
+    // coordinates relative to the element's first node (translation invariant)
+    for (int t = tid; t < EB * NN * 3; t += blockDim.x) {
+        const int el = t / (NN * 3), a = (t / 3) % NN, j = t % 3;
+        const int e = s_el[el];
+        T v = 0;
+        if (e >= 0) {
+            const int n0 = conn[(size_t)e * NN], na = conn[(size_t)e * NN + a];
+            v = (T)(xyz[3 * (size_t)na + j] - xyz[3 * (size_t)n0 + j]);
+        }
+        s_x[el][a][j] = v;
+    }
+    __syncthreads();
+    // Gauss-point data: J = sum_a x_a dN_a^T, dN/dx = dN/ds J^-1
+    if (tid < EB * NIP) {
+        const int el = tid / NIP, gp = tid % NIP;
+        T J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int a = 0; a < NN; ++a) {
+            T n, dn[3];
+            shape_ref<NN, T>(gp, a, n, dn);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) J[i][j] += s_x[el][a][i] * dn[j];
+        }
+        const T c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const T c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const T c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        const T det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        const T id = (T)1 / det;
+        T Ji[3][3];
+        Ji[0][0] = c00 * id;
+        Ji[1][0] = c01 * id;
+        Ji[2][0] = c02 * id;
+        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+        for (int a = 0; a < NN; ++a) {
+            T n, dn[3];
+            shape_ref<NN, T>(gp, a, n, dn);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) s_g[el][gp][a][j] = dn[0] * Ji[0][j] + dn[1] * Ji[1][j] + dn[2] * Ji[2][j];
+        }
+        s_w[el][gp] = det * ((NN == 8) ? (T)1 : (T)(1.0 / 6.0));
+    }
+    __syncthreads();
+    if (tid >= EB * NP) return;
+    const int el = tid / NP, p = tid % NP;
+    const int e = s_el[el];
+    if (e < 0) return;
+    const int a = (NN == 8) ? c_hex_pair[p][0] : c_tet_pair[p][0];
+    const int b = (NN == 8) ? c_hex_pair[p][1] : c_tet_pair[p][1];
+    T S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    T m = 0;
+#pragma unroll
+    for (int gp = 0; gp < NIP; ++gp) {
+        const T w = s_w[el][gp];
+        const T ga0 = s_g[el][gp][a][0] * w, ga1 = s_g[el][gp][a][1] * w, ga2 = s_g[el][gp][a][2] * w;
+        const T gb0 = s_g[el][gp][b][0], gb1 = s_g[el][gp][b][1], gb2 = s_g[el][gp][b][2];
+        S[0][0] += ga0 * gb0; S[0][1] += ga0 * gb1; S[0][2] += ga0 * gb2;
+        S[1][0] += ga1 * gb0; S[1][1] += ga1 * gb1; S[1][2] += ga1 * gb2;
+        S[2][0] += ga2 * gb0; S[2][1] += ga2 * gb1; S[2][2] += ga2 * gb2;
+        if (mvals) {
+            T na, nb, dn[3];
+            shape_ref<NN, T>(gp, a, na, dn);
+            shape_ref<NN, T>(gp, b, nb, dn);
+            m += na * nb * w;
+        }
+    }
+    const double Ee = E[e], ne = nu[e];
+    const T lam = (T)(Ee * ne / ((1.0 + ne) * (1.0 - 2.0 * ne)));
+    const T mu = (T)(Ee / (2.0 * (1.0 + ne)));
+    const T tr = mu * (S[0][0] + S[1][1] + S[2][2]);
+    const T mass = mvals ? m * (T)rho[e] : (T)0;
+    const int32_t slot = slot_map[((size_t)e * NN + a) * NN + b];
+    const int64_t g = slot >> 5, lane = slot & 31;
+    T* vb = vals + (g * 9) * 32 + lane;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            T kij = lam * S[i][j] + mu * S[j][i] + ((i == j) ? tr : (T)0);
+            if (i == j) kij += (T)cM * mass;
+            vb[(i * 3 + j) * 32] += kij;
+        }
+    if (mvals) {
+        double* mb = mvals + (g * 9) * 32 + lane;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) mb[(i * 3 + i) * 32] += (double)mass;
+    }
+    if (a != b) {
+        const int32_t slot2 = slot_map[((size_t)e * NN + b) * NN + a];
+        const int64_t g2 = slot2 >> 5, lane2 = slot2 & 31;
+        T* vt = vals + (g2 * 9) * 32 + lane2;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                T kij = lam * S[i][j] + mu * S[j][i] + ((i == j) ? tr : (T)0);
+                if (i == j) kij += (T)cM * mass;
+                vt[(j * 3 + i) * 32] += kij;
+            }
+        if (mvals) {
+            double* mt = mvals + (g2 * 9) * 32 + lane2;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) mt[(i * 3 + i) * 32] += (double)mass;
+        }
+    }
+}
+
+__global__ void max_abs_kernel(size_t n, const double* __restrict__ v, unsigned long long* out) {
+    double m = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        m = fmax(m, fabs(v[i]));
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+__global__ void penalty_kernel(int n, const int64_t* __restrict__ idx, const double* __restrict__ coef,
+                               double sf, double* vals) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) atomicAdd(&vals[idx[k]], sf * coef[k]);
+}
+
+__global__ void round_kernel(size_t n, const double* __restrict__ src, float* __restrict__ dst) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+__global__ void widen_kernel(size_t n, const float* __restrict__ src, double* __restrict__ dst) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = (double)src[i];
+}
+
+int stream_grid(size_t n) {
+    size_t b = (n + 255) / 256;
+    return (int)std::min<size_t>(b, 152 * 16);
+}
+
+template <int NN, typename T>
+void launch_colours(Ctx& c, T* vals, double* mvals) {
+    constexpr int EB = ElemTraits<NN>::EB, NP = ElemTraits<NN>::NP;
+    const int n_col = (int)c.colour_ptr.size() - 1;
+    for (int k = 0; k < n_col; ++k) {
+        const int n = c.colour_ptr[k + 1] - c.colour_ptr[k];
+        if (n == 0) continue;
+        const int blocks = (n + EB - 1) / EB;
+        assemble_colour_kernel<NN, T><<<blocks, EB * NP, 0, c.stream>>>(
+            n, c.d_colour_elems.p + c.colour_ptr[k], c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, c.d_rho.p,
+            c.d_slot_map.p, vals, mvals, c.cM);
+        ASEND_CUDA(cudaGetLastError());
+        ++c.launches;
+    }
+}
+
+}  // namespace
+
+void assemble_operator(Ctx& c, int precision) {
+    init_tables();
+    Sbell& A = c.A;
+    const size_t nval = (size_t)A.n_groups * 9 * kSlice;
+    A.v64.alloc(nval);
+    A.v32.alloc(nval);
+    A.v64.zero(c.stream);
+    A.v32.zero(c.stream);
+    double* mvals = nullptr;
+    if (c.dynamic) {
+        A.m64.alloc(nval);
+        A.m64.zero(c.stream);
+        mvals = A.m64.p;
+    } else {
+        A.m64.release();
+    }
+    ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
+    if (precision == 64) {
+        if (c.nn == 8) launch_colours<8, double>(c, A.v64.p, mvals);
+        else launch_colours<4, double>(c, A.v64.p, mvals);
+    } else {
+        if (c.nn == 8) launch_colours<8, float>(c, A.v32.p, mvals);
+        else launch_colours<4, float>(c, A.v32.p, mvals);
+        widen_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(nval, A.v32.p, A.v64.p);
+        ++c.launches;
+    }
+    // penalty scale over the element matrix (K [+ cM M]), then the penalty
+    c.d_max_partial.alloc(1);
+    c.d_max_partial.zero(c.stream);
+    max_abs_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(
+        nval, A.v64.p, reinterpret_cast<unsigned long long*>(c.d_max_partial.p));
+    ++c.launches;
+    double mx = 0.0;
+    ASEND_CUDA(cudaMemcpyAsync(&mx, c.d_max_partial.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    ASEND_CUDA(cudaStreamSynchronize(c.stream));
+    c.sf = 100000.0 * mx;
+    const int npen = (int)c.d_pen_idx.n;
+    if (npen > 0) {
+        penalty_kernel<<<(npen + 255) / 256, 256, 0, c.stream>>>(npen, c.d_pen_idx.p, c.d_pen_coef.p, c.sf, A.v64.p);
+        ++c.launches;
+    }
+    round_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(nval, A.v64.p, A.v32.p);
+    ++c.launches;
+    ASEND_CUDA(cudaGetLastError());
+    ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
+    ASEND_CUDA(cudaEventSynchronize(c.ev1));
+    float ms = 0.f;
+    ASEND_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    c.assembled_precision = precision;
+    c.last_assemble_ms = ms;
+}
+
+}  // namespace asend

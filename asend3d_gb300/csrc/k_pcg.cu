@@ -1,0 +1,720 @@
+// k_pcg.cu -- K3: preconditioned CG on the sliced block-ELL operator.
+//
+// Reference: conj_grad_sparse, solverSrc/asend_run_job/src/matrix_functions.rs:285-362
+// (x0 = 0, g = A x - b, alpha = res / h^T A h, beta = r_next / res,
+// SparseMat::vector_multiply list_ent_meth.rs:64-79 plus the penalty product
+// ConstraintList::get_total_vec_mult const_meth.rs:161-168, folded into the
+// assembled operator here).  Stopping: the reference stops on the absolute
+// g^T M^-1 g <= conv_tol; this solver stops on ||b - A x||_2 <= tol ||b||_2
+// evaluated with the FP64 operator (the residual is re-formed in FP64 before
+// convergence is accepted).
+//
+// GB300 design.
+//  * One thread per node row (3 DOFs) of the sliced block-ELL matrix: each
+//    warp reads its 9 block values per column group as 9 coalesced 128-byte
+//    loads, and gathers the search direction as one 16-byte vector per
+//    neighbour node (direction stored node-padded to 4 components).
+//  * METHOD_MIXED: FP32 values, FP32 direction p and A p, FP32 FMAs in the
+//    SpMV; FP64 x, r, all inner products and the scalar recurrence.  A true
+//    FP64 residual b - A64 x replaces the recurrence residual when the latter
+//    converges or drops by 1e4 since the last replacement (reliable updates),
+//    which keeps the FP32 operator error out of the final answer.
+//  * METHOD_FP64: every value, vector and FMA in FP64 (the plain method).
+//  * Inner products: warp shuffles -> shared memory -> one partial per CTA ->
+//    the last CTA (atomic ticket) sums the partials in a fixed order, so the
+//    reductions are deterministic and need no extra launch.
+//  * Three kernels per iteration (SpMV+dot, x/r update+dots, p update),
+//    captured G iterations at a time in a CUDA graph; every kernel returns
+//    at once when all right-hand sides have converged, so a graph may
+//    overrun convergence harmlessly.  Up to 4 right-hand sides share one
+//    matrix read (block SpMM).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace asend {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kMaxRhs = 4;
+
+struct RhsScalars {
+    double rz, rz_new, pAp, rr, bb, alpha, beta, target, rr_last_true;
+    int32_t iter, done, finished, replace, nonfinite, pad0, pad1, pad2;
+};
+struct Control {
+    int32_t all_done;
+    uint32_t ticket[4];
+    int32_t pad[3];
+};
+
+struct PcgArgs {
+    int n_rows, nrhs, n_dof;
+    const int64_t* slice_off;
+    const uint8_t* row_len;
+    const int32_t* col;
+    const float* v32;
+    const double* v64;
+    const double* f;
+    double* x;
+    double* r;
+    void* p;      // node-padded direction (float4 or 2 x double2 per node)
+    void* ap;     // natural layout A p (float or double)
+    const double* dinv;
+    const float* binv;
+    double* partials;  // [gridDim.x][kMaxRhs][3]
+    RhsScalars* sc;
+    Control* ctl;
+};
+
+template <typename TP>
+struct PadVec;
+template <>
+struct PadVec<float> {
+    __device__ static void load(const void* p, size_t node, float (&v)[3]) {
+        const float4 q = reinterpret_cast<const float4*>(p)[node];
+        v[0] = q.x; v[1] = q.y; v[2] = q.z;
+    }
+    __device__ static void store(void* p, size_t node, const double (&v)[3]) {
+        reinterpret_cast<float4*>(p)[node] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
+    }
+};
+template <>
+struct PadVec<double> {
+    __device__ static void load(const void* p, size_t node, double (&v)[3]) {
+        const double2* q = reinterpret_cast<const double2*>(p) + 2 * node;
+        const double2 a = q[0], b = q[1];
+        v[0] = a.x; v[1] = a.y; v[2] = b.x;
+    }
+    __device__ static void store(void* p, size_t node, const double (&v)[3]) {
+        double2* q = reinterpret_cast<double2*>(p) + 2 * node;
+        q[0] = make_double2(v[0], v[1]);
+        q[1] = make_double2(v[2], 0.0);
+    }
+};
+
+// y[k][a] = sum_j sum_c A[r][j](a,c) * p_k[col_j](c) for NR right-hand sides.
+template <typename TV, typename TP, int NR>
+__device__ __forceinline__ void spmv_row(int row, const PcgArgs& A, const TV* __restrict__ vals,
+                                         const void* __restrict__ p, TP (&y)[NR][3]) {
+#pragma unroll
+    for (int k = 0; k < NR; ++k) y[k][0] = y[k][1] = y[k][2] = (TP)0;
+    const int lane = row & 31;
+    const int64_t g0 = A.slice_off[row >> 5];
+    const int len = A.row_len[row];
+    for (int j = 0; j < len; ++j) {
+        const int64_t g = g0 + j;
+        const int c = A.col[g * 32 + lane];
+        const TV* v = vals + (g * 9) * 32 + lane;
+        TV m[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) m[q] = v[q * 32];
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            TP pv[3];
+            PadVec<TP>::load(p, (size_t)k * A.n_rows + c, pv);
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                y[k][a] = fma((TP)m[a * 3 + 0], pv[0], fma((TP)m[a * 3 + 1], pv[1], fma((TP)m[a * 3 + 2], pv[2], y[k][a])));
+        }
+    }
+}
+
+// Preconditioner application z = M^-1 r for one node.
+template <int PC>
+__device__ __forceinline__ void precond(const PcgArgs& A, int row, const double (&r)[3], double (&z)[3]) {
+    if constexpr (PC == ASEND_PC_JACOBI) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) z[a] = A.dinv[3 * (size_t)row + a] * r[a];
+    } else {
+        const float* B = A.binv + 9 * (size_t)row;
+        const float r0 = (float)r[0], r1 = (float)r[1], r2 = (float)r[2];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) z[a] = (double)fmaf(B[3 * a], r0, fmaf(B[3 * a + 1], r1, B[3 * a + 2] * r2));
+    }
+}
+
+// Last-CTA reduction of NV values per RHS; returns true in the last CTA
+// (all its threads) with tot[k][v] valid in every thread.
+template <int NR, int NV>
+__device__ bool last_block_reduce(const PcgArgs& A, double (&val)[NR][NV], int ticket_id,
+                                  double (&tot)[NR][NV]) {
+    __shared__ double sm[32 * NR * NV];
+    __shared__ bool is_last;
+    double flat[NR * NV];
+#pragma unroll
+    for (int k = 0; k < NR; ++k)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) flat[k * NV + v] = val[k][v];
+    block_sum<NR * NV>(flat, sm);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NR * NV; ++q) A.partials[(size_t)blockIdx.x * (kMaxRhs * 3) + q] = flat[q];
+        __threadfence();
+        const uint32_t t = atomicAdd(&A.ctl->ticket[ticket_id], 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+    double acc[NR * NV];
+#pragma unroll
+    for (int q = 0; q < NR * NV; ++q) acc[q] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        const volatile double* pp = A.partials + (size_t)b * (kMaxRhs * 3);
+#pragma unroll
+        for (int q = 0; q < NR * NV; ++q) acc[q] += pp[q];
+    }
+    __syncthreads();
+    block_sum<NR * NV>(acc, sm);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NR * NV; ++q) sm[q] = acc[q];
+        A.ctl->ticket[ticket_id] = 0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NR; ++k)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) tot[k][v] = sm[k * NV + v];
+    return true;
+}
+
+// K_a: Ap = A p, pAp; alpha = rz / pAp.
+template <typename TV, typename TP, int NR>
+__global__ void __launch_bounds__(kThreads) k_spmv_dot(PcgArgs A) {
+    if (A.ctl->all_done) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    double d[NR][1];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) d[k][0] = 0.0;
+    if (row < A.n_rows) {
+        TP y[NR][3];
+        const TV* vals;
+        if constexpr (sizeof(TV) == 4) vals = A.v32; else vals = A.v64;
+        spmv_row<TV, TP, NR>(row, A, vals, A.p, y);
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            TP pv[3];
+            PadVec<TP>::load(A.p, (size_t)k * A.n_rows + row, pv);
+            TP* ap = reinterpret_cast<TP*>(A.ap) + (size_t)k * A.n_dof + 3 * (size_t)row;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                ap[a] = y[k][a];
+                d[k][0] += (double)pv[a] * (double)y[k][a];
+            }
+        }
+    }
+    double tot[NR][1];
+    if (last_block_reduce<NR, 1>(A, d, 0, tot) && threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            RhsScalars& s = A.sc[k];
+            if (s.done) continue;
+            s.pAp = tot[k][0];
+            s.alpha = s.rz / s.pAp;
+        }
+    }
+}
+
+// K_b: x += alpha p; r -= alpha Ap; z = M r; dots (r,z), (r,r); beta.
+template <typename TP, int NR, int PC>
+__global__ void __launch_bounds__(kThreads) k_update_xr(PcgArgs A) {
+    if (A.ctl->all_done) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    double d[NR][2];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) d[k][0] = d[k][1] = 0.0;
+    if (row < A.n_rows) {
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            if (A.sc[k].done) continue;
+            const double alpha = A.sc[k].alpha;
+            TP pv[3];
+            PadVec<TP>::load(A.p, (size_t)k * A.n_rows + row, pv);
+            const size_t o = (size_t)k * A.n_dof + 3 * (size_t)row;
+            const TP* ap = reinterpret_cast<const TP*>(A.ap) + o;
+            double rv[3], z[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                A.x[o + a] += alpha * (double)pv[a];
+                rv[a] = A.r[o + a] - alpha * (double)ap[a];
+                A.r[o + a] = rv[a];
+            }
+            precond<PC>(A, row, rv, z);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                d[k][0] += rv[a] * z[a];
+                d[k][1] += rv[a] * rv[a];
+            }
+        }
+    }
+    double tot[NR][2];
+    if (last_block_reduce<NR, 2>(A, d, 1, tot) && threadIdx.x == 0) {
+        int all = 1;
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            RhsScalars& s = A.sc[k];
+            if (!s.done) {
+                s.rz_new = tot[k][0];
+                s.rr = tot[k][1];
+                s.beta = s.rz_new / s.rz;
+                s.rz = s.rz_new;
+                s.iter += 1;
+                if (!isfinite(s.rr) || !isfinite(s.rz)) {
+                    s.nonfinite = 1;
+                    s.done = 1;
+                } else if (s.rr <= s.target) {
+                    s.done = 1;  // recurrence converged: the host verifies in FP64
+                }
+            }
+            all &= s.done;
+        }
+        if (all) A.ctl->all_done = 1;
+    }
+}
+
+// K_c: p = M r + beta p (node-padded store).
+template <typename TP, int NR, int PC>
+__global__ void __launch_bounds__(kThreads) k_update_p(PcgArgs A) {
+    if (A.ctl->all_done) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= A.n_rows) return;
+#pragma unroll
+    for (int k = 0; k < NR; ++k) {
+        if (A.sc[k].done) continue;
+        const double beta = A.sc[k].beta;
+        const size_t o = (size_t)k * A.n_dof + 3 * (size_t)row;
+        double rv[3] = {A.r[o], A.r[o + 1], A.r[o + 2]}, z[3];
+        precond<PC>(A, row, rv, z);
+        TP pv[3];
+        PadVec<TP>::load(A.p, (size_t)k * A.n_rows + row, pv);
+        double pn[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) pn[a] = z[a] + beta * (double)pv[a];
+        PadVec<TP>::store(A.p, (size_t)k * A.n_rows + row, pn);
+    }
+}
+
+// True FP64 residual r = b - A64 x (x in natural layout), z = M r, dots.
+// mode 0 = initialise (p = z, bb, target), mode 1 = replace for RHS with
+// sc.replace set (p kept).
+template <typename TP, int NR, int PC>
+__global__ void __launch_bounds__(kThreads) k_residual(PcgArgs A, int mode, double tol2) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = row & 31;
+    double d[NR][3];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) d[k][0] = d[k][1] = d[k][2] = 0.0;
+    if (row < A.n_rows) {
+        double y[NR][3];
+#pragma unroll
+        for (int k = 0; k < NR; ++k) y[k][0] = y[k][1] = y[k][2] = 0.0;
+        const int64_t g0 = A.slice_off[row >> 5];
+        const int len = A.row_len[row];
+        for (int j = 0; j < len; ++j) {
+            const int64_t g = g0 + j;
+            const int c = A.col[g * 32 + lane];
+            const double* v = A.v64 + (g * 9) * 32 + lane;
+            double m[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) m[q] = v[q * 32];
+#pragma unroll
+            for (int k = 0; k < NR; ++k) {
+                const double* xk = A.x + (size_t)k * A.n_dof + 3 * (size_t)c;
+                const double x0 = xk[0], x1 = xk[1], x2 = xk[2];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) y[k][a] = fma(m[a * 3], x0, fma(m[a * 3 + 1], x1, fma(m[a * 3 + 2], x2, y[k][a])));
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            if (mode == 1 && !A.sc[k].replace) continue;
+            const size_t o = (size_t)k * A.n_dof + 3 * (size_t)row;
+            double rv[3], z[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                rv[a] = A.f[o + a] - y[k][a];
+                A.r[o + a] = rv[a];
+            }
+            precond<PC>(A, row, rv, z);
+            if (mode == 0) PadVec<TP>::store(A.p, (size_t)k * A.n_rows + row, z);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                d[k][0] += rv[a] * z[a];
+                d[k][1] += rv[a] * rv[a];
+                d[k][2] += A.f[o + a] * A.f[o + a];
+            }
+        }
+    }
+    double tot[NR][3];
+    if (last_block_reduce<NR, 3>(A, d, 2, tot) && threadIdx.x == 0) {
+        int all = 1;
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            RhsScalars& s = A.sc[k];
+            if (mode == 0 || s.replace) {
+                s.rz = tot[k][0];
+                s.rr = tot[k][1];
+                s.rr_last_true = tot[k][1];
+                if (mode == 0) {
+                    s.bb = tot[k][2];
+                    s.target = tol2 * s.bb;
+                    s.iter = 0;
+                    s.beta = 0.0;
+                }
+                s.replace = 0;
+                s.nonfinite = (!isfinite(s.rr) || !isfinite(s.rz)) ? 1 : 0;
+                s.finished = (s.rr <= s.target) || s.nonfinite;
+                s.done = s.finished;
+            }
+            all &= s.done;
+        }
+        A.ctl->all_done = all;
+    }
+}
+
+// apply helpers (tests / timing)
+template <typename TP>
+__global__ void k_pack(int n_rows, const double* __restrict__ x, void* p) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n_rows) return;
+    double v[3] = {x[3 * (size_t)row], x[3 * (size_t)row + 1], x[3 * (size_t)row + 2]};
+    PadVec<TP>::store(p, row, v);
+}
+template <typename TV, typename TP>
+__global__ void __launch_bounds__(kThreads) k_spmv_plain(PcgArgs A, double* __restrict__ y) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= A.n_rows) return;
+    TP acc[1][3];
+    const TV* vals;
+    if constexpr (sizeof(TV) == 4) vals = A.v32; else vals = A.v64;
+    spmv_row<TV, TP, 1>(row, A, vals, A.p, acc);
+    TP* out = reinterpret_cast<TP*>(A.ap) + 3 * (size_t)row;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        out[a] = acc[0][a];
+        if (y) y[3 * (size_t)row + a] = (double)acc[0][a];
+    }
+}
+
+__global__ void k_jacobi(int n_rows, const int64_t* __restrict__ slice_off, const uint8_t* __restrict__ diag,
+                         const double* __restrict__ v64, double* __restrict__ dinv) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n_rows) return;
+    const int64_t g = slice_off[row >> 5] + diag[row];
+    const int lane = row & 31;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) dinv[3 * (size_t)row + a] = 1.0 / v64[(g * 9 + a * 4) * 32 + lane];
+}
+
+__global__ void k_block_inv(int n_rows, const int64_t* __restrict__ slice_off, const uint8_t* __restrict__ diag,
+                            const double* __restrict__ v64, float* __restrict__ binv) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n_rows) return;
+    const int64_t g = slice_off[row >> 5] + diag[row];
+    const int lane = row & 31;
+    double m[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) m[q] = v64[(g * 9 + q) * 32 + lane];
+    // symmetric positive definite 3x3 block: inverse by cofactors
+    const double c00 = m[4] * m[8] - m[5] * m[7];
+    const double c01 = m[5] * m[6] - m[3] * m[8];
+    const double c02 = m[3] * m[7] - m[4] * m[6];
+    const double det = m[0] * c00 + m[1] * c01 + m[2] * c02;
+    const double id = 1.0 / det;
+    double inv[9];
+    inv[0] = c00 * id;
+    inv[1] = (m[2] * m[7] - m[1] * m[8]) * id;
+    inv[2] = (m[1] * m[5] - m[2] * m[4]) * id;
+    inv[3] = c01 * id;
+    inv[4] = (m[0] * m[8] - m[2] * m[6]) * id;
+    inv[5] = (m[2] * m[3] - m[0] * m[5]) * id;
+    inv[6] = c02 * id;
+    inv[7] = (m[1] * m[6] - m[0] * m[7]) * id;
+    inv[8] = (m[0] * m[4] - m[1] * m[3]) * id;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) binv[9 * (size_t)row + q] = (float)inv[q];
+}
+
+int grid_rows(int n_rows) { return (n_rows + kThreads - 1) / kThreads; }
+
+struct Launcher {
+    Ctx& c;
+    PcgArgs a;
+    int method, pc, nr;
+    template <typename TP, int NR, int PC>
+    void iter_t() {
+        const int g = grid_rows(a.n_rows);
+        if (method == ASEND_METHOD_MIXED) k_spmv_dot<float, float, NR><<<g, kThreads, 0, c.stream>>>(a);
+        else k_spmv_dot<double, double, NR><<<g, kThreads, 0, c.stream>>>(a);
+        k_update_xr<TP, NR, PC><<<g, kThreads, 0, c.stream>>>(a);
+        k_update_p<TP, NR, PC><<<g, kThreads, 0, c.stream>>>(a);
+    }
+    template <typename TP, int NR, int PC>
+    void resid_t(int mode, double tol2) {
+        k_residual<TP, NR, PC><<<grid_rows(a.n_rows), kThreads, 0, c.stream>>>(a, mode, tol2);
+    }
+    template <typename TP, int NR>
+    void dispatch_pc(bool iter, int mode, double tol2) {
+        if (pc == ASEND_PC_JACOBI) {
+            if (iter) iter_t<TP, NR, ASEND_PC_JACOBI>(); else resid_t<TP, NR, ASEND_PC_JACOBI>(mode, tol2);
+        } else {
+            if (iter) iter_t<TP, NR, ASEND_PC_BLOCK>(); else resid_t<TP, NR, ASEND_PC_BLOCK>(mode, tol2);
+        }
+    }
+    template <typename TP>
+    void dispatch_nr(bool iter, int mode, double tol2) {
+        switch (nr) {
+            case 1: dispatch_pc<TP, 1>(iter, mode, tol2); break;
+            case 2: dispatch_pc<TP, 2>(iter, mode, tol2); break;
+            case 3: dispatch_pc<TP, 3>(iter, mode, tol2); break;
+            default: dispatch_pc<TP, 4>(iter, mode, tol2); break;
+        }
+    }
+    void iteration() {  // launches are counted per graph launch
+        if (method == ASEND_METHOD_MIXED) dispatch_nr<float>(true, 0, 0.0);
+        else dispatch_nr<double>(true, 0, 0.0);
+    }
+    void residual(int mode, double tol2) {
+        if (method == ASEND_METHOD_MIXED) dispatch_nr<float>(false, mode, tol2);
+        else dispatch_nr<double>(false, mode, tol2);
+        c.launches += 1;
+    }
+};
+
+}  // namespace
+
+// Device-side y = A x (natural layout), value precision 32 or 64.
+void apply_operator_device(Ctx& c, int precision, const double* d_x, double* d_y) {
+    PcgArgs a{};
+    a.n_rows = c.A.n_rows;
+    a.nrhs = 1;
+    a.n_dof = c.n_dof;
+    a.slice_off = c.A.slice_off.p;
+    a.row_len = c.A.row_len.p;
+    a.col = c.A.col.p;
+    a.v32 = c.A.v32.p;
+    a.v64 = c.A.v64.p;
+    const int g = grid_rows(a.n_rows);
+    if (precision == 32) {
+        DArr<float> p, ap;
+        p.alloc((size_t)4 * a.n_rows);
+        ap.alloc(c.n_dof);
+        a.p = p.p;
+        a.ap = ap.p;
+        k_pack<float><<<g, kThreads, 0, c.stream>>>(a.n_rows, d_x, p.p);
+        k_spmv_plain<float, float><<<g, kThreads, 0, c.stream>>>(a, d_y);
+        ASEND_CUDA(cudaGetLastError());
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+    } else {
+        DArr<double> p, ap;
+        p.alloc((size_t)4 * a.n_rows);
+        ap.alloc(c.n_dof);
+        a.p = p.p;
+        a.ap = ap.p;
+        k_pack<double><<<g, kThreads, 0, c.stream>>>(a.n_rows, d_x, p.p);
+        k_spmv_plain<double, double><<<g, kThreads, 0, c.stream>>>(a, d_y);
+        ASEND_CUDA(cudaGetLastError());
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    c.launches += 2;
+}
+
+// Mean time of n_launch SpMV launches (the PCG's dominant kernel) and its
+// algorithmic bytes: values + column indices + one read of the direction +
+// one write of A p.
+double time_spmv(Ctx& c, int precision, int n_launch, double* bytes) {
+    const int n = c.A.n_rows;
+    PcgArgs a{};
+    a.n_rows = n;
+    a.nrhs = 1;
+    a.n_dof = c.n_dof;
+    a.slice_off = c.A.slice_off.p;
+    a.row_len = c.A.row_len.p;
+    a.col = c.A.col.p;
+    a.v32 = c.A.v32.p;
+    a.v64 = c.A.v64.p;
+    const int g = grid_rows(n);
+    const int64_t blocks = c.A.nnz_scalar() / 9;
+    const size_t vsz = (precision == 32) ? 4 : 8;
+    *bytes = (double)blocks * (9.0 * vsz + 4.0) + (double)n * (4.0 * vsz) + (double)c.n_dof * vsz;
+    std::vector<double> ones(c.n_dof, 1.0);
+    DArr<double> x;
+    x.upload(ones, c.stream);
+    DArr<char> p, ap;
+    p.alloc((size_t)4 * n * vsz);
+    ap.alloc((size_t)c.n_dof * vsz);
+    a.p = p.p;
+    a.ap = ap.p;
+    if (precision == 32) k_pack<float><<<g, kThreads, 0, c.stream>>>(n, x.p, p.p);
+    else k_pack<double><<<g, kThreads, 0, c.stream>>>(n, x.p, p.p);
+    for (int w = 0; w < 3; ++w) {
+        if (precision == 32) k_spmv_plain<float, float><<<g, kThreads, 0, c.stream>>>(a, nullptr);
+        else k_spmv_plain<double, double><<<g, kThreads, 0, c.stream>>>(a, nullptr);
+    }
+    ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
+    for (int i = 0; i < n_launch; ++i) {
+        if (precision == 32) k_spmv_plain<float, float><<<g, kThreads, 0, c.stream>>>(a, nullptr);
+        else k_spmv_plain<double, double><<<g, kThreads, 0, c.stream>>>(a, nullptr);
+    }
+    ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
+    ASEND_CUDA(cudaEventSynchronize(c.ev1));
+    ASEND_CUDA(cudaGetLastError());
+    float ms = 0.f;
+    ASEND_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    c.launches += n_launch + 4;
+    return ms / n_launch;
+}
+
+// Batched PCG over all load cases (chunks of up to 4 sharing one matrix read).
+int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f,
+              double* d_x, int nrhs_all) {
+    if (o.method != ASEND_METHOD_FP64 && o.method != ASEND_METHOD_MIXED) throw InputError("unknown method");
+    int pc = o.precond;
+    int status_fallback = 0;
+    if (pc == ASEND_PC_LEARNED) {
+        // the learned blocks are installed by the preconditioner module when
+        // available; without a trained model the Jacobi fallback is used
+        pc = ASEND_PC_JACOBI;
+        status_fallback = 1;
+    }
+    if (pc != ASEND_PC_JACOBI && pc != ASEND_PC_BLOCK) throw InputError("unknown preconditioner");
+    if (!(o.rel_tol > 0.0)) throw InputError("rel_tol must be positive");
+    const int n = c.A.n_rows, nd = c.n_dof;
+    const int max_it = o.max_iter > 0 ? o.max_iter : nd;
+    const int G = o.graph_iters > 0 ? o.graph_iters : 16;
+    const size_t tot = (size_t)nrhs_all * nd;
+    if (!warm) ASEND_CUDA(cudaMemsetAsync(d_x, 0, tot * sizeof(double), c.stream));
+    c.d_r.alloc(std::max(c.d_r.n, tot));
+    const int grid = grid_rows(n);
+    c.d_partials.alloc((size_t)grid * kMaxRhs * 3);
+    // preconditioner
+    if (pc == ASEND_PC_JACOBI) {
+        c.d_dinv.alloc(nd);
+        k_jacobi<<<grid, kThreads, 0, c.stream>>>(n, c.A.slice_off.p, c.A.diag.p, c.A.v64.p, c.d_dinv.p);
+    } else {
+        c.d_binv.alloc((size_t)9 * n);
+        k_block_inv<<<grid, kThreads, 0, c.stream>>>(n, c.A.slice_off.p, c.A.diag.p, c.A.v64.p, c.d_binv.p);
+    }
+    ++c.launches;
+    const bool mixed = o.method == ASEND_METHOD_MIXED;
+    if (mixed) {
+        c.d_p32.alloc((size_t)kMaxRhs * 4 * n);
+        c.d_ap32.alloc((size_t)kMaxRhs * nd);
+    } else {
+        c.d_p64.alloc((size_t)kMaxRhs * 4 * n);
+        c.d_ap64.alloc((size_t)kMaxRhs * nd);
+    }
+    DArr<RhsScalars> d_sc;
+    DArr<Control> d_ctl;
+    d_sc.alloc(kMaxRhs);
+    d_ctl.alloc(1);
+    RhsScalars* h_sc = reinterpret_cast<RhsScalars*>(c.h_sc);
+    static_assert(sizeof(RhsScalars) * kMaxRhs <= sizeof(PcgScalars) * 64, "pinned scalar mirror too small");
+    int iters_max = 0, repl_total = 0, status = 0;
+    double relres_max = 0.0;
+    ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
+    for (int r0 = 0; r0 < nrhs_all; r0 += kMaxRhs) {
+        const int nr = std::min(kMaxRhs, nrhs_all - r0);
+        Launcher L{c, PcgArgs{}, o.method, pc, nr};
+        PcgArgs& a = L.a;
+        a.n_rows = n;
+        a.nrhs = nr;
+        a.n_dof = nd;
+        a.slice_off = c.A.slice_off.p;
+        a.row_len = c.A.row_len.p;
+        a.col = c.A.col.p;
+        a.v32 = c.A.v32.p;
+        a.v64 = c.A.v64.p;
+        a.f = d_f + (size_t)r0 * nd;
+        a.x = d_x + (size_t)r0 * nd;
+        a.r = c.d_r.p + (size_t)r0 * nd;
+        a.p = mixed ? (void*)c.d_p32.p : (void*)c.d_p64.p;
+        a.ap = mixed ? (void*)c.d_ap32.p : (void*)c.d_ap64.p;
+        a.dinv = c.d_dinv.p;
+        a.binv = c.d_binv.p;
+        a.partials = c.d_partials.p;
+        a.sc = d_sc.p;
+        a.ctl = d_ctl.p;
+        d_sc.zero(c.stream);
+        d_ctl.zero(c.stream);
+        L.residual(0, o.rel_tol * o.rel_tol);
+        ASEND_CUDA(cudaGetLastError());
+        // capture G iterations once for this chunk
+        cudaGraph_t graph;
+        cudaGraphExec_t exec;
+        ASEND_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < G; ++i) L.iteration();
+        ASEND_CUDA(cudaStreamEndCapture(c.stream, &graph));
+        ASEND_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+        ASEND_CUDA(cudaGraphDestroy(graph));
+        int since_repl = 0;
+        for (;;) {
+            ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc.p, sizeof(RhsScalars) * nr, cudaMemcpyDeviceToHost, c.stream));
+            ASEND_CUDA(cudaStreamSynchronize(c.stream));
+            bool all_finished = true, any_replace = false, any_nonfinite = false;
+            int it_now = 0;
+            for (int k = 0; k < nr; ++k) {
+                RhsScalars& s = h_sc[k];
+                it_now = std::max(it_now, (int)s.iter);
+                if (s.nonfinite) { any_nonfinite = true; continue; }
+                if (s.finished) continue;
+                all_finished = false;
+                const bool conv = s.done != 0;
+                const bool drop = mixed && s.rr < 1e-4 * s.rr_last_true;
+                const bool periodic = o.replace_every > 0 && since_repl >= o.replace_every;
+                if (conv || drop || periodic) {
+                    s.replace = 1;
+                    any_replace = true;
+                }
+            }
+            if (any_nonfinite) { status = ASEND_NONFINITE; break; }
+            if (all_finished) break;
+            if (it_now >= max_it) { status = std::max(status, (int)ASEND_MAX_ITER); break; }
+            if (any_replace) {
+                ASEND_CUDA(cudaMemcpyAsync(d_sc.p, h_sc, sizeof(RhsScalars) * nr, cudaMemcpyHostToDevice, c.stream));
+                L.residual(1, 0.0);
+                ++repl_total;
+                since_repl = 0;
+                continue;  // re-check (a replaced RHS may now be finished)
+            }
+            ASEND_CUDA(cudaGraphLaunch(exec, c.stream));
+            c.launches += 3 * G;
+            since_repl += G;
+        }
+        ASEND_CUDA(cudaGraphExecDestroy(exec));
+        ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc.p, sizeof(RhsScalars) * nr, cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        for (int k = 0; k < nr; ++k) {
+            iters_max = std::max(iters_max, (int)h_sc[k].iter);
+            const double rel = h_sc[k].bb > 0 ? std::sqrt(h_sc[k].rr_last_true / h_sc[k].bb) : std::sqrt(h_sc[k].rr_last_true);
+            relres_max = std::max(relres_max, rel);
+            if (h_sc[k].nonfinite) status = ASEND_NONFINITE;
+            else if (!h_sc[k].finished) status = std::max(status, (int)ASEND_MAX_ITER);
+        }
+    }
+    ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
+    ASEND_CUDA(cudaEventSynchronize(c.ev1));
+    ASEND_CUDA(cudaGetLastError());
+    float ms = 0.f;
+    ASEND_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    c.last_method = o.method;
+    if (st) {
+        st->iterations = iters_max;
+        st->status = status;
+        st->replacements = repl_total;
+        st->n_rhs = nrhs_all;
+        st->rel_residual = relres_max;
+        st->ms_solve = ms;
+        st->ms_assemble = c.last_assemble_ms;
+        st->penalty_scale = c.sf;
+    }
+    if (status == 0 && status_fallback) status = ASEND_FALLBACK;
+    if (st) st->status = status;
+    return status;
+}
+
+}  // namespace asend

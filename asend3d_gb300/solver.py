@@ -1,0 +1,276 @@
+"""Host-side mirror of the reference's model / load / DV / objective interface,
+driving the CUDA library through its C ABI.
+
+The reference's user interface (asendUtils, Python) describes a model as
+node/element sets, 'displacement' constraints built from (nodeSet, dof,
+coefficient) terms (src/asendUtils/model/Constraint.py), nodal forces and
+surface tractions (Model.addNodalForce / addSurfaceTraction,
+src/asendUtils/model/Model.py:306-354), design variables over element sets
+(src/asendUtils/variables/DesignVariables.py:13-30) and objective terms
+(src/asendUtils/objective/Objective.py:14-39), then runs the Rust solver.
+``Problem`` holds the same description; ``GpuSolver`` hands it to
+``libasend_gpu.so`` (the GB300 replacement of the Rust solver core).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import SolveOpts, SolveStats
+from .mesh import BlockMesh
+
+
+class AsendError(RuntimeError):
+    pass
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+@dataclass
+class Problem:
+    mesh: BlockMesh
+    E: np.ndarray
+    nu: np.ndarray
+    rho: np.ndarray | None = None
+    node_sets: dict = field(default_factory=dict)
+    elem_sets: dict = field(default_factory=dict)
+    # constraints: (terms=[(node_set, comp(1-based), coef), ...], rhs)
+    constraints: list = field(default_factory=list)
+    # loads[case] = list of ("nodalForce", set, load6) | ("surfaceTraction", elset, normDir, normTol, t3)
+    #               | ("vector", f)
+    loads: list = field(default_factory=list)
+    objective: tuple = ("compliance",)
+    # design variables: (elem_set, coefficients)
+    design_vars: list = field(default_factory=list)
+
+    def add_node_set(self, name, nodes):
+        self.node_sets[name] = np.asarray(nodes, dtype=np.int32)
+
+    def add_elem_set(self, name, elems):
+        self.elem_sets[name] = np.asarray(elems, dtype=np.int32)
+
+    def fix_displacement(self, set_name, comps=(1, 2, 3), rhs=0.0):
+        for c in comps:
+            self.constraints.append(([(set_name, c, 1.0)], rhs))
+
+    def _case(self, case):
+        while len(self.loads) <= case:
+            self.loads.append([])
+        return self.loads[case]
+
+    def add_nodal_force(self, set_name, F, case=0):
+        load = np.zeros(6)
+        load[: len(F)] = F
+        self._case(case).append(("nodalForce", set_name, load))
+
+    def add_surface_traction(self, elem_set, normal_dir, traction, norm_tol=1.0, case=0):
+        self._case(case).append(("surfaceTraction", elem_set, np.asarray(normal_dir, float), float(norm_tol),
+                                 np.asarray(traction, float)))
+
+    def add_load_vector(self, f, case=0):
+        self._case(case).append(("vector", np.asarray(f, float)))
+
+
+class GpuSolver:
+    """One library context (one CUDA stream) holding one problem."""
+
+    def __init__(self, problem: Problem, device: int = 0):
+        self.lib = _lib.load()
+        self.ctx = self.lib.asend_create(device)
+        if not self.ctx:
+            raise AsendError("asend_create failed (no CUDA device?)")
+        self.p = problem
+        self.set_ids = {}
+        self.elset_ids = {}
+        self._setup()
+
+    # -- helpers -----------------------------------------------------------
+    def _check(self, rc, what):
+        if rc < 0:
+            msg = self.lib.asend_last_error(self.ctx).decode()
+            raise AsendError(f"{what} failed ({rc}): {msg}")
+        return rc
+
+    def close(self):
+        if self.ctx:
+            self.lib.asend_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _setup(self):
+        p, m = self.p, self.p.mesh
+        coords = np.ascontiguousarray(m.coords, dtype=np.float64)
+        conn = np.ascontiguousarray(m.conn, dtype=np.int32)
+        E = np.ascontiguousarray(p.E, dtype=np.float64)
+        nu = np.ascontiguousarray(np.broadcast_to(p.nu, E.shape), dtype=np.float64)
+        rho = None if p.rho is None else np.ascontiguousarray(np.broadcast_to(p.rho, E.shape), dtype=np.float64)
+        self._keep = (coords, conn, E, nu, rho)
+        self._check(self.lib.asend_set_mesh(self.ctx, m.elem_type, m.n_nodes, _ptr(coords, C.c_double), m.n_elems,
+                                            _ptr(conn, C.c_int32), _ptr(E, C.c_double), _ptr(nu, C.c_double),
+                                            None if rho is None else _ptr(rho, C.c_double), None), "set_mesh")
+        for name, nodes in p.node_sets.items():
+            arr = np.ascontiguousarray(nodes, dtype=np.int32)
+            self.set_ids[name] = self._check(self.lib.asend_add_node_set(self.ctx, len(arr), _ptr(arr, C.c_int32)),
+                                             "add_node_set")
+        for name, els in p.elem_sets.items():
+            arr = np.ascontiguousarray(els, dtype=np.int32)
+            self.elset_ids[name] = self._check(
+                self.lib.asend_add_element_set(self.ctx, len(arr), _ptr(arr, C.c_int32)), "add_element_set")
+        for terms, rhs in p.constraints:
+            sets = np.array([self.set_ids[t[0]] for t in terms], dtype=np.int32)
+            comps = np.array([t[1] for t in terms], dtype=np.int32)
+            coefs = np.array([t[2] for t in terms], dtype=np.float64)
+            self._check(self.lib.asend_add_constraint(self.ctx, len(terms), _ptr(sets, C.c_int32),
+                                                      _ptr(comps, C.c_int32), _ptr(coefs, C.c_double), rhs),
+                        "add_constraint")
+        self.set_loads()
+        obj = p.objective
+        if obj[0] == "compliance":
+            self._check(self.lib.asend_set_objective(self.ctx, _lib.OBJ_COMPLIANCE, -1, 0, 1.0), "set_objective")
+        else:
+            _, set_name, comp, coef = obj
+            self._check(self.lib.asend_set_objective(self.ctx, _lib.OBJ_DISPLACEMENT, self.set_ids[set_name],
+                                                     comp, coef), "set_objective")
+        for elset, coefs in p.design_vars:
+            cf = np.ascontiguousarray(np.atleast_1d(coefs), dtype=np.float64)
+            self._check(self.lib.asend_add_modulus_design_var(self.ctx, self.elset_ids[elset], len(cf),
+                                                              _ptr(cf, C.c_double)), "add_design_var")
+
+    def set_loads(self):
+        self._check(self.lib.asend_clear_loads(self.ctx), "clear_loads")
+        for case, items in enumerate(self.p.loads):
+            for it in items:
+                if it[0] == "nodalForce":
+                    load = np.ascontiguousarray(it[2], dtype=np.float64)
+                    self._check(self.lib.asend_add_nodal_force(self.ctx, case, self.set_ids[it[1]],
+                                                               _ptr(load, C.c_double)), "add_nodal_force")
+                elif it[0] == "surfaceTraction":
+                    nd = np.ascontiguousarray(it[2], dtype=np.float64)
+                    t = np.ascontiguousarray(it[4], dtype=np.float64)
+                    self._check(self.lib.asend_add_surface_traction(self.ctx, case, self.elset_ids[it[1]],
+                                                                    _ptr(nd, C.c_double), it[3],
+                                                                    _ptr(t, C.c_double)), "add_surface_traction")
+                else:
+                    f = np.ascontiguousarray(it[1], dtype=np.float64)
+                    self._check(self.lib.asend_add_load_vector(self.ctx, case, _ptr(f, C.c_double)),
+                                "add_load_vector")
+
+    # -- API ---------------------------------------------------------------
+    @property
+    def n_dof(self) -> int:
+        return self.lib.asend_n_dof(self.ctx)
+
+    @property
+    def n_cases(self) -> int:
+        return self.lib.asend_n_load_cases(self.ctx)
+
+    def set_modulus(self, E):
+        E = np.ascontiguousarray(E, dtype=np.float64)
+        self._keep_E = E
+        self._check(self.lib.asend_set_modulus(self.ctx, _ptr(E, C.c_double)), "set_modulus")
+
+    def assemble(self, precision=64, dynamic=False, dt=0.0, beta=0.25, gamma=0.5):
+        self._check(self.lib.asend_assemble(self.ctx, precision, int(dynamic), dt, beta, gamma), "assemble")
+
+    def load_vector(self, case=0) -> np.ndarray:
+        f = np.zeros(self.n_dof)
+        self._check(self.lib.asend_get_load_vector(self.ctx, case, _ptr(f, C.c_double)), "get_load_vector")
+        return f
+
+    @staticmethod
+    def opts(method=_lib.METHOD_MIXED, precond=_lib.PC_JACOBI, rel_tol=1e-8, max_iter=0, graph_iters=16,
+             warm_start=0, replace_every=0) -> SolveOpts:
+        return SolveOpts(method, precond, rel_tol, max_iter, graph_iters, warm_start, replace_every)
+
+    def static_solve(self, u0=None, **kw):
+        o = self.opts(warm_start=int(u0 is not None), **kw)
+        nc = max(1, self.n_cases)
+        u = np.zeros(nc * self.n_dof) if u0 is None else np.ascontiguousarray(u0, dtype=np.float64).ravel().copy()
+        st = SolveStats()
+        rc = self._check(self.lib.asend_static_solve(self.ctx, C.byref(o), _ptr(u, C.c_double), C.byref(st)),
+                         "static_solve")
+        return u.reshape(nc, self.n_dof), rc, st.as_dict()
+
+    def static_solve_device(self, **kw):
+        o = self.opts(**kw)
+        st = SolveStats()
+        rc = self._check(self.lib.asend_static_solve_device(self.ctx, C.byref(o), C.byref(st)), "static_solve")
+        return rc, st.as_dict()
+
+    def solution(self, case=0) -> np.ndarray:
+        u = np.zeros(self.n_dof)
+        self._check(self.lib.asend_get_solution(self.ctx, case, _ptr(u, C.c_double)), "get_solution")
+        return u
+
+    def adjoint_gradient(self, **kw):
+        o = self.opts(**kw)
+        L = C.c_double(0.0)
+        g = np.zeros(self.p.mesh.n_elems)
+        st = SolveStats()
+        rc = self._check(self.lib.asend_adjoint_gradient(self.ctx, C.byref(o), C.byref(L), _ptr(g, C.c_double),
+                                                         C.byref(st)), "adjoint_gradient")
+        return L.value, g, rc, st.as_dict()
+
+    def design_var_gradient(self, dLdE) -> np.ndarray:
+        dLdE = np.ascontiguousarray(dLdE, dtype=np.float64)
+        out = np.zeros(max(1, len(self.p.design_vars)))
+        n = self._check(self.lib.asend_design_var_gradient(self.ctx, _ptr(dLdE, C.c_double), _ptr(out, C.c_double)),
+                        "design_var_gradient")
+        return out[:n]
+
+    def newmark(self, amp, probe_dof=-1, **kw):
+        o = self.opts(**kw)
+        amp = np.ascontiguousarray(amp, dtype=np.float64)
+        hist = np.zeros(len(amp))
+        u = np.zeros(self.n_dof)
+        st = SolveStats()
+        rc = self._check(self.lib.asend_newmark_run(self.ctx, C.byref(o), len(amp), _ptr(amp, C.c_double), probe_dof,
+                                                    _ptr(hist, C.c_double), _ptr(u, C.c_double), C.byref(st)),
+                         "newmark_run")
+        return hist, u, rc, st.as_dict()
+
+    def csr(self, which=0):
+        nnz = C.c_int64(0)
+        self._check(self.lib.asend_get_csr(self.ctx, which, C.byref(nnz), None, None, None), "get_csr")
+        rp = np.zeros(self.n_dof + 1, dtype=np.int64)
+        col = np.zeros(nnz.value, dtype=np.int32)
+        val = np.zeros(nnz.value, dtype=np.float64)
+        self._check(self.lib.asend_get_csr(self.ctx, which, C.byref(nnz), _ptr(rp, C.c_int64), _ptr(col, C.c_int32),
+                                           _ptr(val, C.c_double)), "get_csr")
+        return rp, col, val
+
+    def coloring(self):
+        col = np.zeros(self.p.mesh.n_elems, dtype=np.int32)
+        n = self._check(self.lib.asend_get_coloring(self.ctx, _ptr(col, C.c_int32)), "get_coloring")
+        return col, n
+
+    def apply(self, x, precision=64):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        self._check(self.lib.asend_apply_operator(self.ctx, precision, _ptr(x, C.c_double), _ptr(y, C.c_double)),
+                    "apply_operator")
+        return y
+
+    def time_spmv(self, precision=32, n_launch=50):
+        ms = C.c_double(0)
+        by = C.c_double(0)
+        self._check(self.lib.asend_time_spmv(self.ctx, precision, n_launch, C.byref(ms), C.byref(by)), "time_spmv")
+        return ms.value, by.value
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.asend_stream(self.ctx) or 0)
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.lib.asend_kernel_launches(self.ctx))

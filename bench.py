@@ -1,0 +1,372 @@
+"""Benchmark: DOF-solves/sec of the static + adjoint solve path on one GB300.
+
+Workload (default): the 200x40x40 hex8 block (1,013,643 DOF) with a seeded
+lognormal modulus field (median 70 GPa, sigma_log 0.3, correlation 0.1 L),
+nu = 0.33, fixed end + distributed end-face traction, compliance objective.
+One step = FP64 element integration + coloured CSR-block assembly + penalty,
+mixed-precision PCG to ||f - A u|| / ||f|| <= 1e-8 (FP64 operator), and the
+adjoint compliance gradient over all 320,000 element moduli.
+
+value  = DOF-solves/s with inputs resident in HBM (device-event timed).
+e2e    = the same through the C ABI with host buffers: per step the element
+         moduli and the load go host->device and the displacement and the
+         gradient come back, inside the timed region.
+The plain FP64 point-Jacobi PCG on the same GPU is timed as well
+(plain_fp64_*); the CPU baseline is the FP64 oracle's restatement of the
+reference's block-LDL^T PCG on the host cores.
+
+--impl reference times the reference's CPU algorithm (the oracle port:
+block-LDL^T-preconditioned CG, reference stopping rule replaced by the same
+1e-8 relative residual) on the host cores, one process per core.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "DOF-solves/sec at 1e-8 rel. residual (static + adjoint), 1 GB300"
+UNIT = "DOF-solves/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=200)
+    ap.add_argument("--ny", type=int, default=40)
+    ap.add_argument("--nz", type=int, default=40)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-nx", type=int, default=40)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM traffic of the FP32 SpMV from the committed ncu summary."""
+    f = ROOT / "profiles" / "spmv_fp32_block_large.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch_full_size:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# CPU reference arm (the oracle's restatement of the reference algorithm)
+# --------------------------------------------------------------------------
+def _cpu_sample(args):
+    nx, seed = args
+    from asend3d_gb300 import configs
+    from oracle import pyoracle as po
+
+    p = configs.block_large(nx=nx, ny=nx // 5, nz=nx // 5, seed=seed)
+    t0 = time.perf_counter()
+    o = po.Oracle(p)
+    f = o.loads()[0] + o.penalty_rhs()
+    u, rc, st = o.solve(f, precond=po.PC_BLOCK_LDL, stop=po.STOP_RELATIVE, tol=1e-8)
+    g, _, _, _ = o.adjoint(u, lam=u)
+    dt = time.perf_counter() - t0
+    return o.n_dof, dt, st["iterations"], st["rel_residual"]
+
+
+def cpu_baseline(nx: int, procs: int):
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_cpu_sample, [(nx, 100 + k) for k in range(procs)])
+    wall = time.perf_counter() - t0
+    ndof = sum(r[0] for r in res)
+    per_proc = statistics.mean(r[1] for r in res)
+    return {"value": ndof / wall, "unit": UNIT, "cores": procs, "kind": "port",
+            "sample": f"{procs} x {nx}x{nx // 5}x{nx // 5} hex8 instances of the same workload "
+                      f"({res[0][0]} DOF each), block-LDL^T PCG to 1e-8 + adjoint, one process per core; "
+                      f"{per_proc:.2f} s per instance, {res[0][2]} iterations",
+            "per_instance_s": per_proc}
+
+
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    vals = []
+    for _ in range(a.warmup):
+        cpu_baseline(a.cpu_sample_nx, procs)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        cb = cpu_baseline(a.cpu_sample_nx, procs)
+        vals.append(cb["value"])
+    wall = time.perf_counter() - t0
+    v = statistics.mean(vals)
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": 1000 * wall / a.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"block_large sample {cb['sample']}"},
+           "cpu_baseline": {**cb, "value": v},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def run_ours(a):
+    import torch
+
+    from asend3d_gb300 import _lib, configs
+    from asend3d_gb300.solver import GpuSolver
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    p = configs.block_large(nx=a.nx, ny=a.ny, nz=a.nz, seed=2024 + rank)
+    g = GpuSolver(p, device=local)
+    stream = torch.cuda.ExternalStream(g.stream, device=torch.device("cuda", local))
+    n_dof = g.n_dof
+    n_el = p.mesh.n_elems
+    mixed = dict(method=_lib.METHOD_MIXED, precond=_lib.PC_JACOBI, rel_tol=1e-8, graph_iters=32)
+
+    def step_device():
+        g.assemble(precision=64)
+        rc, st = g.static_solve_device(**mixed)
+        L, rc2, st2 = adjoint_nocopy()
+        return rc, st
+
+    import ctypes as C
+
+    o_adj = g.opts(**mixed)
+
+    def adjoint_nocopy():
+        Lc = C.c_double(0)
+        st = _lib.SolveStats()
+        rc = g.lib.asend_adjoint_gradient(g.ctx, C.byref(o_adj), C.byref(Lc), None, C.byref(st))
+        return Lc.value, rc, st
+
+    # ---- warm-up
+    for _ in range(a.warmup):
+        rc, st = step_device()
+        assert rc == 0, (rc, st)
+    iters = st["iterations"]
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    launches0 = g.kernel_launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        stats = []
+        for _ in range(a.steps):
+            rc, st = step_device()
+            assert rc == 0, (rc, st)
+            stats.append(st)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = g.kernel_launches - launches0
+    ms_step = ms / a.steps
+    if world > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * n_dof / (ms_step / 1000.0)
+
+    # ---- e2e through the C ABI with pinned host buffers
+    E_h = torch.from_numpy(p.E.copy()).pin_memory()
+    u_h = torch.zeros(n_dof, dtype=torch.float64).pin_memory()
+    gE_h = torch.zeros(n_el, dtype=torch.float64).pin_memory()
+    f_np = g.load_vector(0)  # load (incl. penalty rhs after assembly)
+    f_h = torch.from_numpy(f_np).pin_memory()
+    P = C.POINTER(C.c_double)
+    o_e2e = g.opts(**mixed)
+
+    def step_e2e():
+        g.lib.asend_set_modulus(g.ctx, C.cast(E_h.data_ptr(), P))
+        g.lib.asend_clear_loads(g.ctx)
+        g.lib.asend_add_load_vector(g.ctx, 0, C.cast(f_h.data_ptr(), P))
+        g.lib.asend_assemble(g.ctx, 64, 0, 0.0, 0.25, 0.5)
+        st = _lib.SolveStats()
+        rc = g.lib.asend_static_solve(g.ctx, C.byref(o_e2e), C.cast(u_h.data_ptr(), P), C.byref(st))
+        Lc = C.c_double(0)
+        st2 = _lib.SolveStats()
+        rc2 = g.lib.asend_adjoint_gradient(g.ctx, C.byref(o_e2e), C.byref(Lc), C.cast(gE_h.data_ptr(), P),
+                                           C.byref(st2))
+        return rc, rc2
+
+    for _ in range(2):
+        step_e2e()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        rc, rc2 = step_e2e()
+        assert rc == 0 and rc2 == 0
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / a.steps
+    wall_e2e = (time.perf_counter() - t0) * 1000 / a.steps
+    ms_e2e = max(ms_e2e, wall_e2e)
+    e2e_value = world * n_dof / (ms_e2e / 1000.0)
+    h2d = n_el * 8 + n_dof * 8
+    d2h = n_dof * 8 + n_el * 8 + 8
+
+    # restore the benchmark load for the remaining measurements
+    g.set_loads()
+
+    # ---- plain FP64 Jacobi PCG on the same GPU (the spec comparison)
+    plain = dict(method=_lib.METHOD_FP64, precond=_lib.PC_JACOBI, rel_tol=1e-8, graph_iters=32)
+    g.assemble(precision=64)
+    g.static_solve_device(**plain)
+    torch.cuda.synchronize()
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    n_plain = max(1, min(a.steps, 3))
+    p0.record(stream)
+    for _ in range(n_plain):
+        g.assemble(precision=64)
+        rc, st_plain = g.static_solve_device(**plain)
+        adjoint_nocopy()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    ms_plain = p0.elapsed_time(p1) / n_plain
+    plain_value = world * n_dof / (ms_plain / 1000.0)
+
+    # ---- roofline of the dominant kernel (FP32 sliced block-ELL SpMV)
+    ms_spmv, bytes_spmv = g.time_spmv(precision=32, n_launch=50)
+    ms_spmv64, bytes_spmv64 = g.time_spmv(precision=64, n_launch=20)
+    peak, peak_kind = measured_peak()
+    achieved = bytes_spmv / (ms_spmv * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_spmv_dot<float> (sliced block-ELL FP32 SpMV)", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"of {peak_kind}",
+            "traffic": ncu_traffic(), "algorithmic_bytes_per_launch": bytes_spmv, "ms_per_launch": ms_spmv,
+            "fp64_spmv": {"ms_per_launch": ms_spmv64, "achieved_GBps": bytes_spmv64 / (ms_spmv64 * 1e-3) / 1e9}}
+
+    out = None
+    if rank == 0:
+        cb = None
+        if not a.no_cpu_baseline and world == 1:
+            cb = cpu_baseline(a.cpu_sample_nx, 1)
+            cb["kind"] = "port"
+        clocks = clk.summary()
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+               "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32 SpMV + f64 dots/residual", "data": "synthetic (seeded lognormal field)",
+               "config": {"workload": f"block_large {a.nx}x{a.ny}x{a.nz} hex8 static + adjoint",
+                          "n_dof": n_dof, "n_elems": n_el, "rhs_per_step": 1, "method": "mixed FP32/FP64 PCG, Jacobi",
+                          "rel_tol": 1e-8, "l2": "operator 640 MB FP64 + 330 MB FP32 > 129 MB L2 (inputs larger than L2)",
+                          "parallelism": f"replicas x{world}"},
+               "iterations": iters, "ms_breakdown": {"assemble": stats[-1]["ms_assemble"],
+                                                     "solve": stats[-1]["ms_solve"]},
+               "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "ms_per_step": ms_e2e},
+               "plain_fp64_jacobi": {"value": plain_value, "ms_per_step": ms_plain,
+                                     "iterations": st_plain["iterations"]},
+               "speedup_vs_plain_fp64": value / plain_value,
+               "roofline": roof, "cpu_baseline": cb, "clocks": clocks, "gpu_launches": launches}
+        print(json.dumps(out))
+    g.close()
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return out
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

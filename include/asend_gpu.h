@@ -1,0 +1,210 @@
+/*
+ * asend_gpu.h -- C ABI of the GB300 (sm_103a) linear-elastic solve library.
+ *
+ * Drop-in boundary for ASenD3D's static / Newmark / adjoint solve path.  The
+ * reference drives this path in-process through Rust methods on `Model`
+ * (paths relative to solverSrc/asend_run_job/src/):
+ *   Model::read_model_input / read_constraint_input / read_load_input /
+ *       read_des_var_input / read_objective_input   model_input.rs:312-1375
+ *   Model::analysis_prep                           model_prep.rs:881-952
+ *   Model::solve                                   model_analysis.rs:560-673
+ *   Model::solve_step (elastic branch)             model_analysis.rs:450-534
+ *   conj_grad_sparse                               matrix_functions.rs:285-362
+ *   Model::solve_for_adjoint                       model_analysis.rs:1065-1231
+ *   Model::get_obj_gradient                        model_analysis.rs:1544-1706
+ * Each entry point below names the reference interface it replaces.
+ *
+ * Conventions
+ *   - Plain pointers and sizes; no C++ or torch types cross the boundary.
+ *   - Host buffers are caller-owned; device memory is library-owned.
+ *   - Return codes: 0 ok, 1 iteration cap reached, 2 non-finite values,
+ *     3 preconditioner fallback used, negative = input / CUDA error
+ *     (asend_last_error() gives the message).  Nothing aborts the process.
+ *   - One context per host thread; a context owns one CUDA stream.
+ *   - DOF numbering is natural: dof = node * dof_per_node + component
+ *     (component 0-based).  Element types use the reference codes:
+ *     8 = hex8 (brick8), 4 = tet4, 41 = shell4 (quad shell).
+ */
+#ifndef ASEND_GPU_H
+#define ASEND_GPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct asend_ctx asend_ctx;
+
+/* status codes */
+#define ASEND_OK 0
+#define ASEND_MAX_ITER 1
+#define ASEND_NONFINITE 2
+#define ASEND_FALLBACK 3
+#define ASEND_EINVAL (-1)
+#define ASEND_ECUDA (-2)
+#define ASEND_ESTATE (-3)
+
+/* solver methods */
+#define ASEND_METHOD_FP64 0   /* plain FP64 PCG (values, SpMV, vectors all FP64)           */
+#define ASEND_METHOD_MIXED 1  /* FP32 SpMV + FP64 vectors/dots + FP64 residual replacement */
+
+/* preconditioners */
+#define ASEND_PC_JACOBI 0     /* point Jacobi                                             */
+#define ASEND_PC_BLOCK 1      /* nodal block Jacobi (dof_per_node x dof_per_node blocks)  */
+#define ASEND_PC_LEARNED 2    /* MLP-predicted nodal blocks, Jacobi fallback              */
+
+/* objective kinds (reference objective categories, objective_meth.rs:592-942) */
+#define ASEND_OBJ_DISPLACEMENT 0 /* 'displacement' + 'powerNorm' on a node set            */
+#define ASEND_OBJ_COMPLIANCE 1   /* f^T u summed over load cases (self-adjoint)           */
+
+typedef struct asend_solve_opts {
+    int32_t method;       /* ASEND_METHOD_*                                          */
+    int32_t precond;      /* ASEND_PC_*                                              */
+    double rel_tol;       /* target ||f - A u||_2 / ||f||_2 with the FP64 operator   */
+    int32_t max_iter;     /* iteration cap (0 = n_dof, as model_prep.rs:236-244)      */
+    int32_t graph_iters;  /* PCG iterations per captured CUDA graph (0 = 16)         */
+    int32_t warm_start;   /* 1: use u_io on entry as the initial guess               */
+    int32_t replace_every;/* mixed: force a true-residual replacement after this many
+                             iterations without one (0 = only on residual drops)     */
+} asend_solve_opts;
+
+typedef struct asend_solve_stats {
+    int32_t iterations;     /* PCG iterations (max over right-hand sides)           */
+    int32_t status;         /* ASEND_OK / ASEND_MAX_ITER / ...                      */
+    int32_t replacements;   /* FP64 true-residual replacements (mixed method)       */
+    int32_t n_rhs;
+    double rel_residual;    /* final ||f - A u|| / ||f|| (FP64 operator), max over RHS */
+    double ms_assemble;     /* device time of the last assembly                     */
+    double ms_solve;        /* device time of the solve (event-timed on the stream) */
+    double ms_adjoint;      /* device time of the adjoint contraction               */
+    double penalty_scale;   /* sf = 1e5 * max|K_ij| (model_analysis.rs:255-259)     */
+} asend_solve_stats;
+
+/* ---- context -------------------------------------------------------------- */
+asend_ctx* asend_create(int32_t device);
+void asend_destroy(asend_ctx* ctx);
+const char* asend_last_error(const asend_ctx* ctx);
+/* Version / build string (sm arch, compile flags). */
+const char* asend_version(void);
+
+/* ---- model input (replaces model_input.rs:312-860 read_model_input) --------
+ * One element type per mesh.  coords[n_nodes*3]; conn[n_elems*nodes_per_elem];
+ * per-element isotropic material E, nu, rho (rho may be NULL for statics);
+ * thickness per element for shells (else NULL). */
+int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const double* coords,
+                   int32_t n_elems, const int32_t* conn, const double* E, const double* nu,
+                   const double* rho, const double* thickness);
+/* Replace the per-element moduli (a new design / UQ sample) without
+ * rebuilding the pattern.  Replaces the DV-perturbed property path of
+ * element_properties.rs:648-764 for the isotropic-modulus case. */
+int asend_set_modulus(asend_ctx* ctx, const double* E);
+
+/* Node / element sets (model_input.rs:720-860 'sets' blocks).  Returns the
+ * set id (>= 0) or a negative error code. */
+int asend_add_node_set(asend_ctx* ctx, int32_t n, const int32_t* nodes);
+int asend_add_element_set(asend_ctx* ctx, int32_t n, const int32_t* elems);
+
+/* 'displacement' constraint (read_constraint_input model_input.rs:872-969;
+ * matrix rows per const_meth.rs:30-90): sum_t coef_t * u[node_t, comp_t] = rhs
+ * for every row, where a term over an n-node set contributes its k-th node to
+ * row k and a term over a 1-node set contributes to every row.  comp is the
+ * reference's 1-based DOF component. */
+int asend_add_constraint(asend_ctx* ctx, int32_t n_terms, const int32_t* node_set,
+                         const int32_t* comp, const double* coef, double rhs);
+
+/* ---- loads (read_load_input model_input.rs:981-1123;
+ *      build_elastic_app_load model_analysis.rs:21-75) ----------------------
+ * Loads accumulate into load case `rhs` (0-based; cases are created on use). */
+int asend_add_nodal_force(asend_ctx* ctx, int32_t rhs, int32_t node_set, const double* load6);
+int asend_add_surface_traction(asend_ctx* ctx, int32_t rhs, int32_t elem_set,
+                               const double* norm_dir, double norm_tol_deg,
+                               const double* traction);
+/* Raw load vector in natural DOF numbering (adds to load case `rhs`). */
+int asend_add_load_vector(asend_ctx* ctx, int32_t rhs, const double* f);
+int asend_clear_loads(asend_ctx* ctx);
+int asend_n_dof(const asend_ctx* ctx);
+int asend_n_load_cases(const asend_ctx* ctx);
+/* Copy load case `rhs` (with the penalty right-hand side folded in once the
+ * operator is assembled) to the host. */
+int asend_get_load_vector(asend_ctx* ctx, int32_t rhs, double* f_out);
+
+/* ---- assembly (analysis_prep + prep_matrix_factorizations,
+ *      model_prep.rs:556-618, 881-952; element loop model_analysis.rs:179-201;
+ *      element kernels element_equations.rs:206-418 / 852-1062) ------------
+ * precision: 64 = FP64 element integration (FP32 copy made by rounding),
+ *            32 = FP32 element integration (FP64 copy made by widening).
+ * dynamic != 0 assembles K + c_M M with c_M = -1/(dt^2 (beta - gamma)) and
+ * keeps M (Newmark, element_equations.rs:977-988). */
+int asend_assemble(asend_ctx* ctx, int32_t precision, int32_t dynamic, double dt, double beta,
+                   double gamma);
+/* Assembled operator (K [+ c_M M] + sf C^T C) as scalar CSR in natural DOF
+ * numbering with sorted columns.  Pass NULL to query sizes: *nnz_out. */
+int asend_get_csr(asend_ctx* ctx, int32_t which, int64_t* nnz_out, int64_t* row_ptr,
+                  int32_t* col, double* val);
+/* Element colouring used by the scatter assembly (no two elements of one
+ * colour share a node).  colour[n_elems]; returns the number of colours. */
+int asend_get_coloring(asend_ctx* ctx, int32_t* colour_out);
+
+/* ---- static solve (Model::solve / solve_step, model_analysis.rs:450-673;
+ *      conj_grad_sparse matrix_functions.rs:285-362) -----------------------
+ * Solves A u_r = f_r + sf C^T q for every load case r.  u_io[n_rhs*n_dof]
+ * (natural numbering, case-major); used as the initial guess when
+ * opts->warm_start, overwritten with the solution. */
+int asend_static_solve(asend_ctx* ctx, const asend_solve_opts* opts, double* u_io,
+                       asend_solve_stats* stats);
+/* Device-resident variant: the solution stays on the device (for chained
+ * solve -> adjoint calls without host copies). */
+int asend_static_solve_device(asend_ctx* ctx, const asend_solve_opts* opts,
+                              asend_solve_stats* stats);
+int asend_get_solution(asend_ctx* ctx, int32_t rhs, double* u_out);
+
+/* ---- objective + adjoint gradient (read_objective_input
+ *      model_input.rs:1298-1375; Model::get_obj_gradient static branch
+ *      model_analysis.rs:1632-1704; solve_for_adjoint :1065-1126;
+ *      d_relasticd_d :1379-1457) --------------------------------------------
+ * kind ASEND_OBJ_DISPLACEMENT: L = coef * sum_{n in set} u[n, comp]
+ *   ('powerNorm' with exponent 1, objective_meth.rs:329-337), comp 1-based.
+ * kind ASEND_OBJ_COMPLIANCE: L = sum_r f_r^T u_r.
+ * Gradient w.r.t. the per-element isotropic modulus: dLdE[n_elems].
+ * The solution of the preceding asend_static_solve* call is used. */
+int asend_set_objective(asend_ctx* ctx, int32_t kind, int32_t node_set, int32_t comp,
+                        double coef);
+int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double* L_out,
+                           double* dLdE_out, asend_solve_stats* stats);
+/* Design variables over element sets with per-element coefficients
+ * (read_des_var_input model_input.rs:1218-1296; element coefficient lists
+ * model_prep.rs:414-442): dL/dD_i = sum_e coef_ie dL/dE_e. */
+int asend_add_modulus_design_var(asend_ctx* ctx, int32_t elem_set, int32_t n_coef,
+                                 const double* coefs);
+int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_out);
+
+/* ---- Newmark transient (Model::solve dynamic loop model_analysis.rs:591-624;
+ *      Node::update_vel_acc node_meth.rs:127-138, advance_disp :158-165) -----
+ * Load at step i (time i*dt) = amp[i] * (load case 0).  Records
+ * u[probe_dof] after each step in probe_hist[n_steps] (may be NULL) and the
+ * final displacement in u_final[n_dof] (may be NULL).  Requires
+ * asend_assemble(..., dynamic=1, dt, beta, gamma).  Each step's PCG is
+ * warm-started from the previous step's increment. */
+int asend_newmark_run(asend_ctx* ctx, const asend_solve_opts* opts, int32_t n_steps,
+                      const double* amp, int32_t probe_dof, double* probe_hist,
+                      double* u_final, asend_solve_stats* stats);
+
+/* ---- kernel-level entry points (measurement / tests) ----------------------
+ * y = A x with the assembled operator at the given value precision (32/64),
+ * host buffers.  Equivalent of SparseMat::vector_multiply
+ * (list_ent_meth.rs:64-79) plus the penalty product (const_meth.rs:92-103). */
+int asend_apply_operator(asend_ctx* ctx, int32_t precision, const double* x, double* y);
+/* Time n_launch back-to-back operator applications on the library stream with
+ * CUDA events; returns the mean ms per launch and the algorithmic bytes per
+ * launch. */
+int asend_time_spmv(asend_ctx* ctx, int32_t precision, int32_t n_launch, double* ms_per_launch,
+                    double* bytes_per_launch);
+/* Number of kernels this library launched since the context was created. */
+int64_t asend_kernel_launches(const asend_ctx* ctx);
+/* The context's CUDA stream (cudaStream_t as void*), so a caller can record
+ * its own CUDA events around library calls. */
+void* asend_stream(const asend_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1116 @@
+// asend_oracle.cpp -- FP64 CPU restatement of the reference's linear-elastic
+// solve path.  TEST INFRASTRUCTURE: the checker for the CUDA library, never
+// linked into it.  Citations are "file:line" relative to
+// solverSrc/asend_run_job/src/ of MSDOToolz/ASenD3D.
+//
+// Parity status: pinned by the reference's analytic known answers
+// (examples/testCases/hexBeam/notes.txt, singleHex) and by central finite
+// differences; the reference itself (Rust) cannot be built here.
+#include "asend_oracle.h"
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+namespace {
+
+constexpr double kTol = 1e-12;                 // constants.rs:13 (TOL)
+constexpr double kR1ORt3 = 0.5773502691896257; // constants.rs:3
+constexpr double kR1O6 = 0.16666666666666666;  // constants.rs:6
+constexpr double kPi = 3.14159265358979323846;
+
+// ---------------------------------------------------------------------------
+// Element type tables: element_meth.rs:74-448 (initialize_type)
+// ---------------------------------------------------------------------------
+struct TypeInfo {
+    int type = 0, nn = 0, dpn = 3, nip = 0, nfaces = 0;
+    double ip[8 * 3] = {};
+    double wt[8] = {};
+    int faces[6][4] = {};
+    int face_nn = 0;
+};
+
+TypeInfo type_info(int type) {
+    TypeInfo t;
+    t.type = type;
+    if (type == 8) {
+        // hex8: 2x2x2 Gauss points ordered with s0 fastest (element_meth.rs:157-189)
+        t.nn = 8; t.dpn = 3; t.nip = 8; t.nfaces = 6; t.face_nn = 4;
+        const double sv[2] = {-kR1ORt3, kR1ORt3};
+        int k = 0;
+        for (int c = 0; c < 2; ++c)
+            for (int b = 0; b < 2; ++b)
+                for (int a = 0; a < 2; ++a) {
+                    t.ip[3 * k + 0] = sv[a];
+                    t.ip[3 * k + 1] = sv[b];
+                    t.ip[3 * k + 2] = sv[c];
+                    t.wt[k] = 1.0;
+                    ++k;
+                }
+        // faces: element_meth.rs:525-591 (initialize_faces, hex branch)
+        const int f[6][4] = {{3, 2, 1, 0}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                             {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+        std::memcpy(t.faces, f, sizeof(f));
+    } else if (type == 4) {
+        // tet4: one point at (1/4,1/4,1/4), weight 1/6 (element_meth.rs:84-101)
+        t.nn = 4; t.dpn = 3; t.nip = 1; t.nfaces = 4; t.face_nn = 3;
+        t.ip[0] = t.ip[1] = t.ip[2] = 0.25;
+        t.wt[0] = kR1O6;
+        const int f[4][4] = {{0, 2, 1, 0}, {0, 1, 3, 0}, {1, 2, 3, 0}, {0, 3, 2, 0}};
+        std::memcpy(t.faces, f, sizeof(f));
+    }
+    return t;
+}
+
+// Shape functions and parametric derivatives: element_soln_fields.rs:120-229
+// (tet4 :121-140, hex8 :171-211).  dn[3*n + j] = dN_n/ds_j.
+void shape(int type, const double* s, double* n, double* dn) {
+    if (type == 8) {
+        const double sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                 {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+        for (int a = 0; a < 8; ++a) {
+            const double f0 = 1.0 + sg[a][0] * s[0];
+            const double f1 = 1.0 + sg[a][1] * s[1];
+            const double f2 = 1.0 + sg[a][2] * s[2];
+            n[a] = 0.125 * f0 * f1 * f2;
+            dn[3 * a + 0] = 0.125 * sg[a][0] * f1 * f2;
+            dn[3 * a + 1] = 0.125 * sg[a][1] * f0 * f2;
+            dn[3 * a + 2] = 0.125 * sg[a][2] * f0 * f1;
+        }
+    } else if (type == 4) {
+        n[0] = 1.0 - s[0] - s[1] - s[2];
+        n[1] = s[0]; n[2] = s[1]; n[3] = s[2];
+        const double d[12] = {-1, -1, -1, 1, 0, 0, 0, 1, 0, 0, 0, 1};
+        std::memcpy(dn, d, sizeof(d));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Givens QR with angle storage (matrix_functions.rs:50-105 q_rfactor_ar,
+// :107-165 solveq_rx_eqb_ar), full square case (tri_diag = 0), and the
+// determinant / inverse built on it (matrix_functions.rs:1707-1729).
+// ---------------------------------------------------------------------------
+void givens_factor(double* a, int n) {
+    for (int c = 0; c < n; ++c) {
+        for (int r = c + 1; r < n; ++r) {
+            double& piv = a[c * n + c];
+            if (std::fabs(piv) < kTol) piv = kTol;
+            const double th = std::atan(a[r * n + c] / piv);
+            const double sn = std::sin(th), cs = std::cos(th);
+            for (int k = c; k < n; ++k) {
+                const double top = a[c * n + k], bot = a[r * n + k];
+                a[c * n + k] = cs * top + sn * bot;
+                a[r * n + k] = -sn * top + cs * bot;
+            }
+            a[r * n + c] = th;  // the rotation angle replaces the zeroed entry
+        }
+    }
+}
+
+void givens_solve(double* x, const double* a, double* b, int n) {
+    for (int c = 0; c < n; ++c) {
+        for (int r = c + 1; r < n; ++r) {
+            const double th = a[r * n + c];
+            const double sn = std::sin(th), cs = std::cos(th);
+            const double top = b[c], bot = b[r];
+            b[c] = cs * top + sn * bot;
+            b[r] = -sn * top + cs * bot;
+        }
+        x[c] = 0.0;
+    }
+    for (int c = n - 1; c >= 0; --c) {
+        double acc = 0.0;
+        for (int k = c + 1; k < n; ++k) acc += a[c * n + k] * x[k];
+        x[c] = (b[c] - acc) / a[c * n + c];
+    }
+}
+
+double det_inv(double* inv, const double* mat_in, int n) {
+    double a[36];
+    std::memcpy(a, mat_in, sizeof(double) * n * n);
+    givens_factor(a, n);
+    double det = 1.0, b[6], x[6];
+    for (int col = 0; col < n; ++col) {
+        for (int k = 0; k < n; ++k) b[k] = (k == col) ? 1.0 : 0.0;
+        givens_solve(x, a, b, n);
+        for (int k = 0; k < n; ++k) inv[k * n + col] = x[k];
+        det *= a[col * n + col];
+    }
+    return det;
+}
+
+// Integration point data: element_soln_fields.rs:383-463 (solid branch).
+// xyz[3*nn] node-major.  Returns detJ; dndx[3*a + j] = dN_a/dx_j.
+double ip_data(int type, int nn, const double* xyz, const double* s, double* n, double* dndx) {
+    double dn[24];
+    shape(type, s, n, dn);
+    double J[9] = {0};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+            for (int a = 0; a < nn; ++a) acc += xyz[3 * a + i] * dn[3 * a + j];
+            J[3 * i + j] = acc;
+        }
+    double Ji[9];
+    const double det = det_inv(Ji, J, 3);
+    for (int a = 0; a < nn; ++a)
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+            for (int k = 0; k < 3; ++k) acc += dn[3 * a + k] * Ji[3 * k + j];
+            dndx[3 * a + j] = acc;
+        }
+    return det;
+}
+
+// Solid 6x6 stiffness from the compliance matrix: element_properties.rs:648-764
+// (get_solid_stiff_dfd0, engineering-constant branch).  Voigt order
+// 11,22,33,12,13,23.  e/nu/g are (E1,E2,E3), (nu12,nu13,nu23), (G12,G13,G23).
+void solid_cmat(const double e[3], const double nu[3], const double g[3], double* C) {
+    double S[36] = {0};
+    S[0] = 1.0 / e[0];
+    S[1] = -nu[0] / e[0];
+    S[2] = -nu[1] / e[0];
+    S[6] = S[1];
+    S[7] = 1.0 / e[1];
+    S[8] = -nu[2] / e[1];
+    S[12] = S[2];
+    S[13] = S[8];
+    S[14] = 1.0 / e[2];
+    S[21] = 1.0 / g[0];
+    S[28] = 1.0 / g[1];
+    S[35] = 1.0 / g[2];
+    det_inv(C, S, 6);
+}
+
+void iso_cmat(double E, double nu, double* C) {
+    const double e[3] = {E, E, E};
+    const double n3[3] = {nu, nu, nu};
+    const double G = E / (2.0 * (1.0 + nu));
+    const double g[3] = {G, G, G};
+    solid_cmat(e, n3, g, C);
+}
+
+// Strain-displacement columns: element_soln_fields.rs:1345-1461
+// (get_solid_strain_dfd0, single-DOF derivative branch, identity orientation).
+// B[6 * tot + col] layout (row k = strain component).
+void solid_bmat(int nn, const double* dndx, double* B) {
+    const int tot = 3 * nn;
+    std::fill(B, B + 6 * tot, 0.0);
+    for (int a = 0; a < nn; ++a) {
+        const double* g = dndx + 3 * a;
+        for (int d = 0; d < 3; ++d) {
+            const int col = 3 * a + d;
+            double sm[9] = {0};
+            for (int i = 0; i < 3; ++i)
+                for (int j = i; j < 3; ++j) {
+                    if (i == d) sm[3 * i + j] += g[j];
+                    if (j == d) sm[3 * i + j] += g[i];
+                }
+            B[0 * tot + col] = 0.5 * sm[0];
+            B[1 * tot + col] = 0.5 * sm[4];
+            B[2 * tot + col] = 0.5 * sm[8];
+            B[3 * tot + col] = sm[1];
+            B[4 * tot + col] = sm[2];
+            B[5 * tot + col] = sm[5];
+        }
+    }
+}
+
+// Element stiffness: element_equations.rs:206-418 (get_ruk_dfd0 with
+// get_matrix, linear geometry, dpn == 3): K += B^T (C B) detJ w per point,
+// with C*B scaled by detJ*w first (:377-395).
+void solid_ke(int type, const double* xyz, const double* C, double* ke) {
+    const TypeInfo t = type_info(type);
+    const int nn = t.nn, tot = 3 * nn;
+    std::fill(ke, ke + tot * tot, 0.0);
+    double n[8], dndx[24], B[6 * 24], CB[6 * 24];
+    for (int p = 0; p < t.nip; ++p) {
+        const double det = ip_data(type, nn, xyz, t.ip + 3 * p, n, dndx);
+        const double djw = det * t.wt[p];
+        solid_bmat(nn, dndx, B);
+        for (int k = 0; k < 6; ++k)
+            for (int c = 0; c < tot; ++c) {
+                double acc = 0.0;
+                for (int l = 0; l < 6; ++l) acc += C[6 * k + l] * B[l * tot + c];
+                CB[k * tot + c] = acc * djw;
+            }
+        for (int i = 0; i < tot; ++i)
+            for (int j = 0; j < tot; ++j) {
+                double acc = 0.0;
+                for (int k = 0; k < 6; ++k) acc += B[k * tot + i] * CB[k * tot + j];
+                ke[i * tot + j] += acc;
+            }
+    }
+}
+
+// Consistent mass: element_equations.rs:583-609 (get_rum_dfd0, solid branch)
+void solid_me(int type, const double* xyz, double rho, double* me) {
+    const TypeInfo t = type_info(type);
+    const int nn = t.nn, tot = 3 * nn;
+    std::fill(me, me + tot * tot, 0.0);
+    double n[8], dndx[24];
+    for (int p = 0; p < t.nip; ++p) {
+        const double det = ip_data(type, nn, xyz, t.ip + 3 * p, n, dndx);
+        const double djw = det * t.wt[p];
+        for (int i = 0; i < tot; ++i)
+            for (int j = 0; j < tot; ++j)
+                if (i % 3 == j % 3) me[i * tot + j] += n[i / 3] * n[j / 3] * rho * djw;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sparse matrix with a fixed pattern (sorted columns) and element-order
+// accumulation.  The reference keeps row linked lists and add_entry appends or
+// accumulates (list_ent_meth.rs:6-18); every (i,j) sum is accumulated in
+// element order, which this CSR reproduces.
+// ---------------------------------------------------------------------------
+struct Csr {
+    int n = 0;
+    std::vector<int64_t> ptr;
+    std::vector<int32_t> col;
+    std::vector<double> val;
+    int64_t find(int r, int c) const {
+        auto b = col.begin() + ptr[r], e = col.begin() + ptr[r + 1];
+        auto it = std::lower_bound(b, e, c);
+        return (it != e && *it == c) ? (it - col.begin()) : -1;
+    }
+    void matvec(const double* x, double* y) const {  // y += A x (list_ent_meth.rs:64-79)
+        for (int r = 0; r < n; ++r) {
+            double acc = y[r];
+            for (int64_t k = ptr[r]; k < ptr[r + 1]; ++k) acc += val[k] * x[col[k]];
+            y[r] = acc;
+        }
+    }
+    double max_abs() const {  // list_ent_meth.rs:81-94
+        double m = 0.0;
+        for (double v : val) m = std::max(m, std::fabs(v));
+        return m;
+    }
+};
+
+}  // namespace
+
+struct orc_model {
+    TypeInfo ti;
+    int n_nodes = 0, n_el = 0, dpn = 3, n_dof = 0;
+    std::vector<double> xyz, E, nu, rho, thk;
+    std::vector<int32_t> conn;
+    // constraint rows (const_meth.rs:30-90 builds C with one row per set member)
+    std::vector<int32_t> c_ptr, c_dof;
+    std::vector<double> c_coef, c_rhs;
+    Csr K, M;           // K holds the full solve matrix (K + c_M M when dynamic)
+    bool dynamic = false;
+    double cM = 0.0;    // coefficient of M inside K (Newmark)
+    double sf = 0.0;    // penalty scale (model_analysis.rs:255-259)
+    bool assembled = false;
+};
+
+namespace {
+
+void elem_xyz(const orc_model* m, int e, double* xyz) {
+    const int nn = m->ti.nn;
+    for (int a = 0; a < nn; ++a) {
+        const int nd = m->conn[(size_t)e * nn + a];
+        for (int j = 0; j < 3; ++j) xyz[3 * a + j] = m->xyz[3 * (size_t)nd + j];
+    }
+}
+
+// Node adjacency from element connectivity, sorted; defines the full 3x3-block
+// pattern the reference creates by add_entry on every element DOF pair.
+void build_pattern(const orc_model* m, Csr& A) {
+    const int nn = m->ti.nn, dpn = m->dpn;
+    std::vector<std::vector<int32_t>> adj(m->n_nodes);
+    for (int e = 0; e < m->n_el; ++e)
+        for (int a = 0; a < nn; ++a)
+            for (int b = 0; b < nn; ++b)
+                adj[m->conn[(size_t)e * nn + a]].push_back(m->conn[(size_t)e * nn + b]);
+    A.n = m->n_dof;
+    A.ptr.assign(A.n + 1, 0);
+    for (int nd = 0; nd < m->n_nodes; ++nd) {
+        auto& v = adj[nd];
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        for (int c = 0; c < dpn; ++c) A.ptr[(size_t)nd * dpn + c + 1] = (int64_t)v.size() * dpn;
+    }
+    for (int r = 0; r < A.n; ++r) A.ptr[r + 1] += A.ptr[r];
+    A.col.resize(A.ptr[A.n]);
+    for (int nd = 0; nd < m->n_nodes; ++nd)
+        for (int c = 0; c < dpn; ++c) {
+            int64_t k = A.ptr[(size_t)nd * dpn + c];
+            for (int32_t nb : adj[nd])
+                for (int cc = 0; cc < dpn; ++cc) A.col[k++] = nb * dpn + cc;
+        }
+    A.val.assign(A.col.size(), 0.0);
+}
+
+// Penalty constraint operator pieces (const_meth.rs:92-119).
+// y += sf * C^T (C x)
+void constraint_apply(const orc_model* m, const double* x, double* y) {
+    const int nr = (int)m->c_rhs.size();
+    for (int r = 0; r < nr; ++r) {
+        double cx = 0.0;
+        for (int k = m->c_ptr[r]; k < m->c_ptr[r + 1]; ++k) cx += m->c_coef[k] * x[m->c_dof[k]];
+        cx *= m->sf;
+        for (int k = m->c_ptr[r]; k < m->c_ptr[r + 1]; ++k) y[m->c_dof[k]] += m->c_coef[k] * cx;
+    }
+}
+// f += -sf C^T (C u - q)   (const_meth.rs:105-119 get_load)
+void constraint_load(const orc_model* m, const double* u, double* f) {
+    const int nr = (int)m->c_rhs.size();
+    for (int r = 0; r < nr; ++r) {
+        double q = -m->c_rhs[r];
+        for (int k = m->c_ptr[r]; k < m->c_ptr[r + 1]; ++k) q += m->c_coef[k] * u[m->c_dof[k]];
+        q *= -m->sf;
+        for (int k = m->c_ptr[r]; k < m->c_ptr[r + 1]; ++k) f[m->c_dof[k]] += m->c_coef[k] * q;
+    }
+}
+
+void apply_A(const orc_model* m, const double* x, double* y) {
+    std::fill(y, y + m->n_dof, 0.0);
+    m->K.matvec(x, y);
+    constraint_apply(m, x, y);
+}
+
+// ---------------------------------------------------------------------------
+// Skyline LDL^T restricted to diagonal blocks (lower_tri_mat_meth.rs:15-241).
+// Works in the permuted ("reference") DOF numbering given by perm (new->old).
+// ---------------------------------------------------------------------------
+struct Skyline {
+    int dim = 0, max_bw = 0;
+    std::vector<int64_t> range;  // start offset per row, size dim+1
+    std::vector<int32_t> min_col;
+    std::vector<double> mat;
+    std::vector<double> z;
+};
+
+struct PermOp {
+    std::vector<int32_t> new_of_old, old_of_new;  // DOF permutations
+};
+
+// allocate_from_sparse_mat :15-90 + populate_from_sparse_mat :96-140
+void skyline_build(const orc_model* m, const PermOp& P, int block_dofs, Skyline& S) {
+    const int n = m->n_dof;
+    S.dim = n;
+    std::vector<int64_t> rng(n + 1, 0);
+    for (int rn = 0; rn < n; ++rn) rng[rn] = 1;
+    // element matrix contributions
+    for (int ro = 0; ro < n; ++ro) {
+        const int rn = P.new_of_old[ro];
+        const int blk_mc = block_dofs * (rn / block_dofs);
+        for (int64_t k = m->K.ptr[ro]; k < m->K.ptr[ro + 1]; ++k) {
+            const int cn = P.new_of_old[m->K.col[k]];
+            if (cn <= rn && cn >= blk_mc) rng[rn] = std::max<int64_t>(rng[rn], rn - cn + 1);
+        }
+    }
+    // constraint couplings (C^T C)
+    const int nr = (int)m->c_rhs.size();
+    for (int r = 0; r < nr; ++r)
+        for (int k = m->c_ptr[r]; k < m->c_ptr[r + 1]; ++k) {
+            const int i2 = P.new_of_old[m->c_dof[k]];
+            const int blk_mc = block_dofs * (i2 / block_dofs);
+            for (int k2 = m->c_ptr[r]; k2 < m->c_ptr[r + 1]; ++k2) {
+                const int i3 = P.new_of_old[m->c_dof[k2]];
+                if (i3 <= i2 && i3 >= blk_mc) rng[i2] = std::max<int64_t>(rng[i2], i2 - i3 + 1);
+            }
+        }
+    S.min_col.resize(n);
+    S.range.assign(n + 1, 0);
+    S.max_bw = 0;
+    for (int i = 0; i < n; ++i) {
+        S.min_col[i] = i - (int)(rng[i] - 1);
+        S.max_bw = std::max<int>(S.max_bw, (int)rng[i]);
+        S.range[i + 1] = S.range[i] + rng[i];
+    }
+    S.mat.assign(S.range[n], 0.0);
+    S.z.assign(n, 0.0);
+    for (int ro = 0; ro < n; ++ro) {
+        const int rn = P.new_of_old[ro];
+        for (int64_t k = m->K.ptr[ro]; k < m->K.ptr[ro + 1]; ++k) {
+            const int cn = P.new_of_old[m->K.col[k]];
+            if (cn <= rn && cn >= S.min_col[rn]) S.mat[S.range[rn] + (cn - S.min_col[rn])] += m->K.val[k];
+        }
+    }
+    for (int r = 0; r < nr; ++r)
+        for (int k = m->c_ptr[r]; k < m->c_ptr[r + 1]; ++k) {
+            const int i2 = P.new_of_old[m->c_dof[k]];
+            for (int k2 = m->c_ptr[r]; k2 < m->c_ptr[r + 1]; ++k2) {
+                const int i3 = P.new_of_old[m->c_dof[k2]];
+                if (i3 <= i2 && i3 >= S.min_col[i2])
+                    S.mat[S.range[i2] + (i3 - S.min_col[i2])] += m->sf * m->c_coef[k] * m->c_coef[k2];
+            }
+        }
+}
+
+// ldl_factor :142-192
+void skyline_factor(Skyline& S) {
+    const int n = S.dim;
+    std::vector<double> ld(n, 0.0);
+    for (int c = 0; c < n; ++c) {
+        int64_t i3 = S.range[c];
+        for (int k = S.min_col[c]; k < c; ++k) {
+            ld[k] = S.mat[i3] * S.mat[S.range[k + 1] - 1];
+            ++i3;
+        }
+        double sum = 0.0;
+        int64_t i2 = S.range[c];
+        for (int k = S.min_col[c]; k < c; ++k) sum += ld[k] * S.mat[i2++];
+        S.mat[S.range[c + 1] - 1] -= sum;
+        const double dcc = S.mat[S.range[c + 1] - 1];
+        for (int r = c + 1; r < c + S.max_bw && r < n; ++r) {
+            if (S.min_col[r] <= c) {
+                const int st = std::max(S.min_col[r], S.min_col[c]);
+                int64_t i4 = S.range[r] + (st - S.min_col[r]);
+                double s2 = 0.0;
+                for (int k = st; k < c; ++k) s2 += ld[k] * S.mat[i4++];
+                const int64_t idx = S.range[r] + (c - S.min_col[r]);
+                S.mat[idx] = (S.mat[idx] - s2) / dcc;
+            }
+        }
+    }
+}
+
+// ldl_solve :194-227
+void skyline_solve(Skyline& S, double* x, const double* rhs) {
+    const int n = S.dim;
+    S.z[0] = rhs[0];
+    for (int i = 1; i < n; ++i) {
+        int64_t k = S.range[i];
+        double sum = 0.0;
+        for (int c = S.min_col[i]; c < i; ++c) sum += S.mat[k++] * S.z[c];
+        S.z[i] = rhs[i] - sum;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        double sum = 0.0;
+        const int stop = std::min(n, i + S.max_bw + 1);
+        for (int r = i + 1; r < stop; ++r)
+            if (i >= S.min_col[r]) sum += S.mat[S.range[r] + (i - S.min_col[r])] * x[r];
+        x[i] = S.z[i] / S.mat[S.range[i + 1] - 1] - sum;
+    }
+}
+
+// pos_def :229-241
+bool skyline_pos_def(const Skyline& S) {
+    for (int i = 0; i < S.dim; ++i)
+        if (S.mat[S.range[i + 1] - 1] < 0.0) return false;
+    return true;
+}
+
+// Node reordering: model_prep.rs:56-303 (reorder_nodes).  Connectivity sets
+// keep insertion order (nd_el_set_meth.rs:5-13 add_if_absent); constraint
+// couplings per model_prep.rs:20-54 (add_constraint_conn) for rows built from
+// one node set with a single term (each constrained node coupled to itself).
+std::vector<int32_t> reorder_nodes(const orc_model* m, int block_dim) {
+    const int nn = m->ti.nn, N = m->n_nodes;
+    std::vector<std::vector<int32_t>> conn(N);
+    auto add = [&](int a, int b) {
+        auto& v = conn[a];
+        if (std::find(v.begin(), v.end(), b) == v.end()) v.push_back(b);
+    };
+    for (int e = 0; e < m->n_el; ++e)
+        for (int i = 0; i < nn; ++i)
+            for (int j = i + 1; j < nn; ++j) {
+                const int a = m->conn[(size_t)e * nn + i], b = m->conn[(size_t)e * nn + j];
+                add(a, b);
+                add(b, a);
+            }
+    const int nr = (int)m->c_rhs.size();
+    for (int r = 0; r < nr; ++r)
+        for (int k = m->c_ptr[r]; k < m->c_ptr[r + 1]; ++k)
+            for (int k2 = m->c_ptr[r]; k2 < m->c_ptr[r + 1]; ++k2) {
+                const int a = m->c_dof[k] / m->dpn, b = m->c_dof[k2] / m->dpn;
+                add(a, b);
+                add(b, a);
+            }
+    int min_ct = N, min_nd = 0;
+    for (int i = 0; i < N; ++i)
+        if ((int)conn[i].size() < min_ct) { min_nd = i; min_ct = (int)conn[i].size(); }
+    std::vector<int32_t> ordered(N, -1);
+    std::vector<char> ins(N, 0);
+    ordered[0] = min_nd;
+    int on_len = 1, on_i = 0, nd1 = min_nd, since = 0;
+    ins[min_nd] = 1;
+    while (on_len < N) {
+        size_t it = 0;
+        bool end = false;
+        int nd2 = -1;
+        while (!end && since < block_dim) {
+            if (it < conn[nd1].size()) nd2 = conn[nd1][it++];
+            else end = true;
+            // the reference re-tests the last neighbour when the list ends
+            if (nd2 >= 0 && !ins[nd2]) {
+                ordered[on_len++] = nd2;
+                ins[nd2] = 1;
+                ++since;
+            }
+        }
+        if (on_len < N) {
+            if (since >= block_dim || on_i == on_len - 1) {
+                nd1 = ordered[on_len - 1];
+                double best = 1e100;
+                int best_i = min_nd;
+                const double* p1 = &m->xyz[3 * (size_t)nd1];
+                for (int i = 0; i < N; ++i)
+                    if (!ins[i]) {
+                        const double* p2 = &m->xyz[3 * (size_t)i];
+                        const double dx = p1[0] - p2[0], dy = p1[1] - p2[1], dz = p1[2] - p2[2];
+                        const double d = std::sqrt(dx * dx + dy * dy + dz * dz);
+                        if (d < best) { best = d; best_i = i; }
+                    }
+                min_nd = best_i;
+                ordered[on_len++] = min_nd;
+                nd1 = min_nd;
+                ins[min_nd] = 1;
+                ++since;
+                on_i = on_len - 1;
+                if (since >= block_dim) since = 0;
+            } else {
+                ++on_i;
+                nd1 = ordered[on_i];
+            }
+        }
+    }
+    return ordered;
+}
+
+// block_dim rule: model_prep.rs:888-902 (smallest multiple of 6 whose square
+// reaches the node count); the elastic preconditioner uses 6*block_dim DOFs
+// per block (model_prep.rs:610).
+int default_block_dim(int n_nodes) {
+    int b = 6;
+    while (b * b < n_nodes) b += 6;
+    return b;
+}
+
+struct Precond {
+    int kind = ORC_PC_NONE;
+    std::vector<double> dinv;
+    PermOp P;
+    Skyline S;
+    std::vector<double> tmp_in, tmp_out;
+    void setup(const orc_model* m, int kind_in, int block_dim) {
+        kind = kind_in;
+        const int n = m->n_dof;
+        if (kind == ORC_PC_JACOBI) {
+            std::vector<double> d(n, 0.0);
+            for (int r = 0; r < n; ++r) {
+                const int64_t k = m->K.find(r, r);
+                d[r] = (k >= 0) ? m->K.val[k] : 0.0;
+            }
+            const int nr = (int)m->c_rhs.size();
+            for (int r = 0; r < nr; ++r)
+                for (int k = m->c_ptr[r]; k < m->c_ptr[r + 1]; ++k)
+                    d[m->c_dof[k]] += m->sf * m->c_coef[k] * m->c_coef[k];
+            dinv.resize(n);
+            for (int r = 0; r < n; ++r) dinv[r] = 1.0 / d[r];
+        } else if (kind == ORC_PC_BLOCK_LDL || kind == ORC_PC_DIRECT) {
+            int block_dofs;
+            std::vector<int32_t> order;
+            if (kind == ORC_PC_DIRECT) {
+                block_dofs = 2000000000;  // model_prep.rs:885-887
+                order = reorder_nodes(m, 2000000000);
+            } else {
+                const int bd = block_dim > 0 ? block_dim : default_block_dim(m->n_nodes);
+                block_dofs = 6 * bd;
+                order = reorder_nodes(m, bd);
+            }
+            P.old_of_new.resize(n);
+            P.new_of_old.resize(n);
+            for (int i = 0; i < m->n_nodes; ++i)
+                for (int c = 0; c < m->dpn; ++c) {
+                    const int o = order[i] * m->dpn + c, nw = i * m->dpn + c;
+                    P.old_of_new[nw] = o;
+                    P.new_of_old[o] = nw;
+                }
+            skyline_build(m, P, block_dofs, S);
+            skyline_factor(S);
+            tmp_in.resize(n);
+            tmp_out.resize(n);
+        }
+    }
+    void apply(const double* g, double* w) {
+        const int n = (int)(kind == ORC_PC_JACOBI ? dinv.size() : tmp_in.size());
+        if (kind == ORC_PC_JACOBI) {
+            for (int i = 0; i < n; ++i) w[i] = dinv[i] * g[i];
+        } else if (kind == ORC_PC_BLOCK_LDL || kind == ORC_PC_DIRECT) {
+            for (int i = 0; i < n; ++i) tmp_in[i] = g[P.old_of_new[i]];
+            skyline_solve(S, tmp_out.data(), tmp_in.data());
+            for (int i = 0; i < n; ++i) w[P.old_of_new[i]] = tmp_out[i];
+        }
+    }
+};
+
+
+double true_rel_residual(const orc_model* m, const double* f, const double* u) {
+    const int n = m->n_dof;
+    std::vector<double> y(n);
+    apply_A(m, u, y.data());
+    double rr = 0.0, ff = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double r = f[i] - y[i];
+        rr += r * r;
+        ff += f[i] * f[i];
+    }
+    return ff > 0.0 ? std::sqrt(rr / ff) : std::sqrt(rr);
+}
+
+// PCG: matrix_functions.rs:285-362 (conj_grad_sparse).  x0 = 0, g = A x - b,
+// stop when g^T M^-1 g <= conv_tol (reference rule) or, with the relative
+// rule, when ||g||_2 <= tol ||b||_2.
+int pcg(orc_model* m, Precond& pc, const double* rhs, double* soln, int stop_rule, double tol,
+        int max_it, orc_stats* st) {
+    const int n = m->n_dof;
+    std::vector<double> h(n), g(n), z(n), w(n);
+    double bb = 0.0;
+    for (int i = 0; i < n; ++i) {
+        soln[i] = 0.0;
+        g[i] = -rhs[i];
+        bb += rhs[i] * rhs[i];
+    }
+    const double stop_gg = tol * tol * bb;
+    if (pc.kind == ORC_PC_NONE) std::copy(g.begin(), g.end(), w.begin());
+    else pc.apply(g.data(), w.data());
+    double res = 0.0, gg = 0.0;
+    for (int i = 0; i < n; ++i) {
+        h[i] = -w[i];
+        res += g[i] * w[i];
+        gg += g[i] * g[i];
+    }
+    auto keep_going = [&]() {
+        return stop_rule == ORC_STOP_REFERENCE ? (res > tol) : (gg > stop_gg);
+    };
+    int it = 0, status = 0;
+    while (it < max_it && keep_going()) {
+        apply_A(m, h.data(), z.data());
+        double dp = 0.0;
+        for (int i = 0; i < n; ++i) dp += h[i] * z[i];
+        const double alpha = res / dp;
+        for (int i = 0; i < n; ++i) {
+            soln[i] += alpha * h[i];
+            g[i] += alpha * z[i];
+        }
+        if (pc.kind == ORC_PC_NONE) std::copy(g.begin(), g.end(), w.begin());
+        else pc.apply(g.data(), w.data());
+        double rn = 0.0;
+        gg = 0.0;
+        for (int i = 0; i < n; ++i) {
+            rn += g[i] * w[i];
+            gg += g[i] * g[i];
+        }
+        const double beta = rn / res;
+        for (int i = 0; i < n; ++i) h[i] = -w[i] + beta * h[i];
+        res = rn;
+        ++it;
+        if (!std::isfinite(res)) { status = 2; break; }
+    }
+    if (status == 0 && keep_going()) status = 1;
+    if (st) {
+        st->iterations += it;
+        st->status = status;
+        st->final_res = res;
+    }
+    return status;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C API
+// ---------------------------------------------------------------------------
+extern "C" {
+
+orc_model* orc_create(int32_t elem_type, int32_t n_nodes, const double* coords, int32_t n_elems,
+                      const int32_t* conn, const double* E, const double* nu, const double* rho,
+                      const double* thickness) {
+    if (elem_type != 8 && elem_type != 4) return nullptr;
+    auto* m = new orc_model();
+    m->ti = type_info(elem_type);
+    m->n_nodes = n_nodes;
+    m->n_el = n_elems;
+    m->dpn = m->ti.dpn;
+    m->n_dof = n_nodes * m->dpn;
+    m->xyz.assign(coords, coords + (size_t)3 * n_nodes);
+    m->conn.assign(conn, conn + (size_t)n_elems * m->ti.nn);
+    m->E.assign(E, E + n_elems);
+    m->nu.assign(nu, nu + n_elems);
+    if (rho) m->rho.assign(rho, rho + n_elems);
+    else m->rho.assign(n_elems, 0.0);
+    if (thickness) m->thk.assign(thickness, thickness + n_elems);
+    m->c_ptr.assign(1, 0);
+    return m;
+}
+
+void orc_destroy(orc_model* m) { delete m; }
+int32_t orc_dof_per_node(const orc_model* m) { return m->dpn; }
+int32_t orc_n_dof(const orc_model* m) { return m->n_dof; }
+
+int orc_set_constraints(orc_model* m, int32_t n_rows, const int32_t* row_ptr, const int32_t* dof,
+                        const double* coef, const double* rhs) {
+    m->c_ptr.assign(row_ptr, row_ptr + n_rows + 1);
+    const int nt = row_ptr[n_rows];
+    for (int k = 0; k < nt; ++k)
+        if (dof[k] < 0 || dof[k] >= m->n_dof) return -1;
+    m->c_dof.assign(dof, dof + nt);
+    m->c_coef.assign(coef, coef + nt);
+    m->c_rhs.assign(rhs, rhs + n_rows);
+    return 0;
+}
+
+// Assembly: model_analysis.rs:179-201 (build_elastic_soln_load with the
+// matrix) -> element_equations.rs:852-1062 (get_ru_dfd0; Newmark mass term
+// c1 = -1/(dt^2 (beta - gamma)) at :977-988) -> add_entry per element DOF pair
+// (:1040-1059).  Penalty scale: model_analysis.rs:255-259 over that matrix.
+int orc_assemble(orc_model* m, int32_t dynamic, double dt, double beta, double gamma) {
+    build_pattern(m, m->K);
+    m->dynamic = dynamic != 0;
+    if (m->dynamic) {
+        m->M = m->K;
+        m->cM = -1.0 / (dt * dt * (beta - gamma));
+    }
+    const int nn = m->ti.nn, tot = 3 * nn;
+    std::vector<double> ke(tot * tot), me(tot * tot);
+    double xyz[24], C[36];
+    std::vector<int32_t> dofs(tot);
+    for (int e = 0; e < m->n_el; ++e) {
+        elem_xyz(m, e, xyz);
+        iso_cmat(m->E[e], m->nu[e], C);
+        solid_ke(m->ti.type, xyz, C, ke.data());
+        if (m->dynamic) {
+            solid_me(m->ti.type, xyz, m->rho[e], me.data());
+            for (int i = 0; i < tot * tot; ++i) ke[i] += m->cM * me[i];
+        }
+        for (int a = 0; a < nn; ++a)
+            for (int c = 0; c < 3; ++c) dofs[3 * a + c] = m->conn[(size_t)e * nn + a] * 3 + c;
+        for (int i = 0; i < tot; ++i)
+            for (int j = 0; j < tot; ++j) {
+                const int64_t k = m->K.find(dofs[i], dofs[j]);
+                m->K.val[k] += ke[i * tot + j];
+                if (m->dynamic) m->M.val[k] += me[i * tot + j];
+            }
+    }
+    m->sf = 100000.0 * m->K.max_abs();
+    m->assembled = true;
+    return 0;
+}
+
+int64_t orc_nnz(const orc_model* m) { return (int64_t)m->K.col.size(); }
+double orc_penalty_scale(const orc_model* m) { return m->sf; }
+
+int orc_get_csr(const orc_model* m, int32_t which, int64_t* row_ptr, int32_t* col, double* val) {
+    if (!m->assembled) return -1;
+    const Csr& A = (which == 1) ? m->M : m->K;
+    if (which == 1 && !m->dynamic) return -2;
+    if (row_ptr) std::copy(A.ptr.begin(), A.ptr.end(), row_ptr);
+    if (col) std::copy(A.col.begin(), A.col.end(), col);
+    if (val) {
+        std::copy(A.val.begin(), A.val.end(), val);
+        if (which == 2) {
+            const int nr = (int)m->c_rhs.size();
+            for (int r = 0; r < nr; ++r)
+                for (int k = m->c_ptr[r]; k < m->c_ptr[r + 1]; ++k)
+                    for (int k2 = m->c_ptr[r]; k2 < m->c_ptr[r + 1]; ++k2) {
+                        const int64_t idx = A.find(m->c_dof[k], m->c_dof[k2]);
+                        if (idx < 0) return -3;
+                        val[idx] += m->sf * m->c_coef[k] * m->c_coef[k2];
+                    }
+        }
+    }
+    return 0;
+}
+
+int orc_element_stiffness(int32_t elem_type, const double* xyz, double E, double nu,
+                          double /*thickness*/, double* ke) {
+    if (elem_type != 8 && elem_type != 4) return -1;
+    double C[36];
+    iso_cmat(E, nu, C);
+    solid_ke(elem_type, xyz, C, ke);
+    return 0;
+}
+
+int orc_element_mass(int32_t elem_type, const double* xyz, double rho, double /*thickness*/,
+                     double* me) {
+    if (elem_type != 8 && elem_type != 4) return -1;
+    solid_me(elem_type, xyz, rho, me);
+    return 0;
+}
+
+// Surface traction: element_equations.rs:1970-2043 (get_app_load_dfd0,
+// surfaceTraction branch).  A face is loaded when it lies on the surface
+// (not shared with another element; model_prep.rs:510-554) and its unit
+// normal (face_meth.rs:174-221) is within norm_tol degrees of norm_dir.  The
+// face load is the unit-density consistent-mass image of the traction applied
+// at the face nodes, restricted to the face nodes and scaled so its magnitude
+// is area*|t|.  Only the last loaded face of an element survives (the
+// reference recomputes the element load per face before accumulating).
+int orc_surface_traction(const orc_model* m, int32_t n_set, const int32_t* elem_set,
+                         const double* norm_dir, double norm_tol_deg, const double* traction,
+                         double* f) {
+    const TypeInfo& t = m->ti;
+    const int nn = t.nn, tot = 3 * nn;
+    // face multiplicity over the whole mesh
+    std::vector<std::array<int32_t, 4>> keys;
+    keys.reserve((size_t)m->n_el * t.nfaces);
+    auto face_key = [&](int e, int fi) {
+        std::array<int32_t, 4> k{-1, -1, -1, -1};
+        for (int q = 0; q < t.face_nn; ++q) k[q] = m->conn[(size_t)e * nn + t.faces[fi][q]];
+        for (int i = 1; i < t.face_nn; ++i)  // insertion sort of the face's node ids
+            for (int j = i; j > 0 && k[j - 1] > k[j]; --j) std::swap(k[j - 1], k[j]);
+        return k;
+    };
+    for (int e = 0; e < m->n_el; ++e)
+        for (int fi = 0; fi < t.nfaces; ++fi) keys.push_back(face_key(e, fi));
+    std::vector<std::array<int32_t, 4>> sorted = keys;
+    std::sort(sorted.begin(), sorted.end());
+    auto count = [&](const std::array<int32_t, 4>& k) {
+        auto r = std::equal_range(sorted.begin(), sorted.end(), k);
+        return (int)(r.second - r.first);
+    };
+    const double cos_tol = std::cos(kPi / 180.0 * norm_tol_deg);
+    std::vector<double> me(tot * tot), el_ld(tot);
+    double xyz[24];
+    for (int s = 0; s < n_set; ++s) {
+        const int e = elem_set[s];
+        elem_xyz(m, e, xyz);
+        bool any = false;
+        for (int fi = 0; fi < t.nfaces; ++fi) {
+            if (count(keys[(size_t)e * t.nfaces + fi]) != 1) continue;
+            const int* ln = t.faces[fi];
+            double v1[3], v2[3], nrm[3];
+            for (int i = 0; i < 3; ++i) {
+                if (t.face_nn == 4) {
+                    v1[i] = xyz[3 * ln[2] + i] - xyz[3 * ln[0] + i];
+                    v2[i] = xyz[3 * ln[3] + i] - xyz[3 * ln[1] + i];
+                } else {
+                    v1[i] = xyz[3 * ln[1] + i] - xyz[3 * ln[0] + i];
+                    v2[i] = xyz[3 * ln[2] + i] - xyz[3 * ln[0] + i];
+                }
+            }
+            nrm[0] = v1[1] * v2[2] - v1[2] * v2[1];
+            nrm[1] = v1[2] * v2[0] - v1[0] * v2[2];
+            nrm[2] = v1[0] * v2[1] - v1[1] * v2[0];
+            double area = std::sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+            for (double& x : nrm) x /= area;
+            area *= 0.5;
+            const double dp = norm_dir[0] * nrm[0] + norm_dir[1] * nrm[1] + norm_dir[2] * nrm[2];
+            if (!(dp > cos_tol)) continue;
+            // acceleration = traction at face nodes, zero elsewhere
+            double acc[24] = {0};
+            for (int q = 0; q < t.face_nn; ++q)
+                for (int i = 0; i < 3; ++i) acc[3 * ln[q] + i] = traction[i];
+            solid_me(t.type, xyz, 1.0, me.data());
+            double tot_f[3] = {0, 0, 0};
+            for (int i = 0; i < tot; ++i) {
+                double a = 0.0;
+                for (int j = 0; j < tot; ++j) a += me[i * tot + j] * acc[j];
+                bool in_face = false;
+                for (int q = 0; q < t.face_nn; ++q) in_face |= (ln[q] == i / 3);
+                el_ld[i] = in_face ? a : 0.0;
+                tot_f[i % 3] += el_ld[i];
+            }
+            double vmag = 0.0, imag = 0.0;
+            for (int i = 0; i < 3; ++i) {
+                vmag += tot_f[i] * tot_f[i];
+                imag += traction[i] * traction[i];
+            }
+            const double scale = area * std::sqrt(imag) / std::sqrt(vmag);
+            for (int i = 0; i < tot; ++i) el_ld[i] *= scale;
+            any = true;
+        }
+        if (any)
+            for (int i = 0; i < tot; ++i) f[m->conn[(size_t)e * nn + i / 3] * 3 + i % 3] += el_ld[i];
+    }
+    return 0;
+}
+
+int orc_apply_operator(const orc_model* m, const double* x, double* y) {
+    if (!m->assembled) return -1;
+    apply_A(m, x, y);
+    return 0;
+}
+
+// Static solve: model_analysis.rs:450-534 (solve_step, elastic linear branch):
+// load = f_app - R(u=0) + penalty load (:467-487), solve, u += du (:503-513).
+int orc_static_solve(orc_model* m, const double* f, double* u, int32_t precond, int32_t stop_rule,
+                     double tol, int32_t max_it, int32_t block_dim, orc_stats* st) {
+    if (!m->assembled) return -1;
+    const int n = m->n_dof;
+    std::vector<double> load(f, f + n), zero(n, 0.0);
+    constraint_load(m, zero.data(), load.data());
+    if (st) std::memset(st, 0, sizeof(*st));
+    auto t0 = std::chrono::steady_clock::now();
+    Precond pc;
+    pc.setup(m, precond, block_dim);
+    int status = 0;
+    if (precond == ORC_PC_DIRECT) {
+        pc.apply(load.data(), u);
+    } else {
+        if (precond == ORC_PC_BLOCK_LDL && !skyline_pos_def(pc.S) && st) st->status = 3;
+        status = pcg(m, pc, load.data(), u, stop_rule, tol, max_it > 0 ? max_it : n, st);
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    if (st) {
+        st->seconds = std::chrono::duration<double>(t1 - t0).count();
+        st->rel_residual = true_rel_residual(m, load.data(), u);
+    }
+    return status;
+}
+
+// Static adjoint: model_analysis.rs:1065-1126 (solve_for_adjoint: same
+// operator and solver for lambda = A^-1 dL/du) and :1632-1704 with
+// d_relasticd_d :1379-1457; for a modulus DV on element e the only nonzero
+// dR/dD is the element's internal force, so dL/dE_e = -lambda_e^T dK_e/dE_e u_e
+// (isotropic at fixed nu: dK_e/dE_e = K_e / E_e).
+int orc_adjoint_modulus_gradient(orc_model* m, const double* u, const double* dLdu,
+                                 const double* lambda_in, double* lambda_out, double* gE,
+                                 int32_t precond, int32_t stop_rule, double tol, int32_t max_it,
+                                 orc_stats* st) {
+    if (!m->assembled) return -1;
+    const int n = m->n_dof;
+    std::vector<double> lam(n, 0.0);
+    int status = 0;
+    if (st) std::memset(st, 0, sizeof(*st));
+    if (dLdu) {
+        Precond pc;
+        pc.setup(m, precond, 0);
+        if (precond == ORC_PC_DIRECT) pc.apply(dLdu, lam.data());
+        else status = pcg(m, pc, dLdu, lam.data(), stop_rule, tol, max_it > 0 ? max_it : n, st);
+        if (st) st->rel_residual = true_rel_residual(m, dLdu, lam.data());
+    } else if (lambda_in) {
+        std::copy(lambda_in, lambda_in + n, lam.begin());
+    } else {
+        return -2;
+    }
+    if (lambda_out) std::copy(lam.begin(), lam.end(), lambda_out);
+    const int nn = m->ti.nn, tot = 3 * nn;
+    std::vector<double> ke(tot * tot);
+    double xyz[24], C[36];
+    for (int e = 0; e < m->n_el; ++e) {
+        elem_xyz(m, e, xyz);
+        iso_cmat(m->E[e], m->nu[e], C);
+        solid_ke(m->ti.type, xyz, C, ke.data());
+        double acc = 0.0;
+        for (int i = 0; i < tot; ++i) {
+            const int gi = m->conn[(size_t)e * nn + i / 3] * 3 + i % 3;
+            double ki = 0.0;
+            for (int j = 0; j < tot; ++j) ki += ke[i * tot + j] * u[m->conn[(size_t)e * nn + j / 3] * 3 + j % 3];
+            acc += lam[gi] * ki;
+        }
+        gE[e] = -acc / m->E[e];
+    }
+    return status;
+}
+
+// Orthotropic "modulus" DV component k (element_properties.rs:700-711 adds the
+// DV to E_k; dC/dE_k = -C (dS/dE_k) C by differentiating the compliance
+// inverse of :724-760).
+int orc_adjoint_modulus_component_gradient(orc_model* m, const double* u, const double* lambda,
+                                           int32_t component, double* gD) {
+    if (component < 1 || component > 3) return -1;
+    const int k = component - 1;
+    const TypeInfo& t = m->ti;
+    const int nn = t.nn, tot = 3 * nn;
+    double xyz[24], C[36], dS[36], tmp[36], dC[36], n[8], dndx[24], B[6 * 24];
+    for (int e = 0; e < m->n_el; ++e) {
+        elem_xyz(m, e, xyz);
+        const double E = m->E[e], nu = m->nu[e];
+        iso_cmat(E, nu, C);
+        std::fill(dS, dS + 36, 0.0);
+        // compliance entries depending on E_k: S[k][k] = 1/E_k; S[k][j] = -nu/E_k
+        dS[7 * k] = -1.0 / (E * E);
+        const int pair[3][2] = {{1, 2}, {0, 2}, {0, 1}};
+        (void)pair;
+        if (k == 0) { dS[1] = dS[6] = nu / (E * E); dS[2] = dS[12] = nu / (E * E); }
+        if (k == 1) { dS[8] = dS[13] = nu / (E * E); }
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                double a = 0.0;
+                for (int l = 0; l < 6; ++l) a += dS[6 * i + l] * C[6 * l + j];
+                tmp[6 * i + j] = a;
+            }
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                double a = 0.0;
+                for (int l = 0; l < 6; ++l) a += C[6 * i + l] * tmp[6 * l + j];
+                dC[6 * i + j] = -a;
+            }
+        double acc = 0.0;
+        for (int p = 0; p < t.nip; ++p) {
+            const double det = ip_data(t.type, nn, xyz, t.ip + 3 * p, n, dndx);
+            solid_bmat(nn, dndx, B);
+            double eu[6] = {0}, el[6] = {0};
+            for (int q = 0; q < 6; ++q)
+                for (int c = 0; c < tot; ++c) {
+                    const int gdof = m->conn[(size_t)e * nn + c / 3] * 3 + c % 3;
+                    eu[q] += B[q * tot + c] * u[gdof];
+                    el[q] += B[q * tot + c] * lambda[gdof];
+                }
+            for (int i = 0; i < 6; ++i)
+                for (int j = 0; j < 6; ++j) acc += el[i] * dC[6 * i + j] * eu[j] * det * t.wt[p];
+        }
+        gD[e] = -acc;
+    }
+    return 0;
+}
+
+// Newmark transient: model_analysis.rs:591-624 (solve, dynamic loop) with
+// solve_step :450-534 and node_meth.rs:127-138 (update_vel_acc),
+// :158-165 (advance_disp).  a = c1 (u_prev - u + dt v_prev + c2 a_prev),
+// c1 = 1/(dt^2 (beta - gamma)), c2 = dt^2 (0.5 + beta - gamma);
+// v = v_prev + dt ((1 - gamma) a_prev + gamma a).
+int orc_newmark_run(orc_model* m, int32_t n_steps, double dt, double beta, double gamma,
+                    const double* f_shape, const double* amp, int32_t probe_dof,
+                    double* probe_hist, int32_t precond, int32_t stop_rule, double tol,
+                    int32_t max_it, double* u_final, int32_t* total_iters) {
+    if (!m->assembled || !m->dynamic) return -1;
+    const int n = m->n_dof;
+    std::vector<double> u(n, 0.0), v(n, 0.0), a(n, 0.0), up(n, 0.0), vp(n, 0.0), ap(n, 0.0);
+    std::vector<double> load(n), du(n), tmp(n), ku(n);
+    const double c1 = 1.0 / (dt * dt * (beta - gamma));
+    const double c2 = dt * dt * (0.5 + beta - gamma);
+    auto update_vel_acc = [&]() {
+        for (int i = 0; i < n; ++i) {
+            a[i] = c1 * (up[i] - u[i] + dt * vp[i] + c2 * ap[i]);
+            v[i] = vp[i] + dt * ((1.0 - gamma) * ap[i] + gamma * a[i]);
+        }
+    };
+    update_vel_acc();  // prep_matrix_factorizations, model_prep.rs:584-590
+    Precond pc;
+    pc.setup(m, precond, 0);
+    orc_stats st{};
+    int status = 0;
+    for (int s = 0; s < n_steps; ++s) {
+        // residual R = K u + M a (K here is K + cM*M, so subtract cM*M u)
+        std::fill(ku.begin(), ku.end(), 0.0);
+        m->K.matvec(u.data(), ku.data());
+        for (int i = 0; i < n; ++i) tmp[i] = a[i] - m->cM * u[i];
+        m->M.matvec(tmp.data(), ku.data());
+        for (int i = 0; i < n; ++i) load[i] = amp[s] * f_shape[i] - ku[i];
+        constraint_load(m, u.data(), load.data());
+        if (precond == ORC_PC_DIRECT) {
+            pc.apply(load.data(), du.data());
+        } else {
+            const int rc = pcg(m, pc, load.data(), du.data(), stop_rule, tol, max_it > 0 ? max_it : n, &st);
+            if (rc == 2) { status = 2; break; }
+            if (rc == 1) status = 1;
+        }
+        for (int i = 0; i < n; ++i) u[i] += du[i];
+        update_vel_acc();
+        if (probe_hist) probe_hist[s] = u[probe_dof];
+        up = u; vp = v; ap = a;
+        update_vel_acc();
+    }
+    if (u_final) std::copy(u.begin(), u.end(), u_final);
+    if (total_iters) *total_iters = st.iterations;
+    return status;
+}
+
+int orc_reorder_nodes(const orc_model* m, int32_t block_dim, int32_t* order_out) {
+    const auto o = reorder_nodes(m, block_dim > 0 ? block_dim : default_block_dim(m->n_nodes));
+    std::copy(o.begin(), o.end(), order_out);
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,113 @@
+/*
+ * asend_oracle.h -- FP64 CPU oracle for the ASenD3D linear-elastic solve path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: the parity tests,
+ * the smoke test and bench.py's CPU-baseline leg may call it; the product
+ * (libasend_gpu.so) never links or calls it.
+ *
+ * It restates, in plain single-threaded C++ and FP64 (as the reference runs),
+ * the reference's CPU algorithms for:
+ *   - element integration (hex8 type 8, tet4 type 4, shell4 type 41),
+ *   - row-list sparse assembly, penalty constraints,
+ *   - the block-LDL^T preconditioned CG and the direct skyline LDL^T,
+ *   - the spatial node reordering that defines the preconditioner blocks,
+ *   - the static adjoint gradient, and the Newmark time loop.
+ * Each function in asend_oracle.cpp cites the reference file:line it follows
+ * (paths relative to solverSrc/asend_run_job/src/ of MSDOToolz/ASenD3D).
+ *
+ * Parity pinning: the reference ships no recorded solver outputs and its Rust
+ * toolchain is absent, so the oracle is pinned by the reference's analytic
+ * known answers (the notes.txt files under examples/testCases) and by central
+ * finite differences and self-consistency (tests/golden holds the fixtures).
+ */
+#ifndef ASEND_ORACLE_H
+#define ASEND_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_model orc_model;
+
+typedef struct orc_stats {
+    int32_t iterations;     /* CG iterations (summed over restarts)            */
+    int32_t status;         /* 0 converged, 1 max-iter, 2 non-finite           */
+    double  final_res;      /* reference stopping quantity g^T M^-1 g at exit  */
+    double  rel_residual;   /* ||f - K u||_2 / ||f||_2 with the FP64 operator  */
+    double  seconds;        /* wall time of the solve only                     */
+} orc_stats;
+
+/* preconditioners */
+enum { ORC_PC_NONE = 0, ORC_PC_JACOBI = 1, ORC_PC_BLOCK_LDL = 2, ORC_PC_DIRECT = 3 };
+/* stopping rules */
+enum { ORC_STOP_REFERENCE = 0, ORC_STOP_RELATIVE = 1 };
+
+/* Mesh of one element type (8 hex8, 4 tet4, 41 shell4).  coords[n_nodes*3],
+ * conn[n_elems*nodes_per_elem] (0-based), per-element isotropic E, nu, rho.
+ * For shell4, thickness[n_elems] gives the section thickness (else NULL). */
+orc_model* orc_create(int32_t elem_type, int32_t n_nodes, const double* coords,
+                      int32_t n_elems, const int32_t* conn, const double* E,
+                      const double* nu, const double* rho, const double* thickness);
+void orc_destroy(orc_model* m);
+int32_t orc_dof_per_node(const orc_model* m);
+int32_t orc_n_dof(const orc_model* m);
+
+/* Linear constraint rows C u = q in natural DOF numbering (node*dpn + comp). */
+int orc_set_constraints(orc_model* m, int32_t n_rows, const int32_t* row_ptr,
+                        const int32_t* dof, const double* coef, const double* rhs);
+
+/* Assemble K (and M when dynamic != 0) in natural numbering, element order.
+ * Sets the penalty scale sf = 1e5 * max|K_ij|. */
+int orc_assemble(orc_model* m, int32_t dynamic, double dt, double beta, double gamma);
+int64_t orc_nnz(const orc_model* m);
+/* which: 0 = K, 1 = M, 2 = operator (K [+ c_M M] + sf C^T C) */
+int orc_get_csr(const orc_model* m, int32_t which, int64_t* row_ptr, int32_t* col, double* val);
+double orc_penalty_scale(const orc_model* m);
+
+/* Single element stiffness (natural element DOF order node*dpn+comp). */
+int orc_element_stiffness(int32_t elem_type, const double* xyz, double E, double nu,
+                          double thickness, double* ke);
+int orc_element_mass(int32_t elem_type, const double* xyz, double rho, double thickness,
+                     double* me);
+
+/* Load builders (reference load types). */
+int orc_surface_traction(const orc_model* m, int32_t n_set, const int32_t* elem_set,
+                         const double* norm_dir, double norm_tol_deg, const double* traction,
+                         double* f);
+
+/* Static linear solve: (K + sf C^T C) u = f + sf C^T q, x0 = 0. */
+int orc_static_solve(orc_model* m, const double* f, double* u, int32_t precond,
+                     int32_t stop_rule, double tol, int32_t max_it, int32_t block_dim,
+                     orc_stats* st);
+
+/* Apply the solve operator (natural numbering): y = A x. */
+int orc_apply_operator(const orc_model* m, const double* x, double* y);
+
+/* Static adjoint: lambda = A^-1 dLdu, then per-element isotropic-modulus
+ * sensitivity gE[e] = -lambda_e^T (dK_e/dE_e) u_e.  lambda may be supplied
+ * (self-adjoint objectives) by passing dLdu == NULL and lambda_in != NULL. */
+int orc_adjoint_modulus_gradient(orc_model* m, const double* u, const double* dLdu,
+                                 const double* lambda_in, double* lambda_out, double* gE,
+                                 int32_t precond, int32_t stop_rule, double tol,
+                                 int32_t max_it, orc_stats* st);
+
+/* Reference-style orthotropic "modulus" DV (component 1..3) on every element
+ * of the mesh, one DV per element: gD[e] = -lambda_e^T dK_e/dE_k u_e. */
+int orc_adjoint_modulus_component_gradient(orc_model* m, const double* u, const double* lambda,
+                                           int32_t component, double* gD);
+
+/* Newmark (reference convention) linear transient run.  The load at step i
+ * (time = i*dt) is amp[i] * f_shape.  Records u[probe_dof] after each step.
+ * Initial u, v, a are zero.  orc_assemble(m, 1, dt, beta, gamma) first. */
+int orc_newmark_run(orc_model* m, int32_t n_steps, double dt, double beta, double gamma,
+                    const double* f_shape, const double* amp, int32_t probe_dof,
+                    double* probe_hist, int32_t precond, int32_t stop_rule, double tol,
+                    int32_t max_it, double* u_final, int32_t* total_iters);
+
+/* Reference node reordering (spatial BFS blocks); perm[new] = old node. */
+int orc_reorder_nodes(const orc_model* m, int32_t block_dim, int32_t* order_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

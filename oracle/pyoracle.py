@@ -1,0 +1,222 @@
+"""ctypes front end of the FP64 CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module, as the checker.  It takes the same ``Problem`` description as the
+GPU solver and restates, in Python, the reference's constraint-row building
+(const_meth.rs:30-90) and nodal-force load building (model_analysis.rs:37-46);
+the numerics live in ``liboracle.so`` (asend_oracle.cpp).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+
+PC_NONE, PC_JACOBI, PC_BLOCK_LDL, PC_DIRECT = 0, 1, 2, 3
+STOP_REFERENCE, STOP_RELATIVE = 0, 1
+
+P_d = C.POINTER(C.c_double)
+P_i = C.POINTER(C.c_int32)
+P_l = C.POINTER(C.c_int64)
+
+
+class Stats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("status", C.c_int32), ("final_res", C.c_double),
+                ("rel_residual", C.c_double), ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            from oracle import build as _b
+            _b.build()
+        lib = C.CDLL(str(LIB))
+        sig = {
+            "orc_create": (C.c_void_p, [C.c_int32, C.c_int32, P_d, C.c_int32, P_i, P_d, P_d, P_d, P_d]),
+            "orc_destroy": (None, [C.c_void_p]),
+            "orc_n_dof": (C.c_int32, [C.c_void_p]),
+            "orc_set_constraints": (C.c_int, [C.c_void_p, C.c_int32, P_i, P_i, P_d, P_d]),
+            "orc_assemble": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double]),
+            "orc_nnz": (C.c_int64, [C.c_void_p]),
+            "orc_get_csr": (C.c_int, [C.c_void_p, C.c_int32, P_l, P_i, P_d]),
+            "orc_penalty_scale": (C.c_double, [C.c_void_p]),
+            "orc_element_stiffness": (C.c_int, [C.c_int32, P_d, C.c_double, C.c_double, C.c_double, P_d]),
+            "orc_element_mass": (C.c_int, [C.c_int32, P_d, C.c_double, C.c_double, P_d]),
+            "orc_surface_traction": (C.c_int, [C.c_void_p, C.c_int32, P_i, P_d, C.c_double, P_d, P_d]),
+            "orc_static_solve": (C.c_int, [C.c_void_p, P_d, P_d, C.c_int32, C.c_int32, C.c_double, C.c_int32,
+                                           C.c_int32, C.POINTER(Stats)]),
+            "orc_apply_operator": (C.c_int, [C.c_void_p, P_d, P_d]),
+            "orc_adjoint_modulus_gradient": (C.c_int, [C.c_void_p, P_d, P_d, P_d, P_d, P_d, C.c_int32, C.c_int32,
+                                                       C.c_double, C.c_int32, C.POINTER(Stats)]),
+            "orc_adjoint_modulus_component_gradient": (C.c_int, [C.c_void_p, P_d, P_d, C.c_int32, P_d]),
+            "orc_newmark_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double, P_d, P_d,
+                                          C.c_int32, P_d, C.c_int32, C.c_int32, C.c_double, C.c_int32, P_d, P_i]),
+            "orc_reorder_nodes": (C.c_int, [C.c_void_p, C.c_int32, P_i]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _p(a, t=C.c_double):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def constraint_rows(problem, dpn=3):
+    """Constraint::build_mat (const_meth.rs:30-90): rows = largest term-set
+    size; a one-node term contributes to every row, an n-node term its k-th
+    node to row k."""
+    ptr, dof, coef, rhs = [0], [], [], []
+    for terms, q in problem.constraints:
+        rows = max(len(problem.node_sets[t[0]]) for t in terms)
+        for r in range(rows):
+            for set_name, comp, cf in terms:
+                s = problem.node_sets[set_name]
+                nd = s[0] if len(s) == 1 else s[r]
+                dof.append(int(nd) * dpn + comp - 1)
+                coef.append(cf)
+            ptr.append(len(dof))
+            rhs.append(q)
+    return (np.array(ptr, np.int32), np.array(dof, np.int32), np.array(coef, np.float64), np.array(rhs, np.float64))
+
+
+class Oracle:
+    def __init__(self, problem, dynamic=False, dt=0.0, beta=0.25, gamma=0.5):
+        self.lib = load()
+        self.p = problem
+        m = problem.mesh
+        self._coords = np.ascontiguousarray(m.coords, np.float64)
+        self._conn = np.ascontiguousarray(m.conn, np.int32)
+        self._E = np.ascontiguousarray(problem.E, np.float64)
+        self._nu = np.ascontiguousarray(np.broadcast_to(problem.nu, self._E.shape), np.float64)
+        rho = problem.rho if problem.rho is not None else np.zeros_like(self._E)
+        self._rho = np.ascontiguousarray(np.broadcast_to(rho, self._E.shape), np.float64)
+        self.m = self.lib.orc_create(m.elem_type, m.n_nodes, _p(self._coords), m.n_elems, _p(self._conn, C.c_int32),
+                                     _p(self._E), _p(self._nu), _p(self._rho), None)
+        if not self.m:
+            raise RuntimeError("orc_create failed")
+        self.n_dof = self.lib.orc_n_dof(self.m)
+        ptr, dof, coef, rhs = constraint_rows(problem)
+        self._c = (ptr, dof, coef, rhs)
+        if len(rhs):
+            rc = self.lib.orc_set_constraints(self.m, len(rhs), _p(ptr, C.c_int32), _p(dof, C.c_int32), _p(coef),
+                                              _p(rhs))
+            assert rc == 0
+        self.lib.orc_assemble(self.m, int(dynamic), dt, beta, gamma)
+        self.sf = self.lib.orc_penalty_scale(self.m)
+
+    def __del__(self):
+        try:
+            if self.m:
+                self.lib.orc_destroy(self.m)
+        except Exception:
+            pass
+
+    def loads(self):
+        """Load cases in natural numbering (without the penalty rhs)."""
+        out = []
+        for items in self.p.loads:
+            f = np.zeros(self.n_dof)
+            for it in items:
+                if it[0] == "nodalForce":
+                    for nd in self.p.node_sets[it[1]]:
+                        f[3 * nd:3 * nd + 3] += it[2][:3]
+                elif it[0] == "surfaceTraction":
+                    els = np.ascontiguousarray(self.p.elem_sets[it[1]], np.int32)
+                    nd = np.ascontiguousarray(it[2], np.float64)
+                    t = np.ascontiguousarray(it[4], np.float64)
+                    self.lib.orc_surface_traction(self.m, len(els), _p(els, C.c_int32), _p(nd), it[3], _p(t), _p(f))
+                else:
+                    f += it[1]
+            out.append(f)
+        return out
+
+    def penalty_rhs(self):
+        ptr, dof, coef, rhs = self._c
+        b = np.zeros(self.n_dof)
+        for r in range(len(rhs)):
+            for k in range(ptr[r], ptr[r + 1]):
+                b[dof[k]] += coef[k] * self.sf * rhs[r]
+        return b
+
+    def csr(self, which=0):
+        nnz = self.lib.orc_nnz(self.m)
+        rp = np.zeros(self.n_dof + 1, np.int64)
+        col = np.zeros(nnz, np.int32)
+        val = np.zeros(nnz)
+        rc = self.lib.orc_get_csr(self.m, which, _p(rp, C.c_int64), _p(col, C.c_int32), _p(val))
+        assert rc == 0, rc
+        return rp, col, val
+
+    def apply(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        self.lib.orc_apply_operator(self.m, _p(x), _p(y))
+        return y
+
+    def solve(self, f, precond=PC_JACOBI, stop=STOP_RELATIVE, tol=1e-8, max_it=0, block_dim=0):
+        f = np.ascontiguousarray(f, np.float64)
+        u = np.zeros(self.n_dof)
+        st = Stats()
+        rc = self.lib.orc_static_solve(self.m, _p(f), _p(u), precond, stop, tol, max_it, block_dim, C.byref(st))
+        return u, rc, st.as_dict()
+
+    def adjoint(self, u, dLdu=None, lam=None, precond=PC_JACOBI, stop=STOP_RELATIVE, tol=1e-10, max_it=0):
+        u = np.ascontiguousarray(u, np.float64)
+        g = np.zeros(self.p.mesh.n_elems)
+        lam_out = np.zeros(self.n_dof)
+        st = Stats()
+        d = None if dLdu is None else np.ascontiguousarray(dLdu, np.float64)
+        li = None if lam is None else np.ascontiguousarray(lam, np.float64)
+        rc = self.lib.orc_adjoint_modulus_gradient(self.m, _p(u), None if d is None else _p(d),
+                                                   None if li is None else _p(li), _p(lam_out), _p(g), precond, stop,
+                                                   tol, max_it, C.byref(st))
+        return g, lam_out, rc, st.as_dict()
+
+    def component_gradient(self, u, lam, component):
+        g = np.zeros(self.p.mesh.n_elems)
+        u = np.ascontiguousarray(u, np.float64)
+        lam = np.ascontiguousarray(lam, np.float64)
+        rc = self.lib.orc_adjoint_modulus_component_gradient(self.m, _p(u), _p(lam), component, _p(g))
+        assert rc == 0
+        return g
+
+    def newmark(self, n_steps, dt, beta, gamma, f_shape, amp, probe_dof, precond=PC_JACOBI, stop=STOP_RELATIVE,
+                tol=1e-10, max_it=0):
+        f_shape = np.ascontiguousarray(f_shape, np.float64)
+        amp = np.ascontiguousarray(amp, np.float64)
+        hist = np.zeros(n_steps)
+        u = np.zeros(self.n_dof)
+        its = C.c_int32(0)
+        rc = self.lib.orc_newmark_run(self.m, n_steps, dt, beta, gamma, _p(f_shape), _p(amp), probe_dof, _p(hist),
+                                      precond, stop, tol, max_it, _p(u), C.byref(its))
+        return hist, u, rc, its.value
+
+    def reorder(self, block_dim=0):
+        out = np.zeros(self.p.mesh.n_nodes, np.int32)
+        self.lib.orc_reorder_nodes(self.m, block_dim, _p(out, C.c_int32))
+        return out
+
+
+def element_stiffness(elem_type, xyz, E, nu):
+    lib = load()
+    xyz = np.ascontiguousarray(xyz, np.float64).ravel()
+    n = xyz.size
+    ke = np.zeros(n * n)
+    rc = lib.orc_element_stiffness(elem_type, _p(xyz), E, nu, 0.0, _p(ke))
+    assert rc == 0
+    return ke.reshape(n, n)

@@ -1,0 +1,223 @@
+"""GPU parity tests: the sm_103a library through its C ABI vs the FP64 oracle.
+
+Tolerances (written here, per quantity):
+  * assembly pattern (row pointers, column indices) and element colouring
+    validity: bit-exact;
+  * FP64-assembled operator values: 1e-12 relative to max|K| (closed-form
+    3x3 adjugate vs the reference's Givens-QR inverse differ by rounding);
+  * FP32-assembled values: 2e-6 relative to max|K|;
+  * displacements after a solve to rel. residual tol: 10 * tol * cond-margin
+    (checked as ||u - u_ref|| / ||u_ref|| <= 1e-7 at tol 1e-10);
+  * adjoint gradients: 1e-6 relative (norm-wise), as the benchmark target.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from asend3d_gb300 import _lib, configs
+from asend3d_gb300.mesh import block_hex8, block_tet4
+from asend3d_gb300.solver import AsendError, GpuSolver, Problem
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(np.asarray(b)), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def small(gpu_lib, oracle_lib):
+    p = configs.cantilever_small()
+    g = GpuSolver(p)
+    g.assemble(precision=64)
+    o = oracle_lib.Oracle(p)
+    yield p, g, o
+    g.close()
+
+
+def test_assembly_pattern_bit_exact_and_values(small):
+    p, g, o = small
+    rp, col, val = g.csr(which=2)  # operator without the penalty terms
+    orp, ocol, oval = o.csr(which=0)
+    assert np.array_equal(rp, orp)
+    assert np.array_equal(col, ocol)
+    scale = np.abs(oval).max()
+    assert np.abs(val - oval).max() <= 1e-12 * scale
+
+
+def test_assembly_fp32_values(gpu_lib, oracle_lib):
+    p = configs.cantilever_small()
+    g = GpuSolver(p)
+    g.assemble(precision=32)
+    _, _, val = g.csr(which=2)
+    _, _, oval = oracle_lib.Oracle(p).csr(which=0)
+    assert np.abs(val - oval).max() <= 2e-6 * np.abs(oval).max()
+    g.close()
+
+
+def test_penalty_and_operator(small):
+    p, g, o = small
+    _, _, val = g.csr(which=0)
+    _, _, oval = o.csr(which=2)
+    assert np.abs(val - oval).max() <= 1e-12 * np.abs(oval).max()
+    x = np.random.default_rng(0).standard_normal(o.n_dof)
+    y_ref = o.apply(x)
+    assert rel(g.apply(x, 64), y_ref) < 1e-12
+    assert rel(g.apply(x, 32), y_ref) < 2e-6
+
+
+def test_colouring_valid(small):
+    p, g, o = small
+    colour, n = g.coloring()
+    assert n == 8  # structured hex: 2 x 2 x 2 parity colouring
+    conn = p.mesh.conn
+    for c in range(n):
+        nodes = conn[colour == c].ravel()
+        assert len(np.unique(nodes)) == len(nodes), f"colour {c} has elements sharing a node"
+
+
+@pytest.mark.parametrize("method,pc", [(_lib.METHOD_FP64, _lib.PC_JACOBI), (_lib.METHOD_MIXED, _lib.PC_JACOBI),
+                                       (_lib.METHOD_MIXED, _lib.PC_BLOCK), (_lib.METHOD_FP64, _lib.PC_BLOCK)])
+def test_static_solve_parity(small, method, pc):
+    p, g, o = small
+    gold = np.load(GOLD / "cantilever_small.npz")
+    u, rc, st = g.static_solve(method=method, precond=pc, rel_tol=1e-10)
+    assert rc == 0, st
+    assert st["rel_residual"] <= 1e-10
+    f = o.loads()[0] + o.penalty_rhs()
+    true_res = np.linalg.norm(f - o.apply(u[0])) / np.linalg.norm(f)
+    assert true_res <= 1.01e-10
+    assert rel(u[0], gold["u"]) < 1e-7
+    assert np.allclose(g.load_vector(0), f, rtol=1e-13, atol=0)
+
+
+def test_adjoint_tip_gradient_golden(small):
+    p, g, o = small
+    gold = np.load(GOLD / "cantilever_small.npz")
+    g.static_solve(rel_tol=1e-12)
+    L, dLdE, rc, st = g.adjoint_gradient(rel_tol=1e-12)
+    assert rc == 0
+    assert L == pytest.approx(float(gold["L"]), rel=1e-9)
+    assert rel(dLdE, gold["dLdE"]) < 1e-6
+    dLdD = g.design_var_gradient(dLdE)
+    assert len(dLdD) == 80
+    assert rel(dLdD, gold["dLdD"]) < 1e-6
+
+
+def test_compliance_gradient_lognormal(gpu_lib, oracle_lib):
+    p = configs.block_large(nx=24, ny=6, nz=6, seed=5)
+    g = GpuSolver(p)
+    g.assemble()
+    u, rc, _ = g.static_solve(rel_tol=1e-11)
+    assert rc == 0
+    L, dLdE, rc, _ = g.adjoint_gradient()
+    o = oracle_lib.Oracle(p)
+    f = o.loads()[0] + o.penalty_rhs()
+    ur, _, _ = o.solve(f, precond=oracle_lib.PC_DIRECT)
+    gr, _, _, _ = o.adjoint(ur, lam=ur)
+    assert L == pytest.approx(f @ ur, rel=1e-9)
+    assert rel(dLdE, gr) < 1e-6
+    # homogeneity checksum: sum_e E_e dC/dE_e = -C (penalty held fixed: 1e-4)
+    assert np.dot(p.E, dLdE) == pytest.approx(-L, rel=1e-4)
+    g.close()
+
+
+def test_multi_rhs_batch(gpu_lib, oracle_lib):
+    p = configs.batch_instance(3)
+    g = GpuSolver(p)
+    g.assemble()
+    assert g.n_cases == 4
+    u, rc, st = g.static_solve(rel_tol=1e-10)
+    assert rc == 0 and st["n_rhs"] == 4
+    o = oracle_lib.Oracle(p)
+    for k, fk in enumerate(o.loads()):
+        f = fk + o.penalty_rhs()
+        ur, _, _ = o.solve(f, precond=oracle_lib.PC_DIRECT)
+        assert rel(u[k], ur) < 1e-7
+    g.close()
+
+
+def test_tet4_golden(gpu_lib):
+    gold = np.load(GOLD / "tet_block.npz")
+    m = block_tet4(4, 2, 2, 1.0, 0.5, 0.5)
+    p = Problem(m, np.full(m.n_elems, 7.0e10), np.full(m.n_elems, 0.33), None)
+    p.add_node_set("xMin", m.nodes_in_range(xr=(-1e-9, 1e-9)))
+    p.fix_displacement("xMin")
+    p.add_elem_set("all", np.arange(m.n_elems, dtype=np.int32))
+    p.add_surface_traction("all", (1.0, 0.0, 0.0), (0.0, 0.0, -1.0e6))
+    g = GpuSolver(p)
+    g.assemble()
+    u, rc, _ = g.static_solve(rel_tol=1e-11)
+    assert rc == 0
+    assert rel(u[0], gold["u"]) < 1e-8
+    g.close()
+
+
+def test_newmark_parity(gpu_lib, oracle_lib):
+    p = configs.cantilever_small(nx=10, ny=2, nz=2)
+    dt, beta, gamma = 1e-4, 0.25, 0.5
+    n = 60
+    t = np.arange(n) * dt
+    amp = np.exp(-0.5 * ((t - 2e-3) / 5e-4) ** 2)
+    tip = int(p.node_sets["tip"][0])
+    g = GpuSolver(p)
+    g.assemble(dynamic=True, dt=dt, beta=beta, gamma=gamma)
+    hist, u, rc, st = g.newmark(amp, probe_dof=3 * tip + 2, rel_tol=1e-12)
+    assert rc == 0
+    o = oracle_lib.Oracle(p, dynamic=True, dt=dt, beta=beta, gamma=gamma)
+    href, uref, rc2, _ = o.newmark(n, dt, beta, gamma, o.loads()[0], amp, 3 * tip + 2, precond=oracle_lib.PC_DIRECT)
+    assert rc2 == 0
+    assert rel(hist, href) < 1e-8
+    assert rel(u, uref) < 1e-8
+    g.close()
+
+
+def test_input_errors_are_reported(gpu_lib):
+    m = block_hex8(2, 1, 1, 2.0, 1.0, 1.0)
+    bad = Problem(m, np.array([1e9, -1.0]), np.full(2, 0.3))
+    with pytest.raises(AsendError, match="modulus"):
+        GpuSolver(bad)
+    p = Problem(m, np.full(2, 1e9), np.full(2, 0.3))
+    g = GpuSolver(p)
+    with pytest.raises(AsendError, match="assemble first"):
+        g.static_solve()
+    g.close()
+
+
+def test_zero_and_nonfinite_loads(gpu_lib):
+    p = configs.cantilever_small(nx=4, ny=2, nz=2)
+    p.loads = [[("vector", np.zeros(p.mesh.n_dof))]]
+    g = GpuSolver(p)
+    g.assemble()
+    u, rc, _ = g.static_solve()
+    assert rc == 0 and not np.any(u)
+    f = np.zeros(p.mesh.n_dof)
+    f[5] = np.nan
+    p.loads = [[("vector", f)]]
+    g.set_loads()
+    u, rc, st = g.static_solve()
+    assert rc == _lib.ASEND_NONFINITE
+    g.close()
+
+
+def test_full_size_block_properties(gpu_lib):
+    """Full-size 200x40x40 block (1.01 M DOF): size-independent checks."""
+    p = configs.block_large()
+    g = GpuSolver(p)
+    g.assemble(precision=64)
+    rc, st = g.static_solve_device(method=_lib.METHOD_MIXED, rel_tol=1e-8)
+    assert rc == 0 and st["rel_residual"] <= 1e-8
+    u_mixed = g.solution(0)
+    L, dLdE, rc, _ = g.adjoint_gradient()
+    assert rc == 0 and L > 0
+    assert np.all(dLdE < 0)  # stiffening any element lowers the compliance
+    assert np.dot(p.E, dLdE) == pytest.approx(-L, rel=1e-4)
+    f = g.load_vector(0)
+    res = np.linalg.norm(f - g.apply(u_mixed, 64)) / np.linalg.norm(f)
+    assert res <= 1.05e-8
+    rc, st64 = g.static_solve_device(method=_lib.METHOD_FP64, rel_tol=1e-8)
+    assert rc == 0
+    assert rel(u_mixed, g.solution(0)) < 1e-6
+    g.close()
