@@ -19,7 +19,7 @@ P_dbl = C.POINTER(C.c_double)
 ASEND_OK, ASEND_MAX_ITER, ASEND_NONFINITE, ASEND_FALLBACK = 0, 1, 2, 3
 ASEND_EINVAL, ASEND_ECUDA, ASEND_ESTATE = -1, -2, -3
 METHOD_FP64, METHOD_MIXED = 0, 1
-PC_JACOBI, PC_BLOCK, PC_LEARNED = 0, 1, 2
+PC_JACOBI, PC_BLOCK, PC_LEARNED, PC_MG = 0, 1, 2, 3
 OBJ_DISPLACEMENT, OBJ_COMPLIANCE = 0, 1
 
 
@@ -45,6 +45,8 @@ SIGNATURES = [
     ("asend_version", C.c_char_p, []),
     ("asend_set_mesh", c_int, [C.c_void_p, c_int, c_int, P_dbl, c_int, P_int, P_dbl, P_dbl, P_dbl, P_dbl]),
     ("asend_set_modulus", c_int, [C.c_void_p, P_dbl]),
+    ("asend_set_block_structure", c_int, [C.c_void_p, c_int, c_int, c_int]),
+    ("asend_mg_levels", c_int, [C.c_void_p]),
     ("asend_add_node_set", c_int, [C.c_void_p, c_int, P_int]),
     ("asend_add_element_set", c_int, [C.c_void_p, c_int, P_int]),
     ("asend_add_constraint", c_int, [C.c_void_p, c_int, P_int, P_int, P_dbl, c_dbl]),

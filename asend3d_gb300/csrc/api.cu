@@ -155,6 +155,7 @@ void ensure_case(Ctx& c, int rhs) {
     require(rhs >= 0 && rhs < 4096, "load case index out of range");
     require(c.n_dof > 0, "set the mesh before adding loads");
     while ((int)c.loads.size() <= rhs) c.loads.emplace_back(c.n_dof, 0.0);
+    ++c.loads_version;  // every caller modifies the load case next
 }
 
 }  // namespace
@@ -273,8 +274,14 @@ void build_pattern(Ctx& c) {
 // Load vectors incl. the penalty right-hand side -sf C^T (C*0 - q) = sf C^T q
 // (const_meth.rs:105-119 at u = 0) to the device.
 void upload_rhs(Ctx& c) {
-    const int nr = std::max<int>(1, (int)c.loads.size());
-    if (c.loads.empty()) c.loads.emplace_back(c.n_dof, 0.0);
+    if (c.loads.empty()) {
+        c.loads.emplace_back(c.n_dof, 0.0);
+        ++c.loads_version;
+    }
+    const int nr = (int)c.loads.size();
+    if (c.rhs_version == c.loads_version && c.rhs_sf == c.sf && c.d_f.n == (size_t)nr * c.n_dof) return;
+    c.rhs_version = c.loads_version;
+    c.rhs_sf = c.sf;
     std::vector<double> f((size_t)nr * c.n_dof);
     for (int r = 0; r < nr; ++r) {
         double* fr = &f[(size_t)r * c.n_dof];
@@ -377,10 +384,13 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         c.c_coef.clear();
         c.c_rhs.clear();
         c.loads.clear();
+        ++c.loads_version;
         c.dv_ptr.assign(1, 0);
         c.dv_el.clear();
         c.dv_coef.clear();
         c.pattern_ready = c.assembled = c.solved = false;
+        c.bx = c.by = c.bz = 0;
+        c.mg.reset();
         c.d_xyz.upload(c.xyz, c.stream);
         c.d_conn.upload(c.conn, c.stream);
         c.d_E.upload(c.E, c.stream);
@@ -389,6 +399,38 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         ASEND_CUDA(cudaStreamSynchronize(c.stream));
         return ASEND_OK;
     });
+}
+
+// Declares the mesh to be the structured block produced by the reference's
+// swept hex meshing: node (i,j,k) = (i*(ny+1)+j)*(nz+1)+k, element (i,j,k) =
+// (i*ny+j)*nz+k with corners in the hex8 order.  Enables ASEND_PC_MG.
+int asend_set_block_structure(asend_ctx* ctx, int32_t nx, int32_t ny, int32_t nz) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.type == 8, "block structure needs a hex8 mesh");
+        require(nx > 0 && ny > 0 && nz > 0 && (int64_t)nx * ny * nz == c.n_el &&
+                    (int64_t)(nx + 1) * (ny + 1) * (nz + 1) == c.n_nodes,
+                "block dimensions do not match the mesh");
+        const int co[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+        for (int i = 0; i < nx; ++i)
+            for (int j = 0; j < ny; ++j)
+                for (int k = 0; k < nz; ++k) {
+                    const size_t e = ((size_t)i * ny + j) * nz + k;
+                    for (int a = 0; a < 8; ++a) {
+                        const int expect = ((i + co[a][0]) * (ny + 1) + (j + co[a][1])) * (nz + 1) + (k + co[a][2]);
+                        require(c.conn[e * 8 + a] == expect, "connectivity does not follow the block numbering");
+                    }
+                }
+        c.bx = nx;
+        c.by = ny;
+        c.bz = nz;
+        c.mg.reset();
+        return ASEND_OK;
+    });
+}
+
+int asend_mg_levels(const asend_ctx* ctx) {
+    const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
+    return c ? mg_levels(*c) : ASEND_EINVAL;
 }
 
 int asend_set_modulus(asend_ctx* ctx, const double* E) {
@@ -448,6 +490,8 @@ int asend_add_constraint(asend_ctx* ctx, int32_t n_terms, const int32_t* node_se
             c.c_ptr.push_back((int32_t)c.c_dof.size());
             c.c_rhs.push_back(rhs);
         }
+        ++c.loads_version;  // the penalty right-hand side changes with the rows
+        c.mg.reset();
         c.pattern_ready = c.assembled = c.solved = false;
         return ASEND_OK;
     });
@@ -539,6 +583,7 @@ int asend_add_load_vector(asend_ctx* ctx, int32_t rhs, const double* f) {
 int asend_clear_loads(asend_ctx* ctx) {
     return guarded(ctx, [&](Ctx& c) {
         c.loads.clear();
+        ++c.loads_version;
         c.solved = false;
         return ASEND_OK;
     });

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -92,8 +93,14 @@ struct PcgScalars {
     uint32_t ticket_a, ticket_b, ticket_c, pad;
 };
 
+struct MgHierarchy;
+
 struct Ctx {
     int device = 0;
+    // structured-block metadata (multigrid) and its hierarchy
+    int bx = 0, by = 0, bz = 0;
+    std::shared_ptr<MgHierarchy> mg;
+    int64_t assembly_epoch = 0;
     cudaStream_t stream = nullptr;
     std::string err;
     int64_t launches = 0;
@@ -109,6 +116,8 @@ struct Ctx {
     std::vector<double> c_coef, c_rhs;
     // load cases (FP64 host, natural numbering, without penalty rhs)
     std::vector<std::vector<double>> loads;
+    int64_t loads_version = 0, rhs_version = -1;  // device copy valid when equal
+    double rhs_sf = -1.0;
     // objective + design variables
     int obj_kind = ASEND_OBJ_COMPLIANCE, obj_set = -1, obj_comp = 1;
     double obj_coef = 1.0;
@@ -202,5 +211,11 @@ void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g,
 int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* amp, int probe,
                 double* probe_hist, double* u_final, asend_solve_stats* st);
 void upload_rhs(Ctx& c);
+// multigrid (k_mg.cu)
+void mg_prepare(Ctx& c);
+void mg_apply(Ctx& c, const float* d_b, float* d_z4);
+int mg_levels(const Ctx& c);
+int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f, double* d_x,
+                 int nrhs);
 
 }  // namespace asend

@@ -313,6 +313,7 @@ void assemble_operator(Ctx& c, int precision) {
     float ms = 0.f;
     ASEND_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
     c.assembled_precision = precision;
+    ++c.assembly_epoch;
     c.last_assemble_ms = ms;
 }
 

@@ -1,0 +1,156 @@
+// pcg_common.cuh -- data structures and device helpers shared by the PCG
+// drivers (k_pcg.cu: Jacobi / block-Jacobi; k_mg.cu: multigrid-preconditioned).
+#pragma once
+#include "common.cuh"
+
+namespace asend {
+namespace pcg {
+
+constexpr int kThreads = 128;
+constexpr int kMaxRhs = 4;
+
+struct RhsScalars {
+    double rz, rz_new, pAp, rr, bb, alpha, beta, target, rr_last_true;
+    int32_t iter, done, finished, replace, nonfinite, pad0, pad1, pad2;
+};
+struct Control {
+    int32_t all_done;
+    uint32_t ticket[4];
+    int32_t pad[3];
+};
+
+struct PcgArgs {
+    int n_rows, nrhs, n_dof;
+    const int64_t* slice_off;
+    const uint8_t* row_len;
+    const int32_t* col;
+    const float* v32;
+    const double* v64;
+    const double* f;
+    double* x;
+    double* r;
+    void* p;      // node-padded direction (float4 or 2 x double2 per node)
+    void* ap;     // natural layout A p (float or double)
+    const double* dinv;
+    const float* binv;
+    double* partials;  // [gridDim.x][kMaxRhs][3]
+    RhsScalars* sc;
+    Control* ctl;
+};
+
+template <typename TP>
+struct PadVec;
+template <>
+struct PadVec<float> {
+    __device__ static void load(const void* p, size_t node, float (&v)[3]) {
+        const float4 q = reinterpret_cast<const float4*>(p)[node];
+        v[0] = q.x; v[1] = q.y; v[2] = q.z;
+    }
+    __device__ static void store(void* p, size_t node, const double (&v)[3]) {
+        reinterpret_cast<float4*>(p)[node] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
+    }
+};
+template <>
+struct PadVec<double> {
+    __device__ static void load(const void* p, size_t node, double (&v)[3]) {
+        const double2* q = reinterpret_cast<const double2*>(p) + 2 * node;
+        const double2 a = q[0], b = q[1];
+        v[0] = a.x; v[1] = a.y; v[2] = b.x;
+    }
+    __device__ static void store(void* p, size_t node, const double (&v)[3]) {
+        double2* q = reinterpret_cast<double2*>(p) + 2 * node;
+        q[0] = make_double2(v[0], v[1]);
+        q[1] = make_double2(v[2], 0.0);
+    }
+};
+
+// y[k][a] = sum_j sum_c A[r][j](a,c) * p_k[col_j](c) for NR right-hand sides.
+template <typename TV, typename TP, int NR>
+__device__ __forceinline__ void spmv_row(int row, const PcgArgs& A, const TV* __restrict__ vals,
+                                         const void* __restrict__ p, TP (&y)[NR][3]) {
+#pragma unroll
+    for (int k = 0; k < NR; ++k) y[k][0] = y[k][1] = y[k][2] = (TP)0;
+    const int lane = row & 31;
+    const int64_t g0 = A.slice_off[row >> 5];
+    const int len = A.row_len[row];
+    for (int j = 0; j < len; ++j) {
+        const int64_t g = g0 + j;
+        const int c = A.col[g * 32 + lane];
+        const TV* v = vals + (g * 9) * 32 + lane;
+        TV m[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) m[q] = v[q * 32];
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            TP pv[3];
+            PadVec<TP>::load(p, (size_t)k * A.n_rows + c, pv);
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                y[k][a] = fma((TP)m[a * 3 + 0], pv[0], fma((TP)m[a * 3 + 1], pv[1], fma((TP)m[a * 3 + 2], pv[2], y[k][a])));
+        }
+    }
+}
+
+// Preconditioner application z = M^-1 r for one node.
+template <int PC>
+__device__ __forceinline__ void precond(const PcgArgs& A, int row, const double (&r)[3], double (&z)[3]) {
+    if constexpr (PC == ASEND_PC_JACOBI) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) z[a] = A.dinv[3 * (size_t)row + a] * r[a];
+    } else {
+        const float* B = A.binv + 9 * (size_t)row;
+        const float r0 = (float)r[0], r1 = (float)r[1], r2 = (float)r[2];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) z[a] = (double)fmaf(B[3 * a], r0, fmaf(B[3 * a + 1], r1, B[3 * a + 2] * r2));
+    }
+}
+
+// Last-CTA reduction of NV values per RHS; returns true in the last CTA
+// (all its threads) with tot[k][v] valid in every thread.
+template <int NR, int NV>
+__device__ __forceinline__ bool last_block_reduce(const PcgArgs& A, double (&val)[NR][NV], int ticket_id,
+                                  double (&tot)[NR][NV]) {
+    __shared__ double sm[32 * NR * NV];
+    __shared__ bool is_last;
+    double flat[NR * NV];
+#pragma unroll
+    for (int k = 0; k < NR; ++k)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) flat[k * NV + v] = val[k][v];
+    block_sum<NR * NV>(flat, sm);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NR * NV; ++q) A.partials[(size_t)blockIdx.x * (kMaxRhs * 3) + q] = flat[q];
+        __threadfence();
+        const uint32_t t = atomicAdd(&A.ctl->ticket[ticket_id], 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+    double acc[NR * NV];
+#pragma unroll
+    for (int q = 0; q < NR * NV; ++q) acc[q] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        const volatile double* pp = A.partials + (size_t)b * (kMaxRhs * 3);
+#pragma unroll
+        for (int q = 0; q < NR * NV; ++q) acc[q] += pp[q];
+    }
+    __syncthreads();
+    block_sum<NR * NV>(acc, sm);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NR * NV; ++q) sm[q] = acc[q];
+        A.ctl->ticket[ticket_id] = 0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NR; ++k)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) tot[k][v] = sm[k * NV + v];
+    return true;
+}
+
+
+}  // namespace pcg
+}  // namespace asend

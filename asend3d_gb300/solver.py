@@ -118,6 +118,8 @@ class GpuSolver:
         self._check(self.lib.asend_set_mesh(self.ctx, m.elem_type, m.n_nodes, _ptr(coords, C.c_double), m.n_elems,
                                             _ptr(conn, C.c_int32), _ptr(E, C.c_double), _ptr(nu, C.c_double),
                                             None if rho is None else _ptr(rho, C.c_double), None), "set_mesh")
+        if m.elem_type == 8 and m.conn.shape[0] == m.nx * m.ny * m.nz:
+            self._check(self.lib.asend_set_block_structure(self.ctx, m.nx, m.ny, m.nz), "set_block_structure")
         for name, nodes in p.node_sets.items():
             arr = np.ascontiguousarray(nodes, dtype=np.int32)
             self.set_ids[name] = self._check(self.lib.asend_add_node_set(self.ctx, len(arr), _ptr(arr, C.c_int32)),

@@ -4,7 +4,8 @@ Workload (default): the 200x40x40 hex8 block (1,013,643 DOF) with a seeded
 lognormal modulus field (median 70 GPa, sigma_log 0.3, correlation 0.1 L),
 nu = 0.33, fixed end + distributed end-face traction, compliance objective.
 One step = FP64 element integration + coloured CSR-block assembly + penalty,
-mixed-precision PCG to ||f - A u|| / ||f|| <= 1e-8 (FP64 operator), and the
+multigrid-preconditioned CG (FP64 operator and recurrence, FP32 V-cycle) to
+||f - A u|| / ||f|| <= 1e-8 (FP64 operator), and the
 adjoint compliance gradient over all 320,000 element moduli.
 
 value  = DOF-solves/s with inputs resident in HBM (device-event timed).
@@ -210,7 +211,7 @@ def run_ours(a):
     stream = torch.cuda.ExternalStream(g.stream, device=torch.device("cuda", local))
     n_dof = g.n_dof
     n_el = p.mesh.n_elems
-    mixed = dict(method=_lib.METHOD_MIXED, precond=_lib.PC_JACOBI, rel_tol=1e-8, graph_iters=32)
+    mixed = dict(method=_lib.METHOD_FP64, precond=_lib.PC_MG, rel_tol=1e-8, graph_iters=8)
 
     def step_device():
         g.assemble(precision=64)
@@ -339,9 +340,9 @@ def run_ours(a):
         clocks = clk.summary()
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f32 SpMV + f64 dots/residual", "data": "synthetic (seeded lognormal field)",
+               "vs_baseline": None, "dtype": "f64 operator/dots + f32 multigrid", "data": "synthetic (seeded lognormal field)",
                "config": {"workload": f"block_large {a.nx}x{a.ny}x{a.nz} hex8 static + adjoint",
-                          "n_dof": n_dof, "n_elems": n_el, "rhs_per_step": 1, "method": "mixed FP32/FP64 PCG, Jacobi",
+                          "n_dof": n_dof, "n_elems": n_el, "rhs_per_step": 1, "method": "CG + geometric multigrid V-cycle (FP32 levels), FP64 operator",
                           "rel_tol": 1e-8, "l2": "operator 640 MB FP64 + 330 MB FP32 > 129 MB L2 (inputs larger than L2)",
                           "parallelism": f"replicas x{world}"},
                "iterations": iters, "ms_breakdown": {"assemble": stats[-1]["ms_assemble"],

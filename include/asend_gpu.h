@@ -51,6 +51,7 @@ typedef struct asend_ctx asend_ctx;
 #define ASEND_PC_JACOBI 0     /* point Jacobi                                             */
 #define ASEND_PC_BLOCK 1      /* nodal block Jacobi (dof_per_node x dof_per_node blocks)  */
 #define ASEND_PC_LEARNED 2    /* MLP-predicted nodal blocks, Jacobi fallback              */
+#define ASEND_PC_MG 3         /* geometric multigrid V-cycle (structured hex8 blocks)     */
 
 /* objective kinds (reference objective categories, objective_meth.rs:592-942) */
 #define ASEND_OBJ_DISPLACEMENT 0 /* 'displacement' + 'powerNorm' on a node set            */
@@ -97,6 +98,15 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
  * rebuilding the pattern.  Replaces the DV-perturbed property path of
  * element_properties.rs:648-764 for the isotropic-modulus case. */
 int asend_set_modulus(asend_ctx* ctx, const double* E);
+
+/* Declare the hex8 mesh a structured nx*ny*nz block in the numbering of the
+ * reference's swept meshing (node (i,j,k) = (i*(ny+1)+j)*(nz+1)+k, element
+ * (i,j,k) = (i*ny+j)*nz+k, hex8 corner order).  Enables ASEND_PC_MG, which
+ * replaces the reference's block-LDL^T preconditioner
+ * (lower_tri_mat_meth.rs:15-241).  Validated against the connectivity. */
+int asend_set_block_structure(asend_ctx* ctx, int32_t nx, int32_t ny, int32_t nz);
+/* Number of multigrid levels built so far (0 before the first MG solve). */
+int asend_mg_levels(const asend_ctx* ctx);
 
 /* Node / element sets (model_input.rs:720-860 'sets' blocks).  Returns the
  * set id (>= 0) or a negative error code. */
