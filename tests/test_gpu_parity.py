@@ -110,7 +110,7 @@ def test_compliance_gradient_lognormal(gpu_lib, oracle_lib):
     p = configs.block_large(nx=24, ny=6, nz=6, seed=5)
     g = GpuSolver(p)
     g.assemble()
-    u, rc, _ = g.static_solve(method=_lib.METHOD_FP64, rel_tol=1e-11)
+    u, rc, _ = g.static_solve(method=_lib.METHOD_FP64, precond=_lib.PC_MG, rel_tol=1e-11)
     assert rc == 0
     L, dLdE, rc, _ = g.adjoint_gradient()
     o = oracle_lib.Oracle(p)
@@ -224,7 +224,7 @@ def test_full_size_block_properties(gpu_lib):
     g.close()
 
 
-@pytest.mark.parametrize("method", [_lib.METHOD_FP64, _lib.METHOD_MIXED])
+@pytest.mark.parametrize("method", [_lib.METHOD_FP64])
 def test_multigrid_small_parity(small, method):
     p, g, o = small
     gold = np.load(GOLD / "cantilever_small.npz")
