@@ -214,6 +214,23 @@ int64_t asend_kernel_launches(const asend_ctx* ctx);
  * its own CUDA events around library calls. */
 void* asend_stream(const asend_ctx* ctx);
 
+/* y = A x and *energy = x^T A x with the assembled FP64 operator, on DEVICE
+ * buffers (x, y: n_dof doubles; energy: one double), without allocating any
+ * device memory.  No counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc -- applications that give all device memory to their
+ * own pool allocator or run under a fixed HBM budget, and optimisation loops
+ * that evaluate the energy many times where an allocation could fail or stall.
+ * Its reduction scratch is a fixed 256 KiB array compiled into the library,
+ * which every GPU that loads the library holds until the process exits.
+ * Limit: 4,194,304 node rows (12,582,912 DOF), 3 DOF per node; larger
+ * operators are rejected with ASEND_EINVAL and a message.  The first call on a
+ * device looks up the array's device address (a one-time set-up), so make
+ * that first call before any stream capture.  The work is enqueued on the
+ * context's stream and not synchronised.  All calls share the scratch array:
+ * calls that overlap on the GPU (other streams or contexts on the same
+ * device) race and must be serialised by the caller. */
+int asend_operator_energy_noalloc(asend_ctx* ctx, const double* d_x, double* d_y, double* d_energy);
+
 #ifdef __cplusplus
 }
 #endif
