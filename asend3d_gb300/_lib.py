@@ -47,6 +47,7 @@ SIGNATURES = [
     ("asend_set_modulus", c_int, [C.c_void_p, P_dbl]),
     ("asend_set_block_structure", c_int, [C.c_void_p, c_int, c_int, c_int]),
     ("asend_mg_levels", c_int, [C.c_void_p]),
+    ("asend_set_instances", c_int, [C.c_void_p, c_int, P_int]),
     ("asend_add_node_set", c_int, [C.c_void_p, c_int, P_int]),
     ("asend_add_element_set", c_int, [C.c_void_p, c_int, P_int]),
     ("asend_add_constraint", c_int, [C.c_void_p, c_int, P_int, P_int, P_dbl, c_dbl]),

@@ -97,3 +97,14 @@ def learned_grid(seed=11, nx=128, ny=64, nz=64, median=70e9, sigma_log=0.5, corr
     p.add_surface_traction("xMaxEls", (1.0, 0.0, 0.0), (0.0, 0.0, -1.0e6))
     p.objective = ("compliance",)
     return p
+
+
+def batch_uq(n_inst: int = 64, seed: int = 7):
+    """The batched UQ / design sweep: n_inst uneven cantilevers, 4 load cases
+    each, combined into one stacked problem.  Returns (problem, node_ptr,
+    elem_ptr, instances)."""
+    from .solver import combine
+
+    inst = [batch_instance(k, seed=seed) for k in range(n_inst)]
+    prob, node_ptr, elem_ptr = combine(inst)
+    return prob, node_ptr, elem_ptr, inst

@@ -176,9 +176,13 @@ void build_pattern(Ctx& c) {
         for (int k = c.c_ptr[r]; k < c.c_ptr[r + 1]; ++k)
             for (int k2 = c.c_ptr[r]; k2 < c.c_ptr[r + 1]; ++k2)
                 adj[c.c_dof[k] / b].push_back(c.c_dof[k2] / b);
+    std::vector<int32_t> isolated;
     for (int i = 0; i < N; ++i) {
         auto& v = adj[i];
-        if (v.empty()) v.push_back(i);  // isolated node keeps a diagonal block
+        if (v.empty()) {  // node without elements or constraints (e.g. instance padding)
+            v.push_back(i);
+            isolated.push_back(i);
+        }
         std::sort(v.begin(), v.end());
         v.erase(std::unique(v.begin(), v.end()), v.end());
         require(v.size() <= 255, "a node has more than 255 neighbouring nodes");
@@ -225,6 +229,7 @@ void build_pattern(Ctx& c) {
     // penalty entries: value index of (dof_i, dof_j) for every term pair
     std::vector<int64_t> pen_idx;
     std::vector<double> pen_coef;
+    std::vector<int32_t> pen_dof;
     for (int r = 0; r < nrow_c; ++r)
         for (int k = c.c_ptr[r]; k < c.c_ptr[r + 1]; ++k)
             for (int k2 = c.c_ptr[r]; k2 < c.c_ptr[r + 1]; ++k2) {
@@ -234,6 +239,7 @@ void build_pattern(Ctx& c) {
                 const int64_t g = slot / kSlice, lane = slot % kSlice;
                 pen_idx.push_back((g * b2 + ai * b + aj) * kSlice + lane);
                 pen_coef.push_back(c.c_coef[k] * c.c_coef[k2]);
+                pen_dof.push_back(di);
             }
     // greedy colouring with per-node colour masks
     std::vector<uint64_t> mask(N, 0);
@@ -257,8 +263,16 @@ void build_pattern(Ctx& c) {
         std::vector<int32_t> fill(c.colour_ptr.begin(), c.colour_ptr.end() - 1);
         for (int e = 0; e < c.n_el; ++e) c.colour_elems[fill[c.colour_of[e]]++] = e;
     }
+    // unit diagonal for isolated nodes (their DOFs decouple: x = f)
+    std::vector<int64_t> unit_idx;
+    for (int nd : isolated) {
+        const int64_t slot = A.slot(nd, pos(nd, nd));
+        const int64_t g = slot / kSlice, lane = slot % kSlice;
+        for (int a = 0; a < b; ++a) unit_idx.push_back((g * b2 + a * b + a) * kSlice + lane);
+    }
     // uploads
     cudaStream_t s = c.stream;
+    c.d_unit_idx.upload(unit_idx, s);
     A.slice_off.upload(A.h_slice_off, s);
     A.col.upload(A.h_col, s);
     A.row_len.upload(A.h_row_len, s);
@@ -267,8 +281,33 @@ void build_pattern(Ctx& c) {
     c.d_colour_elems.upload(c.colour_elems, s);
     c.d_pen_idx.upload(pen_idx, s);
     c.d_pen_coef.upload(pen_coef, s);
+    c.pen_dof = pen_dof;
+    c.pen_coef_host = pen_coef;
     ASEND_CUDA(cudaStreamSynchronize(s));
     c.pattern_ready = true;
+}
+
+int instance_of_node(const Ctx& c, int node) {
+    if (c.n_inst <= 1) return 0;
+    return (int)(std::upper_bound(c.inst_node_ptr.begin(), c.inst_node_ptr.end(), node) - c.inst_node_ptr.begin()) - 1;
+}
+
+// Penalty scale of constraint row `row`: per instance in a batched stack
+// (each instance is its own model, as the reference scales per model).
+double row_penalty_scale(const Ctx& c, int row) {
+    if (c.n_inst <= 1 || c.sf_inst.empty()) return c.sf;
+    return c.sf_inst[instance_of_node(c, c.c_dof[c.c_ptr[row]] / c.dpn)];
+}
+
+// Pinned host mirror of the PCG scalars, grown on demand.
+void ensure_pinned_scalars(Ctx& c, size_t bytes) {
+    if (bytes <= c.h_sc_bytes) return;
+    ASEND_CUDA(cudaStreamSynchronize(c.stream));
+    if (c.h_sc) cudaFreeHost(c.h_sc);
+    c.h_sc = nullptr;
+    c.h_sc_bytes = 0;
+    ASEND_CUDA(cudaMallocHost(&c.h_sc, bytes));
+    c.h_sc_bytes = bytes;
 }
 
 // Load vectors incl. the penalty right-hand side -sf C^T (C*0 - q) = sf C^T q
@@ -279,7 +318,9 @@ void upload_rhs(Ctx& c) {
         ++c.loads_version;
     }
     const int nr = (int)c.loads.size();
-    if (c.rhs_version == c.loads_version && c.rhs_sf == c.sf && c.d_f.n == (size_t)nr * c.n_dof) return;
+    if (c.rhs_version == c.loads_version && c.rhs_sf == c.sf && c.d_f.n == (size_t)nr * c.n_dof &&
+        c.n_inst <= 1)
+        return;
     c.rhs_version = c.loads_version;
     c.rhs_sf = c.sf;
     std::vector<double> f((size_t)nr * c.n_dof);
@@ -288,7 +329,7 @@ void upload_rhs(Ctx& c) {
         std::copy(c.loads[r].begin(), c.loads[r].end(), fr);
         const int nrow_c = (int)c.c_rhs.size();
         for (int q = 0; q < nrow_c; ++q) {
-            const double qq = c.sf * c.c_rhs[q];
+            const double qq = row_penalty_scale(c, q) * c.c_rhs[q];
             for (int k = c.c_ptr[q]; k < c.c_ptr[q + 1]; ++k) fr[c.c_dof[k]] += c.c_coef[k] * qq;
         }
     }
@@ -313,7 +354,8 @@ asend_ctx* asend_create(int32_t device) {
     }
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
-    if (cudaMallocHost(&c->h_sc, sizeof(PcgScalars) * 64) != cudaSuccess) {
+    c->h_sc_bytes = sizeof(PcgScalars) * 64;
+    if (cudaMallocHost(&c->h_sc, c->h_sc_bytes) != cudaSuccess) {
         delete c;
         return nullptr;
     }
@@ -391,6 +433,8 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         c.pattern_ready = c.assembled = c.solved = false;
         c.bx = c.by = c.bz = 0;
         c.mg.reset();
+        c.n_inst = 0;
+        c.inst_node_ptr.clear();
         c.d_xyz.upload(c.xyz, c.stream);
         c.d_conn.upload(c.conn, c.stream);
         c.d_E.upload(c.E, c.stream);
@@ -424,6 +468,49 @@ int asend_set_block_structure(asend_ctx* ctx, int32_t nx, int32_t ny, int32_t nz
         c.by = ny;
         c.bz = nz;
         c.mg.reset();
+        return ASEND_OK;
+    });
+}
+
+// Declares the mesh a stack of independent sub-systems (e.g. a batch of UQ /
+// design instances): instance i owns nodes [node_ptr[i], node_ptr[i+1]) and
+// every element and constraint lies inside one instance.  Each instance must
+// start on a multiple of 128 nodes (pad with unused nodes), so every CTA of
+// the PCG kernels belongs to one instance; convergence, step lengths and
+// stopping are then per instance and load case.
+int asend_set_instances(asend_ctx* ctx, int32_t n_inst, const int32_t* node_ptr) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.n_nodes > 0, "set the mesh first");
+        require(n_inst >= 1 && node_ptr, "need at least one instance");
+        require(node_ptr[0] == 0 && node_ptr[n_inst] == c.n_nodes, "node_ptr must span all nodes");
+        for (int i = 0; i < n_inst; ++i) {
+            require(node_ptr[i + 1] > node_ptr[i], "empty instance");
+            require(node_ptr[i] % 128 == 0, "each instance must start at a multiple of 128 nodes");
+        }
+        std::vector<int32_t> inst_of(c.n_nodes);
+        for (int i = 0; i < n_inst; ++i)
+            for (int v = node_ptr[i]; v < node_ptr[i + 1]; ++v) inst_of[v] = i;
+        for (int e = 0; e < c.n_el; ++e)
+            for (int a = 1; a < c.nn; ++a)
+                require(inst_of[c.conn[(size_t)e * c.nn + a]] == inst_of[c.conn[(size_t)e * c.nn]],
+                        "an element spans two instances");
+        for (size_t r = 0; r + 1 < c.c_ptr.size(); ++r)
+            for (int k = c.c_ptr[r] + 1; k < c.c_ptr[r + 1]; ++k)
+                require(inst_of[c.c_dof[k] / c.dpn] == inst_of[c.c_dof[c.c_ptr[r]] / c.dpn],
+                        "a constraint spans two instances");
+        const int n_cta = (c.n_nodes + 127) / 128;
+        std::vector<int32_t> cta_inst(n_cta), cta0(n_inst), ncta(n_inst, 0);
+        for (int b = 0; b < n_cta; ++b) cta_inst[b] = inst_of[b * 128];
+        for (int b = n_cta - 1; b >= 0; --b) {
+            cta0[cta_inst[b]] = b;
+            ncta[cta_inst[b]]++;
+        }
+        c.n_inst = n_inst;
+        c.inst_node_ptr.assign(node_ptr, node_ptr + n_inst + 1);
+        c.d_cta_inst.upload(cta_inst, c.stream);
+        c.d_inst_cta0.upload(cta0, c.stream);
+        c.d_inst_ncta.upload(ncta, c.stream);
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
         return ASEND_OK;
     });
 }
@@ -605,7 +692,8 @@ int asend_get_load_vector(asend_ctx* ctx, int32_t rhs, double* f_out) {
         if (c.assembled) {
             const int nrow_c = (int)c.c_rhs.size();
             for (int q = 0; q < nrow_c; ++q)
-                for (int k = c.c_ptr[q]; k < c.c_ptr[q + 1]; ++k) f_out[c.c_dof[k]] += c.c_coef[k] * c.sf * c.c_rhs[q];
+                for (int k = c.c_ptr[q]; k < c.c_ptr[q + 1]; ++k)
+                    f_out[c.c_dof[k]] += c.c_coef[k] * row_penalty_scale(c, q) * c.c_rhs[q];
         }
         return ASEND_OK;
     });

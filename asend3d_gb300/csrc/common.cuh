@@ -161,6 +161,17 @@ struct Ctx {
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
+    // independent instances stacked in one operator (batched solves)
+    int n_inst = 0;
+    std::vector<int32_t> inst_node_ptr;
+    DArr<int32_t> d_cta_inst, d_inst_cta0, d_inst_ncta;
+    DArr<int64_t> d_unit_idx;  // diagonal entries of nodes without elements (set to 1)
+    std::vector<double> sf_inst;             // penalty scale per instance
+    std::vector<int32_t> pen_dof;            // DOF of each penalty entry (host)
+    std::vector<double> pen_coef_host;       // coef_i * coef_j of each penalty entry (host)
+    DArr<double> d_pen_val;                  // per-entry penalty values (batched)
+    size_t h_sc_bytes = 0;
+
     // graphs
     cudaGraphExec_t graph = nullptr;
     int graph_key[6] = {-1, -1, -1, -1, -1, -1};
@@ -211,6 +222,9 @@ void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g,
 int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* amp, int probe,
                 double* probe_hist, double* u_final, asend_solve_stats* st);
 void upload_rhs(Ctx& c);
+void ensure_pinned_scalars(Ctx& c, size_t bytes);
+int instance_of_node(const Ctx& c, int node);
+double row_penalty_scale(const Ctx& c, int row);
 // multigrid (k_mg.cu)
 void mg_prepare(Ctx& c);
 void mg_apply(Ctx& c, const float* d_b, float* d_z4);

@@ -17,6 +17,9 @@
 // transpose into the sliced block-ELL values through a precomputed slot map.
 // Elements of one colour share no node, so the scatter needs no atomics and
 // the summation order is fixed (deterministic).
+#include <algorithm>
+#include <vector>
+
 #include "common.cuh"
 
 namespace asend {
@@ -232,6 +235,29 @@ __global__ void penalty_kernel(int n, const int64_t* __restrict__ idx, const dou
     if (k < n) atomicAdd(&vals[idx[k]], sf * coef[k]);
 }
 
+__global__ void unit_kernel(int n, const int64_t* __restrict__ idx, double* vals) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) vals[idx[k]] = 1.0;
+}
+
+// per-instance max |value| over contiguous value ranges (blockIdx.y = instance)
+__global__ void max_abs_seg_kernel(const int64_t* __restrict__ seg, const double* __restrict__ v,
+                                   unsigned long long* out) {
+    const int inst = blockIdx.y;
+    const int64_t b = seg[inst], e = seg[inst + 1];
+    double m = 0.0;
+    for (int64_t i = b + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < e; i += (int64_t)gridDim.x * blockDim.x)
+        m = fmax(m, fabs(v[i]));
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) atomicMax(&out[inst], (unsigned long long)__double_as_longlong(m));
+}
+
+__global__ void penalty_val_kernel(int n, const int64_t* __restrict__ idx, const double* __restrict__ val,
+                                   double* vals) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) atomicAdd(&vals[idx[k]], val[k]);
+}
+
 __global__ void round_kernel(size_t n, const double* __restrict__ src, float* __restrict__ dst) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         dst[i] = (float)src[i];
@@ -291,18 +317,60 @@ void assemble_operator(Ctx& c, int precision) {
         ++c.launches;
     }
     // penalty scale over the element matrix (K [+ cM M]), then the penalty
-    c.d_max_partial.alloc(1);
-    c.d_max_partial.zero(c.stream);
-    max_abs_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(
-        nval, A.v64.p, reinterpret_cast<unsigned long long*>(c.d_max_partial.p));
-    ++c.launches;
-    double mx = 0.0;
-    ASEND_CUDA(cudaMemcpyAsync(&mx, c.d_max_partial.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-    ASEND_CUDA(cudaStreamSynchronize(c.stream));
-    c.sf = 100000.0 * mx;
     const int npen = (int)c.d_pen_idx.n;
-    if (npen > 0) {
-        penalty_kernel<<<(npen + 255) / 256, 256, 0, c.stream>>>(npen, c.d_pen_idx.p, c.d_pen_coef.p, c.sf, A.v64.p);
+    if (c.n_inst > 1) {
+        // one scale per instance (each instance is its own model)
+        const int ni = c.n_inst;
+        std::vector<int64_t> seg(ni + 1);
+        for (int i = 0; i <= ni; ++i) {
+            const int node = c.inst_node_ptr[i];
+            const int s = std::min((node + kSlice - 1) / kSlice, A.n_slices);
+            seg[i] = A.h_slice_off[s] * 9 * kSlice;
+        }
+        DArr<int64_t> d_seg;
+        d_seg.upload(seg, c.stream);
+        c.d_max_partial.alloc(ni);
+        c.d_max_partial.zero(c.stream);
+        max_abs_seg_kernel<<<dim3(64, ni), 256, 0, c.stream>>>(d_seg.p, A.v64.p,
+                                                               reinterpret_cast<unsigned long long*>(c.d_max_partial.p));
+        ++c.launches;
+        std::vector<double> mx(ni);
+        ASEND_CUDA(cudaMemcpyAsync(mx.data(), c.d_max_partial.p, sizeof(double) * ni, cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        c.sf_inst.resize(ni);
+        c.sf = 0.0;
+        for (int i = 0; i < ni; ++i) {
+            c.sf_inst[i] = 100000.0 * mx[i];
+            c.sf = std::max(c.sf, c.sf_inst[i]);
+        }
+        if (npen > 0) {
+            std::vector<double> val(npen);
+            for (int k = 0; k < npen; ++k)
+                val[k] = c.sf_inst[instance_of_node(c, c.pen_dof[k] / c.dpn)] * c.pen_coef_host[k];
+            c.d_pen_val.upload(val, c.stream);
+            penalty_val_kernel<<<(npen + 255) / 256, 256, 0, c.stream>>>(npen, c.d_pen_idx.p, c.d_pen_val.p, A.v64.p);
+            ++c.launches;
+        }
+    } else {
+        c.sf_inst.clear();
+        c.d_max_partial.alloc(1);
+        c.d_max_partial.zero(c.stream);
+        max_abs_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(
+            nval, A.v64.p, reinterpret_cast<unsigned long long*>(c.d_max_partial.p));
+        ++c.launches;
+        double mx = 0.0;
+        ASEND_CUDA(cudaMemcpyAsync(&mx, c.d_max_partial.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        c.sf = 100000.0 * mx;
+        if (npen > 0) {
+            penalty_kernel<<<(npen + 255) / 256, 256, 0, c.stream>>>(npen, c.d_pen_idx.p, c.d_pen_coef.p, c.sf,
+                                                                     A.v64.p);
+            ++c.launches;
+        }
+    }
+    const int nunit = (int)c.d_unit_idx.n;
+    if (nunit > 0) {
+        unit_kernel<<<(nunit + 255) / 256, 256, 0, c.stream>>>(nunit, c.d_unit_idx.p, A.v64.p);
         ++c.launches;
     }
     round_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(nval, A.v64.p, A.v32.p);

@@ -53,6 +53,7 @@ struct MgLevel {
     std::vector<float> h_pen;     // lumped penalty per DOF (in units of sf)
     DArr<float> pen;
     DArr<float> binv, b, r, x4, y4;
+    DArr<float> t1, t2;           // restriction intermediates (after the z and y passes)
 };
 
 struct MgHierarchy {
@@ -86,121 +87,122 @@ struct LevelView {  // kernel-side view of one level's interpolation tables
 // ---------------------------------------------------------------------------
 // Galerkin coarsening by elements
 // ---------------------------------------------------------------------------
-// FP32 hex8 element stiffness of fine element e into shared Ke[24][24]
-// (same closed form as the assembly kernel; 2x2x2 Gauss points).
-__device__ void ke_hex8_f32(const double* xyz, const int32_t* conn, int e, double E, double nu, float* Ke,
-                            float (*g)[8][3], float* w, float (*x)[3]) {
-    const int t = threadIdx.x;
-    if (t < 24) {
-        const int a = t / 3, j = t % 3;
-        const int n0 = conn[(size_t)e * 8], na = conn[(size_t)e * 8 + a];
-        x[a][j] = (float)(xyz[3 * (size_t)na + j] - xyz[3 * (size_t)n0 + j]);
-    }
-    __syncthreads();
-    if (t < 8) {
-        const float gq = 0.5773502691896257f;
-        const float s[3] = {(t & 1) ? gq : -gq, (t & 2) ? gq : -gq, (t & 4) ? gq : -gq};
-        float dn[8][3];
-        float J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-        for (int a = 0; a < 8; ++a) {
-            const float sg0 = c_corner[a][0] ? 1.f : -1.f, sg1 = c_corner[a][1] ? 1.f : -1.f,
-                        sg2 = c_corner[a][2] ? 1.f : -1.f;
-            const float f0 = 1 + sg0 * s[0], f1 = 1 + sg1 * s[1], f2 = 1 + sg2 * s[2];
-            dn[a][0] = 0.125f * sg0 * f1 * f2;
-            dn[a][1] = 0.125f * sg1 * f0 * f2;
-            dn[a][2] = 0.125f * sg2 * f0 * f1;
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) J[i][j] += x[a][i] * dn[a][j];
-        }
-        const float c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-        const float c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-        const float c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-        const float det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-        const float id = 1.f / det;
-        float Ji[3][3];
-        Ji[0][0] = c00 * id;
-        Ji[1][0] = c01 * id;
-        Ji[2][0] = c02 * id;
-        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-        for (int a = 0; a < 8; ++a)
-            for (int j = 0; j < 3; ++j) g[t][a][j] = dn[a][0] * Ji[0][j] + dn[a][1] * Ji[1][j] + dn[a][2] * Ji[2][j];
-        w[t] = det;
-    }
-    __syncthreads();
-    const float lam = (float)(E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)));
-    const float mu = (float)(E / (2.0 * (1.0 + nu)));
-    for (int p = t; p < 64; p += blockDim.x) {
-        const int a = p >> 3, b = p & 7;
-        float S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-        for (int gp = 0; gp < 8; ++gp)
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) S[i][j] += w[gp] * g[gp][a][i] * g[gp][b][j];
-        const float tr = mu * (S[0][0] + S[1][1] + S[2][2]);
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j)
-                Ke[(3 * a + i) * 24 + 3 * b + j] = lam * S[i][j] + mu * S[j][i] + ((i == j) ? tr : 0.f);
-    }
-    __syncthreads();
-}
-
-// One CTA per coarse element C of level l; children are elements of level
-// l-1 (from geometry when fine_ke == nullptr).
-__global__ void __launch_bounds__(256)
+// One CTA (512 threads) per coarse element C of level l.  Its <= 8 children
+// (elements of level l-1) are processed together: each child's FP32 stiffness
+// comes from the stored Galerkin matrices of level l-1, or for l = 1 is
+// integrated here from the fine geometry (2x2x2 Gauss points, closed-form
+// isotropic blocks as in the assembly kernel); then T_e = K_e (Q_e x I3) and
+// K_C = sum_e (Q_e x I3)^T T_e.
+__global__ void __launch_bounds__(512)
 k_coarsen(LevelView cv, int fny, int fnz, const float* __restrict__ fine_ke, const double* __restrict__ xyz,
           const int32_t* __restrict__ conn0, const double* __restrict__ E, const double* __restrict__ nu,
           float* __restrict__ coarse_ke) {
-    __shared__ float Ke[576], T[576], KC[576], Q[8][8];
-    __shared__ float g[8][8][3], w[8], x[8][3];
+    __shared__ float Ke[8][576];
+    __shared__ float T[8][576];
+    __shared__ float Q[8][8][8];
+    __shared__ float g[8][8][8][3];
+    __shared__ float wdet[8][8];
+    __shared__ float xl[8][8][3];
+    __shared__ int fe[8];
+    const int t = threadIdx.x;
     const int C = blockIdx.x;
     const int ci = C / (cv.ny * cv.nz), cj = (C / cv.nz) % cv.ny, ck = C % cv.nz;
     const int s0 = cv.xs[cv.ox0 + ci], w0 = cv.xs[cv.ox0 + ci + 1] - s0;
     const int s1 = cv.xs[cv.ox1 + cj], w1 = cv.xs[cv.ox1 + cj + 1] - s1;
     const int s2 = cv.xs[cv.ox2 + ck], w2 = cv.xs[cv.ox2 + ck + 1] - s2;
-    for (int q = threadIdx.x; q < 576; q += blockDim.x) KC[q] = 0.f;
-    for (int o0 = 0; o0 < w0; ++o0)
-        for (int o1 = 0; o1 < w1; ++o1)
-            for (int o2 = 0; o2 < w2; ++o2) {
-                const int fe = ((s0 + o0) * fny + (s1 + o1)) * fnz + (s2 + o2);
-                __syncthreads();
-                if (fine_ke) {
-                    for (int q = threadIdx.x; q < 576; q += blockDim.x) Ke[q] = fine_ke[(size_t)fe * 576 + q];
-                } else {
-                    ke_hex8_f32(xyz, conn0, fe, E[fe], nu[fe], Ke, g, w, x);
-                }
-                if (threadIdx.x < 64) {
-                    const int a = threadIdx.x >> 3, b = threadIdx.x & 7;
-                    const float xi0 = (float)(o0 + c_corner[a][0]) / w0;
-                    const float xi1 = (float)(o1 + c_corner[a][1]) / w1;
-                    const float xi2 = (float)(o2 + c_corner[a][2]) / w2;
-                    Q[a][b] = (c_corner[b][0] ? xi0 : 1.f - xi0) * (c_corner[b][1] ? xi1 : 1.f - xi1) *
-                              (c_corner[b][2] ? xi2 : 1.f - xi2);
-                }
-                __syncthreads();
-                // T = Ke (Q x I3)
-                for (int q = threadIdx.x; q < 576; q += blockDim.x) {
-                    const int row = q / 24, col = q % 24, b = col / 3, c2 = col % 3;
-                    float acc = 0.f;
-#pragma unroll
-                    for (int a2 = 0; a2 < 8; ++a2) acc += Ke[row * 24 + 3 * a2 + c2] * Q[a2][b];
-                    T[q] = acc;
-                }
-                __syncthreads();
-                // KC += (Q x I3)^T T
-                for (int q = threadIdx.x; q < 576; q += blockDim.x) {
-                    const int row = q / 24, col = q % 24, b = row / 3, c1 = row % 3;
-                    float acc = 0.f;
-#pragma unroll
-                    for (int a = 0; a < 8; ++a) acc += Q[a][b] * T[(3 * a + c1) * 24 + col];
-                    KC[q] += acc;
-                }
-            }
+    const int nch = w0 * w1 * w2;
+    if (t < nch * 64) {  // interpolation weights of child ch: fine corner a <- coarse corner b
+        const int ch = t >> 6, a = (t >> 3) & 7, b = t & 7;
+        const int o0 = ch / (w1 * w2), o1 = (ch / w2) % w1, o2 = ch % w2;
+        const float xi0 = (float)(o0 + c_corner[a][0]) / w0;
+        const float xi1 = (float)(o1 + c_corner[a][1]) / w1;
+        const float xi2 = (float)(o2 + c_corner[a][2]) / w2;
+        Q[ch][a][b] = (c_corner[b][0] ? xi0 : 1.f - xi0) * (c_corner[b][1] ? xi1 : 1.f - xi1) *
+                      (c_corner[b][2] ? xi2 : 1.f - xi2);
+        if (a == 0 && b == 0) fe[ch] = ((s0 + o0) * fny + (s1 + o1)) * fnz + (s2 + o2);
+    }
     __syncthreads();
-    for (int q = threadIdx.x; q < 576; q += blockDim.x) coarse_ke[(size_t)C * 576 + q] = KC[q];
+    if (fine_ke) {
+        for (int q = t; q < nch * 576; q += blockDim.x) Ke[q / 576][q % 576] = fine_ke[(size_t)fe[q / 576] * 576 + q % 576];
+    } else {
+        if (t < nch * 24) {
+            const int ch = t / 24, a = (t / 3) % 8, j = t % 3;
+            const int e = fe[ch];
+            const int n0 = conn0[(size_t)e * 8], na = conn0[(size_t)e * 8 + a];
+            xl[ch][a][j] = (float)(xyz[3 * (size_t)na + j] - xyz[3 * (size_t)n0 + j]);
+        }
+        __syncthreads();
+        if (t < nch * 8) {  // Gauss-point data of child ch, point gp
+            const int ch = t >> 3, gp = t & 7;
+            const float gq = 0.5773502691896257f;
+            const float s[3] = {(gp & 1) ? gq : -gq, (gp & 2) ? gq : -gq, (gp & 4) ? gq : -gq};
+            float dn[8][3];
+            float J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            for (int a = 0; a < 8; ++a) {
+                const float sg0 = c_corner[a][0] ? 1.f : -1.f, sg1 = c_corner[a][1] ? 1.f : -1.f,
+                            sg2 = c_corner[a][2] ? 1.f : -1.f;
+                const float f0 = 1 + sg0 * s[0], f1 = 1 + sg1 * s[1], f2 = 1 + sg2 * s[2];
+                dn[a][0] = 0.125f * sg0 * f1 * f2;
+                dn[a][1] = 0.125f * sg1 * f0 * f2;
+                dn[a][2] = 0.125f * sg2 * f0 * f1;
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) J[i][j] += xl[ch][a][i] * dn[a][j];
+            }
+            const float c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+            const float c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+            const float c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+            const float det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+            const float id = 1.f / det;
+            float Ji[3][3];
+            Ji[0][0] = c00 * id;
+            Ji[1][0] = c01 * id;
+            Ji[2][0] = c02 * id;
+            Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+            Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+            Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+            Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+            Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+            Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+            for (int a = 0; a < 8; ++a)
+                for (int j = 0; j < 3; ++j)
+                    g[ch][gp][a][j] = dn[a][0] * Ji[0][j] + dn[a][1] * Ji[1][j] + dn[a][2] * Ji[2][j];
+            wdet[ch][gp] = det;
+        }
+        __syncthreads();
+        if (t < nch * 64) {  // node-pair block (a, b) of child ch
+            const int ch = t >> 6, a = (t >> 3) & 7, b = t & 7;
+            const double Ee = E[fe[ch]], ne = nu[fe[ch]];
+            const float lam = (float)(Ee * ne / ((1.0 + ne) * (1.0 - 2.0 * ne)));
+            const float mu = (float)(Ee / (2.0 * (1.0 + ne)));
+            float S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            for (int gp = 0; gp < 8; ++gp)
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) S[i][j] += wdet[ch][gp] * g[ch][gp][a][i] * g[ch][gp][b][j];
+            const float tr = mu * (S[0][0] + S[1][1] + S[2][2]);
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                    Ke[ch][(3 * a + i) * 24 + 3 * b + j] = lam * S[i][j] + mu * S[j][i] + ((i == j) ? tr : 0.f);
+        }
+    }
+    __syncthreads();
+    // T_ch = K_ch (Q_ch x I3)
+    for (int q = t; q < nch * 576; q += blockDim.x) {
+        const int ch = q / 576, r = q % 576, row = r / 24, col = r % 24, b = col / 3, c2 = col % 3;
+        float acc = 0.f;
+#pragma unroll
+        for (int a2 = 0; a2 < 8; ++a2) acc = fmaf(Ke[ch][row * 24 + 3 * a2 + c2], Q[ch][a2][b], acc);
+        T[ch][r] = acc;
+    }
+    __syncthreads();
+    // K_C = sum_ch (Q_ch x I3)^T T_ch
+    for (int q = t; q < 576; q += blockDim.x) {
+        const int row = q / 24, col = q % 24, b = row / 3, c1 = row % 3;
+        float acc = 0.f;
+        for (int ch = 0; ch < nch; ++ch)
+#pragma unroll
+            for (int a = 0; a < 8; ++a) acc = fmaf(Q[ch][a][b], T[ch][(3 * a + c1) * 24 + col], acc);
+        coarse_ke[(size_t)C * 576 + q] = acc;
+    }
 }
 
 // Coloured scatter of stored element matrices into a level's FP32 values.
@@ -270,9 +272,18 @@ __global__ void k_dense_build(int n_rows, const int64_t* __restrict__ slice_off,
     }
 }
 
-__global__ void __launch_bounds__(1024) k_gauss_jordan(int n, float* __restrict__ A) {
+// In-place Gauss-Jordan inverse of an SPD matrix (no pivoting).  With
+// in_smem the whole matrix lives in dynamic shared memory for the n steps
+// (n*n*4 bytes, n <= 238); otherwise it is updated in global memory.
+__global__ void __launch_bounds__(1024) k_gauss_jordan(int n, float* __restrict__ Ag, int in_smem) {
+    extern __shared__ float dyn[];
     __shared__ float colk[1024];
     __shared__ float rowk[1024];
+    float* A = in_smem ? dyn : Ag;
+    if (in_smem) {
+        for (int q = threadIdx.x; q < n * n; q += blockDim.x) dyn[q] = Ag[q];
+        __syncthreads();
+    }
     for (int k = 0; k < n; ++k) {
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             colk[i] = A[(size_t)i * n + k];
@@ -290,6 +301,8 @@ __global__ void __launch_bounds__(1024) k_gauss_jordan(int n, float* __restrict_
         }
         __syncthreads();
     }
+    if (in_smem)
+        for (int q = threadIdx.x; q < n * n; q += blockDim.x) Ag[q] = dyn[q];
 }
 
 // ---------------------------------------------------------------------------
@@ -303,12 +316,35 @@ struct SbView {
     const float* v;
 };
 
+// Row product with three block columns in flight per step: the column
+// indices, 27 values and three gathers of a step are independent loads, so
+// their latencies overlap instead of forming one 27-long dependent chain.
 __device__ __forceinline__ void sb_row(const SbView& A, int row, const float4* __restrict__ x, float (&y)[3]) {
     y[0] = y[1] = y[2] = 0.f;
     const int lane = row & 31;
     const int64_t g0 = A.slice_off[row >> 5];
     const int len = A.row_len[row];
-    for (int j = 0; j < len; ++j) {
+    int j = 0;
+    for (; j + 3 <= len; j += 3) {
+        const int64_t g = g0 + j;
+        int c[3];
+        float m[3][9];
+#pragma unroll
+        for (int u = 0; u < 3; ++u) c[u] = A.col[(g + u) * 32 + lane];
+#pragma unroll
+        for (int u = 0; u < 3; ++u)
+#pragma unroll
+            for (int q = 0; q < 9; ++q) m[u][q] = A.v[((g + u) * 9 + q) * 32 + lane];
+        float4 p[3];
+#pragma unroll
+        for (int u = 0; u < 3; ++u) p[u] = x[c[u]];
+#pragma unroll
+        for (int u = 0; u < 3; ++u)
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                y[a] = fmaf(m[u][a * 3], p[u].x, fmaf(m[u][a * 3 + 1], p[u].y, fmaf(m[u][a * 3 + 2], p[u].z, y[a])));
+    }
+    for (; j < len; ++j) {
         const int64_t g = g0 + j;
         const int c = A.col[g * 32 + lane];
         const float* v = A.v + (g * 9) * 32 + lane;
@@ -437,19 +473,60 @@ __global__ void k_vc_prolong(LevelView cv, int fnx, int fny, int fnz, const floa
     xf[f] = acc;
 }
 
-__global__ void k_vc_dense(int n, const float* __restrict__ ainv, const float* __restrict__ b, float4* __restrict__ y,
-                           const Control* ctl) {
+// Coarsest solve y = A_c^-1 b: one warp per row, lanes stride the row
+// (coalesced), shuffle reduction.  y is node-padded (4 floats per node).
+__global__ void __launch_bounds__(1024) k_vc_dense(int n, const float* __restrict__ ainv, const float* __restrict__ b,
+                                                   float* __restrict__ y4, const Control* ctl) {
     if (ctl && ctl->all_done) return;
     __shared__ float sb[1024];
     for (int i = threadIdx.x; i < n; i += blockDim.x) sb[i] = b[i];
     __syncthreads();
-    for (int node = threadIdx.x; node < n / 3; node += blockDim.x) {
-        float acc[3] = {0.f, 0.f, 0.f};
-        for (int a = 0; a < 3; ++a) {
-            const float* row = ainv + (size_t)(3 * node + a) * n;
-            for (int j = 0; j < n; ++j) acc[a] += row[j] * sb[j];
-        }
-        y[node] = make_float4(acc[0], acc[1], acc[2], 0.f);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int row = warp; row < n; row += nw) {
+        const float* ar = ainv + (size_t)row * n;
+        float acc = 0.f;
+        for (int j = lane; j < n; j += 32) acc = fmaf(ar[j], sb[j], acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) y4[4 * (row / 3) + row % 3] = acc;
+    }
+}
+
+// Separable trilinear restriction, one axis per pass (z, then y, then x):
+// out[o] = sum_f w(f, m) in[f] along axis AX, m the output index on that
+// axis; output dims d0 x d1 x d2 (nodes), input extent in_n along AX.  The
+// last (x) pass writes the coarse right-hand side and, fused, the coarse
+// level's first smoothing sweep x4 = B^-1 b.
+template <int AX>
+__global__ void k_vc_restrict_axis(int d0, int d1, int d2, int in_n, const int32_t* __restrict__ xs,
+                                   const int32_t* __restrict__ lo, const float* __restrict__ w, int n_c,
+                                   const float* __restrict__ in, float* __restrict__ out,
+                                   const float* __restrict__ binv, float4* __restrict__ x4, const Control* ctl) {
+    if (ctl && ctl->all_done) return;
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= d0 * d1 * d2) return;
+    const int i0 = o / (d1 * d2), i1 = (o / d2) % d1, i2 = o % d2;
+    const int m = (AX == 0) ? i0 : (AX == 1) ? i1 : i2;
+    const int f_lo = xs[max(m - 1, 0)], f_hi = xs[min(m + 1, n_c)];
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    for (int f = f_lo; f <= f_hi; ++f) {
+        const float wf = (lo[f] == m) ? 1.f - w[f] : ((lo[f] + 1 == m) ? w[f] : 0.f);
+        if (wf == 0.f) continue;
+        int src;
+        if (AX == 0) src = (f * d1 + i1) * d2 + i2;
+        else if (AX == 1) src = (i0 * in_n + f) * d2 + i2;
+        else src = (i0 * d1 + i1) * in_n + f;
+        s0 = fmaf(wf, in[3 * src], s0);
+        s1 = fmaf(wf, in[3 * src + 1], s1);
+        s2 = fmaf(wf, in[3 * src + 2], s2);
+    }
+    out[3 * o] = s0;
+    out[3 * o + 1] = s1;
+    out[3 * o + 2] = s2;
+    if (AX == 0 && binv) {
+        const float* B = binv + 9 * (size_t)o;
+        x4[o] = make_float4(B[0] * s0 + B[1] * s1 + B[2] * s2, B[3] * s0 + B[4] * s1 + B[5] * s2,
+                            B[6] * s0 + B[7] * s1 + B[8] * s2, 0.f);
     }
 }
 
@@ -457,10 +534,19 @@ __global__ void k_vc_dense(int n, const float* __restrict__ ainv, const float* _
 // multigrid-preconditioned flexible CG kernels (one right-hand side)
 // ---------------------------------------------------------------------------
 struct MgPcg {
-    PcgArgs a;        // outer operator, x, r, p, ap, partials, sc, ctl (nrhs = 1)
-    float* b0;        // V-cycle input (level-0 rhs, FP32 r)
-    const float4* z;  // V-cycle output (level-0 y4)
+    PcgArgs a;            // outer operator, x, r, p, ap, partials, sc, ctl (nrhs = 1)
+    float* b0;            // V-cycle input (level-0 rhs, FP32 r)
+    const float4* z;      // V-cycle output (level-0 y4)
+    const float* binv0;   // level-0 smoother blocks: the first sweep
+    float4* x40;          // x4 = B^-1 r is fused into the kernels writing b0
 };
+
+__device__ __forceinline__ void fused_smooth0(const MgPcg& M, int row, const double (&r)[3]) {
+    const float* B = M.binv0 + 9 * (size_t)row;
+    const float r0 = (float)r[0], r1 = (float)r[1], r2 = (float)r[2];
+    M.x40[row] = make_float4(B[0] * r0 + B[1] * r1 + B[2] * r2, B[3] * r0 + B[4] * r1 + B[5] * r2,
+                             B[6] * r0 + B[7] * r1 + B[8] * r2, 0.f);
+}
 
 template <typename TV, typename TP>
 __global__ void __launch_bounds__(kThreads) k_mg_spmv_dot(MgPcg M) {
@@ -501,6 +587,7 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_xr(MgPcg M) {
         TP pv[3];
         PadVec<TP>::load(A.p, row, pv);
         const TP* ap = reinterpret_cast<const TP*>(A.ap) + 3 * (size_t)row;
+        double rr[3];
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             const size_t o = 3 * (size_t)row + q;
@@ -508,8 +595,10 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_xr(MgPcg M) {
             const double rv = A.r[o] - alpha * (double)ap[q];
             A.r[o] = rv;
             M.b0[o] = (float)rv;
+            rr[q] = rv;
             d[0][0] += rv * rv;
         }
+        fused_smooth0(M, row, rr);
     }
     double tot[1][1];
     if (last_block_reduce<1, 1>(A, d, 1, tot) && threadIdx.x == 0) {
@@ -591,15 +680,18 @@ __global__ void __launch_bounds__(kThreads) k_mg_residual(MgPcg M, int init, dou
 #pragma unroll
             for (int a = 0; a < 3; ++a) y[a] = fma(v[(a * 3) * 32], x0, fma(v[(a * 3 + 1) * 32], x1, fma(v[(a * 3 + 2) * 32], x2, y[a])));
         }
+        double rr[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const size_t o = 3 * (size_t)row + a;
             const double rv = A.f[o] - y[a];
             A.r[o] = rv;
             M.b0[o] = (float)rv;
+            rr[a] = rv;
             d[0][0] += rv * rv;
             d[0][1] += A.f[o] * A.f[o];
         }
+        fused_smooth0(M, row, rr);
     }
     double tot[1][2];
     if (last_block_reduce<1, 2>(A, d, 3, tot) && threadIdx.x == 0) {
@@ -800,6 +892,8 @@ void build_hierarchy(Ctx& c) {
                 }
         level_pattern(c, *L);
         L->Ke.alloc((size_t)L->n_el * 576);
+        L->t1.alloc((size_t)3 * (F.nx + 1) * (F.ny + 1) * (L->nz + 1));
+        L->t2.alloc((size_t)3 * (F.nx + 1) * (L->ny + 1) * (L->nz + 1));
         H->L.push_back(std::move(L));
     }
     for (auto& Lp : H->L) {
@@ -832,7 +926,7 @@ void setup_values(Ctx& c) {
     for (size_t l = 1; l < H.L.size(); ++l) {
         MgLevel& L = *H.L[l];
         MgLevel& F = *H.L[l - 1];
-        k_coarsen<<<L.n_el, 256, 0, c.stream>>>(view_of(L), F.ny, F.nz, l == 1 ? nullptr : F.Ke.p, c.d_xyz.p,
+        k_coarsen<<<L.n_el, 512, 0, c.stream>>>(view_of(L), F.ny, F.nz, l == 1 ? nullptr : F.Ke.p, c.d_xyz.p,
                                                 c.d_conn.p, c.d_E.p, c.d_nu.p, L.Ke.p);
         L.own.v32.zero(c.stream);
         for (size_t k = 0; k + 1 < L.colour_ptr.size(); ++k) {
@@ -851,27 +945,46 @@ void setup_values(Ctx& c) {
     MgLevel& Lc = *H.L.back();
     k_dense_build<<<Lc.n_nodes, 128, 0, c.stream>>>(Lc.n_nodes, Lc.A->slice_off.p, Lc.A->row_len.p, Lc.A->col.p,
                                                     Lc.A->v32.p, H.dense.p);
-    k_gauss_jordan<<<1, 1024, 0, c.stream>>>(H.n_coarse, H.dense.p);
+    const size_t gj_smem = sizeof(float) * (size_t)H.n_coarse * H.n_coarse;
+    const bool in_smem = gj_smem <= 220 * 1024;
+    if (in_smem)
+        ASEND_CUDA(cudaFuncSetAttribute(k_gauss_jordan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gj_smem));
+    k_gauss_jordan<<<1, 1024, in_smem ? gj_smem : 0, c.stream>>>(H.n_coarse, H.dense.p, in_smem ? 1 : 0);
     c.launches += 2;
     ASEND_CUDA(cudaGetLastError());
     H.epoch = c.assembly_epoch;
 }
 
 // z = V-cycle(b0) (levels' b of level 0 must hold the input)
-void vcycle(Ctx& c, const Control* ctl) {
+// One V(1,1) cycle on level 0's b.  With fused0, the caller has already
+// written level 0's first sweep x4 = B^-1 b (fused into the PCG update).
+void vcycle(Ctx& c, const Control* ctl, bool fused0) {
     MgHierarchy& H = *c.mg;
     const int nl = (int)H.L.size();
+    if (!fused0 && nl > 1) {
+        MgLevel& L = *H.L[0];
+        k_vc_smooth0<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(L.n_nodes, L.binv.p, L.b.p,
+                                                              reinterpret_cast<float4*>(L.x4.p), ctl);
+    }
     for (int l = 0; l < nl - 1; ++l) {
         MgLevel& L = *H.L[l];
         MgLevel& C = *H.L[l + 1];
-        k_vc_smooth0<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(L.n_nodes, L.binv.p, L.b.p,
-                                                              reinterpret_cast<float4*>(L.x4.p), ctl);
         k_vc_resid<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(sbview(L), L.b.p, reinterpret_cast<float4*>(L.x4.p), L.r.p,
                                                             ctl);
-        k_vc_restrict<<<grid_of(C.n_nodes), kT, 0, c.stream>>>(view_of(C), L.ny, L.nz, L.r.p, C.b.p, ctl);
+        const bool last = (l + 1 == nl - 1);  // the coarsest level is solved directly: no sweep
+        const int n1 = (L.nx + 1) * (L.ny + 1) * (C.nz + 1), n2 = (L.nx + 1) * (C.ny + 1) * (C.nz + 1);
+        k_vc_restrict_axis<2><<<grid_of(n1), kT, 0, c.stream>>>(
+            L.nx + 1, L.ny + 1, C.nz + 1, L.nz + 1, C.d_xs.p + C.ox[2], C.d_lo.p + C.ol[2], C.d_w.p + C.ol[2], C.nz,
+            L.r.p, C.t1.p, nullptr, nullptr, ctl);
+        k_vc_restrict_axis<1><<<grid_of(n2), kT, 0, c.stream>>>(
+            L.nx + 1, C.ny + 1, C.nz + 1, L.ny + 1, C.d_xs.p + C.ox[1], C.d_lo.p + C.ol[1], C.d_w.p + C.ol[1], C.ny,
+            C.t1.p, C.t2.p, nullptr, nullptr, ctl);
+        k_vc_restrict_axis<0><<<grid_of(C.n_nodes), kT, 0, c.stream>>>(
+            C.nx + 1, C.ny + 1, C.nz + 1, L.nx + 1, C.d_xs.p + C.ox[0], C.d_lo.p + C.ol[0], C.d_w.p + C.ol[0], C.nx,
+            C.t2.p, C.b.p, last ? nullptr : C.binv.p, reinterpret_cast<float4*>(C.x4.p), ctl);
     }
     MgLevel& Lc = *H.L.back();
-    k_vc_dense<<<1, 256, 0, c.stream>>>(H.n_coarse, H.dense.p, Lc.b.p, reinterpret_cast<float4*>(Lc.y4.p), ctl);
+    k_vc_dense<<<1, 1024, 0, c.stream>>>(H.n_coarse, H.dense.p, Lc.b.p, Lc.y4.p, ctl);
     for (int l = nl - 2; l >= 0; --l) {
         MgLevel& L = *H.L[l];
         MgLevel& C = *H.L[l + 1];
@@ -884,7 +997,7 @@ void vcycle(Ctx& c, const Control* ctl) {
     }
 }
 
-int vcycle_launches(const MgHierarchy& H) { return 5 * ((int)H.L.size() - 1) + 1; }
+int vcycle_launches(const MgHierarchy& H) { return 6 * ((int)H.L.size() - 1) + 1; }
 
 }  // namespace
 
@@ -897,7 +1010,7 @@ void mg_apply(Ctx& c, const float* d_b, float* d_z4) {
     mg_prepare(c);
     MgLevel& L0 = *c.mg->L[0];
     ASEND_CUDA(cudaMemcpyAsync(L0.b.p, d_b, sizeof(float) * c.n_dof, cudaMemcpyDeviceToDevice, c.stream));
-    vcycle(c, nullptr);
+    vcycle(c, nullptr, false);
     ASEND_CUDA(cudaMemcpyAsync(d_z4, L0.y4.p, sizeof(float) * 4 * c.n_nodes, cudaMemcpyDeviceToDevice, c.stream));
     c.launches += vcycle_launches(*c.mg);
 }
@@ -954,6 +1067,8 @@ int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool 
         a.ctl = d_ctl.p;
         M.b0 = L0.b.p;
         M.z = reinterpret_cast<const float4*>(L0.y4.p);
+        M.binv0 = L0.binv.p;
+        M.x40 = reinterpret_cast<float4*>(L0.x4.p);
         d_sc.zero(c.stream);
         d_ctl.zero(c.stream);
         auto launch_residual = [&](int init) {
@@ -965,7 +1080,7 @@ int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool 
             else k_mg_spmv_dot<double, double><<<grid, kThreads, 0, c.stream>>>(M);
             if (mixed) k_mg_update_xr<float><<<grid, kThreads, 0, c.stream>>>(M);
             else k_mg_update_xr<double><<<grid, kThreads, 0, c.stream>>>(M);
-            vcycle(c, a.ctl);
+            vcycle(c, a.ctl, true);
             if (mixed) {
                 k_mg_rz<float><<<grid, kThreads, 0, c.stream>>>(M, 0);
                 k_mg_update_p<float><<<grid, kThreads, 0, c.stream>>>(M);
@@ -975,7 +1090,7 @@ int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool 
             }
         };
         auto launch_start = [&](int mode) {  // V-cycle on the current b0, then p = z / rz
-            vcycle(c, nullptr);
+            vcycle(c, nullptr, true);
             if (mixed) k_mg_rz<float><<<grid, kThreads, 0, c.stream>>>(M, mode);
             else k_mg_rz<double><<<grid, kThreads, 0, c.stream>>>(M, mode);
             c.launches += vcycle_launches(H) + 1;

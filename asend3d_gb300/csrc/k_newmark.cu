@@ -98,7 +98,8 @@ int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* am
     {
         const int nrow_c = (int)c.c_rhs.size();
         for (int q = 0; q < nrow_c; ++q)
-            for (int k = c.c_ptr[q]; k < c.c_ptr[q + 1]; ++k) pen[c.c_dof[k]] += c.c_coef[k] * c.sf * c.c_rhs[q];
+            for (int k = c.c_ptr[q]; k < c.c_ptr[q + 1]; ++k)
+                pen[c.c_dof[k]] += c.c_coef[k] * row_penalty_scale(c, q) * c.c_rhs[q];
     }
     DArr<double> d_f0, d_pen, u, v, a, up, vp, ap, du, rhs, hist;
     d_f0.upload(c.loads.empty() ? std::vector<double>(n, 0.0) : c.loads[0], c.stream);

@@ -41,7 +41,8 @@ using namespace pcg;
 // K_a: Ap = A p, pAp; alpha = rz / pAp.
 template <typename TV, typename TP, int NR>
 __global__ void __launch_bounds__(kThreads) k_spmv_dot(PcgArgs A) {
-    if (A.ctl->all_done) return;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (cta_done<NR>(A, S)) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     double d[NR][1];
 #pragma unroll
@@ -67,7 +68,7 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(PcgArgs A) {
     if (last_block_reduce<NR, 1>(A, d, 0, tot) && threadIdx.x == 0) {
 #pragma unroll
         for (int k = 0; k < NR; ++k) {
-            RhsScalars& s = A.sc[k];
+            RhsScalars& s = S[k];
             if (s.done) continue;
             s.pAp = tot[k][0];
             s.alpha = s.rz / s.pAp;
@@ -78,7 +79,8 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(PcgArgs A) {
 // K_b: x += alpha p; r -= alpha Ap; z = M r; dots (r,z), (r,r); beta.
 template <typename TP, int NR, int PC>
 __global__ void __launch_bounds__(kThreads) k_update_xr(PcgArgs A) {
-    if (A.ctl->all_done) return;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (cta_done<NR>(A, S)) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     double d[NR][2];
 #pragma unroll
@@ -86,8 +88,8 @@ __global__ void __launch_bounds__(kThreads) k_update_xr(PcgArgs A) {
     if (row < A.n_rows) {
 #pragma unroll
         for (int k = 0; k < NR; ++k) {
-            if (A.sc[k].done) continue;
-            const double alpha = A.sc[k].alpha;
+            if (S[k].done) continue;
+            const double alpha = S[k].alpha;
             TP pv[3];
             PadVec<TP>::load(A.p, (size_t)k * A.n_rows + row, pv);
             const size_t o = (size_t)k * A.n_dof + 3 * (size_t)row;
@@ -112,7 +114,7 @@ __global__ void __launch_bounds__(kThreads) k_update_xr(PcgArgs A) {
         int all = 1;
 #pragma unroll
         for (int k = 0; k < NR; ++k) {
-            RhsScalars& s = A.sc[k];
+            RhsScalars& s = S[k];
             if (!s.done) {
                 s.rz_new = tot[k][0];
                 s.rr = tot[k][1];
@@ -128,20 +130,21 @@ __global__ void __launch_bounds__(kThreads) k_update_xr(PcgArgs A) {
             }
             all &= s.done;
         }
-        if (all) A.ctl->all_done = 1;
+        if (all && !A.cta_inst) A.ctl->all_done = 1;
     }
 }
 
 // K_c: p = M r + beta p (node-padded store).
 template <typename TP, int NR, int PC>
 __global__ void __launch_bounds__(kThreads) k_update_p(PcgArgs A) {
-    if (A.ctl->all_done) return;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (cta_done<NR>(A, S)) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= A.n_rows) return;
 #pragma unroll
     for (int k = 0; k < NR; ++k) {
-        if (A.sc[k].done) continue;
-        const double beta = A.sc[k].beta;
+        if (S[k].done) continue;
+        const double beta = S[k].beta;
         const size_t o = (size_t)k * A.n_dof + 3 * (size_t)row;
         double rv[3] = {A.r[o], A.r[o + 1], A.r[o + 2]}, z[3];
         precond<PC>(A, row, rv, z);
@@ -159,6 +162,13 @@ __global__ void __launch_bounds__(kThreads) k_update_p(PcgArgs A) {
 // sc.replace set (p kept).
 template <typename TP, int NR, int PC>
 __global__ void __launch_bounds__(kThreads) k_residual(PcgArgs A, int mode, double tol2) {
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (mode == 1 && A.cta_inst) {  // nothing to replace in this instance
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < NR; ++k) any |= (S[k].replace != 0);
+        if (!any) return;
+    }
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = row & 31;
     double d[NR][3];
@@ -187,7 +197,7 @@ __global__ void __launch_bounds__(kThreads) k_residual(PcgArgs A, int mode, doub
         }
 #pragma unroll
         for (int k = 0; k < NR; ++k) {
-            if (mode == 1 && !A.sc[k].replace) continue;
+            if (mode == 1 && !S[k].replace) continue;
             const size_t o = (size_t)k * A.n_dof + 3 * (size_t)row;
             double rv[3], z[3];
 #pragma unroll
@@ -210,7 +220,7 @@ __global__ void __launch_bounds__(kThreads) k_residual(PcgArgs A, int mode, doub
         int all = 1;
 #pragma unroll
         for (int k = 0; k < NR; ++k) {
-            RhsScalars& s = A.sc[k];
+            RhsScalars& s = S[k];
             if (mode == 0 || s.replace) {
                 s.rz = tot[k][0];
                 s.rr = tot[k][1];
@@ -228,7 +238,7 @@ __global__ void __launch_bounds__(kThreads) k_residual(PcgArgs A, int mode, doub
             }
             all &= s.done;
         }
-        A.ctl->all_done = all;
+        if (!A.cta_inst) A.ctl->all_done = all;
     }
 }
 
@@ -466,12 +476,17 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
         c.d_p64.alloc((size_t)kMaxRhs * 4 * n);
         c.d_ap64.alloc((size_t)kMaxRhs * nd);
     }
+    // independent instances: one scalar set per (instance, load case)
+    const int NI = c.n_inst > 1 ? c.n_inst : 1;
     DArr<RhsScalars> d_sc;
     DArr<Control> d_ctl;
-    d_sc.alloc(kMaxRhs);
+    DArr<uint32_t> d_tk;
+    d_sc.alloc((size_t)NI * kMaxRhs);
     d_ctl.alloc(1);
+    if (NI > 1) d_tk.alloc((size_t)NI * 4);
+    ensure_pinned_scalars(c, sizeof(RhsScalars) * NI * kMaxRhs);
     RhsScalars* h_sc = reinterpret_cast<RhsScalars*>(c.h_sc);
-    static_assert(sizeof(RhsScalars) * kMaxRhs <= sizeof(PcgScalars) * 64, "pinned scalar mirror too small");
+    const size_t sc_bytes = sizeof(RhsScalars) * NI * kMaxRhs;
     int iters_max = 0, repl_total = 0, status = 0;
     double relres_max = 0.0;
     ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
@@ -497,6 +512,13 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
         a.partials = c.d_partials.p;
         a.sc = d_sc.p;
         a.ctl = d_ctl.p;
+        if (NI > 1) {
+            a.cta_inst = c.d_cta_inst.p;
+            a.inst_cta0 = c.d_inst_cta0.p;
+            a.inst_ncta = c.d_inst_ncta.p;
+            a.tickets = d_tk.p;
+            d_tk.zero(c.stream);
+        }
         d_sc.zero(c.stream);
         d_ctl.zero(c.stream);
         L.residual(0, o.rel_tol * o.rel_tol);
@@ -511,12 +533,13 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
         ASEND_CUDA(cudaGraphDestroy(graph));
         int since_repl = 0;
         for (;;) {
-            ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc.p, sizeof(RhsScalars) * nr, cudaMemcpyDeviceToHost, c.stream));
+            ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc.p, sc_bytes, cudaMemcpyDeviceToHost, c.stream));
             ASEND_CUDA(cudaStreamSynchronize(c.stream));
             bool all_finished = true, any_replace = false, any_nonfinite = false;
             int it_now = 0;
-            for (int k = 0; k < nr; ++k) {
-                RhsScalars& s = h_sc[k];
+            for (int q = 0; q < NI * kMaxRhs; ++q) {
+                if (q % kMaxRhs >= nr) continue;
+                RhsScalars& s = h_sc[q];
                 it_now = std::max(it_now, (int)s.iter);
                 if (s.nonfinite) { any_nonfinite = true; continue; }
                 if (s.finished) continue;
@@ -533,7 +556,7 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
             if (all_finished) break;
             if (it_now >= max_it) { status = std::max(status, (int)ASEND_MAX_ITER); break; }
             if (any_replace) {
-                ASEND_CUDA(cudaMemcpyAsync(d_sc.p, h_sc, sizeof(RhsScalars) * nr, cudaMemcpyHostToDevice, c.stream));
+                ASEND_CUDA(cudaMemcpyAsync(d_sc.p, h_sc, sc_bytes, cudaMemcpyHostToDevice, c.stream));
                 L.residual(1, 0.0);
                 ++repl_total;
                 since_repl = 0;
@@ -544,14 +567,16 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
             since_repl += G;
         }
         ASEND_CUDA(cudaGraphExecDestroy(exec));
-        ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc.p, sizeof(RhsScalars) * nr, cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc.p, sc_bytes, cudaMemcpyDeviceToHost, c.stream));
         ASEND_CUDA(cudaStreamSynchronize(c.stream));
-        for (int k = 0; k < nr; ++k) {
-            iters_max = std::max(iters_max, (int)h_sc[k].iter);
-            const double rel = h_sc[k].bb > 0 ? std::sqrt(h_sc[k].rr_last_true / h_sc[k].bb) : std::sqrt(h_sc[k].rr_last_true);
-            relres_max = std::max(relres_max, rel);
-            if (h_sc[k].nonfinite) status = ASEND_NONFINITE;
-            else if (!h_sc[k].finished) status = std::max(status, (int)ASEND_MAX_ITER);
+        for (int q = 0; q < NI * kMaxRhs; ++q) {
+            if (q % kMaxRhs >= nr) continue;
+            const RhsScalars& s = h_sc[q];
+            iters_max = std::max(iters_max, (int)s.iter);
+            if (s.bb == 0.0) continue;  // empty load case of this instance
+            relres_max = std::max(relres_max, std::sqrt(s.rr_last_true / s.bb));
+            if (s.nonfinite) status = ASEND_NONFINITE;
+            else if (!s.finished) status = std::max(status, (int)ASEND_MAX_ITER);
         }
     }
     ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));

@@ -34,9 +34,31 @@ struct PcgArgs {
     const double* dinv;
     const float* binv;
     double* partials;  // [gridDim.x][kMaxRhs][3]
-    RhsScalars* sc;
+    RhsScalars* sc;    // [n_inst][kMaxRhs]
     Control* ctl;
+    // Independent instances (disconnected sub-systems stacked in one
+    // operator, each starting on a CTA boundary): CTA -> instance map, first
+    // CTA and CTA count per instance, 4 reduction tickets per instance.
+    // nullptr = a single instance spanning the whole grid.
+    const int32_t* cta_inst;
+    const int32_t* inst_cta0;
+    const int32_t* inst_ncta;
+    uint32_t* tickets;
 };
+
+__device__ __forceinline__ int cta_instance(const PcgArgs& A) { return A.cta_inst ? A.cta_inst[blockIdx.x] : 0; }
+
+// True when this CTA has nothing left to do: everything converged (single
+// instance) or every right-hand side of the CTA's instance is done.
+template <int NR>
+__device__ __forceinline__ bool cta_done(const PcgArgs& A, const RhsScalars* S) {
+    if (A.ctl->all_done) return true;
+    if (!A.cta_inst) return false;
+#pragma unroll
+    for (int k = 0; k < NR; ++k)
+        if (!S[k].done) return false;
+    return true;
+}
 
 template <typename TP>
 struct PadVec;
@@ -73,7 +95,31 @@ __device__ __forceinline__ void spmv_row(int row, const PcgArgs& A, const TV* __
     const int lane = row & 31;
     const int64_t g0 = A.slice_off[row >> 5];
     const int len = A.row_len[row];
-    for (int j = 0; j < len; ++j) {
+    int j = 0;
+    if constexpr (NR == 1) {
+        // three block columns in flight per step (independent loads overlap)
+        for (; j + 3 <= len; j += 3) {
+            const int64_t g = g0 + j;
+            int c[3];
+            TV m[3][9];
+#pragma unroll
+            for (int u = 0; u < 3; ++u) c[u] = A.col[(g + u) * 32 + lane];
+#pragma unroll
+            for (int u = 0; u < 3; ++u)
+#pragma unroll
+                for (int q = 0; q < 9; ++q) m[u][q] = vals[((g + u) * 9 + q) * 32 + lane];
+            TP pv[3][3];
+#pragma unroll
+            for (int u = 0; u < 3; ++u) PadVec<TP>::load(p, (size_t)c[u], pv[u]);
+#pragma unroll
+            for (int u = 0; u < 3; ++u)
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                    y[0][a] = fma((TP)m[u][a * 3 + 0], pv[u][0],
+                                  fma((TP)m[u][a * 3 + 1], pv[u][1], fma((TP)m[u][a * 3 + 2], pv[u][2], y[0][a])));
+        }
+    }
+    for (; j < len; ++j) {
         const int64_t g = g0 + j;
         const int c = A.col[g * 32 + lane];
         const TV* v = vals + (g * 9) * 32 + lane;
@@ -118,12 +164,17 @@ __device__ __forceinline__ bool last_block_reduce(const PcgArgs& A, double (&val
 #pragma unroll
         for (int v = 0; v < NV; ++v) flat[k * NV + v] = val[k][v];
     block_sum<NR * NV>(flat, sm);
+    // the CTAs of this CTA's instance reduce together (whole grid if single)
+    const int inst = cta_instance(A);
+    const int b0 = A.cta_inst ? A.inst_cta0[inst] : 0;
+    const int nb = A.cta_inst ? A.inst_ncta[inst] : (int)gridDim.x;
+    uint32_t* ticket = A.tickets ? &A.tickets[inst * 4 + ticket_id] : &A.ctl->ticket[ticket_id];
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int q = 0; q < NR * NV; ++q) A.partials[(size_t)blockIdx.x * (kMaxRhs * 3) + q] = flat[q];
         __threadfence();
-        const uint32_t t = atomicAdd(&A.ctl->ticket[ticket_id], 1u);
-        is_last = (t == gridDim.x - 1);
+        const uint32_t t = atomicAdd(ticket, 1u);
+        is_last = (t == (uint32_t)nb - 1);
     }
     __syncthreads();
     if (!is_last) return false;
@@ -131,7 +182,7 @@ __device__ __forceinline__ bool last_block_reduce(const PcgArgs& A, double (&val
     double acc[NR * NV];
 #pragma unroll
     for (int q = 0; q < NR * NV; ++q) acc[q] = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+    for (int b = b0 + threadIdx.x; b < b0 + nb; b += blockDim.x) {
         const volatile double* pp = A.partials + (size_t)b * (kMaxRhs * 3);
 #pragma unroll
         for (int q = 0; q < NR * NV; ++q) acc[q] += pp[q];
@@ -141,7 +192,7 @@ __device__ __forceinline__ bool last_block_reduce(const PcgArgs& A, double (&val
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int q = 0; q < NR * NV; ++q) sm[q] = acc[q];
-        A.ctl->ticket[ticket_id] = 0;
+        *ticket = 0;
     }
     __syncthreads();
 #pragma unroll

@@ -79,7 +79,7 @@ class Problem:
 class GpuSolver:
     """One library context (one CUDA stream) holding one problem."""
 
-    def __init__(self, problem: Problem, device: int = 0):
+    def __init__(self, problem: Problem, device: int = 0, instances=None):
         self.lib = _lib.load()
         self.ctx = self.lib.asend_create(device)
         if not self.ctx:
@@ -87,6 +87,7 @@ class GpuSolver:
         self.p = problem
         self.set_ids = {}
         self.elset_ids = {}
+        self.instances = None if instances is None else np.ascontiguousarray(instances, dtype=np.int32)
         self._setup()
 
     # -- helpers -----------------------------------------------------------
@@ -135,6 +136,9 @@ class GpuSolver:
             self._check(self.lib.asend_add_constraint(self.ctx, len(terms), _ptr(sets, C.c_int32),
                                                       _ptr(comps, C.c_int32), _ptr(coefs, C.c_double), rhs),
                         "add_constraint")
+        if self.instances is not None:  # validated against elements and constraints
+            self._check(self.lib.asend_set_instances(self.ctx, len(self.instances) - 1,
+                                                     _ptr(self.instances, C.c_int32)), "set_instances")
         self.set_loads()
         obj = p.objective
         if obj[0] == "compliance":
@@ -276,3 +280,52 @@ class GpuSolver:
     @property
     def kernel_launches(self) -> int:
         return int(self.lib.asend_kernel_launches(self.ctx))
+
+
+def combine(problems, align: int = 128):
+    """Stack independent problems into one (disconnected) problem for a batched
+    solve.  Instance i's nodes start at node_ptr[i], a multiple of ``align``
+    (padding nodes carry no element and stay zero); node/element set names get
+    the suffix ``@i``; load case k of the result holds every instance's case k.
+    Returns (problem, node_ptr, elem_ptr)."""
+    node_ptr, elem_ptr = [0], [0]
+    for p in problems:
+        n = p.mesh.n_nodes
+        node_ptr.append(node_ptr[-1] + ((n + align - 1) // align) * align)
+        elem_ptr.append(elem_ptr[-1] + p.mesh.n_elems)
+    node_ptr[-1] = node_ptr[-2] + problems[-1].mesh.n_nodes  # no padding after the last instance
+    n_nodes = node_ptr[-1]
+    coords = np.zeros((n_nodes, 3))
+    conn = np.zeros((elem_ptr[-1], problems[0].mesh.conn.shape[1]), dtype=np.int32)
+    E = np.zeros(elem_ptr[-1])
+    nu = np.zeros(elem_ptr[-1])
+    rho = np.zeros(elem_ptr[-1])
+    out_sets, out_elsets, cons = {}, {}, []
+    n_cases = max(len(p.loads) for p in problems)
+    loads = [[] for _ in range(n_cases)]
+    for i, p in enumerate(problems):
+        m, o, eo = p.mesh, node_ptr[i], elem_ptr[i]
+        coords[o:o + m.n_nodes] = m.coords
+        conn[eo:eo + m.n_elems] = m.conn + o
+        E[eo:eo + m.n_elems] = p.E
+        nu[eo:eo + m.n_elems] = np.broadcast_to(p.nu, p.E.shape)
+        rho[eo:eo + m.n_elems] = 0.0 if p.rho is None else np.broadcast_to(p.rho, p.E.shape)
+        for name, s in p.node_sets.items():
+            out_sets[f"{name}@{i}"] = np.asarray(s, dtype=np.int32) + o
+        for name, s in p.elem_sets.items():
+            out_elsets[f"{name}@{i}"] = np.asarray(s, dtype=np.int32) + eo
+        for terms, q in p.constraints:
+            cons.append(([(f"{t[0]}@{i}", t[1], t[2]) for t in terms], q))
+        for k, items in enumerate(p.loads):
+            for it in items:
+                if it[0] == "nodalForce":
+                    loads[k].append(("nodalForce", f"{it[1]}@{i}", it[2]))
+                elif it[0] == "surfaceTraction":
+                    loads[k].append(("surfaceTraction", f"{it[1]}@{i}", it[2], it[3], it[4]))
+                else:
+                    f = np.zeros(3 * n_nodes)
+                    f[3 * o:3 * o + 3 * m.n_nodes] = it[1]
+                    loads[k].append(("vector", f))
+    mesh = BlockMesh(0, 0, 0, 0.0, 0.0, 0.0, coords, conn, elem_type=problems[0].mesh.elem_type)
+    prob = Problem(mesh, E, nu, rho, out_sets, out_elsets, cons, loads, ("compliance",))
+    return prob, np.array(node_ptr, dtype=np.int32), np.array(elem_ptr, dtype=np.int32)

@@ -51,7 +51,95 @@ def parse():
     ap.add_argument("--nz", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-nx", type=int, default=40)
+    ap.add_argument("--profile", action="store_true",
+                    help="short run for ncu: one assembly, one multigrid solve, three FP32 SpMV launches")
+    ap.add_argument("--workload", default="block_large", choices=["block_large", "batch_uq"],
+                    help="block_large (default, the benchmark line) or batch_uq (64 uneven instances x 4 cases)")
     return ap.parse_args()
+
+
+def run_batch(a):
+    """64 uneven cantilevers x 4 load cases, one batched block-Jacobi PCG
+    launch sequence per iteration (captured in CUDA graphs) + compliance
+    gradients; compared with plain FP64 Jacobi PCG run instance by instance
+    and load case by load case."""
+    import ctypes as C
+
+    import torch
+
+    from asend3d_gb300 import _lib, configs
+    from asend3d_gb300.solver import GpuSolver
+
+    prob, node_ptr, elem_ptr, inst = configs.batch_uq(64)
+    g = GpuSolver(prob, instances=node_ptr)
+    stream = torch.cuda.ExternalStream(g.stream)
+    n_real = sum(p.mesh.n_dof for p in inst)
+    n_cases = len(prob.loads)
+    best = dict(method=_lib.METHOD_FP64, precond=_lib.PC_BLOCK, rel_tol=1e-8, graph_iters=32)
+    o_adj = g.opts(**best)
+
+    def step():
+        g.assemble(precision=64)
+        rc, st = g.static_solve_device(**best)
+        Lc = C.c_double(0)
+        s2 = _lib.SolveStats()
+        rc2 = g.lib.asend_adjoint_gradient(g.ctx, C.byref(o_adj), C.byref(Lc), None, C.byref(s2))
+        return rc, rc2, st
+
+    for _ in range(a.warmup):
+        rc, rc2, st = step()
+        assert rc == 0 and rc2 == 0, st
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        for _ in range(a.steps):
+            rc, rc2, st = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / a.steps
+    value = n_real * n_cases / (ms / 1e3)
+    # plain: FP64 point-Jacobi PCG, one instance and one load case at a time
+    plain = dict(method=_lib.METHOD_FP64, precond=_lib.PC_JACOBI, rel_tol=1e-8, graph_iters=32)
+    t_plain = 0.0
+    it_plain = 0
+    for p in inst:
+        for k in range(n_cases):
+            q = type(p)(p.mesh, p.E, p.nu, p.rho, p.node_sets, p.elem_sets, p.constraints, [p.loads[k]],
+                        ("compliance",))
+            gi = GpuSolver(q)
+            gi.assemble(precision=64)
+            rc, sti = gi.static_solve_device(**plain)
+            t_plain += sti["ms_solve"] + sti["ms_assemble"]
+            it_plain = max(it_plain, sti["iterations"])
+            gi.close()
+    plain_value = n_real * n_cases / (t_plain / 1e3)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64 operator/dots, f32 block-Jacobi", "data": "synthetic (seeded lognormal fields)",
+           "config": {"workload": "batch_uq: 64 uneven hex8 cantilevers nx in [20,120], ny=nz in [4,16], 4 load "
+                                  "cases each (256 right-hand sides), batched block-Jacobi PCG + compliance gradient",
+                      "n_dof_total": n_real, "rhs_per_step": 64 * n_cases},
+           "iterations_max": st["iterations"],
+           "plain_fp64_jacobi_sequential": {"value": plain_value, "ms_total": t_plain, "iterations_max": it_plain},
+           "speedup_vs_plain_fp64": value / plain_value, "clocks": clk.summary(), "gpu_launches": None}
+    print(json.dumps(out))
+    g.close()
+
+
+def run_profile(a):
+    """The launch sequence the ncu summaries in profiles/ are taken from."""
+    from asend3d_gb300 import _lib, configs
+    from asend3d_gb300.solver import GpuSolver
+
+    p = configs.block_large(nx=a.nx, ny=a.ny, nz=a.nz)
+    g = GpuSolver(p)
+    g.assemble(precision=64)
+    rc, st = g.static_solve_device(method=_lib.METHOD_FP64, precond=_lib.PC_MG, rel_tol=1e-8)
+    ms, by = g.time_spmv(precision=32, n_launch=3)
+    print(json.dumps({"rc": rc, "iterations": st["iterations"], "ms_solve": st["ms_solve"], "spmv_ms": ms,
+                      "spmv_bytes": by, "launches": g.kernel_launches}))
+    g.close()
 
 
 def dist_env():
@@ -363,7 +451,11 @@ def run_ours(a):
 
 def main():
     a = parse()
-    if a.impl == "reference":
+    if a.profile:
+        run_profile(a)
+    elif a.workload == "batch_uq" and a.impl != "reference":
+        run_batch(a)
+    elif a.impl == "reference":
         run_reference(a)
     else:
         run_ours(a)

@@ -108,6 +108,16 @@ int asend_set_block_structure(asend_ctx* ctx, int32_t nx, int32_t ny, int32_t nz
 /* Number of multigrid levels built so far (0 before the first MG solve). */
 int asend_mg_levels(const asend_ctx* ctx);
 
+/* Batched solves (no counterpart in the single-model reference; it replaces
+ * running the reference's Model::solve once per UQ / design sample): the
+ * mesh is a stack of n_inst independent sub-systems, instance i owning nodes
+ * [node_ptr[i], node_ptr[i+1]).  Each instance must start at a multiple of
+ * 128 nodes (pad with unused nodes, which get a unit diagonal and stay 0)
+ * and no element or constraint may span two instances.  Every PCG kernel
+ * then runs over all instances at once while step lengths, convergence and
+ * stopping are kept per instance and load case. */
+int asend_set_instances(asend_ctx* ctx, int32_t n_inst, const int32_t* node_ptr);
+
 /* Node / element sets (model_input.rs:720-860 'sets' blocks).  Returns the
  * set id (>= 0) or a negative error code. */
 int asend_add_node_set(asend_ctx* ctx, int32_t n, const int32_t* nodes);
