@@ -15,12 +15,14 @@ c_dbl = C.c_double
 P_int = C.POINTER(C.c_int32)
 P_i64 = C.POINTER(C.c_int64)
 P_dbl = C.POINTER(C.c_double)
+P_flt = C.POINTER(C.c_float)
 
 ASEND_OK, ASEND_MAX_ITER, ASEND_NONFINITE, ASEND_FALLBACK = 0, 1, 2, 3
 ASEND_EINVAL, ASEND_ECUDA, ASEND_ESTATE = -1, -2, -3
 METHOD_FP64, METHOD_MIXED = 0, 1
-PC_JACOBI, PC_BLOCK, PC_LEARNED, PC_MG = 0, 1, 2, 3
+PC_JACOBI, PC_BLOCK, PC_LEARNED, PC_MG, PC_MG_LEARNED = 0, 1, 2, 3, 4
 OBJ_DISPLACEMENT, OBJ_COMPLIANCE = 0, 1
+LEARN_BLOCK, LEARN_MG = 0, 1
 
 
 class SolveOpts(C.Structure):
@@ -47,6 +49,9 @@ SIGNATURES = [
     ("asend_set_modulus", c_int, [C.c_void_p, P_dbl]),
     ("asend_set_block_structure", c_int, [C.c_void_p, c_int, c_int, c_int]),
     ("asend_mg_levels", c_int, [C.c_void_p]),
+    ("asend_mg_set_damping", c_int, [C.c_void_p, c_dbl]),
+    ("asend_mg_level_info", c_int, [C.c_void_p, c_int, P_int, P_dbl, P_dbl, P_dbl]),
+    ("asend_mg_vcycle", c_int, [C.c_void_p, P_flt, P_flt]),
     ("asend_set_instances", c_int, [C.c_void_p, c_int, P_int]),
     ("asend_add_node_set", c_int, [C.c_void_p, c_int, P_int]),
     ("asend_add_element_set", c_int, [C.c_void_p, c_int, P_int]),
@@ -75,6 +80,19 @@ SIGNATURES = [
     ("asend_kernel_launches", C.c_int64, [C.c_void_p]),
     ("asend_stream", C.c_void_p, [C.c_void_p]),
     ("asend_operator_energy_noalloc", c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("asend_learned_n_params", c_int, []),
+    ("asend_learned_init", c_int, [C.c_void_p, C.c_uint64]),
+    ("asend_learned_set_params", c_int, [C.c_void_p, P_flt]),
+    ("asend_learned_get_params", c_int, [C.c_void_p, P_flt]),
+    ("asend_learned_add_samples", c_int, [C.c_void_p, c_int, P_int, c_int, C.c_uint64]),
+    ("asend_learned_set_objective", c_int, [C.c_void_p, c_int]),
+    ("asend_learned_set_samples", c_int, [C.c_void_p, c_int, P_flt]),
+    ("asend_learned_train", c_int, [C.c_void_p, c_int, C.c_float, P_dbl]),
+    ("asend_learned_loss_grad", c_int, [C.c_void_p, P_dbl, P_flt]),
+    ("asend_learned_features", c_int, [C.c_void_p, P_flt, P_flt, P_flt]),
+    ("asend_learned_blocks", c_int, [C.c_void_p, c_int, P_flt]),
+    ("asend_learned_forward", c_int, [C.c_void_p, c_int, P_flt, P_flt]),
+    ("asend_learned_backward", c_int, [C.c_void_p, c_int, P_flt, P_flt, P_flt]),
 ]
 
 _lib = None

@@ -13,6 +13,7 @@ No public dataset is involved; every input is generated here from a seed.
                      each, 4 load cases (tip -z, tip +y, torsion couple,
                      uniform end traction).
   learned_grid       128x64x64 hex8 (1.6 M DOF), sigma_log 0.5, corr 0.05 L.
+  learned_patch      training patch with learned_grid's element size.
 """
 from __future__ import annotations
 
@@ -91,6 +92,22 @@ def batch_instance(k: int, seed: int = 7, median=70e9, sigma_log=0.3, corr=0.1, 
 def learned_grid(seed=11, nx=128, ny=64, nz=64, median=70e9, sigma_log=0.5, corr=0.05, nu=0.33) -> Problem:
     m = block_hex8(nx, ny, nz, *BAR)
     E = lognormal_modulus(m, median, sigma_log, corr, seed)
+    p = Problem(m, E, np.full(m.n_elems, nu), np.full(m.n_elems, 2700.0))
+    _fixed_end(p, m)
+    p.add_elem_set("xMaxEls", m.elem_id(nx - 1, *np.meshgrid(np.arange(ny), np.arange(nz), indexing="ij")).ravel())
+    p.add_surface_traction("xMaxEls", (1.0, 0.0, 0.0), (0.0, 0.0, -1.0e6))
+    p.objective = ("compliance",)
+    return p
+
+
+def learned_patch(nx=32, ny=16, nz=16, full=(128, 64, 64), seed=0, median=70e9, sigma_log=0.5,
+                  corr_abs=0.1, nu=0.33) -> Problem:
+    """A smaller block with the element size of the ``full`` grid over the
+    bar, the same supports and load type, and the same absolute correlation
+    length (0.05 of the 2 m bar)."""
+    lx, ly, lz = BAR[0] * nx / full[0], BAR[1] * ny / full[1], BAR[2] * nz / full[2]
+    m = block_hex8(nx, ny, nz, lx, ly, lz)
+    E = lognormal_modulus(m, median, sigma_log, corr_abs / lx, seed)
     p = Problem(m, E, np.full(m.n_elems, nu), np.full(m.n_elems, 2700.0))
     _fixed_end(p, m)
     p.add_elem_set("xMaxEls", m.elem_id(nx - 1, *np.meshgrid(np.arange(ny), np.arange(nz), indexing="ij")).ravel())

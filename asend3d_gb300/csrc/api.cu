@@ -433,6 +433,7 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         c.pattern_ready = c.assembled = c.solved = false;
         c.bx = c.by = c.bz = 0;
         c.mg.reset();
+        learned_mesh_changed(c);
         c.n_inst = 0;
         c.inst_node_ptr.clear();
         c.d_xyz.upload(c.xyz, c.stream);
@@ -515,9 +516,35 @@ int asend_set_instances(asend_ctx* ctx, int32_t n_inst, const int32_t* node_ptr)
     });
 }
 
+int asend_mg_set_damping(asend_ctx* ctx, double factor) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(std::isfinite(factor) && factor > 0.0 && factor < 2.0, "damping factor must be in (0, 2)");
+        c.mg_damping = (float)factor;
+        mg_invalidate_values(c);  // recompute the smoothers at the next solve
+        return ASEND_OK;
+    });
+}
+
 int asend_mg_levels(const asend_ctx* ctx) {
     const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
     return c ? mg_levels(*c) : ASEND_EINVAL;
+}
+
+int asend_mg_level_info(asend_ctx* ctx, int32_t level, int32_t* dims, double* lambda_est, double* lambda_bound,
+                        double* omega) {
+    return guarded(ctx, [&](Ctx& c) {
+        mg_level_info(c, level, dims, lambda_est, lambda_bound, omega);
+        return ASEND_OK;
+    });
+}
+
+int asend_mg_vcycle(asend_ctx* ctx, const float* b, float* z) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(b && z, "null vector");
+        require(c.assembled, "assemble first");
+        mg_vcycle_host(c, b, z);
+        return ASEND_OK;
+    });
 }
 
 int asend_set_modulus(asend_ctx* ctx, const double* E) {
@@ -972,6 +999,129 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
             dLdD_out[i] = s;
         }
         return ndv;
+    });
+}
+
+// ---- learned nodal preconditioner blocks ----------------------------------
+int32_t asend_learned_n_params(void) { return learned_n_params(); }
+
+int asend_learned_init(asend_ctx* ctx, uint64_t seed) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.n_nodes > 0, "set the mesh first");
+        learned_init(c, seed);
+        return ASEND_OK;
+    });
+}
+
+int asend_learned_set_params(asend_ctx* ctx, const float* params) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.n_nodes > 0, "set the mesh first");
+        require(params != nullptr, "null params");
+        for (int i = 0; i < learned_n_params(); ++i) require(std::isfinite(params[i]), "non-finite parameter");
+        learned_set_params(c, params);
+        return ASEND_OK;
+    });
+}
+
+int asend_learned_get_params(asend_ctx* ctx, float* params) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(params != nullptr, "null params");
+        require(learned_ready(c), "no learned weights");
+        learned_get_params(c, params);
+        return ASEND_OK;
+    });
+}
+
+int asend_learned_add_samples(asend_ctx* ctx, int32_t n_samples, const int32_t* iters, int32_t append,
+                              uint64_t seed) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(n_samples > 0 && iters != nullptr, "need at least one sample");
+        require(c.assembled, "assemble first");
+        bool stationary = false;
+        for (int s = 0; s < n_samples; ++s) stationary |= iters[s] < 0;
+        require(!stationary || (c.type == 8 && c.bx > 0), "multigrid samples need a structured hex8 block");
+        learned_add_samples(c, n_samples, iters, append != 0, seed);
+        return ASEND_OK;
+    });
+}
+
+int asend_learned_set_objective(asend_ctx* ctx, int32_t kind) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.n_nodes > 0, "set the mesh first");
+        learned_set_objective(c, kind);
+        return ASEND_OK;
+    });
+}
+
+int asend_learned_set_samples(asend_ctx* ctx, int32_t n_samples, const float* samples) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(n_samples > 0 && samples != nullptr, "need at least one sample");
+        require(c.n_nodes > 0, "set the mesh first");
+        learned_set_samples(c, n_samples, samples);
+        return ASEND_OK;
+    });
+}
+
+int asend_learned_train(asend_ctx* ctx, int32_t n_steps, float lr, double* loss_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(learned_ready(c), "no learned weights");
+        require(c.assembled, "assemble first");
+        require(n_steps >= 0 && std::isfinite(lr) && lr >= 0.f, "bad training arguments");
+        const double loss = learned_train(c, n_steps, lr);
+        if (loss_out) *loss_out = loss;
+        return std::isfinite(loss) ? ASEND_OK : ASEND_NONFINITE;
+    });
+}
+
+int asend_learned_loss_grad(asend_ctx* ctx, double* loss_out, float* grad_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(learned_ready(c), "no learned weights");
+        require(c.assembled, "assemble first");
+        const double loss = learned_loss_grad(c, grad_out != nullptr);
+        if (loss_out) *loss_out = loss;
+        if (grad_out) learned_get_grad(c, grad_out);
+        return ASEND_OK;
+    });
+}
+
+int asend_learned_features(asend_ctx* ctx, float* feat, float* chol, float* outputs) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.assembled, "assemble first");
+        require(!outputs || learned_ready(c), "no learned weights");
+        learned_get_features(c, feat, chol, outputs);
+        return ASEND_OK;
+    });
+}
+
+int asend_learned_blocks(asend_ctx* ctx, int32_t use_net, float* blocks_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.assembled, "assemble first");
+        require(blocks_out != nullptr, "null output");
+        require(!use_net || learned_ready(c), "no learned weights");
+        DArr<float> b;
+        b.alloc((size_t)9 * c.n_nodes);
+        learned_blocks(c, b.p, use_net != 0);
+        ASEND_CUDA(cudaMemcpyAsync(blocks_out, b.p, sizeof(float) * 9 * c.n_nodes, cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        return ASEND_OK;
+    });
+}
+
+int asend_learned_forward(asend_ctx* ctx, int32_t n, const float* feat, float* outputs) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(n > 0 && feat && outputs, "bad arguments");
+        require(learned_ready(c), "no learned weights");
+        learned_forward_host(c, n, feat, outputs);
+        return ASEND_OK;
+    });
+}
+
+int asend_learned_backward(asend_ctx* ctx, int32_t n, const float* feat, const float* dy, float* grad_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(n > 0 && feat && dy && grad_out, "bad arguments");
+        require(learned_ready(c), "no learned weights");
+        learned_backward_host(c, n, feat, dy, grad_out);
+        return ASEND_OK;
     });
 }
 

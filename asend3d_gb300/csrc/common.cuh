@@ -94,12 +94,15 @@ struct PcgScalars {
 };
 
 struct MgHierarchy;
+struct LearnedState;
 
 struct Ctx {
     int device = 0;
     // structured-block metadata (multigrid) and its hierarchy
     int bx = 0, by = 0, bz = 0;
     std::shared_ptr<MgHierarchy> mg;
+    float mg_damping = 1.5f;  // smoother omega = mg_damping / lambda_max(D^-1 A)
+    std::shared_ptr<LearnedState> learned;  // learned nodal preconditioner blocks
     int64_t assembly_epoch = 0;
     cudaStream_t stream = nullptr;
     std::string err;
@@ -227,9 +230,34 @@ int instance_of_node(const Ctx& c, int node);
 double row_penalty_scale(const Ctx& c, int row);
 // multigrid (k_mg.cu)
 void mg_prepare(Ctx& c);
+void mg_invalidate_values(Ctx& c);
+void mg_level_info(Ctx& c, int level, int32_t* dims, double* lam_est, double* lam_bound, double* omega);
+void mg_vcycle_host(Ctx& c, const float* b, float* z);
+void mg_select_smoother(Ctx& c, bool learned);
+void mg_stationary_residual(Ctx& c, float* r_host, int k, bool learned_smoother);
+void mg_learned_loss_grad(Ctx& c, const float* samples, int n_samples, float* gblk, double* d_loss);
 void mg_apply(Ctx& c, const float* d_b, float* d_z4);
 int mg_levels(const Ctx& c);
 int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f, double* d_x,
                  int nrhs);
+// learned nodal preconditioner blocks (k_learned.cu)
+bool learned_ready(const Ctx& c);
+void learned_mesh_changed(Ctx& c);
+void learned_init(Ctx& c, uint64_t seed);
+void learned_set_objective(Ctx& c, int kind);
+void learned_set_params(Ctx& c, const float* params);
+void learned_get_params(Ctx& c, float* params);
+int learned_n_params();
+int learned_n_features();
+int learned_n_outputs();
+void learned_blocks(Ctx& c, float* d_binv, bool use_net);
+void learned_add_samples(Ctx& c, int n_samples, const int32_t* iters, bool append, uint64_t seed);
+void learned_set_samples(Ctx& c, int n_samples, const float* samples);
+double learned_loss_grad(Ctx& c, bool grad);
+double learned_train(Ctx& c, int n_steps, float lr);
+void learned_get_grad(Ctx& c, float* out);
+void learned_get_features(Ctx& c, float* feat, float* cfac, float* y);
+void learned_forward_host(Ctx& c, int n, const float* feat, float* y_out);
+void learned_backward_host(Ctx& c, int n, const float* feat, const float* dy, float* grad_out);
 
 }  // namespace asend

@@ -25,6 +25,7 @@
 //    beta = -alpha (z . Ap) / (r_old . z_old), which tolerates the FP32
 //    preconditioner's rounding asymmetry.
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <memory>
 
@@ -61,8 +62,18 @@ struct MgHierarchy {
     DArr<float> dense, ainv;      // coarsest operator (n x n) and its inverse
     int n_coarse = 0;
     int64_t epoch = -1;
-    float omega = 0.6f;
+    float omega = 0.6f;           // damping used when the eigenvalue estimate fails
+    bool l0_learned = false;      // finest-level smoother blocks come from the learned model
+    DArr<float> pow_nrm;          // power-iteration norms per level [levels][kPowSteps + 1]
+    DArr<uint32_t> pow_ticket;    // last-CTA tickets per level and step
+    DArr<double> pow_part;        // per-CTA partial sums
+    DArr<unsigned int> pow_bound; // ||D^-1 A||_inf per level (float bits)
+    DArr<float> pow_omega;        // damping in use per level
+    bool safe_damping = false;    // omega from the guaranteed bound (after a failed solve)
+    DArr<float> vl_q, vl_mw, vl_t4, vl_r2, vl_w;  // learned-smoother training vectors
 };
+
+constexpr int kPowSteps = 10;
 
 namespace {
 using namespace pcg;
@@ -392,6 +403,197 @@ __global__ void __launch_bounds__(kT) k_vc_post(SbView A, const float* __restric
                           xv.z + B[6] * d0 + B[7] * d1 + B[8] * d2, 0.f);
 }
 
+// ---------------------------------------------------------------------------
+// Gradient of the V-cycle residual loss with respect to the finest-level
+// smoother blocks M (learned smoother training).  With z = V(b), x2 the
+// level-0 iterate before post-smoothing, q = b - A z, r2 = b - A x2,
+// w = A q, t = w - A M w and v = t - A P C R t (C: coarse V-cycle,
+// R = P^T), the loss ||q||^2 has dL/dM_n = -2 (v_n b_n^T + w_n r2_n^T).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float4 f4of(const float* a, int row) {
+    return make_float4(a[3 * row], a[3 * row + 1], a[3 * row + 2], 0.f);
+}
+
+// q = b - A z, r2 = b - A x2; loss += ||q||^2
+__global__ void __launch_bounds__(kT) k_vl_resid(SbView A, const float* __restrict__ b, const float4* __restrict__ z,
+                                                 const float4* __restrict__ x2, float4* __restrict__ q,
+                                                 float* __restrict__ r2, double* __restrict__ loss) {
+    __shared__ double sm[32];
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc[1] = {0.0};
+    if (row < A.n_rows) {
+        float y[3], u[3];
+        sb_row(A, row, z, y);
+        sb_row(A, row, x2, u);
+        const float q0 = b[3 * row] - y[0], q1 = b[3 * row + 1] - y[1], q2 = b[3 * row + 2] - y[2];
+        q[row] = make_float4(q0, q1, q2, 0.f);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) r2[3 * row + a] = b[3 * row + a] - u[a];
+        acc[0] = (double)q0 * q0 + (double)q1 * q1 + (double)q2 * q2;
+    }
+    block_sum<1>(acc, sm);
+    if (threadIdx.x == 0 && acc[0] != 0.0) atomicAdd(loss, acc[0]);
+}
+
+// w = A q (stored as float[3n]); mw = M w (float4)
+__global__ void __launch_bounds__(kT) k_vl_w(SbView A, const float* __restrict__ M, const float4* __restrict__ q,
+                                             float* __restrict__ w, float4* __restrict__ mw) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= A.n_rows) return;
+    float y[3];
+    sb_row(A, row, q, y);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) w[3 * row + a] = y[a];
+    const float* B = M + 9 * (size_t)row;
+    mw[row] = make_float4(B[0] * y[0] + B[1] * y[1] + B[2] * y[2], B[3] * y[0] + B[4] * y[1] + B[5] * y[2],
+                          B[6] * y[0] + B[7] * y[1] + B[8] * y[2], 0.f);
+}
+
+// t = w - A mw (float[3n] and float4 copies)
+__global__ void __launch_bounds__(kT) k_vl_t(SbView A, const float* __restrict__ w, const float4* __restrict__ mw,
+                                             float* __restrict__ t, float4* __restrict__ t4) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= A.n_rows) return;
+    float y[3];
+    sb_row(A, row, mw, y);
+    const float t0 = w[3 * row] - y[0], t1 = w[3 * row + 1] - y[1], t2 = w[3 * row + 2] - y[2];
+    t[3 * row] = t0;
+    t[3 * row + 1] = t1;
+    t[3 * row + 2] = t2;
+    t4[row] = make_float4(t0, t1, t2, 0.f);
+}
+
+// r := r - A z (stationary multigrid iteration on residuals)
+__global__ void __launch_bounds__(kT) k_vl_rstep(SbView A, const float4* __restrict__ z, float* __restrict__ r) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= A.n_rows) return;
+    float y[3];
+    sb_row(A, row, z, y);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) r[3 * row + a] -= y[a];
+}
+
+// v = t - A cc (cc = P C R t); G_n += -sym(2 (v b^T + w r2^T)), G stored g00 g11 g22 g01 g02 g12
+__global__ void __launch_bounds__(kT) k_vl_grad(SbView A, const float4* __restrict__ t4, const float4* __restrict__ cc,
+                                                const float* __restrict__ b, const float* __restrict__ w,
+                                                const float* __restrict__ r2, float* __restrict__ G) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= A.n_rows) return;
+    float y[3];
+    sb_row(A, row, cc, y);
+    const float4 tv = t4[row];
+    const float v[3] = {tv.x - y[0], tv.y - y[1], tv.z - y[2]};
+    const float bb[3] = {b[3 * row], b[3 * row + 1], b[3 * row + 2]};
+    const float ww[3] = {w[3 * row], w[3 * row + 1], w[3 * row + 2]};
+    const float rr[3] = {r2[3 * row], r2[3 * row + 1], r2[3 * row + 2]};
+    auto gij = [&](int i, int j) { return -(v[i] * bb[j] + v[j] * bb[i] + ww[i] * rr[j] + ww[j] * rr[i]); };
+    float* g = G + 6 * (size_t)row;
+    g[0] += gij(0, 0);
+    g[1] += gij(1, 1);
+    g[2] += gij(2, 2);
+    g[3] += gij(0, 1);
+    g[4] += gij(0, 2);
+    g[5] += gij(1, 2);
+}
+
+// ---------------------------------------------------------------------------
+// Smoother damping: omega = 4 / (3 lambda), lambda an estimate of the largest
+// eigenvalue of D^-1 A by power iteration (D = nodal diagonal blocks), so the
+// damped block-Jacobi sweep stays a contraction on elongated or strongly
+// heterogeneous elements.  All on the device: step k computes
+// y = D^-1 A (x / nrm[k]) and nrm[k+1] = ||y||; the last CTA of a step sums
+// the per-CTA partials in CTA order (deterministic).
+// ---------------------------------------------------------------------------
+__global__ void k_pow_init(int n, float4* __restrict__ x, float* __restrict__ nrm) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row == 0) nrm[0] = 1.f;
+    if (row >= n) return;
+    auto h = [](uint32_t v) {  // integer hash -> [-1, 1)
+        v ^= v >> 16; v *= 0x7feb352du; v ^= v >> 15; v *= 0x846ca68bu; v ^= v >> 16;
+        return (float)(v >> 8) * (2.f / 16777216.f) - 1.f;
+    };
+    x[row] = make_float4(h(3u * row + 1u), h(3u * row + 2u), h(3u * row + 3u), 0.f);
+}
+
+__global__ void __launch_bounds__(kT) k_pow_step(SbView A, const float* __restrict__ dinv, const float4* __restrict__ x,
+                                                 float4* __restrict__ y4, float* __restrict__ nrm, int k,
+                                                 double* __restrict__ part, uint32_t* __restrict__ ticket) {
+    __shared__ double sm[32];
+    __shared__ bool last;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    const float inv = 1.f / nrm[k];
+    double acc[1] = {0.0};
+    if (row < A.n_rows) {
+        float y[3];
+        sb_row(A, row, x, y);
+        const float* B = dinv + 9 * (size_t)row;
+        const float z0 = inv * (B[0] * y[0] + B[1] * y[1] + B[2] * y[2]);
+        const float z1 = inv * (B[3] * y[0] + B[4] * y[1] + B[5] * y[2]);
+        const float z2 = inv * (B[6] * y[0] + B[7] * y[1] + B[8] * y[2]);
+        y4[row] = make_float4(z0, z1, z2, 0.f);
+        acc[0] = (double)z0 * z0 + (double)z1 * z1 + (double)z2 * z2;
+    }
+    block_sum<1>(acc, sm);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = acc[0];
+        __threadfence();
+        last = atomicAdd(ticket + k, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double s[1] = {0.0};
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s[0] += ((volatile double*)part)[b];
+    block_sum<1>(s, sm);
+    if (threadIdx.x == 0) nrm[k + 1] = (float)sqrt(s[0]);
+}
+
+// Guaranteed bound ||D^-1 A||_inf >= lambda_max(D^-1 A): the largest absolute
+// row sum of D_n^-1 A_nm over the row's blocks (binv holds D^-1), as the
+// float bits of a non-negative value under atomicMax.
+__global__ void __launch_bounds__(kT) k_inf_bound(SbView A, const float* __restrict__ dinv,
+                                                  unsigned int* __restrict__ bound_bits) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    float best = 0.f;
+    if (row < A.n_rows) {
+        const float* B = dinv + 9 * (size_t)row;
+        const int lane = row & 31;
+        const int64_t g0 = A.slice_off[row >> 5];
+        const int len = A.row_len[row];
+        float sum[3] = {0.f, 0.f, 0.f};
+        for (int j = 0; j < len; ++j) {
+            const float* v = A.v + ((g0 + j) * 9) * 32 + lane;
+            float m[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) m[q] = v[q * 32];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b)
+                    sum[a] += fabsf(B[3 * a] * m[b] + B[3 * a + 1] * m[3 + b] + B[3 * a + 2] * m[6 + b]);
+        }
+        best = fmaxf(sum[0], fmaxf(sum[1], sum[2]));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if ((threadIdx.x & 31) == 0 && best > 0.f) atomicMax(bound_bits, __float_as_uint(best));
+}
+
+// binv := omega * binv (binv held D^-1) with omega = scale / lambda, lambda =
+// the power estimate nrm[k], or the guaranteed bound when safe is set
+__global__ void k_scale_blocks(int n, float* __restrict__ binv, const float* __restrict__ nrm, int k,
+                               const unsigned int* __restrict__ bound_bits, int safe, float scale,
+                               float* __restrict__ omega_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 9 * n) return;
+    const float est = nrm[k], bound = __uint_as_float(*bound_bits);
+    float lam = safe ? bound : est;
+    if (!(lam > 0.f) || !isfinite(lam)) lam = bound;
+    const float omega = (lam > 0.f && isfinite(lam)) ? scale / lam : 0.5f;
+    binv[i] *= omega;
+    if (i == 0) *omega_out = omega;
+}
+
 __device__ __forceinline__ float restrict_w(const LevelView& v, int axis, int i, int m) {
     const int32_t* lo = v.lo + (axis == 0 ? v.ol0 : axis == 1 ? v.ol1 : v.ol2);
     const float* w = v.w + (axis == 0 ? v.ol0 : axis == 1 ? v.ol1 : v.ol2);
@@ -714,10 +916,14 @@ __global__ void __launch_bounds__(kThreads) k_mg_residual(MgPcg M, int init, dou
 // ---------------------------------------------------------------------------
 // host: hierarchy construction
 // ---------------------------------------------------------------------------
-MgAxis make_axis(int n_f) {
+// Coarse-node positions on one axis: every second fine node (the last cell
+// of an odd count is merged into its neighbour), or all of them when the axis
+// is not coarsened at this level (semi-coarsening).
+MgAxis make_axis(int n_f, bool coarsen) {
     MgAxis a;
     a.n_f = n_f;
-    for (int i = 0; i <= n_f; i += 2) a.xs.push_back(i);
+    const int step = coarsen ? 2 : 1;
+    for (int i = 0; i <= n_f; i += step) a.xs.push_back(i);
     if (a.xs.back() != n_f) a.xs.push_back(n_f);
     a.n_c = (int)a.xs.size() - 1;
     a.lo.assign(n_f + 1, 0);
@@ -845,12 +1051,36 @@ void build_hierarchy(Ctx& c) {
     for (size_t r = 0; r + 1 < c.c_ptr.size(); ++r)
         for (int k = c.c_ptr[r]; k < c.c_ptr[r + 1]; ++k) L0->h_pen[c.c_dof[k]] += (float)(c.c_coef[k] * c.c_coef[k]);
     H->L.push_back(std::move(L0));
+    // element spacing per axis at level 0 (block node numbering)
+    double h[3];
+    {
+        const int n100 = (c.by + 1) * (c.bz + 1), n010 = c.bz + 1, n001 = 1;
+        const int nb[3] = {n100, n010, n001};
+        for (int ax = 0; ax < 3; ++ax) {
+            double d2 = 0.0;
+            for (int j = 0; j < 3; ++j) {
+                const double d = c.xyz[3 * (size_t)nb[ax] + j] - c.xyz[j];
+                d2 += d * d;
+            }
+            h[ax] = std::sqrt(d2);
+        }
+    }
     for (;;) {
         MgLevel& F = *H->L.back();
         if (F.n_dof <= 256 || (F.nx <= 1 && F.ny <= 1 && F.nz <= 1)) break;
         auto L = std::make_unique<MgLevel>();
         const int nf[3] = {F.nx, F.ny, F.nz};
-        for (int ax = 0; ax < 3; ++ax) L->ax[ax] = make_axis(nf[ax]);
+        // semi-coarsening: coarsen only the axes whose spacing is within a
+        // factor sqrt(2) of the smallest (the strongly coupled directions of
+        // stretched elements); the others wait until the cells are isotropic
+        double hmin = 1e300;
+        for (int ax = 0; ax < 3; ++ax)
+            if (nf[ax] >= 2) hmin = std::min(hmin, h[ax]);
+        for (int ax = 0; ax < 3; ++ax) {
+            const bool coarsen = nf[ax] >= 2 && h[ax] <= 1.4142135623730951 * hmin;
+            L->ax[ax] = make_axis(nf[ax], coarsen);
+            h[ax] *= (double)nf[ax] / (double)L->ax[ax].n_c;
+        }
         L->nx = L->ax[0].n_c;
         L->ny = L->ax[1].n_c;
         L->nz = L->ax[2].n_c;
@@ -912,16 +1142,49 @@ void build_hierarchy(Ctx& c) {
     c.mg = H;
 }
 
+// omega * D^-1 on level l, omega = damping / lambda with lambda a
+// kPowSteps-step power-iteration estimate of the largest eigenvalue of D^-1 A
+void damp_smoother(Ctx& c, int l) {
+    MgHierarchy& H = *c.mg;
+    MgLevel& L = *H.L[l];
+    float* nrm = H.pow_nrm.p + (size_t)l * (kPowSteps + 1);
+    uint32_t* tk = H.pow_ticket.p + (size_t)l * kPowSteps;
+    float4* xa = reinterpret_cast<float4*>(L.x4.p);
+    float4* xb = reinterpret_cast<float4*>(L.y4.p);
+    const int g = grid_of(L.n_nodes);
+    ASEND_CUDA(cudaMemsetAsync(tk, 0, sizeof(uint32_t) * kPowSteps, c.stream));
+    ASEND_CUDA(cudaMemsetAsync(H.pow_bound.p + l, 0, sizeof(unsigned int), c.stream));
+    k_pow_init<<<g, kT, 0, c.stream>>>(L.n_nodes, xa, nrm);
+    for (int k = 0; k < kPowSteps; ++k) {
+        k_pow_step<<<g, kT, 0, c.stream>>>(sbview(L), L.binv.p, xa, xb, nrm, k, H.pow_part.p, tk);
+        std::swap(xa, xb);
+    }
+    unsigned int* bound = H.pow_bound.p + l;
+    k_inf_bound<<<g, kT, 0, c.stream>>>(sbview(L), L.binv.p, bound);
+    k_scale_blocks<<<(9 * L.n_nodes + 255) / 256, 256, 0, c.stream>>>(L.n_nodes, L.binv.p, nrm, kPowSteps, bound,
+                                                                       H.safe_damping ? 1 : 0, c.mg_damping,
+                                                                       H.pow_omega.p + l);
+    c.launches += kPowSteps + 3;
+}
+
 // per-assembly values: Galerkin element matrices, level operators, penalty,
 // smoother blocks, coarsest inverse
 void setup_values(Ctx& c) {
     MgHierarchy& H = *c.mg;
-    const float omega = H.omega;
+    const int n_lev = (int)H.L.size();
+    H.pow_nrm.alloc((size_t)n_lev * (kPowSteps + 1));
+    H.pow_bound.alloc((size_t)n_lev);
+    H.pow_omega.alloc((size_t)n_lev);
+    H.pow_bound.zero(c.stream);
+    H.pow_omega.zero(c.stream);
+    H.pow_ticket.alloc((size_t)n_lev * kPowSteps);
+    H.pow_part.alloc((size_t)grid_of(H.L[0]->n_nodes));
     {
         MgLevel& L0 = *H.L[0];
         k_smoother_blocks<double><<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(L0.n_nodes, c.A.slice_off.p, c.A.diag.p,
-                                                                            c.A.v64.p, omega, L0.binv.p);
+                                                                            c.A.v64.p, 1.f, L0.binv.p);
         ++c.launches;
+        damp_smoother(c, 0);
     }
     for (size_t l = 1; l < H.L.size(); ++l) {
         MgLevel& L = *H.L[l];
@@ -939,8 +1202,9 @@ void setup_values(Ctx& c) {
         k_add_pen<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(L.n_nodes, L.own.slice_off.p, L.own.diag.p, L.pen.p,
                                                            (float)c.sf, L.own.v32.p);
         k_smoother_blocks<float><<<grid_of(L.n_nodes), kT, 0, c.stream>>>(L.n_nodes, L.own.slice_off.p, L.own.diag.p,
-                                                                          L.own.v32.p, omega, L.binv.p);
+                                                                          L.own.v32.p, 1.f, L.binv.p);
         c.launches += 3;
+        if (l + 1 < H.L.size()) damp_smoother(c, (int)l);  // the coarsest level is solved directly
     }
     MgLevel& Lc = *H.L.back();
     k_dense_build<<<Lc.n_nodes, 128, 0, c.stream>>>(Lc.n_nodes, Lc.A->slice_off.p, Lc.A->row_len.p, Lc.A->col.p,
@@ -999,15 +1263,85 @@ void vcycle(Ctx& c, const Control* ctl, bool fused0) {
 
 int vcycle_launches(const MgHierarchy& H) { return 6 * ((int)H.L.size() - 1) + 1; }
 
+// L0.x4 = P C R (L0.r): the coarse-grid correction of one V-cycle alone
+// (restriction of level 0's r, the V-cycle of the coarser levels, and the
+// prolongation into a zeroed level-0 vector; no level-0 smoothing).
+void coarse_correction(Ctx& c) {
+    MgHierarchy& H = *c.mg;
+    const int nl = (int)H.L.size();
+    MgLevel& L0 = *H.L[0];
+    for (int l = 0; l < nl - 1; ++l) {
+        MgLevel& L = *H.L[l];
+        MgLevel& C = *H.L[l + 1];
+        if (l > 0)
+            k_vc_resid<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(sbview(L), L.b.p, reinterpret_cast<float4*>(L.x4.p),
+                                                                L.r.p, nullptr);
+        const bool last = (l + 1 == nl - 1);
+        const int n1 = (L.nx + 1) * (L.ny + 1) * (C.nz + 1), n2 = (L.nx + 1) * (C.ny + 1) * (C.nz + 1);
+        k_vc_restrict_axis<2><<<grid_of(n1), kT, 0, c.stream>>>(
+            L.nx + 1, L.ny + 1, C.nz + 1, L.nz + 1, C.d_xs.p + C.ox[2], C.d_lo.p + C.ol[2], C.d_w.p + C.ol[2], C.nz,
+            L.r.p, C.t1.p, nullptr, nullptr, nullptr);
+        k_vc_restrict_axis<1><<<grid_of(n2), kT, 0, c.stream>>>(
+            L.nx + 1, C.ny + 1, C.nz + 1, L.ny + 1, C.d_xs.p + C.ox[1], C.d_lo.p + C.ol[1], C.d_w.p + C.ol[1], C.ny,
+            C.t1.p, C.t2.p, nullptr, nullptr, nullptr);
+        k_vc_restrict_axis<0><<<grid_of(C.n_nodes), kT, 0, c.stream>>>(
+            C.nx + 1, C.ny + 1, C.nz + 1, L.nx + 1, C.d_xs.p + C.ox[0], C.d_lo.p + C.ol[0], C.d_w.p + C.ol[0], C.nx,
+            C.t2.p, C.b.p, last ? nullptr : C.binv.p, reinterpret_cast<float4*>(C.x4.p), nullptr);
+    }
+    MgLevel& Lc = *H.L.back();
+    k_vc_dense<<<1, 1024, 0, c.stream>>>(H.n_coarse, H.dense.p, Lc.b.p, Lc.y4.p, nullptr);
+    ASEND_CUDA(cudaMemsetAsync(L0.x4.p, 0, sizeof(float) * 4 * L0.n_nodes, c.stream));
+    for (int l = nl - 2; l >= 0; --l) {
+        MgLevel& L = *H.L[l];
+        MgLevel& C = *H.L[l + 1];
+        k_vc_prolong<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(view_of(C), L.nx, L.ny, L.nz,
+                                                              reinterpret_cast<const float4*>(C.y4.p),
+                                                              reinterpret_cast<float4*>(L.x4.p), nullptr);
+        if (l > 0)
+            k_vc_post<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(sbview(L), L.binv.p, L.b.p,
+                                                               reinterpret_cast<const float4*>(L.x4.p),
+                                                               reinterpret_cast<float4*>(L.y4.p), nullptr);
+    }
+    c.launches += 6 * (nl - 1) - 1;
+}
+
+
 }  // namespace
+
+void mg_invalidate_values(Ctx& c) {
+    if (c.mg) c.mg->epoch = -1;
+}
 
 void mg_prepare(Ctx& c) {
     if (!c.mg) build_hierarchy(c);
-    if (c.mg->epoch != c.assembly_epoch) setup_values(c);
+    if (c.mg->epoch != c.assembly_epoch) {
+        setup_values(c);
+        c.mg->l0_learned = false;
+    }
+}
+
+// Finest-level smoother blocks: damped block Jacobi (omega D_n^-1, omega from
+// the eigenvalue estimate), or the
+// learned nodal blocks M_n (recomputed on every request, since the weights
+// may have changed since the last one).
+void mg_select_smoother(Ctx& c, bool learned) {
+    MgHierarchy& H = *c.mg;
+    MgLevel& L0 = *H.L[0];
+    if (learned) {
+        learned_blocks(c, L0.binv.p, true);
+        H.l0_learned = true;
+    } else if (H.l0_learned) {
+        k_smoother_blocks<double><<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(L0.n_nodes, c.A.slice_off.p, c.A.diag.p,
+                                                                            c.A.v64.p, 1.f, L0.binv.p);
+        ++c.launches;
+        damp_smoother(c, 0);
+        H.l0_learned = false;
+    }
 }
 
 void mg_apply(Ctx& c, const float* d_b, float* d_z4) {
     mg_prepare(c);
+    mg_select_smoother(c, false);
     MgLevel& L0 = *c.mg->L[0];
     ASEND_CUDA(cudaMemcpyAsync(L0.b.p, d_b, sizeof(float) * c.n_dof, cudaMemcpyDeviceToDevice, c.stream));
     vcycle(c, nullptr, false);
@@ -1017,10 +1351,132 @@ void mg_apply(Ctx& c, const float* d_b, float* d_z4) {
 
 int mg_levels(const Ctx& c) { return c.mg ? (int)c.mg->L.size() : 0; }
 
-// Multigrid-preconditioned flexible CG, one right-hand side at a time.
+// per-level diagnostics: dims (nx, ny, nz), power estimate and guaranteed
+// bound of lambda_max(D^-1 A), damping in use (the coarsest level: zeros)
+void mg_level_info(Ctx& c, int level, int32_t* dims, double* lam_est, double* lam_bound, double* omega) {
+    if (!c.mg || level < 0 || level >= (int)c.mg->L.size()) throw InputError("no such multigrid level");
+    MgHierarchy& H = *c.mg;
+    MgLevel& L = *H.L[level];
+    if (dims) {
+        dims[0] = L.nx;
+        dims[1] = L.ny;
+        dims[2] = L.nz;
+    }
+    float nrm = 0.f, om = 0.f;
+    unsigned int bb = 0;
+    if (H.pow_nrm.n) {
+        ASEND_CUDA(cudaMemcpyAsync(&nrm, H.pow_nrm.p + (size_t)level * (kPowSteps + 1) + kPowSteps, sizeof(float),
+                                   cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaMemcpyAsync(&bb, H.pow_bound.p + level, sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaMemcpyAsync(&om, H.pow_omega.p + level, sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    float bf;
+    std::memcpy(&bf, &bb, sizeof(float));
+    if (lam_est) *lam_est = nrm;
+    if (lam_bound) *lam_bound = bf;
+    if (omega) *omega = om;
+}
+
+// z = V(b) with the current finest-level smoother, host FP32 vectors [n_dof]
+void mg_vcycle_host(Ctx& c, const float* b, float* z) {
+    mg_prepare(c);
+    MgHierarchy& H = *c.mg;
+    MgLevel& L0 = *H.L[0];
+    if (H.L.size() < 2) throw InputError("multigrid hierarchy has a single level");
+    ASEND_CUDA(cudaMemcpyAsync(L0.b.p, b, sizeof(float) * c.n_dof, cudaMemcpyHostToDevice, c.stream));
+    vcycle(c, nullptr, false);
+    c.launches += vcycle_launches(H);
+    std::vector<float> y4((size_t)4 * c.n_nodes);
+    ASEND_CUDA(cudaMemcpyAsync(y4.data(), L0.y4.p, sizeof(float) * y4.size(), cudaMemcpyDeviceToHost, c.stream));
+    ASEND_CUDA(cudaStreamSynchronize(c.stream));
+    for (int i = 0; i < c.n_nodes; ++i)
+        for (int a = 0; a < 3; ++a) z[3 * (size_t)i + a] = y4[4 * (size_t)i + a];
+}
+
+// r := (I - A V)^k r on a host FP32 vector [n_dof] with the finest-level
+// smoother in force (learned or damped): the residual after k stationary
+// V-cycle iterations, dominated by the modes the V-cycle reduces slowest.
+void mg_stationary_residual(Ctx& c, float* r_host, int k, bool learned_smoother) {
+    mg_prepare(c);
+    mg_select_smoother(c, learned_smoother);
+    MgHierarchy& H = *c.mg;
+    MgLevel& L0 = *H.L[0];
+    if (H.L.size() < 2) throw InputError("multigrid hierarchy has a single level");
+    if (H.vl_w.n != (size_t)c.n_dof) H.vl_w.alloc(c.n_dof);
+    ASEND_CUDA(cudaMemcpyAsync(H.vl_w.p, r_host, sizeof(float) * c.n_dof, cudaMemcpyHostToDevice, c.stream));
+    const int g = grid_of(L0.n_nodes);
+    for (int i = 0; i < k; ++i) {
+        ASEND_CUDA(cudaMemcpyAsync(L0.b.p, H.vl_w.p, sizeof(float) * c.n_dof, cudaMemcpyDeviceToDevice, c.stream));
+        vcycle(c, nullptr, false);
+        k_vl_rstep<<<g, kT, 0, c.stream>>>(sbview(L0), reinterpret_cast<const float4*>(L0.y4.p), H.vl_w.p);
+        c.launches += vcycle_launches(H) + 1;
+    }
+    ASEND_CUDA(cudaMemcpyAsync(r_host, H.vl_w.p, sizeof(float) * c.n_dof, cudaMemcpyDeviceToHost, c.stream));
+    ASEND_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+// Loss sum_s ||b_s - A V(b_s)||^2 over the samples (FP32, unit-norm b_s) with
+// the learned finest-level smoother blocks, added to *d_loss; the block
+// gradient (summed over samples) is added to gblk [n_nodes][6].  The caller
+// has installed the learned blocks (mg_select_smoother(c, true)).
+void mg_learned_loss_grad(Ctx& c, const float* samples, int n_samples, float* gblk, double* d_loss) {
+    MgHierarchy& H = *c.mg;
+    MgLevel& L0 = *H.L[0];
+    const int n = L0.n_nodes, nd = 3 * n;
+    if (H.L.size() < 2) throw InputError("multigrid hierarchy has a single level");
+    if (H.vl_q.n != (size_t)4 * n) {
+        H.vl_q.alloc((size_t)4 * n);
+        H.vl_mw.alloc((size_t)4 * n);
+        H.vl_t4.alloc((size_t)4 * n);
+        H.vl_r2.alloc(nd);
+        H.vl_w.alloc(nd);
+    }
+    float4* q = reinterpret_cast<float4*>(H.vl_q.p);
+    float4* mw = reinterpret_cast<float4*>(H.vl_mw.p);
+    float4* t4 = reinterpret_cast<float4*>(H.vl_t4.p);
+    const int g = grid_of(n);
+    for (int s = 0; s < n_samples; ++s) {
+        const float* b = samples + (size_t)s * nd;
+        ASEND_CUDA(cudaMemcpyAsync(L0.b.p, b, sizeof(float) * nd, cudaMemcpyDeviceToDevice, c.stream));
+        vcycle(c, nullptr, false);  // z in L0.y4, x2 in L0.x4
+        k_vl_resid<<<g, kT, 0, c.stream>>>(sbview(L0), b, reinterpret_cast<const float4*>(L0.y4.p),
+                                          reinterpret_cast<const float4*>(L0.x4.p), q, H.vl_r2.p, d_loss);
+        k_vl_w<<<g, kT, 0, c.stream>>>(sbview(L0), L0.binv.p, q, H.vl_w.p, mw);
+        k_vl_t<<<g, kT, 0, c.stream>>>(sbview(L0), H.vl_w.p, mw, L0.r.p, t4);
+        coarse_correction(c);  // L0.x4 = P C R t
+        k_vl_grad<<<g, kT, 0, c.stream>>>(sbview(L0), t4, reinterpret_cast<const float4*>(L0.x4.p), b, H.vl_w.p,
+                                         H.vl_r2.p, gblk);
+        c.launches += vcycle_launches(H) + 4;
+    }
+    ASEND_CUDA(cudaGetLastError());
+}
+
+
+namespace {
+int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f,
+                      double* d_x, int nrhs_all);
+}
+
+// Multigrid-preconditioned flexible CG, one right-hand side at a time.  A
+// solve that turns non-finite (a smoother damped from an eigenvalue estimate
+// that fell short of a localised top mode) is repeated from zero with every
+// level's damping taken from the guaranteed bound ||D^-1 A||_inf, which then
+// stays in force for this hierarchy.
 int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f, double* d_x,
                  int nrhs_all) {
+    const int rc = pcg_solve_mg_once(c, o, st, warm, d_f, d_x, nrhs_all);
+    if (rc != ASEND_NONFINITE || !c.mg || c.mg->safe_damping) return rc;
+    c.mg->safe_damping = true;
+    mg_invalidate_values(c);
+    return pcg_solve_mg_once(c, o, st, false, d_f, d_x, nrhs_all);
+}
+
+namespace {
+int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f,
+                      double* d_x, int nrhs_all) {
     mg_prepare(c);
+    mg_select_smoother(c, o.precond == ASEND_PC_MG_LEARNED);
     MgHierarchy& H = *c.mg;
     const int n = c.A.n_rows, nd = c.n_dof;
     const int max_it = o.max_iter > 0 ? o.max_iter : nd;
@@ -1152,5 +1608,7 @@ int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool 
     }
     return status;
 }
+
+}  // namespace
 
 }  // namespace asend

@@ -440,14 +440,29 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
               double* d_x, int nrhs_all) {
     if (o.method != ASEND_METHOD_FP64 && o.method != ASEND_METHOD_MIXED) throw InputError("unknown method");
     if (!(o.rel_tol > 0.0)) throw InputError("rel_tol must be positive");
-    if (o.precond == ASEND_PC_MG) return pcg_solve_mg(c, o, st, warm, d_f, d_x, nrhs_all);
+    if (o.precond == ASEND_PC_MG || o.precond == ASEND_PC_MG_LEARNED) {
+        if (o.precond == ASEND_PC_MG_LEARNED && !learned_ready(c)) throw InputError("no learned weights");
+        return pcg_solve_mg(c, o, st, warm, d_f, d_x, nrhs_all);
+    }
     int pc = o.precond;
-    int status_fallback = 0;
+    bool use_learned = false;
     if (pc == ASEND_PC_LEARNED) {
-        // the learned blocks are installed by the preconditioner module when
-        // available; without a trained model the Jacobi fallback is used
-        pc = ASEND_PC_JACOBI;
-        status_fallback = 1;
+        if (learned_ready(c)) {
+            // learned nodal blocks through the block-Jacobi kernels; on a
+            // non-finite or non-converged solve the plain Jacobi PCG is rerun
+            // from zero and judges convergence
+            use_learned = true;
+            pc = ASEND_PC_BLOCK;
+        } else {
+            asend_solve_opts oj = o;
+            oj.precond = ASEND_PC_JACOBI;
+            const int rc = pcg_solve(c, oj, st, warm, d_f, d_x, nrhs_all);
+            if (rc == ASEND_OK) {
+                if (st) st->status = ASEND_FALLBACK;
+                return ASEND_FALLBACK;
+            }
+            return rc;
+        }
     }
     if (pc != ASEND_PC_JACOBI && pc != ASEND_PC_BLOCK) throw InputError("unknown preconditioner");
     if (!(o.rel_tol > 0.0)) throw InputError("rel_tol must be positive");
@@ -465,9 +480,14 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
         k_jacobi<<<grid, kThreads, 0, c.stream>>>(n, c.A.slice_off.p, c.A.diag.p, c.A.v64.p, c.d_dinv.p);
     } else {
         c.d_binv.alloc((size_t)9 * n);
-        k_block_inv<<<grid, kThreads, 0, c.stream>>>(n, c.A.slice_off.p, c.A.diag.p, c.A.v64.p, c.d_binv.p);
+        if (use_learned) {
+            learned_blocks(c, c.d_binv.p, true);
+        } else {
+            k_block_inv<<<grid, kThreads, 0, c.stream>>>(n, c.A.slice_off.p, c.A.diag.p, c.A.v64.p, c.d_binv.p);
+            ++c.launches;
+        }
     }
-    ++c.launches;
+    if (pc == ASEND_PC_JACOBI) ++c.launches;
     const bool mixed = o.method == ASEND_METHOD_MIXED;
     if (mixed) {
         c.d_p32.alloc((size_t)kMaxRhs * 4 * n);
@@ -595,7 +615,12 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
         st->ms_assemble = c.last_assemble_ms;
         st->penalty_scale = c.sf;
     }
-    if (status == 0 && status_fallback) status = ASEND_FALLBACK;
+    if (use_learned && (status == ASEND_NONFINITE || status == ASEND_MAX_ITER)) {
+        asend_solve_opts oj = o;
+        oj.precond = ASEND_PC_JACOBI;
+        const int rc = pcg_solve(c, oj, st, false, d_f, d_x, nrhs_all);
+        status = rc == ASEND_OK ? ASEND_FALLBACK : rc;
+    }
     if (st) st->status = status;
     return status;
 }

@@ -277,6 +277,104 @@ class GpuSolver:
     def stream(self) -> int:
         return int(self.lib.asend_stream(self.ctx) or 0)
 
+    def mg_set_damping(self, factor):
+        """Multigrid smoother omega = factor / lambda_max(D^-1 A) (default 1.5)."""
+        self._check(self.lib.asend_mg_set_damping(self.ctx, factor), "mg_set_damping")
+
+    @property
+    def mg_levels(self) -> int:
+        return int(self.lib.asend_mg_levels(self.ctx))
+
+    def mg_level_info(self, level):
+        dims = np.zeros(3, dtype=np.int32)
+        est, bound, om = C.c_double(0), C.c_double(0), C.c_double(0)
+        self._check(self.lib.asend_mg_level_info(self.ctx, level, _ptr(dims, C.c_int32), C.byref(est),
+                                                 C.byref(bound), C.byref(om)), "mg_level_info")
+        return {"dims": tuple(int(d) for d in dims), "lambda_est": est.value, "lambda_bound": bound.value,
+                "omega": om.value}
+
+    def mg_vcycle(self, b) -> np.ndarray:
+        b = np.ascontiguousarray(b, dtype=np.float32)
+        z = np.zeros_like(b)
+        self._check(self.lib.asend_mg_vcycle(self.ctx, _ptr(b, C.c_float), _ptr(z, C.c_float)), "mg_vcycle")
+        return z
+
+    # -- learned nodal preconditioner blocks -------------------------------
+    @property
+    def n_learned_params(self) -> int:
+        return int(self.lib.asend_learned_n_params())
+
+    def learned_init(self, seed=0):
+        self._check(self.lib.asend_learned_init(self.ctx, seed), "learned_init")
+
+    def learned_params(self) -> np.ndarray:
+        w = np.zeros(self.n_learned_params, dtype=np.float32)
+        self._check(self.lib.asend_learned_get_params(self.ctx, _ptr(w, C.c_float)), "learned_get_params")
+        return w
+
+    def set_learned_params(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        if w.shape != (self.n_learned_params,):
+            raise ValueError(f"expected {self.n_learned_params} parameters")
+        self._check(self.lib.asend_learned_set_params(self.ctx, _ptr(w, C.c_float)), "learned_set_params")
+
+    def learned_add_samples(self, iters, append=False, seed=0):
+        it = np.ascontiguousarray(np.atleast_1d(iters), dtype=np.int32)
+        self._check(self.lib.asend_learned_add_samples(self.ctx, len(it), _ptr(it, C.c_int32), int(append), seed),
+                    "learned_add_samples")
+
+    def learned_set_objective(self, kind):
+        """kind: _lib.LEARN_BLOCK (blocks for PCG) or _lib.LEARN_MG (multigrid smoother)."""
+        self._check(self.lib.asend_learned_set_objective(self.ctx, kind), "learned_set_objective")
+
+    def learned_set_samples(self, samples):
+        a = np.ascontiguousarray(np.atleast_2d(samples), dtype=np.float32)
+        self._check(self.lib.asend_learned_set_samples(self.ctx, a.shape[0], _ptr(a, C.c_float)),
+                    "learned_set_samples")
+
+    def learned_train(self, n_steps=1, lr=1e-3) -> float:
+        loss = C.c_double(0)
+        rc = self._check(self.lib.asend_learned_train(self.ctx, n_steps, lr, C.byref(loss)), "learned_train")
+        if rc != _lib.ASEND_OK:
+            raise AsendError(f"learned_train returned status {rc} (loss {loss.value})")
+        return loss.value
+
+    def learned_loss_grad(self):
+        loss = C.c_double(0)
+        g = np.zeros(self.n_learned_params, dtype=np.float32)
+        self._check(self.lib.asend_learned_loss_grad(self.ctx, C.byref(loss), _ptr(g, C.c_float)),
+                    "learned_loss_grad")
+        return loss.value, g
+
+    def learned_features(self, outputs=True):
+        n = self.p.mesh.n_nodes
+        f = np.zeros((n, 16), dtype=np.float32)
+        ch = np.zeros((n, 6), dtype=np.float32)
+        y = np.zeros((n, 8), dtype=np.float32) if outputs else None
+        self._check(self.lib.asend_learned_features(self.ctx, _ptr(f, C.c_float), _ptr(ch, C.c_float),
+                                                    None if y is None else _ptr(y, C.c_float)), "learned_features")
+        return f, ch, y
+
+    def learned_blocks(self, use_net=True) -> np.ndarray:
+        b = np.zeros((self.p.mesh.n_nodes, 3, 3), dtype=np.float32)
+        self._check(self.lib.asend_learned_blocks(self.ctx, int(use_net), _ptr(b, C.c_float)), "learned_blocks")
+        return b
+
+    def learned_forward(self, feat) -> np.ndarray:
+        feat = np.ascontiguousarray(feat, dtype=np.float32)
+        y = np.zeros((feat.shape[0], 8), dtype=np.float32)
+        self._check(self.lib.asend_learned_forward(self.ctx, feat.shape[0], _ptr(feat, C.c_float),
+                                                   _ptr(y, C.c_float)), "learned_forward")
+        return y
+
+    def learned_backward(self, feat, dy) -> np.ndarray:
+        feat = np.ascontiguousarray(feat, dtype=np.float32)
+        dy = np.ascontiguousarray(dy, dtype=np.float32)
+        g = np.zeros(self.n_learned_params, dtype=np.float32)
+        self._check(self.lib.asend_learned_backward(self.ctx, feat.shape[0], _ptr(feat, C.c_float),
+                                                    _ptr(dy, C.c_float), _ptr(g, C.c_float)), "learned_backward")
+        return g
+
     @property
     def kernel_launches(self) -> int:
         return int(self.lib.asend_kernel_launches(self.ctx))

@@ -52,6 +52,12 @@ typedef struct asend_ctx asend_ctx;
 #define ASEND_PC_BLOCK 1      /* nodal block Jacobi (dof_per_node x dof_per_node blocks)  */
 #define ASEND_PC_LEARNED 2    /* MLP-predicted nodal blocks, Jacobi fallback              */
 #define ASEND_PC_MG 3         /* geometric multigrid V-cycle (structured hex8 blocks)     */
+#define ASEND_PC_MG_LEARNED 4 /* multigrid with learned finest-level smoother blocks      */
+
+/* training objectives of the learned blocks */
+#define ASEND_LEARN_BLOCK 0   /* mean ||r - A M r||^2: blocks used directly by PCG        */
+#define ASEND_LEARN_MG 1      /* mean ||b - A V(b)||^2, V = V-cycle with the blocks as the
+                                 finest-level smoother (needs the block structure)       */
 
 /* objective kinds (reference objective categories, objective_meth.rs:592-942) */
 #define ASEND_OBJ_DISPLACEMENT 0 /* 'displacement' + 'powerNorm' on a node set            */
@@ -107,6 +113,21 @@ int asend_set_modulus(asend_ctx* ctx, const double* E);
 int asend_set_block_structure(asend_ctx* ctx, int32_t nx, int32_t ny, int32_t nz);
 /* Number of multigrid levels built so far (0 before the first MG solve). */
 int asend_mg_levels(const asend_ctx* ctx);
+/* Smoother damping of the multigrid levels: omega = factor / lambda, lambda a
+ * power-iteration estimate of the largest eigenvalue of D^-1 A on each level
+ * (D = nodal diagonal blocks).  Default 1.5; factor in (0, 2). */
+int asend_mg_set_damping(asend_ctx* ctx, double factor);
+/* Level diagnostics after a multigrid solve: dims[3] = (nx, ny, nz) of the
+ * level's cells, the power-iteration estimate and the guaranteed bound
+ * ||D^-1 A||_inf of lambda_max(D^-1 A), and the smoother damping in use (the
+ * coarsest level, solved directly, reports zeros).  Any pointer may be NULL.
+ * The damping switches to factor / bound on every level after a multigrid
+ * solve turned non-finite (the solve is then repeated from zero). */
+int asend_mg_level_info(asend_ctx* ctx, int32_t level, int32_t* dims, double* lambda_est,
+                        double* lambda_bound, double* omega);
+/* z = V(b): one V-cycle with the current smoothers (FP32 host vectors of
+ * n_dof entries); builds the hierarchy if needed. */
+int asend_mg_vcycle(asend_ctx* ctx, const float* b, float* z);
 
 /* Batched solves (no counterpart in the single-model reference; it replaces
  * running the reference's Model::solve once per UQ / design sample): the
@@ -240,6 +261,63 @@ void* asend_stream(const asend_ctx* ctx);
  * calls that overlap on the GPU (other streams or contexts on the same
  * device) race and must be serialised by the caller. */
 int asend_operator_energy_noalloc(asend_ctx* ctx, const double* d_x, double* d_y, double* d_energy);
+
+/* ---- learned nodal preconditioner blocks (no reference counterpart; the
+ *      reference preconditions CG with block LDL^T factors,
+ *      lower_tri_mat_meth.rs:15-241) -------------------------------------------
+ * A 3-layer MLP (16 -> 64 -> 64 -> 8, ReLU; BF16 weights and activations, FP32
+ * accumulation) maps per-node features to a lower-triangular correction U of
+ * the block-Jacobi inverse: M_n = C_n U_n U_n^T C_n^T with C_n C_n^T = D_n^-1,
+ * so every block is SPD and a zero output is plain block Jacobi.
+ * Features (16 per node, 12 used): the node's diagonal 3x3 block divided by
+ * its mean diagonal (6 entries), 0.1 * (log mean diagonal - mesh mean), mean,
+ * standard deviation and range of log E - mean log E over the adjacent
+ * elements, adjacent-element count / 8, and a flag for penalty-dominated
+ * nodes.  Parameters, FP32, in the order W1[64][16] b1[64] W2[64][64] b2[64]
+ * W3[8][64] b3[8] (row-major [out][in]).
+ * The weights belong to the context and survive asend_set_mesh and
+ * asend_set_modulus, so a model trained on small meshes is applied to a large
+ * one in the same context (or moved with get/set_params).
+ * ASEND_PC_LEARNED solves with the blocks; a non-finite or non-converged
+ * solve is rerun with point-Jacobi PCG (status ASEND_FALLBACK when that
+ * converges), and with no weights the solve is the Jacobi one with status
+ * ASEND_FALLBACK.  ASEND_PC_MG_LEARNED uses the blocks as the multigrid
+ * finest-level smoother and needs weights. */
+int32_t asend_learned_n_params(void);
+/* Random initial weights (last layer ~1e-3, i.e. block Jacobi); resets Adam. */
+int asend_learned_init(asend_ctx* ctx, uint64_t seed);
+int asend_learned_set_params(asend_ctx* ctx, const float* params);
+int asend_learned_get_params(asend_ctx* ctx, float* params);
+/* Training samples from the assembled operator and load case 0: sample s is
+ * the residual of plain point-Jacobi PCG after iters[s] > 0 iterations; for
+ * iters[s] == 0 a standard normal vector from the seed; for iters[s] < 0 the
+ * residual after -iters[s] stationary multigrid V-cycle iterations from such
+ * a vector (the modes the V-cycle reduces slowest; needs the block
+ * structure).  Each is normalised.  append = 0 replaces the stored samples. */
+int asend_learned_add_samples(asend_ctx* ctx, int32_t n_samples, const int32_t* iters, int32_t append,
+                              uint64_t seed);
+/* Caller-supplied samples [n_samples][n_dof] (each scaled to unit norm),
+ * replacing the stored ones. */
+int asend_learned_set_samples(asend_ctx* ctx, int32_t n_samples, const float* samples);
+/* Selects the training loss (ASEND_LEARN_*; default ASEND_LEARN_BLOCK). */
+int asend_learned_set_objective(asend_ctx* ctx, int32_t kind);
+/* Loss = the selected objective's mean over the samples (FP32 operator).  train:
+ * n_steps Adam steps (beta 0.9/0.999) at learning rate lr on the stored
+ * samples, on the GPU; *loss_out = the loss before the last step (n_steps = 0:
+ * the current loss, no step). */
+int asend_learned_train(asend_ctx* ctx, int32_t n_steps, float lr, double* loss_out);
+/* Current loss and its gradient with respect to the parameters (no step). */
+int asend_learned_loss_grad(asend_ctx* ctx, double* loss_out, float* grad_out);
+/* Per-node features [n_nodes][16] (the BF16 values), Cholesky factors of
+ * D_n^-1 [n_nodes][6] (l00 l10 l11 l20 l21 l22) and network outputs
+ * [n_nodes][8]; any pointer may be NULL (outputs need weights). */
+int asend_learned_features(asend_ctx* ctx, float* feat, float* chol, float* outputs);
+/* The nodal blocks M_n [n_nodes][9] (use_net = 0: block-Jacobi inverse). */
+int asend_learned_blocks(asend_ctx* ctx, int32_t use_net, float* blocks_out);
+/* Kernel checks: network outputs [n][8] for features [n][16] (rounded to
+ * BF16), and the parameter gradient of sum(outputs * dy) over the n rows. */
+int asend_learned_forward(asend_ctx* ctx, int32_t n, const float* feat, float* outputs);
+int asend_learned_backward(asend_ctx* ctx, int32_t n, const float* feat, const float* dy, float* grad_out);
 
 #ifdef __cplusplus
 }
