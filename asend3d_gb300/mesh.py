@@ -40,8 +40,13 @@ class BlockMesh:
         return self.conn.shape[0]
 
     @property
+    def dpn(self) -> int:
+        """DOF per node: 6 for shells (u v w thx thy thz), else 3."""
+        return 6 if self.elem_type == 41 else 3
+
+    @property
     def n_dof(self) -> int:
-        return 3 * self.n_nodes
+        return self.dpn * self.n_nodes
 
     def node_id(self, i, j, k):
         return (np.asarray(i) * (self.ny + 1) + np.asarray(j)) * (self.nz + 1) + np.asarray(k)
@@ -133,3 +138,24 @@ def lognormal_modulus(mesh: BlockMesh, median: float, sigma_log: float, corr_fra
     if mesh.elem_type == 4:
         e = np.tile(e, 6)
     return e.astype(np.float64)
+
+
+def plate_quad4(nx: int, ny: int, lx: float, ly: float) -> BlockMesh:
+    """Structured quad4 shell mesh of the rectangle [0, lx] x [0, ly] at z = 0
+    (the reference's structured quad surface meshing with shell4 elements,
+    Model.addMeshData quad -> shell4): node (i, j) = i*(ny+1) + j, element
+    (i, j) = i*ny + j with corners (i,j), (i+1,j), (i+1,j+1), (i,j+1)
+    (counter-clockwise, normal +z).  nz = 0, lz = 0."""
+    xs = np.linspace(0.0, lx, nx + 1)
+    ys = np.linspace(0.0, ly, ny + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    coords = np.stack([X.ravel(), Y.ravel(), np.zeros(X.size)], axis=1)
+    i, j = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    i, j = i.ravel(), j.ravel()
+
+    def nid(a, b):
+        return a * (ny + 1) + b
+
+    conn = np.stack([nid(i, j), nid(i + 1, j), nid(i + 1, j + 1), nid(i, j + 1)], axis=1).astype(np.int32)
+    return BlockMesh(nx, ny, 0, lx, ly, 0.0, coords, conn, elem_type=41)
+

@@ -47,6 +47,7 @@ class Problem:
     objective: tuple = ("compliance",)
     # design variables: (elem_set, coefficients)
     design_vars: list = field(default_factory=list)
+    thickness: np.ndarray | None = None  # per element (shell sections)
 
     def add_node_set(self, name, nodes):
         self.node_sets[name] = np.asarray(nodes, dtype=np.int32)

@@ -55,6 +55,11 @@ TypeInfo type_info(int type) {
         const int f[6][4] = {{3, 2, 1, 0}, {4, 5, 6, 7}, {0, 1, 5, 4},
                              {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
         std::memcpy(t.faces, f, sizeof(f));
+    } else if (type == 41) {
+        // shell4 as 8 pseudo-nodes of 3 DOF: node a's translations are
+        // pseudo-node 2a, its rotations 2a+1, so DOF 6a + c keeps the
+        // reference's node-major numbering (element_meth.rs:424-431)
+        t.nn = 8; t.dpn = 3; t.nip = 4; t.nfaces = 0; t.face_nn = 0;
     } else if (type == 4) {
         // tet4: one point at (1/4,1/4,1/4), weight 1/6 (element_meth.rs:84-101)
         t.nn = 4; t.dpn = 3; t.nip = 1; t.nfaces = 4; t.face_nn = 3;
@@ -263,6 +268,151 @@ void solid_me(int type, const double* xyz, double rho, double* me) {
 }
 
 // ---------------------------------------------------------------------------
+// shell4 (type 41): 4 nodes x 6 DOF (u v w thx thy thz) + 8 internal DOF,
+// 2x2 Gauss points (element_meth.rs:326-370).  Flat elements in a plane
+// z = const, where the reference's element frame (correct_orient,
+// element_properties.rs:2052-2150) stays the section frame: identity here.
+// ---------------------------------------------------------------------------
+// Shape functions: element_soln_fields.rs:313-363 (4 bilinear, two in-plane
+// incompatible modes 1-s^2, 1-t^2, four edge bubbles for w).
+void shell_shape(double s, double t, double* n, double* ds, double* dt) {
+    n[0] = 0.25 * (1 - s) * (1 - t); ds[0] = -0.25 * (1 - t); dt[0] = -0.25 * (1 - s);
+    n[1] = 0.25 * (1 + s) * (1 - t); ds[1] = 0.25 * (1 - t);  dt[1] = -0.25 * (1 + s);
+    n[2] = 0.25 * (1 + s) * (1 + t); ds[2] = 0.25 * (1 + t);  dt[2] = 0.25 * (1 + s);
+    n[3] = 0.25 * (1 - s) * (1 + t); ds[3] = -0.25 * (1 + t); dt[3] = 0.25 * (1 - s);
+    n[4] = 1 - s * s;             ds[4] = -2 * s;            dt[4] = 0;
+    n[5] = 1 - t * t;             ds[5] = 0;                 dt[5] = -2 * t;
+    n[6] = (1 - s * s) * (1 - t); ds[6] = -2 * s * (1 - t);  dt[6] = -1 + s * s;
+    n[7] = (1 - t * t) * (1 + s); ds[7] = 1 - t * t;         dt[7] = -2 * t * (1 + s);
+    n[8] = (1 - s * s) * (1 + t); ds[8] = -2 * s * (1 + t);  dt[8] = 1 - s * s;
+    n[9] = (1 - t * t) * (1 - s); ds[9] = -1 + t * t;        dt[9] = -2 * t * (1 - s);
+}
+
+// Jacobian with the synthetic third axis (element_soln_fields.rs:404-422):
+// J = [x_s x_t 0; y_s y_t 0; z_s z_t +-1], sign of x_s y_t - y_s x_t.
+double shell_jac(const double* xyz, const double* ds, const double* dt, double* jinv) {
+    double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int a = 0; a < 4; ++a)
+        for (int i = 0; i < 3; ++i) {
+            J[3 * i] += xyz[3 * a + i] * ds[a];
+            J[3 * i + 1] += xyz[3 * a + i] * dt[a];
+        }
+    J[8] = (J[0] * J[4] - J[3] * J[1] > 0.0) ? 1.0 : -1.0;
+    return det_inv(jinv, J, 3);
+}
+
+// Section stiffness ABD (element_properties.rs:766-876, get_abd_dfd0) of one
+// isotropic layer of thickness t centred on the reference plane: A = t Q,
+// B = 0, D = t^3/12 Q, and the transverse-shear and drilling diagonal entries
+// copy A66.  Q = inverse of the plane-stress compliance (get_layer_q_dfd0
+// :138-235, inverted by Givens QR).
+void shell_abd(double E, double nu, double t, double* C) {
+    const double G = E / (2.0 * (1.0 + nu));
+    double S[9] = {1.0 / E, -nu / E, 0, -nu / E, 1.0 / E, 0, 0, 0, 1.0 / G}, Q[9];
+    det_inv(Q, S, 3);
+    for (int i = 0; i < 81; ++i) C[i] = 0.0;
+    const double zmin = -0.5 * t, zmax = 0.5 * t;
+    const double a = zmax - zmin, d = (zmax * zmax * zmax - zmin * zmin * zmin) / 3.0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            C[9 * i + j] = a * Q[3 * i + j];
+            C[9 * (i + 3) + j + 3] = d * Q[3 * i + j];
+        }
+    C[60] = C[70] = C[80] = C[20];
+}
+
+// Section deformation columns (element_soln_fields.rs:1160-1343,
+// get_section_def_dfd0, single-DOF branches) for the 32 element DOF: node DOF
+// 6a + c, then the internal DOF (shape function, component) =
+// (4,u) (5,u) (4,v) (5,v) (6,w) (7,w) (8,w) (9,w) (element_meth.rs:357-372).
+// Rows: eps_xx, eps_yy, gamma_xy, kappa_xx, kappa_yy, kappa_xy, gamma_xz,
+// gamma_yz, drill.
+void shell_bmat(const double* n, const double* dndx /* [10][3] */, double* B /* [9][32] */) {
+    constexpr int tot = 32;
+    for (int i = 0; i < 9 * tot; ++i) B[i] = 0.0;
+    auto trans = [&](int col, int f, int c) {
+        const double dx = dndx[3 * f], dy = dndx[3 * f + 1];
+        if (c == 0) { B[0 * tot + col] = dx; B[2 * tot + col] = dy; B[8 * tot + col] = dy; }
+        if (c == 1) { B[1 * tot + col] = dy; B[2 * tot + col] = dx; B[8 * tot + col] = -dx; }
+        if (c == 2) { B[6 * tot + col] = dx; B[7 * tot + col] = dy; }
+    };
+    for (int a = 0; a < 4; ++a) {
+        for (int c = 0; c < 3; ++c) trans(6 * a + c, a, c);
+        const double dx = dndx[3 * a], dy = dndx[3 * a + 1], N = n[a];
+        B[3 * tot + 6 * a + 4] = dx;            // kappa_xx = d thy / dx
+        B[5 * tot + 6 * a + 4] = dy;            // kappa_xy = d thy/dy - d thx/dx
+        B[6 * tot + 6 * a + 4] = N;             // gamma_xz = dw/dx + thy
+        B[4 * tot + 6 * a + 3] = -dy;           // kappa_yy = -d thx / dy
+        B[5 * tot + 6 * a + 3] = -dx;
+        B[7 * tot + 6 * a + 3] = -N;            // gamma_yz = dw/dy - thx
+        B[8 * tot + 6 * a + 5] = 2.0 * N;       // drill = 2 thz - dv/dx + du/dy
+    }
+    const int fi[8] = {4, 5, 4, 5, 6, 7, 8, 9}, ci[8] = {0, 0, 1, 1, 2, 2, 2, 2};
+    for (int k = 0; k < 8; ++k) trans(24 + k, fi[k], ci[k]);
+}
+
+// Element stiffness (element_equations.rs:206-418, get_ruk_dfd0 shell branch:
+// K += B^T (C B) detJ w) with the internal DOF condensed
+// (element_equations.rs:19-57, condense_mat: K_nn - K_ni K_ii^-1 K_in by Givens
+// QR), and the consistent mass (get_rum_dfd0 :514-581 with the section mass of
+// get_shell_mass_dfd0, element_properties.rs:1354-1408: rho t on the
+// translations, rho t^3/12 on the rotations) over the 24 node DOF.
+void shell_km(const double* xyz, double E, double nu, double rho, double t, double* ke, double* me) {
+    constexpr int tot = 32, nd = 24;
+    double C[81];
+    shell_abd(E, nu, t, C);
+    std::vector<double> K(tot * tot, 0.0), B(9 * tot), CB(9 * tot);
+    if (me) for (int i = 0; i < nd * nd; ++i) me[i] = 0.0;
+    double n0[10], ds0[10], dt0[10], jinv0[9];
+    shell_shape(0.0, 0.0, n0, ds0, dt0);
+    shell_jac(xyz, ds0, dt0, jinv0);  // centroid Jacobian for the non-nodal functions
+    const double sp[4][2] = {{-kR1ORt3, -kR1ORt3}, {kR1ORt3, -kR1ORt3}, {-kR1ORt3, kR1ORt3}, {kR1ORt3, kR1ORt3}};
+    const double msec[6] = {rho * t, rho * t, rho * t, rho * t * t * t / 12.0, rho * t * t * t / 12.0,
+                            rho * t * t * t / 12.0};
+    for (int ip = 0; ip < 4; ++ip) {
+        double n[10], ds[10], dt[10], jinv[9], dndx[30];
+        shell_shape(sp[ip][0], sp[ip][1], n, ds, dt);
+        const double detj = shell_jac(xyz, ds, dt, jinv);
+        for (int f = 0; f < 10; ++f) {
+            const double* ji = (f < 4) ? jinv : jinv0;
+            for (int k = 0; k < 3; ++k) dndx[3 * f + k] = ds[f] * ji[k] + dt[f] * ji[3 + k];
+        }
+        shell_bmat(n, dndx, B.data());
+        for (int i = 0; i < 9; ++i)
+            for (int c = 0; c < tot; ++c) {
+                double acc = 0.0;
+                for (int k = 0; k < 9; ++k) acc += C[9 * i + k] * B[k * tot + c];
+                CB[i * tot + c] = acc * detj;  // weight 1
+            }
+        for (int r = 0; r < tot; ++r)
+            for (int c = 0; c < tot; ++c) {
+                double acc = 0.0;
+                for (int k = 0; k < 9; ++k) acc += B[k * tot + r] * CB[k * tot + c];
+                K[r * tot + c] += acc;
+            }
+        if (me)
+            for (int a = 0; a < 4; ++a)
+                for (int b = 0; b < 4; ++b)
+                    for (int c = 0; c < 6; ++c) me[(6 * a + c) * nd + 6 * b + c] += msec[c] * n[a] * n[b] * detj;
+    }
+    // static condensation of the internal DOF
+    double Kii[64];
+    for (int i = 0; i < 8; ++i)
+        for (int j = 0; j < 8; ++j) Kii[8 * i + j] = K[(24 + i) * tot + 24 + j];
+    givens_factor(Kii, 8);
+    for (int r = 0; r < nd; ++r) {
+        double rhs[8], x[8];
+        for (int i = 0; i < 8; ++i) rhs[i] = K[(24 + i) * tot + r];
+        givens_solve(x, Kii, rhs, 8);
+        for (int c = 0; c < nd; ++c) {
+            double acc = 0.0;
+            for (int i = 0; i < 8; ++i) acc += K[c * tot + 24 + i] * x[i];
+            ke[c * nd + r] = K[c * tot + r] - acc;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Sparse matrix with a fixed pattern (sorted columns) and element-order
 // accumulation.  The reference keeps row linked lists and add_entry appends or
 // accumulates (list_ent_meth.rs:6-18); every (i,j) sum is accumulated in
@@ -307,6 +457,12 @@ struct orc_model {
     double cM = 0.0;    // coefficient of M inside K (Newmark)
     double sf = 0.0;    // penalty scale (model_analysis.rs:255-259)
     bool assembled = false;
+    // shell4: physical nodes and connectivity (the assembly view above uses
+    // two pseudo-nodes per physical node)
+    bool shell = false;
+    int n_phys = 0;
+    std::vector<double> phys_xyz;
+    std::vector<int32_t> conn4;
 };
 
 namespace {
@@ -317,6 +473,23 @@ void elem_xyz(const orc_model* m, int e, double* xyz) {
         const int nd = m->conn[(size_t)e * nn + a];
         for (int j = 0; j < 3; ++j) xyz[3 * a + j] = m->xyz[3 * (size_t)nd + j];
     }
+}
+
+// Element stiffness (and mass when me != null) in the assembly view's DOF
+// order: solids from the isotropic C, shells from the shell4 routine.
+void elem_km(const orc_model* m, int e, double* ke, double* me) {
+    if (m->shell) {
+        double xyz[12];
+        for (int a = 0; a < 4; ++a)
+            for (int j = 0; j < 3; ++j) xyz[3 * a + j] = m->phys_xyz[3 * (size_t)m->conn4[(size_t)e * 4 + a] + j];
+        shell_km(xyz, m->E[e], m->nu[e], m->rho[e], m->thk[e], ke, me);
+        return;
+    }
+    double xyz[24], C[36];
+    elem_xyz(m, e, xyz);
+    iso_cmat(m->E[e], m->nu[e], C);
+    solid_ke(m->ti.type, xyz, C, ke);
+    if (me) solid_me(m->ti.type, xyz, m->rho[e], me);
 }
 
 // Node adjacency from element connectivity, sorted; defines the full 3x3-block
@@ -725,15 +898,38 @@ extern "C" {
 orc_model* orc_create(int32_t elem_type, int32_t n_nodes, const double* coords, int32_t n_elems,
                       const int32_t* conn, const double* E, const double* nu, const double* rho,
                       const double* thickness) {
-    if (elem_type != 8 && elem_type != 4) return nullptr;
+    if (elem_type != 8 && elem_type != 4 && elem_type != 41) return nullptr;
     auto* m = new orc_model();
     m->ti = type_info(elem_type);
-    m->n_nodes = n_nodes;
     m->n_el = n_elems;
     m->dpn = m->ti.dpn;
-    m->n_dof = n_nodes * m->dpn;
-    m->xyz.assign(coords, coords + (size_t)3 * n_nodes);
-    m->conn.assign(conn, conn + (size_t)n_elems * m->ti.nn);
+    if (elem_type == 41) {
+        if (!thickness) { delete m; return nullptr; }
+        for (int e = 0; e < n_elems; ++e)  // flat elements in a plane z = const
+            for (int a = 1; a < 4; ++a)
+                if (coords[3 * (size_t)conn[4 * (size_t)e + a] + 2] != coords[3 * (size_t)conn[4 * (size_t)e] + 2]) {
+                    delete m;
+                    return nullptr;
+                }
+        m->shell = true;
+        m->n_phys = n_nodes;
+        m->phys_xyz.assign(coords, coords + (size_t)3 * n_nodes);
+        m->conn4.assign(conn, conn + (size_t)n_elems * 4);
+        m->n_nodes = 2 * n_nodes;
+        m->xyz.resize((size_t)6 * n_nodes);
+        for (int i = 0; i < n_nodes; ++i)
+            for (int j = 0; j < 3; ++j) m->xyz[6 * (size_t)i + j] = m->xyz[6 * (size_t)i + 3 + j] = coords[3 * (size_t)i + j];
+        m->conn.resize((size_t)n_elems * 8);
+        for (size_t k = 0; k < (size_t)n_elems * 4; ++k) {
+            m->conn[2 * k] = 2 * conn[k];
+            m->conn[2 * k + 1] = 2 * conn[k] + 1;
+        }
+    } else {
+        m->n_nodes = n_nodes;
+        m->xyz.assign(coords, coords + (size_t)3 * n_nodes);
+        m->conn.assign(conn, conn + (size_t)n_elems * m->ti.nn);
+    }
+    m->n_dof = m->n_nodes * m->dpn;
     m->E.assign(E, E + n_elems);
     m->nu.assign(nu, nu + n_elems);
     if (rho) m->rho.assign(rho, rho + n_elems);
@@ -772,16 +968,11 @@ int orc_assemble(orc_model* m, int32_t dynamic, double dt, double beta, double g
     }
     const int nn = m->ti.nn, tot = 3 * nn;
     std::vector<double> ke(tot * tot), me(tot * tot);
-    double xyz[24], C[36];
     std::vector<int32_t> dofs(tot);
     for (int e = 0; e < m->n_el; ++e) {
-        elem_xyz(m, e, xyz);
-        iso_cmat(m->E[e], m->nu[e], C);
-        solid_ke(m->ti.type, xyz, C, ke.data());
-        if (m->dynamic) {
-            solid_me(m->ti.type, xyz, m->rho[e], me.data());
+        elem_km(m, e, ke.data(), m->dynamic ? me.data() : nullptr);
+        if (m->dynamic)
             for (int i = 0; i < tot * tot; ++i) ke[i] += m->cM * me[i];
-        }
         for (int a = 0; a < nn; ++a)
             for (int c = 0; c < 3; ++c) dofs[3 * a + c] = m->conn[(size_t)e * nn + a] * 3 + c;
         for (int i = 0; i < tot; ++i)
@@ -822,7 +1013,13 @@ int orc_get_csr(const orc_model* m, int32_t which, int64_t* row_ptr, int32_t* co
 }
 
 int orc_element_stiffness(int32_t elem_type, const double* xyz, double E, double nu,
-                          double /*thickness*/, double* ke) {
+                          double thickness, double* ke) {
+    if (elem_type == 41) {
+        for (int a = 1; a < 4; ++a)
+            if (xyz[3 * a + 2] != xyz[2]) return -2;
+        shell_km(xyz, E, nu, 0.0, thickness, ke, nullptr);
+        return 0;
+    }
     if (elem_type != 8 && elem_type != 4) return -1;
     double C[36];
     iso_cmat(E, nu, C);
@@ -830,8 +1027,15 @@ int orc_element_stiffness(int32_t elem_type, const double* xyz, double E, double
     return 0;
 }
 
-int orc_element_mass(int32_t elem_type, const double* xyz, double rho, double /*thickness*/,
+int orc_element_mass(int32_t elem_type, const double* xyz, double rho, double thickness,
                      double* me) {
+    if (elem_type == 41) {
+        for (int a = 1; a < 4; ++a)
+            if (xyz[3 * a + 2] != xyz[2]) return -2;
+        std::vector<double> ke(24 * 24);
+        shell_km(xyz, 1.0, 0.3, rho, thickness, ke.data(), me);
+        return 0;
+    }
     if (elem_type != 8 && elem_type != 4) return -1;
     solid_me(elem_type, xyz, rho, me);
     return 0;
@@ -848,6 +1052,7 @@ int orc_element_mass(int32_t elem_type, const double* xyz, double rho, double /*
 int orc_surface_traction(const orc_model* m, int32_t n_set, const int32_t* elem_set,
                          const double* norm_dir, double norm_tol_deg, const double* traction,
                          double* f) {
+    if (m->shell) return -1;  // solid faces only
     const TypeInfo& t = m->ti;
     const int nn = t.nn, tot = 3 * nn;
     // face multiplicity over the whole mesh
@@ -986,11 +1191,8 @@ int orc_adjoint_modulus_gradient(orc_model* m, const double* u, const double* dL
     if (lambda_out) std::copy(lam.begin(), lam.end(), lambda_out);
     const int nn = m->ti.nn, tot = 3 * nn;
     std::vector<double> ke(tot * tot);
-    double xyz[24], C[36];
     for (int e = 0; e < m->n_el; ++e) {
-        elem_xyz(m, e, xyz);
-        iso_cmat(m->E[e], m->nu[e], C);
-        solid_ke(m->ti.type, xyz, C, ke.data());
+        elem_km(m, e, ke.data(), nullptr);
         double acc = 0.0;
         for (int i = 0; i < tot; ++i) {
             const int gi = m->conn[(size_t)e * nn + i / 3] * 3 + i % 3;
@@ -1008,7 +1210,7 @@ int orc_adjoint_modulus_gradient(orc_model* m, const double* u, const double* dL
 // inverse of :724-760).
 int orc_adjoint_modulus_component_gradient(orc_model* m, const double* u, const double* lambda,
                                            int32_t component, double* gD) {
-    if (component < 1 || component > 3) return -1;
+    if (component < 1 || component > 3 || m->shell) return -1;
     const int k = component - 1;
     const TypeInfo& t = m->ti;
     const int nn = t.nn, tot = 3 * nn;

@@ -105,12 +105,16 @@ class Oracle:
         self._nu = np.ascontiguousarray(np.broadcast_to(problem.nu, self._E.shape), np.float64)
         rho = problem.rho if problem.rho is not None else np.zeros_like(self._E)
         self._rho = np.ascontiguousarray(np.broadcast_to(rho, self._E.shape), np.float64)
+        thk = getattr(problem, "thickness", None)
+        self._thk = None if thk is None else np.ascontiguousarray(np.broadcast_to(thk, self._E.shape), np.float64)
         self.m = self.lib.orc_create(m.elem_type, m.n_nodes, _p(self._coords), m.n_elems, _p(self._conn, C.c_int32),
-                                     _p(self._E), _p(self._nu), _p(self._rho), None)
+                                     _p(self._E), _p(self._nu), _p(self._rho),
+                                     None if self._thk is None else _p(self._thk))
         if not self.m:
             raise RuntimeError("orc_create failed")
         self.n_dof = self.lib.orc_n_dof(self.m)
-        ptr, dof, coef, rhs = constraint_rows(problem)
+        self.dpn = 6 if m.elem_type == 41 else 3
+        ptr, dof, coef, rhs = constraint_rows(problem, self.dpn)
         self._c = (ptr, dof, coef, rhs)
         if len(rhs):
             rc = self.lib.orc_set_constraints(self.m, len(rhs), _p(ptr, C.c_int32), _p(dof, C.c_int32), _p(coef),
@@ -133,8 +137,9 @@ class Oracle:
             f = np.zeros(self.n_dof)
             for it in items:
                 if it[0] == "nodalForce":
+                    d = self.dpn
                     for nd in self.p.node_sets[it[1]]:
-                        f[3 * nd:3 * nd + 3] += it[2][:3]
+                        f[d * nd:d * nd + d] += it[2][:d]
                 elif it[0] == "surfaceTraction":
                     els = np.ascontiguousarray(self.p.elem_sets[it[1]], np.int32)
                     nd = np.ascontiguousarray(it[2], np.float64)

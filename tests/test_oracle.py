@@ -210,3 +210,88 @@ def test_newmark_static_limit(oracle_lib):
     os_ = po.Oracle(p)
     us, _, _ = os_.solve(os_.loads()[0] + os_.penalty_rhs(), precond=po.PC_DIRECT)
     assert hist[-1] == pytest.approx(us[3 * tip + 2], rel=0.05)
+
+
+def _shell_beam(F):
+    from asend3d_gb300.mesh import plate_quad4
+    m = plate_quad4(10, 1, 10.0, 1.0)
+    p = Problem(m, np.full(m.n_elems, 1e6), np.full(m.n_elems, 0.0), np.full(m.n_elems, 1.0),
+                thickness=np.full(m.n_elems, 0.1))
+    p.add_node_set("xMin", m.nodes_in_range(xr=(-0.1, 0.1)))
+    p.add_node_set("xMax", m.nodes_in_range(xr=(9.9, 10.1)))
+    p.fix_displacement("xMin", comps=(1, 2, 3, 4, 5, 6))
+    p.add_nodal_force("xMax", F)
+    return p
+
+
+def test_shell_beam_pins(oracle_lib):
+    """shell4 (type 41) cantilever of the reference's shellBeam case: tip
+    deflection, dw/dE through the adjoint, axial stretch, and the first
+    natural frequency (consistent shell mass) against notes.txt."""
+    pins = json.loads((GOLD / "analytic_pins.json").read_text())
+    p = _shell_beam([0.0, 0.0, 1.0])
+    o = oracle_lib.Oracle(p)
+    assert o.dpn == 6 and o.n_dof == 6 * 22
+    u, rc, st = o.solve(o.loads()[0] + o.penalty_rhs(), precond=oracle_lib.PC_DIRECT)
+    tip = p.node_sets["xMax"]
+    w = u[6 * tip + 2]
+    pin = pins["shellBeam_transverse_tip"]
+    assert np.allclose(w, pin["value"], rtol=pin["rtol"])
+    # L = 0.5 * sum of tip w (powerNorm, coefficient 0.5); sum_e dL/dE_e = dL/dE
+    dLdu = np.zeros(o.n_dof)
+    dLdu[6 * tip + 2] = 0.5
+    g, lam, rc, st = o.adjoint(u, dLdu=dLdu, precond=oracle_lib.PC_DIRECT)
+    assert g.sum() == pytest.approx(pin["dwdE"], rel=pin["rtol"])
+    assert g.sum() == pytest.approx(-0.5 * w.sum() / 1e6, rel=1e-8)  # K is linear in E
+    pa = _shell_beam([1.0, 0.0, 0.0])
+    oa = oracle_lib.Oracle(pa)
+    ua, rc, _ = oa.solve(oa.loads()[0] + oa.penalty_rhs(), precond=oracle_lib.PC_DIRECT)
+    pin = pins["shellBeam_axial_tip"]
+    assert np.allclose(ua[6 * tip], pin["value"], rtol=pin["rtol"])
+    # first natural frequency: K x = w^2 M x with the fixed DOF eliminated (a
+    # 1e10 penalty next to the ~1e-6 rotary inertias leaves the generalized
+    # eigensolver no accuracy for the smallest eigenvalue)
+    import scipy.linalg as sla
+    od = oracle_lib.Oracle(p, dynamic=True, dt=1.0, beta=0.25, gamma=0.5)
+    n = od.n_dof
+    rp, col, val = od.csr(0)
+    _, _, mval = od.csr(1)
+    A = np.zeros((n, n))
+    Mm = np.zeros((n, n))
+    for r in range(n):
+        A[r, col[rp[r]:rp[r + 1]]] = val[rp[r]:rp[r + 1]]
+        Mm[r, col[rp[r]:rp[r + 1]]] = mval[rp[r]:rp[r + 1]]
+    cM = -1.0 / (1.0 * (0.25 - 0.5))  # the operator holds K + c_M M (Newmark, dt = 1)
+    fixed = np.concatenate([6 * p.node_sets["xMin"] + c for c in range(6)])
+    keep = np.setdiff1d(np.arange(n), fixed)
+    K = (A - cM * Mm)[np.ix_(keep, keep)]
+    lam_min = sla.eigh(K, Mm[np.ix_(keep, keep)], eigvals_only=True, subset_by_index=[0, 0])[0]
+    f1 = np.sqrt(lam_min) / (2 * np.pi)
+    pin = pins["shellBeam_first_frequency_hz"]
+    assert f1 == pytest.approx(pin["value"], rel=pin["rtol"])
+
+
+def test_shell_element_properties(oracle_lib):
+    """Single shell4 element: symmetric, positive semi-definite with exactly
+    six rigid-body modes; mass symmetric positive definite with total
+    translational mass rho t A."""
+    import ctypes as C
+    lib = oracle_lib.load()
+    xyz = np.array([[0, 0, 0], [1.2, 0.1, 0], [1.0, 0.9, 0], [-0.1, 1.1, 0]], float)
+    ke = np.zeros(576)
+    me = np.zeros(576)
+    P = C.POINTER(C.c_double)
+    assert lib.orc_element_stiffness(41, xyz.ctypes.data_as(P), 7e10, 0.33, 0.005, ke.ctypes.data_as(P)) == 0
+    assert lib.orc_element_mass(41, xyz.ctypes.data_as(P), 2700.0, 0.005, me.ctypes.data_as(P)) == 0
+    K, M = ke.reshape(24, 24), me.reshape(24, 24)
+    assert np.abs(K - K.T).max() <= 1e-12 * np.abs(K).max()
+    ev = np.linalg.eigvalsh(K)
+    assert np.sum(ev < 1e-9 * ev[-1]) == 6 and ev[0] > -1e-9 * ev[-1]
+    assert np.all(np.linalg.eigvalsh(M) > 0)
+    area = 0.5 * abs(np.cross(xyz[2] - xyz[0], xyz[3] - xyz[1])[2])
+    ones = np.zeros(24)
+    ones[0::6] = 1.0
+    assert ones @ M @ ones == pytest.approx(2700.0 * 0.005 * area, rel=1e-12)
+    # a non-planar element is rejected
+    xyz[2, 2] = 0.1
+    assert lib.orc_element_stiffness(41, xyz.ctypes.data_as(P), 7e10, 0.33, 0.005, ke.ctypes.data_as(P)) != 0
