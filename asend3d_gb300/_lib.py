@@ -79,6 +79,7 @@ SIGNATURES = [
     ("asend_time_spmv", c_int, [C.c_void_p, c_int, c_int, P_dbl, P_dbl]),
     ("asend_kernel_launches", C.c_int64, [C.c_void_p]),
     ("asend_stream", C.c_void_p, [C.c_void_p]),
+    ("asend_element_matrices", c_int, [C.c_void_p, c_int, c_int, P_dbl, P_dbl]),
     ("asend_operator_energy_noalloc", c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("asend_learned_n_params", c_int, []),
     ("asend_learned_init", c_int, [C.c_void_p, C.c_uint64]),

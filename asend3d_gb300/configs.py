@@ -14,12 +14,14 @@ No public dataset is involved; every input is generated here from a seed.
                      uniform end traction).
   learned_grid       128x64x64 hex8 (1.6 M DOF), sigma_log 0.5, corr 0.05 L.
   learned_patch      training patch with learned_grid's element size.
+  shell_plate        200x200 quad4 shell plate 1 x 1 m, t = 5 mm, aluminium,
+                     simply supported, Gaussian central impulse (Newmark).
 """
 from __future__ import annotations
 
 import numpy as np
 
-from .mesh import block_hex8, lognormal_modulus
+from .mesh import block_hex8, lognormal_modulus, plate_quad4
 from .solver import Problem
 
 BAR = (2.0, 0.4, 0.4)
@@ -125,3 +127,35 @@ def batch_uq(n_inst: int = 64, seed: int = 7):
     inst = [batch_instance(k, seed=seed) for k in range(n_inst)]
     prob, node_ptr, elem_ptr = combine(inst)
     return prob, node_ptr, elem_ptr, inst
+
+
+def shell_plate(n=200, L=1.0, t=0.005, E=70e9, nu=0.33, rho=2700.0, peak=100.0) -> Problem:
+    """Simply supported square plate of shell4 elements under a central point
+    load (load case 0: peak newtons in -z at the centre node; the time history
+    scales it).  Supports: w = 0 on the four edges; the in-plane rigid motions
+    are removed by u = v = 0 at the corner (0, 0) and v = 0 at the corner
+    (L, 0); rotations are free (simple support)."""
+    m = plate_quad4(n, n, L, L)
+    p = Problem(m, np.full(m.n_elems, E), np.full(m.n_elems, nu), np.full(m.n_elems, rho),
+                thickness=np.full(m.n_elems, t))
+    x, y = m.coords[:, 0], m.coords[:, 1]
+    tol = 1e-9 * L
+    edge = np.nonzero((x < tol) | (x > L - tol) | (y < tol) | (y > L - tol))[0]
+    p.add_node_set("edges", edge)
+    p.fix_displacement("edges", comps=(3,))
+    p.add_node_set("c00", [int(np.nonzero((x < tol) & (y < tol))[0][0])])
+    p.add_node_set("cL0", [int(np.nonzero((x > L - tol) & (y < tol))[0][0])])
+    p.fix_displacement("c00", comps=(1, 2))
+    p.fix_displacement("cL0", comps=(2,))
+    centre = int(np.argmin((x - L / 2) ** 2 + (y - L / 2) ** 2))
+    p.add_node_set("centre", [centre])
+    p.add_nodal_force("centre", [0.0, 0.0, -peak])
+    p.objective = ("displacement", "centre", 3, 1.0)
+    return p
+
+
+def gaussian_pulse(n_steps=2000, dt=2e-6, width=50e-6, t0=200e-6) -> np.ndarray:
+    """Load amplitude at step i (time i*dt): exp(-(t - t0)^2 / (2 width^2))."""
+    tt = np.arange(n_steps) * dt
+    return np.exp(-0.5 * ((tt - t0) / width) ** 2)
+

@@ -23,6 +23,7 @@ int nodes_per_elem(int type) {
     switch (type) {
         case 8: return 8;
         case 4: return 4;
+        case 41: return 4;
         default: return 0;
     }
 }
@@ -395,7 +396,7 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
                    const double* rho, const double* thickness) {
     return guarded(ctx, [&](Ctx& c) {
         const int nn = nodes_per_elem(elem_type);
-        require(nn > 0, "unsupported element type (supported: 8 hex8, 4 tet4)");
+        require(nn > 0, "unsupported element type (supported: 8 hex8, 4 tet4, 41 shell4)");
         require(n_nodes > 0 && n_elems > 0 && coords && conn && E && nu, "empty or null mesh input");
         for (int64_t k = 0; k < (int64_t)n_elems * nn; ++k)
             require(conn[k] >= 0 && conn[k] < n_nodes, "connectivity refers to a node out of range");
@@ -403,16 +404,53 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
             require(std::isfinite(E[e]) && E[e] > 0.0, "element modulus must be positive and finite");
             require(nu[e] > -1.0 && nu[e] < 0.5, "Poisson ratio out of range (-1, 0.5)");
         }
+        const bool shell = elem_type == 41;
+        if (shell) {
+            require(n_nodes <= (1 << 29), "too many shell nodes");
+            require(thickness != nullptr, "shell4 elements need a thickness per element");
+            for (int e = 0; e < n_elems; ++e) {
+                require(std::isfinite(thickness[e]) && thickness[e] > 0.0, "shell thickness must be positive");
+                for (int a = 1; a < 4; ++a)
+                    require(coords[3 * (size_t)conn[4 * (size_t)e + a] + 2] == coords[3 * (size_t)conn[4 * (size_t)e] + 2],
+                            "shell4 elements must be flat in a plane z = const");
+            }
+        }
         ASEND_CUDA(cudaSetDevice(c.device));
         c.type = elem_type;
-        c.nn = nn;
         c.dpn = 3;
-        c.nip = (elem_type == 8) ? 8 : 1;
-        c.n_nodes = n_nodes;
+        c.n_unodes = n_nodes;
         c.n_el = n_elems;
-        c.n_dof = n_nodes * c.dpn;
-        c.xyz.assign(coords, coords + (size_t)3 * n_nodes);
-        c.conn.assign(conn, conn + (size_t)n_elems * nn);
+        if (shell) {
+            // two internal 3-DOF nodes per shell node: DOF 6 n + c stays the caller's numbering
+            c.nn = 8;
+            c.udpn = 6;
+            c.nip = 4;
+            c.n_nodes = 2 * n_nodes;
+            c.xyz.resize((size_t)6 * n_nodes);
+            for (int i = 0; i < n_nodes; ++i)
+                for (int j = 0; j < 3; ++j)
+                    c.xyz[6 * (size_t)i + j] = c.xyz[6 * (size_t)i + 3 + j] = coords[3 * (size_t)i + j];
+            c.conn.resize((size_t)n_elems * 8);
+            for (size_t k = 0; k < (size_t)n_elems * 4; ++k) {
+                c.conn[2 * k] = 2 * conn[k];
+                c.conn[2 * k + 1] = 2 * conn[k] + 1;
+            }
+            std::vector<int32_t> c4(conn, conn + (size_t)n_elems * 4);
+            std::vector<double> x3(coords, coords + (size_t)3 * n_nodes);
+            c.d_shell_conn.upload(c4, c.stream);
+            c.d_shell_xyz.upload(x3, c.stream);
+            ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        } else {
+            c.nn = nn;
+            c.udpn = 3;
+            c.nip = (elem_type == 8) ? 8 : 1;
+            c.n_nodes = n_nodes;
+            c.xyz.assign(coords, coords + (size_t)3 * n_nodes);
+            c.conn.assign(conn, conn + (size_t)n_elems * nn);
+            c.d_shell_conn.release();
+            c.d_shell_xyz.release();
+        }
+        c.n_dof = c.n_nodes * c.dpn;
         c.E.assign(E, E + n_elems);
         c.nu.assign(nu, nu + n_elems);
         c.rho.assign(n_elems, 0.0);
@@ -441,6 +479,8 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         c.d_E.upload(c.E, c.stream);
         c.d_nu.upload(c.nu, c.stream);
         c.d_rho.upload(c.rho, c.stream);
+        if (!c.thk.empty()) c.d_thk.upload(c.thk, c.stream);
+        else c.d_thk.release();
         ASEND_CUDA(cudaStreamSynchronize(c.stream));
         return ASEND_OK;
     });
@@ -482,6 +522,7 @@ int asend_set_block_structure(asend_ctx* ctx, int32_t nx, int32_t ny, int32_t nz
 int asend_set_instances(asend_ctx* ctx, int32_t n_inst, const int32_t* node_ptr) {
     return guarded(ctx, [&](Ctx& c) {
         require(c.n_nodes > 0, "set the mesh first");
+        require(c.type != 41, "batched instances take solid meshes");
         require(n_inst >= 1 && node_ptr, "need at least one instance");
         require(node_ptr[0] == 0 && node_ptr[n_inst] == c.n_nodes, "node_ptr must span all nodes");
         for (int i = 0; i < n_inst; ++i) {
@@ -562,7 +603,7 @@ int asend_set_modulus(asend_ctx* ctx, const double* E) {
 int asend_add_node_set(asend_ctx* ctx, int32_t n, const int32_t* nodes) {
     return guarded(ctx, [&](Ctx& c) {
         require(n >= 1 && nodes, "empty node set");
-        for (int i = 0; i < n; ++i) require(nodes[i] >= 0 && nodes[i] < c.n_nodes, "node set entry out of range");
+        for (int i = 0; i < n; ++i) require(nodes[i] >= 0 && nodes[i] < c.n_unodes, "node set entry out of range");
         c.node_sets.emplace_back(nodes, nodes + n);
         return (int)c.node_sets.size() - 1;
     });
@@ -587,7 +628,7 @@ int asend_add_constraint(asend_ctx* ctx, int32_t n_terms, const int32_t* node_se
         size_t rows = 1;
         for (int t = 0; t < n_terms; ++t) {
             require(node_set[t] >= 0 && node_set[t] < (int)c.node_sets.size(), "unknown node set");
-            require(comp[t] >= 1 && comp[t] <= c.dpn, "constraint component out of range");
+            require(comp[t] >= 1 && comp[t] <= c.udpn, "constraint component out of range");
             rows = std::max(rows, c.node_sets[node_set[t]].size());
         }
         for (int t = 0; t < n_terms; ++t) {
@@ -598,7 +639,7 @@ int asend_add_constraint(asend_ctx* ctx, int32_t n_terms, const int32_t* node_se
             for (int t = 0; t < n_terms; ++t) {
                 const auto& set = c.node_sets[node_set[t]];
                 const int nd = (set.size() == 1) ? set[0] : set[r];
-                c.c_dof.push_back(nd * c.dpn + comp[t] - 1);
+                c.c_dof.push_back(nd * c.udpn + comp[t] - 1);
                 c.c_coef.push_back(coef[t]);
             }
             c.c_ptr.push_back((int32_t)c.c_dof.size());
@@ -617,7 +658,7 @@ int asend_add_nodal_force(asend_ctx* ctx, int32_t rhs, int32_t node_set, const d
         ensure_case(c, rhs);
         require(node_set >= 0 && node_set < (int)c.node_sets.size() && load6, "unknown node set");
         for (int nd : c.node_sets[node_set])
-            for (int k = 0; k < c.dpn; ++k) c.loads[rhs][(size_t)nd * c.dpn + k] += load6[k];
+            for (int k = 0; k < c.udpn; ++k) c.loads[rhs][(size_t)nd * c.udpn + k] += load6[k];
         return ASEND_OK;
     });
 }
@@ -627,6 +668,7 @@ int asend_add_nodal_force(asend_ctx* ctx, int32_t rhs, int32_t node_set, const d
 int asend_add_surface_traction(asend_ctx* ctx, int32_t rhs, int32_t elem_set, const double* norm_dir,
                                double norm_tol_deg, const double* traction) {
     return guarded(ctx, [&](Ctx& c) {
+        require(c.type == 8 || c.type == 4, "surface tractions apply to solid element faces");
         ensure_case(c, rhs);
         require(elem_set >= 0 && elem_set < (int)c.elem_sets.size() && norm_dir && traction, "unknown element set");
         const int nf = (c.type == 8) ? 6 : 4, fnn = (c.type == 8) ? 4 : 3;
@@ -877,7 +919,7 @@ int asend_set_objective(asend_ctx* ctx, int32_t kind, int32_t node_set, int32_t 
         require(kind == ASEND_OBJ_DISPLACEMENT || kind == ASEND_OBJ_COMPLIANCE, "unknown objective kind");
         if (kind == ASEND_OBJ_DISPLACEMENT) {
             require(node_set >= 0 && node_set < (int)c.node_sets.size(), "unknown node set");
-            require(comp >= 1 && comp <= c.dpn, "objective component out of range");
+            require(comp >= 1 && comp <= c.udpn, "objective component out of range");
         }
         c.obj_kind = kind;
         c.obj_set = node_set;
@@ -918,7 +960,7 @@ int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double*
             // L = coef * sum_r sum_{node in set} u_r[node, comp]  ('powerNorm', exponent 1)
             const auto& set = c.node_sets[c.obj_set];
             std::vector<double> dldu(n, 0.0);
-            for (int nd : set) dldu[(size_t)nd * c.dpn + c.obj_comp - 1] += c.obj_coef;
+            for (int nd : set) dldu[(size_t)nd * c.udpn + c.obj_comp - 1] += c.obj_coef;
             DArr<double> d_dldu, d_usum;
             d_dldu.upload(dldu, c.stream);
             d_usum.alloc(n);
@@ -999,6 +1041,15 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
             dLdD_out[i] = s;
         }
         return ndv;
+    });
+}
+
+int asend_element_matrices(asend_ctx* ctx, int32_t first, int32_t count, double* ke, double* me) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.type == 41, "element matrix export is available for shell4 meshes");
+        require(first >= 0 && count > 0 && (int64_t)first + count <= c.n_el && ke, "bad element range");
+        shell_element_matrices(c, first, count, ke, me);
+        return ASEND_OK;
     });
 }
 

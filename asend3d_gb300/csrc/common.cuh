@@ -108,9 +108,12 @@ struct Ctx {
     std::string err;
     int64_t launches = 0;
 
-    // ---- mesh (host)
+    // ---- mesh (host).  The solver works on nodes of dpn = 3 DOF; a shell4
+    // node (6 DOF) is two of them (translations, rotations), so n_nodes counts
+    // those internal nodes while n_unodes / udpn are the caller's.
     int type = 0, nn = 0, dpn = 3, nip = 0;
     int n_nodes = 0, n_el = 0, n_dof = 0;
+    int n_unodes = 0, udpn = 3;
     std::vector<double> xyz, E, nu, rho, thk;
     std::vector<int32_t> conn;
     std::vector<std::vector<int32_t>> node_sets, elem_sets;
@@ -130,6 +133,8 @@ struct Ctx {
     // ---- device mesh
     DArr<double> d_xyz, d_E, d_nu, d_rho, d_thk;
     DArr<int32_t> d_conn;
+    DArr<int32_t> d_shell_conn;  // shell4: 4 physical nodes per element
+    DArr<double> d_shell_xyz;    // shell4: physical node coordinates
     bool pattern_ready = false, assembled = false, dynamic = false;
     double dt = 0, beta = 0.25, gamma = 0.5, cM = 0;
     double sf = 0;
@@ -240,6 +245,10 @@ void mg_apply(Ctx& c, const float* d_b, float* d_z4);
 int mg_levels(const Ctx& c);
 int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f, double* d_x,
                  int nrhs);
+// shell4 elements (k_shell.cu)
+void shell_assemble(Ctx& c, double* vals, double* mvals);
+void shell_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate);
+void shell_element_matrices(Ctx& c, int e0, int n, double* ke_host, double* me_host);
 // learned nodal preconditioner blocks (k_learned.cu)
 bool learned_ready(const Ctx& c);
 void learned_mesh_changed(Ctx& c);

@@ -172,6 +172,10 @@ void device_axpy(Ctx& c, size_t n, double alpha, const double* x, double* y) {
 }
 
 void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g, bool accumulate) {
+    if (c.type == 41) {
+        shell_adjoint(c, d_b, d_a, d_g, accumulate);
+        return;
+    }
     const int blocks = (c.n_el + 127) / 128;
     if (c.nn == 8)
         k_adjoint_modulus<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, d_a, d_b, d_g,

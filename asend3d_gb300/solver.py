@@ -116,10 +116,13 @@ class GpuSolver:
         E = np.ascontiguousarray(p.E, dtype=np.float64)
         nu = np.ascontiguousarray(np.broadcast_to(p.nu, E.shape), dtype=np.float64)
         rho = None if p.rho is None else np.ascontiguousarray(np.broadcast_to(p.rho, E.shape), dtype=np.float64)
-        self._keep = (coords, conn, E, nu, rho)
+        thk = None if p.thickness is None else np.ascontiguousarray(np.broadcast_to(p.thickness, E.shape),
+                                                                    dtype=np.float64)
+        self._keep = (coords, conn, E, nu, rho, thk)
         self._check(self.lib.asend_set_mesh(self.ctx, m.elem_type, m.n_nodes, _ptr(coords, C.c_double), m.n_elems,
                                             _ptr(conn, C.c_int32), _ptr(E, C.c_double), _ptr(nu, C.c_double),
-                                            None if rho is None else _ptr(rho, C.c_double), None), "set_mesh")
+                                            None if rho is None else _ptr(rho, C.c_double),
+                                            None if thk is None else _ptr(thk, C.c_double)), "set_mesh")
         if m.elem_type == 8 and m.conn.shape[0] == m.nx * m.ny * m.nz:
             self._check(self.lib.asend_set_block_structure(self.ctx, m.nx, m.ny, m.nz), "set_block_structure")
         for name, nodes in p.node_sets.items():
@@ -273,6 +276,15 @@ class GpuSolver:
         by = C.c_double(0)
         self._check(self.lib.asend_time_spmv(self.ctx, precision, n_launch, C.byref(ms), C.byref(by)), "time_spmv")
         return ms.value, by.value
+
+    def element_matrices(self, first=0, count=None, mass=True):
+        """shell4 element stiffness (and mass) matrices [count][24][24]."""
+        n = self.p.mesh.n_elems - first if count is None else count
+        ke = np.zeros((n, 24, 24))
+        me = np.zeros((n, 24, 24)) if mass else None
+        self._check(self.lib.asend_element_matrices(self.ctx, first, n, _ptr(ke, C.c_double),
+                                                    None if me is None else _ptr(me, C.c_double)), "element_matrices")
+        return ke, me
 
     @property
     def stream(self) -> int:

@@ -96,7 +96,12 @@ const char* asend_version(void);
 /* ---- model input (replaces model_input.rs:312-860 read_model_input) --------
  * One element type per mesh.  coords[n_nodes*3]; conn[n_elems*nodes_per_elem];
  * per-element isotropic material E, nu, rho (rho may be NULL for statics);
- * thickness per element for shells (else NULL). */
+ * thickness per element for shells (else NULL).  shell4 (41): 4 nodes per
+ * element, 6 DOF per node (u v w thx thy thz), one isotropic layer centred
+ * on the element plane; elements must be flat in a plane z = const (their
+ * frame is then the global one).  Shell meshes take nodal forces/moments,
+ * constraints and objectives on all 6 components; surface tractions,
+ * multigrid and batched instances take solid meshes. */
 int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const double* coords,
                    int32_t n_elems, const int32_t* conn, const double* E, const double* nu,
                    const double* rho, const double* thickness);
@@ -244,6 +249,12 @@ int64_t asend_kernel_launches(const asend_ctx* ctx);
 /* The context's CUDA stream (cudaStream_t as void*), so a caller can record
  * its own CUDA events around library calls. */
 void* asend_stream(const asend_ctx* ctx);
+
+/* shell4 element matrices of elements [first, first + count): ke (and me
+ * when not NULL) [count][24][24] in node-major DOF order (u v w thx thy thz
+ * per node), stiffness after condensing the 8 internal DOF
+ * (element_equations.rs:19-57), consistent section mass (:514-581). */
+int asend_element_matrices(asend_ctx* ctx, int32_t first, int32_t count, double* ke, double* me);
 
 /* y = A x and *energy = x^T A x with the assembled FP64 operator, on DEVICE
  * buffers (x, y: n_dof doubles; energy: one double), without allocating any

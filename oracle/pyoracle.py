@@ -212,7 +212,7 @@ class Oracle:
         return hist, u, rc, its.value
 
     def reorder(self, block_dim=0):
-        out = np.zeros(self.p.mesh.n_nodes, np.int32)
+        out = np.zeros(self.n_dof // 3, np.int32)
         self.lib.orc_reorder_nodes(self.m, block_dim, _p(out, C.c_int32))
         return out
 
