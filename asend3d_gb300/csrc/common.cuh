@@ -181,8 +181,12 @@ struct Ctx {
     size_t h_sc_bytes = 0;
 
     // graphs
+    // cached PCG iteration graph and the launch arguments it was captured
+    // with (reused while they are identical, e.g. every Newmark step), and
+    // the persistent scalar / control / ticket buffers it points at
     cudaGraphExec_t graph = nullptr;
-    int graph_key[6] = {-1, -1, -1, -1, -1, -1};
+    std::vector<uint8_t> graph_key;
+    DArr<uint8_t> pcg_sc, pcg_ctl, pcg_tk;
 };
 
 // ---- device reductions -----------------------------------------------------

@@ -498,12 +498,15 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
     }
     // independent instances: one scalar set per (instance, load case)
     const int NI = c.n_inst > 1 ? c.n_inst : 1;
-    DArr<RhsScalars> d_sc;
-    DArr<Control> d_ctl;
-    DArr<uint32_t> d_tk;
-    d_sc.alloc((size_t)NI * kMaxRhs);
-    d_ctl.alloc(1);
-    if (NI > 1) d_tk.alloc((size_t)NI * 4);
+    // persistent scalar buffers (grow only), so repeated solves with the same
+    // vectors reuse the captured iteration graph
+    const size_t sc_need = sizeof(RhsScalars) * NI * kMaxRhs, tk_need = sizeof(uint32_t) * NI * 4;
+    if (c.pcg_sc.n < sc_need) c.pcg_sc.alloc(sc_need);
+    if (c.pcg_ctl.n < sizeof(Control)) c.pcg_ctl.alloc(sizeof(Control));
+    if (NI > 1 && c.pcg_tk.n < tk_need) c.pcg_tk.alloc(tk_need);
+    RhsScalars* d_sc_p = reinterpret_cast<RhsScalars*>(c.pcg_sc.p);
+    Control* d_ctl_p = reinterpret_cast<Control*>(c.pcg_ctl.p);
+    uint32_t* d_tk_p = reinterpret_cast<uint32_t*>(c.pcg_tk.p);
     ensure_pinned_scalars(c, sizeof(RhsScalars) * NI * kMaxRhs);
     RhsScalars* h_sc = reinterpret_cast<RhsScalars*>(c.h_sc);
     const size_t sc_bytes = sizeof(RhsScalars) * NI * kMaxRhs;
@@ -514,6 +517,7 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
         const int nr = std::min(kMaxRhs, nrhs_all - r0);
         Launcher L{c, PcgArgs{}, o.method, pc, nr};
         PcgArgs& a = L.a;
+        std::memset(&a, 0, sizeof(PcgArgs));  // padding too: the bytes key the cached graph
         a.n_rows = n;
         a.nrhs = nr;
         a.n_dof = nd;
@@ -530,30 +534,40 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
         a.dinv = c.d_dinv.p;
         a.binv = c.d_binv.p;
         a.partials = c.d_partials.p;
-        a.sc = d_sc.p;
-        a.ctl = d_ctl.p;
+        a.sc = d_sc_p;
+        a.ctl = d_ctl_p;
         if (NI > 1) {
             a.cta_inst = c.d_cta_inst.p;
             a.inst_cta0 = c.d_inst_cta0.p;
             a.inst_ncta = c.d_inst_ncta.p;
-            a.tickets = d_tk.p;
-            d_tk.zero(c.stream);
+            a.tickets = d_tk_p;
+            ASEND_CUDA(cudaMemsetAsync(d_tk_p, 0, tk_need, c.stream));
         }
-        d_sc.zero(c.stream);
-        d_ctl.zero(c.stream);
+        ASEND_CUDA(cudaMemsetAsync(d_sc_p, 0, sc_need, c.stream));
+        ASEND_CUDA(cudaMemsetAsync(d_ctl_p, 0, sizeof(Control), c.stream));
         L.residual(0, o.rel_tol * o.rel_tol);
         ASEND_CUDA(cudaGetLastError());
-        // capture G iterations once for this chunk
-        cudaGraph_t graph;
-        cudaGraphExec_t exec;
-        ASEND_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-        for (int i = 0; i < G; ++i) L.iteration();
-        ASEND_CUDA(cudaStreamEndCapture(c.stream, &graph));
-        ASEND_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-        ASEND_CUDA(cudaGraphDestroy(graph));
+        // G iterations as one graph; the executable is kept and reused while
+        // the launch arguments are the same (they fully define the graph)
+        std::vector<uint8_t> key(sizeof(PcgArgs) + 4 * sizeof(int));
+        std::memcpy(key.data(), &a, sizeof(PcgArgs));
+        const int extra[4] = {o.method, pc, nr, G};
+        std::memcpy(key.data() + sizeof(PcgArgs), extra, sizeof(extra));
+        if (!c.graph || key != c.graph_key) {
+            if (c.graph) ASEND_CUDA(cudaGraphExecDestroy(c.graph));
+            c.graph = nullptr;
+            cudaGraph_t graph;
+            ASEND_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+            for (int i = 0; i < G; ++i) L.iteration();
+            ASEND_CUDA(cudaStreamEndCapture(c.stream, &graph));
+            ASEND_CUDA(cudaGraphInstantiate(&c.graph, graph, 0));
+            ASEND_CUDA(cudaGraphDestroy(graph));
+            c.graph_key = key;
+        }
+        cudaGraphExec_t exec = c.graph;
         int since_repl = 0;
         for (;;) {
-            ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc.p, sc_bytes, cudaMemcpyDeviceToHost, c.stream));
+            ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc_p, sc_bytes, cudaMemcpyDeviceToHost, c.stream));
             ASEND_CUDA(cudaStreamSynchronize(c.stream));
             bool all_finished = true, any_replace = false, any_nonfinite = false;
             int it_now = 0;
@@ -576,7 +590,7 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
             if (all_finished) break;
             if (it_now >= max_it) { status = std::max(status, (int)ASEND_MAX_ITER); break; }
             if (any_replace) {
-                ASEND_CUDA(cudaMemcpyAsync(d_sc.p, h_sc, sc_bytes, cudaMemcpyHostToDevice, c.stream));
+                ASEND_CUDA(cudaMemcpyAsync(d_sc_p, h_sc, sc_bytes, cudaMemcpyHostToDevice, c.stream));
                 L.residual(1, 0.0);
                 ++repl_total;
                 since_repl = 0;
@@ -586,8 +600,7 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
             c.launches += 3 * G;
             since_repl += G;
         }
-        ASEND_CUDA(cudaGraphExecDestroy(exec));
-        ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc.p, sc_bytes, cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc_p, sc_bytes, cudaMemcpyDeviceToHost, c.stream));
         ASEND_CUDA(cudaStreamSynchronize(c.stream));
         for (int q = 0; q < NI * kMaxRhs; ++q) {
             if (q % kMaxRhs >= nr) continue;
