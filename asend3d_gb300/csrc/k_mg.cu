@@ -55,6 +55,9 @@ struct MgLevel {
     DArr<float> pen;
     DArr<float> binv, b, r, x4, y4;
     DArr<float> t1, t2;           // restriction intermediates (after the z and y passes)
+    DArr<float> pow_vec;          // last power-iteration vector (warm start)
+    bool pow_warm = false;
+    int pow_steps = 0;            // steps of the last estimate
 };
 
 struct MgHierarchy {
@@ -73,7 +76,8 @@ struct MgHierarchy {
     DArr<float> vl_q, vl_mw, vl_t4, vl_r2, vl_w;  // learned-smoother training vectors
 };
 
-constexpr int kPowSteps = 10;
+constexpr int kPowSteps = 10;      // from a hashed start vector
+constexpr int kPowWarmSteps = 4;   // from the previous assembly's vector
 
 namespace {
 using namespace pcg;
@@ -504,10 +508,10 @@ __global__ void __launch_bounds__(kT) k_vl_grad(SbView A, const float4* __restri
 // y = D^-1 A (x / nrm[k]) and nrm[k+1] = ||y||; the last CTA of a step sums
 // the per-CTA partials in CTA order (deterministic).
 // ---------------------------------------------------------------------------
-__global__ void k_pow_init(int n, float4* __restrict__ x, float* __restrict__ nrm) {
+__global__ void k_pow_init(int n, float4* __restrict__ x, float* __restrict__ nrm, int fill) {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row == 0) nrm[0] = 1.f;
-    if (row >= n) return;
+    if (row >= n || !fill) return;
     auto h = [](uint32_t v) {  // integer hash -> [-1, 1)
         v ^= v >> 16; v *= 0x7feb352du; v ^= v >> 15; v *= 0x846ca68bu; v ^= v >> 16;
         return (float)(v >> 8) * (2.f / 16777216.f) - 1.f;
@@ -1067,7 +1071,8 @@ void build_hierarchy(Ctx& c) {
     }
     for (;;) {
         MgLevel& F = *H->L.back();
-        if (F.n_dof <= 256 || (F.nx <= 1 && F.ny <= 1 && F.nz <= 1)) break;
+        // coarsest level: an explicit inverse, so keep it small (<= 96 DOF)
+        if (F.n_dof <= 96 || (F.nx <= 1 && F.ny <= 1 && F.nz <= 1)) break;
         auto L = std::make_unique<MgLevel>();
         const int nf[3] = {F.nx, F.ny, F.nz};
         // semi-coarsening: coarsen only the axes whose spacing is within a
@@ -1152,19 +1157,30 @@ void damp_smoother(Ctx& c, int l) {
     float4* xa = reinterpret_cast<float4*>(L.x4.p);
     float4* xb = reinterpret_cast<float4*>(L.y4.p);
     const int g = grid_of(L.n_nodes);
+    // later assemblies start from the previous dominant vector (the operator
+    // changes little between assemblies of one hierarchy): fewer steps
+    const bool warm = L.pow_warm;
+    const int steps = warm ? kPowWarmSteps : kPowSteps;
+    if (L.pow_vec.n != (size_t)4 * L.n_nodes) L.pow_vec.alloc((size_t)4 * L.n_nodes);
     ASEND_CUDA(cudaMemsetAsync(tk, 0, sizeof(uint32_t) * kPowSteps, c.stream));
     ASEND_CUDA(cudaMemsetAsync(H.pow_bound.p + l, 0, sizeof(unsigned int), c.stream));
-    k_pow_init<<<g, kT, 0, c.stream>>>(L.n_nodes, xa, nrm);
-    for (int k = 0; k < kPowSteps; ++k) {
+    if (warm)
+        ASEND_CUDA(cudaMemcpyAsync(xa, L.pow_vec.p, sizeof(float) * 4 * L.n_nodes, cudaMemcpyDeviceToDevice,
+                                   c.stream));
+    k_pow_init<<<g, kT, 0, c.stream>>>(L.n_nodes, xa, nrm, warm ? 0 : 1);
+    for (int k = 0; k < steps; ++k) {
         k_pow_step<<<g, kT, 0, c.stream>>>(sbview(L), L.binv.p, xa, xb, nrm, k, H.pow_part.p, tk);
         std::swap(xa, xb);
     }
+    ASEND_CUDA(cudaMemcpyAsync(L.pow_vec.p, xa, sizeof(float) * 4 * L.n_nodes, cudaMemcpyDeviceToDevice, c.stream));
+    L.pow_warm = true;
+    L.pow_steps = steps;
     unsigned int* bound = H.pow_bound.p + l;
     k_inf_bound<<<g, kT, 0, c.stream>>>(sbview(L), L.binv.p, bound);
-    k_scale_blocks<<<(9 * L.n_nodes + 255) / 256, 256, 0, c.stream>>>(L.n_nodes, L.binv.p, nrm, kPowSteps, bound,
+    k_scale_blocks<<<(9 * L.n_nodes + 255) / 256, 256, 0, c.stream>>>(L.n_nodes, L.binv.p, nrm, steps, bound,
                                                                        H.safe_damping ? 1 : 0, c.mg_damping,
                                                                        H.pow_omega.p + l);
-    c.launches += kPowSteps + 3;
+    c.launches += steps + 3;
 }
 
 // per-assembly values: Galerkin element matrices, level operators, penalty,
@@ -1365,7 +1381,7 @@ void mg_level_info(Ctx& c, int level, int32_t* dims, double* lam_est, double* la
     float nrm = 0.f, om = 0.f;
     unsigned int bb = 0;
     if (H.pow_nrm.n) {
-        ASEND_CUDA(cudaMemcpyAsync(&nrm, H.pow_nrm.p + (size_t)level * (kPowSteps + 1) + kPowSteps, sizeof(float),
+        ASEND_CUDA(cudaMemcpyAsync(&nrm, H.pow_nrm.p + (size_t)level * (kPowSteps + 1) + L.pow_steps, sizeof(float),
                                    cudaMemcpyDeviceToHost, c.stream));
         ASEND_CUDA(cudaMemcpyAsync(&bb, H.pow_bound.p + level, sizeof(unsigned int), cudaMemcpyDeviceToHost, c.stream));
         ASEND_CUDA(cudaMemcpyAsync(&om, H.pow_omega.p + level, sizeof(float), cudaMemcpyDeviceToHost, c.stream));
