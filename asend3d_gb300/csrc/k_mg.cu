@@ -1078,14 +1078,22 @@ void build_hierarchy(Ctx& c) {
         // semi-coarsening: coarsen only the axes whose spacing is within a
         // factor sqrt(2) of the smallest (the strongly coupled directions of
         // stretched elements); the others wait until the cells are isotropic
+        // An axis two cells thick is coarsened to one cell only once every
+        // axis is that thin: a one-cell-thick coarse grid of a deep bar is a
+        // poor coarse space.
+        const bool all_thin = nf[0] <= 2 && nf[1] <= 2 && nf[2] <= 2;
+        auto eligible = [&](int ax) { return nf[ax] >= 2 && (nf[ax] > 2 || all_thin); };
         double hmin = 1e300;
         for (int ax = 0; ax < 3; ++ax)
-            if (nf[ax] >= 2) hmin = std::min(hmin, h[ax]);
+            if (eligible(ax)) hmin = std::min(hmin, h[ax]);
+        bool any = false;
         for (int ax = 0; ax < 3; ++ax) {
-            const bool coarsen = nf[ax] >= 2 && h[ax] <= 1.4142135623730951 * hmin;
+            const bool coarsen = eligible(ax) && h[ax] <= 1.4142135623730951 * hmin;
+            any |= coarsen;
             L->ax[ax] = make_axis(nf[ax], coarsen);
             h[ax] *= (double)nf[ax] / (double)L->ax[ax].n_c;
         }
+        if (!any) break;
         L->nx = L->ax[0].n_c;
         L->ny = L->ax[1].n_c;
         L->nz = L->ax[2].n_c;
