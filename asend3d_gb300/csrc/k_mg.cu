@@ -1071,8 +1071,8 @@ void build_hierarchy(Ctx& c) {
     }
     for (;;) {
         MgLevel& F = *H->L.back();
-        // coarsest level: an explicit inverse, so keep it small (<= 96 DOF)
-        if (F.n_dof <= 96 || (F.nx <= 1 && F.ny <= 1 && F.nz <= 1)) break;
+        // coarsest level: an explicit inverse (<= 256 DOF)
+        if (F.n_dof <= 256 || (F.nx <= 1 && F.ny <= 1 && F.nz <= 1)) break;
         auto L = std::make_unique<MgLevel>();
         const int nf[3] = {F.nx, F.ny, F.nz};
         // semi-coarsening: coarsen only the axes whose spacing is within a

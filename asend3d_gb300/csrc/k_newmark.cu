@@ -109,6 +109,7 @@ int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* am
         z->zero(c.stream);
     }
     hist.alloc(std::max(1, n_steps));
+    hist.zero(c.stream);
     // prep predictor (model_prep.rs:584-590): all zero initial state -> zeros
     const int rows = c.A.n_rows;
     const int g_rows = (rows + 127) / 128, g_dof = (n + 255) / 256;

@@ -126,6 +126,11 @@ __global__ void __launch_bounds__(kThreads) k_update_xr(PcgArgs A) {
                     s.done = 1;
                 } else if (s.rr <= s.target) {
                     s.done = 1;  // recurrence converged: the host verifies in FP64
+                } else if (sizeof(TP) == 4 && s.rr < 1e-4 * s.rr_last_true) {
+                    // mixed: the FP32-operator recurrence has dropped 1e4 below
+                    // the last true residual; stop the chunk so the host
+                    // replaces it before the two drift apart
+                    s.done = 1;
                 }
             }
             all &= s.done;

@@ -234,7 +234,7 @@ def test_multigrid_small_parity(small, method):
     dims = [g.mg_level_info(l)["dims"] for l in range(nl)]
     assert dims[:2] == [(20, 4, 4), (10, 2, 2)]  # two-cell axes wait until all axes are thin
     cx, cy, cz = dims[-1]
-    assert 3 * (cx + 1) * (cy + 1) * (cz + 1) <= 96
+    assert 3 * (cx + 1) * (cy + 1) * (cz + 1) <= 256
     assert st["iterations"] < 60
     f = o.loads()[0] + o.penalty_rhs()
     assert np.linalg.norm(f - o.apply(u[0])) / np.linalg.norm(f) <= 1.01e-10
