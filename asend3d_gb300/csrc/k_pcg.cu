@@ -43,6 +43,22 @@ template <typename TV, typename TP, int NR>
 __global__ void __launch_bounds__(kThreads) k_spmv_dot(PcgArgs A) {
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (cta_done<NR>(A, S)) return;
+    if constexpr (sizeof(TP) == 4) {
+        // Mixed: once the FP32-operator recurrence has dropped 1e4 below the
+        // last true residual, stop this graph chunk at an iteration boundary
+        // (p is consistent) so the host replaces the residual before the two
+        // drift apart.  Every CTA decides from scalars no kernel of this
+        // iteration has changed; the instance's first CTA records it.
+        const int b0 = A.cta_inst ? A.inst_cta0[cta_instance(A)] : 0;
+        bool skip_all = true;
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            const bool drop = !S[k].done && S[k].rr < 1e-4 * S[k].rr_last_true;
+            skip_all &= S[k].done || drop;
+            if (drop && blockIdx.x == b0 && threadIdx.x == 0) S[k].done = 1;
+        }
+        if (skip_all) return;
+    }
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     double d[NR][1];
 #pragma unroll
@@ -126,11 +142,6 @@ __global__ void __launch_bounds__(kThreads) k_update_xr(PcgArgs A) {
                     s.done = 1;
                 } else if (s.rr <= s.target) {
                     s.done = 1;  // recurrence converged: the host verifies in FP64
-                } else if (sizeof(TP) == 4 && s.rr < 1e-4 * s.rr_last_true) {
-                    // mixed: the FP32-operator recurrence has dropped 1e4 below
-                    // the last true residual; stop the chunk so the host
-                    // replaces it before the two drift apart
-                    s.done = 1;
                 }
             }
             all &= s.done;
