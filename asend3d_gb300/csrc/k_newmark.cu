@@ -16,7 +16,8 @@
 // operator and mass values (same slots, one column-index read); the
 // corrector, history shift and next predictor are one streaming FP64 kernel
 // over (u, v, a, u_prev, v_prev, a_prev); each step's PCG starts from the
-// previous step's increment.
+// previous step's increment, or (opts.warm_start == 2) from the linear
+// extrapolation of the two previous increments.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -81,6 +82,16 @@ __global__ void k_newmark_update(int n, double dt, double gamma, double c1, doub
     v[i] = vn + dt * ((1.0 - gamma) * an + gamma * a2);
 }
 
+// Initial guess of the step's increment by linear extrapolation of the two
+// previous increments: du := 2 du - du_prev, du_prev := the old du.
+__global__ void k_extrapolate(int n, double* __restrict__ du, double* __restrict__ du_prev) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double d = du[i];
+    du[i] = 2.0 * d - du_prev[i];
+    du_prev[i] = d;
+}
+
 __global__ void k_probe(const double* __restrict__ u, int dof, double* __restrict__ hist, int step) {
     if (threadIdx.x == 0 && blockIdx.x == 0) hist[step] = u[dof];
 }
@@ -101,10 +112,10 @@ int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* am
             for (int k = c.c_ptr[q]; k < c.c_ptr[q + 1]; ++k)
                 pen[c.c_dof[k]] += c.c_coef[k] * row_penalty_scale(c, q) * c.c_rhs[q];
     }
-    DArr<double> d_f0, d_pen, u, v, a, up, vp, ap, du, rhs, hist;
+    DArr<double> d_f0, d_pen, u, v, a, up, vp, ap, du, du_prev, rhs, hist;
     d_f0.upload(c.loads.empty() ? std::vector<double>(n, 0.0) : c.loads[0], c.stream);
     d_pen.upload(pen, c.stream);
-    for (DArr<double>* z : {&u, &v, &a, &up, &vp, &ap, &du, &rhs}) {
+    for (DArr<double>* z : {&u, &v, &a, &up, &vp, &ap, &du, &du_prev, &rhs}) {
         z->alloc(n);
         z->zero(c.stream);
     }
@@ -126,6 +137,14 @@ int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* am
                                                       c.A.m64.p, c.cM, amp[s], d_f0.p, d_pen.p, u.p, a.p, rhs.p);
         ASEND_CUDA(cudaGetLastError());
         ++c.launches;
+        if (s >= 1 && o.warm_start == 2) {  // extrapolated start (the previous increment at step 1)
+            if (s >= 2) {
+                k_extrapolate<<<g_dof, 256, 0, c.stream>>>(n, du.p, du_prev.p);
+            } else {
+                ASEND_CUDA(cudaMemcpyAsync(du_prev.p, du.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+            }
+            ++c.launches;
+        }
         asend_solve_stats ps{};
         const int rc = pcg_solve(c, so, &ps, s > 0, rhs.p, du.p, 1);
         iters_total += ps.iterations;

@@ -229,7 +229,8 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
  * u[probe_dof] after each step in probe_hist[n_steps] (may be NULL) and the
  * final displacement in u_final[n_dof] (may be NULL).  Requires
  * asend_assemble(..., dynamic=1, dt, beta, gamma).  Each step's PCG is
- * warm-started from the previous step's increment. */
+ * warm-started from the previous step's increment, or with
+ * opts->warm_start == 2 from 2 du_{n-1} - du_{n-2} (linear extrapolation). */
 int asend_newmark_run(asend_ctx* ctx, const asend_solve_opts* opts, int32_t n_steps,
                       const double* amp, int32_t probe_dof, double* probe_hist,
                       double* u_final, asend_solve_stats* stats);

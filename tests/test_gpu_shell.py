@@ -115,6 +115,11 @@ def test_shell_plate_newmark_matches_oracle(gpu_lib, oracle_lib):
     hm, um, rcm, stm = g.newmark(amp, probe_dof=probe, method=_lib.METHOD_MIXED, rel_tol=1e-10)
     assert rcm == _lib.ASEND_OK
     assert rel(hm, href) < 1e-6
+    # extrapolated initial increments: same history, fewer iterations
+    hx, ux, rcx, stx = g.newmark(amp, probe_dof=probe, method=_lib.METHOD_FP64, rel_tol=1e-12, warm_start=2)
+    assert rcx == _lib.ASEND_OK
+    assert rel(hx, href) < 1e-7
+    assert stx["iterations"] < st["iterations"]
     g.close()
 
 
