@@ -92,87 +92,6 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(PcgArgs A) {
     }
 }
 
-// K_a for one right-hand side with two threads per row: 256 threads cover
-// the CTA's 128 rows; the half-warps take alternate block columns of a row
-// (each still a coalesced 16-row segment of the slice) and combine with one
-// shuffle, which halves each thread's dependent load chain on short
-// operators where one thread per row leaves the SMs latency-bound.
-template <typename TV, typename TP>
-__global__ void __launch_bounds__(2 * kThreads) k_spmv_dot2(PcgArgs A) {
-    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
-    if (cta_done<1>(A, S)) return;
-    if constexpr (sizeof(TP) == 4) {  // mixed: residual-replacement trigger (as k_spmv_dot)
-        const int b0 = A.cta_inst ? A.inst_cta0[cta_instance(A)] : 0;
-        const bool drop = !S[0].done && S[0].rr < 1e-4 * S[0].rr_last_true;
-        if (drop && blockIdx.x == b0 && threadIdx.x == 0) S[0].done = 1;
-        if (S[0].done || drop) return;
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int h = lane >> 4;
-    const int row = blockIdx.x * kThreads + warp * 16 + (lane & 15);
-    const bool valid = row < A.n_rows;
-    const TV* vals;
-    if constexpr (sizeof(TV) == 4) vals = A.v32; else vals = A.v64;
-    TP y[3] = {(TP)0, (TP)0, (TP)0};
-    if (valid) {
-        const int sl = row & 31;
-        const int64_t g0 = A.slice_off[row >> 5];
-        const int len = A.row_len[row];
-        int j = h;
-        for (; j + 2 < len; j += 4) {  // two block columns per thread in flight
-            const int64_t ga = g0 + j, gb = ga + 2;
-            const int ca = A.col[ga * 32 + sl], cb = A.col[gb * 32 + sl];
-            TV ma[9], mb[9];
-#pragma unroll
-            for (int q = 0; q < 9; ++q) {
-                ma[q] = vals[(ga * 9 + q) * 32 + sl];
-                mb[q] = vals[(gb * 9 + q) * 32 + sl];
-            }
-            TP pa[3], pb[3];
-            PadVec<TP>::load(A.p, (size_t)ca, pa);
-            PadVec<TP>::load(A.p, (size_t)cb, pb);
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                y[a] = fma((TP)ma[a * 3], pa[0], fma((TP)ma[a * 3 + 1], pa[1], fma((TP)ma[a * 3 + 2], pa[2], y[a])));
-                y[a] = fma((TP)mb[a * 3], pb[0], fma((TP)mb[a * 3 + 1], pb[1], fma((TP)mb[a * 3 + 2], pb[2], y[a])));
-            }
-        }
-        for (; j < len; j += 2) {
-            const int64_t g = g0 + j;
-            const int c = A.col[g * 32 + sl];
-            TV m[9];
-#pragma unroll
-            for (int q = 0; q < 9; ++q) m[q] = vals[(g * 9 + q) * 32 + sl];
-            TP pv[3];
-            PadVec<TP>::load(A.p, (size_t)c, pv);
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-                y[a] = fma((TP)m[a * 3], pv[0], fma((TP)m[a * 3 + 1], pv[1], fma((TP)m[a * 3 + 2], pv[2], y[a])));
-        }
-    }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) y[a] += __shfl_xor_sync(0xffffffffu, y[a], 16);
-    double d[1][1] = {{0.0}};
-    if (valid && h == 0) {
-        TP pv[3];
-        PadVec<TP>::load(A.p, (size_t)row, pv);
-        TP* ap = reinterpret_cast<TP*>(A.ap) + 3 * (size_t)row;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            ap[a] = y[a];
-            d[0][0] += (double)pv[a] * (double)y[a];
-        }
-    }
-    double tot[1][1];
-    if (last_block_reduce<1, 1>(A, d, 0, tot) && threadIdx.x == 0) {
-        RhsScalars& s = S[0];
-        if (!s.done) {
-            s.pAp = tot[0][0];
-            s.alpha = s.rz / s.pAp;
-        }
-    }
-}
-
 // K_b: x += alpha p; r -= alpha Ap; z = M r; dots (r,z), (r,r); beta.
 template <typename TP, int NR, int PC>
 __global__ void __launch_bounds__(kThreads) k_update_xr(PcgArgs A) {
@@ -411,13 +330,8 @@ struct Launcher {
     template <typename TP, int NR, int PC>
     void iter_t() {
         const int g = grid_rows(a.n_rows);
-        if constexpr (NR == 1) {
-            if (method == ASEND_METHOD_MIXED) k_spmv_dot2<float, float><<<g, 2 * kThreads, 0, c.stream>>>(a);
-            else k_spmv_dot2<double, double><<<g, 2 * kThreads, 0, c.stream>>>(a);
-        } else {
-            if (method == ASEND_METHOD_MIXED) k_spmv_dot<float, float, NR><<<g, kThreads, 0, c.stream>>>(a);
-            else k_spmv_dot<double, double, NR><<<g, kThreads, 0, c.stream>>>(a);
-        }
+        if (method == ASEND_METHOD_MIXED) k_spmv_dot<float, float, NR><<<g, kThreads, 0, c.stream>>>(a);
+        else k_spmv_dot<double, double, NR><<<g, kThreads, 0, c.stream>>>(a);
         k_update_xr<TP, NR, PC><<<g, kThreads, 0, c.stream>>>(a);
         k_update_p<TP, NR, PC><<<g, kThreads, 0, c.stream>>>(a);
     }
