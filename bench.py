@@ -196,7 +196,7 @@ def run_shell(a):
     achieved = spmv_bytes / (spmv_ms / 1e3) / 1e9
     out = {"metric": METRIC.replace("(static + adjoint)", "(Newmark steps)"), "value": value, "unit": UNIT,
            "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32 operator products, f64 vectors/dots",
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (uniform aluminium plate, Gaussian impulse)",
            "config": {"workload": "shell_plate 200x200 shell4, 2000 Newmark steps of 2 us (one bench step = "
                                   "the whole run)", "n_dof": n_dof, "time_steps": n_steps, "rel_tol": 1e-8,
