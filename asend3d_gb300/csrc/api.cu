@@ -22,6 +22,7 @@ constexpr double kPi = 3.14159265358979323846;
 int nodes_per_elem(int type) {
     switch (type) {
         case 8: return 8;
+        case 81: return 8;
         case 4: return 4;
         case 41: return 4;
         default: return 0;
@@ -71,7 +72,7 @@ void face_load(const Ctx& c, int e, const int* ln, int fnn, const double* trac, 
     double pts[8][3];
     double wts[8];
     int np;
-    if (c.type == 8) {
+    if (c.nn == 8) {  // hex8 / brickIM: the node shape functions
         np = 8;
         int k = 0;
         for (int zc = 0; zc < 2; ++zc)
@@ -95,7 +96,7 @@ void face_load(const Ctx& c, int e, const int* ln, int fnn, const double* trac, 
     for (int p = 0; p < np; ++p) {
         double N[8], dN[8][3];
         const double* s = pts[p];
-        if (c.type == 8) {
+        if (c.nn == 8) {
             const double sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
                                      {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
             for (int a = 0; a < 8; ++a) {
@@ -396,7 +397,7 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
                    const double* rho, const double* thickness) {
     return guarded(ctx, [&](Ctx& c) {
         const int nn = nodes_per_elem(elem_type);
-        require(nn > 0, "unsupported element type (supported: 8 hex8, 4 tet4, 41 shell4)");
+        require(nn > 0, "unsupported element type (supported: 8 hex8, 81 brickIM, 4 tet4, 41 shell4)");
         require(n_nodes > 0 && n_elems > 0 && coords && conn && E && nu, "empty or null mesh input");
         for (int64_t k = 0; k < (int64_t)n_elems * nn; ++k)
             require(conn[k] >= 0 && conn[k] < n_nodes, "connectivity refers to a node out of range");
@@ -443,7 +444,7 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         } else {
             c.nn = nn;
             c.udpn = 3;
-            c.nip = (elem_type == 8) ? 8 : 1;
+            c.nip = (nn == 8) ? 8 : 1;
             c.n_nodes = n_nodes;
             c.xyz.assign(coords, coords + (size_t)3 * n_nodes);
             c.conn.assign(conn, conn + (size_t)n_elems * nn);
@@ -491,7 +492,7 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
 // (i*ny+j)*nz+k with corners in the hex8 order.  Enables ASEND_PC_MG.
 int asend_set_block_structure(asend_ctx* ctx, int32_t nx, int32_t ny, int32_t nz) {
     return guarded(ctx, [&](Ctx& c) {
-        require(c.type == 8, "block structure needs a hex8 mesh");
+        require(c.type == 8 || c.type == 81, "block structure needs a hex8 / brickIM mesh");
         require(nx > 0 && ny > 0 && nz > 0 && (int64_t)nx * ny * nz == c.n_el &&
                     (int64_t)(nx + 1) * (ny + 1) * (nz + 1) == c.n_nodes,
                 "block dimensions do not match the mesh");
@@ -668,11 +669,11 @@ int asend_add_nodal_force(asend_ctx* ctx, int32_t rhs, int32_t node_set, const d
 int asend_add_surface_traction(asend_ctx* ctx, int32_t rhs, int32_t elem_set, const double* norm_dir,
                                double norm_tol_deg, const double* traction) {
     return guarded(ctx, [&](Ctx& c) {
-        require(c.type == 8 || c.type == 4, "surface tractions apply to solid element faces");
+        require(c.type == 8 || c.type == 81 || c.type == 4, "surface tractions apply to solid element faces");
         ensure_case(c, rhs);
         require(elem_set >= 0 && elem_set < (int)c.elem_sets.size() && norm_dir && traction, "unknown element set");
-        const int nf = (c.type == 8) ? 6 : 4, fnn = (c.type == 8) ? 4 : 3;
-        auto face_nodes = [&](int fi) -> const int* { return c.type == 8 ? kHexFaces[fi] : kTetFaces[fi]; };
+        const int nf = (c.nn == 8) ? 6 : 4, fnn = (c.nn == 8) ? 4 : 3;
+        auto face_nodes = [&](int fi) -> const int* { return c.nn == 8 ? kHexFaces[fi] : kTetFaces[fi]; };
         auto key = [&](int e, int fi) {
             std::array<int32_t, 4> k{-1, -1, -1, -1};
             const int* ln = face_nodes(fi);
@@ -1046,9 +1047,10 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
 
 int asend_element_matrices(asend_ctx* ctx, int32_t first, int32_t count, double* ke, double* me) {
     return guarded(ctx, [&](Ctx& c) {
-        require(c.type == 41, "element matrix export is available for shell4 meshes");
+        require(c.type == 41 || c.type == 81, "element matrix export is available for shell4 and brickIM meshes");
         require(first >= 0 && count > 0 && (int64_t)first + count <= c.n_el && ke, "bad element range");
-        shell_element_matrices(c, first, count, ke, me);
+        if (c.type == 41) shell_element_matrices(c, first, count, ke, me);
+        else brickim_element_matrices(c, first, count, ke, me);
         return ASEND_OK;
     });
 }
@@ -1090,7 +1092,7 @@ int asend_learned_add_samples(asend_ctx* ctx, int32_t n_samples, const int32_t* 
         require(c.assembled, "assemble first");
         bool stationary = false;
         for (int s = 0; s < n_samples; ++s) stationary |= iters[s] < 0;
-        require(!stationary || (c.type == 8 && c.bx > 0), "multigrid samples need a structured hex8 block");
+        require(!stationary || ((c.type == 8 || c.type == 81) && c.bx > 0), "multigrid samples need a structured hex8 block");
         learned_add_samples(c, n_samples, iters, append != 0, seed);
         return ASEND_OK;
     });

@@ -253,6 +253,10 @@ int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool 
 void shell_assemble(Ctx& c, double* vals, double* mvals);
 void shell_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate);
 void shell_element_matrices(Ctx& c, int e0, int n, double* ke_host, double* me_host);
+// brickIM elements (k_brickim.cu)
+void brickim_assemble(Ctx& c, double* vals, double* mvals);
+void brickim_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate);
+void brickim_element_matrices(Ctx& c, int e0, int n, double* ke_host, double* me_host);
 // learned nodal preconditioner blocks (k_learned.cu)
 bool learned_ready(const Ctx& c);
 void learned_mesh_changed(Ctx& c);

@@ -176,6 +176,10 @@ void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g,
         shell_adjoint(c, d_b, d_a, d_g, accumulate);
         return;
     }
+    if (c.type == 81) {
+        brickim_adjoint(c, d_b, d_a, d_g, accumulate);
+        return;
+    }
     const int blocks = (c.n_el + 127) / 128;
     if (c.nn == 8)
         k_adjoint_modulus<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, d_a, d_b, d_g,

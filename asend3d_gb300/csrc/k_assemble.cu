@@ -309,6 +309,8 @@ void assemble_operator(Ctx& c, int precision) {
     ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
     if (c.type == 41) {
         shell_assemble(c, A.v64.p, mvals);  // FP64 element matrices at either precision
+    } else if (c.type == 81) {
+        brickim_assemble(c, A.v64.p, mvals);  // FP64 condensed element matrices at either precision
     } else if (precision == 64) {
         if (c.nn == 8) launch_colours<8, double>(c, A.v64.p, mvals);
         else launch_colours<4, double>(c, A.v64.p, mvals);

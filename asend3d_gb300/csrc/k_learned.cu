@@ -679,7 +679,7 @@ int learned_n_params() { return kNParam; }
 
 void learned_set_objective(Ctx& c, int kind) {
     if (kind != ASEND_LEARN_BLOCK && kind != ASEND_LEARN_MG) throw InputError("unknown learning objective");
-    if (kind == ASEND_LEARN_MG && (c.type != 8 || c.bx <= 0))
+    if (kind == ASEND_LEARN_MG && ((c.type != 8 && c.type != 81) || c.bx <= 0))
         throw InputError("the multigrid objective needs a structured hex8 block");
     state(c).objective = kind;
 }

@@ -1040,7 +1040,8 @@ SbView sbview(const MgLevel& L) {
 }
 
 void build_hierarchy(Ctx& c) {
-    if (c.type != 8 || c.bx <= 0) throw InputError("multigrid needs a structured hex8 block (asend_set_block_structure)");
+    if ((c.type != 8 && c.type != 81) || c.bx <= 0)
+        throw InputError("multigrid needs a structured hex8 / brickIM block (asend_set_block_structure)");
     auto H = std::make_shared<MgHierarchy>();
     auto L0 = std::make_unique<MgLevel>();
     L0->nx = c.bx;

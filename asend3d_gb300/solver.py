@@ -123,7 +123,7 @@ class GpuSolver:
                                             _ptr(conn, C.c_int32), _ptr(E, C.c_double), _ptr(nu, C.c_double),
                                             None if rho is None else _ptr(rho, C.c_double),
                                             None if thk is None else _ptr(thk, C.c_double)), "set_mesh")
-        if m.elem_type == 8 and m.conn.shape[0] == m.nx * m.ny * m.nz:
+        if m.elem_type in (8, 81) and m.conn.shape[0] == m.nx * m.ny * m.nz:
             self._check(self.lib.asend_set_block_structure(self.ctx, m.nx, m.ny, m.nz), "set_block_structure")
         for name, nodes in p.node_sets.items():
             arr = np.ascontiguousarray(nodes, dtype=np.int32)
@@ -278,7 +278,7 @@ class GpuSolver:
         return ms.value, by.value
 
     def element_matrices(self, first=0, count=None, mass=True):
-        """shell4 element stiffness (and mass) matrices [count][24][24]."""
+        """shell4 / brickIM element stiffness (and mass) matrices [count][24][24]."""
         n = self.p.mesh.n_elems - first if count is None else count
         ke = np.zeros((n, 24, 24))
         me = np.zeros((n, 24, 24)) if mass else None

@@ -23,7 +23,8 @@
  *   - One context per host thread; a context owns one CUDA stream.
  *   - DOF numbering is natural: dof = node * dof_per_node + component
  *     (component 0-based).  Element types use the reference codes:
- *     8 = hex8 (brick8), 4 = tet4, 41 = shell4 (quad shell).
+ *     8 = hex8 (brick8), 81 = brickIM (hex8 + 9 condensed incompatible
+ *     modes, the reference's default hex), 4 = tet4, 41 = shell4 (quad shell).
  */
 #ifndef ASEND_GPU_H
 #define ASEND_GPU_H
@@ -251,10 +252,11 @@ int64_t asend_kernel_launches(const asend_ctx* ctx);
  * its own CUDA events around library calls. */
 void* asend_stream(const asend_ctx* ctx);
 
-/* shell4 element matrices of elements [first, first + count): ke (and me
- * when not NULL) [count][24][24] in node-major DOF order (u v w thx thy thz
- * per node), stiffness after condensing the 8 internal DOF
- * (element_equations.rs:19-57), consistent section mass (:514-581). */
+/* shell4 / brickIM element matrices of elements [first, first + count): ke
+ * (and me when not NULL) [count][24][24] in node-major DOF order (shell4:
+ * u v w thx thy thz per node; brickIM: u v w per node), stiffness after
+ * condensing the internal DOF (element_equations.rs:19-57: 8 for shell4, 9
+ * for brickIM), consistent mass over the node DOF (:420-626). */
 int asend_element_matrices(asend_ctx* ctx, int32_t first, int32_t count, double* ke, double* me);
 
 /* y = A x and *energy = x^T A x with the assembled FP64 operator, on DEVICE

@@ -55,6 +55,11 @@ TypeInfo type_info(int type) {
         const int f[6][4] = {{3, 2, 1, 0}, {4, 5, 6, 7}, {0, 1, 5, 4},
                              {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
         std::memcpy(t.faces, f, sizeof(f));
+    } else if (type == 81) {
+        // brickIM: hex8 points, faces and nodes plus 9 internal DOF
+        // (element_meth.rs:157-201)
+        t = type_info(8);
+        t.type = 81;
     } else if (type == 41) {
         // shell4 as 8 pseudo-nodes of 3 DOF: node a's translations are
         // pseudo-node 2a, its rotations 2a+1, so DOF 6a + c keeps the
@@ -228,7 +233,13 @@ void solid_bmat(int nn, const double* dndx, double* B) {
 // Element stiffness: element_equations.rs:206-418 (get_ruk_dfd0 with
 // get_matrix, linear geometry, dpn == 3): K += B^T (C B) detJ w per point,
 // with C*B scaled by detJ*w first (:377-395).
+void brickim_ke(const double* xyz, const double* C, double* ke);
+
 void solid_ke(int type, const double* xyz, const double* C, double* ke) {
+    if (type == 81) {
+        brickim_ke(xyz, C, ke);
+        return;
+    }
     const TypeInfo t = type_info(type);
     const int nn = t.nn, tot = 3 * nn;
     std::fill(ke, ke + tot * tot, 0.0);
@@ -252,8 +263,82 @@ void solid_ke(int type, const double* xyz, const double* C, double* ke) {
     }
 }
 
+// brickIM (type 81) stiffness: hex8 plus the bubbles 1-s^2, 1-t^2, 1-u^2 on
+// each displacement component (element_soln_fields.rs:212-227, dof_table
+// element_meth.rs:192-201), whose derivatives at the point use the centroid
+// Jacobian (element_soln_fields.rs:424-461); the 9 internal DOF are condensed
+// (element_equations.rs:19-57).
+void brickim_ke(const double* xyz, const double* C, double* ke) {
+    constexpr int tot = 33, nd = 24;
+    const TypeInfo t = type_info(8);
+    double n0[8], dn0[24], J0[9] = {0}, Ji0[9];
+    const double s0[3] = {0.0, 0.0, 0.0};
+    shape(8, s0, n0, dn0);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int a = 0; a < 8; ++a) J0[3 * i + j] += xyz[3 * a + i] * dn0[3 * a + j];
+    det_inv(Ji0, J0, 3);
+    std::vector<double> K(tot * tot, 0.0), B(6 * tot), CB(6 * tot);
+    double n[8], dndx[24], B24[6 * 24];
+    for (int p = 0; p < t.nip; ++p) {
+        const double* sp = t.ip + 3 * p;
+        const double det = ip_data(8, 8, xyz, sp, n, dndx);
+        const double djw = det * t.wt[p];
+        solid_bmat(8, dndx, B24);
+        std::fill(B.begin(), B.end(), 0.0);
+        for (int k = 0; k < 6; ++k)
+            for (int c = 0; c < nd; ++c) B[k * tot + c] = B24[k * 24 + c];
+        for (int f = 0; f < 3; ++f) {  // bubble f: d/ds_f = -2 s_f
+            double g[3];
+            for (int j = 0; j < 3; ++j) g[j] = -2.0 * sp[f] * Ji0[3 * f + j];
+            for (int d = 0; d < 3; ++d) {
+                const int col = nd + 3 * f + d;
+                double sm[9] = {0};
+                for (int i = 0; i < 3; ++i)
+                    for (int j = i; j < 3; ++j) {
+                        if (i == d) sm[3 * i + j] += g[j];
+                        if (j == d) sm[3 * i + j] += g[i];
+                    }
+                B[0 * tot + col] = 0.5 * sm[0];
+                B[1 * tot + col] = 0.5 * sm[4];
+                B[2 * tot + col] = 0.5 * sm[8];
+                B[3 * tot + col] = sm[1];
+                B[4 * tot + col] = sm[2];
+                B[5 * tot + col] = sm[5];
+            }
+        }
+        for (int k = 0; k < 6; ++k)
+            for (int c = 0; c < tot; ++c) {
+                double acc = 0.0;
+                for (int l = 0; l < 6; ++l) acc += C[6 * k + l] * B[l * tot + c];
+                CB[k * tot + c] = acc * djw;
+            }
+        for (int i = 0; i < tot; ++i)
+            for (int j = 0; j < tot; ++j) {
+                double acc = 0.0;
+                for (int k = 0; k < 6; ++k) acc += B[k * tot + i] * CB[k * tot + j];
+                K[i * tot + j] += acc;
+            }
+    }
+    double Kii[81];
+    for (int i = 0; i < 9; ++i)
+        for (int j = 0; j < 9; ++j) Kii[9 * i + j] = K[(nd + i) * tot + nd + j];
+    givens_factor(Kii, 9);
+    for (int r = 0; r < nd; ++r) {
+        double rhs[9], x[9];
+        for (int i = 0; i < 9; ++i) rhs[i] = K[(nd + i) * tot + r];
+        givens_solve(x, Kii, rhs, 9);
+        for (int c = 0; c < nd; ++c) {
+            double acc = 0.0;
+            for (int i = 0; i < 9; ++i) acc += K[c * tot + nd + i] * x[i];
+            ke[c * nd + r] = K[c * tot + r] - acc;
+        }
+    }
+}
+
 // Consistent mass: element_equations.rs:583-609 (get_rum_dfd0, solid branch)
 void solid_me(int type, const double* xyz, double rho, double* me) {
+    if (type == 81) type = 8;  // the internal DOF carry no mass (element_equations.rs:420-626)
     const TypeInfo t = type_info(type);
     const int nn = t.nn, tot = 3 * nn;
     std::fill(me, me + tot * tot, 0.0);
@@ -898,7 +983,7 @@ extern "C" {
 orc_model* orc_create(int32_t elem_type, int32_t n_nodes, const double* coords, int32_t n_elems,
                       const int32_t* conn, const double* E, const double* nu, const double* rho,
                       const double* thickness) {
-    if (elem_type != 8 && elem_type != 4 && elem_type != 41) return nullptr;
+    if (elem_type != 8 && elem_type != 81 && elem_type != 4 && elem_type != 41) return nullptr;
     auto* m = new orc_model();
     m->ti = type_info(elem_type);
     m->n_el = n_elems;
@@ -1020,7 +1105,7 @@ int orc_element_stiffness(int32_t elem_type, const double* xyz, double E, double
         shell_km(xyz, E, nu, 0.0, thickness, ke, nullptr);
         return 0;
     }
-    if (elem_type != 8 && elem_type != 4) return -1;
+    if (elem_type != 8 && elem_type != 81 && elem_type != 4) return -1;
     double C[36];
     iso_cmat(E, nu, C);
     solid_ke(elem_type, xyz, C, ke);
@@ -1036,7 +1121,7 @@ int orc_element_mass(int32_t elem_type, const double* xyz, double rho, double th
         shell_km(xyz, 1.0, 0.3, rho, thickness, ke.data(), me);
         return 0;
     }
-    if (elem_type != 8 && elem_type != 4) return -1;
+    if (elem_type != 8 && elem_type != 81 && elem_type != 4) return -1;
     solid_me(elem_type, xyz, rho, me);
     return 0;
 }
@@ -1210,7 +1295,7 @@ int orc_adjoint_modulus_gradient(orc_model* m, const double* u, const double* dL
 // inverse of :724-760).
 int orc_adjoint_modulus_component_gradient(orc_model* m, const double* u, const double* lambda,
                                            int32_t component, double* gD) {
-    if (component < 1 || component > 3 || m->shell) return -1;
+    if (component < 1 || component > 3 || m->shell || m->ti.type == 81) return -1;
     const int k = component - 1;
     const TypeInfo& t = m->ti;
     const int nn = t.nn, tot = 3 * nn;

@@ -295,3 +295,56 @@ def test_shell_element_properties(oracle_lib):
     # a non-planar element is rejected
     xyz[2, 2] = 0.1
     assert lib.orc_element_stiffness(41, xyz.ctypes.data_as(P), 7e10, 0.33, 0.005, ke.ctypes.data_as(P)) != 0
+
+
+def test_brickim_beam_bending_pin(oracle_lib):
+    """brickIM (type 81, the reference's default hex element) on the hexBeam
+    case: tip deflection F L^3 / 3EI = 8 and dw/dE = -8e-6
+    (examples/testCases/hexBeam/notes.txt:10-13); plain hex8 locks in
+    bending on the one-element-thick bar."""
+    po = oracle_lib
+    pin = pins()["hexBeam_transverse_tip"]
+    out = {}
+    for et in (8, 81):
+        m = block_hex8(100, 10, 1, 10.0, 1.0, 0.1)
+        m.elem_type = et
+        p = Problem(m, np.full(m.n_elems, 1e6), np.full(m.n_elems, 0.0), None)
+        p.add_node_set("xMin", m.nodes_in_range(xr=(-0.1, 0.1)))
+        p.fix_displacement("xMin")
+        xmax = m.nodes_in_range(xr=(9.99, 10.01))
+        p.add_node_set("xMax", xmax)
+        p.add_nodal_force("xMax", [0.0, 0.0, 2.0 / len(xmax)])
+        o = po.Oracle(p)
+        u, rc, st = o.solve(o.loads()[0] + o.penalty_rhs(), precond=po.PC_DIRECT)
+        w = u[3 * xmax + 2].mean()
+        out[et] = w
+        if et == 81:
+            assert w == pytest.approx(pin["value"], rel=pin["rtol"])
+            dLdu = np.zeros(o.n_dof)
+            dLdu[3 * xmax + 2] = 1.0 / len(xmax)
+            g, _, _, _ = o.adjoint(u, dLdu=dLdu, precond=po.PC_DIRECT)
+            assert g.sum() == pytest.approx(pin["dwdE"], rel=pin["rtol"])
+            assert g.sum() == pytest.approx(-w / 1e6, rel=1e-8)
+    assert out[8] < 0.8 * out[81]  # hex8 locks
+
+
+def test_brickim_element_properties(oracle_lib):
+    """Condensed brickIM stiffness: symmetric PSD with six rigid-body modes,
+    softer in bending than hex8 on a distorted element; same mass as hex8."""
+    import ctypes as C
+    lib = oracle_lib.load()
+    P = C.POINTER(C.c_double)
+    rng = np.random.default_rng(4)
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float)
+    xyz += rng.uniform(-0.1, 0.1, xyz.shape)
+    k81, k8, m81, m8 = (np.zeros(576) for _ in range(4))
+    assert lib.orc_element_stiffness(81, xyz.ctypes.data_as(P), 2e11, 0.3, 0.0, k81.ctypes.data_as(P)) == 0
+    assert lib.orc_element_stiffness(8, xyz.ctypes.data_as(P), 2e11, 0.3, 0.0, k8.ctypes.data_as(P)) == 0
+    assert lib.orc_element_mass(81, xyz.ctypes.data_as(P), 7850.0, 0.0, m81.ctypes.data_as(P)) == 0
+    assert lib.orc_element_mass(8, xyz.ctypes.data_as(P), 7850.0, 0.0, m8.ctypes.data_as(P)) == 0
+    K, K8 = k81.reshape(24, 24), k8.reshape(24, 24)
+    assert np.abs(K - K.T).max() <= 1e-10 * np.abs(K).max()
+    ev = np.linalg.eigvalsh(0.5 * (K + K.T))
+    assert np.sum(ev < 1e-9 * ev[-1]) == 6 and ev[0] > -1e-9 * ev[-1]
+    assert np.all(np.linalg.eigvalsh(K8 - K) > -1e-6 * ev[-1])  # condensation only softens
+    np.testing.assert_array_equal(m81, m8)
