@@ -259,7 +259,24 @@ k_brick_export(int e0, const int32_t* __restrict__ conn, const double* __restric
     }
 }
 
+// all condensed element stiffness matrices, FP32 [n_el][24][24] (the fine
+// level's input to Galerkin multigrid coarsening)
+__global__ void __launch_bounds__(kBT)
+k_brick_ke32(const int32_t* __restrict__ conn, const double* __restrict__ xyz, const double* __restrict__ E,
+             const double* __restrict__ nu, float* __restrict__ ke) {
+    __shared__ BrickSmem S;
+    const int e = blockIdx.x;
+    brick_element(S, e, conn, xyz, E, nu, nullptr);
+    for (int q = threadIdx.x; q < kNd * kNd; q += kBT) ke[(size_t)e * kNd * kNd + q] = (float)S.K24[q / kNd][q % kNd];
+}
+
 }  // namespace
+
+void brickim_element_ke32(Ctx& c, float* d_ke) {
+    k_brick_ke32<<<c.n_el, kBT, 0, c.stream>>>(c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, d_ke);
+    ASEND_CUDA(cudaGetLastError());
+    ++c.launches;
+}
 
 void brickim_assemble(Ctx& c, double* vals, double* mvals) {
     const int n_col = (int)c.colour_ptr.size() - 1;

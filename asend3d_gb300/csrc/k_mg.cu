@@ -1214,8 +1214,19 @@ void setup_values(Ctx& c) {
     for (size_t l = 1; l < H.L.size(); ++l) {
         MgLevel& L = *H.L[l];
         MgLevel& F = *H.L[l - 1];
-        k_coarsen<<<L.n_el, 512, 0, c.stream>>>(view_of(L), F.ny, F.nz, l == 1 ? nullptr : F.Ke.p, c.d_xyz.p,
-                                                c.d_conn.p, c.d_E.p, c.d_nu.p, L.Ke.p);
+        const float* fine_ke = F.Ke.p;
+        if (l == 1) {
+            // level 0: hex8 matrices are integrated inside k_coarsen; brickIM
+            // ones (condensed incompatible modes) are computed first
+            fine_ke = nullptr;
+            if (c.type == 81) {
+                F.Ke.alloc((size_t)c.n_el * 576);
+                brickim_element_ke32(c, F.Ke.p);
+                fine_ke = F.Ke.p;
+            }
+        }
+        k_coarsen<<<L.n_el, 512, 0, c.stream>>>(view_of(L), F.ny, F.nz, fine_ke, c.d_xyz.p, c.d_conn.p, c.d_E.p,
+                                                c.d_nu.p, L.Ke.p);
         L.own.v32.zero(c.stream);
         for (size_t k = 0; k + 1 < L.colour_ptr.size(); ++k) {
             const int n = L.colour_ptr[k + 1] - L.colour_ptr[k];
