@@ -822,7 +822,7 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_xr(MgPcg M) {
 }
 
 // mode 0: after an iteration's V-cycle -> beta (Polak-Ribiere), rz
-// mode 1: initialisation -> p = z, rz
+// mode 1: initialisation, or a restart after a replacement -> p = z, rz
 // mode 2: after a residual replacement -> rz only
 template <typename TP>
 __global__ void __launch_bounds__(kThreads) k_mg_rz(MgPcg M, int mode) {
@@ -1609,7 +1609,9 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
             const bool periodic = o.replace_every > 0 && since_repl >= o.replace_every;
             if (h->done || drop || periodic) {
                 launch_residual(0);
-                launch_start(2);
+                // after convergence of the recurrence the last p update was
+                // skipped: restart the direction (p = z); otherwise keep p
+                launch_start(h->done ? 1 : 2);
                 ++repl;
                 since_repl = 0;
                 continue;

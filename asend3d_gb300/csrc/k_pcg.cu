@@ -142,6 +142,7 @@ __global__ void __launch_bounds__(kThreads) k_update_xr(PcgArgs A) {
                     s.done = 1;
                 } else if (s.rr <= s.target) {
                     s.done = 1;  // recurrence converged: the host verifies in FP64
+                    s.restart = 1;
                 }
             }
             all &= s.done;
@@ -222,7 +223,9 @@ __global__ void __launch_bounds__(kThreads) k_residual(PcgArgs A, int mode, doub
                 A.r[o + a] = rv[a];
             }
             precond<PC>(A, row, rv, z);
-            if (mode == 0) PadVec<TP>::store(A.p, (size_t)k * A.n_rows + row, z);
+            // initial residual, or a replacement after the recurrence converged
+            // (the last p update was skipped): restart the direction p = z
+            if (mode == 0 || S[k].restart) PadVec<TP>::store(A.p, (size_t)k * A.n_rows + row, z);
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 d[k][0] += rv[a] * z[a];
@@ -248,6 +251,7 @@ __global__ void __launch_bounds__(kThreads) k_residual(PcgArgs A, int mode, doub
                     s.beta = 0.0;
                 }
                 s.replace = 0;
+                s.restart = 0;
                 s.nonfinite = (!isfinite(s.rr) || !isfinite(s.rz)) ? 1 : 0;
                 s.finished = (s.rr <= s.target) || s.nonfinite;
                 s.done = s.finished;

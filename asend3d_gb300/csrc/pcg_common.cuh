@@ -11,7 +11,9 @@ constexpr int kMaxRhs = 4;
 
 struct RhsScalars {
     double rz, rz_new, pAp, rr, bb, alpha, beta, target, rr_last_true;
-    int32_t iter, done, finished, replace, nonfinite, pad0, pad1, pad2;
+    int32_t iter, done, finished, replace, nonfinite;
+    int32_t restart;  // done by convergence: that iteration's p update was skipped
+    int32_t pad1, pad2;
 };
 struct Control {
     int32_t all_done;
