@@ -5,7 +5,8 @@ Tolerances (written here, per quantity):
   * element stiffness / mass (FP64 both sides; Gauss-Jordan vs the
     reference's Givens-QR condensation): 1e-11 relative to max|K_e|, max|M_e|;
   * assembled operator: pattern bit-exact, values 2e-11 relative to max|K|;
-  * displacements after a solve to rel. residual 1e-10: 1e-6 relative;
+  * displacements after a solve to rel. residual 1e-8 (the thin beam's FP64
+    floor): 1e-6 relative;
   * adjoint modulus gradients: 1e-5 relative (norm-wise).
 """
 import ctypes as C
@@ -51,7 +52,7 @@ def test_brickim_beam_bending_and_adjoint(gpu_lib, oracle_lib):
     m = block_hex8(100, 10, 1, 10.0, 1.0, 0.1)
     m.elem_type = 81
     p = Problem(m, np.full(m.n_elems, 1e6), np.full(m.n_elems, 0.0), None)
-    p.add_node_set("xMin", m.nodes_in_range(xr=(-0.1, 0.1)))
+    p.add_node_set("xMin", m.nodes_in_range(xr=(-0.01, 0.01)))  # clamp at x = 0 only
     p.fix_displacement("xMin")
     xmax = m.nodes_in_range(xr=(9.99, 10.01))
     p.add_node_set("xMax", xmax)
@@ -65,20 +66,21 @@ def test_brickim_beam_bending_and_adjoint(gpu_lib, oracle_lib):
     np.testing.assert_array_equal(rp, rpo)
     np.testing.assert_array_equal(col, colo)
     assert np.abs(val - valo).max() <= 2e-11 * np.abs(valo).max()
-    # point Jacobi: this one-element-thick, 100:1 beam is no multigrid case
-    kw = dict(method=_lib.METHOD_FP64, precond=_lib.PC_JACOBI, rel_tol=1e-10, max_iter=400000)
+    # the penalty-stiffened thin beam's FP64 true residual bottoms out near
+    # 1e-8 (every preconditioner), so parity is checked at that tolerance
+    kw = dict(method=_lib.METHOD_FP64, precond=_lib.PC_JACOBI, rel_tol=1e-8, max_iter=400000)
     u, rc, st = g.static_solve(**kw)
     assert rc == _lib.ASEND_OK, st
     uo, _, _ = o.solve(o.loads()[0] + o.penalty_rhs(), precond=oracle_lib.PC_DIRECT)
     assert rel(u[0], uo) < 1e-6
-    assert u[0][3 * xmax + 2].mean() == pytest.approx(8.0, rel=0.03)
+    assert u[0][3 * xmax + 2].mean() == pytest.approx(8.0, rel=1e-3)
     L, gE, rc, st = g.adjoint_gradient(**kw)
     assert rc == _lib.ASEND_OK
     dLdu = np.zeros(o.n_dof)
     dLdu[3 * xmax + 2] = 1.0 / len(xmax)
     go, _, _, _ = o.adjoint(uo, dLdu=dLdu, precond=oracle_lib.PC_DIRECT)
     assert rel(gE, go) < 1e-5
-    assert gE.sum() == pytest.approx(-8e-6, rel=0.03)
+    assert gE.sum() == pytest.approx(-8e-6, rel=1e-3)
     g.close()
 
 

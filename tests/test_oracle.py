@@ -309,7 +309,7 @@ def test_brickim_beam_bending_pin(oracle_lib):
         m = block_hex8(100, 10, 1, 10.0, 1.0, 0.1)
         m.elem_type = et
         p = Problem(m, np.full(m.n_elems, 1e6), np.full(m.n_elems, 0.0), None)
-        p.add_node_set("xMin", m.nodes_in_range(xr=(-0.1, 0.1)))
+        p.add_node_set("xMin", m.nodes_in_range(xr=(-0.01, 0.01)))  # clamp at x = 0 only
         p.fix_displacement("xMin")
         xmax = m.nodes_in_range(xr=(9.99, 10.01))
         p.add_node_set("xMax", xmax)
