@@ -39,6 +39,20 @@ class SolveStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class EigenOpts(C.Structure):
+    _fields_ = [("n_modes", c_int), ("block_size", c_int), ("max_subspace", c_int), ("reserved", c_int),
+                ("shift", c_dbl), ("tol", c_dbl), ("inner", SolveOpts)]
+
+
+class EigenStats(C.Structure):
+    _fields_ = [("n_found", c_int), ("n_converged", c_int), ("subspace", c_int), ("n_solves", c_int),
+                ("inner_iterations", C.c_int64), ("status", c_int), ("inner_capped", c_int),
+                ("max_rel_residual", c_dbl), ("max_pencil_residual", c_dbl), ("ms", c_dbl)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # (name, restype, argtypes) for every symbol declared in include/asend_gpu.h
 SIGNATURES = [
     ("asend_create", C.c_void_p, [c_int]),
@@ -80,6 +94,9 @@ SIGNATURES = [
     ("asend_kernel_launches", C.c_int64, [C.c_void_p]),
     ("asend_stream", C.c_void_p, [C.c_void_p]),
     ("asend_element_matrices", c_int, [C.c_void_p, c_int, c_int, P_dbl, P_dbl]),
+    ("asend_eigen_solve", c_int, [C.c_void_p, C.POINTER(EigenOpts), P_dbl, P_dbl, P_dbl, P_dbl,
+                                  C.POINTER(EigenStats)]),
+    ("asend_dense_sym_eigen", c_int, [c_int, P_dbl, P_dbl, P_dbl]),
     ("asend_operator_energy_noalloc", c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("asend_learned_n_params", c_int, []),
     ("asend_learned_init", c_int, [C.c_void_p, C.c_uint64]),

@@ -774,16 +774,16 @@ int asend_assemble(asend_ctx* ctx, int32_t precision, int32_t dynamic, double dt
     return guarded(ctx, [&](Ctx& c) {
         require(c.n_el > 0, "set the mesh first");
         require(precision == 32 || precision == 64, "precision must be 32 or 64");
-        if (dynamic) {
-            require(dt > 0.0 && beta != gamma, "Newmark needs dt > 0 and beta != gamma");
-            for (double r : c.rho) require(r > 0.0, "dynamic assembly needs positive densities");
-        }
+        require(dynamic >= 0 && dynamic <= 2, "dynamic must be 0, 1 or 2");
+        if (dynamic == 1) require(dt > 0.0 && beta != gamma, "Newmark needs dt > 0 and beta != gamma");
+        if (dynamic) for (double r : c.rho) require(r > 0.0, "dynamic / modal assembly needs positive densities");
         ASEND_CUDA(cudaSetDevice(c.device));
         c.dynamic = dynamic != 0;
+        c.modal = dynamic == 2;
         c.dt = dt;
         c.beta = beta;
         c.gamma = gamma;
-        c.cM = c.dynamic ? -1.0 / (dt * dt * (beta - gamma)) : 0.0;
+        c.cM = dynamic == 1 ? -1.0 / (dt * dt * (beta - gamma)) : 0.0;
         if (!c.pattern_ready) build_pattern(c);
         assemble_operator(c, precision);
         c.assembled = true;
@@ -1011,10 +1011,36 @@ int asend_newmark_run(asend_ctx* ctx, const asend_solve_opts* opts, int32_t n_st
                       int32_t probe_dof, double* probe_hist, double* u_final, asend_solve_stats* stats) {
     return guarded(ctx, [&](Ctx& c) {
         require(opts && amp && n_steps > 0, "bad Newmark arguments");
-        require(c.assembled && c.dynamic, "assemble with dynamic=1 first");
+        require(c.assembled && c.dynamic && !c.modal, "assemble with dynamic=1 first");
         require(probe_dof < c.n_dof, "probe DOF out of range");
         return newmark_run(c, *opts, n_steps, amp, probe_dof, probe_hist, u_final, stats);
     });
+}
+
+int asend_eigen_solve(asend_ctx* ctx, const asend_eigen_opts* opts, double* eig_out, double* freq_out,
+                      double* modes_out, double* diag_mass_out, asend_eigen_stats* stats) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(opts != nullptr, "null options");
+        require(c.n_el > 0, "set the mesh first");
+        require(c.n_inst <= 1, "modal analysis takes one model, not a batch of instances");
+        for (double r : c.rho) require(r > 0.0, "modal analysis needs positive densities");
+        ASEND_CUDA(cudaSetDevice(c.device));
+        if (!(c.assembled && c.modal)) {
+            c.dynamic = true;
+            c.modal = true;
+            c.cM = 0.0;
+            if (!c.pattern_ready) build_pattern(c);
+            assemble_operator(c, 64);
+            c.assembled = true;
+            c.solved = false;
+        }
+        return eigen_solve(c, *opts, eig_out, freq_out, modes_out, diag_mass_out, stats);
+    });
+}
+
+int asend_dense_sym_eigen(int32_t m, const double* a, double* vals, double* vecs) {
+    if (m < 0 || (m > 0 && (!a || !vals))) return ASEND_EINVAL;
+    return sym_eigen_dense(m, a, vals, vecs) == 0 ? ASEND_OK : ASEND_MAX_ITER;
 }
 
 int asend_add_modulus_design_var(asend_ctx* ctx, int32_t elem_set, int32_t n_coef, const double* coefs) {

@@ -136,6 +136,7 @@ struct Ctx {
     DArr<int32_t> d_shell_conn;  // shell4: 4 physical nodes per element
     DArr<double> d_shell_xyz;    // shell4: physical node coordinates
     bool pattern_ready = false, assembled = false, dynamic = false;
+    bool modal = false;  // K and M assembled apart (c_M = 0) for the frequency job
     double dt = 0, beta = 0.25, gamma = 0.5, cM = 0;
     double sf = 0;
     int assembled_precision = 64;
@@ -231,6 +232,9 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
 void device_dot(Ctx& c, size_t n, const double* a, const double* b, double* d_out, double* d_part);
 void device_axpy(Ctx& c, size_t n, double alpha, const double* x, double* y);
 void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g, bool accumulate);
+int eigen_solve(Ctx& c, const asend_eigen_opts& eo, double* eig_out, double* freq_out, double* modes_out,
+                double* diag_mass_out, asend_eigen_stats* st);
+int sym_eigen_dense(int m, const double* a, double* vals, double* vecs);
 int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* amp, int probe,
                 double* probe_hist, double* u_final, asend_solve_stats* st);
 void upload_rhs(Ctx& c);

@@ -249,6 +249,26 @@ class GpuSolver:
                          "newmark_run")
         return hist, u, rc, st.as_dict()
 
+    def eigen(self, n_modes, shift=0.0, block_size=2, tol=1e-8, max_subspace=0, modes=True, **inner):
+        """Frequency job: the n_modes eigenpairs of (K + penalty) x = lambda D x
+        nearest to ``shift`` (lowest first), D the row-sum diagonal mass.
+        ``inner`` are the shift-invert solve options (default FP64 Jacobi PCG
+        to 1e-10).  Returns (eigenvalues, frequencies [Hz], modes [n, n_dof]
+        or None, diagonal mass, rc, stats)."""
+        kw = dict(method=_lib.METHOD_FP64, precond=_lib.PC_JACOBI, rel_tol=1e-10)
+        kw.update(inner)
+        eo = _lib.EigenOpts(n_modes, block_size, max_subspace, 0, shift, tol, self.opts(**kw))
+        ev = np.zeros(n_modes)
+        fr = np.zeros(n_modes)
+        vecs = np.zeros((n_modes, self.n_dof)) if modes else None
+        dm = np.zeros(self.n_dof)
+        st = _lib.EigenStats()
+        rc = self._check(self.lib.asend_eigen_solve(self.ctx, C.byref(eo), _ptr(ev, C.c_double), _ptr(fr, C.c_double),
+                                                    None if vecs is None else _ptr(vecs, C.c_double),
+                                                    _ptr(dm, C.c_double), C.byref(st)), "eigen_solve")
+        k = st.n_found
+        return ev[:k], fr[:k], None if vecs is None else vecs[:k], dm, rc, st.as_dict()
+
     def csr(self, which=0):
         nnz = C.c_int64(0)
         self._check(self.lib.asend_get_csr(self.ctx, which, C.byref(nnz), None, None, None), "get_csr")

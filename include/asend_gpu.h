@@ -179,8 +179,9 @@ int asend_get_load_vector(asend_ctx* ctx, int32_t rhs, double* f_out);
  *      element kernels element_equations.rs:206-418 / 852-1062) ------------
  * precision: 64 = FP64 element integration (FP32 copy made by rounding),
  *            32 = FP32 element integration (FP64 copy made by widening).
- * dynamic != 0 assembles K + c_M M with c_M = -1/(dt^2 (beta - gamma)) and
- * keeps M (Newmark, element_equations.rs:977-988). */
+ * dynamic = 1 assembles K + c_M M with c_M = -1/(dt^2 (beta - gamma)) and
+ * keeps M (Newmark, element_equations.rs:977-988); dynamic = 2 assembles K
+ * and keeps M apart (modal analysis; dt, beta, gamma unused). */
 int asend_assemble(asend_ctx* ctx, int32_t precision, int32_t dynamic, double dt, double beta,
                    double gamma);
 /* Assembled operator (K [+ c_M M] + sf C^T C) as scalar CSR in natural DOF
@@ -251,6 +252,55 @@ int64_t asend_kernel_launches(const asend_ctx* ctx);
 /* The context's CUDA stream (cudaStream_t as void*), so a caller can record
  * its own CUDA events around library calls. */
 void* asend_stream(const asend_ctx* ctx);
+
+/* ---- modal analysis (frequency job: Model::eigen_solve model_analysis.rs:711-880,
+ *      eigen_sparse_direct matrix_functions.rs:1099-1265) -------------------
+ * The n_modes eigenpairs of (K + sf C^T C) x = lambda D x nearest to the
+ * shift (the reference's tgtEval), lowest first.  D is the row-sum diagonal
+ * mass (model_analysis.rs:748-766) with entries below 1e-6 mean|D| raised to
+ * it (:768-779).  Shift-invert block Lanczos on D^1/2 (A - shift D)^-1 D^1/2
+ * with full reorthogonalisation; the inner solves use `inner` (any method /
+ * preconditioner of asend_static_solve; A - shift D must be positive
+ * definite).  Assembles K and M itself (FP64, c_M = 0) unless the last
+ * assembly was asend_assemble(..., dynamic = 2).  Outputs (each may be NULL):
+ * eig_out[n_modes], freq_out[n_modes] = sqrt(lambda) / (2 pi) (-1 for
+ * lambda < 0, :874-879), modes_out[n_modes][n_dof] at unit 2-norm with the
+ * largest-magnitude component positive, diag_mass_out[n_dof].  Returns
+ * ASEND_OK when every wanted pair met tol, else ASEND_MAX_ITER (results
+ * still written). */
+typedef struct asend_eigen_opts {
+    int32_t n_modes;        /* eigenpairs wanted                                       */
+    int32_t block_size;     /* right-hand sides per shift-invert solve, 1..4 (0 = 2)   */
+    int32_t max_subspace;   /* basis size cap (0 = max(5 n_modes, n_modes + 20)
+                               x max(1, block_size / 2))                               */
+    int32_t reserved;
+    double shift;           /* tgtEval; eigenvalues are returned unshifted              */
+    double tol;             /* Ritz residual ||Op y - theta y|| <= tol theta (0 = 1e-8)   */
+    asend_solve_opts inner; /* options of the shift-invert solves                      */
+} asend_eigen_opts;
+
+typedef struct asend_eigen_stats {
+    int32_t n_found;        /* pairs written                                           */
+    int32_t n_converged;    /* pairs within tol                                         */
+    int32_t subspace;       /* Lanczos basis size at exit                               */
+    int32_t n_solves;       /* shift-invert right-hand sides solved                     */
+    int64_t inner_iterations;
+    int32_t status;
+    int32_t inner_capped;   /* shift-invert solves that stopped at their iteration cap  */
+    double max_rel_residual;/* max_k Ritz residual ||Op y_k - theta_k y_k|| / theta_k,
+                               Op = D^1/2 (A - shift D)^-1 D^1/2 (the stopping measure) */
+    double max_pencil_residual; /* max_k ||A x_k - lambda_k D x_k|| / ||A x_k|| (FP64);
+                               the penalty rows (sf = 1e5 max|K|) dominate it          */
+    double ms;              /* device time                                              */
+} asend_eigen_stats;
+
+int asend_eigen_solve(asend_ctx* ctx, const asend_eigen_opts* opts, double* eig_out, double* freq_out,
+                      double* modes_out, double* diag_mass_out, asend_eigen_stats* stats);
+
+/* Dense symmetric eigenproblem of a row-major m x m matrix (host routine of
+ * the Lanczos projection; no device needed): eigenvalues ascending in
+ * vals[m], vecs[k*m + i] = component i of eigenvector k (may be NULL). */
+int asend_dense_sym_eigen(int32_t m, const double* a, double* vals, double* vecs);
 
 /* shell4 / brickIM element matrices of elements [first, first + count): ke
  * (and me when not NULL) [count][24][24] in node-major DOF order (shell4:

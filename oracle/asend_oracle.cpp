@@ -13,6 +13,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <vector>
 
@@ -975,6 +976,145 @@ int pcg(orc_model* m, Precond& pc, const double* rhs, double* soln, int stop_rul
 
 }  // namespace
 
+
+// ---------------------------------------------------------------------------
+// Modal analysis (frequency job): model_analysis.rs:711-880 and
+// matrix_functions.rs:940-1265
+// ---------------------------------------------------------------------------
+namespace {
+
+// sym_eigen_solve (matrix_functions.rs:940-1097) with tri_diag = 1: pair i
+// starts from sin(j (i+1)), is Gram-Schmidt projected off the converged
+// vectors and iterated v <- T v / |T v| (T v deflated likewise) until
+// |v.Tv| >= (1 - 1e-8) |T v| or 10000 products; eigenvalue = v.Tv; the
+// pairs are sorted ascending (bubble sort, stable for ties).  T is row-major
+// d x d, read on its tridiagonal band only.
+void sym_eigen_tri(const std::vector<double>& T, int d, std::vector<double>& vals, std::vector<double>& vecs) {
+    std::vector<double> v1(d), v2(d), tmp((size_t)d * d);
+    vals.assign(d, 0.0);
+    for (int i = 0; i < d; ++i) {
+        for (int j = 0; j < d; ++j) v1[j] = std::sin((double)j * (double)(i + 1));
+        for (int k = 0; k < i; ++k) {
+            double dp = 0.0;
+            for (int j = 0; j < d; ++j) dp += v1[j] * tmp[(size_t)k * d + j];
+            for (int j = 0; j < d; ++j) v1[j] -= dp * tmp[(size_t)k * d + j];
+        }
+        double mag = 0.0;
+        for (int j = 0; j < d; ++j) mag += v1[j] * v1[j];
+        mag = 1.0 / std::sqrt(mag);
+        for (int j = 0; j < d; ++j) v1[j] *= mag;
+        double dp = 0.0;
+        int loops = 0;
+        while (std::fabs(dp) < 0.99999999 * mag && loops < 10000) {
+            for (int r = 0; r < d; ++r) {
+                const int c0 = r == 0 ? 0 : r - 1, c1 = std::min(r + 2, d);
+                double acc = 0.0;
+                for (int c = c0; c < c1; ++c) acc += T[(size_t)r * d + c] * v1[c];
+                v2[r] = acc;
+            }
+            for (int k = 0; k < i; ++k) {
+                double q = 0.0;
+                for (int j = 0; j < d; ++j) q += v2[j] * tmp[(size_t)k * d + j];
+                for (int j = 0; j < d; ++j) v2[j] -= q * tmp[(size_t)k * d + j];
+            }
+            mag = 0.0;
+            dp = 0.0;
+            for (int j = 0; j < d; ++j) {
+                mag += v2[j] * v2[j];
+                dp += v1[j] * v2[j];
+            }
+            mag = std::sqrt(mag);
+            for (int j = 0; j < d; ++j) v1[j] = v2[j] / mag;
+            ++loops;
+        }
+        vals[i] = dp;
+        std::copy(v1.begin(), v1.end(), tmp.begin() + (size_t)i * d);
+    }
+    std::vector<int> order(d);
+    std::iota(order.begin(), order.end(), 0);
+    for (int pass = 0; pass < d; ++pass)
+        for (int j = 0; j + 1 < d; ++j)
+            if (vals[j + 1] < vals[j]) {
+                std::swap(vals[j], vals[j + 1]);
+                std::swap(order[j], order[j + 1]);
+            }
+    vecs.resize((size_t)d * d);
+    for (int i = 0; i < d; ++i)
+        std::copy(tmp.begin() + (size_t)order[i] * d, tmp.begin() + (size_t)(order[i] + 1) * d,
+                  vecs.begin() + (size_t)i * d);
+}
+
+// eigen_sparse_direct (matrix_functions.rs:1099-1265): Lanczos on
+// D^1/2 A^-1 D^1/2 with h = 5 n_pairs vectors, the first A^-1 s with
+// s_i = sin(n + i), each new vector orthogonalised against the previous two
+// only; Ritz pairs from the largest Ritz value down (never the smallest),
+// eigenvector D^-1/2 Q y scaled to unit 2-norm, a pair skipped when its
+// vector has |cos| >= 0.9 with the previously accepted one; eigenvalue
+// 1 / Ritz value.
+int lanczos_direct(const std::function<void(const double*, double*)>& solve, const std::vector<double>& D,
+                   int n_pairs, double* e_vals, double* e_vecs) {
+    const int n = (int)D.size();
+    const int h = 5 * n_pairs;
+    if (h < 2 || h > n) return -2;
+    std::vector<double> Q((size_t)h * n), t1(n), t2(n), T((size_t)h * (h - 1), 0.0), sq(n);
+    for (int i = 0; i < n; ++i) sq[i] = std::sqrt(D[i]);
+    for (int i = 0; i < n; ++i) t2[i] = std::sin((double)(n + i));
+    solve(t2.data(), Q.data());
+    double mag = 0.0;
+    for (int i = 0; i < n; ++i) mag += Q[i] * Q[i];
+    mag = 1.0 / std::sqrt(mag);
+    for (int i = 0; i < n; ++i) Q[i] *= mag;
+    for (int j = 1; j < h; ++j) {
+        const double* qp = &Q[(size_t)(j - 1) * n];
+        for (int i = 0; i < n; ++i) t1[i] = sq[i] * qp[i];
+        solve(t1.data(), t2.data());
+        for (int i = 0; i < n; ++i) t1[i] = t2[i] * sq[i];
+        for (int k = (j == 1 ? 0 : j - 2); k < j; ++k) {
+            const double* qk = &Q[(size_t)k * n];
+            double dp = 0.0;
+            for (int i = 0; i < n; ++i) dp += t1[i] * qk[i];
+            for (int i = 0; i < n; ++i) t1[i] -= dp * qk[i];
+            T[(size_t)(h - 1) * k + (j - 1)] = dp;
+        }
+        mag = 0.0;
+        for (int i = 0; i < n; ++i) mag += t1[i] * t1[i];
+        mag = std::sqrt(mag);
+        T[(size_t)(h - 1) * j + (j - 1)] = mag;
+        double* qj = &Q[(size_t)j * n];
+        for (int i = 0; i < n; ++i) qj[i] = t1[i] / mag;
+    }
+    const int d = h - 1;
+    std::vector<double> Td(T.begin(), T.begin() + (size_t)d * d), th, S;
+    sym_eigen_tri(Td, d, th, S);
+    int acc = 0;
+    for (int k = d - 1; acc < n_pairs && k > 0; --k) {
+        std::fill(t1.begin(), t1.end(), 0.0);
+        for (int c = 0; c < d; ++c) {
+            const double y = S[(size_t)k * d + c];
+            const double* qc = &Q[(size_t)c * n];
+            for (int i = 0; i < n; ++i) t1[i] += qc[i] * y;
+        }
+        mag = 0.0;
+        for (int i = 0; i < n; ++i) {
+            t2[i] = t1[i] / sq[i];
+            mag += t2[i] * t2[i];
+        }
+        mag = 1.0 / std::sqrt(mag);
+        for (int i = 0; i < n; ++i) t2[i] *= mag;
+        if (acc > 0) {
+            double c = 0.0;
+            for (int i = 0; i < n; ++i) c += e_vecs[(size_t)(acc - 1) * n + i] * t2[i];
+            if (std::fabs(c) >= 0.9) continue;
+        }
+        std::copy(t2.begin(), t2.end(), e_vecs + (size_t)acc * n);
+        e_vals[acc] = 1.0 / th[k];
+        ++acc;
+    }
+    return acc;
+}
+
+}  // namespace
+
 // ---------------------------------------------------------------------------
 // C API
 // ---------------------------------------------------------------------------
@@ -1047,9 +1187,12 @@ int orc_set_constraints(orc_model* m, int32_t n_rows, const int32_t* row_ptr, co
 int orc_assemble(orc_model* m, int32_t dynamic, double dt, double beta, double gamma) {
     build_pattern(m, m->K);
     m->dynamic = dynamic != 0;
+    m->cM = 0.0;
     if (m->dynamic) {
         m->M = m->K;
-        m->cM = -1.0 / (dt * dt * (beta - gamma));
+        // dynamic == 2: modal analysis, K and M kept apart (model_analysis.rs:783-786
+        // assembles the static matrix; the mass enters only as the diagonal D)
+        if (dynamic != 2) m->cM = -1.0 / (dt * dt * (beta - gamma));
     }
     const int nn = m->ti.nn, tot = 3 * nn;
     std::vector<double> ke(tot * tot), me(tot * tot);
@@ -1351,7 +1494,7 @@ int orc_newmark_run(orc_model* m, int32_t n_steps, double dt, double beta, doubl
                     const double* f_shape, const double* amp, int32_t probe_dof,
                     double* probe_hist, int32_t precond, int32_t stop_rule, double tol,
                     int32_t max_it, double* u_final, int32_t* total_iters) {
-    if (!m->assembled || !m->dynamic) return -1;
+    if (!m->assembled || !m->dynamic || m->cM == 0.0) return -1;
     const int n = m->n_dof;
     std::vector<double> u(n, 0.0), v(n, 0.0), a(n, 0.0), up(n, 0.0), vp(n, 0.0), ap(n, 0.0);
     std::vector<double> load(n), du(n), tmp(n), ku(n);
@@ -1398,6 +1541,48 @@ int orc_reorder_nodes(const orc_model* m, int32_t block_dim, int32_t* order_out)
     const auto o = reorder_nodes(m, block_dim > 0 ? block_dim : default_block_dim(m->n_nodes));
     std::copy(o.begin(), o.end(), order_out);
     return 0;
+}
+
+
+// Frequency job (model_analysis.rs:711-880, eigen_solve):
+//   D = row sums of the consistent mass (get_rum with unit acceleration,
+//   :748-766), entries below 1e-6 mean|D| raised to it (:768-779);
+//   A = K - shift D with the penalty terms (:783-789), factored directly
+//   (:790-795); eigen_sparse_direct; eigenvalue += shift (:803-805);
+//   frequency sqrt(lambda) / (2 pi), -1 for a negative eigenvalue (:874-879).
+// Needs orc_assemble(m, 2, ...).  Returns the number of pairs found, or < 0.
+int orc_eigen_solve(orc_model* m, int32_t n_modes, double shift, double* eig, double* freq, double* modes,
+                    double* diag_mass) {
+    if (!m->assembled || !m->dynamic || m->cM != 0.0) return -1;
+    const int n = m->n_dof;
+    std::vector<double> D(n, 0.0), ones(n, 1.0);
+    m->M.matvec(ones.data(), D.data());
+    double avg = 0.0;
+    for (int i = 0; i < n; ++i) avg += std::fabs(D[i]);
+    avg /= (double)n;
+    const double dmin = 1e-6 * avg;
+    for (int i = 0; i < n; ++i)
+        if (D[i] < dmin) D[i] = dmin;
+    if (diag_mass) std::copy(D.begin(), D.end(), diag_mass);
+    std::vector<double> dsave(n);
+    for (int i = 0; i < n; ++i) {
+        const int64_t k = m->K.find(i, i);
+        dsave[i] = m->K.val[k];
+        m->K.val[k] += -shift * D[i];
+    }
+    Precond pc;
+    pc.setup(m, ORC_PC_DIRECT, 0);
+    for (int i = 0; i < n; ++i) m->K.val[m->K.find(i, i)] = dsave[i];
+    std::vector<double> vecs((size_t)n_modes * n, 0.0);
+    auto solve = [&](const double* b, double* x) { pc.apply(b, x); };
+    const int found = lanczos_direct(solve, D, n_modes, eig, vecs.data());
+    if (found < 0) return found;
+    for (int k = 0; k < found; ++k) {
+        eig[k] += shift;
+        if (freq) freq[k] = eig[k] >= 0.0 ? 0.159154943091895335 * std::sqrt(eig[k]) : -1.0;
+    }
+    if (modes) std::copy(vecs.begin(), vecs.begin() + (size_t)found * n, modes);
+    return found;
 }
 
 }  // extern "C"

@@ -58,6 +58,7 @@ int orc_set_constraints(orc_model* m, int32_t n_rows, const int32_t* row_ptr,
 
 /* Assemble K (and M when dynamic != 0) in natural numbering, element order.
  * Sets the penalty scale sf = 1e5 * max|K_ij|. */
+/* dynamic: 0 static, 1 Newmark operator K + cM M (M kept), 2 modal (K and M kept apart). */
 int orc_assemble(orc_model* m, int32_t dynamic, double dt, double beta, double gamma);
 int64_t orc_nnz(const orc_model* m);
 /* which: 0 = K, 1 = M, 2 = operator (K [+ c_M M] + sf C^T C) */
@@ -105,6 +106,12 @@ int orc_newmark_run(orc_model* m, int32_t n_steps, double dt, double beta, doubl
                     int32_t max_it, double* u_final, int32_t* total_iters);
 
 /* Reference node reordering (spatial BFS blocks); perm[new] = old node. */
+/* Frequency job: eigen pairs of (K + penalty - shift D) x = (lambda - shift) D x
+ * with D the row-sum diagonal mass, by the reference's shift-invert Lanczos.
+ * Needs orc_assemble(m, 2, ...).  Returns the number of pairs found. */
+int orc_eigen_solve(orc_model* m, int32_t n_modes, double shift, double* eig, double* freq, double* modes,
+                    double* diag_mass);
+
 int orc_reorder_nodes(const orc_model* m, int32_t block_dim, int32_t* order_out);
 
 #ifdef __cplusplus

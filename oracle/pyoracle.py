@@ -63,6 +63,7 @@ def load():
             "orc_newmark_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double, P_d, P_d,
                                           C.c_int32, P_d, C.c_int32, C.c_int32, C.c_double, C.c_int32, P_d, P_i]),
             "orc_reorder_nodes": (C.c_int, [C.c_void_p, C.c_int32, P_i]),
+            "orc_eigen_solve": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, P_d, P_d, P_d, P_d]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -95,7 +96,7 @@ def constraint_rows(problem, dpn=3):
 
 
 class Oracle:
-    def __init__(self, problem, dynamic=False, dt=0.0, beta=0.25, gamma=0.5):
+    def __init__(self, problem, dynamic=False, dt=0.0, beta=0.25, gamma=0.5, modal=False):
         self.lib = load()
         self.p = problem
         m = problem.mesh
@@ -120,7 +121,7 @@ class Oracle:
             rc = self.lib.orc_set_constraints(self.m, len(rhs), _p(ptr, C.c_int32), _p(dof, C.c_int32), _p(coef),
                                               _p(rhs))
             assert rc == 0
-        self.lib.orc_assemble(self.m, int(dynamic), dt, beta, gamma)
+        self.lib.orc_assemble(self.m, 2 if modal else int(dynamic), dt, beta, gamma)
         self.sf = self.lib.orc_penalty_scale(self.m)
 
     def __del__(self):
@@ -210,6 +211,18 @@ class Oracle:
         rc = self.lib.orc_newmark_run(self.m, n_steps, dt, beta, gamma, _p(f_shape), _p(amp), probe_dof, _p(hist),
                                       precond, stop, tol, max_it, _p(u), C.byref(its))
         return hist, u, rc, its.value
+
+    def eigen(self, n_modes, shift=0.0):
+        """Frequency job (construct with modal=True): eigenvalues, frequencies
+        [Hz], unit-norm mode shapes [n_found, n_dof] and the diagonal mass."""
+        ev = np.zeros(n_modes)
+        fr = np.zeros(n_modes)
+        vecs = np.zeros((n_modes, self.n_dof))
+        dm = np.zeros(self.n_dof)
+        k = self.lib.orc_eigen_solve(self.m, n_modes, shift, _p(ev), _p(fr), _p(vecs), _p(dm))
+        if k < 0:
+            raise RuntimeError(f"orc_eigen_solve failed ({k})")
+        return ev[:k], fr[:k], vecs[:k], dm
 
     def reorder(self, block_dim=0):
         out = np.zeros(self.n_dof // 3, np.int32)

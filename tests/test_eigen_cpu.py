@@ -1,0 +1,120 @@
+"""Modal analysis on the CPU: the library's dense symmetric eigensolver (host
+code of the Lanczos projection) against numpy, and the oracle's restatement of
+the reference's frequency job (model_analysis.rs:711-880,
+matrix_functions.rs:940-1265) against a dense generalised eigensolve and the
+Euler-Bernoulli cantilever frequency.
+
+Tolerances (written here, per quantity):
+  * dense symmetric eigenvalues: 1e-12 * ||A||_2 absolute; residual
+    ||A v - lambda v|| <= 1e-11 ||A||_2; orthonormality 1e-12;
+  * oracle eigenvalues vs the dense inverse operator D^1/2 (K + penalty)^-1
+    D^1/2: 1e-5 relative, mode shapes 1 - |cos| <= 1e-5 (the reference's Ritz
+    values come from a deflated power iteration that stops at
+    |v.Tv| >= (1 - 1e-8) |Tv|, matrix_functions.rs:989);
+  * reference quirk kept by the restatement: its Lanczos orthogonalises each
+    vector against the previous two only (matrix_functions.rs:1156-1176), so a
+    spurious Ritz pair can be reported in place of a true one (the tet4 case
+    shows one; which pair depends on rounding); oracle pairs are matched to
+    the dense spectrum by value;
+  * brickIM cantilever first bending frequency vs Euler-Bernoulli
+    (1.875104^2 / (2 pi L^2) sqrt(EI / rho A)): 1 %.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from asend3d_gb300 import _lib
+from eigen_cases import SMALL_MODELS, cantilever, dense_reference, genuine_pairs
+
+
+def dense_eig(A):
+    lib = _lib.load()
+    m = A.shape[0]
+    a = np.ascontiguousarray(A, np.float64)
+    vals = np.zeros(m)
+    vecs = np.zeros((m, m))
+    P = C.POINTER(C.c_double)
+    rc = lib.asend_dense_sym_eigen(m, a.ctypes.data_as(P), vals.ctypes.data_as(P), vecs.ctypes.data_as(P))
+    assert rc == 0
+    return vals, vecs
+
+
+@pytest.mark.parametrize("m", [1, 2, 3, 7, 40, 121])
+def test_dense_sym_eigen_random(m):
+    rng = np.random.default_rng(m)
+    X = rng.standard_normal((m, m))
+    A = X + X.T
+    vals, vecs = dense_eig(A)
+    ref = np.linalg.eigvalsh(A)
+    nrm = max(np.abs(ref).max(), 1e-300)
+    assert np.abs(vals - ref).max() <= 1e-12 * nrm * max(1, m / 10)
+    assert np.abs(A @ vecs.T - vecs.T * vals).max() <= 1e-11 * nrm * max(1, m / 10)
+    assert np.abs(vecs @ vecs.T - np.eye(m)).max() <= 1e-12 * max(1, m / 10)
+
+
+def test_dense_sym_eigen_structured():
+    # tridiagonal (the b = 1 Lanczos matrix), banded, repeated and zero spectra
+    rng = np.random.default_rng(5)
+    m = 60
+    T = np.diag(rng.uniform(1, 2, m)) + np.diag(rng.uniform(0.1, 1, m - 1), 1)
+    T = T + np.triu(T, 1).T
+    B = np.zeros((m, m))
+    for k in range(3):
+        d = rng.standard_normal(m - k)
+        B += np.diag(d, k) + (np.diag(d, -k) if k else 0)
+    Q, _ = np.linalg.qr(rng.standard_normal((m, m)))
+    R = Q @ np.diag(np.repeat([1.0, 2.0, 2.0, 5.0, 5.0, 5.0], 10)) @ Q.T
+    R = 0.5 * (R + R.T)
+    for A in (T, B, R, np.zeros((m, m)), np.eye(m)):
+        vals, vecs = dense_eig(A)
+        ref = np.linalg.eigvalsh(A)
+        nrm = max(np.abs(ref).max(), 1.0)
+        assert np.abs(vals - ref).max() <= 1e-12 * nrm * 6
+        assert np.abs(A @ vecs.T - vecs.T * vals).max() <= 1e-11 * nrm * 6
+        assert np.abs(vecs @ vecs.T - np.eye(m)).max() <= 1e-12 * 6
+
+
+@pytest.mark.parametrize("kind", list(SMALL_MODELS))
+def test_oracle_eigen_matches_dense(oracle_lib, kind):
+    p = SMALL_MODELS[kind]()
+    o = oracle_lib.Oracle(p, modal=True)
+    ev, fr, vec, D = o.eigen(4)
+    ref, K, _, X = dense_reference(o, 8)
+    assert len(ev) == 4
+    pairs = genuine_pairs(ev, ref)
+    # hex8 / brickIM / shell4: all four pairs are the lowest four; tet4: the
+    # reference's Lanczos reports a spurious pair among its four here
+    if kind == "tet4":
+        assert len(pairs) >= 2 and len(pairs) < 4
+    else:
+        assert [j for _, j in pairs] == [0, 1, 2, 3]
+    np.testing.assert_allclose(fr, np.sqrt(ev) / (2 * np.pi), rtol=1e-14)
+    # mode shapes: unit 2-norm, parallel to the dense eigenvectors
+    for k, j in pairs:
+        assert np.linalg.norm(vec[k]) == pytest.approx(1.0, rel=1e-12)
+        assert abs(vec[k] @ X[:, j]) >= 1 - 1e-5
+    # the diagonal mass is the row sum of the consistent mass
+    rp, col, val = o.csr(1)
+    rows = np.add.reduceat(val, rp[:-1])
+    np.testing.assert_allclose(D, np.maximum(rows, 1e-6 * np.abs(rows).mean()), rtol=1e-13)
+
+
+def test_oracle_eigen_shift(oracle_lib):
+    p = cantilever(8, 2, 2, 0.8, 0.2, 0.1, 81)
+    o = oracle_lib.Oracle(p, modal=True)
+    ev0, _, _, _ = o.eigen(3)
+    ev1, _, _, _ = o.eigen(3, shift=-0.5 * ev0[0])
+    np.testing.assert_allclose(ev1, ev0, rtol=1e-5)
+
+
+def test_oracle_cantilever_frequency_pin(oracle_lib):
+    """Slender brickIM cantilever, bending about the thin axis."""
+    L, b, h, E, rho = 4.0, 0.2, 0.1, 70e9, 2700.0
+    p = cantilever(40, 2, 1, L, b, h, 81, E=E, nu=0.0, rho=rho)
+    o = oracle_lib.Oracle(p, modal=True)
+    _, fr, _, _ = o.eigen(3)
+    f1 = 1.875104069 ** 2 / (2 * np.pi * L ** 2) * np.sqrt(E * (b * h ** 3 / 12) / (rho * b * h))
+    f1y = 1.875104069 ** 2 / (2 * np.pi * L ** 2) * np.sqrt(E * (h * b ** 3 / 12) / (rho * b * h))
+    assert fr[0] == pytest.approx(f1, rel=0.01)
+    assert fr[1] == pytest.approx(f1y, rel=0.01)
