@@ -27,6 +27,7 @@ from asend3d_gb300.mesh import block_hex8
 from asend3d_gb300.solver import AsendError, GpuSolver, Problem
 
 from eigen_cases import SMALL_MODELS, cantilever, dense_reference, genuine_pairs
+from test_eigen_cpu import shell_beam, shell_beam_pin
 
 pytestmark = pytest.mark.gpu
 
@@ -155,6 +156,20 @@ def test_eigen_large_block_properties(gpu_lib):
     assert fr[1] == pytest.approx(fr[0], rel=1e-7)
     f1 = 1.875104069 ** 2 / (2 * np.pi * L ** 2) * np.sqrt(E * (b ** 4 / 12) / (rho * b * b))
     assert 0.95 * f1 <= fr[0] <= 1.005 * f1
+    g.close()
+
+
+def test_eigen_shell_beam_frequency_pin(gpu_lib, oracle_lib):
+    """The reference's shellBeam known answer (first natural frequency)."""
+    p = shell_beam()
+    o = oracle_lib.Oracle(p, modal=True)
+    ref, _, _, _ = dense_reference(o, 3)
+    g = GpuSolver(p)
+    ev, fr, _, _, rc, st = g.eigen(3, tol=1e-10, rel_tol=1e-10, precond=_lib.PC_BLOCK, max_iter=200000)
+    assert rc == _lib.ASEND_OK, st
+    np.testing.assert_allclose(ev, ref, rtol=1e-7)
+    pin = shell_beam_pin()
+    assert fr[0] == pytest.approx(pin["value"], rel=pin["rtol"])
     g.close()
 
 
