@@ -1,0 +1,572 @@
+"""Drop-in job runner for the reference's `asend_run_job <job.yaml>` on the
+linear-elastic static, Newmark and modal path.
+
+It reads the reference's input files with the reference's own line grammar
+(solverSrc/asend_run_job/src/model_input.rs:34-119, read_input_line: up to
+four heading levels tracked by indentation, values split at spaces, commas
+and brackets, '#' comments), runs the commands on the GPU library, and
+writes the reference's result files (results_io):
+
+  job file        model_input.rs:121-310 (read_job)
+  model file      :312-860 nodes, elements (brick8, brickIM, tet4, shell4),
+                  node / element sets (labels, [a, b(, step)) ranges with b
+                  excluded, as :456-470), sections (solid, shell with one
+                  isotropic layer), materials (density, isotropic E, nu, G)
+  constraints     :872-970 (terms of nodeSet / dof / coef, rhs)
+  loads           :981-1124 (nodalForce, surfaceTraction; activeTime)
+  objective       :1298-1375 (displacement / velocity / acceleration with
+                  powerNorm, objective_meth.rs:329-337 and :592-663)
+  commands        model_meth.rs:20-140: readModelInput, readConstraints,
+                  readLoads, readObjectiveInput, solvePrep, solve (static or
+                  dynamic elastic), zeroSolution, modalAnalysis (frequency),
+                  calcObjective, writeNodeResults, writeModalResults,
+                  writeObjective.
+
+Anything outside that subset (thermal, fluid, nonlinear geometry, design
+variables, other element or load types) raises NotImplementedError naming
+the item, rather than running something else.  Usage:
+
+    python -m asend3d_gb300.job path/to/job.yaml
+"""
+from __future__ import annotations
+
+import sys
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+ELEMENT_TYPES = {"brick8": 8, "brickIM": 81, "tet4": 4, "shell4": 41}
+OTHER_ELEMENT_TYPES = ("wedge6", "tet10", "shell3", "beam2", "frcFld", "mass", "fl4", "fl6", "fl8", "fl10")
+
+
+# ---------------------------------------------------------------------------
+# the reference's line grammar
+# ---------------------------------------------------------------------------
+class LineReader:
+    """read_input_line (model_input.rs:34-119).  feed(line) returns
+    (headings, data, is_key_line); headings holds four levels."""
+
+    def __init__(self):
+        self.headings = ["", "", "", ""]
+        self.space = [0, 0, 0, 0]
+
+    @staticmethod
+    def _tokens(s: str) -> list[str]:
+        for ch in ",[]\t\n":
+            s = s.replace(ch, " ")
+        return [t for t in s.split(" ") if t]
+
+    def feed(self, line: str):
+        i = line.find("#")
+        if i >= 0:
+            line = line[:i]
+        line = line + " "
+        colon = line.find(":")
+        if colon >= 0:
+            lead = len(line) - len(line.lstrip(" -\n\t"))
+            word = line[lead:colon]
+            h, sp = self.headings, self.space
+            if h[0] == "" or sp[0] == lead:
+                h[:] = [word, "", "", ""]
+                sp[:] = [lead, 0, 0, 0]
+            elif h[1] == "" or sp[1] == lead:
+                h[1:] = [word, "", ""]
+                sp[1:] = [lead, 0, 0]
+            elif h[2] == "" or sp[2] == lead:
+                h[2:] = [word, ""]
+                sp[2:] = [lead, 0]
+            else:
+                h[3] = word
+                sp[3] = lead
+            return tuple(h), self._tokens(line[colon + 1:]), True
+        dash = line.find("- ")
+        data = self._tokens(line[dash + 1:]) if dash >= 0 else []
+        return tuple(self.headings), data, False
+
+
+def read_records(path):
+    r = LineReader()
+    with open(path) as fh:
+        for line in fh:
+            yield r.feed(line.rstrip("\n"))
+
+
+def _range(data):
+    """A set entry: one label, or [start, end(, step)) with end excluded."""
+    if len(data) == 1:
+        return [int(data[0])]
+    a, b = int(data[0]), int(data[1])
+    step = int(data[2]) if len(data) == 3 else 1
+    return list(range(a, b, step))
+
+
+# ---------------------------------------------------------------------------
+# input files
+# ---------------------------------------------------------------------------
+def read_job(path) -> list[dict]:
+    cmds: list[dict] = []
+    yes = lambda d: "yes" in d[0]
+    conv = {"fileName": str, "dynamic": yes, "elastic": yes, "thermal": yes, "diffusion": yes, "fluid": yes,
+            "nonlinearGeom": yes, "saveSolnHist": yes, "lumpMass": yes, "userUpdate": yes,
+            "loadRampSteps": int, "solverBlockDim": int, "solverBandwidth": int, "maxIterations": int,
+            "numModes": int, "mode": int, "newmarkBeta": float, "newmarkGamma": float, "simPeriod": float,
+            "convergenceTol": float, "timeStep": float, "targetEigenvalue": float, "maxAmplitude": float,
+            "solverMethod": str, "type": str, "solnField": str, "nodeSet": str, "elementSet": str,
+            "position": str, "solnHistDir": str}
+    lists = {"fields", "properties", "include", "staticLoadTime"}
+    for h, data, _ in read_records(path):
+        key = h[1]
+        if key == "command" and len(data) == 1:
+            cmds.append({"command": data[0]})
+            continue
+        if not cmds:
+            continue
+        c = cmds[-1]
+        if key in lists and len(data) == 1:
+            c.setdefault(key, []).append(float(data[0]) if key == "staticLoadTime" else data[0])
+        elif key in ("writeModes", "writeGradient") and len(data) == 1:
+            c[key] = data[0] == "yes"
+        elif key == "timeSteps" and data:
+            if len(data) == 1 and data[0] in ("all", "last"):
+                c["timeStepTag"] = data[0]
+            else:
+                c.setdefault("timeSteps", []).extend(_range(data))
+        elif key in conv and len(data) == 1:
+            f = conv[key]
+            c[key] = f(data) if f is yes else f(data[0])
+    return cmds
+
+
+@dataclass
+class ModelInput:
+    node_labels: list = field(default_factory=list)
+    coords: list = field(default_factory=list)
+    elem_type: int | None = None
+    elem_labels: list = field(default_factory=list)
+    conn: list = field(default_factory=list)
+    node_sets: dict = field(default_factory=dict)
+    elem_sets: dict = field(default_factory=dict)
+    sections: list = field(default_factory=list)
+    materials: dict = field(default_factory=dict)
+
+
+def read_model(path) -> ModelInput:
+    m = ModelInput()
+    cur_set = None
+    for h, data, key_line in read_records(path):
+        h0, h1, h2, h3 = h
+        if h0 == "nodes" and len(data) == 4:
+            m.node_labels.append(int(data[0]))
+            m.coords.append([float(v) for v in data[1:]])
+        elif h0 == "elements":
+            if h1 == "type" and len(data) == 1:
+                if data[0] in OTHER_ELEMENT_TYPES:
+                    raise NotImplementedError(f"element type {data[0]} is not on the GPU path")
+                if data[0] not in ELEMENT_TYPES:
+                    raise ValueError(f"unrecognized element type: {data[0]}")
+                t = ELEMENT_TYPES[data[0]]
+                if m.elem_type is not None and m.elem_type != t:
+                    raise NotImplementedError("one element type per model")
+                m.elem_type = t
+            elif h1 == "connectivity" and len(data) > 1:
+                m.elem_labels.append(int(data[0]))
+                m.conn.append([int(v) for v in data[1:]])
+        elif h0 == "sets" and h1 in ("node", "element") and h2 != "":
+            sets = m.node_sets if h1 == "node" else m.elem_sets
+            if key_line:
+                cur_set = sets.setdefault(h2, [])
+            elif data and cur_set is not None:
+                cur_set.extend(_range(data))
+        elif h0 == "sections":
+            if h1 == "type" and len(data) == 1:
+                m.sections.append({"type": data[0], "layers": []})
+            elif not m.sections:
+                continue
+            elif h1 in ("material", "elementSet") and len(data) == 1:
+                m.sections[-1][h1] = data[0]
+            elif h1 == "orientation" and len(data) == 6:
+                m.sections[-1]["orientation"] = [float(v) for v in data]
+            elif h1 == "layup":
+                if h2 == "zOffset" and len(data) == 1:
+                    m.sections[-1]["zOffset"] = float(data[0])
+                elif h2 == "layers" and h3 == "material" and len(data) == 1:
+                    m.sections[-1]["layers"].append({"material": data[0]})
+                elif h2 == "layers" and h3 in ("thickness", "angle") and len(data) == 1:
+                    m.sections[-1]["layers"][-1][h3] = float(data[0])
+            elif h1 in ("beamProps", "potField", "dampField", "thermField") and data:
+                raise NotImplementedError(f"section {h1} is not on the GPU path")
+        elif h0 == "materials" and h1 != "":
+            if h2 == "" and key_line:
+                m.materials[h1] = {}
+            elif h2 == "density" and len(data) == 1:
+                m.materials[h1]["density"] = float(data[0])
+            elif h2 == "elastic" and h3 in ("E", "nu", "G") and data:
+                vals = [float(v) for v in data]
+                m.materials[h1][h3] = vals * 3 if len(vals) == 1 else vals
+            elif h2 == "elastic" and h3 == "stiffness" and data:
+                raise NotImplementedError("anisotropic stiffness matrices are not on the GPU path")
+    return m
+
+
+def read_constraints(path) -> list:
+    out = []
+    for h, data, _ in read_records(path):
+        if h[0] != "constraints":
+            continue
+        if h[1] == "type" and len(data) == 1:
+            if data[0] != "displacement":
+                raise NotImplementedError(f"{data[0]} constraints are not on the GPU path")
+            out.append({"terms": [], "rhs": 0.0})
+        elif not out:
+            continue
+        elif h[1] == "terms":
+            if h[2] == "nodeSet" and len(data) == 1:
+                out[-1]["terms"].append([data[0], 1, 1.0])
+            elif h[2] == "dof" and len(data) == 1:
+                out[-1]["terms"][-1][1] = int(data[0])
+            elif h[2] == "coef" and len(data) == 1:
+                out[-1]["terms"][-1][2] = float(data[0])
+        elif h[1] == "rhs" and len(data) == 1:
+            out[-1]["rhs"] = float(data[0])
+    return out
+
+
+def read_loads(path) -> list:
+    out = []
+    for h, data, _ in read_records(path):
+        if h[0] != "loads":
+            continue
+        if h[1] == "type" and len(data) == 1:
+            if data[0] not in ("nodalForce", "surfaceTraction"):
+                raise NotImplementedError(f"{data[0]} loads are not on the GPU path")
+            out.append({"type": data[0], "load": [0.0] * 6, "activeTime": [0.0, 1e100], "normTolerance": 1.0})
+        elif not out:
+            continue
+        elif h[1] == "load" and data:
+            vals = [float(v) for v in data]
+            out[-1]["load"][:len(vals)] = vals
+        elif h[1] in ("nodeSet", "elementSet") and len(data) == 1:
+            out[-1][h[1]] = data[0]
+        elif h[1] == "normDir" and len(data) == 3:
+            out[-1]["normDir"] = [float(v) for v in data]
+        elif h[1] == "normTolerance" and len(data) == 1:
+            out[-1]["normTolerance"] = float(data[0])
+        elif h[1] == "activeTime" and data:
+            out[-1]["activeTime"] = [float(data[0]), float(data[1]) if len(data) > 1 else 1e100]
+    return out
+
+
+def read_objective(path) -> list:
+    out = []
+    for h, data, _ in read_records(path):
+        if h[0] != "objectiveTerms":
+            continue
+        if h[1] == "category" and len(data) == 1:
+            # defaults of ObjectiveTerm::new (objective.rs:45-49)
+            out.append({"category": data[0], "operator": "", "component": 0, "layer": 0,
+                        "coefficient": 0.0, "exponent": 0.0, "activeTime": [0.0, 1e100], "targets": []})
+        elif not out:
+            continue
+        elif h[1] in ("operator", "elementSet", "nodeSet") and len(data) == 1:
+            out[-1][h[1]] = data[0]
+        elif h[1] in ("component", "layer") and len(data) == 1:
+            out[-1][h[1]] = int(data[0])
+        elif h[1] in ("coefficient", "exponent") and len(data) == 1:
+            out[-1][h[1]] = float(data[0])
+        elif h[1] == "activeTime" and data:
+            out[-1]["activeTime"] = [float(data[0]), float(data[1]) if len(data) > 1 else 1e100]
+        elif h[1] == "targetValue" and data:
+            out[-1]["targets"].extend(float(v) for v in data)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# the runner
+# ---------------------------------------------------------------------------
+class JobRunner:
+    def __init__(self, job_path, device=0):
+        self.job_path = Path(job_path)
+        self.base = self.job_path.parent
+        self.cmds = read_job(job_path)
+        self.device = device
+        self.model = None
+        self.constraints: list = []
+        self.loads: list = []
+        self.objective: list = []
+        self.g = None
+        self.solve_cmd: dict = {}
+        self.state = None          # {"u", "v", "a"} per node [n, dpn]
+        self.modal = None
+        self.obj_values = None
+        self.log: list = []
+
+    def _path(self, name):
+        p = Path(name)
+        return p if p.is_absolute() else (Path.cwd() / p if (Path.cwd() / p).exists() else self.base / p)
+
+    # -- model -> Problem ---------------------------------------------------
+    def _problem(self):
+        from .mesh import BlockMesh
+        from .solver import Problem
+        m = self.model
+        if m.elem_type is None:
+            raise ValueError("the model has no elements")
+        nidx = {lab: i for i, lab in enumerate(m.node_labels)}
+        self.node_index = nidx
+        conn = np.array([[nidx[n] for n in row] for row in m.conn], dtype=np.int32)
+        coords = np.array(m.coords, dtype=np.float64)
+        mesh = BlockMesh(0, 0, 0, 0.0, 0.0, 0.0, coords, conn, elem_type=m.elem_type)
+        eidx = {lab: i for i, lab in enumerate(m.elem_labels)}
+        ne = len(m.elem_labels)
+        E, nu, rho, thk = (np.full(ne, np.nan) for _ in range(4))
+        for sec in m.sections:
+            es = sec.get("elementSet")
+            if es is None or es not in m.elem_sets:
+                raise ValueError(f"section without a valid elementSet: {sec}")
+            els = [eidx[e] for e in m.elem_sets[es]]
+            if sec["type"] == "solid":
+                mat = m.materials[sec["material"]]
+                t = np.nan
+            elif sec["type"] == "shell":
+                if len(sec["layers"]) != 1 or sec.get("zOffset", 0.0) != 0.0:
+                    raise NotImplementedError("shell sections with one centred layer only")
+                lay = sec["layers"][0]
+                mat = m.materials[lay["material"]]
+                t = lay["thickness"]
+            else:
+                raise NotImplementedError(f"{sec['type']} sections are not on the GPU path")
+            Ev, nv = mat.get("E", [np.nan] * 3), mat.get("nu", [np.nan] * 3)
+            if len(set(Ev)) != 1 or len(set(nv)) != 1:
+                raise NotImplementedError("orthotropic materials are not on the GPU path")
+            if "G" in mat:
+                G = mat["G"]
+                if len(set(G)) != 1 or abs(G[0] - Ev[0] / (2 * (1 + nv[0]))) > 1e-9 * abs(G[0]):
+                    raise NotImplementedError("G must equal E / (2 (1 + nu)) on the isotropic GPU path")
+            E[els], nu[els], rho[els], thk[els] = Ev[0], nv[0], mat.get("density", 0.0), t
+        if np.isnan(E).any():
+            raise ValueError("elements without a section")
+        p = Problem(mesh, E, nu, rho, thickness=None if np.isnan(thk).all() else thk)
+        for name, labs in m.node_sets.items():
+            p.add_node_set(name, [nidx[v] for v in labs])
+        if "all" not in m.node_sets:
+            p.add_node_set("all", np.arange(len(m.node_labels)))
+        for name, labs in m.elem_sets.items():
+            p.add_elem_set(name, [eidx[v] for v in labs])
+        if "all" not in m.elem_sets:
+            p.add_elem_set("all", np.arange(ne))
+        for c in self.constraints:
+            p.constraints.append(([(s, d, cf) for s, d, cf in c["terms"]], c["rhs"]))
+        p.objective = ("compliance",)
+        return p
+
+    def _static_loads(self, p, time):
+        for ld in self.loads:
+            if not (ld["activeTime"][0] <= time <= ld["activeTime"][1]):
+                continue
+            if ld["type"] == "nodalForce":
+                p.add_nodal_force(ld["nodeSet"], ld["load"])
+            else:
+                p.add_surface_traction(ld["elementSet"], tuple(ld["normDir"]), tuple(ld["load"][:3]),
+                                       norm_tol=ld["normTolerance"])
+
+    def _solver(self, time=0.0):
+        from .solver import GpuSolver
+        if self.g is not None:
+            self.g.close()
+        self.problem = self._problem()
+        self._static_loads(self.problem, time)
+        self.g = GpuSolver(self.problem, device=self.device)
+        return self.g
+
+    def _opts(self, cmd):
+        from . import _lib
+        method = cmd.get("solverMethod", "iterative")
+        kw = dict(method=_lib.METHOD_FP64, precond=_lib.PC_JACOBI, rel_tol=cmd.get("convergenceTol", 1e-12))
+        if method == "direct":
+            kw["rel_tol"] = 1e-12  # a direct solve, replaced by PCG to the FP64 floor
+        if cmd.get("maxIterations"):
+            kw["max_iter"] = cmd["maxIterations"]
+        if self.model.elem_type in (8, 81) and self.problem.mesh.nx > 0:
+            kw["precond"] = _lib.PC_MG
+        return kw
+
+    # -- commands ------------------------------------------------------------
+    def run(self):
+        for c in self.cmds:
+            name = c["command"]
+            fn = getattr(self, "cmd_" + name, None)
+            if fn is None:
+                raise NotImplementedError(f"job command {name} is not on the GPU path")
+            fn(c)
+            self.log.append(name)
+        if self.g is not None:
+            self.g.close()
+        return self
+
+    def cmd_readModelInput(self, c):
+        self.model = read_model(self._path(c["fileName"]))
+
+    def cmd_readConstraints(self, c):
+        self.constraints.extend(read_constraints(self._path(c["fileName"])))
+
+    def cmd_readLoads(self, c):
+        self.loads.extend(read_loads(self._path(c["fileName"])))
+
+    def cmd_readObjectiveInput(self, c):
+        self.objective.extend(read_objective(self._path(c["fileName"])))
+
+    def cmd_readDesignVarInput(self, c):
+        raise NotImplementedError("design variables through job files are not on the GPU path yet; "
+                                  "use asend_add_modulus_design_var + asend_adjoint_gradient")
+
+    def cmd_solvePrep(self, c):
+        self.solve_cmd.update({k: v for k, v in c.items() if k != "command"})
+
+    def cmd_zeroSolution(self, c):
+        self.state = None
+
+    def cmd_solve(self, c):
+        from . import _lib
+        cmd = dict(self.solve_cmd)
+        cmd.update({k: v for k, v in c.items() if k != "command"})
+        self.solve_cmd = cmd
+        for k in ("thermal", "diffusion", "fluid", "nonlinearGeom"):
+            if cmd.get(k):
+                raise NotImplementedError(f"{k} analysis is not on the GPU path")
+        g = self._solver()
+        dpn = self.problem.mesh.dpn
+        n = self.problem.mesh.n_nodes
+        if not cmd.get("dynamic"):
+            if len(cmd.get("staticLoadTime", [0.0])) > 1:
+                raise NotImplementedError("several static load times are not on the GPU path")
+            g.assemble(precision=64)
+            u, rc, st = g.static_solve(**self._opts(cmd))
+            if rc not in (_lib.ASEND_OK, _lib.ASEND_MAX_ITER):
+                raise RuntimeError(f"static solve failed: {st}")
+            self.state = {"u": u[0].reshape(n, dpn), "v": np.zeros((n, dpn)), "a": np.zeros((n, dpn)),
+                          "time": cmd.get("staticLoadTime", [0.0])[0]}
+        else:
+            dt = cmd["timeStep"]
+            beta, gamma = cmd.get("newmarkBeta", 0.25), cmd.get("newmarkGamma", 0.5)
+            n_steps = int(round(cmd["simPeriod"] / dt))
+            for ld in self.loads:
+                if ld["activeTime"] != [0.0, 1e100]:
+                    raise NotImplementedError("time-windowed loads in dynamic jobs are not on the GPU path")
+            g.assemble(precision=64, dynamic=True, dt=dt, beta=beta, gamma=gamma)
+            kw = self._opts(cmd)
+            kw["precond"] = _lib.PC_JACOBI if kw["precond"] == _lib.PC_MG else kw["precond"]
+            hist, u, rc, st = g.newmark(np.ones(n_steps), **kw)
+            if rc not in (_lib.ASEND_OK, _lib.ASEND_MAX_ITER):
+                raise RuntimeError(f"Newmark run failed: {st}")
+            self.state = {"u": u.reshape(n, dpn), "v": None, "a": None, "time": n_steps * dt}
+
+    def cmd_modalAnalysis(self, c):
+        from . import _lib
+        if c.get("type", "frequency") != "frequency":
+            raise NotImplementedError("buckling analysis is not on the GPU path")
+        g = self.g or self._solver()
+        kw = self._opts(c)
+        kw["rel_tol"] = 1e-10
+        kw.setdefault("max_iter", 100000)
+        ev, fr, modes, _, rc, st = g.eigen(c.get("numModes", 10), shift=c.get("targetEigenvalue", 0.0), **kw)
+        if rc != _lib.ASEND_OK:
+            raise RuntimeError(f"eigen solve did not converge: {st}")
+        dpn = self.problem.mesh.dpn
+        self.modal = {"eig": ev, "freq": fr, "modes": modes.reshape(len(ev), -1, dpn)}
+
+    def cmd_calcObjective(self, c):
+        if self.state is None:
+            raise RuntimeError("calcObjective before a solve")
+        if self.solve_cmd.get("dynamic"):
+            raise NotImplementedError("time-integrated objectives of dynamic runs are not on the GPU path")
+        vals = []
+        fields = {"displacement": "u", "velocity": "v", "acceleration": "a"}
+        for t in self.objective:
+            if t["category"] not in fields or t["operator"] != "powerNorm":
+                raise NotImplementedError(f"objective {t['category']}/{t['operator']} is not on the GPU path")
+            arr = self.state[fields[t["category"]]]
+            if arr is None:
+                raise NotImplementedError(f"{t['category']} of a dynamic run is not kept")
+            if not (t["activeTime"][0] <= self.state["time"] <= t["activeTime"][1]):
+                vals.append(0.0)
+                continue
+            if t["component"] < 1:
+                raise ValueError("objective term without a component")
+            idx = [self.node_index[v] for v in self.model.node_sets[t["nodeSet"]]]
+            q = arr[idx, t["component"] - 1]
+            tg = np.zeros(len(q))
+            if t["targets"]:
+                tg[:] = t["targets"][0] if len(t["targets"]) == 1 else t["targets"]
+            # objective_meth.rs:329-337: coef * (sum (q - tgt)^p)^(1/p)
+            p = t["exponent"]
+            with np.errstate(invalid="ignore"):
+                vals.append(float(t["coefficient"] * np.power(np.sum(np.power(q - tg, p)), 1.0 / p)))
+        self.obj_values = vals
+
+    def cmd_writeNodeResults(self, c):
+        from .results_io import write_node_results
+        if c.get("timeSteps") or c.get("timeStepTag"):
+            raise NotImplementedError("time-step histories are not written by the GPU path")
+        if self.state is None:
+            raise RuntimeError("writeNodeResults before a solve")
+        fields = {}
+        for f in c.get("fields", ["displacement"]):
+            if f == "displacement":
+                fields[f] = self.state["u"]
+            elif f == "reactionForce":
+                fields[f] = self._reaction()
+            elif f in ("velocity", "acceleration") and self.state[f[0]] is not None:
+                fields[f] = self.state[f[0]]
+            else:
+                raise NotImplementedError(f"node field {f} is not written by the GPU path")
+        labels = self.model.node_sets.get(c.get("nodeSet", "all"), self.model.node_labels)
+        write_node_results(self._out(c["fileName"]), labels, fields, time=-1.0,
+                           rows=[self.node_index[v] for v in labels])
+
+    def _reaction(self):
+        """R(u) = K u (element internal forces, model_output.rs:207-216 with
+        build_elastic_soln_load, model_analysis.rs:179-201): the operator
+        product minus its penalty part."""
+        from . import _lib
+        if self.g is None or self.state is None:
+            raise RuntimeError("reaction forces before a solve")
+        if self.solve_cmd.get("dynamic"):
+            raise NotImplementedError("reaction forces of a dynamic run are not written by the GPU path")
+        u = self.state["u"].ravel()
+        rp, col, val = self.g.csr(2)
+        r = np.add.reduceat(val * u[col], rp[:-1])
+        return r.reshape(self.state["u"].shape)
+
+    def _out(self, name):
+        p = Path(name)
+        return p if p.is_absolute() else Path.cwd() / p
+
+    def cmd_writeModalResults(self, c):
+        from .results_io import write_modal_results
+        if self.modal is None:
+            raise RuntimeError("writeModalResults before modalAnalysis")
+        write_modal_results(str(self._out(c["fileName"])), self.modal["eig"], self.modal["freq"],
+                            modes=self.modal["modes"] if c.get("writeModes") else None,
+                            labels=self.model.node_labels)
+
+    def cmd_writeObjective(self, c):
+        from .results_io import write_objective
+        if self.obj_values is None:
+            raise RuntimeError("writeObjective before calcObjective")
+        if c.get("writeGradient"):
+            raise NotImplementedError("objective gradients through job files are not on the GPU path yet")
+        write_objective(str(self._out(c["fileName"])), self.obj_values, self.objective, c.get("include", ()))
+
+
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    if len(argv) != 1:
+        print("usage: python -m asend3d_gb300.job <job.yaml>", file=sys.stderr)
+        return 2
+    JobRunner(argv[0]).run()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

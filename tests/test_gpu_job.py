@@ -1,0 +1,68 @@
+"""A whole job file through the drop-in runner on the GPU: static solve,
+objective, node results (displacement and reaction force), modal analysis
+and the result files, against the oracle on the same model.
+
+Tolerances: displacements and reactions 1e-8 relative to their largest
+entry (PCG to 1e-11 on a 4-element beam); the objective 1e-8; frequencies
+1e-5 against the oracle's genuine Ritz pairs (its power-iteration
+accuracy); the tip deflection against Euler-Bernoulli FL^3 / 3EI = 4.096e-3
+within 3 % (L/h = 8: shear deformation adds about 1 %)."""
+import numpy as np
+import pytest
+
+from asend3d_gb300 import job as J
+from asend3d_gb300.solver import Problem
+
+from eigen_cases import dense_reference, genuine_pairs
+from test_job import write_cantilever_job
+
+pytestmark = pytest.mark.gpu
+
+
+def read_csv(path):
+    lines = path.read_text().splitlines()
+    return lines[0].split(","), np.array([[float(v) for v in ln.split(",")] for ln in lines[1:]])
+
+
+def test_job_static_and_modal(gpu_lib, oracle_lib, tmp_path):
+    m, xmin, xmax = write_cantilever_job(tmp_path)
+    r = J.JobRunner(tmp_path / "job.yaml").run()
+    assert r.log[-1] == "writeModalResults"
+    # the same model through the oracle
+    m.elem_type = 81
+    p = Problem(m, np.full(m.n_elems, 1e6), np.full(m.n_elems, 0.0), np.full(m.n_elems, 1.0))
+    p.add_node_set("xMin", xmin)
+    p.add_node_set("xMax", xmax)
+    p.fix_displacement("xMin")
+    p.add_nodal_force("xMax", [0.0, 0.0, -2.0 / len(xmax)])
+    o = oracle_lib.Oracle(p)
+    uo, rc, _ = o.solve(o.loads()[0] + o.penalty_rhs(), precond=oracle_lib.PC_DIRECT)
+    uo = uo.reshape(-1, 3)
+    head, rows = read_csv(tmp_path / "nodes.csv")
+    assert head == ["node", "U1", "U2", "U3", "R1", "R2", "R3", "RF1", "RF2", "RF3", "RM1", "RM2", "RM3", "time"]
+    np.testing.assert_array_equal(rows[:, 0], xmax)
+    assert np.abs(rows[:, 1:4] - uo[xmax]).max() <= 1e-8 * np.abs(uo).max()
+    assert np.all(rows[:, 4:7] == 0.0) and np.all(rows[:, -1] == -1.0)
+    rp, col, val = o.csr(0)  # K without the penalty terms
+    ku = np.add.reduceat(val * uo.ravel()[col], rp[:-1]).reshape(-1, 3)
+    assert np.abs(rows[:, 7:10] - ku[xmax]).max() <= 1e-8 * np.abs(ku).max()
+    # the tip carries the applied load as its internal force
+    np.testing.assert_allclose(rows[:, 9].sum(), -2.0, rtol=1e-8)
+    lines = (tmp_path / "obj.csv").read_text().splitlines()
+    assert lines[0] == "objectiveTerm,value,category,coefficient"
+    w = float(lines[1].split(",")[1])
+    assert w == pytest.approx(uo[xmax, 2].mean(), rel=1e-8)
+    assert w == pytest.approx(-4.096e-3, rel=0.03)
+    # modal results against the oracle's frequency job
+    om = oracle_lib.Oracle(p, modal=True)
+    evo, fro, _, _ = om.eigen(3)
+    ref, _, _, _ = dense_reference(om, 6)
+    head, modal = read_csv(tmp_path / "modal.csv")
+    assert head == ["mode", "eigenvalue", "frequency"]
+    np.testing.assert_allclose(modal[:, 1], ref[:3], rtol=1e-8)
+    for k, j in genuine_pairs(evo, ref):
+        if j < 3:
+            assert modal[j, 1] == pytest.approx(evo[k], rel=1e-5)
+    np.testing.assert_allclose(modal[:, 2], np.sqrt(modal[:, 1]) / (2 * np.pi), rtol=1e-12)
+    mode0 = (tmp_path / "modal_mode0.csv").read_text().splitlines()
+    assert mode0[0] == "Node,U1,U2,U3,R1,R2,R3" and len(mode0) == m.n_nodes + 1

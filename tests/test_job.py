@@ -1,0 +1,156 @@
+"""Job-file drop-in: the reference's line grammar (model_input.rs:34-119), its
+job / model / constraint / load / objective readers, the Problem built from
+them, objective evaluation (objective_meth.rs:329-337) and the result files.
+Input files are written here in the layout the reference's Python layer
+produces (PyYAML block style, rows as bracketed strings with the quotes
+removed, asendUtils/model/Model.py:467-480).  The GPU run of a whole job is
+in test_gpu_job.py."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from asend3d_gb300 import job as J
+from asend3d_gb300.mesh import block_hex8
+
+
+def write_cantilever_job(d: Path, nx=4, ny=1, nz=1, L=4.0, etype="brickIM", modal=True):
+    """A cantilever of nx*ny*nz hex elements clamped at x = 0 with a -z tip
+    load of 2 spread over the tip nodes, mean tip deflection objective."""
+    m = block_hex8(nx, ny, nz, L, 1.0, 0.5)
+    lines = ["nodes:"]
+    lines += [f"- [{i}, {float(x)!r}, {float(y)!r}, {float(z)!r}]" for i, (x, y, z) in enumerate(m.coords)]
+    lines += ["elements:", f"- type: {etype}", "  connectivity:"]
+    lines += ["  - [" + ", ".join(str(v) for v in [e, *row]) + "]" for e, row in enumerate(m.conn)]
+    xmin = m.nodes_in_range(xr=(-1e-9, 1e-9))
+    xmax = m.nodes_in_range(xr=(L - 1e-9, L + 1e-9))
+    lines += ["sets:", "  node:", "    xMin:"] + [f"    - {v}" for v in xmin]
+    lines += ["    xMax:"] + [f"    - {v}" for v in xmax]
+    lines += ["  element:", "    all:", f"    - [0, {m.n_elems}]"]
+    lines += ["sections:", "- type: solid", "  material: mat1", "  elementSet: all"]
+    lines += ["materials:", "  mat1:   # isotropic", "    density: 1.0", "    elastic:",
+              "      E: [1000000.0]", "      nu: 0.0", "      G: 500000.0"]
+    (d / "model.yaml").write_text("\n".join(lines) + "\n")
+    cons = ["constraints:"]
+    for dof in (1, 2, 3):
+        cons += ["- type: displacement", "  terms:", "  - nodeSet: xMin", f"    dof: {dof}", "    coef: 1.0",
+                 "  rhs: 0.0"]
+    (d / "constraints.yaml").write_text("\n".join(cons) + "\n")
+    f = float(-2.0 / len(xmax))
+    (d / "loads.yaml").write_text("loads:\n- type: nodalForce\n  nodeSet: xMax\n"
+                                  f"  load: [0.0, 0.0, {f!r}, 0.0, 0.0, 0.0]\n")
+    (d / "objective.yaml").write_text("objectiveTerms:\n- category: displacement\n  operator: powerNorm\n"
+                                      f"  nodeSet: xMax\n  component: 3\n  coefficient: {float(1.0 / len(xmax))!r}\n"
+                                      "  exponent: 1.0\n")
+    job = ["jobCommands:",
+           "- command: readModelInput", "  fileName: model.yaml",
+           "- command: readConstraints", "  fileName: constraints.yaml",
+           "- command: readLoads", "  fileName: loads.yaml",
+           "- command: readObjectiveInput", "  fileName: objective.yaml",
+           "- command: solve", "  elastic: yes", "  dynamic: no", "  solverMethod: iterative",
+           "  convergenceTol: 1.0e-11", "  maxIterations: 20000",
+           "- command: calcObjective",
+           "- command: writeNodeResults", f"  fileName: {d / 'nodes.csv'}", "  nodeSet: xMax",
+           "  fields:", "  - displacement", "  - reactionForce",
+           "- command: writeObjective", f"  fileName: {d / 'obj.csv'}", "  include:", "  - category",
+           "  - coefficient"]
+    if modal:
+        job += ["- command: modalAnalysis", "  type: frequency", "  numModes: 3",
+                "- command: writeModalResults", f"  fileName: {d / 'modal.csv'}", "  writeModes: yes"]
+    (d / "job.yaml").write_text("\n".join(job) + "\n")
+    return m, xmin, xmax
+
+
+def test_line_grammar():
+    r = J.LineReader()
+    assert r.feed("nodes:") == (("nodes", "", "", ""), [], True)
+    assert r.feed("- [3, 1.5, -2e-3, 0.0]  # comment") == (("nodes", "", "", ""), ["3", "1.5", "-2e-3", "0.0"], False)
+    assert r.feed("sets:")[0] == ("sets", "", "", "")
+    assert r.feed("  node:")[0] == ("sets", "node", "", "")
+    assert r.feed("    tip:")[0] == ("sets", "node", "tip", "")
+    assert r.feed("    - [0, 10, 2]")[1] == ["0", "10", "2"]
+    r.feed("sections:")
+    assert r.feed("- type: shell")[:2] == (("sections", "type", "", ""), ["shell"])
+    assert r.feed("  layup:")[0] == ("sections", "layup", "", "")
+    assert r.feed("    layers:")[0] == ("sections", "layup", "layers", "")
+    assert r.feed("    - material: al")[:2] == (("sections", "layup", "layers", "material"), ["al"])
+    assert r.feed("      thickness: 0.1")[:2] == (("sections", "layup", "layers", "thickness"), ["0.1"])
+    assert r.feed("  elementSet: all")[:2] == (("sections", "elementSet", "", ""), ["all"])
+    assert J._range(["0", "10", "3"]) == [0, 3, 6, 9]
+
+
+def test_readers(tmp_path):
+    m, xmin, xmax = write_cantilever_job(tmp_path)
+    cmds = J.read_job(tmp_path / "job.yaml")
+    assert [c["command"] for c in cmds] == ["readModelInput", "readConstraints", "readLoads", "readObjectiveInput",
+                                            "solve", "calcObjective", "writeNodeResults", "writeObjective",
+                                            "modalAnalysis", "writeModalResults"]
+    assert cmds[4]["elastic"] is True and cmds[4]["dynamic"] is False and cmds[4]["convergenceTol"] == 1e-11
+    assert cmds[4]["maxIterations"] == 20000
+    assert cmds[6]["fields"] == ["displacement", "reactionForce"] and cmds[9]["writeModes"] is True
+    mi = J.read_model(tmp_path / "model.yaml")
+    assert mi.elem_type == 81 and mi.node_labels == list(range(m.n_nodes))
+    np.testing.assert_array_equal(np.array(mi.coords), m.coords)
+    np.testing.assert_array_equal(np.array(mi.conn), m.conn)
+    assert mi.node_sets["xMin"] == list(xmin) and mi.elem_sets["all"] == list(range(m.n_elems))
+    assert mi.materials["mat1"] == {"density": 1.0, "E": [1e6] * 3, "nu": [0.0] * 3, "G": [5e5] * 3}
+    assert mi.sections == [{"type": "solid", "layers": [], "material": "mat1", "elementSet": "all"}]
+    cons = J.read_constraints(tmp_path / "constraints.yaml")
+    assert [c["terms"] for c in cons] == [[["xMin", d, 1.0]] for d in (1, 2, 3)]
+    loads = J.read_loads(tmp_path / "loads.yaml")
+    assert loads[0]["type"] == "nodalForce" and loads[0]["load"][2] == pytest.approx(-2.0 / len(xmax))
+    obj = J.read_objective(tmp_path / "objective.yaml")
+    assert obj[0]["component"] == 3 and obj[0]["exponent"] == 1.0 and obj[0]["nodeSet"] == "xMax"
+
+
+def test_problem_from_job(tmp_path):
+    m, xmin, xmax = write_cantilever_job(tmp_path)
+    r = J.JobRunner(tmp_path / "job.yaml")
+    for c in r.cmds[:4]:
+        getattr(r, "cmd_" + c["command"])(c)
+    p = r._problem()
+    r._static_loads(p, 0.0)
+    assert p.mesh.elem_type == 81
+    np.testing.assert_array_equal(p.mesh.conn, m.conn)
+    assert np.all(p.E == 1e6) and np.all(p.nu == 0.0) and np.all(p.rho == 1.0)
+    np.testing.assert_array_equal(p.node_sets["xMin"], xmin)
+    assert len(p.constraints) == 3 and p.loads[0][0][0] == "nodalForce"
+
+
+def test_objective_and_writers(tmp_path):
+    m, xmin, xmax = write_cantilever_job(tmp_path)
+    r = J.JobRunner(tmp_path / "job.yaml")
+    for c in r.cmds[:4]:
+        getattr(r, "cmd_" + c["command"])(c)
+    r.problem = r._problem()
+    n = m.n_nodes
+    u = np.zeros((n, 3))
+    u[xmax, 2] = -8.0
+    r.state = {"u": u, "v": np.zeros((n, 3)), "a": np.zeros((n, 3)), "time": 0.0}
+    r.cmd_calcObjective({})
+    assert r.obj_values == [pytest.approx(-8.0)]
+    r.objective[0]["exponent"] = 2.0
+    r.objective[0]["targets"] = [-7.0]
+    r.cmd_calcObjective({})
+    # coef * (sum (q - t)^2)^(1/2) over the tip nodes
+    assert r.obj_values[0] == pytest.approx(np.sqrt(len(xmax)) / len(xmax))
+    r.cmd_writeObjective({"fileName": str(tmp_path / "o.csv"), "include": ["category"]})
+    assert (tmp_path / "o.csv").read_text().splitlines()[1].startswith("0,")
+    with pytest.raises(NotImplementedError):
+        r.cmd_writeObjective({"fileName": str(tmp_path / "o.csv"), "writeGradient": True})
+    with pytest.raises(NotImplementedError):
+        r.cmd_readDesignVarInput({"fileName": "x"})
+
+
+def test_unsupported_inputs(tmp_path):
+    (tmp_path / "m.yaml").write_text("elements:\n- type: beam2\n")
+    with pytest.raises(NotImplementedError, match="beam2"):
+        J.read_model(tmp_path / "m.yaml")
+    (tmp_path / "l.yaml").write_text("loads:\n- type: gravitational\n")
+    with pytest.raises(NotImplementedError, match="gravitational"):
+        J.read_loads(tmp_path / "l.yaml")
+    (tmp_path / "j.yaml").write_text("jobCommands:\n- command: solve\n  thermal: yes\n")
+    r = J.JobRunner(tmp_path / "j.yaml")
+    r.model = J.ModelInput()
+    with pytest.raises(NotImplementedError, match="thermal"):
+        r.cmd_solve(r.cmds[0])
