@@ -23,6 +23,7 @@ METHOD_FP64, METHOD_MIXED = 0, 1
 PC_JACOBI, PC_BLOCK, PC_LEARNED, PC_MG, PC_MG_LEARNED = 0, 1, 2, 3, 4
 OBJ_DISPLACEMENT, OBJ_COMPLIANCE = 0, 1
 LEARN_BLOCK, LEARN_MG = 0, 1
+DV_MODULUS, DV_SHEAR_MODULUS, DV_POISSON_RATIO = 0, 1, 2
 
 
 class SolveOpts(C.Structure):
@@ -97,6 +98,8 @@ SIGNATURES = [
     ("asend_eigen_solve", c_int, [C.c_void_p, C.POINTER(EigenOpts), P_dbl, P_dbl, P_dbl, P_dbl,
                                   C.POINTER(EigenStats)]),
     ("asend_dense_sym_eigen", c_int, [c_int, P_dbl, P_dbl, P_dbl]),
+    ("asend_adjoint_strain_pairs", c_int, [C.c_void_p, P_dbl]),
+    ("asend_material_dv_gradient", c_int, [C.c_void_p, c_int, c_int, c_int, c_int, P_dbl, P_dbl]),
     ("asend_operator_energy_noalloc", c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("asend_learned_n_params", c_int, []),
     ("asend_learned_init", c_int, [C.c_void_p, C.c_uint64]),

@@ -962,7 +962,8 @@ int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double*
             const auto& set = c.node_sets[c.obj_set];
             std::vector<double> dldu(n, 0.0);
             for (int nd : set) dldu[(size_t)nd * c.udpn + c.obj_comp - 1] += c.obj_coef;
-            DArr<double> d_dldu, d_usum;
+            DArr<double> d_dldu;
+            DArr<double>& d_usum = c.d_adj_b;
             d_dldu.upload(dldu, c.stream);
             d_usum.alloc(n);
             d_usum.zero(c.stream);
@@ -991,6 +992,8 @@ int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double*
             ast.ms_adjoint = mc;
         }
         ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
+        c.adj_kind = c.obj_kind;
+        ++c.adj_serial;
         if (dLdE_out)
             ASEND_CUDA(cudaMemcpyAsync(dLdE_out, c.d_gE.p, sizeof(double) * c.n_el, cudaMemcpyDeviceToHost, c.stream));
         ASEND_CUDA(cudaStreamSynchronize(c.stream));
@@ -1068,6 +1071,99 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
             dLdD_out[i] = s;
         }
         return ndv;
+    });
+}
+
+// Strain-pair tensors of the last adjoint gradient, P_e = sum_gp w detJ
+// eps(lambda) eps(u)^T (compliance: sum over load cases of the u_r pairs).
+static void ensure_pairs(Ctx& c) {
+    require(c.adj_kind >= 0, "run asend_adjoint_gradient first");
+    if (c.pairs_serial == c.adj_serial) return;
+    const size_t n = c.n_dof;
+    DArr<double> P;
+    P.alloc((size_t)c.n_el * 36);
+    if (c.adj_kind == ASEND_OBJ_COMPLIANCE) {
+        for (int r = 0; r < c.nrhs; ++r) adjoint_pairs(c, c.d_x.p + r * n, c.d_x.p + r * n, P.p, r > 0);
+    } else {
+        adjoint_pairs(c, c.d_lam.p, c.d_adj_b.p, P.p, false);
+    }
+    c.h_pairs.resize((size_t)c.n_el * 36);
+    ASEND_CUDA(cudaMemcpyAsync(c.h_pairs.data(), P.p, sizeof(double) * c.h_pairs.size(), cudaMemcpyDeviceToHost,
+                               c.stream));
+    ASEND_CUDA(cudaStreamSynchronize(c.stream));
+    c.pairs_serial = c.adj_serial;
+}
+
+int asend_adjoint_strain_pairs(asend_ctx* ctx, double* pairs_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        ensure_pairs(c);
+        if (pairs_out) std::copy(c.h_pairs.begin(), c.h_pairs.end(), pairs_out);
+        return ASEND_OK;
+    });
+}
+
+// dL/dD for a material design variable over an element set
+// (model_analysis.rs:1692-1700 with d_relasticd_d :1379-1457): the element
+// stiffness C = S^-1 from the compliance S(E1..3, nu12, nu13, nu23,
+// G12, G13, G23) of get_solid_stiff (element_properties.rs:648-764), here
+// isotropic per element (E_e, nu_e, G = E_e / (2 (1 + nu_e))); the DV adds
+// coef * D to its component, so dC/dD = -coef C (dS/dE_k | dS/dG_k |
+// dS/dnu_k) C and dL/dD = -sum_e sum_ij (dC/dD)_ij P_e[i][j].
+int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t component, int32_t elem_set,
+                               int32_t n_coef, const double* coefs, double* grad_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(category >= ASEND_DV_MODULUS && category <= ASEND_DV_POISSON_RATIO, "unknown DV category");
+        require(component >= 1 && component <= 3, "component must be 1, 2 or 3");
+        require(elem_set >= 0 && elem_set < (int)c.elem_sets.size(), "unknown element set");
+        require(grad_out, "null output");
+        const auto& set = c.elem_sets[elem_set];
+        require(n_coef <= 1 || (size_t)n_coef == set.size(), "coefficient list does not match the element set");
+        require(n_coef == 0 || coefs, "null coefficients");
+        ensure_pairs(c);
+        const int k = component - 1;
+        double g = 0.0;
+        for (size_t q = 0; q < set.size(); ++q) {
+            const int e = set[q];
+            const double E = c.E[e], nu = c.nu[e], G = E / (2.0 * (1.0 + nu));
+            const double la = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), mu = G;
+            double C[36] = {0};
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) C[6 * i + j] = la + (i == j ? 2.0 * mu : 0.0);
+            for (int i = 3; i < 6; ++i) C[7 * i] = mu;
+            double dS[36] = {0};
+            if (category == ASEND_DV_MODULUS) {
+                // S00 = 1/E1, S01 = -nu12/E1, S02 = -nu13/E1, S11 = 1/E2, S12 = -nu23/E2, S22 = 1/E3
+                dS[7 * k] = -1.0 / (E * E);
+                if (k == 0) dS[1] = dS[6] = dS[2] = dS[12] = nu / (E * E);
+                if (k == 1) dS[8] = dS[13] = nu / (E * E);
+            } else if (category == ASEND_DV_SHEAR_MODULUS) {
+                dS[7 * (3 + k)] = -1.0 / (G * G);
+            } else {
+                const int pr[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+                const int a = pr[k][0], b = pr[k][1];
+                dS[6 * a + b] = dS[6 * b + a] = -1.0 / E;
+            }
+            double T[36], dC[36];
+            for (int i = 0; i < 6; ++i)
+                for (int j = 0; j < 6; ++j) {
+                    double s = 0.0;
+                    for (int l = 0; l < 6; ++l) s += dS[6 * i + l] * C[6 * l + j];
+                    T[6 * i + j] = s;
+                }
+            for (int i = 0; i < 6; ++i)
+                for (int j = 0; j < 6; ++j) {
+                    double s = 0.0;
+                    for (int l = 0; l < 6; ++l) s += C[6 * i + l] * T[6 * l + j];
+                    dC[6 * i + j] = -s;
+                }
+            const double* P = &c.h_pairs[(size_t)e * 36];
+            double s = 0.0;
+            for (int i = 0; i < 36; ++i) s += dC[i] * P[i];
+            const double cf = n_coef == 0 ? 1.0 : (n_coef == 1 ? coefs[0] : coefs[q]);
+            g -= cf * s;
+        }
+        *grad_out = g;
+        return ASEND_OK;
     });
 }
 

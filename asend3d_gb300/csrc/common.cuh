@@ -166,6 +166,10 @@ struct Ctx {
 
     // adjoint
     DArr<double> d_lam, d_gE;
+    DArr<double> d_adj_b;          // second field of the last adjoint contraction (displacement objective)
+    int adj_kind = -1;             // objective of the last adjoint gradient (-1: none)
+    int64_t adj_serial = 0, pairs_serial = -1;
+    std::vector<double> h_pairs;   // strain-pair tensors of the last adjoint [n_el][36]
 
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -232,6 +236,7 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
 void device_dot(Ctx& c, size_t n, const double* a, const double* b, double* d_out, double* d_part);
 void device_axpy(Ctx& c, size_t n, double alpha, const double* x, double* y);
 void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g, bool accumulate);
+void adjoint_pairs(Ctx& c, const double* d_a, const double* d_b, double* d_P, bool accumulate);
 int eigen_solve(Ctx& c, const asend_eigen_opts& eo, double* eig_out, double* freq_out, double* modes_out,
                 double* diag_mass_out, asend_eigen_stats* st);
 int sym_eigen_dense(int m, const double* a, double* vals, double* vecs);

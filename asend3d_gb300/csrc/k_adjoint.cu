@@ -23,15 +23,12 @@
 namespace asend {
 namespace {
 
+// Element-relative node data of element e: coordinates and the two
+// displacement fields with node 0's translation removed.
 template <int NN>
-__global__ void __launch_bounds__(128)
-k_adjoint_modulus(int n_el, const int32_t* __restrict__ conn, const double* __restrict__ xyz,
-                  const double* __restrict__ E, const double* __restrict__ nu,
-                  const double* __restrict__ av, const double* __restrict__ bv, double* __restrict__ g,
-                  int accumulate) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n_el) return;
-    double x[NN][3], ua[NN][3], ub[NN][3];
+__device__ __forceinline__ void gather_element(int e, const int32_t* __restrict__ conn, const double* __restrict__ xyz,
+                                               const double* __restrict__ av, const double* __restrict__ bv,
+                                               double (&x)[NN][3], double (&ua)[NN][3], double (&ub)[NN][3]) {
     int nd[NN];
 #pragma unroll
     for (int a = 0; a < NN; ++a) nd[a] = conn[(size_t)e * NN + a];
@@ -50,88 +47,138 @@ k_adjoint_modulus(int n_el, const int32_t* __restrict__ conn, const double* __re
             ua[a][j] -= ua[0][j];
             ub[a][j] -= ub[0][j];
         }
+}
+
+// Voigt strains (11,22,33,12,13,23, engineering shear) of both fields at
+// Gauss point gp, and its weight w detJ.
+template <int NN>
+__device__ __forceinline__ double point_strains(int gp, const double (&x)[NN][3], const double (&ua)[NN][3],
+                                                const double (&ub)[NN][3], double (&ea)[6], double (&eb)[6]) {
+    const double gq = 0.5773502691896257;
+    double dn[NN][3];
+    double wt;
+    if constexpr (NN == 8) {
+        const double s0 = (gp & 1) ? gq : -gq, s1 = (gp & 2) ? gq : -gq, s2 = (gp & 4) ? gq : -gq;
+        const double sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                 {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            const double f0 = 1 + sg[a][0] * s0, f1 = 1 + sg[a][1] * s1, f2 = 1 + sg[a][2] * s2;
+            dn[a][0] = 0.125 * sg[a][0] * f1 * f2;
+            dn[a][1] = 0.125 * sg[a][1] * f0 * f2;
+            dn[a][2] = 0.125 * sg[a][2] * f0 * f1;
+        }
+        wt = 1.0;
+    } else {
+        const double d[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) dn[a][j] = d[a][j];
+        wt = 1.0 / 6.0;
+    }
+    double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int a = 0; a < NN; ++a)
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) J[i][j] += x[a][i] * dn[a][j];
+    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    const double id = 1.0 / det;
+    double Ji[3][3];
+    Ji[0][0] = c00 * id;
+    Ji[1][0] = c01 * id;
+    Ji[2][0] = c02 * id;
+    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+    // displacement gradients H[i][j] = du_i/dx_j
+    double Ha[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Hb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int a = 1; a < NN; ++a) {
+        double gx[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) gx[j] = dn[a][0] * Ji[0][j] + dn[a][1] * Ji[1][j] + dn[a][2] * Ji[2][j];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                Ha[i][j] += ua[a][i] * gx[j];
+                Hb[i][j] += ub[a][i] * gx[j];
+            }
+    }
+    ea[0] = Ha[0][0]; ea[1] = Ha[1][1]; ea[2] = Ha[2][2];
+    ea[3] = Ha[0][1] + Ha[1][0]; ea[4] = Ha[0][2] + Ha[2][0]; ea[5] = Ha[1][2] + Ha[2][1];
+    eb[0] = Hb[0][0]; eb[1] = Hb[1][1]; eb[2] = Hb[2][2];
+    eb[3] = Hb[0][1] + Hb[1][0]; eb[4] = Hb[0][2] + Hb[2][0]; eb[5] = Hb[1][2] + Hb[2][1];
+    return det * wt;
+}
+
+template <int NN>
+__global__ void __launch_bounds__(128)
+k_adjoint_modulus(int n_el, const int32_t* __restrict__ conn, const double* __restrict__ xyz,
+                  const double* __restrict__ nu, const double* __restrict__ av, const double* __restrict__ bv,
+                  double* __restrict__ g, int accumulate) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_el) return;
+    double x[NN][3], ua[NN][3], ub[NN][3];
+    gather_element<NN>(e, conn, xyz, av, bv, x, ua, ub);
     const double ne = nu[e];
     const double lam = ne / ((1.0 + ne) * (1.0 - 2.0 * ne));  // C / E
     const double mu = 1.0 / (2.0 * (1.0 + ne));
-    const double gq = 0.5773502691896257;
     constexpr int NIP = (NN == 8) ? 8 : 1;
     double acc = 0.0;
 #pragma unroll
     for (int gp = 0; gp < NIP; ++gp) {
-        double dn[NN][3];
-        double wt;
-        if constexpr (NN == 8) {
-            const double s0 = (gp & 1) ? gq : -gq, s1 = (gp & 2) ? gq : -gq, s2 = (gp & 4) ? gq : -gq;
-            const double sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
-                                     {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
-#pragma unroll
-            for (int a = 0; a < 8; ++a) {
-                const double f0 = 1 + sg[a][0] * s0, f1 = 1 + sg[a][1] * s1, f2 = 1 + sg[a][2] * s2;
-                dn[a][0] = 0.125 * sg[a][0] * f1 * f2;
-                dn[a][1] = 0.125 * sg[a][1] * f0 * f2;
-                dn[a][2] = 0.125 * sg[a][2] * f0 * f1;
-            }
-            wt = 1.0;
-        } else {
-            const double d[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-#pragma unroll
-            for (int a = 0; a < 4; ++a)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) dn[a][j] = d[a][j];
-            wt = 1.0 / 6.0;
-        }
-        double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-#pragma unroll
-        for (int a = 0; a < NN; ++a)
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) J[i][j] += x[a][i] * dn[a][j];
-        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-        const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-        const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-        const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-        const double id = 1.0 / det;
-        double Ji[3][3];
-        Ji[0][0] = c00 * id;
-        Ji[1][0] = c01 * id;
-        Ji[2][0] = c02 * id;
-        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-        // displacement gradients H[i][j] = du_i/dx_j
-        double Ha[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Hb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-#pragma unroll
-        for (int a = 1; a < NN; ++a) {
-            double gx[3];
-#pragma unroll
-            for (int j = 0; j < 3; ++j) gx[j] = dn[a][0] * Ji[0][j] + dn[a][1] * Ji[1][j] + dn[a][2] * Ji[2][j];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    Ha[i][j] += ua[a][i] * gx[j];
-                    Hb[i][j] += ub[a][i] * gx[j];
-                }
-        }
-        // Voigt strains (11,22,33,12,13,23), engineering shear
-        const double ea[6] = {Ha[0][0], Ha[1][1], Ha[2][2], Ha[0][1] + Ha[1][0], Ha[0][2] + Ha[2][0], Ha[1][2] + Ha[2][1]};
-        const double eb[6] = {Hb[0][0], Hb[1][1], Hb[2][2], Hb[0][1] + Hb[1][0], Hb[0][2] + Hb[2][0], Hb[1][2] + Hb[2][1]};
+        double ea[6], eb[6];
+        const double wd = point_strains<NN>(gp, x, ua, ub, ea, eb);
         const double trb = eb[0] + eb[1] + eb[2];
         double s = 0.0;
 #pragma unroll
         for (int i = 0; i < 3; ++i) s += ea[i] * (lam * trb + 2.0 * mu * eb[i]);
 #pragma unroll
         for (int i = 3; i < 6; ++i) s += ea[i] * (mu * eb[i]);
-        acc += s * det * wt;
+        acc += s * wd;
     }
-    const double v = -acc;  // (1/E) dK/d? folded: C/E used above
+    const double v = -acc;  // -(1/E) eps(a)^T C eps(b), C / E folded into lam, mu
     if (accumulate) g[e] += v;
     else g[e] = v;
-    (void)E;
+}
+
+// Strain-pair tensors P_e[i][j] = sum_gp w detJ eps_i(a) eps_j(b): any
+// material derivative of the element's internal force then contracts as
+// a^T dR_e/dD = sum_ij (dC/dD)_ij P_e[i][j] (C constant over the element).
+template <int NN>
+__global__ void __launch_bounds__(128)
+k_adjoint_pairs(int n_el, const int32_t* __restrict__ conn, const double* __restrict__ xyz,
+                const double* __restrict__ av, const double* __restrict__ bv, double* __restrict__ P, int accumulate) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_el) return;
+    double x[NN][3], ua[NN][3], ub[NN][3];
+    gather_element<NN>(e, conn, xyz, av, bv, x, ua, ub);
+    constexpr int NIP = (NN == 8) ? 8 : 1;
+    double acc[36];
+#pragma unroll
+    for (int k = 0; k < 36; ++k) acc[k] = 0.0;
+#pragma unroll 1
+    for (int gp = 0; gp < NIP; ++gp) {
+        double ea[6], eb[6];
+        const double wd = point_strains<NN>(gp, x, ua, ub, ea, eb);
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+            for (int j = 0; j < 6; ++j) acc[6 * i + j] += ea[i] * eb[j] * wd;
+    }
+    double* out = P + (size_t)e * 36;
+#pragma unroll
+    for (int k = 0; k < 36; ++k) out[k] = accumulate ? out[k] + acc[k] : acc[k];
 }
 
 __global__ void k_dot_partial(size_t n, const double* __restrict__ a, const double* __restrict__ b,
@@ -182,11 +229,23 @@ void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g,
     }
     const int blocks = (c.n_el + 127) / 128;
     if (c.nn == 8)
-        k_adjoint_modulus<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, d_a, d_b, d_g,
+        k_adjoint_modulus<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_nu.p, d_a, d_b, d_g,
                                                             accumulate ? 1 : 0);
     else
-        k_adjoint_modulus<4><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, d_a, d_b, d_g,
+        k_adjoint_modulus<4><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_nu.p, d_a, d_b, d_g,
                                                             accumulate ? 1 : 0);
+    ASEND_CUDA(cudaGetLastError());
+    ++c.launches;
+}
+
+void adjoint_pairs(Ctx& c, const double* d_a, const double* d_b, double* d_P, bool accumulate) {
+    if (c.type != 8 && c.type != 4)
+        throw InputError("strain-pair tensors are built for hex8 and tet4 meshes (no condensed internal DOF)");
+    const int blocks = (c.n_el + 127) / 128;
+    if (c.nn == 8)
+        k_adjoint_pairs<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, d_a, d_b, d_P, accumulate ? 1 : 0);
+    else
+        k_adjoint_pairs<4><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, d_a, d_b, d_P, accumulate ? 1 : 0);
     ASEND_CUDA(cudaGetLastError());
     ++c.launches;
 }

@@ -16,15 +16,18 @@ writes the reference's result files (results_io):
   loads           :981-1124 (nodalForce, surfaceTraction; activeTime)
   objective       :1298-1375 (displacement / velocity / acceleration with
                   powerNorm, objective_meth.rs:329-337 and :592-663)
+  design vars     :1218-1296 (modulus, shearModulus, poissonRatio components
+                  over element sets; hex8 / tet4 meshes)
   commands        model_meth.rs:20-140: readModelInput, readConstraints,
-                  readLoads, readObjectiveInput, solvePrep, solve (static or
-                  dynamic elastic), zeroSolution, modalAnalysis (frequency),
-                  calcObjective, writeNodeResults, writeModalResults,
-                  writeObjective.
+                  readLoads, readObjectiveInput, readDesignVarInput, solvePrep,
+                  solve (static or dynamic elastic), zeroSolution,
+                  modalAnalysis (frequency), calcObjective, calcObjGradient
+                  (static), writeNodeResults, writeModalResults,
+                  writeObjective (with the _grad file).
 
-Anything outside that subset (thermal, fluid, nonlinear geometry, design
-variables, other element or load types) raises NotImplementedError naming
-the item, rather than running something else.  Usage:
+Anything outside that subset (thermal, fluid, nonlinear geometry, other
+design-variable categories, other element or load types) raises
+NotImplementedError naming the item, rather than running something else.  Usage:
 
     python -m asend3d_gb300.job path/to/job.yaml
 """
@@ -257,6 +260,35 @@ def read_loads(path) -> list:
     return out
 
 
+DV_CATEGORIES = ("modulus", "shearModulus", "poissonRatio")
+
+
+def read_design_vars(path) -> list:
+    """read_des_var_input (model_input.rs:1218-1296)."""
+    out = []
+    for h, data, _ in read_records(path):
+        if h[0] != "designVariables":
+            continue
+        if h[1] == "category" and len(data) == 1:
+            out.append({"category": data[0], "component": 0, "layer": 0, "coefficients": [],
+                        "activeTime": [0.0, 1e100]})
+        elif not out:
+            continue
+        elif h[1] in ("elementSet", "nodeSet") and len(data) == 1:
+            out[-1][h[1]] = data[0]
+        elif h[1] == "component" and len(data) == 1:
+            out[-1]["component"] = int(data[0])
+        elif h[1] == "component" and len(data) == 2:
+            out[-1]["component"] = (int(data[0]), int(data[1]))
+        elif h[1] == "layer" and len(data) == 1:
+            out[-1]["layer"] = int(data[0])
+        elif h[1] == "coefficients" and len(data) == 1:
+            out[-1]["coefficients"].append(float(data[0]))
+        elif h[1] == "activeTime" and data:
+            out[-1]["activeTime"] = [float(data[0]), float(data[1]) if len(data) > 1 else 1e100]
+    return out
+
+
 def read_objective(path) -> list:
     out = []
     for h, data, _ in read_records(path):
@@ -299,6 +331,8 @@ class JobRunner:
         self.state = None          # {"u", "v", "a"} per node [n, dpn]
         self.modal = None
         self.obj_values = None
+        self.obj_gradient = None
+        self.dvs: list = []
         self.log: list = []
 
     def _path(self, name):
@@ -417,8 +451,39 @@ class JobRunner:
         self.objective.extend(read_objective(self._path(c["fileName"])))
 
     def cmd_readDesignVarInput(self, c):
-        raise NotImplementedError("design variables through job files are not on the GPU path yet; "
-                                  "use asend_add_modulus_design_var + asend_adjoint_gradient")
+        for dv in read_design_vars(self._path(c["fileName"])):
+            if dv["category"] not in DV_CATEGORIES:
+                raise NotImplementedError(f"design variable category {dv['category']} is not on the GPU path")
+            if not isinstance(dv["component"], int) or not 1 <= dv["component"] <= 3 or "elementSet" not in dv:
+                raise ValueError(f"design variable needs an element set and a component 1-3: {dv}")
+            self.dvs.append(dv)
+
+    def cmd_calcObjGradient(self, c):
+        """model_analysis.rs:1544-1706 (static branch): the adjoint of each
+        powerNorm displacement term of exponent 1 (its dL/du is then the
+        coefficient on the set's component, whatever the targets), summed;
+        each DV's gradient from the strain-pair tensors."""
+        from . import _lib
+        if self.g is None or self.state is None:
+            raise RuntimeError("calcObjGradient before a solve")
+        if self.solve_cmd.get("dynamic"):
+            raise NotImplementedError("transient objective gradients are not on the GPU path")
+        grad = np.zeros(len(self.dvs))
+        opts = self._opts(self.solve_cmd)
+        for t in self.objective:
+            if t["category"] != "displacement" or t["operator"] != "powerNorm" or t["exponent"] != 1.0:
+                raise NotImplementedError("gradients of displacement powerNorm terms of exponent 1 only")
+            if not (t["activeTime"][0] <= self.state["time"] <= t["activeTime"][1]):
+                continue
+            self.g.set_objective(("displacement", t["nodeSet"], t["component"], t["coefficient"]))
+            _, _, rc, st = self.g.adjoint_gradient(**opts)
+            if rc not in (_lib.ASEND_OK, _lib.ASEND_MAX_ITER):
+                raise RuntimeError(f"adjoint solve failed: {st}")
+            for i, dv in enumerate(self.dvs):
+                if dv["activeTime"][0] <= self.state["time"] <= dv["activeTime"][1]:
+                    grad[i] += self.g.material_dv_gradient(dv["category"], dv["component"], dv["elementSet"],
+                                                           dv["coefficients"])
+        self.obj_gradient = grad
 
     def cmd_solvePrep(self, c):
         self.solve_cmd.update({k: v for k, v in c.items() if k != "command"})
@@ -554,9 +619,13 @@ class JobRunner:
         from .results_io import write_objective
         if self.obj_values is None:
             raise RuntimeError("writeObjective before calcObjective")
+        grad = None
         if c.get("writeGradient"):
-            raise NotImplementedError("objective gradients through job files are not on the GPU path yet")
-        write_objective(str(self._out(c["fileName"])), self.obj_values, self.objective, c.get("include", ()))
+            if self.obj_gradient is None:
+                raise RuntimeError("writeGradient before calcObjGradient")
+            grad = self.obj_gradient
+        write_objective(str(self._out(c["fileName"])), self.obj_values, self.objective, c.get("include", ()),
+                        gradient=grad)
 
 
 def main(argv=None):

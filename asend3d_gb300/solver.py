@@ -231,6 +231,34 @@ class GpuSolver:
                                                          C.byref(st)), "adjoint_gradient")
         return L.value, g, rc, st.as_dict()
 
+    def set_objective(self, objective):
+        """("compliance",) or ("displacement", node_set, component, coefficient)."""
+        if objective[0] == "compliance":
+            rc = self.lib.asend_set_objective(self.ctx, _lib.OBJ_COMPLIANCE, -1, 0, 1.0)
+        else:
+            _, set_name, comp, coef = objective
+            rc = self.lib.asend_set_objective(self.ctx, _lib.OBJ_DISPLACEMENT, self.set_ids[set_name], comp, coef)
+        self._check(rc, "set_objective")
+
+    def strain_pairs(self) -> np.ndarray:
+        """[n_el, 6, 6] strain-pair tensors of the last adjoint gradient."""
+        P = np.zeros((self.p.mesh.n_elems, 6, 6))
+        self._check(self.lib.asend_adjoint_strain_pairs(self.ctx, _ptr(P, C.c_double)), "adjoint_strain_pairs")
+        return P
+
+    def material_dv_gradient(self, category, component, elem_set, coefs=()) -> float:
+        """dL/dD of a single-component material DV ('modulus', 'shearModulus',
+        'poissonRatio' or the _lib.DV_* code) over an element set, from the
+        last adjoint gradient."""
+        cat = {"modulus": _lib.DV_MODULUS, "shearModulus": _lib.DV_SHEAR_MODULUS,
+               "poissonRatio": _lib.DV_POISSON_RATIO}.get(category, category)
+        cf = np.ascontiguousarray(np.atleast_1d(coefs), dtype=np.float64)
+        out = C.c_double(0.0)
+        self._check(self.lib.asend_material_dv_gradient(self.ctx, cat, component, self.elset_ids[elem_set], len(cf),
+                                                        _ptr(cf, C.c_double) if len(cf) else None, C.byref(out)),
+                    "material_dv_gradient")
+        return out.value
+
     def design_var_gradient(self, dLdE) -> np.ndarray:
         dLdE = np.ascontiguousarray(dLdE, dtype=np.float64)
         out = np.zeros(max(1, len(self.p.design_vars)))

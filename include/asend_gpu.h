@@ -225,6 +225,24 @@ int asend_add_modulus_design_var(asend_ctx* ctx, int32_t elem_set, int32_t n_coe
                                  const double* coefs);
 int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_out);
 
+/* Material design variables of single components (the reference's
+ * 'modulus', 'shearModulus', 'poissonRatio' categories with component 1-3,
+ * DesignVariable design_var.rs:8-40 applied by get_solid_stiff,
+ * element_properties.rs:648-764).  After asend_adjoint_gradient:
+ *   asend_adjoint_strain_pairs fills pairs_out[n_el][6][6] with
+ *     P_e = sum_gp w detJ eps(lambda) eps(u)^T (Voigt 11,22,33,12,13,23,
+ *     engineering shear), so that lambda^T dR_e/dD = sum_ij (dC/dD)_ij P_e;
+ *   asend_material_dv_gradient returns dL/dD for one DV over an element set
+ *     (coefficients as asend_add_modulus_design_var), with C = S^-1 from the
+ *     reference's compliance form at the element's isotropic E, nu.
+ * hex8 and tet4 meshes (elements without condensed internal DOF). */
+#define ASEND_DV_MODULUS 0
+#define ASEND_DV_SHEAR_MODULUS 1
+#define ASEND_DV_POISSON_RATIO 2
+int asend_adjoint_strain_pairs(asend_ctx* ctx, double* pairs_out);
+int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t component, int32_t elem_set,
+                               int32_t n_coef, const double* coefs, double* grad_out);
+
 /* ---- Newmark transient (Model::solve dynamic loop model_analysis.rs:591-624;
  *      Node::update_vel_acc node_meth.rs:127-138, advance_disp :158-165) -----
  * Load at step i (time i*dt) = amp[i] * (load case 0).  Records

@@ -14,7 +14,7 @@ from asend3d_gb300 import job as J
 from asend3d_gb300.mesh import block_hex8
 
 
-def write_cantilever_job(d: Path, nx=4, ny=1, nz=1, L=4.0, etype="brickIM", modal=True):
+def write_cantilever_job(d: Path, nx=4, ny=1, nz=1, L=4.0, etype="brickIM", modal=True, dvs=False):
     """A cantilever of nx*ny*nz hex elements clamped at x = 0 with a -z tip
     load of 2 spread over the tip nodes, mean tip deflection objective."""
     m = block_hex8(nx, ny, nz, L, 1.0, 0.5)
@@ -42,18 +42,29 @@ def write_cantilever_job(d: Path, nx=4, ny=1, nz=1, L=4.0, etype="brickIM", moda
     (d / "objective.yaml").write_text("objectiveTerms:\n- category: displacement\n  operator: powerNorm\n"
                                       f"  nodeSet: xMax\n  component: 3\n  coefficient: {float(1.0 / len(xmax))!r}\n"
                                       "  exponent: 1.0\n")
+    (d / "dvars.yaml").write_text(
+        "designVariables:\n"
+        "- category: modulus\n  component: 1\n  layer: 0\n  elementSet: all\n  coefficients: 1.0\n"
+        "- category: shearModulus\n  component: 2\n  elementSet: all\n"
+        "- category: poissonRatio\n  component: 3\n  elementSet: all\n  coefficients:\n"
+        + "".join(f"  - {v}\n" for v in (2.0, 3.0, 4.0, 5.0)))
     job = ["jobCommands:",
            "- command: readModelInput", "  fileName: model.yaml",
            "- command: readConstraints", "  fileName: constraints.yaml",
            "- command: readLoads", "  fileName: loads.yaml",
-           "- command: readObjectiveInput", "  fileName: objective.yaml",
-           "- command: solve", "  elastic: yes", "  dynamic: no", "  solverMethod: iterative",
+           "- command: readObjectiveInput", "  fileName: objective.yaml"]
+    if dvs:
+        job += ["- command: readDesignVarInput", "  fileName: dvars.yaml"]
+    job += ["- command: solve", "  elastic: yes", "  dynamic: no", "  solverMethod: iterative",
            "  convergenceTol: 1.0e-11", "  maxIterations: 20000",
            "- command: calcObjective",
            "- command: writeNodeResults", f"  fileName: {d / 'nodes.csv'}", "  nodeSet: xMax",
            "  fields:", "  - displacement", "  - reactionForce",
-           "- command: writeObjective", f"  fileName: {d / 'obj.csv'}", "  include:", "  - category",
-           "  - coefficient"]
+    ]
+    if dvs:
+        job += ["- command: calcObjGradient"]
+    job += ["- command: writeObjective", f"  fileName: {d / 'obj.csv'}", "  include:", "  - category",
+            "  - coefficient"] + (["  writeGradient: yes"] if dvs else [])
     if modal:
         job += ["- command: modalAnalysis", "  type: frequency", "  numModes: 3",
                 "- command: writeModalResults", f"  fileName: {d / 'modal.csv'}", "  writeModes: yes"]
@@ -136,10 +147,28 @@ def test_objective_and_writers(tmp_path):
     assert r.obj_values[0] == pytest.approx(np.sqrt(len(xmax)) / len(xmax))
     r.cmd_writeObjective({"fileName": str(tmp_path / "o.csv"), "include": ["category"]})
     assert (tmp_path / "o.csv").read_text().splitlines()[1].startswith("0,")
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(RuntimeError, match="calcObjGradient"):
         r.cmd_writeObjective({"fileName": str(tmp_path / "o.csv"), "writeGradient": True})
-    with pytest.raises(NotImplementedError):
-        r.cmd_readDesignVarInput({"fileName": "x"})
+    r.obj_gradient = np.array([-8e-6, 1.0])
+    r.cmd_writeObjective({"fileName": str(tmp_path / "o.csv"), "writeGradient": True})
+    assert (tmp_path / "o_grad.csv").read_text() == "designVariable,objGrad\n0,-8.000000000000e-6\n1,1.000000000000e0\n"
+
+
+def test_design_var_reader(tmp_path):
+    write_cantilever_job(tmp_path, dvs=True)
+    dvs = J.read_design_vars(tmp_path / "dvars.yaml")
+    assert dvs == [{"category": "modulus", "component": 1, "layer": 0, "coefficients": [1.0], "activeTime": [0.0, 1e100],
+                    "elementSet": "all"},
+                   {"category": "shearModulus", "component": 2, "layer": 0, "coefficients": [], "activeTime": [0.0, 1e100],
+                    "elementSet": "all"},
+                   {"category": "poissonRatio", "component": 3, "layer": 0, "coefficients": [2.0, 3.0, 4.0, 5.0],
+                    "activeTime": [0.0, 1e100], "elementSet": "all"}]
+    r = J.JobRunner(tmp_path / "job.yaml")
+    r.cmd_readDesignVarInput({"fileName": "dvars.yaml"})
+    assert len(r.dvs) == 3
+    (tmp_path / "bad.yaml").write_text("designVariables:\n- category: nodeCoord\n  component: 1\n  nodeSet: xMax\n")
+    with pytest.raises(NotImplementedError, match="nodeCoord"):
+        r.cmd_readDesignVarInput({"fileName": "bad.yaml"})
 
 
 def test_unsupported_inputs(tmp_path):
