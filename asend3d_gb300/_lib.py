@@ -100,6 +100,7 @@ SIGNATURES = [
     ("asend_dense_sym_eigen", c_int, [c_int, P_dbl, P_dbl, P_dbl]),
     ("asend_adjoint_strain_pairs", c_int, [C.c_void_p, P_dbl]),
     ("asend_material_dv_gradient", c_int, [C.c_void_p, c_int, c_int, c_int, c_int, P_dbl, P_dbl]),
+    ("asend_material_dC", c_int, [c_int, c_int, c_dbl, c_dbl, P_dbl]),
     ("asend_operator_energy_noalloc", c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("asend_learned_n_params", c_int, []),
     ("asend_learned_init", c_int, [C.c_void_p, C.c_uint64]),

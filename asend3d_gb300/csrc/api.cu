@@ -1074,6 +1074,53 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
     });
 }
 
+// dC/dD of an isotropic element (E, nu, G = E / (2 (1 + nu))) for a DV on one
+// component of the reference's compliance S (element_properties.rs:648-764:
+// S00 = 1/E1, S01 = -nu12/E1, S02 = -nu13/E1, S11 = 1/E2, S12 = -nu23/E2,
+// S22 = 1/E3, S33..S55 = 1/G12, 1/G13, 1/G23; C = S^-1): dC = -C dS C.
+static void material_dC(int category, int component, double E, double nu, double* dC) {
+    const int k = component - 1;
+    const double G = E / (2.0 * (1.0 + nu));
+    const double la = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), mu = G;
+    double C[36] = {0};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) C[6 * i + j] = la + (i == j ? 2.0 * mu : 0.0);
+    for (int i = 3; i < 6; ++i) C[7 * i] = mu;
+    double dS[36] = {0};
+    if (category == ASEND_DV_MODULUS) {
+        dS[7 * k] = -1.0 / (E * E);
+        if (k == 0) dS[1] = dS[6] = dS[2] = dS[12] = nu / (E * E);
+        if (k == 1) dS[8] = dS[13] = nu / (E * E);
+    } else if (category == ASEND_DV_SHEAR_MODULUS) {
+        dS[7 * (3 + k)] = -1.0 / (G * G);
+    } else {
+        const int pr[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+        const int a = pr[k][0], b = pr[k][1];
+        dS[6 * a + b] = dS[6 * b + a] = -1.0 / E;
+    }
+    double T[36];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            double s = 0.0;
+            for (int l = 0; l < 6; ++l) s += dS[6 * i + l] * C[6 * l + j];
+            T[6 * i + j] = s;
+        }
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            double s = 0.0;
+            for (int l = 0; l < 6; ++l) s += C[6 * i + l] * T[6 * l + j];
+            dC[6 * i + j] = -s;
+        }
+}
+
+int asend_material_dC(int32_t category, int32_t component, double E, double nu, double* dC_out) {
+    if (category < ASEND_DV_MODULUS || category > ASEND_DV_POISSON_RATIO || component < 1 || component > 3 ||
+        !dC_out || !(E > 0.0) || !(nu > -1.0 && nu < 0.5))
+        return ASEND_EINVAL;
+    material_dC(category, component, E, nu, dC_out);
+    return ASEND_OK;
+}
+
 // Strain-pair tensors of the last adjoint gradient, P_e = sum_gp w detJ
 // eps(lambda) eps(u)^T (compliance: sum over load cases of the u_r pairs).
 static void ensure_pairs(Ctx& c) {
@@ -1120,42 +1167,11 @@ int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t compone
         require(n_coef <= 1 || (size_t)n_coef == set.size(), "coefficient list does not match the element set");
         require(n_coef == 0 || coefs, "null coefficients");
         ensure_pairs(c);
-        const int k = component - 1;
         double g = 0.0;
         for (size_t q = 0; q < set.size(); ++q) {
             const int e = set[q];
-            const double E = c.E[e], nu = c.nu[e], G = E / (2.0 * (1.0 + nu));
-            const double la = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), mu = G;
-            double C[36] = {0};
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) C[6 * i + j] = la + (i == j ? 2.0 * mu : 0.0);
-            for (int i = 3; i < 6; ++i) C[7 * i] = mu;
-            double dS[36] = {0};
-            if (category == ASEND_DV_MODULUS) {
-                // S00 = 1/E1, S01 = -nu12/E1, S02 = -nu13/E1, S11 = 1/E2, S12 = -nu23/E2, S22 = 1/E3
-                dS[7 * k] = -1.0 / (E * E);
-                if (k == 0) dS[1] = dS[6] = dS[2] = dS[12] = nu / (E * E);
-                if (k == 1) dS[8] = dS[13] = nu / (E * E);
-            } else if (category == ASEND_DV_SHEAR_MODULUS) {
-                dS[7 * (3 + k)] = -1.0 / (G * G);
-            } else {
-                const int pr[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-                const int a = pr[k][0], b = pr[k][1];
-                dS[6 * a + b] = dS[6 * b + a] = -1.0 / E;
-            }
-            double T[36], dC[36];
-            for (int i = 0; i < 6; ++i)
-                for (int j = 0; j < 6; ++j) {
-                    double s = 0.0;
-                    for (int l = 0; l < 6; ++l) s += dS[6 * i + l] * C[6 * l + j];
-                    T[6 * i + j] = s;
-                }
-            for (int i = 0; i < 6; ++i)
-                for (int j = 0; j < 6; ++j) {
-                    double s = 0.0;
-                    for (int l = 0; l < 6; ++l) s += C[6 * i + l] * T[6 * l + j];
-                    dC[6 * i + j] = -s;
-                }
+            double dC[36];
+            material_dC(category, component, c.E[e], c.nu[e], dC);
             const double* P = &c.h_pairs[(size_t)e * 36];
             double s = 0.0;
             for (int i = 0; i < 36; ++i) s += dC[i] * P[i];

@@ -242,6 +242,10 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
 int asend_adjoint_strain_pairs(asend_ctx* ctx, double* pairs_out);
 int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t component, int32_t elem_set,
                                int32_t n_coef, const double* coefs, double* grad_out);
+/* dC/dD (row-major 6 x 6, Voigt order) of an isotropic element (E, nu,
+ * G = E / (2 (1 + nu))) for a DV of the given category on one component;
+ * host only, used by asend_material_dv_gradient. */
+int asend_material_dC(int32_t category, int32_t component, double E, double nu, double* dC_out);
 
 /* ---- Newmark transient (Model::solve dynamic loop model_analysis.rs:591-624;
  *      Node::update_vel_acc node_meth.rs:127-138, advance_disp :158-165) -----
