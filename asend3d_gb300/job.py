@@ -21,7 +21,8 @@ writes the reference's result files (results_io):
   commands        model_meth.rs:20-140: readModelInput, readConstraints,
                   readLoads, readObjectiveInput, readDesignVarInput, solvePrep,
                   solve (static or dynamic elastic), zeroSolution,
-                  modalAnalysis (frequency), calcObjective, calcObjGradient
+                  modalAnalysis (frequency), setSolnToMode, calcObjective,
+                  calcObjGradient
                   (static), writeNodeResults, writeModalResults,
                   writeObjective (with the _grad file).
 
@@ -440,6 +441,7 @@ class JobRunner:
 
     def cmd_readModelInput(self, c):
         self.model = read_model(self._path(c["fileName"]))
+        self.node_index = {lab: i for i, lab in enumerate(self.model.node_labels)}
 
     def cmd_readConstraints(self, c):
         self.constraints.extend(read_constraints(self._path(c["fileName"])))
@@ -539,6 +541,28 @@ class JobRunner:
             raise RuntimeError(f"eigen solve did not converge: {st}")
         dpn = self.problem.mesh.dpn
         self.modal = {"eig": ev, "freq": fr, "modes": modes.reshape(len(ev), -1, dpn)}
+
+    def cmd_setSolnToMode(self, c):
+        """set_soln_to_mode (model_analysis.rs:890-933): the field becomes mode
+        `mode` (0-based; the job default is 1, job.rs:97-99) scaled so that its
+        largest |component| equals maxAmplitude.  Mode signs are those of the
+        eigen solve (largest-magnitude component positive)."""
+        if self.modal is None:
+            raise RuntimeError("setSolnToMode before modalAnalysis")
+        field = c.get("solnField", "displacement")
+        k = c.get("mode", 1)
+        amp = c.get("maxAmplitude", 1.0)
+        if field not in ("displacement", "velocity", "acceleration"):
+            print(f"Warning: {field} is not a valid field to Set to a mode. Aborting setSolnToMode()")
+            return
+        if not 0 <= k < len(self.modal["eig"]):
+            raise ValueError(f"mode {k} was not computed")
+        mode = self.modal["modes"][k]
+        shape = mode.shape
+        if self.state is None:
+            self.state = {"u": np.zeros(shape), "v": np.zeros(shape), "a": np.zeros(shape), "time": 0.0}
+        key = {"displacement": "u", "velocity": "v", "acceleration": "a"}[field]
+        self.state[key] = (amp / np.abs(mode).max()) * mode
 
     def cmd_calcObjective(self, c):
         if self.state is None:

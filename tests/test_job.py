@@ -183,3 +183,25 @@ def test_unsupported_inputs(tmp_path):
     r.model = J.ModelInput()
     with pytest.raises(NotImplementedError, match="thermal"):
         r.cmd_solve(r.cmds[0])
+
+
+def test_set_soln_to_mode(tmp_path):
+    m, xmin, xmax = write_cantilever_job(tmp_path)
+    r = J.JobRunner(tmp_path / "job.yaml")
+    for c in r.cmds[:4]:
+        getattr(r, "cmd_" + c["command"])(c)
+    n = m.n_nodes
+    rng = np.random.default_rng(1)
+    modes = rng.standard_normal((3, n, 3))
+    r.modal = {"eig": np.array([1.0, 2.0, 3.0]), "freq": np.zeros(3), "modes": modes}
+    r.cmd_setSolnToMode({})  # defaults: displacement, mode 1, amplitude 1
+    np.testing.assert_allclose(r.state["u"], modes[1] / np.abs(modes[1]).max())
+    r.cmd_setSolnToMode({"solnField": "velocity", "mode": 2, "maxAmplitude": 0.5})
+    assert np.abs(r.state["v"]).max() == pytest.approx(0.5)
+    np.testing.assert_allclose(r.state["u"], modes[1] / np.abs(modes[1]).max())
+    r.cmd_writeNodeResults({"fileName": str(tmp_path / "m.csv"), "fields": ["displacement", "velocity"]})
+    lines = (tmp_path / "m.csv").read_text().splitlines()
+    assert len(lines) == n + 1 and lines[0].startswith("node,U1,U2,U3,R1,R2,R3,V1")
+    r.cmd_setSolnToMode({"solnField": "stress"})  # the reference warns and leaves the state
+    with pytest.raises(ValueError):
+        r.cmd_setSolnToMode({"mode": 7})
