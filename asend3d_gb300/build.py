@@ -1,4 +1,5 @@
-"""Build the in-tree CUDA library ``asend3d_gb300/libasend_gpu.so`` for sm_103a.
+"""Build the in-tree CUDA library ``asend3d_gb300/libasend_gpu.so`` for sm_103a
+and the job-file CLI ``asend3d_gb300/asend_run_job`` on its C ABI.
 
 Each ``csrc/*.cu`` translation unit is compiled by nvcc in parallel, then
 linked into one shared library exporting the C ABI of
@@ -63,7 +64,28 @@ def build(verbose: bool = False) -> Path:
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    build_cli(verbose)
     return LIB
+
+
+CLI_SRC = PKG / "cli" / "asend_run_job.cpp"
+CLI = PKG / "asend_run_job"
+
+
+def build_cli(verbose: bool = False) -> Path:
+    """The job-file CLI (host C++ on the C ABI), linked against the library."""
+    newest = max(CLI_SRC.stat().st_mtime, (ROOT / "include" / "asend_gpu.h").stat().st_mtime, LIB.stat().st_mtime)
+    if CLI.exists() and CLI.stat().st_mtime >= newest:
+        return CLI
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", f"-I{ROOT / 'include'}", str(CLI_SRC), f"-L{PKG}", "-lasend_gpu",
+           "-Wl,-rpath,$ORIGIN", "-o", str(CLI)]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"asend_run_job build failed:\n{res.stdout}\n{res.stderr}")
+    return CLI
 
 
 if __name__ == "__main__":

@@ -66,3 +66,31 @@ def test_job_static_and_modal(gpu_lib, oracle_lib, tmp_path):
     np.testing.assert_allclose(modal[:, 2], np.sqrt(modal[:, 1]) / (2 * np.pi), rtol=1e-12)
     mode0 = (tmp_path / "modal_mode0.csv").read_text().splitlines()
     assert mode0[0] == "Node,U1,U2,U3,R1,R2,R3" and len(mode0) == m.n_nodes + 1
+
+
+def test_cli_matches_python_runner(gpu_lib, tmp_path):
+    """The C++ asend_run_job and the Python runner make the same library calls:
+    the same headers and values (1e-12) in every result file."""
+    import subprocess
+
+    from asend3d_gb300 import build
+    build.build()
+    d1, d2 = tmp_path / "py", tmp_path / "cli"
+    d1.mkdir()
+    d2.mkdir()
+    write_cantilever_job(d1, etype="brick8", dvs=True)
+    write_cantilever_job(d2, etype="brick8", dvs=True)
+    J.JobRunner(d1 / "job.yaml").run()
+    out = subprocess.run([str(build.CLI), str(d2 / "job.yaml")], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    def numbers(lines):
+        return np.array([float(v) for ln in lines for v in ln.split(",")[1:] if v[:1].isdigit() or v[:1] in "-."])
+
+    for name in ("nodes.csv", "obj.csv", "obj_grad.csv", "modal.csv", "modal_mode0.csv"):
+        a, b = (d1 / name).read_text().splitlines(), (d2 / name).read_text().splitlines()
+        assert a[0] == b[0] and len(a) == len(b), name
+        assert [ln.split(",")[0] for ln in a] == [ln.split(",")[0] for ln in b], name
+        fa, fb = numbers(a[1:]), numbers(b[1:])
+        assert fa.shape == fb.shape, name
+        # summation order differs (numpy vs the C++ loop) in reactions and sums
+        assert np.allclose(fa, fb, rtol=1e-12, atol=1e-12 * np.abs(fa).max()), name
