@@ -64,7 +64,10 @@ def build(verbose: bool = False) -> Path:
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    build_cli(verbose)
+    try:
+        build_cli(verbose)
+    except (RuntimeError, OSError) as err:  # the library stays usable; the CLI's own tests report it
+        print(f"warning: asend_run_job was not built: {err}", file=sys.stderr)
     return LIB
 
 
@@ -78,8 +81,9 @@ def build_cli(verbose: bool = False) -> Path:
     if CLI.exists() and CLI.stat().st_mtime >= newest:
         return CLI
     cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cuda_lib = Path(nvcc()).resolve().parent.parent / "lib64"  # libcudart, needed by the library
     cmd = [cxx, "-O2", "-std=c++17", f"-I{ROOT / 'include'}", str(CLI_SRC), f"-L{PKG}", "-lasend_gpu",
-           "-Wl,-rpath,$ORIGIN", "-o", str(CLI)]
+           f"-L{cuda_lib}", f"-Wl,-rpath-link,{cuda_lib}", "-Wl,-rpath,$ORIGIN", "-o", str(CLI)]
     if verbose:
         print(" ".join(cmd), flush=True)
     res = subprocess.run(cmd, capture_output=True, text=True)

@@ -75,6 +75,7 @@ def test_cli_matches_python_runner(gpu_lib, tmp_path):
 
     from asend3d_gb300 import build
     build.build()
+    build.build_cli()
     d1, d2 = tmp_path / "py", tmp_path / "cli"
     d1.mkdir()
     d2.mkdir()

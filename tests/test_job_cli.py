@@ -18,7 +18,7 @@ from test_job import write_cantilever_job
 @pytest.fixture(scope="module")
 def cli():
     build.build()
-    return str(build.CLI)
+    return str(build.build_cli())  # raises with the compiler's message if the CLI does not build
 
 
 def test_parse_matches_python_readers(cli, tmp_path):
