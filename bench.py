@@ -443,6 +443,30 @@ def cpu_baseline(nx: int, procs: int):
             "per_instance_s": per_proc}
 
 
+def sample_accuracy(nx: int, kw: dict) -> dict:
+    """The CPU-baseline sample (the first instance of the pool, seed 100)
+    solved by this library with the benchmark's options and by the FP64
+    oracle's direct LDL^T: relative errors of u, the compliance and its
+    per-element gradient."""
+    from asend3d_gb300 import configs
+    from asend3d_gb300.solver import GpuSolver
+    from oracle import pyoracle as po
+
+    p = configs.block_large(nx=nx, ny=nx // 5, nz=nx // 5, seed=100)
+    g = GpuSolver(p)
+    g.assemble(precision=64)
+    u, rc, _ = g.static_solve(**kw)
+    L, gE, rc2, _ = g.adjoint_gradient(**kw)
+    g.close()
+    o = po.Oracle(p)
+    f = o.loads()[0] + o.penalty_rhs()
+    ur, _, _ = o.solve(f, precond=po.PC_DIRECT)
+    gr, _, _, _ = o.adjoint(ur, lam=ur)
+    rel = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))
+    return {"sample": f"{nx}x{nx // 5}x{nx // 5} hex8, seed 100, oracle direct LDL^T", "rc": [rc, rc2],
+            "u_rel": rel(u[0], ur), "compliance_rel": abs(L - f @ ur) / abs(f @ ur), "gradient_rel": rel(gE, gr)}
+
+
 def run_reference(a):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -606,12 +630,34 @@ def run_ours(a):
             "traffic": ncu_traffic(), "algorithmic_bytes_per_launch": bytes_spmv, "ms_per_launch": ms_spmv,
             "fp64_spmv": {"ms_per_launch": ms_spmv64, "achieved_GBps": bytes_spmv64 / (ms_spmv64 * 1e-3) / 1e9}}
 
+    # ---- accuracy at full size: the benchmark's 1e-8 solution and gradient
+    # against the same library at 1e-11 (FP64 operator); never fatal
+    accuracy = {}
+    if rank == 0:
+        try:
+            g.assemble(precision=64)
+            u8, _, _ = g.static_solve(**mixed)
+            L8, gE8, _, _ = g.adjoint_gradient(**mixed)
+            tight = dict(mixed, rel_tol=1e-11, max_iter=400)
+            u11, rc11, st11 = g.static_solve(**tight)
+            L11, gE11, _, _ = g.adjoint_gradient(**tight)
+            rel = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))
+            accuracy["full_size_vs_fp64_1e-11"] = {"u_rel": rel(u8, u11), "compliance_rel": abs(L8 - L11) / abs(L11),
+                                                    "gradient_rel": rel(gE8, gE11), "rc_1e-11": rc11,
+                                                    "rel_residual_1e-11": st11["rel_residual"]}
+        except Exception as err:  # the measurement above stands on its own
+            accuracy["full_size_error"] = repr(err)[:200]
+
     out = None
     if rank == 0:
         cb = None
         if not a.no_cpu_baseline and world == 1:
             cb = cpu_baseline(a.cpu_sample_nx, 1)
             cb["kind"] = "port"
+            try:
+                accuracy["sample_vs_oracle"] = sample_accuracy(a.cpu_sample_nx, mixed)
+            except Exception as err:
+                accuracy["sample_vs_oracle_error"] = repr(err)[:200]
         clocks = clk.summary()
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -627,7 +673,8 @@ def run_ours(a):
                "plain_fp64_jacobi": {"value": plain_value, "ms_per_step": ms_plain,
                                      "iterations": st_plain["iterations"]},
                "speedup_vs_plain_fp64": value / plain_value,
-               "roofline": roof, "cpu_baseline": cb, "clocks": clocks, "gpu_launches": launches}
+               "roofline": roof, "cpu_baseline": cb, "clocks": clocks, "gpu_launches": launches,
+               "accuracy": accuracy}
         print(json.dumps(out))
     g.close()
     if world > 1:
