@@ -407,6 +407,14 @@ void write_text(const std::string& path, const std::string& s) {
 // ---------------------------------------------------------------------------
 // the runner
 // ---------------------------------------------------------------------------
+// The reference's solver log lines (matrix_functions.rs:358-359), scraped by
+// job scripts for "Total CG iterations:"; the second line carries this
+// library's final ||f - A u|| / ||f|| (the reference prints g^T M^-1 g).
+void cg_log(long long iterations, double residual) {
+    std::printf("Total CG iterations: %lld\nFinal residual norm: %.17g\n", iterations, residual);
+    std::fflush(stdout);
+}
+
 struct Runner {
     std::string base;
     std::vector<Command> cmds;
@@ -547,6 +555,7 @@ struct Runner {
             const int rc = asend_static_solve(ctx, &o, u.data(), &st);
             check(rc, "static_solve");
             if (rc == ASEND_NONFINITE) throw Fail("static solve turned non-finite");
+            cg_log(st.iterations, st.rel_residual);
         } else {
             const double dt = num(solve_kv.at("timeStep"));
             const double beta = solve_kv.count("newmarkBeta") ? num(solve_kv["newmarkBeta"]) : 0.25;
@@ -559,6 +568,7 @@ struct Runner {
             const int rc = asend_newmark_run(ctx, &o, steps, amp.data(), -1, nullptr, u.data(), &st);
             check(rc, "newmark_run");
             if (rc == ASEND_NONFINITE) throw Fail("Newmark run turned non-finite");
+            cg_log(st.iterations, st.rel_residual);
             time = steps * dt;
         }
         solved = true;
@@ -581,6 +591,7 @@ struct Runner {
         const int rc = asend_eigen_solve(ctx, &eo, eig.data(), freq.data(), modes.data(), nullptr, &st);
         check(rc, "eigen_solve");
         if (rc != ASEND_OK) throw Fail("eigen solve did not converge");
+        cg_log(st.inner_iterations, st.max_rel_residual);
         eig.resize(st.n_found);
         freq.resize(st.n_found);
     }
@@ -618,6 +629,7 @@ struct Runner {
             double L = 0.0;
             asend_solve_stats st{};
             check(asend_adjoint_gradient(ctx, &o, &L, nullptr, &st), "adjoint_gradient");
+            cg_log(st.iterations, st.rel_residual);
             for (size_t i = 0; i < dvs.size(); ++i) {
                 const DesignVar& dv = dvs[i];
                 if (!(dv.t0 <= time && time <= dv.t1)) continue;

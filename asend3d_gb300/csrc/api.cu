@@ -12,6 +12,16 @@
 #include <numeric>
 
 #include "common.cuh"
+#include <nvtx3/nvToolsExt.h>
+
+namespace {
+// NVTX range over one ABI call (named phases in Nsight timelines; a no-op
+// without a profiler attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+}  // namespace
 
 using namespace asend;
 
@@ -772,6 +782,7 @@ int asend_get_load_vector(asend_ctx* ctx, int32_t rhs, double* f_out) {
 int asend_assemble(asend_ctx* ctx, int32_t precision, int32_t dynamic, double dt, double beta,
                    double gamma) {
     return guarded(ctx, [&](Ctx& c) {
+        NvtxRange nvtx_range("asend_assemble");
         require(c.n_el > 0, "set the mesh first");
         require(precision == 32 || precision == 64, "precision must be 32 or 64");
         require(dynamic >= 0 && dynamic <= 2, "dynamic must be 0, 1 or 2");
@@ -878,6 +889,7 @@ int asend_time_spmv(asend_ctx* ctx, int32_t precision, int32_t n_launch, double*
 
 int asend_static_solve_device(asend_ctx* ctx, const asend_solve_opts* opts, asend_solve_stats* stats) {
     return guarded(ctx, [&](Ctx& c) {
+        NvtxRange nvtx_range("asend_static_solve_device");
         require(opts != nullptr, "null options");
         require(c.assembled, "assemble first");
         upload_rhs(c);
@@ -890,6 +902,7 @@ int asend_static_solve_device(asend_ctx* ctx, const asend_solve_opts* opts, asen
 
 int asend_static_solve(asend_ctx* ctx, const asend_solve_opts* opts, double* u_io, asend_solve_stats* stats) {
     return guarded(ctx, [&](Ctx& c) {
+        NvtxRange nvtx_range("asend_static_solve");
         require(opts != nullptr && u_io != nullptr, "null argument");
         require(c.assembled, "assemble first");
         upload_rhs(c);
@@ -935,6 +948,7 @@ int asend_set_objective(asend_ctx* ctx, int32_t kind, int32_t node_set, int32_t 
 int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double* L_out, double* dLdE_out,
                            asend_solve_stats* stats) {
     return guarded(ctx, [&](Ctx& c) {
+        NvtxRange nvtx_range("asend_adjoint_gradient");
         require(opts != nullptr, "null options");
         require(c.solved, "run a static solve before the adjoint gradient");
         const size_t n = c.n_dof;
@@ -1013,6 +1027,7 @@ int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double*
 int asend_newmark_run(asend_ctx* ctx, const asend_solve_opts* opts, int32_t n_steps, const double* amp,
                       int32_t probe_dof, double* probe_hist, double* u_final, asend_solve_stats* stats) {
     return guarded(ctx, [&](Ctx& c) {
+        NvtxRange nvtx_range("asend_newmark_run");
         require(opts && amp && n_steps > 0, "bad Newmark arguments");
         require(c.assembled && c.dynamic && !c.modal, "assemble with dynamic=1 first");
         require(probe_dof < c.n_dof, "probe DOF out of range");
@@ -1023,6 +1038,7 @@ int asend_newmark_run(asend_ctx* ctx, const asend_solve_opts* opts, int32_t n_st
 int asend_eigen_solve(asend_ctx* ctx, const asend_eigen_opts* opts, double* eig_out, double* freq_out,
                       double* modes_out, double* diag_mass_out, asend_eigen_stats* stats) {
     return guarded(ctx, [&](Ctx& c) {
+        NvtxRange nvtx_range("asend_eigen_solve");
         require(opts != nullptr, "null options");
         require(c.n_el > 0, "set the mesh first");
         require(c.n_inst <= 1, "modal analysis takes one model, not a batch of instances");

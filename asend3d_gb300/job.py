@@ -317,6 +317,13 @@ def read_objective(path) -> list:
 # ---------------------------------------------------------------------------
 # the runner
 # ---------------------------------------------------------------------------
+def _cg_log(iterations, residual):
+    """The reference's solver log lines (matrix_functions.rs:358-359), which
+    job scripts scrape for "Total CG iterations:"; the second line carries
+    this library's final ||f - A u|| / ||f|| (the reference prints g^T M^-1 g)."""
+    print(f"Total CG iterations: {int(iterations)}", flush=True)
+    print(f"Final residual norm: {residual!r}", flush=True)
+
 class JobRunner:
     def __init__(self, job_path, device=0):
         self.job_path = Path(job_path)
@@ -481,6 +488,7 @@ class JobRunner:
             _, _, rc, st = self.g.adjoint_gradient(**opts)
             if rc not in (_lib.ASEND_OK, _lib.ASEND_MAX_ITER):
                 raise RuntimeError(f"adjoint solve failed: {st}")
+            _cg_log(st["iterations"], st["rel_residual"])
             for i, dv in enumerate(self.dvs):
                 if dv["activeTime"][0] <= self.state["time"] <= dv["activeTime"][1]:
                     grad[i] += self.g.material_dv_gradient(dv["category"], dv["component"], dv["elementSet"],
@@ -511,6 +519,7 @@ class JobRunner:
             u, rc, st = g.static_solve(**self._opts(cmd))
             if rc not in (_lib.ASEND_OK, _lib.ASEND_MAX_ITER):
                 raise RuntimeError(f"static solve failed: {st}")
+            _cg_log(st["iterations"], st["rel_residual"])
             self.state = {"u": u[0].reshape(n, dpn), "v": np.zeros((n, dpn)), "a": np.zeros((n, dpn)),
                           "time": cmd.get("staticLoadTime", [0.0])[0]}
         else:
@@ -526,6 +535,7 @@ class JobRunner:
             hist, u, rc, st = g.newmark(np.ones(n_steps), **kw)
             if rc not in (_lib.ASEND_OK, _lib.ASEND_MAX_ITER):
                 raise RuntimeError(f"Newmark run failed: {st}")
+            _cg_log(st["iterations"], st["rel_residual"])
             self.state = {"u": u.reshape(n, dpn), "v": None, "a": None, "time": n_steps * dt}
 
     def cmd_modalAnalysis(self, c):
@@ -539,6 +549,7 @@ class JobRunner:
         ev, fr, modes, _, rc, st = g.eigen(c.get("numModes", 10), shift=c.get("targetEigenvalue", 0.0), **kw)
         if rc != _lib.ASEND_OK:
             raise RuntimeError(f"eigen solve did not converge: {st}")
+        _cg_log(st["inner_iterations"], st["max_rel_residual"])
         dpn = self.problem.mesh.dpn
         self.modal = {"eig": ev, "freq": fr, "modes": modes.reshape(len(ev), -1, dpn)}
 

@@ -205,3 +205,12 @@ def test_set_soln_to_mode(tmp_path):
     r.cmd_setSolnToMode({"solnField": "stress"})  # the reference warns and leaves the state
     with pytest.raises(ValueError):
         r.cmd_setSolnToMode({"mode": 7})
+
+
+def test_cg_log_lines(capsys):
+    """Job scripts sum the integer after "Total CG iterations:" (the
+    reference's matrix_functions.rs:358-359 lines)."""
+    J._cg_log(25, 3.5e-9)
+    out = capsys.readouterr().out.splitlines()
+    assert out == ["Total CG iterations: 25", "Final residual norm: 3.5e-09"]
+    assert int(out[0].split(":")[1]) == 25
