@@ -1585,4 +1585,111 @@ int orc_eigen_solve(orc_model* m, int32_t n_modes, double shift, double* eig, do
     return found;
 }
 
+
+// Transient adjoint, elastic Newmark (model_analysis.rs:1544-1631 dynamic
+// branch; augmentd_ld_u :936-1063; solve_for_adjoint :1065-1126) for
+//   L = sum_{n=1..N} sum_k w_k u_n[dof_k]
+// (a displacement powerNorm of exponent 1 evaluated at every saved step) and
+// per-element isotropic modulus DVs.  The forward run is orc_newmark_run's
+// with a direct solve and every step's (u, v, a) kept, as the solnTStep
+// history; the sweep runs n = N..1:
+//   step n < N adds the coupling to step n+1's adjoints (augmentd_ld_u):
+//     dL/du -= (d_ad_up M) u_adj, dL/dv -= (d_ad_vp M) u_adj,
+//     dL/da -= (d_ad_ap M) u_adj (no damping on this path), then
+//     dL/du += c1 a_adj, dL/da += c2 a_adj + c3 v_adj, dL/dv += c4 a_adj + v_adj
+//     with d_ad_up = c1 = 1/(dt^2 (beta - gamma)), d_ad_vp = dt d_ad_up,
+//     d_ad_ap = c2 = dt^2 (0.5 + beta - gamma) d_ad_up, c3 = dt (1 - gamma),
+//     c4 = 1/(dt (beta - gamma));
+//   dL/du += w (the step's objective term); v_adj = dL/dv;
+//   a_adj = dL/da + dt gamma v_adj; dL/du -= a_adj / (dt^2 (beta - gamma));
+//   A u_adj = dL/du with the step operator A = K + c_M M + penalty;
+//   dL/dE_e -= u_adj_e^T (K_e / E_e) u_n,e (only K depends on E).
+// The reference holds `time` at the end time through the sweep (:1563-1566);
+// with the objective and loads active at all times that changes nothing here.
+// Needs orc_assemble(m, 1, dt, beta, gamma).  gE[n_el], *L_out.
+int orc_newmark_adjoint(orc_model* m, int32_t n_steps, double dt, double beta, double gamma,
+                        const double* f_shape, const double* amp, int32_t n_obj, const int32_t* obj_dof,
+                        const double* obj_w, double* L_out, double* gE) {
+    if (!m->assembled || !m->dynamic || m->cM == 0.0 || n_steps < 1) return -1;
+    const int n = m->n_dof;
+    std::vector<double> u(n, 0.0), v(n, 0.0), a(n, 0.0), up(n, 0.0), vp(n, 0.0), ap(n, 0.0);
+    std::vector<double> load(n), du(n), tmp(n), ku(n);
+    const double c1n = 1.0 / (dt * dt * (beta - gamma));
+    const double c2n = dt * dt * (0.5 + beta - gamma);
+    auto update_vel_acc = [&]() {
+        for (int i = 0; i < n; ++i) {
+            a[i] = c1n * (up[i] - u[i] + dt * vp[i] + c2n * ap[i]);
+            v[i] = vp[i] + dt * ((1.0 - gamma) * ap[i] + gamma * a[i]);
+        }
+    };
+    update_vel_acc();
+    Precond pc;
+    pc.setup(m, ORC_PC_DIRECT, 0);
+    std::vector<std::vector<double>> hist_u(n_steps + 1, std::vector<double>(n, 0.0));
+    for (int s = 0; s < n_steps; ++s) {
+        std::fill(ku.begin(), ku.end(), 0.0);
+        m->K.matvec(u.data(), ku.data());
+        for (int i = 0; i < n; ++i) tmp[i] = a[i] - m->cM * u[i];
+        m->M.matvec(tmp.data(), ku.data());
+        for (int i = 0; i < n; ++i) load[i] = amp[s] * f_shape[i] - ku[i];
+        constraint_load(m, u.data(), load.data());
+        pc.apply(load.data(), du.data());
+        for (int i = 0; i < n; ++i) u[i] += du[i];
+        update_vel_acc();
+        hist_u[s + 1] = u;
+        up = u; vp = v; ap = a;
+        update_vel_acc();
+    }
+    double L = 0.0;
+    for (int s = 1; s <= n_steps; ++s)
+        for (int k = 0; k < n_obj; ++k) L += obj_w[k] * hist_u[s][obj_dof[k]];
+    if (L_out) *L_out = L;
+    // backward sweep
+    const double d_ad_up = 1.0 / (dt * dt * (beta - gamma));
+    const double d_ad_vp = d_ad_up * dt;
+    const double d_ad_ap = d_ad_up * dt * dt * (0.5 + beta - gamma);
+    const double c1 = d_ad_up, c2 = d_ad_ap, c3 = dt * (1.0 - gamma), c4 = 1.0 / (dt * (beta - gamma));
+    std::vector<double> u_adj(n, 0.0), v_adj(n, 0.0), a_adj(n, 0.0), dldu(n), dldv(n), dlda(n), mu(n);
+    std::fill(gE, gE + m->n_el, 0.0);
+    const int nn = m->ti.nn, tot = 3 * nn;
+    std::vector<double> ke(tot * tot);
+    for (int s = n_steps; s >= 1; --s) {
+        std::fill(dldu.begin(), dldu.end(), 0.0);
+        std::fill(dldv.begin(), dldv.end(), 0.0);
+        std::fill(dlda.begin(), dlda.end(), 0.0);
+        if (s < n_steps) {
+            std::fill(mu.begin(), mu.end(), 0.0);
+            m->M.matvec(u_adj.data(), mu.data());
+            for (int i = 0; i < n; ++i) {
+                dldu[i] -= d_ad_up * mu[i];
+                dlda[i] -= d_ad_ap * mu[i];
+                dldv[i] -= d_ad_vp * mu[i];
+                dldu[i] += c1 * a_adj[i];
+                dlda[i] += c2 * a_adj[i] + c3 * v_adj[i];
+                dldv[i] += c4 * a_adj[i] + v_adj[i];
+            }
+        }
+        for (int k = 0; k < n_obj; ++k) dldu[obj_dof[k]] += obj_w[k];
+        for (int i = 0; i < n; ++i) {
+            v_adj[i] = dldv[i];
+            a_adj[i] = dlda[i] + dt * gamma * v_adj[i];
+            dldu[i] -= d_ad_up * a_adj[i];
+        }
+        pc.apply(dldu.data(), u_adj.data());
+        const std::vector<double>& us = hist_u[s];
+        for (int e = 0; e < m->n_el; ++e) {
+            elem_km(m, e, ke.data(), nullptr);
+            double acc = 0.0;
+            for (int i = 0; i < tot; ++i) {
+                const int gi = m->conn[(size_t)e * nn + i / 3] * 3 + i % 3;
+                double ki = 0.0;
+                for (int j = 0; j < tot; ++j) ki += ke[i * tot + j] * us[m->conn[(size_t)e * nn + j / 3] * 3 + j % 3];
+                acc += u_adj[gi] * ki;
+            }
+            gE[e] -= acc / m->E[e];
+        }
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -112,6 +112,13 @@ int orc_newmark_run(orc_model* m, int32_t n_steps, double dt, double beta, doubl
 int orc_eigen_solve(orc_model* m, int32_t n_modes, double shift, double* eig, double* freq, double* modes,
                     double* diag_mass);
 
+/* Transient adjoint of L = sum over the N steps of sum_k w_k u_n[dof_k] with
+ * respect to the per-element moduli (direct solves; the reference's reverse
+ * sweep).  Needs orc_assemble(m, 1, dt, beta, gamma). */
+int orc_newmark_adjoint(orc_model* m, int32_t n_steps, double dt, double beta, double gamma,
+                        const double* f_shape, const double* amp, int32_t n_obj, const int32_t* obj_dof,
+                        const double* obj_w, double* L_out, double* gE);
+
 int orc_reorder_nodes(const orc_model* m, int32_t block_dim, int32_t* order_out);
 
 #ifdef __cplusplus

@@ -64,6 +64,8 @@ def load():
                                           C.c_int32, P_d, C.c_int32, C.c_int32, C.c_double, C.c_int32, P_d, P_i]),
             "orc_reorder_nodes": (C.c_int, [C.c_void_p, C.c_int32, P_i]),
             "orc_eigen_solve": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, P_d, P_d, P_d, P_d]),
+            "orc_newmark_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double, P_d, P_d,
+                                              C.c_int32, P_i, P_d, P_d, P_d]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -223,6 +225,21 @@ class Oracle:
         if k < 0:
             raise RuntimeError(f"orc_eigen_solve failed ({k})")
         return ev[:k], fr[:k], vecs[:k], dm
+
+    def newmark_adjoint(self, n_steps, dt, beta, gamma, f_shape, amp, obj_dof, obj_w):
+        """Transient adjoint (construct with dynamic=True): L = sum over steps of
+        sum_k w_k u_n[dof_k] and dL/dE per element."""
+        f_shape = np.ascontiguousarray(f_shape, np.float64)
+        amp = np.ascontiguousarray(amp, np.float64)
+        dof = np.ascontiguousarray(obj_dof, np.int32)
+        w = np.ascontiguousarray(obj_w, np.float64)
+        L = C.c_double(0.0)
+        g = np.zeros(self.p.mesh.n_elems)
+        rc = self.lib.orc_newmark_adjoint(self.m, n_steps, dt, beta, gamma, _p(f_shape), _p(amp), len(dof),
+                                          _p(dof, C.c_int32), _p(w), C.byref(L), _p(g))
+        if rc != 0:
+            raise RuntimeError(f"orc_newmark_adjoint failed ({rc})")
+        return L.value, g
 
     def reorder(self, block_dim=0):
         out = np.zeros(self.n_dof // 3, np.int32)
