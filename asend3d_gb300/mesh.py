@@ -112,6 +112,29 @@ def block_tet4(nx: int, ny: int, nz: int, lx: float, ly: float, lz: float) -> Bl
     return BlockMesh(nx, ny, nz, lx, ly, lz, hexm.coords, tets.astype(np.int32), elem_type=4)
 
 
+def block_tet10(nx: int, ny: int, nz: int, lx: float, ly: float, lz: float) -> BlockMesh:
+    """block_tet4 with a node added at the middle of every edge: quadratic
+    tets (type 10) with the reference's node order, corners 0-3 then the
+    edges 0-1, 1-2, 0-2, 0-3, 1-3, 2-3 (element_soln_fields.rs:229-298)."""
+    t4 = block_tet4(nx, ny, nz, lx, ly, lz)
+    coords = list(map(tuple, t4.coords))
+    edge_node: dict = {}
+    pairs = ((0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3))
+    conn = []
+    for tet in t4.conn:
+        row = [int(v) for v in tet]
+        for i, j in pairs:
+            a, b = int(tet[i]), int(tet[j])
+            key = (min(a, b), max(a, b))
+            if key not in edge_node:
+                edge_node[key] = len(coords)
+                coords.append(tuple(0.5 * (t4.coords[a] + t4.coords[b])))
+            row.append(edge_node[key])
+        conn.append(row)
+    return BlockMesh(nx, ny, nz, lx, ly, lz, np.array(coords, dtype=np.float64), np.array(conn, dtype=np.int32),
+                     elem_type=10)
+
+
 def ar1_field(shape, spacing, corr_len, rng: np.random.Generator) -> np.ndarray:
     """Standard Gaussian field on a grid with separable exponential correlation
     exp(-|dx|/l - |dy|/l - |dz|/l), generated exactly by AR(1) recursions along

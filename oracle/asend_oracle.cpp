@@ -23,13 +23,16 @@ constexpr double kTol = 1e-12;                 // constants.rs:13 (TOL)
 constexpr double kR1ORt3 = 0.5773502691896257; // constants.rs:3
 constexpr double kR1O6 = 0.16666666666666666;  // constants.rs:6
 constexpr double kPi = 3.14159265358979323846;
+constexpr double kRTet1 = 0.1381966011250071;  // constants.rs:10 (R_TET1)
+constexpr double kRTet2 = 0.585410196624929;   // constants.rs:11 (R_TET2)
+constexpr double kR1O24 = 0.041666666666666664; // constants.rs:7 (R_1O24)
 
 // ---------------------------------------------------------------------------
 // Element type tables: element_meth.rs:74-448 (initialize_type)
 // ---------------------------------------------------------------------------
 struct TypeInfo {
     int type = 0, nn = 0, dpn = 3, nip = 0, nfaces = 0;
-    double ip[8 * 3] = {};
+    double ip[8 * 3] = {};  // at most 8 points (hex8); tet10 uses 4
     double wt[8] = {};
     int faces[6][4] = {};
     int face_nn = 0;
@@ -66,6 +69,17 @@ TypeInfo type_info(int type) {
         // pseudo-node 2a, its rotations 2a+1, so DOF 6a + c keeps the
         // reference's node-major numbering (element_meth.rs:424-431)
         t.nn = 8; t.dpn = 3; t.nip = 4; t.nfaces = 0; t.face_nn = 0;
+    } else if (type == 10) {
+        // tet10: 4 points (R_TET1 x3 with R_TET2 in turn on each axis after
+        // the first), weights 1/24 (element_meth.rs:228-262); face loads are
+        // not restated for it
+        t.nn = 10; t.dpn = 3; t.nip = 4; t.nfaces = 0; t.face_nn = 0;
+        const double pts[4][3] = {{kRTet1, kRTet1, kRTet1}, {kRTet2, kRTet1, kRTet1},
+                                  {kRTet1, kRTet2, kRTet1}, {kRTet1, kRTet1, kRTet2}};
+        for (int k = 0; k < 4; ++k) {
+            for (int j = 0; j < 3; ++j) t.ip[3 * k + j] = pts[k][j];
+            t.wt[k] = kR1O24;
+        }
     } else if (type == 4) {
         // tet4: one point at (1/4,1/4,1/4), weight 1/6 (element_meth.rs:84-101)
         t.nn = 4; t.dpn = 3; t.nip = 1; t.nfaces = 4; t.face_nn = 3;
@@ -97,6 +111,30 @@ void shape(int type, const double* s, double* n, double* dn) {
         n[1] = s[0]; n[2] = s[1]; n[3] = s[2];
         const double d[12] = {-1, -1, -1, 1, 0, 0, 0, 1, 0, 0, 0, 1};
         std::memcpy(dn, d, sizeof(d));
+    } else if (type == 10) {
+        // quadratic tetrahedron (element_soln_fields.rs:229-298): corners
+        // 0..3, mid-edge nodes 4 (0-1), 5 (1-2), 6 (0-2), 7 (0-3), 8 (1-3), 9 (2-3)
+        const double p1 = 1.0 - s[0] - s[1] - s[2], p2 = p1 - 0.5;
+        n[0] = 2.0 * p1 * p2;
+        dn[0] = dn[1] = dn[2] = 2.0 * (-p2 - p1);
+        for (int k = 0; k < 3; ++k) {
+            n[1 + k] = -2.0 * s[k] * (0.5 - s[k]);
+            for (int j = 0; j < 3; ++j) dn[3 * (1 + k) + j] = (j == k) ? -2.0 * (0.5 - 2.0 * s[k]) : 0.0;
+        }
+        // mid-edge node on the edge (0, k): 4 s_k p1
+        const int m0[3] = {4, 6, 7};
+        for (int k = 0; k < 3; ++k) {
+            const int a = m0[k];
+            n[a] = 4.0 * s[k] * p1;
+            for (int j = 0; j < 3; ++j) dn[3 * a + j] = (j == k) ? 4.0 * (p1 - s[k]) : -4.0 * s[k];
+        }
+        // mid-edge node on the edge (i, j) of corners 1..3: 4 s_i s_j
+        const int mm[3][3] = {{5, 0, 1}, {8, 0, 2}, {9, 1, 2}};
+        for (const auto& e : mm) {
+            const int a = e[0], i = e[1], j = e[2];
+            n[a] = 4.0 * s[i] * s[j];
+            for (int q = 0; q < 3; ++q) dn[3 * a + q] = (q == i) ? 4.0 * s[j] : (q == j ? 4.0 * s[i] : 0.0);
+        }
     }
 }
 
@@ -157,7 +195,7 @@ double det_inv(double* inv, const double* mat_in, int n) {
 // Integration point data: element_soln_fields.rs:383-463 (solid branch).
 // xyz[3*nn] node-major.  Returns detJ; dndx[3*a + j] = dN_a/dx_j.
 double ip_data(int type, int nn, const double* xyz, const double* s, double* n, double* dndx) {
-    double dn[24];
+    double dn[30];
     shape(type, s, n, dn);
     double J[9] = {0};
     for (int i = 0; i < 3; ++i)
@@ -244,7 +282,7 @@ void solid_ke(int type, const double* xyz, const double* C, double* ke) {
     const TypeInfo t = type_info(type);
     const int nn = t.nn, tot = 3 * nn;
     std::fill(ke, ke + tot * tot, 0.0);
-    double n[8], dndx[24], B[6 * 24], CB[6 * 24];
+    double n[10], dndx[30], B[6 * 30], CB[6 * 30];
     for (int p = 0; p < t.nip; ++p) {
         const double det = ip_data(type, nn, xyz, t.ip + 3 * p, n, dndx);
         const double djw = det * t.wt[p];
@@ -343,7 +381,7 @@ void solid_me(int type, const double* xyz, double rho, double* me) {
     const TypeInfo t = type_info(type);
     const int nn = t.nn, tot = 3 * nn;
     std::fill(me, me + tot * tot, 0.0);
-    double n[8], dndx[24];
+    double n[10], dndx[30];
     for (int p = 0; p < t.nip; ++p) {
         const double det = ip_data(type, nn, xyz, t.ip + 3 * p, n, dndx);
         const double djw = det * t.wt[p];
@@ -571,7 +609,7 @@ void elem_km(const orc_model* m, int e, double* ke, double* me) {
         shell_km(xyz, m->E[e], m->nu[e], m->rho[e], m->thk[e], ke, me);
         return;
     }
-    double xyz[24], C[36];
+    double xyz[30], C[36];
     elem_xyz(m, e, xyz);
     iso_cmat(m->E[e], m->nu[e], C);
     solid_ke(m->ti.type, xyz, C, ke);
@@ -1123,7 +1161,7 @@ extern "C" {
 orc_model* orc_create(int32_t elem_type, int32_t n_nodes, const double* coords, int32_t n_elems,
                       const int32_t* conn, const double* E, const double* nu, const double* rho,
                       const double* thickness) {
-    if (elem_type != 8 && elem_type != 81 && elem_type != 4 && elem_type != 41) return nullptr;
+    if (elem_type != 8 && elem_type != 81 && elem_type != 4 && elem_type != 10 && elem_type != 41) return nullptr;
     auto* m = new orc_model();
     m->ti = type_info(elem_type);
     m->n_el = n_elems;
@@ -1248,7 +1286,7 @@ int orc_element_stiffness(int32_t elem_type, const double* xyz, double E, double
         shell_km(xyz, E, nu, 0.0, thickness, ke, nullptr);
         return 0;
     }
-    if (elem_type != 8 && elem_type != 81 && elem_type != 4) return -1;
+    if (elem_type != 8 && elem_type != 81 && elem_type != 4 && elem_type != 10) return -1;
     double C[36];
     iso_cmat(E, nu, C);
     solid_ke(elem_type, xyz, C, ke);
@@ -1264,7 +1302,7 @@ int orc_element_mass(int32_t elem_type, const double* xyz, double rho, double th
         shell_km(xyz, 1.0, 0.3, rho, thickness, ke.data(), me);
         return 0;
     }
-    if (elem_type != 8 && elem_type != 81 && elem_type != 4) return -1;
+    if (elem_type != 8 && elem_type != 81 && elem_type != 4 && elem_type != 10) return -1;
     solid_me(elem_type, xyz, rho, me);
     return 0;
 }
@@ -1280,7 +1318,7 @@ int orc_element_mass(int32_t elem_type, const double* xyz, double rho, double th
 int orc_surface_traction(const orc_model* m, int32_t n_set, const int32_t* elem_set,
                          const double* norm_dir, double norm_tol_deg, const double* traction,
                          double* f) {
-    if (m->shell) return -1;  // solid faces only
+    if (m->shell || m->ti.nfaces == 0) return -1;  // solid element faces only (none restated for tet10)
     const TypeInfo& t = m->ti;
     const int nn = t.nn, tot = 3 * nn;
     // face multiplicity over the whole mesh
@@ -1442,7 +1480,7 @@ int orc_adjoint_modulus_component_gradient(orc_model* m, const double* u, const 
     const int k = component - 1;
     const TypeInfo& t = m->ti;
     const int nn = t.nn, tot = 3 * nn;
-    double xyz[24], C[36], dS[36], tmp[36], dC[36], n[8], dndx[24], B[6 * 24];
+    double xyz[30], C[36], dS[36], tmp[36], dC[36], n[10], dndx[30], B[6 * 30];
     for (int e = 0; e < m->n_el; ++e) {
         elem_xyz(m, e, xyz);
         const double E = m->E[e], nu = m->nu[e];
