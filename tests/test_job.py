@@ -214,3 +214,40 @@ def test_cg_log_lines(capsys):
     out = capsys.readouterr().out.splitlines()
     assert out == ["Total CG iterations: 25", "Final residual norm: 3.5e-09"]
     assert int(out[0].split(":")[1]) == 25
+
+
+def write_shell_job(d: Path, nx=3, ny=2, t=0.004, z_offset=0.0, layers=1):
+    from asend3d_gb300.mesh import plate_quad4
+    m = plate_quad4(nx, ny, 0.6, 0.4)
+    lines = ["nodes:"] + [f"- [{i}, {float(x)!r}, {float(y)!r}, {float(z)!r}]" for i, (x, y, z) in enumerate(m.coords)]
+    lines += ["elements:", "- type: shell4", "  connectivity:"]
+    lines += ["  - [" + ", ".join(str(v) for v in [e, *row]) + "]" for e, row in enumerate(m.conn)]
+    lines += ["sets:", "  node:", "    edge:"] + [f"    - {v}" for v in m.nodes_in_range(xr=(-1e-9, 1e-9))]
+    lines += ["  element:", "    all:", f"    - [0, {m.n_elems}]"]
+    lines += ["sections:", "- type: shell", "  layup:", f"    zOffset: {z_offset}", "    layers:"]
+    for _ in range(layers):
+        lines += ["    - material: al", f"      thickness: {t}", "      angle: 0.0"]
+    lines += ["  elementSet: all", "materials:", "  al:", "    density: 2700.0", "    elastic:",
+              "      E: 70000000000.0", "      nu: 0.33"]
+    (d / "model.yaml").write_text("\n".join(lines) + "\n")
+    (d / "job.yaml").write_text("jobCommands:\n- command: readModelInput\n  fileName: model.yaml\n")
+    return m
+
+
+def test_shell_job_problem(tmp_path):
+    m = write_shell_job(tmp_path)
+    r = J.JobRunner(tmp_path / "job.yaml")
+    r.cmd_readModelInput(r.cmds[0])
+    assert r.model.sections[0]["layers"] == [{"material": "al", "thickness": 0.004, "angle": 0.0}]
+    p = r._problem()
+    assert p.mesh.elem_type == 41 and p.mesh.dpn == 6
+    np.testing.assert_array_equal(p.thickness, np.full(m.n_elems, 0.004))
+    assert np.all(p.E == 70e9) and np.all(p.rho == 2700.0)
+    for kw, msg in ((dict(layers=2), "one centred layer"), (dict(z_offset=0.001), "one centred layer")):
+        d = tmp_path / f"bad{len(msg)}{kw.get('layers', 1)}"
+        d.mkdir()
+        write_shell_job(d, **kw)
+        rb = J.JobRunner(d / "job.yaml")
+        rb.cmd_readModelInput(rb.cmds[0])
+        with pytest.raises(NotImplementedError, match=msg):
+            rb._problem()

@@ -56,3 +56,13 @@ def test_cli_errors(cli, tmp_path):
     assert out.returncode == 1 and "job command buildMesh is not on the GPU path" in out.stderr
     out = subprocess.run([cli], capture_output=True, text=True)
     assert out.returncode == 2 and "usage" in out.stderr
+
+
+def test_parse_shell_model(cli, tmp_path):
+    from test_job import write_shell_job
+    m = write_shell_job(tmp_path)
+    out = subprocess.run([cli, "--parse", str(tmp_path / "job.yaml")], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    j = json.loads(out.stdout)
+    assert j["elem_type"] == 41 and len(j["conn"]) == m.n_elems and all(len(r) == 4 for r in j["conn"])
+    assert j["elem_sets"]["all"] == list(range(m.n_elems))
