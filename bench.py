@@ -28,6 +28,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -382,7 +383,8 @@ def ncu_traffic():
 class ClockSampler:
     def __init__(self, gpu_index: int):
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+        # raw samples (the JSON line carries their summary); ASEND_CLOCK_DIR keeps them
+        self.path = Path(os.environ.get("ASEND_CLOCK_DIR", tempfile.gettempdir())) / f"clocks_bench_{os.getpid()}.csv"
         self.gpu = gpu_index
 
     def __enter__(self):
@@ -620,7 +622,7 @@ def run_ours(a):
     # restore the benchmark load for the remaining measurements
     g.set_loads()
 
-    # ---- plain FP64 Jacobi PCG on the same GPU (the spec comparison)
+    # ---- plain FP64 Jacobi PCG on the same GPU (the method the speed-up is measured against)
     plain = dict(method=_lib.METHOD_FP64, precond=_lib.PC_JACOBI, rel_tol=1e-8, graph_iters=32)
     g.assemble(precision=64)
     g.static_solve_device(**plain)
