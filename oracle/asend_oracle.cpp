@@ -307,45 +307,61 @@ void solid_ke(int type, const double* xyz, const double* C, double* ke) {
 // element_meth.rs:192-201), whose derivatives at the point use the centroid
 // Jacobian (element_soln_fields.rs:424-461); the 9 internal DOF are condensed
 // (element_equations.rs:19-57).
-void brickim_ke(const double* xyz, const double* C, double* ke) {
-    constexpr int tot = 33, nd = 24;
-    const TypeInfo t = type_info(8);
-    double n0[8], dn0[24], J0[9] = {0}, Ji0[9];
+// Inverse Jacobian at the element centroid (the bubbles' derivatives use it).
+void brickim_centroid_jinv(const double* xyz, double* Ji0) {
+    double n0[8], dn0[24], J0[9] = {0};
     const double s0[3] = {0.0, 0.0, 0.0};
     shape(8, s0, n0, dn0);
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
             for (int a = 0; a < 8; ++a) J0[3 * i + j] += xyz[3 * a + i] * dn0[3 * a + j];
     det_inv(Ji0, J0, 3);
-    std::vector<double> K(tot * tot, 0.0), B(6 * tot), CB(6 * tot);
+}
+
+// B (6 x 33: the 24 node DOF, then bubble f = 0..2 x component d) at Gauss
+// point p; returns w detJ.
+double brickim_bmat(const double* xyz, const double* Ji0, int p, double* B) {
+    constexpr int tot = 33, nd = 24;
+    const TypeInfo t = type_info(8);
     double n[8], dndx[24], B24[6 * 24];
-    for (int p = 0; p < t.nip; ++p) {
-        const double* sp = t.ip + 3 * p;
-        const double det = ip_data(8, 8, xyz, sp, n, dndx);
-        const double djw = det * t.wt[p];
-        solid_bmat(8, dndx, B24);
-        std::fill(B.begin(), B.end(), 0.0);
-        for (int k = 0; k < 6; ++k)
-            for (int c = 0; c < nd; ++c) B[k * tot + c] = B24[k * 24 + c];
-        for (int f = 0; f < 3; ++f) {  // bubble f: d/ds_f = -2 s_f
-            double g[3];
-            for (int j = 0; j < 3; ++j) g[j] = -2.0 * sp[f] * Ji0[3 * f + j];
-            for (int d = 0; d < 3; ++d) {
-                const int col = nd + 3 * f + d;
-                double sm[9] = {0};
-                for (int i = 0; i < 3; ++i)
-                    for (int j = i; j < 3; ++j) {
-                        if (i == d) sm[3 * i + j] += g[j];
-                        if (j == d) sm[3 * i + j] += g[i];
-                    }
-                B[0 * tot + col] = 0.5 * sm[0];
-                B[1 * tot + col] = 0.5 * sm[4];
-                B[2 * tot + col] = 0.5 * sm[8];
-                B[3 * tot + col] = sm[1];
-                B[4 * tot + col] = sm[2];
-                B[5 * tot + col] = sm[5];
-            }
+    const double* sp = t.ip + 3 * p;
+    const double det = ip_data(8, 8, xyz, sp, n, dndx);
+    solid_bmat(8, dndx, B24);
+    std::fill(B, B + 6 * tot, 0.0);
+    for (int k = 0; k < 6; ++k)
+        for (int c = 0; c < nd; ++c) B[k * tot + c] = B24[k * 24 + c];
+    for (int f = 0; f < 3; ++f) {  // bubble f: d/ds_f = -2 s_f
+        double g[3];
+        for (int j = 0; j < 3; ++j) g[j] = -2.0 * sp[f] * Ji0[3 * f + j];
+        for (int d = 0; d < 3; ++d) {
+            const int col = nd + 3 * f + d;
+            double sm[9] = {0};
+            for (int i = 0; i < 3; ++i)
+                for (int j = i; j < 3; ++j) {
+                    if (i == d) sm[3 * i + j] += g[j];
+                    if (j == d) sm[3 * i + j] += g[i];
+                }
+            B[0 * tot + col] = 0.5 * sm[0];
+            B[1 * tot + col] = 0.5 * sm[4];
+            B[2 * tot + col] = 0.5 * sm[8];
+            B[3 * tot + col] = sm[1];
+            B[4 * tot + col] = sm[2];
+            B[5 * tot + col] = sm[5];
         }
+    }
+    return det * t.wt[p];
+}
+
+// Full 33 x 33 brickIM stiffness before condensation.
+void brickim_kfull(const double* xyz, const double* C, double* K) {
+    constexpr int tot = 33;
+    const TypeInfo t = type_info(8);
+    double Ji0[9];
+    brickim_centroid_jinv(xyz, Ji0);
+    std::fill(K, K + tot * tot, 0.0);
+    std::vector<double> B(6 * tot), CB(6 * tot);
+    for (int p = 0; p < t.nip; ++p) {
+        const double djw = brickim_bmat(xyz, Ji0, p, B.data());
         for (int k = 0; k < 6; ++k)
             for (int c = 0; c < tot; ++c) {
                 double acc = 0.0;
@@ -359,6 +375,12 @@ void brickim_ke(const double* xyz, const double* C, double* ke) {
                 K[i * tot + j] += acc;
             }
     }
+}
+
+void brickim_ke(const double* xyz, const double* C, double* ke) {
+    constexpr int tot = 33, nd = 24;
+    std::vector<double> K(tot * tot);
+    brickim_kfull(xyz, C, K.data());
     double Kii[81];
     for (int i = 0; i < 9; ++i)
         for (int j = 0; j < 9; ++j) Kii[9 * i + j] = K[(nd + i) * tot + nd + j];
@@ -1726,6 +1748,86 @@ int orc_newmark_adjoint(orc_model* m, int32_t n_steps, double dt, double beta, d
             }
             gE[e] -= acc / m->E[e];
         }
+    }
+    return 0;
+}
+
+
+// Strain-pair tensors of an adjoint pair (u, lambda): per element
+// P_e = sum_gp w detJ eps(lambda_e) eps(u_e)^T (Voigt 11,22,33,12,13,23,
+// engineering shear), so that lambda_e^T dR_e/dD = sum_ij (dC/dD)_ij P_e[i][j]
+// for any material derivative of a solid element (d_relasticd_d,
+// model_analysis.rs:1379-1457, with C constant over the element).  brickIM:
+// the strains include the condensed modes, recovered as
+// x_i = -K_ii^-1 K_ie x_e for both fields (update_internal,
+// element_equations.rs:147-194), since d(K_ee - K_ei K_ii^-1 K_ie)/dD
+// contracted with (lambda_e, u_e) equals the full dK/dD contracted with the
+// recovered (lambda, u).  Solid types (8, 81, 4, 10); P[n_el][36].
+int orc_adjoint_strain_pairs(const orc_model* m, const double* u, const double* lam, double* P) {
+    if (!m->assembled || m->shell) return -1;
+    const TypeInfo& t = m->ti;
+    const int nn = t.nn;
+    for (int e = 0; e < m->n_el; ++e) {
+        double xyz[30];
+        elem_xyz(m, e, xyz);
+        double acc[36] = {0};
+        if (t.type == 81) {
+            constexpr int tot = 33, nd = 24;
+            double C[36];
+            iso_cmat(m->E[e], m->nu[e], C);
+            std::vector<double> K(tot * tot), B(6 * tot);
+            brickim_kfull(xyz, C, K.data());
+            double Kii[81];
+            for (int i = 0; i < 9; ++i)
+                for (int j = 0; j < 9; ++j) Kii[9 * i + j] = K[(nd + i) * tot + nd + j];
+            givens_factor(Kii, 9);
+            double uf[tot], lf[tot];
+            for (int c = 0; c < nd; ++c) {
+                const int g = m->conn[(size_t)e * nn + c / 3] * 3 + c % 3;
+                uf[c] = u[g];
+                lf[c] = lam[g];
+            }
+            for (double* f : {uf, lf}) {
+                double rhs[9], x[9];
+                for (int i = 0; i < 9; ++i) {
+                    double a = 0.0;
+                    for (int c = 0; c < nd; ++c) a += K[(nd + i) * tot + c] * f[c];
+                    rhs[i] = a;
+                }
+                givens_solve(x, Kii, rhs, 9);
+                for (int i = 0; i < 9; ++i) f[nd + i] = -x[i];
+            }
+            double Ji0[9];
+            brickim_centroid_jinv(xyz, Ji0);
+            for (int p = 0; p < t.nip; ++p) {
+                const double djw = brickim_bmat(xyz, Ji0, p, B.data());
+                double eu[6] = {0}, el[6] = {0};
+                for (int q = 0; q < 6; ++q)
+                    for (int c = 0; c < tot; ++c) {
+                        eu[q] += B[q * tot + c] * uf[c];
+                        el[q] += B[q * tot + c] * lf[c];
+                    }
+                for (int i = 0; i < 6; ++i)
+                    for (int j = 0; j < 6; ++j) acc[6 * i + j] += el[i] * eu[j] * djw;
+            }
+        } else {
+            const int tot = 3 * nn;
+            double n[10], dndx[30], B[6 * 30];
+            for (int p = 0; p < t.nip; ++p) {
+                const double djw = ip_data(t.type, nn, xyz, t.ip + 3 * p, n, dndx) * t.wt[p];
+                solid_bmat(nn, dndx, B);
+                double eu[6] = {0}, el[6] = {0};
+                for (int q = 0; q < 6; ++q)
+                    for (int c = 0; c < tot; ++c) {
+                        const int g = m->conn[(size_t)e * nn + c / 3] * 3 + c % 3;
+                        eu[q] += B[q * tot + c] * u[g];
+                        el[q] += B[q * tot + c] * lam[g];
+                    }
+                for (int i = 0; i < 6; ++i)
+                    for (int j = 0; j < 6; ++j) acc[6 * i + j] += el[i] * eu[j] * djw;
+            }
+        }
+        std::copy(acc, acc + 36, P + (size_t)e * 36);
     }
     return 0;
 }

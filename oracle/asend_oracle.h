@@ -119,6 +119,10 @@ int orc_newmark_adjoint(orc_model* m, int32_t n_steps, double dt, double beta, d
                         const double* f_shape, const double* amp, int32_t n_obj, const int32_t* obj_dof,
                         const double* obj_w, double* L_out, double* gE);
 
+/* Strain-pair tensors P[n_el][36] = sum_gp w detJ eps(lambda_e) eps(u_e)^T of
+ * solid elements (brickIM with its condensed modes recovered). */
+int orc_adjoint_strain_pairs(const orc_model* m, const double* u, const double* lam, double* P);
+
 int orc_reorder_nodes(const orc_model* m, int32_t block_dim, int32_t* order_out);
 
 #ifdef __cplusplus

@@ -64,6 +64,7 @@ def load():
                                           C.c_int32, P_d, C.c_int32, C.c_int32, C.c_double, C.c_int32, P_d, P_i]),
             "orc_reorder_nodes": (C.c_int, [C.c_void_p, C.c_int32, P_i]),
             "orc_eigen_solve": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, P_d, P_d, P_d, P_d]),
+            "orc_adjoint_strain_pairs": (C.c_int, [C.c_void_p, P_d, P_d, P_d]),
             "orc_newmark_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double, P_d, P_d,
                                               C.c_int32, P_i, P_d, P_d, P_d]),
         }
@@ -225,6 +226,16 @@ class Oracle:
         if k < 0:
             raise RuntimeError(f"orc_eigen_solve failed ({k})")
         return ev[:k], fr[:k], vecs[:k], dm
+
+    def strain_pairs(self, u, lam):
+        """[n_el, 6, 6] strain-pair tensors of (u, lambda) (solid elements)."""
+        u = np.ascontiguousarray(u, np.float64)
+        lam = np.ascontiguousarray(lam, np.float64)
+        P = np.zeros((self.p.mesh.n_elems, 6, 6))
+        rc = self.lib.orc_adjoint_strain_pairs(self.m, _p(u), _p(lam), _p(P))
+        if rc != 0:
+            raise RuntimeError(f"orc_adjoint_strain_pairs failed ({rc})")
+        return P
 
     def newmark_adjoint(self, n_steps, dt, beta, gamma, f_shape, amp, obj_dof, obj_w):
         """Transient adjoint (construct with dynamic=True): L = sum over steps of
