@@ -4,6 +4,7 @@ import re
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
 
@@ -81,3 +82,30 @@ def test_constraint_rows_semantics():
     assert len(rhs) == 4
     assert list(dof[ptr[0]:ptr[1]]) == [1, 16]
     assert list(coef[ptr[3]:ptr[4]]) == [1.0, -1.0]
+
+
+def test_header_is_plain_c(gpu_lib, tmp_path):
+    """include/asend_gpu.h compiles as strict C99 and a C program links and
+    runs against the library (no device call): the boundary is a C ABI."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    root = Path(__file__).resolve().parents[1]
+    src = tmp_path / "abi.c"
+    src.write_text('#include "asend_gpu.h"\n#include <string.h>\n'
+                   "int main(void) { asend_solve_opts o; asend_eigen_opts e; memset(&o, 0, sizeof o);\n"
+                   "  memset(&e, 0, sizeof e); e.inner = o; return asend_version() ? 0 : 1; }\n")
+    from asend3d_gb300 import build
+    cuda_lib = Path(build.nvcc()).resolve().parent.parent / "lib64"
+    exe = tmp_path / "abi"
+    cmd = [gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", f"-I{root / 'include'}", str(src),
+           f"-L{root / 'asend3d_gb300'}", "-lasend_gpu", f"-L{cuda_lib}", f"-Wl,-rpath-link,{cuda_lib}",
+           f"-Wl,-rpath,{root / 'asend3d_gb300'}", "-o", str(exe)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert run.returncode == 0, run.stderr
