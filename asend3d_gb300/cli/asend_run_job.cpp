@@ -543,6 +543,11 @@ struct Runner {
         for (const char* k : {"thermal", "diffusion", "fluid", "nonlinearGeom"})
             if (solve_kv.count(k) && solve_kv[k].find("yes") != std::string::npos)
                 throw Fail(std::string(k) + " analysis is not on the GPU path");
+        // element_equations.rs:950-971; the GPU path uses the consistent mass
+        if (solve_kv.count("lumpMass") && solve_kv["lumpMass"].find("yes") != std::string::npos)
+            throw Fail("lumped-mass dynamics is not on the GPU path");
+        if (solve_kv.count("userUpdate") && solve_kv["userUpdate"].find("yes") != std::string::npos)
+            throw Fail("user update hooks are not on the GPU path");
         if (ctx) { asend_destroy(ctx); ctx = nullptr; }
         setup();
         const asend_solve_opts o = opts(false);

@@ -509,6 +509,10 @@ class JobRunner:
         for k in ("thermal", "diffusion", "fluid", "nonlinearGeom"):
             if cmd.get(k):
                 raise NotImplementedError(f"{k} analysis is not on the GPU path")
+        if cmd.get("lumpMass"):  # element_equations.rs:950-971; the GPU path uses the consistent mass
+            raise NotImplementedError("lumped-mass dynamics is not on the GPU path")
+        if cmd.get("userUpdate"):
+            raise NotImplementedError("user update hooks are not on the GPU path")
         g = self._solver()
         dpn = self.problem.mesh.dpn
         n = self.problem.mesh.n_nodes
