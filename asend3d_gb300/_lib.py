@@ -19,7 +19,7 @@ P_flt = C.POINTER(C.c_float)
 
 ASEND_OK, ASEND_MAX_ITER, ASEND_NONFINITE, ASEND_FALLBACK = 0, 1, 2, 3
 ASEND_EINVAL, ASEND_ECUDA, ASEND_ESTATE = -1, -2, -3
-METHOD_FP64, METHOD_MIXED = 0, 1
+METHOD_FP64, METHOD_MIXED, METHOD_SPLIT = 0, 1, 2
 PC_JACOBI, PC_BLOCK, PC_LEARNED, PC_MG, PC_MG_LEARNED = 0, 1, 2, 3, 4
 OBJ_DISPLACEMENT, OBJ_COMPLIANCE = 0, 1
 LEARN_BLOCK, LEARN_MG = 0, 1
@@ -68,6 +68,7 @@ SIGNATURES = [
     ("asend_mg_level_info", c_int, [C.c_void_p, c_int, P_int, P_dbl, P_dbl, P_dbl]),
     ("asend_mg_vcycle", c_int, [C.c_void_p, P_flt, P_flt]),
     ("asend_set_instances", c_int, [C.c_void_p, c_int, P_int]),
+    ("asend_set_instance_blocks", c_int, [C.c_void_p, c_int, P_int]),
     ("asend_add_node_set", c_int, [C.c_void_p, c_int, P_int]),
     ("asend_add_element_set", c_int, [C.c_void_p, c_int, P_int]),
     ("asend_add_constraint", c_int, [C.c_void_p, c_int, P_int, P_int, P_dbl, c_dbl]),
@@ -101,6 +102,7 @@ SIGNATURES = [
     ("asend_adjoint_strain_pairs", c_int, [C.c_void_p, P_dbl]),
     ("asend_material_dv_gradient", c_int, [C.c_void_p, c_int, c_int, c_int, c_int, P_dbl, P_dbl]),
     ("asend_material_dC", c_int, [c_int, c_int, c_dbl, c_dbl, P_dbl]),
+    ("asend_time_mg_kernel", c_int, [C.c_void_p, c_int, c_int, c_int, P_dbl, P_dbl]),
     ("asend_operator_energy_noalloc", c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("asend_learned_n_params", c_int, []),
     ("asend_learned_init", c_int, [C.c_void_p, C.c_uint64]),

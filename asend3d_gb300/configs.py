@@ -62,14 +62,23 @@ def block_large(nx=200, ny=40, nz=40, median=70e9, sigma_log=0.3, corr=0.1, nu=0
     return p
 
 
-def batch_instance(k: int, seed: int = 7, median=70e9, sigma_log=0.3, corr=0.1, nu=0.33) -> Problem:
-    """Instance k of the 64-instance sweep with its 4 load cases."""
+def _batch_draw(k: int, seed: int):
     rng = np.random.default_rng([seed, k])
     nx = int(rng.integers(20, 121))
     ny = int(rng.integers(4, 17))
-    nz = ny
+    return nx, ny, ny, int(rng.integers(1 << 30))
+
+
+def batch_dims(k: int, seed: int = 7):
+    """(nx, ny, nz) of instance k of the sweep, without building it."""
+    return _batch_draw(k, seed)[:3]
+
+
+def batch_instance(k: int, seed: int = 7, median=70e9, sigma_log=0.3, corr=0.1, nu=0.33) -> Problem:
+    """Instance k of the 64-instance sweep with its 4 load cases."""
+    nx, ny, nz, field_seed = _batch_draw(k, seed)
     m = block_hex8(nx, ny, nz, *BAR)
-    E = lognormal_modulus(m, median, sigma_log, corr, int(rng.integers(1 << 30)))
+    E = lognormal_modulus(m, median, sigma_log, corr, field_seed)
     p = Problem(m, E, np.full(m.n_elems, nu), np.full(m.n_elems, 2700.0))
     _fixed_end(p, m)
     end = m.nodes_in_range(xr=(BAR[0] - 1e-9, BAR[0] + 1e-9))
@@ -118,13 +127,15 @@ def learned_patch(nx=32, ny=16, nz=16, full=(128, 64, 64), seed=0, median=70e9, 
     return p
 
 
-def batch_uq(n_inst: int = 64, seed: int = 7):
+def batch_uq(n_inst: int = 64, seed: int = 7, which=None):
     """The batched UQ / design sweep: n_inst uneven cantilevers, 4 load cases
-    each, combined into one stacked problem.  Returns (problem, node_ptr,
-    elem_ptr, instances)."""
+    each, combined into one stacked problem (``which``: a subset of instance
+    indices).  Returns (problem, node_ptr, elem_ptr, instances); the
+    instances' structured blocks are ``[(p.mesh.nx, p.mesh.ny, p.mesh.nz)]``."""
     from .solver import combine
 
-    inst = [batch_instance(k, seed=seed) for k in range(n_inst)]
+    ks = range(n_inst) if which is None else which
+    inst = [batch_instance(k, seed=seed) for k in ks]
     prob, node_ptr, elem_ptr = combine(inst)
     return prob, node_ptr, elem_ptr, inst
 

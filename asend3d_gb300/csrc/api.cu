@@ -296,6 +296,7 @@ void build_pattern(Ctx& c) {
     c.pen_dof = pen_dof;
     c.pen_coef_host = pen_coef;
     ASEND_CUDA(cudaStreamSynchronize(s));
+    build_classes(c, slot_map);
     c.pattern_ready = true;
 }
 
@@ -485,6 +486,7 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         learned_mesh_changed(c);
         c.n_inst = 0;
         c.inst_node_ptr.clear();
+        c.inst_dims.clear();
         c.d_xyz.upload(c.xyz, c.stream);
         c.d_conn.upload(c.conn, c.stream);
         c.d_E.upload(c.E, c.stream);
@@ -560,10 +562,50 @@ int asend_set_instances(asend_ctx* ctx, int32_t n_inst, const int32_t* node_ptr)
         }
         c.n_inst = n_inst;
         c.inst_node_ptr.assign(node_ptr, node_ptr + n_inst + 1);
+        c.inst_dims.clear();
+        c.mg.reset();
         c.d_cta_inst.upload(cta_inst, c.stream);
         c.d_inst_cta0.upload(cta0, c.stream);
         c.d_inst_ncta.upload(ncta, c.stream);
         ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        return ASEND_OK;
+    });
+}
+
+// Declares every instance of a batched stack a structured block in the
+// numbering of asend_set_block_structure, relative to the instance's first
+// node: instance i's elements are the next nx*ny*nz elements (instances in
+// order).  Enables ASEND_PC_MG on the whole stack: one V-cycle over every
+// instance's hierarchy at once.
+int asend_set_instance_blocks(asend_ctx* ctx, int32_t n_inst, const int32_t* dims) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.type == 8 || c.type == 81, "instance blocks need a hex8 / brickIM mesh");
+        require(c.n_inst >= 1 && n_inst == c.n_inst && dims, "declare the instances first (asend_set_instances)");
+        const int co[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+        int64_t el0 = 0;
+        for (int q = 0; q < n_inst; ++q) {
+            const int nx = dims[3 * q], ny = dims[3 * q + 1], nz = dims[3 * q + 2];
+            require(nx > 0 && ny > 0 && nz > 0, "block dimensions must be positive");
+            const int node0 = c.inst_node_ptr[q];
+            require((int64_t)(nx + 1) * (ny + 1) * (nz + 1) <= (int64_t)c.inst_node_ptr[q + 1] - node0,
+                    "block does not fit the instance's nodes");
+            require(el0 + (int64_t)nx * ny * nz <= c.n_el, "block dimensions exceed the element count");
+            for (int i = 0; i < nx; ++i)
+                for (int j = 0; j < ny; ++j)
+                    for (int k = 0; k < nz; ++k) {
+                        const size_t e = (size_t)el0 + ((size_t)i * ny + j) * nz + k;
+                        for (int a = 0; a < 8; ++a) {
+                            const int expect =
+                                node0 + ((i + co[a][0]) * (ny + 1) + (j + co[a][1])) * (nz + 1) + (k + co[a][2]);
+                            require(c.conn[e * 8 + a] == expect,
+                                    "connectivity does not follow the block numbering of its instance");
+                        }
+                    }
+            el0 += (int64_t)nx * ny * nz;
+        }
+        require(el0 == c.n_el, "the instance blocks do not cover every element");
+        c.inst_dims.assign(dims, dims + 3 * n_inst);
+        c.mg.reset();
         return ASEND_OK;
     });
 }
@@ -864,6 +906,7 @@ int asend_apply_operator(asend_ctx* ctx, int32_t precision, const double* x, dou
     return guarded(ctx, [&](Ctx& c) {
         require(c.assembled, "assemble first");
         require(x && y, "null vector");
+        require(precision == 32 || precision == 48 || precision == 64, "precision must be 32, 48 or 64");
         DArr<double> dx, dy;
         dx.upload(x, c.n_dof, c.stream);
         dy.alloc(c.n_dof);
@@ -879,8 +922,25 @@ int asend_time_spmv(asend_ctx* ctx, int32_t precision, int32_t n_launch, double*
     return guarded(ctx, [&](Ctx& c) {
         require(c.assembled, "assemble first");
         require(n_launch > 0, "n_launch must be positive");
+        require(precision == 32 || precision == 48 || precision == 64, "precision must be 32, 48 or 64");
         double bytes = 0.0;
         const double ms = time_spmv(c, precision, n_launch, &bytes);
+        if (ms_per_launch) *ms_per_launch = ms;
+        if (bytes_per_launch) *bytes_per_launch = bytes;
+        return ASEND_OK;
+    });
+}
+
+int asend_time_mg_kernel(asend_ctx* ctx, int32_t kernel, int32_t method, int32_t n_launch, double* ms_per_launch,
+                         double* bytes_per_launch) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.assembled, "assemble first");
+        require(n_launch > 0, "n_launch must be positive");
+        require(kernel >= 0 && kernel <= 2, "kernel must be 0, 1 or 2");
+        require(method == ASEND_METHOD_FP64 || method == ASEND_METHOD_MIXED || method == ASEND_METHOD_SPLIT,
+                "unknown method");
+        double bytes = 0.0;
+        const double ms = mg_time_kernel(c, kernel, method, n_launch, &bytes);
         if (ms_per_launch) *ms_per_launch = ms;
         if (bytes_per_launch) *bytes_per_launch = bytes;
         return ASEND_OK;

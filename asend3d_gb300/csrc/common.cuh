@@ -75,8 +75,10 @@ struct Sbell {
     DArr<int64_t> slice_off;
     DArr<int32_t> col;
     DArr<uint8_t> row_len, diag;
-    DArr<double> v64, m64;  // operator values (K [+cM M] + penalty), mass values
-    DArr<float> v32;
+    DArr<double> v64, m64;  // operator values (K [+cM M] [+cD D] + penalty), mass values
+    DArr<double> d64;       // damping values (Newmark with damping)
+    DArr<float> v32;        // FP32 values: float(v64), the high part of each value
+    DArr<float> v32lo;      // low parts float(v64 - v32): v64 = v32 + v32lo to 2^-48 relative
     int64_t nnz_scalar() const {  // stored scalar entries excluding padding
         int64_t s = 0;
         for (int r = 0; r < n_rows; ++r) s += (int64_t)h_row_len[r];
@@ -138,12 +140,32 @@ struct Ctx {
     bool pattern_ready = false, assembled = false, dynamic = false;
     bool modal = false;  // K and M assembled apart (c_M = 0) for the frequency job
     double dt = 0, beta = 0.25, gamma = 0.5, cM = 0;
+    double cD = 0;                  // damping coefficient of the Newmark operator (dt gamma cM)
+    // material model beyond isotropic E, nu (solids without internal DOF):
+    // engineering constants per element [n_el][9] = E1 E2 E3 nu12 nu13 nu23
+    // G12 G13 G23 and the 6x6 stiffness from them
+    std::vector<double> ortho;
+    DArr<double> d_cmat;
+    // damping: Rayleigh coefficients and material damping matrices [n_el][36]
+    double ray_cm = 0, ray_ck = 0;
+    std::vector<double> dmat;
+    DArr<double> d_dmat;
+    bool lump = false;              // row-sum lumped mass in Newmark assemblies
     double sf = 0;
     int assembled_precision = 64;
     float last_assemble_ms = 0.f;
 
     // ---- pattern / assembly
     Sbell A;
+    // geometry classes: elements whose matrices at unit modulus (and unit
+    // density) coincide share one reference matrix; K_e = E_e * Khat_class
+    int cls_type = 0, n_cls = 0;
+    std::vector<int32_t> h_cls_of;
+    DArr<int32_t> d_cls_of;          // class of each element
+    DArr<double> cls_ke, cls_me;     // [n_cls][(3 nn)^2] stiffness, [n_cls][nn nn] mass (FP64)
+    DArr<float> cls_ke32;            // FP32 copy of cls_ke (multigrid coarsening)
+    DArr<int32_t> d_gat_ptr, d_gat;  // per value slot: contributing (element, a, b) entries
+    bool cls_ready = false;
     DArr<int32_t> d_slot_map;  // [n_el * nn * nn] slot of block (a, b)
     std::vector<int32_t> colour_of, colour_ptr, colour_elems;
     DArr<int32_t> d_colour_elems;
@@ -177,6 +199,7 @@ struct Ctx {
     // independent instances stacked in one operator (batched solves)
     int n_inst = 0;
     std::vector<int32_t> inst_node_ptr;
+    std::vector<int32_t> inst_dims;          // structured block (nx, ny, nz) per instance (multigrid)
     DArr<int32_t> d_cta_inst, d_inst_cta0, d_inst_ncta;
     DArr<int64_t> d_unit_idx;  // diagonal entries of nodes without elements (set to 1)
     std::vector<double> sf_inst;             // penalty scale per instance
@@ -228,6 +251,7 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double* smem /* [32*K]
 
 // host-side helpers implemented in the .cu files
 void assemble_operator(Ctx& c, int precision);
+void build_classes(Ctx& c, const std::vector<int32_t>& slot_map);
 void build_pattern(Ctx& c);
 void apply_operator_device(Ctx& c, int precision, const double* d_x, double* d_y);
 double time_spmv(Ctx& c, int precision, int n_launch, double* bytes);
@@ -245,6 +269,7 @@ int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* am
 void upload_rhs(Ctx& c);
 void ensure_pinned_scalars(Ctx& c, size_t bytes);
 int instance_of_node(const Ctx& c, int node);
+bool orthotropic_cmat(const double* props9, double* C36);
 double row_penalty_scale(const Ctx& c, int row);
 // multigrid (k_mg.cu)
 void mg_prepare(Ctx& c);
@@ -256,6 +281,7 @@ void mg_stationary_residual(Ctx& c, float* r_host, int k, bool learned_smoother)
 void mg_learned_loss_grad(Ctx& c, const float* samples, int n_samples, float* gblk, double* d_loss);
 void mg_apply(Ctx& c, const float* d_b, float* d_z4);
 int mg_levels(const Ctx& c);
+double mg_time_kernel(Ctx& c, int kernel, int method, int n_launch, double* bytes);
 int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f, double* d_x,
                  int nrhs);
 // shell4 elements (k_shell.cu)

@@ -18,6 +18,9 @@
 // Elements of one colour share no node, so the scatter needs no atomics and
 // the summation order is fixed (deterministic).
 #include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
 #include <vector>
 
 #include "common.cuh"
@@ -258,13 +261,185 @@ __global__ void penalty_val_kernel(int n, const int64_t* __restrict__ idx, const
     if (k < n) atomicAdd(&vals[idx[k]], val[k]);
 }
 
-__global__ void round_kernel(size_t n, const double* __restrict__ src, float* __restrict__ dst) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        dst[i] = (float)src[i];
+// FP32 copy (high parts) and the low parts of the FP64 values
+__global__ void round_kernel(size_t n, const double* __restrict__ src, float* __restrict__ dst,
+                             float* __restrict__ lo) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double v = src[i];
+        const float hi = (float)v;
+        dst[i] = hi;
+        lo[i] = (float)(v - (double)hi);
+    }
 }
 __global__ void widen_kernel(size_t n, const float* __restrict__ src, double* __restrict__ dst) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         dst[i] = (double)src[i];
+}
+
+// ---- geometry classes and the gather assembly --------------------------------
+// Unit-modulus (E = 1) stiffness and unit-density mass of hex8 elements
+// reps[r] (one per geometry class): the closed-form isotropic blocks of
+// assemble_colour_kernel at E = 1.  One CTA (64 threads = node pairs) per
+// element.
+__global__ void __launch_bounds__(64) k_hex8_unit(const int32_t* __restrict__ reps, const int32_t* __restrict__ conn,
+                                                  const double* __restrict__ xyz, const double* __restrict__ nu,
+                                                  double* __restrict__ ke, double* __restrict__ me) {
+    __shared__ double s_x[8][3];
+    __shared__ double s_g[8][8][3];
+    __shared__ double s_w[8];
+    const int r = blockIdx.x, t = threadIdx.x;
+    const int e = reps[r];
+    if (t < 24) {
+        const int a = t / 3, j = t % 3;
+        const int n0 = conn[(size_t)e * 8], na = conn[(size_t)e * 8 + a];
+        s_x[a][j] = xyz[3 * (size_t)na + j] - xyz[3 * (size_t)n0 + j];
+    }
+    __syncthreads();
+    if (t < 8) {
+        const int gp = t;
+        double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int a = 0; a < 8; ++a)
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) J[i][j] += s_x[a][i] * c_hex_dn[gp][a][j];
+        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        const double id = 1.0 / det;
+        double Ji[3][3];
+        Ji[0][0] = c00 * id;
+        Ji[1][0] = c01 * id;
+        Ji[2][0] = c02 * id;
+        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+        for (int a = 0; a < 8; ++a)
+            for (int j = 0; j < 3; ++j)
+                s_g[gp][a][j] = c_hex_dn[gp][a][0] * Ji[0][j] + c_hex_dn[gp][a][1] * Ji[1][j] + c_hex_dn[gp][a][2] * Ji[2][j];
+        s_w[gp] = det;
+    }
+    __syncthreads();
+    const int a = t >> 3, b = t & 7;
+    double S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double m = 0.0;
+    for (int gp = 0; gp < 8; ++gp) {
+        const double w = s_w[gp];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) S[i][j] += s_g[gp][a][i] * w * s_g[gp][b][j];
+        m += c_hex_n[gp][a] * c_hex_n[gp][b] * w;
+    }
+    const double ne = nu[e];
+    const double lam = ne / ((1.0 + ne) * (1.0 - 2.0 * ne));
+    const double mu = 1.0 / (2.0 * (1.0 + ne));
+    const double tr = mu * (S[0][0] + S[1][1] + S[2][2]);
+    double* K = ke + (size_t)r * 576;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            K[(3 * a + i) * 24 + 3 * b + j] = lam * S[i][j] + mu * S[j][i] + ((i == j) ? tr : 0.0);
+    me[(size_t)r * 64 + t] = m;
+}
+
+// Gather assembly: one CTA per slice of 32 node rows; thread (lane, jj)
+// forms the slots j = jj, jj + 8, ... of row slice*32 + lane.  Each value is
+// summed once from its contributing (element, a, b) entries,
+//   K_slot = sum E_e Khat_class(e)[a, b] (+ c_M rho_e Mhat_class(e)[a, b] I),
+// and written once in FP64 and as FP32 hi / lo parts (no colouring, no
+// read-modify-write, no zeroing pass); the largest |value| of the slice's
+// instance is reduced on the way (the penalty scale).  A slot's entries are
+// fetched up to 8 at a time (independent loads in flight).
+__global__ void __launch_bounds__(256)
+k_gather_assemble(const int64_t* __restrict__ slice_off, const int32_t* __restrict__ gat_ptr,
+                  const int32_t* __restrict__ gat, const int32_t* __restrict__ cls_of,
+                  const double* __restrict__ cls_ke, const double* __restrict__ cls_me, const double* __restrict__ E,
+                  const double* __restrict__ rho, double cM, double* __restrict__ v64, float* __restrict__ v32,
+                  float* __restrict__ v32lo, double* __restrict__ m64, const int32_t* __restrict__ slice_inst,
+                  unsigned long long* __restrict__ max_out) {
+    __shared__ double s_max[8];
+    const int sl = blockIdx.x, lane = threadIdx.x & 31, jj = threadIdx.x >> 5;
+    const int64_t g0 = slice_off[sl];
+    const int W = (int)(slice_off[sl + 1] - g0);
+    double mx = 0.0;
+    for (int j = jj; j < W; j += 8) {
+        const int64_t g = g0 + j;
+        const int64_t slot = g * 32 + lane;
+        double k[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) k[q] = 0.0;
+        double m = 0.0;
+        const int q0 = gat_ptr[slot], q1 = gat_ptr[slot + 1];
+        for (int base = q0; base < q1; base += 8) {
+            int ent[8], cl[8];
+            double Ee[8], re[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) ent[u] = (base + u < q1) ? gat[base + u] : -1;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                cl[u] = 0;
+                Ee[u] = 0.0;
+                re[u] = 0.0;
+                if (ent[u] >= 0) {
+                    const int e = ent[u] >> 6;
+                    cl[u] = cls_of[e];
+                    Ee[u] = E[e];
+                    if (m64) re[u] = rho[e];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (ent[u] < 0) continue;
+                const int a = (ent[u] >> 3) & 7, b = ent[u] & 7;
+                const double* K = cls_ke + (size_t)cl[u] * 576 + (3 * a) * 24 + 3 * b;
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int c2 = 0; c2 < 3; ++c2) k[i * 3 + c2] = fma(Ee[u], K[i * 24 + c2], k[i * 3 + c2]);
+                if (m64) m = fma(re[u], cls_me[(size_t)cl[u] * 64 + a * 8 + b], m);
+            }
+        }
+        if (m64) {
+            k[0] += cM * m;
+            k[4] += cM * m;
+            k[8] += cM * m;
+        }
+        double* vb = v64 + (g * 9) * 32 + lane;
+        float* wb = v32 + (g * 9) * 32 + lane;
+        float* lb = v32lo + (g * 9) * 32 + lane;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const float hi = (float)k[q];
+            vb[q * 32] = k[q];
+            wb[q * 32] = hi;
+            lb[q * 32] = (float)(k[q] - (double)hi);
+            mx = fmax(mx, fabs(k[q]));
+        }
+        if (m64) {
+            double* mb = m64 + (g * 9) * 32 + lane;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) mb[q * 32] = (q == 0 || q == 4 || q == 8) ? m : 0.0;
+        }
+    }
+    mx = warp_max(mx);
+    if (lane == 0) s_max[jj] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t = fmax(t, s_max[w]);
+        atomicMax(&max_out[slice_inst ? slice_inst[sl] : 0], (unsigned long long)__double_as_longlong(t));
+    }
+}
+
+// FP32 hi / lo copies of the entries the penalty or the unit diagonal changed
+__global__ void k_refresh32(int n, const int64_t* __restrict__ idx, const double* __restrict__ v64,
+                            float* __restrict__ v32, float* __restrict__ v32lo) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double v = v64[idx[k]];
+    const float hi = (float)v;
+    v32[idx[k]] = hi;
+    v32lo[idx[k]] = (float)(v - (double)hi);
 }
 
 int stream_grid(size_t n) {
@@ -290,57 +465,215 @@ void launch_colours(Ctx& c, T* vals, double* mvals) {
 
 }  // namespace
 
+// Geometry classes of a hex8 / brickIM mesh and the per-slot gather lists.
+// Two elements share a class when their corner offsets from corner 0 agree
+// to 1e-12 of the element size and their Poisson ratios are equal; their
+// matrices at unit modulus and density then agree to that relative level, so
+// K_e = E_e Khat_class and M_e = rho_e Mhat_class.  A structured block has
+// one class (a batch of blocks one per instance); an unstructured mesh has up
+// to one per element.  Without classes (other element types, or more class
+// matrices than fit the memory cap) the colour scatter assembles instead.
+void build_classes(Ctx& c, const std::vector<int32_t>& slot_map) {
+    c.cls_ready = false;
+    c.n_cls = 0;
+    c.cls_ke.release();
+    c.cls_me.release();
+    c.cls_ke32.release();
+    c.d_cls_of.release();
+    c.d_gat_ptr.release();
+    c.d_gat.release();
+    c.h_cls_of.clear();
+    if ((c.type != 8 && c.type != 81) || c.n_el >= (1 << 25)) return;
+    init_tables();
+    const int nn = 8, ne = c.n_el;
+    std::vector<double> rel((size_t)ne * 24), scale(ne);
+    double hmax = 0.0;
+    for (int e = 0; e < ne; ++e) {
+        const int n0 = c.conn[(size_t)e * nn];
+        double s2 = 0.0;
+        for (int a = 0; a < nn; ++a) {
+            const int na = c.conn[(size_t)e * nn + a];
+            for (int j = 0; j < 3; ++j) {
+                const double d = c.xyz[3 * (size_t)na + j] - c.xyz[3 * (size_t)n0 + j];
+                rel[(size_t)e * 24 + 3 * a + j] = d;
+                s2 = std::max(s2, std::fabs(d));
+            }
+        }
+        scale[e] = s2;
+        hmax = std::max(hmax, s2);
+    }
+    if (!(hmax > 0.0)) return;
+    const double grid = 1e-9 * hmax;
+    std::unordered_map<uint64_t, std::vector<int32_t>> buckets;
+    std::vector<int32_t> reps;
+    c.h_cls_of.assign(ne, 0);
+    const size_t cap_bytes = (size_t)1 << 30;
+    for (int e = 0; e < ne; ++e) {
+        const double* r = &rel[(size_t)e * 24];
+        uint64_t h = 1469598103934665603ull;
+        auto mix = [&](uint64_t v) {
+            h ^= v;
+            h *= 1099511628211ull;
+        };
+        for (int i = 0; i < 24; ++i) mix((uint64_t)std::llround(r[i] / grid));
+        uint64_t nub;
+        std::memcpy(&nub, &c.nu[e], sizeof(nub));
+        mix(nub);
+        auto& cand = buckets[h];
+        int found = -1;
+        for (int cl : cand) {
+            const int rp = reps[cl];
+            if (c.nu[rp] != c.nu[e]) continue;
+            const double* q = &rel[(size_t)rp * 24];
+            double d = 0.0;
+            for (int i = 0; i < 24; ++i) d = std::max(d, std::fabs(r[i] - q[i]));
+            if (d <= 1e-12 * scale[e]) {
+                found = cl;
+                break;
+            }
+        }
+        if (found < 0) {
+            found = (int)reps.size();
+            reps.push_back(e);
+            cand.push_back(found);
+            if (reps.size() * 576 * sizeof(double) > cap_bytes || (c.type == 81 && reps.size() > 4096)) {
+                c.h_cls_of.clear();
+                return;
+            }
+        }
+        c.h_cls_of[e] = found;
+    }
+    const int ncl = (int)reps.size();
+    c.cls_ke.alloc((size_t)ncl * 576);
+    c.cls_me.alloc((size_t)ncl * 64);
+    if (c.type == 8) {
+        DArr<int32_t> d_reps;
+        d_reps.upload(reps, c.stream);
+        k_hex8_unit<<<ncl, 64, 0, c.stream>>>(d_reps.p, c.d_conn.p, c.d_xyz.p, c.d_nu.p, c.cls_ke.p, c.cls_me.p);
+        ++c.launches;
+        ASEND_CUDA(cudaGetLastError());
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+    } else {
+        // brickIM: the condensed matrices of each class's element, scaled to
+        // unit modulus and density (the condensation is linear in E)
+        std::vector<double> ke((size_t)ncl * 576), me((size_t)ncl * 64, 0.0), kt(576), mt(576);
+        const bool mass = !c.rho.empty();
+        for (int cl = 0; cl < ncl; ++cl) {
+            const int e = reps[cl];
+            brickim_element_matrices(c, e, 1, kt.data(), mass ? mt.data() : nullptr);
+            for (int q = 0; q < 576; ++q) ke[(size_t)cl * 576 + q] = kt[q] / c.E[e];
+            if (mass && c.rho[e] != 0.0)
+                for (int a = 0; a < 8; ++a)
+                    for (int b = 0; b < 8; ++b) me[(size_t)cl * 64 + a * 8 + b] = mt[(3 * a) * 24 + 3 * b] / c.rho[e];
+        }
+        ASEND_CUDA(cudaMemcpyAsync(c.cls_ke.p, ke.data(), sizeof(double) * ke.size(), cudaMemcpyHostToDevice, c.stream));
+        ASEND_CUDA(cudaMemcpyAsync(c.cls_me.p, me.data(), sizeof(double) * me.size(), cudaMemcpyHostToDevice, c.stream));
+    }
+    {
+        std::vector<double> k64((size_t)ncl * 576);
+        ASEND_CUDA(cudaMemcpyAsync(k64.data(), c.cls_ke.p, sizeof(double) * k64.size(), cudaMemcpyDeviceToHost,
+                                   c.stream));
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        std::vector<float> k32(k64.begin(), k64.end());
+        c.cls_ke32.upload(k32, c.stream);
+    }
+    // per-slot lists of contributing (element, a, b), in element order
+    const Sbell& A = c.A;
+    const size_t n_slots = (size_t)A.n_groups * kSlice;
+    std::vector<int32_t> ptr(n_slots + 1, 0);
+    for (size_t q = 0; q < slot_map.size(); ++q) ptr[(size_t)slot_map[q] + 1]++;
+    for (size_t q = 0; q < n_slots; ++q) ptr[q + 1] += ptr[q];
+    std::vector<int32_t> gat(slot_map.size()), fill(ptr.begin(), ptr.end() - 1);
+    for (int e = 0; e < ne; ++e)
+        for (int ab = 0; ab < 64; ++ab) gat[fill[slot_map[(size_t)e * 64 + ab]]++] = e * 64 + ab;
+    c.d_gat_ptr.upload(ptr, c.stream);
+    c.d_gat.upload(gat, c.stream);
+    c.d_cls_of.upload(c.h_cls_of, c.stream);
+    ASEND_CUDA(cudaStreamSynchronize(c.stream));
+    c.n_cls = ncl;
+    c.cls_type = c.type;
+    c.cls_ready = true;
+}
+
 void assemble_operator(Ctx& c, int precision) {
     init_tables();
     Sbell& A = c.A;
     const size_t nval = (size_t)A.n_groups * 9 * kSlice;
     A.v64.alloc(nval);
     A.v32.alloc(nval);
-    A.v64.zero(c.stream);
-    A.v32.zero(c.stream);
+    A.v32lo.alloc(nval);
+    // gather path: FP64 hex8 / brickIM with geometry classes (every value
+    // written once, the penalty scale reduced on the way)
+    const bool gather = precision == 64 && c.cls_ready && c.cls_type == c.type;
     double* mvals = nullptr;
     if (c.dynamic) {
         A.m64.alloc(nval);
-        A.m64.zero(c.stream);
+        if (!gather) A.m64.zero(c.stream);
         mvals = A.m64.p;
     } else {
         A.m64.release();
     }
+    if (!gather) {
+        A.v64.zero(c.stream);
+        A.v32.zero(c.stream);
+    }
+    const int ni = c.n_inst > 1 ? c.n_inst : 1;
     ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
-    if (c.type == 41) {
-        shell_assemble(c, A.v64.p, mvals);  // FP64 element matrices at either precision
-    } else if (c.type == 81) {
-        brickim_assemble(c, A.v64.p, mvals);  // FP64 condensed element matrices at either precision
-    } else if (precision == 64) {
-        if (c.nn == 8) launch_colours<8, double>(c, A.v64.p, mvals);
-        else launch_colours<4, double>(c, A.v64.p, mvals);
+    c.d_max_partial.alloc(ni);
+    c.d_max_partial.zero(c.stream);
+    unsigned long long* dmax = reinterpret_cast<unsigned long long*>(c.d_max_partial.p);
+    if (gather) {
+        const int32_t* slice_inst = nullptr;
+        DArr<int32_t> d_si;
+        if (ni > 1) {
+            std::vector<int32_t> si(A.n_slices);
+            for (int s2 = 0; s2 < A.n_slices; ++s2) si[s2] = instance_of_node(c, s2 * kSlice);
+            d_si.upload(si, c.stream);
+            slice_inst = d_si.p;
+        }
+        k_gather_assemble<<<A.n_slices, 256, 0, c.stream>>>(A.slice_off.p, c.d_gat_ptr.p, c.d_gat.p, c.d_cls_of.p,
+                                                            c.cls_ke.p, c.cls_me.p, c.d_E.p, c.d_rho.p, c.cM,
+                                                            A.v64.p, A.v32.p, A.v32lo.p, mvals, slice_inst, dmax);
+        ++c.launches;
+        ASEND_CUDA(cudaGetLastError());
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));  // d_si
     } else {
-        if (c.nn == 8) launch_colours<8, float>(c, A.v32.p, mvals);
-        else launch_colours<4, float>(c, A.v32.p, mvals);
-        widen_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(nval, A.v32.p, A.v64.p);
+        if (c.type == 41) {
+            shell_assemble(c, A.v64.p, mvals);  // FP64 element matrices at either precision
+        } else if (c.type == 81) {
+            brickim_assemble(c, A.v64.p, mvals);  // FP64 condensed element matrices at either precision
+        } else if (precision == 64) {
+            if (c.nn == 8) launch_colours<8, double>(c, A.v64.p, mvals);
+            else launch_colours<4, double>(c, A.v64.p, mvals);
+        } else {
+            if (c.nn == 8) launch_colours<8, float>(c, A.v32.p, mvals);
+            else launch_colours<4, float>(c, A.v32.p, mvals);
+            widen_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(nval, A.v32.p, A.v64.p);
+            ++c.launches;
+        }
+        // penalty scale over the element matrix (K [+ cM M]): one per
+        // instance of a batched stack (each instance is its own model)
+        if (ni > 1) {
+            std::vector<int64_t> seg(ni + 1);
+            for (int i = 0; i <= ni; ++i) {
+                const int node = c.inst_node_ptr[i];
+                const int s2 = std::min((node + kSlice - 1) / kSlice, A.n_slices);
+                seg[i] = A.h_slice_off[s2] * 9 * kSlice;
+            }
+            DArr<int64_t> d_seg;
+            d_seg.upload(seg, c.stream);
+            max_abs_seg_kernel<<<dim3(64, ni), 256, 0, c.stream>>>(d_seg.p, A.v64.p, dmax);
+            ASEND_CUDA(cudaStreamSynchronize(c.stream));  // d_seg
+        } else {
+            max_abs_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(nval, A.v64.p, dmax);
+        }
         ++c.launches;
     }
-    // penalty scale over the element matrix (K [+ cM M]), then the penalty
+    std::vector<double> mx(ni);
+    ASEND_CUDA(cudaMemcpyAsync(mx.data(), c.d_max_partial.p, sizeof(double) * ni, cudaMemcpyDeviceToHost, c.stream));
+    ASEND_CUDA(cudaStreamSynchronize(c.stream));
     const int npen = (int)c.d_pen_idx.n;
-    if (c.n_inst > 1) {
-        // one scale per instance (each instance is its own model)
-        const int ni = c.n_inst;
-        std::vector<int64_t> seg(ni + 1);
-        for (int i = 0; i <= ni; ++i) {
-            const int node = c.inst_node_ptr[i];
-            const int s = std::min((node + kSlice - 1) / kSlice, A.n_slices);
-            seg[i] = A.h_slice_off[s] * 9 * kSlice;
-        }
-        DArr<int64_t> d_seg;
-        d_seg.upload(seg, c.stream);
-        c.d_max_partial.alloc(ni);
-        c.d_max_partial.zero(c.stream);
-        max_abs_seg_kernel<<<dim3(64, ni), 256, 0, c.stream>>>(d_seg.p, A.v64.p,
-                                                               reinterpret_cast<unsigned long long*>(c.d_max_partial.p));
-        ++c.launches;
-        std::vector<double> mx(ni);
-        ASEND_CUDA(cudaMemcpyAsync(mx.data(), c.d_max_partial.p, sizeof(double) * ni, cudaMemcpyDeviceToHost, c.stream));
-        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+    if (ni > 1) {
         c.sf_inst.resize(ni);
         c.sf = 0.0;
         for (int i = 0; i < ni; ++i) {
@@ -357,15 +690,7 @@ void assemble_operator(Ctx& c, int precision) {
         }
     } else {
         c.sf_inst.clear();
-        c.d_max_partial.alloc(1);
-        c.d_max_partial.zero(c.stream);
-        max_abs_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(
-            nval, A.v64.p, reinterpret_cast<unsigned long long*>(c.d_max_partial.p));
-        ++c.launches;
-        double mx = 0.0;
-        ASEND_CUDA(cudaMemcpyAsync(&mx, c.d_max_partial.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-        ASEND_CUDA(cudaStreamSynchronize(c.stream));
-        c.sf = 100000.0 * mx;
+        c.sf = 100000.0 * mx[0];
         if (npen > 0) {
             penalty_kernel<<<(npen + 255) / 256, 256, 0, c.stream>>>(npen, c.d_pen_idx.p, c.d_pen_coef.p, c.sf,
                                                                      A.v64.p);
@@ -377,8 +702,17 @@ void assemble_operator(Ctx& c, int precision) {
         unit_kernel<<<(nunit + 255) / 256, 256, 0, c.stream>>>(nunit, c.d_unit_idx.p, A.v64.p);
         ++c.launches;
     }
-    round_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(nval, A.v64.p, A.v32.p);
-    ++c.launches;
+    if (gather) {  // FP32 copies of the entries changed after the gather
+        if (npen > 0)
+            k_refresh32<<<(npen + 255) / 256, 256, 0, c.stream>>>(npen, c.d_pen_idx.p, A.v64.p, A.v32.p, A.v32lo.p);
+        if (nunit > 0)
+            k_refresh32<<<(nunit + 255) / 256, 256, 0, c.stream>>>(nunit, c.d_unit_idx.p, A.v64.p, A.v32.p,
+                                                                   A.v32lo.p);
+        c.launches += (npen > 0) + (nunit > 0);
+    } else {
+        round_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(nval, A.v64.p, A.v32.p, A.v32lo.p);
+        ++c.launches;
+    }
     ASEND_CUDA(cudaGetLastError());
     ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
     ASEND_CUDA(cudaEventSynchronize(c.ev1));

@@ -57,8 +57,8 @@ k_mass_rowsum(int n_rows, const int64_t* __restrict__ slice_off, const uint8_t* 
 // Diagonal entries of the node-diagonal blocks: save (mode 0), add s (mode 1)
 // or restore from the saved copy (mode 2); the FP32 copy follows the FP64 one.
 __global__ void k_diag_entries(int n_rows, const int64_t* __restrict__ slice_off, const uint8_t* __restrict__ diag,
-                               double* __restrict__ v64, float* __restrict__ v32, const double* __restrict__ s,
-                               double* __restrict__ saved, int mode) {
+                               double* __restrict__ v64, float* __restrict__ v32, float* __restrict__ v32lo,
+                               const double* __restrict__ s, double* __restrict__ saved, int mode) {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= n_rows) return;
     const int lane = row & 31;
@@ -73,6 +73,7 @@ __global__ void k_diag_entries(int n_rows, const int64_t* __restrict__ slice_off
             const double v = (mode == 1) ? v64[idx] + s[i] : saved[i];
             v64[idx] = v;
             v32[idx] = (float)v;
+            v32lo[idx] = (float)(v - (double)(float)v);
         }
     }
 }
@@ -361,9 +362,9 @@ int eigen_solve(Ctx& c, const asend_eigen_opts& eo, double* eig_out, double* fre
         sD.upload(s, c.stream);
         saved.alloc(n);
         k_diag_entries<<<(rows + 127) / 128, 128, 0, c.stream>>>(rows, c.A.slice_off.p, c.A.diag.p, c.A.v64.p,
-                                                                c.A.v32.p, nullptr, saved.p, 0);
+                                                                c.A.v32.p, c.A.v32lo.p, nullptr, saved.p, 0);
         k_diag_entries<<<(rows + 127) / 128, 128, 0, c.stream>>>(rows, c.A.slice_off.p, c.A.diag.p, c.A.v64.p,
-                                                                c.A.v32.p, sD.p, saved.p, 1);
+                                                                c.A.v32.p, c.A.v32lo.p, sD.p, saved.p, 1);
         c.launches += 2;
         ++c.assembly_epoch;  // preconditioners and multigrid levels follow the shifted values
     }
@@ -376,7 +377,7 @@ int eigen_solve(Ctx& c, const asend_eigen_opts& eo, double* eig_out, double* fre
             on = false;
             const int rows = c.A.n_rows;
             k_diag_entries<<<(rows + 127) / 128, 128, 0, c.stream>>>(rows, c.A.slice_off.p, c.A.diag.p, c.A.v64.p,
-                                                                    c.A.v32.p, nullptr, saved.p, 2);
+                                                                    c.A.v32.p, c.A.v32lo.p, nullptr, saved.p, 2);
             ++c.launches;
             ++c.assembly_epoch;
         }

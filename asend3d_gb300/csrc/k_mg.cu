@@ -25,6 +25,7 @@
 //    beta = -alpha (z . Ap) / (r_old . z_old), which tolerates the FP32
 //    preconditioner's rounding asymmetry.
 #include <algorithm>
+#include <array>
 #include <cstring>
 #include <cmath>
 #include <memory>
@@ -40,12 +41,39 @@ struct MgAxis {
     std::vector<float> w;         // fine node -> weight of lo + 1
 };
 
+// One structured block of a level: a single model's grid, or one instance of
+// a batched stack.  Block b of every level belongs to instance b; blocks are
+// coarsened independently, and a block that needs no further coarsening is
+// carried down unchanged (identity maps) until every block is coarse enough.
+struct MgBlk {
+    int nx = 0, ny = 0, nz = 0;   // cells
+    int node0 = 0, el0 = 0;       // first node / element in the level numbering
+    MgAxis ax[3];                 // maps from the finer level's block (levels >= 1)
+    int ox[3] = {0, 0, 0}, ol[3] = {0, 0, 0};  // offsets into the level's packed xs / lo, w
+    int t1_0 = 0, t2_0 = 0;       // offsets (nodes) of the restriction intermediates
+    double h[3] = {0, 0, 0};      // cell spacing per axis
+    bool done = false;            // coarse enough: identity maps below this level
+    int n_nodes() const { return (nx + 1) * (ny + 1) * (nz + 1); }
+    int n_el() const { return nx * ny * nz; }
+};
+
+// Device descriptor of block b of a level; levels >= 1 also describe the
+// finer level's block b (f*) and the block's axis maps.
+struct BlkDev {
+    int nx, ny, nz, node0, el0;
+    int fnx, fny, fnz, fnode0, fel0;
+    int ox0, ox1, ox2, ol0, ol1, ol2;
+    int t1_0, t2_0, dense0, pad;
+};
+
 struct MgLevel {
-    int nx = 0, ny = 0, nz = 0, n_nodes = 0, n_el = 0, n_dof = 0;
-    MgAxis ax[3];                 // maps from the finer level (levels >= 1)
-    DArr<int32_t> d_xs, d_lo;     // packed per axis: offsets ox[3] / ol[3]
+    int n_nodes = 0, n_el = 0, n_dof = 0;  // totals (level 0 of a batch includes padding nodes)
+    int n_t1 = 0, n_t2 = 0;       // restriction intermediate sizes (nodes)
+    std::vector<MgBlk> blk;
+    DArr<BlkDev> d_blk;
+    DArr<int32_t> pre_node, pre_el, pre_t1, pre_t2;  // per-block starts (+ total)
+    DArr<int32_t> d_xs, d_lo;     // packed per block and axis
     DArr<float> d_w;
-    int ox[3] = {0, 0, 0}, ol[3] = {0, 0, 0};
     Sbell own;                    // pattern + FP32 values (levels >= 1)
     Sbell* A = nullptr;
     std::vector<int32_t> colour_ptr;
@@ -62,8 +90,16 @@ struct MgLevel {
 
 struct MgHierarchy {
     std::vector<std::unique_ptr<MgLevel>> L;
-    DArr<float> dense, ainv;      // coarsest operator (n x n) and its inverse
-    int n_coarse = 0;
+    DArr<float> dense, ainv;      // coarsest operators, one dense block per instance, inverted in place
+    int n_coarse = 0;             // largest coarsest block (DOF)
+    int n_blk = 1;
+    std::vector<int32_t> h_dense0;  // offset of each block's dense matrix (floats)
+    DArr<double> blk_sf;          // penalty scale per block (instance)
+    // captured outer iterations, reused while the launch arguments match
+    std::vector<std::pair<std::vector<uint8_t>, cudaGraphExec_t>> graphs;
+    ~MgHierarchy() {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    }
     int64_t epoch = -1;
     float omega = 0.6f;           // damping used when the eigenvalue estimate fails
     bool l0_learned = false;      // finest-level smoother blocks come from the learned model
@@ -91,13 +127,24 @@ __device__ __forceinline__ int nid(int i, int j, int k, int ny, int nz) { return
 __constant__ int c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
                                    {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
 
-struct LevelView {  // kernel-side view of one level's interpolation tables
-    int nx, ny, nz;
+struct LevelView {  // kernel-side view of a coarse level's blocks and maps from the finer level
+    int n_blk;
+    const BlkDev* blk;
     const int32_t* xs;
     const int32_t* lo;
     const float* w;
-    int ox0, ox1, ox2, ol0, ol1, ol2;
 };
+
+// Block of index idx: the largest b with pre[b] <= idx (pre ascending).
+__device__ __forceinline__ int find_blk(const int32_t* __restrict__ pre, int n_blk, int idx) {
+    int lo = 0, hi = n_blk - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= idx) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
 // ---------------------------------------------------------------------------
 // Galerkin coarsening by elements
@@ -109,7 +156,8 @@ struct LevelView {  // kernel-side view of one level's interpolation tables
 // isotropic blocks as in the assembly kernel); then T_e = K_e (Q_e x I3) and
 // K_C = sum_e (Q_e x I3)^T T_e.
 __global__ void __launch_bounds__(512)
-k_coarsen(LevelView cv, int fny, int fnz, const float* __restrict__ fine_ke, const double* __restrict__ xyz,
+k_coarsen(LevelView cv, const int32_t* __restrict__ pre_el, const float* __restrict__ fine_ke,
+          const float* __restrict__ cls_ke, const int32_t* __restrict__ cls_of, const double* __restrict__ xyz,
           const int32_t* __restrict__ conn0, const double* __restrict__ E, const double* __restrict__ nu,
           float* __restrict__ coarse_ke) {
     __shared__ float Ke[8][576];
@@ -121,10 +169,12 @@ k_coarsen(LevelView cv, int fny, int fnz, const float* __restrict__ fine_ke, con
     __shared__ int fe[8];
     const int t = threadIdx.x;
     const int C = blockIdx.x;
-    const int ci = C / (cv.ny * cv.nz), cj = (C / cv.nz) % cv.ny, ck = C % cv.nz;
-    const int s0 = cv.xs[cv.ox0 + ci], w0 = cv.xs[cv.ox0 + ci + 1] - s0;
-    const int s1 = cv.xs[cv.ox1 + cj], w1 = cv.xs[cv.ox1 + cj + 1] - s1;
-    const int s2 = cv.xs[cv.ox2 + ck], w2 = cv.xs[cv.ox2 + ck + 1] - s2;
+    const BlkDev& d = cv.blk[find_blk(pre_el, cv.n_blk, C)];
+    const int Cl = C - d.el0;
+    const int ci = Cl / (d.ny * d.nz), cj = (Cl / d.nz) % d.ny, ck = Cl % d.nz;
+    const int s0 = cv.xs[d.ox0 + ci], w0 = cv.xs[d.ox0 + ci + 1] - s0;
+    const int s1 = cv.xs[d.ox1 + cj], w1 = cv.xs[d.ox1 + cj + 1] - s1;
+    const int s2 = cv.xs[d.ox2 + ck], w2 = cv.xs[d.ox2 + ck + 1] - s2;
     const int nch = w0 * w1 * w2;
     if (t < nch * 64) {  // interpolation weights of child ch: fine corner a <- coarse corner b
         const int ch = t >> 6, a = (t >> 3) & 7, b = t & 7;
@@ -134,10 +184,15 @@ k_coarsen(LevelView cv, int fny, int fnz, const float* __restrict__ fine_ke, con
         const float xi2 = (float)(o2 + c_corner[a][2]) / w2;
         Q[ch][a][b] = (c_corner[b][0] ? xi0 : 1.f - xi0) * (c_corner[b][1] ? xi1 : 1.f - xi1) *
                       (c_corner[b][2] ? xi2 : 1.f - xi2);
-        if (a == 0 && b == 0) fe[ch] = ((s0 + o0) * fny + (s1 + o1)) * fnz + (s2 + o2);
+        if (a == 0 && b == 0) fe[ch] = d.fel0 + ((s0 + o0) * d.fny + (s1 + o1)) * d.fnz + (s2 + o2);
     }
     __syncthreads();
-    if (fine_ke) {
+    if (cls_ke) {  // K_e = E_e * (unit-modulus matrix of the element's geometry class)
+        for (int q = t; q < nch * 576; q += blockDim.x) {
+            const int e = fe[q / 576];
+            Ke[q / 576][q % 576] = (float)E[e] * cls_ke[(size_t)cls_of[e] * 576 + q % 576];
+        }
+    } else if (fine_ke) {
         for (int q = t; q < nch * 576; q += blockDim.x) Ke[q / 576][q % 576] = fine_ke[(size_t)fe[q / 576] * 576 + q % 576];
     } else {
         if (t < nch * 24) {
@@ -236,10 +291,14 @@ __global__ void k_scatter_ke(int n, const int32_t* __restrict__ elems, const int
         for (int j = 0; j < 3; ++j) vb[(i * 3 + j) * 32] += K[(3 * a + i) * 24 + 3 * b + j];
 }
 
+// Lumped penalty of a coarse level, scaled by the penalty scale of the
+// node's block (instance).
 __global__ void k_add_pen(int n_rows, const int64_t* __restrict__ slice_off, const uint8_t* __restrict__ diag,
-                          const float* __restrict__ pen, float sf, float* __restrict__ vals) {
+                          const float* __restrict__ pen, const int32_t* __restrict__ pre_node, int n_blk,
+                          const double* __restrict__ blk_sf, float* __restrict__ vals) {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= n_rows) return;
+    const float sf = (float)blk_sf[find_blk(pre_node, n_blk, row)];
     const int64_t g = slice_off[row >> 5] + diag[row];
     const int lane = row & 31;
 #pragma unroll
@@ -270,52 +329,76 @@ __global__ void k_smoother_blocks(int n_rows, const int64_t* __restrict__ slice_
     B[8] = (float)((m[0] * m[4] - m[1] * m[3]) * id);
 }
 
-// coarsest level: dense copy and in-place Gauss-Jordan inverse (SPD, no pivoting)
+// Coarsest level: one dense matrix per block (n_b = 3 x the block's nodes,
+// at offset dense0), filled row by row (one CTA per node row), then inverted
+// in place by Gauss-Jordan (SPD, no pivoting), one CTA per block.
 __global__ void k_dense_build(int n_rows, const int64_t* __restrict__ slice_off, const uint8_t* __restrict__ row_len,
-                              const int32_t* __restrict__ col, const float* __restrict__ vals, float* __restrict__ D) {
+                              const int32_t* __restrict__ col, const float* __restrict__ vals, LevelView cv,
+                              const int32_t* __restrict__ pre_node, float* __restrict__ D) {
     const int row = blockIdx.x;
-    const int n = 3 * n_rows;
-    for (int q = threadIdx.x; q < 3 * n; q += blockDim.x) D[(size_t)(3 * row) * n + q] = 0.f;
+    const BlkDev& d = cv.blk[find_blk(pre_node, cv.n_blk, row)];
+    const int n = 3 * (d.nx + 1) * (d.ny + 1) * (d.nz + 1);
+    const int lr = row - d.node0;
+    if (lr >= n / 3) return;  // padding node between instances
+    float* Db = D + d.dense0;
+    for (int q = threadIdx.x; q < 3 * n; q += blockDim.x) Db[(size_t)(3 * lr) * n + q] = 0.f;
     __syncthreads();
     const int lane = row & 31, len = row_len[row];
     const int64_t g0 = slice_off[row >> 5];
     for (int q = threadIdx.x; q < len * 9; q += blockDim.x) {
         const int j = q / 9, v = q % 9, a = v / 3, c = v % 3;
         const int64_t g = g0 + j;
-        const int cn = col[g * 32 + lane];
-        D[(size_t)(3 * row + a) * n + 3 * cn + c] = vals[(g * 9 + v) * 32 + lane];
+        const int cn = col[g * 32 + lane] - d.node0;
+        Db[(size_t)(3 * lr + a) * n + 3 * cn + c] = vals[(g * 9 + v) * 32 + lane];
     }
 }
 
-// In-place Gauss-Jordan inverse of an SPD matrix (no pivoting).  With
-// in_smem the whole matrix lives in dynamic shared memory for the n steps
-// (n*n*4 bytes, n <= 238); otherwise it is updated in global memory.
-__global__ void __launch_bounds__(1024) k_gauss_jordan(int n, float* __restrict__ Ag, int in_smem) {
+// In-place Gauss-Jordan inverse of block blockIdx.x's matrix.  The 1024
+// threads form a 32 x 32 grid; thread (ty, tx) updates the entries (ty + 32i,
+// tx + 32j), so consecutive threads touch consecutive addresses and no index
+// is divided.  With in_smem the matrix lives in dynamic shared memory for
+// the n steps (n <= 234); otherwise it is updated in global memory.
+__global__ void __launch_bounds__(1024) k_gauss_jordan(LevelView cv, float* __restrict__ Dall, int in_smem) {
     extern __shared__ float dyn[];
     __shared__ float colk[1024];
     __shared__ float rowk[1024];
+    const BlkDev& d = cv.blk[blockIdx.x];
+    const int n = 3 * (d.nx + 1) * (d.ny + 1) * (d.nz + 1);
+    float* Ag = Dall + d.dense0;
     float* A = in_smem ? dyn : Ag;
     if (in_smem) {
         for (int q = threadIdx.x; q < n * n; q += blockDim.x) dyn[q] = Ag[q];
         __syncthreads();
     }
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     for (int k = 0; k < n; ++k) {
+        const float inv = 1.f / A[(size_t)k * n + k];
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             colk[i] = A[(size_t)i * n + k];
-            rowk[i] = A[(size_t)k * n + i];
+            rowk[i] = A[(size_t)k * n + i] * inv;
         }
         __syncthreads();
-        const float inv = 1.f / colk[k];
-        for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
-            const int i = q / n, j = q % n;
-            float v;
-            if (i == k) v = (j == k) ? inv : rowk[j] * inv;
-            else if (j == k) v = -colk[i] * inv;
-            else v = A[q] - colk[i] * rowk[j] * inv;
-            A[q] = v;
+        for (int i = ty; i < n; i += 32) {
+            const float ci = colk[i];
+            float* Ar = A + (size_t)i * n;
+            if (i == k) {
+                for (int j = tx; j < n; j += 32) Ar[j] = (j == k) ? inv : rowk[j];
+            } else {
+                for (int j = tx; j < n; j += 32) Ar[j] = (j == k) ? -ci * inv : fmaf(-ci, rowk[j], Ar[j]);
+            }
         }
         __syncthreads();
     }
+    // the exact inverse is symmetric: average the FP32 rounding asymmetry out,
+    // so the coarse solve (and with it the V-cycle) is a symmetric operator
+    for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
+        const int i = q / n, j = q % n;
+        if (j <= i) continue;
+        const float v = 0.5f * (A[(size_t)i * n + j] + A[(size_t)j * n + i]);
+        A[(size_t)i * n + j] = v;
+        A[(size_t)j * n + i] = v;
+    }
+    __syncthreads();
     if (in_smem)
         for (int q = threadIdx.x; q < n * n; q += blockDim.x) Ag[q] = dyn[q];
 }
@@ -598,63 +681,20 @@ __global__ void k_scale_blocks(int n, float* __restrict__ binv, const float* __r
     if (i == 0) *omega_out = omega;
 }
 
-__device__ __forceinline__ float restrict_w(const LevelView& v, int axis, int i, int m) {
-    const int32_t* lo = v.lo + (axis == 0 ? v.ol0 : axis == 1 ? v.ol1 : v.ol2);
-    const float* w = v.w + (axis == 0 ? v.ol0 : axis == 1 ? v.ol1 : v.ol2);
-    if (lo[i] == m) return 1.f - w[i];
-    if (lo[i] + 1 == m) return w[i];
-    return 0.f;
-}
-
-// b_c[I] = sum_i w_iI r_f[i]; cv describes the coarse level and its maps
-__global__ void k_vc_restrict(LevelView cv, int fny, int fnz, const float* __restrict__ rf, float* __restrict__ bc,
-                              const Control* ctl) {
-    if (ctl && ctl->all_done) return;
-    const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    const int ncn = (cv.nx + 1) * (cv.ny + 1) * (cv.nz + 1);
-    if (I >= ncn) return;
-    const int ci = I / ((cv.ny + 1) * (cv.nz + 1)), cj = (I / (cv.nz + 1)) % (cv.ny + 1), ck = I % (cv.nz + 1);
-    const int m[3] = {ci, cj, ck};
-    const int nc[3] = {cv.nx, cv.ny, cv.nz};
-    const int ox[3] = {cv.ox0, cv.ox1, cv.ox2};
-    int lo_i[3], hi_i[3];
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-        lo_i[ax] = cv.xs[ox[ax] + max(m[ax] - 1, 0)];
-        hi_i[ax] = cv.xs[ox[ax] + min(m[ax] + 1, nc[ax])];
-    }
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    for (int i = lo_i[0]; i <= hi_i[0]; ++i) {
-        const float wi = restrict_w(cv, 0, i, ci);
-        if (wi == 0.f) continue;
-        for (int j = lo_i[1]; j <= hi_i[1]; ++j) {
-            const float wj = restrict_w(cv, 1, j, cj);
-            if (wj == 0.f) continue;
-            for (int k = lo_i[2]; k <= hi_i[2]; ++k) {
-                const float wk = restrict_w(cv, 2, k, ck);
-                if (wk == 0.f) continue;
-                const float ww = wi * wj * wk;
-                const int f = nid(i, j, k, fny, fnz);
-                s0 += ww * rf[3 * f];
-                s1 += ww * rf[3 * f + 1];
-                s2 += ww * rf[3 * f + 2];
-            }
-        }
-    }
-    bc[3 * I] = s0;
-    bc[3 * I + 1] = s1;
-    bc[3 * I + 2] = s2;
-}
-
-// x_f[i] += sum_I w_iI y_c[I]
-__global__ void k_vc_prolong(LevelView cv, int fnx, int fny, int fnz, const float4* __restrict__ yc,
-                             float4* __restrict__ xf, const Control* ctl) {
+// x_f[i] += sum_I w_iI y_c[I] over the fine level's nodes (a fine node outside
+// every block -- padding between instances -- is left alone); cv describes
+// the coarse level, pre_fnode the fine blocks' first nodes.
+__global__ void k_vc_prolong(LevelView cv, const int32_t* __restrict__ pre_fnode, int n_fine,
+                             const float4* __restrict__ yc, float4* __restrict__ xf, const Control* ctl) {
     if (ctl && ctl->all_done) return;
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= (fnx + 1) * (fny + 1) * (fnz + 1)) return;
-    const int i = f / ((fny + 1) * (fnz + 1)), j = (f / (fnz + 1)) % (fny + 1), k = f % (fnz + 1);
-    const int li = cv.lo[cv.ol0 + i], lj = cv.lo[cv.ol1 + j], lk = cv.lo[cv.ol2 + k];
-    const float wi = cv.w[cv.ol0 + i], wj = cv.w[cv.ol1 + j], wk = cv.w[cv.ol2 + k];
+    if (f >= n_fine) return;
+    const BlkDev& d = cv.blk[find_blk(pre_fnode, cv.n_blk, f)];
+    const int fl = f - d.fnode0;
+    if (fl >= (d.fnx + 1) * (d.fny + 1) * (d.fnz + 1)) return;
+    const int i = fl / ((d.fny + 1) * (d.fnz + 1)), j = (fl / (d.fnz + 1)) % (d.fny + 1), k = fl % (d.fnz + 1);
+    const int li = cv.lo[d.ol0 + i], lj = cv.lo[d.ol1 + j], lk = cv.lo[d.ol2 + k];
+    const float wi = cv.w[d.ol0 + i], wj = cv.w[d.ol1 + j], wk = cv.w[d.ol2 + k];
     float4 acc = xf[f];
 #pragma unroll
     for (int di = 0; di < 2; ++di) {
@@ -668,7 +708,7 @@ __global__ void k_vc_prolong(LevelView cv, int fnx, int fny, int fnz, const floa
             for (int dk = 0; dk < 2; ++dk) {
                 const float c = dk ? wk : 1.f - wk;
                 if (c == 0.f) continue;
-                const float4 y = yc[nid(li + di, lj + dj, lk + dk, cv.ny, cv.nz)];
+                const float4 y = yc[d.node0 + nid(li + di, lj + dj, lk + dk, d.ny, d.nz)];
                 const float ww = a * b * c;
                 acc.x += ww * y.x;
                 acc.y += ww * y.y;
@@ -679,39 +719,66 @@ __global__ void k_vc_prolong(LevelView cv, int fnx, int fny, int fnz, const floa
     xf[f] = acc;
 }
 
-// Coarsest solve y = A_c^-1 b: one warp per row, lanes stride the row
-// (coalesced), shuffle reduction.  y is node-padded (4 floats per node).
-__global__ void __launch_bounds__(1024) k_vc_dense(int n, const float* __restrict__ ainv, const float* __restrict__ b,
-                                                   float* __restrict__ y4, const Control* ctl) {
+// Coarsest solve y = A_b^-1 b per block (CTA = block): one warp per row,
+// lanes stride the row (coalesced), shuffle reduction.  y is node-padded.
+__global__ void __launch_bounds__(1024) k_vc_dense(LevelView cv, const float* __restrict__ ainv,
+                                                   const float* __restrict__ b, float* __restrict__ y4,
+                                                   const Control* ctl) {
     if (ctl && ctl->all_done) return;
     __shared__ float sb[1024];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) sb[i] = b[i];
+    const BlkDev& d = cv.blk[blockIdx.x];
+    const int n = 3 * (d.nx + 1) * (d.ny + 1) * (d.nz + 1);
+    const float* bb = b + 3 * (size_t)d.node0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sb[i] = bb[i];
     __syncthreads();
+    const float* Ab = ainv + d.dense0;
+    float* yb = y4 + 4 * (size_t)d.node0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int row = warp; row < n; row += nw) {
-        const float* ar = ainv + (size_t)row * n;
+        const float* ar = Ab + (size_t)row * n;
         float acc = 0.f;
         for (int j = lane; j < n; j += 32) acc = fmaf(ar[j], sb[j], acc);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) y4[4 * (row / 3) + row % 3] = acc;
+        if (lane == 0) yb[4 * (row / 3) + row % 3] = acc;
     }
 }
 
-// Separable trilinear restriction, one axis per pass (z, then y, then x):
-// out[o] = sum_f w(f, m) in[f] along axis AX, m the output index on that
-// axis; output dims d0 x d1 x d2 (nodes), input extent in_n along AX.  The
-// last (x) pass writes the coarse right-hand side and, fused, the coarse
+// Separable trilinear restriction, one axis per pass (z, then y, then x),
+// over every block at once: out[o] = sum_f w(f, m) in[f] along axis AX, m the
+// output index on that axis.  Per block the output dims are
+//   AX = 2: (fnx+1) x (fny+1) x (nz+1) at t1_0, input the fine level at fnode0;
+//   AX = 1: (fnx+1) x (ny+1)  x (nz+1) at t2_0, input t1 at t1_0;
+//   AX = 0: (nx+1)  x (ny+1)  x (nz+1) at node0, input t2 at t2_0.
+// The last (x) pass writes the coarse right-hand side and, fused, the coarse
 // level's first smoothing sweep x4 = B^-1 b.
 template <int AX>
-__global__ void k_vc_restrict_axis(int d0, int d1, int d2, int in_n, const int32_t* __restrict__ xs,
-                                   const int32_t* __restrict__ lo, const float* __restrict__ w, int n_c,
+__global__ void k_vc_restrict_axis(LevelView cv, const int32_t* __restrict__ pre_out, int n_out,
                                    const float* __restrict__ in, float* __restrict__ out,
                                    const float* __restrict__ binv, float4* __restrict__ x4, const Control* ctl) {
     if (ctl && ctl->all_done) return;
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= d0 * d1 * d2) return;
-    const int i0 = o / (d1 * d2), i1 = (o / d2) % d1, i2 = o % d2;
+    if (o >= n_out) return;
+    const BlkDev& d = cv.blk[find_blk(pre_out, cv.n_blk, o)];
+    int d0, d1, d2, in_n, n_c, in0, o0;
+    const int32_t *xs, *lo;
+    const float* w;
+    if (AX == 2) {
+        d0 = d.fnx + 1; d1 = d.fny + 1; d2 = d.nz + 1; in_n = d.fnz + 1; n_c = d.nz;
+        in0 = d.fnode0; o0 = d.t1_0;
+        xs = cv.xs + d.ox2; lo = cv.lo + d.ol2; w = cv.w + d.ol2;
+    } else if (AX == 1) {
+        d0 = d.fnx + 1; d1 = d.ny + 1; d2 = d.nz + 1; in_n = d.fny + 1; n_c = d.ny;
+        in0 = d.t1_0; o0 = d.t2_0;
+        xs = cv.xs + d.ox1; lo = cv.lo + d.ol1; w = cv.w + d.ol1;
+    } else {
+        d0 = d.nx + 1; d1 = d.ny + 1; d2 = d.nz + 1; in_n = d.fnx + 1; n_c = d.nx;
+        in0 = d.t2_0; o0 = d.node0;
+        xs = cv.xs + d.ox0; lo = cv.lo + d.ol0; w = cv.w + d.ol0;
+    }
+    (void)d0;
+    const int ol = o - o0;
+    const int i0 = ol / (d1 * d2), i1 = (ol / d2) % d1, i2 = ol % d2;
     const int m = (AX == 0) ? i0 : (AX == 1) ? i1 : i2;
     const int f_lo = xs[max(m - 1, 0)], f_hi = xs[min(m + 1, n_c)];
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
@@ -722,13 +789,14 @@ __global__ void k_vc_restrict_axis(int d0, int d1, int d2, int in_n, const int32
         if (AX == 0) src = (f * d1 + i1) * d2 + i2;
         else if (AX == 1) src = (i0 * in_n + f) * d2 + i2;
         else src = (i0 * d1 + i1) * in_n + f;
-        s0 = fmaf(wf, in[3 * src], s0);
-        s1 = fmaf(wf, in[3 * src + 1], s1);
-        s2 = fmaf(wf, in[3 * src + 2], s2);
+        src += in0;
+        s0 = fmaf(wf, in[3 * (size_t)src], s0);
+        s1 = fmaf(wf, in[3 * (size_t)src + 1], s1);
+        s2 = fmaf(wf, in[3 * (size_t)src + 2], s2);
     }
-    out[3 * o] = s0;
-    out[3 * o + 1] = s1;
-    out[3 * o + 2] = s2;
+    out[3 * (size_t)o] = s0;
+    out[3 * (size_t)o + 1] = s1;
+    out[3 * (size_t)o + 2] = s2;
     if (AX == 0 && binv) {
         const float* B = binv + 9 * (size_t)o;
         x4[o] = make_float4(B[0] * s0 + B[1] * s1 + B[2] * s2, B[3] * s0 + B[4] * s1 + B[5] * s2,
@@ -737,7 +805,8 @@ __global__ void k_vc_restrict_axis(int d0, int d1, int d2, int in_n, const int32
 }
 
 // ---------------------------------------------------------------------------
-// multigrid-preconditioned flexible CG kernels (one right-hand side)
+// multigrid-preconditioned flexible CG kernels (one right-hand side; every
+// instance of a batched stack at once, with its own scalars and tickets)
 // ---------------------------------------------------------------------------
 struct MgPcg {
     PcgArgs a;            // outer operator, x, r, p, ap, partials, sc, ctl (nrhs = 1)
@@ -745,7 +814,29 @@ struct MgPcg {
     const float4* z;      // V-cycle output (level-0 y4)
     const float* binv0;   // level-0 smoother blocks: the first sweep
     float4* x40;          // x4 = B^-1 r is fused into the kernels writing b0
+    int n_inst;           // instances (1: a single model)
 };
+
+// Instances still iterating are counted in ctl->pad[0]; the one whose
+// recurrence converges last sets all_done, which ends every kernel of the
+// remaining captured iterations at once.
+__device__ __forceinline__ void retire_instance(const PcgArgs& A) {
+    if (atomicSub(&A.ctl->pad[0], 1) == 1) A.ctl->all_done = 1;
+}
+
+// First kernel of a captured chunk of iterations: count the instances not
+// done (all_done when none is left).
+__global__ void k_mg_count_active(MgPcg M) {
+    const PcgArgs& A = M.a;
+    int n = 0;
+    for (int i = threadIdx.x; i < M.n_inst; i += blockDim.x) n += A.sc[(size_t)i * kMaxRhs].done ? 0 : 1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+    if (threadIdx.x == 0) {
+        A.ctl->pad[0] = n;
+        A.ctl->all_done = (n == 0) ? 1 : 0;
+    }
+}
 
 __device__ __forceinline__ void fused_smooth0(const MgPcg& M, int row, const double (&r)[3]) {
     const float* B = M.binv0 + 9 * (size_t)row;
@@ -756,18 +847,20 @@ __device__ __forceinline__ void fused_smooth0(const MgPcg& M, int row, const dou
 
 template <typename TV, typename TP>
 __global__ void __launch_bounds__(kThreads) k_mg_spmv_dot(MgPcg M) {
+    using PV = typename ApOf<TP>::T;
     const PcgArgs& A = M.a;
-    if (A.ctl->all_done) return;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (cta_done<1>(A, S)) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     double d[1][1] = {{0.0}};
     if (row < A.n_rows) {
-        TP y[1][3];
+        PV y[1][3];
         const TV* vals;
         if constexpr (sizeof(TV) == 4) vals = A.v32; else vals = A.v64;
         spmv_row<TV, TP, 1>(row, A, vals, A.p, y);
-        TP pv[3];
+        PV pv[3];
         PadVec<TP>::load(A.p, row, pv);
-        TP* ap = reinterpret_cast<TP*>(A.ap) + 3 * (size_t)row;
+        PV* ap = reinterpret_cast<PV*>(A.ap) + 3 * (size_t)row;
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             ap[q] = y[0][q];
@@ -776,7 +869,7 @@ __global__ void __launch_bounds__(kThreads) k_mg_spmv_dot(MgPcg M) {
     }
     double tot[1][1];
     if (last_block_reduce<1, 1>(A, d, 0, tot) && threadIdx.x == 0) {
-        RhsScalars& s = A.sc[0];
+        RhsScalars& s = S[0];
         s.pAp = tot[0][0];
         s.alpha = s.rz / s.pAp;
     }
@@ -784,15 +877,17 @@ __global__ void __launch_bounds__(kThreads) k_mg_spmv_dot(MgPcg M) {
 
 template <typename TP>
 __global__ void __launch_bounds__(kThreads) k_mg_update_xr(MgPcg M) {
+    using PV = typename ApOf<TP>::T;
     const PcgArgs& A = M.a;
-    if (A.ctl->all_done) return;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (cta_done<1>(A, S)) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     double d[1][1] = {{0.0}};
     if (row < A.n_rows) {
-        const double alpha = A.sc[0].alpha;
-        TP pv[3];
+        const double alpha = S[0].alpha;
+        PV pv[3];
         PadVec<TP>::load(A.p, row, pv);
-        const TP* ap = reinterpret_cast<const TP*>(A.ap) + 3 * (size_t)row;
+        const PV* ap = reinterpret_cast<const PV*>(A.ap) + 3 * (size_t)row;
         double rr[3];
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
@@ -808,7 +903,7 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_xr(MgPcg M) {
     }
     double tot[1][1];
     if (last_block_reduce<1, 1>(A, d, 1, tot) && threadIdx.x == 0) {
-        RhsScalars& s = A.sc[0];
+        RhsScalars& s = S[0];
         s.rr = tot[0][0];
         s.iter += 1;
         if (!isfinite(s.rr)) {
@@ -816,61 +911,80 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_xr(MgPcg M) {
             s.done = 1;
         } else if (s.rr <= s.target) {
             s.done = 1;
+            s.restart = 1;  // this iteration's p update is skipped
         }
-        if (s.done) A.ctl->all_done = 1;
+        if (s.done) retire_instance(A);
     }
 }
 
 // mode 0: after an iteration's V-cycle -> beta (Polak-Ribiere), rz
-// mode 1: initialisation, or a restart after a replacement -> p = z, rz
-// mode 2: after a residual replacement -> rz only
+// mode 1: start of the solve, or after a true-residual evaluation: for every
+//         instance whose refresh flag is set, rz, and p = z when its restart
+//         flag is set (initialisation, or convergence of the recurrence)
 template <typename TP>
 __global__ void __launch_bounds__(kThreads) k_mg_rz(MgPcg M, int mode) {
+    using PV = typename ApOf<TP>::T;
     const PcgArgs& A = M.a;
-    if (mode == 0 && A.ctl->all_done) return;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (mode == 0 && cta_done<1>(A, S)) return;
+    if (mode == 1 && !S[0].refresh) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     double d[1][2] = {{0.0, 0.0}};
     if (row < A.n_rows) {
         const float4 z = M.z[row];
         const double zz[3] = {z.x, z.y, z.z};
-        const TP* ap = reinterpret_cast<const TP*>(A.ap) + 3 * (size_t)row;
+        const PV* ap = reinterpret_cast<const PV*>(A.ap) + 3 * (size_t)row;
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             d[0][0] += zz[q] * A.r[3 * (size_t)row + q];
             if (mode == 0) d[0][1] += zz[q] * (double)ap[q];
         }
-        if (mode == 1) PadVec<TP>::store(A.p, row, zz);
+        if (mode == 1 && S[0].restart) PadVec<TP>::store(A.p, row, zz);
     }
     double tot[1][2];
     if (last_block_reduce<1, 2>(A, d, 2, tot) && threadIdx.x == 0) {
-        RhsScalars& s = A.sc[0];
+        RhsScalars& s = S[0];
         if (mode == 0) s.beta = -s.alpha * tot[0][1] / s.rz;
         s.rz = tot[0][0];
+        if (mode == 1) {
+            s.refresh = 0;
+            s.restart = 0;
+        }
         if (!isfinite(s.rz)) {
             s.nonfinite = 1;
-            s.done = 1;
-            A.ctl->all_done = 1;
+            if (!s.done) {
+                s.done = 1;
+                if (mode == 0) retire_instance(A);
+            }
+            s.finished = 1;
         }
     }
 }
 
 template <typename TP>
 __global__ void __launch_bounds__(kThreads) k_mg_update_p(MgPcg M) {
+    using PV = typename ApOf<TP>::T;
     const PcgArgs& A = M.a;
-    if (A.ctl->all_done) return;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (cta_done<1>(A, S)) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= A.n_rows) return;
-    const double beta = A.sc[0].beta;
+    const double beta = S[0].beta;
     const float4 z = M.z[row];
-    TP pv[3];
+    PV pv[3];
     PadVec<TP>::load(A.p, row, pv);
     const double pn[3] = {z.x + beta * (double)pv[0], z.y + beta * (double)pv[1], z.z + beta * (double)pv[2]};
     PadVec<TP>::store(A.p, row, pn);
 }
 
-// FP64 true residual r = f - A64 x, b0 = float(r); stats into sc (rr, bb).
+// FP64 true residual r = f - A64 x, b0 = float(r) for every instance
+// (init = 1: also |f|^2, the target and fresh recurrence state) or for the
+// instances whose replace flag is set (init = 0).  Marks them for the rz /
+// direction refresh that follows the next V-cycle.
 __global__ void __launch_bounds__(kThreads) k_mg_residual(MgPcg M, int init, double tol2) {
     const PcgArgs& A = M.a;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (!init && !S[0].replace) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = row & 31;
     double d[1][2] = {{0.0, 0.0}};
@@ -886,22 +1000,19 @@ __global__ void __launch_bounds__(kThreads) k_mg_residual(MgPcg M, int init, dou
 #pragma unroll
             for (int a = 0; a < 3; ++a) y[a] = fma(v[(a * 3) * 32], x0, fma(v[(a * 3 + 1) * 32], x1, fma(v[(a * 3 + 2) * 32], x2, y[a])));
         }
-        double rr[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const size_t o = 3 * (size_t)row + a;
             const double rv = A.f[o] - y[a];
             A.r[o] = rv;
             M.b0[o] = (float)rv;
-            rr[a] = rv;
             d[0][0] += rv * rv;
             d[0][1] += A.f[o] * A.f[o];
         }
-        fused_smooth0(M, row, rr);
     }
     double tot[1][2];
     if (last_block_reduce<1, 2>(A, d, 3, tot) && threadIdx.x == 0) {
-        RhsScalars& s = A.sc[0];
+        RhsScalars& s = S[0];
         s.rr = tot[0][0];
         s.rr_last_true = tot[0][0];
         if (init) {
@@ -909,11 +1020,13 @@ __global__ void __launch_bounds__(kThreads) k_mg_residual(MgPcg M, int init, dou
             s.target = tol2 * s.bb;
             s.iter = 0;
             s.beta = 0.0;
+            s.restart = 1;
         }
+        s.replace = 0;
+        s.refresh = 1;
         s.nonfinite = isfinite(s.rr) ? 0 : 1;
         s.finished = (s.rr <= s.target) || s.nonfinite;
         s.done = s.finished;
-        A.ctl->all_done = s.done;
     }
 }
 
@@ -940,23 +1053,28 @@ MgAxis make_axis(int n_f, bool coarsen) {
     return a;
 }
 
+// SBELL pattern, element connectivity, slot map and parity colouring of a
+// level made of the blocks L.blk (nodes and elements numbered block by block;
+// elements of different blocks share no node).
 void level_pattern(Ctx& c, MgLevel& L) {
     const int N = L.n_nodes;
     std::vector<std::vector<int32_t>> adj(N);
-    auto id = [&](int i, int j, int k) { return (i * (L.ny + 1) + j) * (L.nz + 1) + k; };
-    for (int i = 0; i <= L.nx; ++i)
-        for (int j = 0; j <= L.ny; ++j)
-            for (int k = 0; k <= L.nz; ++k) {
-                auto& v = adj[id(i, j, k)];
-                for (int di = -1; di <= 1; ++di)
-                    for (int dj = -1; dj <= 1; ++dj)
-                        for (int dk = -1; dk <= 1; ++dk) {
-                            const int a = i + di, b = j + dj, q = k + dk;
-                            if (a < 0 || b < 0 || q < 0 || a > L.nx || b > L.ny || q > L.nz) continue;
-                            v.push_back(id(a, b, q));
-                        }
-                std::sort(v.begin(), v.end());
-            }
+    for (const MgBlk& B : L.blk) {
+        auto id = [&](int i, int j, int k) { return B.node0 + (i * (B.ny + 1) + j) * (B.nz + 1) + k; };
+        for (int i = 0; i <= B.nx; ++i)
+            for (int j = 0; j <= B.ny; ++j)
+                for (int k = 0; k <= B.nz; ++k) {
+                    auto& v = adj[id(i, j, k)];
+                    for (int di = -1; di <= 1; ++di)
+                        for (int dj = -1; dj <= 1; ++dj)
+                            for (int dk = -1; dk <= 1; ++dk) {
+                                const int a = i + di, b = j + dj, q = k + dk;
+                                if (a < 0 || b < 0 || q < 0 || a > B.nx || b > B.ny || q > B.nz) continue;
+                                v.push_back(id(a, b, q));
+                            }
+                    std::sort(v.begin(), v.end());
+                }
+    }
     Sbell& A = L.own;
     A.b = 3;
     A.n_rows = N;
@@ -985,22 +1103,26 @@ void level_pattern(Ctx& c, MgLevel& L) {
     std::vector<int32_t> conn((size_t)L.n_el * 8), slot((size_t)L.n_el * 64);
     const int co[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
     std::vector<std::vector<int32_t>> colour(8);
-    for (int i = 0; i < L.nx; ++i)
-        for (int j = 0; j < L.ny; ++j)
-            for (int k = 0; k < L.nz; ++k) {
-                const int e = (i * L.ny + j) * L.nz + k;
-                for (int a = 0; a < 8; ++a) conn[(size_t)e * 8 + a] = id(i + co[a][0], j + co[a][1], k + co[a][2]);
-                for (int a = 0; a < 8; ++a) {
-                    const int ra = conn[(size_t)e * 8 + a];
-                    for (int b = 0; b < 8; ++b) {
-                        const int cb = conn[(size_t)e * 8 + b];
-                        const auto& v = adj[ra];
-                        const int p = (int)(std::lower_bound(v.begin(), v.end(), cb) - v.begin());
-                        slot[(size_t)e * 64 + a * 8 + b] = (int32_t)A.slot(ra, p);
+    for (const MgBlk& B : L.blk) {
+        auto id = [&](int i, int j, int k) { return B.node0 + (i * (B.ny + 1) + j) * (B.nz + 1) + k; };
+        for (int i = 0; i < B.nx; ++i)
+            for (int j = 0; j < B.ny; ++j)
+                for (int k = 0; k < B.nz; ++k) {
+                    const int e = B.el0 + (i * B.ny + j) * B.nz + k;
+                    for (int a = 0; a < 8; ++a)
+                        conn[(size_t)e * 8 + a] = id(i + co[a][0], j + co[a][1], k + co[a][2]);
+                    for (int a = 0; a < 8; ++a) {
+                        const int ra = conn[(size_t)e * 8 + a];
+                        for (int b = 0; b < 8; ++b) {
+                            const int cb = conn[(size_t)e * 8 + b];
+                            const auto& v = adj[ra];
+                            const int p = (int)(std::lower_bound(v.begin(), v.end(), cb) - v.begin());
+                            slot[(size_t)e * 64 + a * 8 + b] = (int32_t)A.slot(ra, p);
+                        }
                     }
+                    colour[(i & 1) * 4 + (j & 1) * 2 + (k & 1)].push_back(e);
                 }
-                colour[(i & 1) * 4 + (j & 1) * 2 + (k & 1)].push_back(e);
-            }
+    }
     std::vector<int32_t> ce;
     L.colour_ptr.assign(1, 0);
     for (auto& cl : colour) {
@@ -1018,20 +1140,63 @@ void level_pattern(Ctx& c, MgLevel& L) {
     L.A = &L.own;
 }
 
+// Device block descriptors and per-block start tables of level l (levels
+// >= 1 also describe the finer level's blocks).
+void level_tables(Ctx& c, MgHierarchy& H, int l) {
+    MgLevel& L = *H.L[l];
+    const MgLevel* F = l > 0 ? H.L[l - 1].get() : nullptr;
+    const int nb = (int)L.blk.size();
+    std::vector<BlkDev> dv(nb);
+    std::vector<int32_t> pn(nb + 1), pe(nb + 1), p1(nb + 1), p2(nb + 1);
+    for (int b = 0; b < nb; ++b) {
+        const MgBlk& B = L.blk[b];
+        BlkDev& d = dv[b];
+        std::memset(&d, 0, sizeof(d));
+        d.nx = B.nx;
+        d.ny = B.ny;
+        d.nz = B.nz;
+        d.node0 = B.node0;
+        d.el0 = B.el0;
+        if (F) {
+            const MgBlk& P = F->blk[b];
+            d.fnx = P.nx;
+            d.fny = P.ny;
+            d.fnz = P.nz;
+            d.fnode0 = P.node0;
+            d.fel0 = P.el0;
+        }
+        d.ox0 = B.ox[0];
+        d.ox1 = B.ox[1];
+        d.ox2 = B.ox[2];
+        d.ol0 = B.ol[0];
+        d.ol1 = B.ol[1];
+        d.ol2 = B.ol[2];
+        d.t1_0 = B.t1_0;
+        d.t2_0 = B.t2_0;
+        d.dense0 = (l + 1 == (int)H.L.size() && !H.h_dense0.empty()) ? H.h_dense0[b] : 0;
+        pn[b] = B.node0;
+        pe[b] = B.el0;
+        p1[b] = B.t1_0;
+        p2[b] = B.t2_0;
+    }
+    pn[nb] = L.n_nodes;
+    pe[nb] = L.n_el;
+    p1[nb] = L.n_t1;
+    p2[nb] = L.n_t2;
+    L.d_blk.upload(dv, c.stream);
+    L.pre_node.upload(pn, c.stream);
+    L.pre_el.upload(pe, c.stream);
+    L.pre_t1.upload(p1, c.stream);
+    L.pre_t2.upload(p2, c.stream);
+}
+
 LevelView view_of(const MgLevel& L) {
     LevelView v{};
-    v.nx = L.nx;
-    v.ny = L.ny;
-    v.nz = L.nz;
+    v.n_blk = (int)L.blk.size();
+    v.blk = L.d_blk.p;
     v.xs = L.d_xs.p;
     v.lo = L.d_lo.p;
     v.w = L.d_w.p;
-    v.ox0 = L.ox[0];
-    v.ox1 = L.ox[1];
-    v.ox2 = L.ox[2];
-    v.ol0 = L.ol[0];
-    v.ol1 = L.ol[1];
-    v.ol2 = L.ol[2];
     return v;
 }
 
@@ -1039,105 +1204,170 @@ SbView sbview(const MgLevel& L) {
     return SbView{L.A->n_rows, L.A->slice_off.p, L.A->row_len.p, L.A->col.p, L.A->v32.p};
 }
 
-void build_hierarchy(Ctx& c) {
-    if ((c.type != 8 && c.type != 81) || c.bx <= 0)
-        throw InputError("multigrid needs a structured hex8 / brickIM block (asend_set_block_structure)");
-    auto H = std::make_shared<MgHierarchy>();
-    auto L0 = std::make_unique<MgLevel>();
-    L0->nx = c.bx;
-    L0->ny = c.by;
-    L0->nz = c.bz;
-    L0->n_nodes = c.n_nodes;
-    L0->n_el = c.n_el;
-    L0->n_dof = c.n_dof;
-    L0->A = &c.A;
-    // level-0 lumped penalty (coef^2 per constrained DOF)
-    L0->h_pen.assign(c.n_dof, 0.f);
-    for (size_t r = 0; r + 1 < c.c_ptr.size(); ++r)
-        for (int k = c.c_ptr[r]; k < c.c_ptr[r + 1]; ++k) L0->h_pen[c.c_dof[k]] += (float)(c.c_coef[k] * c.c_coef[k]);
-    H->L.push_back(std::move(L0));
-    // element spacing per axis at level 0 (block node numbering)
-    double h[3];
-    {
-        const int n100 = (c.by + 1) * (c.bz + 1), n010 = c.bz + 1, n001 = 1;
+// Level-0 blocks: the declared structured block, or one block per instance
+// of a batched stack (asend_set_instance_blocks).
+std::vector<MgBlk> level0_blocks(const Ctx& c) {
+    std::vector<MgBlk> out;
+    auto spacing = [&](MgBlk& B) {
+        const int n100 = (B.ny + 1) * (B.nz + 1), n010 = B.nz + 1, n001 = 1;
         const int nb[3] = {n100, n010, n001};
         for (int ax = 0; ax < 3; ++ax) {
             double d2 = 0.0;
             for (int j = 0; j < 3; ++j) {
-                const double d = c.xyz[3 * (size_t)nb[ax] + j] - c.xyz[j];
+                const double d = c.xyz[3 * (size_t)(B.node0 + nb[ax]) + j] - c.xyz[3 * (size_t)B.node0 + j];
                 d2 += d * d;
             }
-            h[ax] = std::sqrt(d2);
+            B.h[ax] = std::sqrt(d2);
         }
+    };
+    if (!c.inst_dims.empty()) {
+        int el0 = 0;
+        for (int i = 0; i < c.n_inst; ++i) {
+            MgBlk B;
+            B.nx = c.inst_dims[3 * i];
+            B.ny = c.inst_dims[3 * i + 1];
+            B.nz = c.inst_dims[3 * i + 2];
+            B.node0 = c.inst_node_ptr[i];
+            B.el0 = el0;
+            el0 += B.n_el();
+            spacing(B);
+            out.push_back(B);
+        }
+    } else if (c.bx > 0) {
+        MgBlk B;
+        B.nx = c.bx;
+        B.ny = c.by;
+        B.nz = c.bz;
+        spacing(B);
+        out.push_back(B);
     }
+    return out;
+}
+
+void build_hierarchy(Ctx& c) {
+    if (c.type != 8 && c.type != 81)
+        throw InputError("multigrid needs structured hex8 / brickIM blocks (asend_set_block_structure or "
+                         "asend_set_instance_blocks)");
+    std::vector<MgBlk> b0 = level0_blocks(c);
+    if (b0.empty())
+        throw InputError("multigrid needs structured hex8 / brickIM blocks (asend_set_block_structure or "
+                         "asend_set_instance_blocks)");
+    auto H = std::make_shared<MgHierarchy>();
+    H->n_blk = (int)b0.size();
+    auto L0 = std::make_unique<MgLevel>();
+    L0->n_nodes = c.n_nodes;
+    L0->n_el = c.n_el;
+    L0->n_dof = c.n_dof;
+    L0->blk = b0;
+    L0->A = &c.A;
+    // level-0 lumped penalty (coef^2 per constrained DOF, in units of the instance's scale)
+    L0->h_pen.assign(c.n_dof, 0.f);
+    for (size_t r = 0; r + 1 < c.c_ptr.size(); ++r)
+        for (int k = c.c_ptr[r]; k < c.c_ptr[r + 1]; ++k) L0->h_pen[c.c_dof[k]] += (float)(c.c_coef[k] * c.c_coef[k]);
+    H->L.push_back(std::move(L0));
     for (;;) {
         MgLevel& F = *H->L.back();
-        // coarsest level: an explicit inverse (<= 256 DOF)
-        if (F.n_dof <= 256 || (F.nx <= 1 && F.ny <= 1 && F.nz <= 1)) break;
-        auto L = std::make_unique<MgLevel>();
-        const int nf[3] = {F.nx, F.ny, F.nz};
-        // semi-coarsening: coarsen only the axes whose spacing is within a
+        // Per block: the coarsest grid is solved directly (<= 256 DOF);
+        // semi-coarsening coarsens only the axes whose spacing is within a
         // factor sqrt(2) of the smallest (the strongly coupled directions of
-        // stretched elements); the others wait until the cells are isotropic
-        // An axis two cells thick is coarsened to one cell only once every
-        // axis is that thin: a one-cell-thick coarse grid of a deep bar is a
-        // poor coarse space.
-        const bool all_thin = nf[0] <= 2 && nf[1] <= 2 && nf[2] <= 2;
-        auto eligible = [&](int ax) { return nf[ax] >= 2 && (nf[ax] > 2 || all_thin); };
-        double hmin = 1e300;
-        for (int ax = 0; ax < 3; ++ax)
-            if (eligible(ax)) hmin = std::min(hmin, h[ax]);
-        bool any = false;
-        for (int ax = 0; ax < 3; ++ax) {
-            const bool coarsen = eligible(ax) && h[ax] <= 1.4142135623730951 * hmin;
-            any |= coarsen;
-            L->ax[ax] = make_axis(nf[ax], coarsen);
-            h[ax] *= (double)nf[ax] / (double)L->ax[ax].n_c;
+        // stretched elements), the others wait until the cells are
+        // isotropic.  An axis two cells thick is coarsened to one cell only
+        // once every axis is that thin: a one-cell-thick coarse grid of a
+        // deep bar is a poor coarse space.  A block that is done is carried
+        // down unchanged while other blocks still coarsen.
+        const int nb = (int)F.blk.size();
+        std::vector<std::array<bool, 3>> co(nb);
+        bool any_block = false;
+        for (int b = 0; b < nb; ++b) {
+            const MgBlk& P = F.blk[b];
+            co[b] = {false, false, false};
+            if (P.done || 3 * P.n_nodes() <= 256 || (P.nx <= 1 && P.ny <= 1 && P.nz <= 1)) continue;
+            const int nf[3] = {P.nx, P.ny, P.nz};
+            const bool all_thin = nf[0] <= 2 && nf[1] <= 2 && nf[2] <= 2;
+            auto eligible = [&](int ax) { return nf[ax] >= 2 && (nf[ax] > 2 || all_thin); };
+            double hmin = 1e300;
+            for (int ax = 0; ax < 3; ++ax)
+                if (eligible(ax)) hmin = std::min(hmin, P.h[ax]);
+            for (int ax = 0; ax < 3; ++ax) {
+                co[b][ax] = eligible(ax) && P.h[ax] <= 1.4142135623730951 * hmin;
+                any_block |= co[b][ax];
+            }
         }
-        if (!any) break;
-        L->nx = L->ax[0].n_c;
-        L->ny = L->ax[1].n_c;
-        L->nz = L->ax[2].n_c;
-        L->n_nodes = (L->nx + 1) * (L->ny + 1) * (L->nz + 1);
-        L->n_el = L->nx * L->ny * L->nz;
-        L->n_dof = 3 * L->n_nodes;
+        if (!any_block) break;
+        auto L = std::make_unique<MgLevel>();
         std::vector<int32_t> xs, lo;
         std::vector<float> w;
-        for (int ax = 0; ax < 3; ++ax) {
-            L->ox[ax] = (int)xs.size();
-            L->ol[ax] = (int)lo.size();
-            xs.insert(xs.end(), L->ax[ax].xs.begin(), L->ax[ax].xs.end());
-            lo.insert(lo.end(), L->ax[ax].lo.begin(), L->ax[ax].lo.end());
-            w.insert(w.end(), L->ax[ax].w.begin(), L->ax[ax].w.end());
+        int node0 = 0, el0 = 0, t1 = 0, t2 = 0;
+        for (int b = 0; b < nb; ++b) {
+            const MgBlk& P = F.blk[b];
+            MgBlk B;
+            const int nf[3] = {P.nx, P.ny, P.nz};
+            bool any = false;
+            for (int ax = 0; ax < 3; ++ax) {
+                B.ax[ax] = make_axis(nf[ax], co[b][ax]);
+                B.h[ax] = P.h[ax] * (double)nf[ax] / (double)B.ax[ax].n_c;
+                any |= co[b][ax];
+            }
+            B.done = !any;
+            B.nx = B.ax[0].n_c;
+            B.ny = B.ax[1].n_c;
+            B.nz = B.ax[2].n_c;
+            B.node0 = node0;
+            B.el0 = el0;
+            B.t1_0 = t1;
+            B.t2_0 = t2;
+            node0 += B.n_nodes();
+            el0 += B.n_el();
+            t1 += (P.nx + 1) * (P.ny + 1) * (B.nz + 1);
+            t2 += (P.nx + 1) * (B.ny + 1) * (B.nz + 1);
+            for (int ax = 0; ax < 3; ++ax) {
+                B.ox[ax] = (int)xs.size();
+                B.ol[ax] = (int)lo.size();
+                xs.insert(xs.end(), B.ax[ax].xs.begin(), B.ax[ax].xs.end());
+                lo.insert(lo.end(), B.ax[ax].lo.begin(), B.ax[ax].lo.end());
+                w.insert(w.end(), B.ax[ax].w.begin(), B.ax[ax].w.end());
+            }
+            L->blk.push_back(B);
         }
+        L->n_nodes = node0;
+        L->n_el = el0;
+        L->n_dof = 3 * node0;
+        L->n_t1 = t1;
+        L->n_t2 = t2;
         L->d_xs.upload(xs, c.stream);
         L->d_lo.upload(lo, c.stream);
         L->d_w.upload(w, c.stream);
         // lumped Galerkin penalty: pen_c[I] = sum_i w_iI pen_f[i]
         L->h_pen.assign(L->n_dof, 0.f);
-        for (int i = 0; i <= F.nx; ++i)
-            for (int j = 0; j <= F.ny; ++j)
-                for (int k = 0; k <= F.nz; ++k) {
-                    const int f = (i * (F.ny + 1) + j) * (F.nz + 1) + k;
-                    const float p0 = F.h_pen[3 * f], p1 = F.h_pen[3 * f + 1], p2 = F.h_pen[3 * f + 2];
-                    if (p0 == 0.f && p1 == 0.f && p2 == 0.f) continue;
-                    const int li[3] = {L->ax[0].lo[i], L->ax[1].lo[j], L->ax[2].lo[k]};
-                    const float wi[3] = {L->ax[0].w[i], L->ax[1].w[j], L->ax[2].w[k]};
-                    for (int d0 = 0; d0 < 2; ++d0)
-                        for (int d1 = 0; d1 < 2; ++d1)
-                            for (int d2 = 0; d2 < 2; ++d2) {
-                                const float ww = (d0 ? wi[0] : 1 - wi[0]) * (d1 ? wi[1] : 1 - wi[1]) * (d2 ? wi[2] : 1 - wi[2]);
-                                if (ww == 0.f) continue;
-                                const int I = ((li[0] + d0) * (L->ny + 1) + (li[1] + d1)) * (L->nz + 1) + (li[2] + d2);
-                                L->h_pen[3 * I] += ww * p0;
-                                L->h_pen[3 * I + 1] += ww * p1;
-                                L->h_pen[3 * I + 2] += ww * p2;
-                            }
-                }
+        for (int b = 0; b < nb; ++b) {
+            const MgBlk& P = F.blk[b];
+            const MgBlk& B = L->blk[b];
+            for (int i = 0; i <= P.nx; ++i)
+                for (int j = 0; j <= P.ny; ++j)
+                    for (int k = 0; k <= P.nz; ++k) {
+                        const int f = P.node0 + (i * (P.ny + 1) + j) * (P.nz + 1) + k;
+                        const float p0 = F.h_pen[3 * f], p1 = F.h_pen[3 * f + 1], p2 = F.h_pen[3 * f + 2];
+                        if (p0 == 0.f && p1 == 0.f && p2 == 0.f) continue;
+                        const int li[3] = {B.ax[0].lo[i], B.ax[1].lo[j], B.ax[2].lo[k]};
+                        const float wi[3] = {B.ax[0].w[i], B.ax[1].w[j], B.ax[2].w[k]};
+                        for (int d0 = 0; d0 < 2; ++d0)
+                            for (int d1 = 0; d1 < 2; ++d1)
+                                for (int d2 = 0; d2 < 2; ++d2) {
+                                    const float ww = (d0 ? wi[0] : 1 - wi[0]) * (d1 ? wi[1] : 1 - wi[1]) *
+                                                     (d2 ? wi[2] : 1 - wi[2]);
+                                    if (ww == 0.f) continue;
+                                    const int I = B.node0 +
+                                                  ((li[0] + d0) * (B.ny + 1) + (li[1] + d1)) * (B.nz + 1) + (li[2] + d2);
+                                    L->h_pen[3 * I] += ww * p0;
+                                    L->h_pen[3 * I + 1] += ww * p1;
+                                    L->h_pen[3 * I + 2] += ww * p2;
+                                }
+                    }
+        }
         level_pattern(c, *L);
         L->Ke.alloc((size_t)L->n_el * 576);
-        L->t1.alloc((size_t)3 * (F.nx + 1) * (F.ny + 1) * (L->nz + 1));
-        L->t2.alloc((size_t)3 * (F.nx + 1) * (L->ny + 1) * (L->nz + 1));
+        L->t1.alloc((size_t)3 * std::max(t1, 1));
+        L->t2.alloc((size_t)3 * std::max(t2, 1));
         H->L.push_back(std::move(L));
     }
     for (auto& Lp : H->L) {
@@ -1149,15 +1379,25 @@ void build_hierarchy(Ctx& c) {
         L.x4.alloc((size_t)4 * L.n_nodes);
         L.y4.alloc((size_t)4 * L.n_nodes);
     }
-    H->n_coarse = H->L.back()->n_dof;
+    // coarsest level: one dense block per instance
+    MgLevel& Lc = *H->L.back();
+    H->h_dense0.assign(H->n_blk, 0);
+    size_t dense_tot = 0;
+    H->n_coarse = 0;
+    for (int b = 0; b < H->n_blk; ++b) {
+        const int nd = 3 * Lc.blk[b].n_nodes();
+        H->h_dense0[b] = (int32_t)dense_tot;
+        dense_tot += (size_t)nd * nd;
+        H->n_coarse = std::max(H->n_coarse, nd);
+    }
     if (H->n_coarse > 1020) throw InputError("multigrid coarsest level too large");
-    H->dense.alloc((size_t)H->n_coarse * H->n_coarse);
+    if (dense_tot > (size_t)INT32_MAX) throw InputError("multigrid coarsest blocks too large");
+    H->dense.alloc(dense_tot);
+    for (int l = 0; l < (int)H->L.size(); ++l) level_tables(c, *H, l);
     ASEND_CUDA(cudaStreamSynchronize(c.stream));
     c.mg = H;
 }
 
-// omega * D^-1 on level l, omega = damping / lambda with lambda a
-// kPowSteps-step power-iteration estimate of the largest eigenvalue of D^-1 A
 void damp_smoother(Ctx& c, int l) {
     MgHierarchy& H = *c.mg;
     MgLevel& L = *H.L[l];
@@ -1193,7 +1433,7 @@ void damp_smoother(Ctx& c, int l) {
 }
 
 // per-assembly values: Galerkin element matrices, level operators, penalty,
-// smoother blocks, coarsest inverse
+// smoother blocks, coarsest inverses
 void setup_values(Ctx& c) {
     MgHierarchy& H = *c.mg;
     const int n_lev = (int)H.L.size();
@@ -1205,28 +1445,40 @@ void setup_values(Ctx& c) {
     H.pow_ticket.alloc((size_t)n_lev * kPowSteps);
     H.pow_part.alloc((size_t)grid_of(H.L[0]->n_nodes));
     {
+        std::vector<double> sf(H.n_blk, c.sf);
+        if (c.n_inst > 1 && (int)c.sf_inst.size() == H.n_blk) sf = c.sf_inst;
+        H.blk_sf.upload(sf, c.stream);
+    }
+    {
         MgLevel& L0 = *H.L[0];
         k_smoother_blocks<double><<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(L0.n_nodes, c.A.slice_off.p, c.A.diag.p,
                                                                             c.A.v64.p, 1.f, L0.binv.p);
         ++c.launches;
-        damp_smoother(c, 0);
+        if (n_lev > 1) damp_smoother(c, 0);
     }
     for (size_t l = 1; l < H.L.size(); ++l) {
         MgLevel& L = *H.L[l];
         MgLevel& F = *H.L[l - 1];
         const float* fine_ke = F.Ke.p;
+        const float* cls_ke = nullptr;
+        const int32_t* cls_of = nullptr;
         if (l == 1) {
-            // level 0: hex8 matrices are integrated inside k_coarsen; brickIM
-            // ones (condensed incompatible modes) are computed first
+            // level 0: K_e = E_e * (unit-modulus matrix of its geometry class)
+            // when the assembly keeps classes; otherwise hex8 matrices are
+            // integrated inside k_coarsen and brickIM ones (condensed
+            // incompatible modes) are computed first
             fine_ke = nullptr;
-            if (c.type == 81) {
+            if (c.cls_ke32.n && c.cls_type == c.type && c.ortho.empty()) {
+                cls_ke = c.cls_ke32.p;
+                cls_of = c.d_cls_of.p;
+            } else if (c.type == 81) {
                 F.Ke.alloc((size_t)c.n_el * 576);
                 brickim_element_ke32(c, F.Ke.p);
                 fine_ke = F.Ke.p;
             }
         }
-        k_coarsen<<<L.n_el, 512, 0, c.stream>>>(view_of(L), F.ny, F.nz, fine_ke, c.d_xyz.p, c.d_conn.p, c.d_E.p,
-                                                c.d_nu.p, L.Ke.p);
+        k_coarsen<<<L.n_el, 512, 0, c.stream>>>(view_of(L), L.pre_el.p, fine_ke, cls_ke, cls_of, c.d_xyz.p,
+                                                c.d_conn.p, c.d_E.p, c.d_nu.p, L.Ke.p);
         L.own.v32.zero(c.stream);
         for (size_t k = 0; k + 1 < L.colour_ptr.size(); ++k) {
             const int n = L.colour_ptr[k + 1] - L.colour_ptr[k];
@@ -1236,7 +1488,7 @@ void setup_values(Ctx& c) {
             ++c.launches;
         }
         k_add_pen<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(L.n_nodes, L.own.slice_off.p, L.own.diag.p, L.pen.p,
-                                                           (float)c.sf, L.own.v32.p);
+                                                           L.pre_node.p, (int)L.blk.size(), H.blk_sf.p, L.own.v32.p);
         k_smoother_blocks<float><<<grid_of(L.n_nodes), kT, 0, c.stream>>>(L.n_nodes, L.own.slice_off.p, L.own.diag.p,
                                                                           L.own.v32.p, 1.f, L.binv.p);
         c.launches += 3;
@@ -1244,18 +1496,49 @@ void setup_values(Ctx& c) {
     }
     MgLevel& Lc = *H.L.back();
     k_dense_build<<<Lc.n_nodes, 128, 0, c.stream>>>(Lc.n_nodes, Lc.A->slice_off.p, Lc.A->row_len.p, Lc.A->col.p,
-                                                    Lc.A->v32.p, H.dense.p);
+                                                    Lc.A->v32.p, view_of(Lc), Lc.pre_node.p, H.dense.p);
     const size_t gj_smem = sizeof(float) * (size_t)H.n_coarse * H.n_coarse;
-    const bool in_smem = gj_smem <= 220 * 1024;
+    const bool in_smem = H.n_coarse <= 234;
     if (in_smem)
         ASEND_CUDA(cudaFuncSetAttribute(k_gauss_jordan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gj_smem));
-    k_gauss_jordan<<<1, 1024, in_smem ? gj_smem : 0, c.stream>>>(H.n_coarse, H.dense.p, in_smem ? 1 : 0);
+    k_gauss_jordan<<<H.n_blk, 1024, in_smem ? gj_smem : 0, c.stream>>>(view_of(Lc), H.dense.p, in_smem ? 1 : 0);
     c.launches += 2;
     ASEND_CUDA(cudaGetLastError());
     H.epoch = c.assembly_epoch;
 }
 
-// z = V-cycle(b0) (levels' b of level 0 must hold the input)
+// Restriction of level l's residual r to level l + 1's right-hand side b (and
+// its first smoothing sweep, unless l + 1 is the coarsest level).
+void restrict_to(Ctx& c, int l, const Control* ctl) {
+    MgHierarchy& H = *c.mg;
+    MgLevel& L = *H.L[l];
+    MgLevel& C = *H.L[l + 1];
+    const bool last = (l + 2 == (int)H.L.size());  // the coarsest level is solved directly: no sweep
+    const LevelView cv = view_of(C);
+    k_vc_restrict_axis<2><<<grid_of(C.n_t1), kT, 0, c.stream>>>(cv, C.pre_t1.p, C.n_t1, L.r.p, C.t1.p, nullptr,
+                                                                 nullptr, ctl);
+    k_vc_restrict_axis<1><<<grid_of(C.n_t2), kT, 0, c.stream>>>(cv, C.pre_t2.p, C.n_t2, C.t1.p, C.t2.p, nullptr,
+                                                                 nullptr, ctl);
+    k_vc_restrict_axis<0><<<grid_of(C.n_nodes), kT, 0, c.stream>>>(cv, C.pre_node.p, C.n_nodes, C.t2.p, C.b.p,
+                                                                    last ? nullptr : C.binv.p,
+                                                                    reinterpret_cast<float4*>(C.x4.p), ctl);
+}
+
+void coarsest_solve(Ctx& c, const Control* ctl) {
+    MgHierarchy& H = *c.mg;
+    MgLevel& Lc = *H.L.back();
+    k_vc_dense<<<H.n_blk, 1024, 0, c.stream>>>(view_of(Lc), H.dense.p, Lc.b.p, Lc.y4.p, ctl);
+}
+
+void prolong_from(Ctx& c, int l, const Control* ctl) {
+    MgHierarchy& H = *c.mg;
+    MgLevel& L = *H.L[l];
+    MgLevel& C = *H.L[l + 1];
+    k_vc_prolong<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(view_of(C), L.pre_node.p, L.n_nodes,
+                                                          reinterpret_cast<const float4*>(C.y4.p),
+                                                          reinterpret_cast<float4*>(L.x4.p), ctl);
+}
+
 // One V(1,1) cycle on level 0's b.  With fused0, the caller has already
 // written level 0's first sweep x4 = B^-1 b (fused into the PCG update).
 void vcycle(Ctx& c, const Control* ctl, bool fused0) {
@@ -1268,29 +1551,14 @@ void vcycle(Ctx& c, const Control* ctl, bool fused0) {
     }
     for (int l = 0; l < nl - 1; ++l) {
         MgLevel& L = *H.L[l];
-        MgLevel& C = *H.L[l + 1];
         k_vc_resid<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(sbview(L), L.b.p, reinterpret_cast<float4*>(L.x4.p), L.r.p,
                                                             ctl);
-        const bool last = (l + 1 == nl - 1);  // the coarsest level is solved directly: no sweep
-        const int n1 = (L.nx + 1) * (L.ny + 1) * (C.nz + 1), n2 = (L.nx + 1) * (C.ny + 1) * (C.nz + 1);
-        k_vc_restrict_axis<2><<<grid_of(n1), kT, 0, c.stream>>>(
-            L.nx + 1, L.ny + 1, C.nz + 1, L.nz + 1, C.d_xs.p + C.ox[2], C.d_lo.p + C.ol[2], C.d_w.p + C.ol[2], C.nz,
-            L.r.p, C.t1.p, nullptr, nullptr, ctl);
-        k_vc_restrict_axis<1><<<grid_of(n2), kT, 0, c.stream>>>(
-            L.nx + 1, C.ny + 1, C.nz + 1, L.ny + 1, C.d_xs.p + C.ox[1], C.d_lo.p + C.ol[1], C.d_w.p + C.ol[1], C.ny,
-            C.t1.p, C.t2.p, nullptr, nullptr, ctl);
-        k_vc_restrict_axis<0><<<grid_of(C.n_nodes), kT, 0, c.stream>>>(
-            C.nx + 1, C.ny + 1, C.nz + 1, L.nx + 1, C.d_xs.p + C.ox[0], C.d_lo.p + C.ol[0], C.d_w.p + C.ol[0], C.nx,
-            C.t2.p, C.b.p, last ? nullptr : C.binv.p, reinterpret_cast<float4*>(C.x4.p), ctl);
+        restrict_to(c, l, ctl);
     }
-    MgLevel& Lc = *H.L.back();
-    k_vc_dense<<<1, 1024, 0, c.stream>>>(H.n_coarse, H.dense.p, Lc.b.p, Lc.y4.p, ctl);
+    coarsest_solve(c, ctl);
     for (int l = nl - 2; l >= 0; --l) {
         MgLevel& L = *H.L[l];
-        MgLevel& C = *H.L[l + 1];
-        k_vc_prolong<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(view_of(C), L.nx, L.ny, L.nz,
-                                                              reinterpret_cast<const float4*>(C.y4.p),
-                                                              reinterpret_cast<float4*>(L.x4.p), ctl);
+        prolong_from(c, l, ctl);
         k_vc_post<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(sbview(L), L.binv.p, L.b.p,
                                                            reinterpret_cast<const float4*>(L.x4.p),
                                                            reinterpret_cast<float4*>(L.y4.p), ctl);
@@ -1308,31 +1576,16 @@ void coarse_correction(Ctx& c) {
     MgLevel& L0 = *H.L[0];
     for (int l = 0; l < nl - 1; ++l) {
         MgLevel& L = *H.L[l];
-        MgLevel& C = *H.L[l + 1];
         if (l > 0)
             k_vc_resid<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(sbview(L), L.b.p, reinterpret_cast<float4*>(L.x4.p),
                                                                 L.r.p, nullptr);
-        const bool last = (l + 1 == nl - 1);
-        const int n1 = (L.nx + 1) * (L.ny + 1) * (C.nz + 1), n2 = (L.nx + 1) * (C.ny + 1) * (C.nz + 1);
-        k_vc_restrict_axis<2><<<grid_of(n1), kT, 0, c.stream>>>(
-            L.nx + 1, L.ny + 1, C.nz + 1, L.nz + 1, C.d_xs.p + C.ox[2], C.d_lo.p + C.ol[2], C.d_w.p + C.ol[2], C.nz,
-            L.r.p, C.t1.p, nullptr, nullptr, nullptr);
-        k_vc_restrict_axis<1><<<grid_of(n2), kT, 0, c.stream>>>(
-            L.nx + 1, C.ny + 1, C.nz + 1, L.ny + 1, C.d_xs.p + C.ox[1], C.d_lo.p + C.ol[1], C.d_w.p + C.ol[1], C.ny,
-            C.t1.p, C.t2.p, nullptr, nullptr, nullptr);
-        k_vc_restrict_axis<0><<<grid_of(C.n_nodes), kT, 0, c.stream>>>(
-            C.nx + 1, C.ny + 1, C.nz + 1, L.nx + 1, C.d_xs.p + C.ox[0], C.d_lo.p + C.ol[0], C.d_w.p + C.ol[0], C.nx,
-            C.t2.p, C.b.p, last ? nullptr : C.binv.p, reinterpret_cast<float4*>(C.x4.p), nullptr);
+        restrict_to(c, l, nullptr);
     }
-    MgLevel& Lc = *H.L.back();
-    k_vc_dense<<<1, 1024, 0, c.stream>>>(H.n_coarse, H.dense.p, Lc.b.p, Lc.y4.p, nullptr);
+    coarsest_solve(c, nullptr);
     ASEND_CUDA(cudaMemsetAsync(L0.x4.p, 0, sizeof(float) * 4 * L0.n_nodes, c.stream));
     for (int l = nl - 2; l >= 0; --l) {
         MgLevel& L = *H.L[l];
-        MgLevel& C = *H.L[l + 1];
-        k_vc_prolong<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(view_of(C), L.nx, L.ny, L.nz,
-                                                              reinterpret_cast<const float4*>(C.y4.p),
-                                                              reinterpret_cast<float4*>(L.x4.p), nullptr);
+        prolong_from(c, l, nullptr);
         if (l > 0)
             k_vc_post<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(sbview(L), L.binv.p, L.b.p,
                                                                reinterpret_cast<const float4*>(L.x4.p),
@@ -1387,16 +1640,89 @@ void mg_apply(Ctx& c, const float* d_b, float* d_z4) {
 
 int mg_levels(const Ctx& c) { return c.mg ? (int)c.mg->L.size() : 0; }
 
+// Mean device time of n_launch back-to-back launches of one kernel of the
+// multigrid CG (0: outer product + p.Ap in the method's value format; 1:
+// level-0 V-cycle residual; 2: level-0 post-smoothing) and its algorithmic
+// bytes per launch.  Scratch scalars keep the kernels from exiting early.
+double mg_time_kernel(Ctx& c, int kernel, int method, int n_launch, double* bytes) {
+    mg_prepare(c);
+    mg_select_smoother(c, false);
+    MgHierarchy& H = *c.mg;
+    MgLevel& L0 = *H.L[0];
+    const int n = c.A.n_rows, nd = c.n_dof;
+    const int grid = grid_of(n);
+    const double blocks = (double)(c.A.nnz_scalar() / 9);
+    if (kernel != 0 && H.L.size() < 2) throw InputError("multigrid hierarchy has a single level");
+    DArr<RhsScalars> sc;
+    DArr<Control> ctl;
+    DArr<double> part, p, ap;
+    sc.alloc(1);
+    ctl.alloc(1);
+    sc.zero(c.stream);
+    ctl.zero(c.stream);
+    part.alloc((size_t)grid * kMaxRhs * 3);
+    p.alloc((size_t)4 * n);
+    ap.alloc(nd);
+    MgPcg M;
+    std::memset(&M, 0, sizeof(M));
+    PcgArgs& a = M.a;
+    a.n_rows = n;
+    a.nrhs = 1;
+    a.n_dof = nd;
+    a.slice_off = c.A.slice_off.p;
+    a.row_len = c.A.row_len.p;
+    a.col = c.A.col.p;
+    a.v32 = c.A.v32.p;
+    a.v32lo = c.A.v32lo.p;
+    a.v64 = c.A.v64.p;
+    a.p = p.p;
+    a.ap = ap.p;
+    a.partials = part.p;
+    a.sc = sc.p;
+    a.ctl = ctl.p;
+    M.n_inst = 1;
+    // the direction's values do not change the kernels' work: zeros
+    ASEND_CUDA(cudaMemsetAsync(p.p, 0, sizeof(double) * 4 * n, c.stream));
+    auto launch = [&]() {
+        if (kernel == 0) {
+            if (method == ASEND_METHOD_MIXED) k_mg_spmv_dot<float, float><<<grid, kThreads, 0, c.stream>>>(M);
+            else if (method == ASEND_METHOD_SPLIT) k_mg_spmv_dot<float, SplitP><<<grid, kThreads, 0, c.stream>>>(M);
+            else k_mg_spmv_dot<double, double><<<grid, kThreads, 0, c.stream>>>(M);
+        } else if (kernel == 1) {
+            k_vc_resid<<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(sbview(L0), L0.b.p, reinterpret_cast<float4*>(L0.x4.p),
+                                                                 L0.r.p, nullptr);
+        } else {
+            k_vc_post<<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(sbview(L0), L0.binv.p, L0.b.p,
+                                                                reinterpret_cast<const float4*>(L0.x4.p),
+                                                                reinterpret_cast<float4*>(L0.y4.p), nullptr);
+        }
+    };
+    const double ps = (method == ASEND_METHOD_MIXED) ? 4.0 : 8.0;  // bytes per value / direction entry
+    if (kernel == 0) *bytes = blocks * (9.0 * ps + 4.0) + (double)n * 4.0 * ps + (double)nd * ps;
+    else if (kernel == 1) *bytes = blocks * 40.0 + (double)n * 16.0 + (double)nd * 8.0;
+    else *bytes = blocks * 40.0 + (double)n * (16.0 + 36.0 + 16.0) + (double)nd * 4.0;
+    for (int w = 0; w < 3; ++w) launch();
+    ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
+    for (int i = 0; i < n_launch; ++i) launch();
+    ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
+    ASEND_CUDA(cudaEventSynchronize(c.ev1));
+    ASEND_CUDA(cudaGetLastError());
+    float ms = 0.f;
+    ASEND_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    c.launches += n_launch + 3;
+    return ms / n_launch;
+}
+
 // per-level diagnostics: dims (nx, ny, nz), power estimate and guaranteed
 // bound of lambda_max(D^-1 A), damping in use (the coarsest level: zeros)
 void mg_level_info(Ctx& c, int level, int32_t* dims, double* lam_est, double* lam_bound, double* omega) {
     if (!c.mg || level < 0 || level >= (int)c.mg->L.size()) throw InputError("no such multigrid level");
     MgHierarchy& H = *c.mg;
     MgLevel& L = *H.L[level];
-    if (dims) {
-        dims[0] = L.nx;
-        dims[1] = L.ny;
-        dims[2] = L.nz;
+    if (dims) {  // the first block (instance 0)
+        dims[0] = L.blk[0].nx;
+        dims[1] = L.blk[0].ny;
+        dims[2] = L.blk[0].nz;
     }
     float nrm = 0.f, om = 0.f;
     unsigned int bb = 0;
@@ -1518,6 +1844,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
     const int max_it = o.max_iter > 0 ? o.max_iter : nd;
     const int G = o.graph_iters > 0 ? o.graph_iters : 8;
     const bool mixed = o.method == ASEND_METHOD_MIXED;
+    const bool split = o.method == ASEND_METHOD_SPLIT;
     if (!warm) ASEND_CUDA(cudaMemsetAsync(d_x, 0, (size_t)nrhs_all * nd * sizeof(double), c.stream));
     c.d_r.alloc(std::max(c.d_r.n, (size_t)nrhs_all * nd));
     const int grid = grid_of(n);
@@ -1525,21 +1852,28 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
     if (mixed) {
         c.d_p32.alloc(std::max(c.d_p32.n, (size_t)kMaxRhs * 4 * n));
         c.d_ap32.alloc(std::max(c.d_ap32.n, (size_t)kMaxRhs * nd));
-    } else {
+    } else {  // FP64: 2 x double2 per node; split: hi + lo float4 per node (same bytes)
         c.d_p64.alloc(std::max(c.d_p64.n, (size_t)kMaxRhs * 4 * n));
         c.d_ap64.alloc(std::max(c.d_ap64.n, (size_t)kMaxRhs * nd));
     }
-    DArr<RhsScalars> d_sc;
-    DArr<Control> d_ctl;
-    d_sc.alloc(1);
-    d_ctl.alloc(1);
+    // one scalar set per instance (slot 0 of kMaxRhs), persistent so the
+    // captured iteration graphs stay valid across solves
+    const int NI = c.n_inst > 1 ? c.n_inst : 1;
+    const size_t sc_need = sizeof(RhsScalars) * NI * kMaxRhs, tk_need = sizeof(uint32_t) * NI * 4;
+    if (c.pcg_sc.n < sc_need) c.pcg_sc.alloc(sc_need);
+    if (c.pcg_ctl.n < sizeof(Control)) c.pcg_ctl.alloc(sizeof(Control));
+    if (NI > 1 && c.pcg_tk.n < tk_need) c.pcg_tk.alloc(tk_need);
+    RhsScalars* d_sc = reinterpret_cast<RhsScalars*>(c.pcg_sc.p);
+    Control* d_ctl = reinterpret_cast<Control*>(c.pcg_ctl.p);
+    ensure_pinned_scalars(c, sc_need);
     RhsScalars* h = reinterpret_cast<RhsScalars*>(c.h_sc);
     int iters_max = 0, repl = 0, status = 0;
     double relmax = 0.0;
     MgLevel& L0 = *H.L[0];
     ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
     for (int r0 = 0; r0 < nrhs_all; ++r0) {
-        MgPcg M{};
+        MgPcg M;
+        std::memset(&M, 0, sizeof(M));  // padding too: the bytes key the cached graph
         PcgArgs& a = M.a;
         a.n_rows = n;
         a.nrhs = 1;
@@ -1548,6 +1882,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         a.row_len = c.A.row_len.p;
         a.col = c.A.col.p;
         a.v32 = c.A.v32.p;
+        a.v32lo = c.A.v32lo.p;
         a.v64 = c.A.v64.p;
         a.f = d_f + (size_t)r0 * nd;
         a.x = d_x + (size_t)r0 * nd;
@@ -1555,78 +1890,133 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         a.p = mixed ? (void*)c.d_p32.p : (void*)c.d_p64.p;
         a.ap = mixed ? (void*)c.d_ap32.p : (void*)c.d_ap64.p;
         a.partials = c.d_partials.p;
-        a.sc = d_sc.p;
-        a.ctl = d_ctl.p;
+        a.sc = d_sc;
+        a.ctl = d_ctl;
+        if (NI > 1) {
+            a.cta_inst = c.d_cta_inst.p;
+            a.inst_cta0 = c.d_inst_cta0.p;
+            a.inst_ncta = c.d_inst_ncta.p;
+            a.tickets = reinterpret_cast<uint32_t*>(c.pcg_tk.p);
+            ASEND_CUDA(cudaMemsetAsync(c.pcg_tk.p, 0, tk_need, c.stream));
+        }
         M.b0 = L0.b.p;
         M.z = reinterpret_cast<const float4*>(L0.y4.p);
         M.binv0 = L0.binv.p;
         M.x40 = reinterpret_cast<float4*>(L0.x4.p);
-        d_sc.zero(c.stream);
-        d_ctl.zero(c.stream);
+        M.n_inst = NI;
+        ASEND_CUDA(cudaMemsetAsync(d_sc, 0, sc_need, c.stream));
+        ASEND_CUDA(cudaMemsetAsync(d_ctl, 0, sizeof(Control), c.stream));
         auto launch_residual = [&](int init) {
             k_mg_residual<<<grid, kThreads, 0, c.stream>>>(M, init, o.rel_tol * o.rel_tol);
             ++c.launches;
         };
         auto launch_iteration = [&]() {
-            if (mixed) k_mg_spmv_dot<float, float><<<grid, kThreads, 0, c.stream>>>(M);
-            else k_mg_spmv_dot<double, double><<<grid, kThreads, 0, c.stream>>>(M);
-            if (mixed) k_mg_update_xr<float><<<grid, kThreads, 0, c.stream>>>(M);
-            else k_mg_update_xr<double><<<grid, kThreads, 0, c.stream>>>(M);
+            if (mixed) {
+                k_mg_spmv_dot<float, float><<<grid, kThreads, 0, c.stream>>>(M);
+                k_mg_update_xr<float><<<grid, kThreads, 0, c.stream>>>(M);
+            } else if (split) {
+                k_mg_spmv_dot<float, SplitP><<<grid, kThreads, 0, c.stream>>>(M);
+                k_mg_update_xr<SplitP><<<grid, kThreads, 0, c.stream>>>(M);
+            } else {
+                k_mg_spmv_dot<double, double><<<grid, kThreads, 0, c.stream>>>(M);
+                k_mg_update_xr<double><<<grid, kThreads, 0, c.stream>>>(M);
+            }
             vcycle(c, a.ctl, true);
             if (mixed) {
                 k_mg_rz<float><<<grid, kThreads, 0, c.stream>>>(M, 0);
                 k_mg_update_p<float><<<grid, kThreads, 0, c.stream>>>(M);
+            } else if (split) {
+                k_mg_rz<SplitP><<<grid, kThreads, 0, c.stream>>>(M, 0);
+                k_mg_update_p<SplitP><<<grid, kThreads, 0, c.stream>>>(M);
             } else {
                 k_mg_rz<double><<<grid, kThreads, 0, c.stream>>>(M, 0);
                 k_mg_update_p<double><<<grid, kThreads, 0, c.stream>>>(M);
             }
         };
-        auto launch_start = [&](int mode) {  // V-cycle on the current b0, then p = z / rz
-            vcycle(c, nullptr, true);
-            if (mixed) k_mg_rz<float><<<grid, kThreads, 0, c.stream>>>(M, mode);
-            else k_mg_rz<double><<<grid, kThreads, 0, c.stream>>>(M, mode);
-            c.launches += vcycle_launches(H) + 1;
+        // V-cycle of every instance's current b0, then rz (and p = z on a
+        // restart) for the instances the residual kernel marked
+        auto launch_start = [&]() {
+            vcycle(c, nullptr, false);
+            if (mixed) k_mg_rz<float><<<grid, kThreads, 0, c.stream>>>(M, 1);
+            else if (split) k_mg_rz<SplitP><<<grid, kThreads, 0, c.stream>>>(M, 1);
+            else k_mg_rz<double><<<grid, kThreads, 0, c.stream>>>(M, 1);
+            c.launches += vcycle_launches(H) + 2;
         };
         launch_residual(1);
-        launch_start(1);
+        launch_start();
         ASEND_CUDA(cudaGetLastError());
-        cudaGraph_t graph;
-        cudaGraphExec_t exec;
-        ASEND_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-        for (int i = 0; i < G; ++i) launch_iteration();
-        ASEND_CUDA(cudaStreamEndCapture(c.stream, &graph));
-        ASEND_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-        ASEND_CUDA(cudaGraphDestroy(graph));
+        // G iterations as one graph, kept with the hierarchy and reused while
+        // the launch arguments are the same (they fully define the graph)
+        std::vector<uint8_t> key(sizeof(MgPcg) + 2 * sizeof(int));
+        std::memcpy(key.data(), &M, sizeof(MgPcg));
+        const int extra[2] = {o.method, G};
+        std::memcpy(key.data() + sizeof(MgPcg), extra, sizeof(extra));
+        cudaGraphExec_t exec = nullptr;
+        for (auto& g : H.graphs)
+            if (g.first == key) exec = g.second;
+        if (!exec) {
+            cudaGraph_t graph;
+            ASEND_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+            k_mg_count_active<<<1, 32, 0, c.stream>>>(M);
+            for (int i = 0; i < G; ++i) launch_iteration();
+            ASEND_CUDA(cudaStreamEndCapture(c.stream, &graph));
+            ASEND_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+            ASEND_CUDA(cudaGraphDestroy(graph));
+            if (H.graphs.size() >= 8) {
+                ASEND_CUDA(cudaGraphExecDestroy(H.graphs.front().second));
+                H.graphs.erase(H.graphs.begin());
+            }
+            H.graphs.emplace_back(key, exec);
+        }
         const int per_iter = 4 + vcycle_launches(H);
+        const size_t sc_bytes = sizeof(RhsScalars) * NI * kMaxRhs;
         int since_repl = 0;
         for (;;) {
-            ASEND_CUDA(cudaMemcpyAsync(h, d_sc.p, sizeof(RhsScalars), cudaMemcpyDeviceToHost, c.stream));
+            ASEND_CUDA(cudaMemcpyAsync(h, d_sc, sc_bytes, cudaMemcpyDeviceToHost, c.stream));
             ASEND_CUDA(cudaStreamSynchronize(c.stream));
-            if (h->nonfinite) { status = ASEND_NONFINITE; break; }
-            if (h->finished) break;
-            if (h->iter >= max_it) { status = std::max(status, (int)ASEND_MAX_ITER); break; }
-            const bool drop = mixed && h->rr < 1e-4 * h->rr_last_true;
-            const bool periodic = o.replace_every > 0 && since_repl >= o.replace_every;
-            if (h->done || drop || periodic) {
-                launch_residual(0);
+            bool all_finished = true, any_replace = false, any_nonfinite = false;
+            int it_now = 0;
+            for (int i = 0; i < NI; ++i) {
+                RhsScalars& s = h[(size_t)i * kMaxRhs];
+                it_now = std::max(it_now, (int)s.iter);
+                if (s.nonfinite) { any_nonfinite = true; continue; }
+                if (s.finished) continue;
+                all_finished = false;
+                const bool drop = mixed && s.rr < 1e-4 * s.rr_last_true;
+                const bool periodic = o.replace_every > 0 && since_repl >= o.replace_every;
+                if (s.done || drop || periodic) {
+                    s.replace = 1;
+                    any_replace = true;
+                }
+            }
+            if (any_nonfinite) { status = ASEND_NONFINITE; break; }
+            if (all_finished) break;
+            if (it_now >= max_it) { status = std::max(status, (int)ASEND_MAX_ITER); break; }
+            if (any_replace) {
                 // after convergence of the recurrence the last p update was
-                // skipped: restart the direction (p = z); otherwise keep p
-                launch_start(h->done ? 1 : 2);
+                // skipped: the instance restarts its direction (p = z);
+                // otherwise p is kept
+                ASEND_CUDA(cudaMemcpyAsync(d_sc, h, sc_bytes, cudaMemcpyHostToDevice, c.stream));
+                launch_residual(0);
+                launch_start();
                 ++repl;
                 since_repl = 0;
                 continue;
             }
             ASEND_CUDA(cudaGraphLaunch(exec, c.stream));
-            c.launches += (int64_t)per_iter * G;
+            c.launches += (int64_t)per_iter * G + 1;
             since_repl += G;
         }
-        ASEND_CUDA(cudaGraphExecDestroy(exec));
-        ASEND_CUDA(cudaMemcpyAsync(h, d_sc.p, sizeof(RhsScalars), cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaMemcpyAsync(h, d_sc, sc_bytes, cudaMemcpyDeviceToHost, c.stream));
         ASEND_CUDA(cudaStreamSynchronize(c.stream));
-        iters_max = std::max(iters_max, (int)h->iter);
-        relmax = std::max(relmax, h->bb > 0 ? std::sqrt(h->rr_last_true / h->bb) : std::sqrt(h->rr_last_true));
-        if (h->nonfinite) status = ASEND_NONFINITE;
-        else if (!h->finished) status = std::max(status, (int)ASEND_MAX_ITER);
+        for (int i = 0; i < NI; ++i) {
+            const RhsScalars& s = h[(size_t)i * kMaxRhs];
+            iters_max = std::max(iters_max, (int)s.iter);
+            if (s.nonfinite) status = ASEND_NONFINITE;
+            else if (!s.finished) status = std::max(status, (int)ASEND_MAX_ITER);
+            if (s.bb == 0.0) continue;  // empty load case of this instance
+            relmax = std::max(relmax, std::sqrt(s.rr_last_true / s.bb));
+        }
     }
     ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
     ASEND_CUDA(cudaEventSynchronize(c.ev1));

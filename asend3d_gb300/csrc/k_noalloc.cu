@@ -95,6 +95,17 @@ extern "C" int asend_operator_energy_noalloc(asend_ctx* ctx, const double* d_x, 
         c->err = "null device buffer";
         return ASEND_EINVAL;
     }
+    {  // the rows read other rows' x after those rows wrote y: no overlap allowed
+        const uintptr_t x0 = reinterpret_cast<uintptr_t>(d_x), y0 = reinterpret_cast<uintptr_t>(d_y);
+        const uintptr_t e0 = reinterpret_cast<uintptr_t>(d_energy), nb = sizeof(double) * (uintptr_t)c->n_dof;
+        const bool xy = x0 < y0 + nb && y0 < x0 + nb;
+        const bool ex = e0 + sizeof(double) > x0 && e0 < x0 + nb;
+        const bool ey = e0 + sizeof(double) > y0 && e0 < y0 + nb;
+        if (xy || ex || ey) {
+            c->err = "asend_operator_energy_noalloc: x, y and energy must not overlap";
+            return ASEND_EINVAL;
+        }
+    }
     if (c->A.n_rows > kNaMaxRows || c->A.b != 3) {
         c->err = "operator too large for asend_operator_energy_noalloc: at most 4194304 node rows "
                  "(12582912 DOF) with 3 DOF per node; use asend_apply_operator";

@@ -43,7 +43,7 @@ template <typename TV, typename TP, int NR>
 __global__ void __launch_bounds__(kThreads) k_spmv_dot(PcgArgs A) {
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (cta_done<NR>(A, S)) return;
-    if constexpr (sizeof(TP) == 4) {
+    if constexpr (std::is_same<TP, float>::value) {
         // Mixed: once the FP32-operator recurrence has dropped 1e4 below the
         // last true residual, stop this graph chunk at an iteration boundary
         // (p is consistent) so the host replaces the residual before the two
@@ -64,15 +64,15 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot(PcgArgs A) {
 #pragma unroll
     for (int k = 0; k < NR; ++k) d[k][0] = 0.0;
     if (row < A.n_rows) {
-        TP y[NR][3];
+        typename ApOf<TP>::T y[NR][3];
         const TV* vals;
         if constexpr (sizeof(TV) == 4) vals = A.v32; else vals = A.v64;
         spmv_row<TV, TP, NR>(row, A, vals, A.p, y);
 #pragma unroll
         for (int k = 0; k < NR; ++k) {
-            TP pv[3];
+            typename ApOf<TP>::T pv[3];
             PadVec<TP>::load(A.p, (size_t)k * A.n_rows + row, pv);
-            TP* ap = reinterpret_cast<TP*>(A.ap) + (size_t)k * A.n_dof + 3 * (size_t)row;
+            typename ApOf<TP>::T* ap = reinterpret_cast<typename ApOf<TP>::T*>(A.ap) + (size_t)k * A.n_dof + 3 * (size_t)row;
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 ap[a] = y[k][a];
@@ -106,10 +106,10 @@ __global__ void __launch_bounds__(kThreads) k_update_xr(PcgArgs A) {
         for (int k = 0; k < NR; ++k) {
             if (S[k].done) continue;
             const double alpha = S[k].alpha;
-            TP pv[3];
+            typename ApOf<TP>::T pv[3];
             PadVec<TP>::load(A.p, (size_t)k * A.n_rows + row, pv);
             const size_t o = (size_t)k * A.n_dof + 3 * (size_t)row;
-            const TP* ap = reinterpret_cast<const TP*>(A.ap) + o;
+            const typename ApOf<TP>::T* ap = reinterpret_cast<const typename ApOf<TP>::T*>(A.ap) + o;
             double rv[3], z[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kThreads) k_update_p(PcgArgs A) {
         const size_t o = (size_t)k * A.n_dof + 3 * (size_t)row;
         double rv[3] = {A.r[o], A.r[o + 1], A.r[o + 2]}, z[3];
         precond<PC>(A, row, rv, z);
-        TP pv[3];
+        typename ApOf<TP>::T pv[3];
         PadVec<TP>::load(A.p, (size_t)k * A.n_rows + row, pv);
         double pn[3];
 #pragma unroll
@@ -274,11 +274,11 @@ template <typename TV, typename TP>
 __global__ void __launch_bounds__(kThreads) k_spmv_plain(PcgArgs A, double* __restrict__ y) {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= A.n_rows) return;
-    TP acc[1][3];
+    typename ApOf<TP>::T acc[1][3];
     const TV* vals;
     if constexpr (sizeof(TV) == 4) vals = A.v32; else vals = A.v64;
     spmv_row<TV, TP, 1>(row, A, vals, A.p, acc);
-    TP* out = reinterpret_cast<TP*>(A.ap) + 3 * (size_t)row;
+    typename ApOf<TP>::T* out = reinterpret_cast<typename ApOf<TP>::T*>(A.ap) + 3 * (size_t)row;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         out[a] = acc[0][a];
@@ -334,7 +334,9 @@ struct Launcher {
     template <typename TP, int NR, int PC>
     void iter_t() {
         const int g = grid_rows(a.n_rows);
-        if (method == ASEND_METHOD_MIXED) k_spmv_dot<float, float, NR><<<g, kThreads, 0, c.stream>>>(a);
+        if constexpr (std::is_same<TP, float>::value) k_spmv_dot<float, float, NR><<<g, kThreads, 0, c.stream>>>(a);
+        else if constexpr (std::is_same<TP, SplitP>::value)
+            k_spmv_dot<float, SplitP, NR><<<g, kThreads, 0, c.stream>>>(a);
         else k_spmv_dot<double, double, NR><<<g, kThreads, 0, c.stream>>>(a);
         k_update_xr<TP, NR, PC><<<g, kThreads, 0, c.stream>>>(a);
         k_update_p<TP, NR, PC><<<g, kThreads, 0, c.stream>>>(a);
@@ -362,10 +364,12 @@ struct Launcher {
     }
     void iteration() {  // launches are counted per graph launch
         if (method == ASEND_METHOD_MIXED) dispatch_nr<float>(true, 0, 0.0);
+        else if (method == ASEND_METHOD_SPLIT) dispatch_nr<SplitP>(true, 0, 0.0);
         else dispatch_nr<double>(true, 0, 0.0);
     }
     void residual(int mode, double tol2) {
         if (method == ASEND_METHOD_MIXED) dispatch_nr<float>(false, mode, tol2);
+        else if (method == ASEND_METHOD_SPLIT) dispatch_nr<SplitP>(false, mode, tol2);
         else dispatch_nr<double>(false, mode, tol2);
         c.launches += 1;
     }
@@ -373,7 +377,8 @@ struct Launcher {
 
 }  // namespace
 
-// Device-side y = A x (natural layout), value precision 32 or 64.
+// Device-side y = A x (natural layout), value precision 32, 64 or 48 (the
+// split FP32 hi + lo product, FP64-accurate).
 void apply_operator_device(Ctx& c, int precision, const double* d_x, double* d_y) {
     PcgArgs a{};
     a.n_rows = c.A.n_rows;
@@ -383,9 +388,20 @@ void apply_operator_device(Ctx& c, int precision, const double* d_x, double* d_y
     a.row_len = c.A.row_len.p;
     a.col = c.A.col.p;
     a.v32 = c.A.v32.p;
+    a.v32lo = c.A.v32lo.p;
     a.v64 = c.A.v64.p;
     const int g = grid_rows(a.n_rows);
-    if (precision == 32) {
+    if (precision == 48) {
+        DArr<double> p, ap;
+        p.alloc((size_t)4 * a.n_rows);
+        ap.alloc(c.n_dof);
+        a.p = p.p;
+        a.ap = ap.p;
+        k_pack<SplitP><<<g, kThreads, 0, c.stream>>>(a.n_rows, d_x, p.p);
+        k_spmv_plain<float, SplitP><<<g, kThreads, 0, c.stream>>>(a, d_y);
+        ASEND_CUDA(cudaGetLastError());
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+    } else if (precision == 32) {
         DArr<float> p, ap;
         p.alloc((size_t)4 * a.n_rows);
         ap.alloc(c.n_dof);
@@ -422,10 +438,11 @@ double time_spmv(Ctx& c, int precision, int n_launch, double* bytes) {
     a.row_len = c.A.row_len.p;
     a.col = c.A.col.p;
     a.v32 = c.A.v32.p;
+    a.v32lo = c.A.v32lo.p;
     a.v64 = c.A.v64.p;
     const int g = grid_rows(n);
     const int64_t blocks = c.A.nnz_scalar() / 9;
-    const size_t vsz = (precision == 32) ? 4 : 8;
+    const size_t vsz = (precision == 32) ? 4 : 8;  // split: hi + lo, 8 bytes per value
     *bytes = (double)blocks * (9.0 * vsz + 4.0) + (double)n * (4.0 * vsz) + (double)c.n_dof * vsz;
     std::vector<double> ones(c.n_dof, 1.0);
     DArr<double> x;
@@ -436,16 +453,16 @@ double time_spmv(Ctx& c, int precision, int n_launch, double* bytes) {
     a.p = p.p;
     a.ap = ap.p;
     if (precision == 32) k_pack<float><<<g, kThreads, 0, c.stream>>>(n, x.p, p.p);
+    else if (precision == 48) k_pack<SplitP><<<g, kThreads, 0, c.stream>>>(n, x.p, p.p);
     else k_pack<double><<<g, kThreads, 0, c.stream>>>(n, x.p, p.p);
-    for (int w = 0; w < 3; ++w) {
+    auto launch = [&]() {
         if (precision == 32) k_spmv_plain<float, float><<<g, kThreads, 0, c.stream>>>(a, nullptr);
+        else if (precision == 48) k_spmv_plain<float, SplitP><<<g, kThreads, 0, c.stream>>>(a, nullptr);
         else k_spmv_plain<double, double><<<g, kThreads, 0, c.stream>>>(a, nullptr);
-    }
+    };
+    for (int w = 0; w < 3; ++w) launch();
     ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
-    for (int i = 0; i < n_launch; ++i) {
-        if (precision == 32) k_spmv_plain<float, float><<<g, kThreads, 0, c.stream>>>(a, nullptr);
-        else k_spmv_plain<double, double><<<g, kThreads, 0, c.stream>>>(a, nullptr);
-    }
+    for (int i = 0; i < n_launch; ++i) launch();
     ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
     ASEND_CUDA(cudaEventSynchronize(c.ev1));
     ASEND_CUDA(cudaGetLastError());
@@ -458,7 +475,8 @@ double time_spmv(Ctx& c, int precision, int n_launch, double* bytes) {
 // Batched PCG over all load cases (chunks of up to 4 sharing one matrix read).
 int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f,
               double* d_x, int nrhs_all) {
-    if (o.method != ASEND_METHOD_FP64 && o.method != ASEND_METHOD_MIXED) throw InputError("unknown method");
+    if (o.method != ASEND_METHOD_FP64 && o.method != ASEND_METHOD_MIXED && o.method != ASEND_METHOD_SPLIT)
+        throw InputError("unknown method");
     if (!(o.rel_tol > 0.0)) throw InputError("rel_tol must be positive");
     if (o.precond == ASEND_PC_MG || o.precond == ASEND_PC_MG_LEARNED) {
         if (o.precond == ASEND_PC_MG_LEARNED && !learned_ready(c)) throw InputError("no learned weights");
@@ -512,7 +530,7 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
     if (mixed) {
         c.d_p32.alloc((size_t)kMaxRhs * 4 * n);
         c.d_ap32.alloc((size_t)kMaxRhs * nd);
-    } else {
+    } else {  // FP64: 2 x double2 per node; split: hi + lo float4 per node (same bytes)
         c.d_p64.alloc((size_t)kMaxRhs * 4 * n);
         c.d_ap64.alloc((size_t)kMaxRhs * nd);
     }
@@ -545,6 +563,7 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
         a.row_len = c.A.row_len.p;
         a.col = c.A.col.p;
         a.v32 = c.A.v32.p;
+        a.v32lo = c.A.v32lo.p;
         a.v64 = c.A.v64.p;
         a.f = d_f + (size_t)r0 * nd;
         a.x = d_x + (size_t)r0 * nd;

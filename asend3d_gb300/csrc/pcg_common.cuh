@@ -1,6 +1,8 @@
 // pcg_common.cuh -- data structures and device helpers shared by the PCG
 // drivers (k_pcg.cu: Jacobi / block-Jacobi; k_mg.cu: multigrid-preconditioned).
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace asend {
@@ -13,12 +15,13 @@ struct RhsScalars {
     double rz, rz_new, pAp, rr, bb, alpha, beta, target, rr_last_true;
     int32_t iter, done, finished, replace, nonfinite;
     int32_t restart;  // done by convergence: that iteration's p update was skipped
-    int32_t pad1, pad2;
+    int32_t refresh;  // multigrid CG: rz (and p when restarting) to be re-formed after a V-cycle
+    int32_t pad2;
 };
 struct Control {
     int32_t all_done;
     uint32_t ticket[4];
-    int32_t pad[3];
+    int32_t pad[3];  // pad[0]: instances still iterating (multigrid CG)
 };
 
 struct PcgArgs {
@@ -26,7 +29,8 @@ struct PcgArgs {
     const int64_t* slice_off;
     const uint8_t* row_len;
     const int32_t* col;
-    const float* v32;
+    const float* v32;    // FP32 values (the high part of each FP64 value)
+    const float* v32lo;  // low parts: v64 = v32 + v32lo to 2^-48 relative (split method)
     const double* v64;
     const double* f;
     double* x;
@@ -62,8 +66,40 @@ __device__ __forceinline__ bool cta_done(const PcgArgs& A, const RhsScalars* S) 
     return true;
 }
 
+// Split precision (ASEND_METHOD_SPLIT): the search direction is stored as
+// FP32 hi + lo pairs (a node: hi float4 then lo float4, 32 bytes like the
+// padded FP64 direction) and products with the hi + lo operator values run
+// in compensated FP32 arithmetic, FP64-accurate on the FP32 pipes.
+struct SplitP {};
+
+// Type in which a direction element is loaded and A p is stored.
+template <typename TP>
+struct ApOf {
+    using T = TP;
+};
+template <>
+struct ApOf<SplitP> {
+    using T = double;
+};
+
 template <typename TP>
 struct PadVec;
+template <>
+struct PadVec<SplitP> {
+    __device__ static void load(const void* p, size_t node, double (&v)[3]) {
+        const float4 h = reinterpret_cast<const float4*>(p)[2 * node];
+        const float4 l = reinterpret_cast<const float4*>(p)[2 * node + 1];
+        v[0] = (double)h.x + (double)l.x;
+        v[1] = (double)h.y + (double)l.y;
+        v[2] = (double)h.z + (double)l.z;
+    }
+    __device__ static void store(void* p, size_t node, const double (&v)[3]) {
+        const float h0 = (float)v[0], h1 = (float)v[1], h2 = (float)v[2];
+        reinterpret_cast<float4*>(p)[2 * node] = make_float4(h0, h1, h2, 0.f);
+        reinterpret_cast<float4*>(p)[2 * node + 1] =
+            make_float4((float)(v[0] - (double)h0), (float)(v[1] - (double)h1), (float)(v[2] - (double)h2), 0.f);
+    }
+};
 template <>
 struct PadVec<float> {
     __device__ static void load(const void* p, size_t node, float (&v)[3]) {
@@ -88,10 +124,102 @@ struct PadVec<double> {
     }
 };
 
+// One compensated product term: (h + l)(xh + xl) added to the running sum
+// (S, C).  p = h xh exactly equals pr + e (e from an FMA); pr enters S by
+// TwoSum (its rounding error goes to C); e, h xl and l xh go to C.  The
+// intrinsics keep the compiler from contracting the error-free steps.
+__device__ __forceinline__ void split_term(float h, float l, float xh, float xl, float& S, float& C) {
+    const float pr = __fmul_rn(h, xh);
+    const float e = __fmaf_rn(h, xh, -pr);
+    const float s = __fadd_rn(S, pr);
+    const float bp = __fsub_rn(s, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s, bp)), __fsub_rn(pr, bp));
+    S = s;
+    C = __fadd_rn(C, __fadd_rn(err, e));
+    C = __fmaf_rn(h, xl, C);
+    C = __fmaf_rn(l, xh, C);
+}
+
+// FP64-accurate row product from FP32 hi / lo values and a split direction.
+template <int NR>
+__device__ __forceinline__ void spmv_row_split(int row, const PcgArgs& A, const void* __restrict__ p,
+                                               double (&y)[NR][3]) {
+    float S[NR][3], Cc[NR][3];
+#pragma unroll
+    for (int k = 0; k < NR; ++k)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) S[k][a] = Cc[k][a] = 0.f;
+    const float4* P = reinterpret_cast<const float4*>(p);
+    const int lane = row & 31;
+    const int64_t g0 = A.slice_off[row >> 5];
+    const int len = A.row_len[row];
+    int j = 0;
+    if constexpr (NR == 1) {
+        // two block columns in flight per step (independent loads overlap)
+        for (; j + 2 <= len; j += 2) {
+            const int64_t g = g0 + j;
+            int c[2];
+            float h[2][9], l[2][9];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) c[u] = A.col[(g + u) * 32 + lane];
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+#pragma unroll
+                for (int q = 0; q < 9; ++q) {
+                    h[u][q] = A.v32[((g + u) * 9 + q) * 32 + lane];
+                    l[u][q] = A.v32lo[((g + u) * 9 + q) * 32 + lane];
+                }
+            float4 xh[2], xl[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                xh[u] = P[2 * (size_t)c[u]];
+                xl[u] = P[2 * (size_t)c[u] + 1];
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    split_term(h[u][3 * a], l[u][3 * a], xh[u].x, xl[u].x, S[0][a], Cc[0][a]);
+                    split_term(h[u][3 * a + 1], l[u][3 * a + 1], xh[u].y, xl[u].y, S[0][a], Cc[0][a]);
+                    split_term(h[u][3 * a + 2], l[u][3 * a + 2], xh[u].z, xl[u].z, S[0][a], Cc[0][a]);
+                }
+        }
+    }
+    for (; j < len; ++j) {
+        const int64_t g = g0 + j;
+        const int c = A.col[g * 32 + lane];
+        float h[9], l[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            h[q] = A.v32[(g * 9 + q) * 32 + lane];
+            l[q] = A.v32lo[(g * 9 + q) * 32 + lane];
+        }
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            const size_t nd = (size_t)k * A.n_rows + c;
+            const float4 xh = P[2 * nd], xl = P[2 * nd + 1];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                split_term(h[3 * a], l[3 * a], xh.x, xl.x, S[k][a], Cc[k][a]);
+                split_term(h[3 * a + 1], l[3 * a + 1], xh.y, xl.y, S[k][a], Cc[k][a]);
+                split_term(h[3 * a + 2], l[3 * a + 2], xh.z, xl.z, S[k][a], Cc[k][a]);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NR; ++k)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) y[k][a] = (double)S[k][a] + (double)Cc[k][a];
+}
+
 // y[k][a] = sum_j sum_c A[r][j](a,c) * p_k[col_j](c) for NR right-hand sides.
 template <typename TV, typename TP, int NR>
 __device__ __forceinline__ void spmv_row(int row, const PcgArgs& A, const TV* __restrict__ vals,
-                                         const void* __restrict__ p, TP (&y)[NR][3]) {
+                                         const void* __restrict__ p, typename ApOf<TP>::T (&y)[NR][3]) {
+    if constexpr (std::is_same<TP, SplitP>::value) {
+        spmv_row_split<NR>(row, A, p, y);
+        return;
+    } else {
 #pragma unroll
     for (int k = 0; k < NR; ++k) y[k][0] = y[k][1] = y[k][2] = (TP)0;
     const int lane = row & 31;
@@ -136,6 +264,7 @@ __device__ __forceinline__ void spmv_row(int row, const PcgArgs& A, const TV* __
             for (int a = 0; a < 3; ++a)
                 y[k][a] = fma((TP)m[a * 3 + 0], pv[0], fma((TP)m[a * 3 + 1], pv[1], fma((TP)m[a * 3 + 2], pv[2], y[k][a])));
         }
+    }
     }
 }
 

@@ -80,7 +80,7 @@ class Problem:
 class GpuSolver:
     """One library context (one CUDA stream) holding one problem."""
 
-    def __init__(self, problem: Problem, device: int = 0, instances=None):
+    def __init__(self, problem: Problem, device: int = 0, instances=None, blocks=None):
         self.lib = _lib.load()
         self.ctx = self.lib.asend_create(device)
         if not self.ctx:
@@ -89,6 +89,8 @@ class GpuSolver:
         self.set_ids = {}
         self.elset_ids = {}
         self.instances = None if instances is None else np.ascontiguousarray(instances, dtype=np.int32)
+        # structured block (nx, ny, nz) of every instance: enables multigrid on the stack
+        self.blocks = None if blocks is None else np.ascontiguousarray(blocks, dtype=np.int32).reshape(-1, 3)
         self._setup()
 
     # -- helpers -----------------------------------------------------------
@@ -143,6 +145,9 @@ class GpuSolver:
         if self.instances is not None:  # validated against elements and constraints
             self._check(self.lib.asend_set_instances(self.ctx, len(self.instances) - 1,
                                                      _ptr(self.instances, C.c_int32)), "set_instances")
+            if self.blocks is not None:
+                self._check(self.lib.asend_set_instance_blocks(self.ctx, len(self.blocks),
+                                                               _ptr(self.blocks, C.c_int32)), "set_instance_blocks")
         self.set_loads()
         obj = p.objective
         if obj[0] == "compliance":
@@ -323,6 +328,15 @@ class GpuSolver:
         ms = C.c_double(0)
         by = C.c_double(0)
         self._check(self.lib.asend_time_spmv(self.ctx, precision, n_launch, C.byref(ms), C.byref(by)), "time_spmv")
+        return ms.value, by.value
+
+    def time_mg_kernel(self, kernel, method=_lib.METHOD_SPLIT, n_launch=20):
+        """(ms per launch, algorithmic bytes per launch) of a multigrid-CG
+        kernel: 0 outer product, 1 level-0 V-cycle residual, 2 post-smoothing."""
+        ms = C.c_double(0)
+        by = C.c_double(0)
+        self._check(self.lib.asend_time_mg_kernel(self.ctx, kernel, method, n_launch, C.byref(ms), C.byref(by)),
+                    "time_mg_kernel")
         return ms.value, by.value
 
     def element_matrices(self, first=0, count=None, mass=True):

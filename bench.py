@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--ny", type=int, default=40)
     ap.add_argument("--nz", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="omit the nested batch_uq block of the default line")
     ap.add_argument("--cpu-sample-nx", type=int, default=40)
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu: one assembly, one multigrid solve, three FP32 SpMV launches")
@@ -63,11 +64,14 @@ def parse():
     return ap.parse_args()
 
 
-def run_batch(a):
-    """64 uneven cantilevers x 4 load cases, one batched block-Jacobi PCG
-    launch sequence per iteration (captured in CUDA graphs) + compliance
-    gradients; compared with plain FP64 Jacobi PCG run instance by instance
-    and load case by load case."""
+def batch_measure(steps: int, warmup: int, plain: bool = True, accuracy: bool = True) -> dict:
+    """The batched sweep: 64 uneven cantilevers x 4 load cases (256
+    right-hand sides) as one stacked operator.  One step = FP64 assembly of
+    the stack + batched multigrid-preconditioned CG over every instance and
+    load case (one V-cycle over all instances' hierarchies, captured in CUDA
+    graphs) + the compliance gradient of every instance.  Compared with the
+    plain FP64 point-Jacobi PCG run instance by instance and load case by
+    load case on the same GPU."""
     import ctypes as C
 
     import torch
@@ -76,11 +80,12 @@ def run_batch(a):
     from asend3d_gb300.solver import GpuSolver
 
     prob, node_ptr, elem_ptr, inst = configs.batch_uq(64)
-    g = GpuSolver(prob, instances=node_ptr)
+    dims = [(p.mesh.nx, p.mesh.ny, p.mesh.nz) for p in inst]
+    g = GpuSolver(prob, instances=node_ptr, blocks=dims)
     stream = torch.cuda.ExternalStream(g.stream)
     n_real = sum(p.mesh.n_dof for p in inst)
     n_cases = len(prob.loads)
-    best = dict(method=_lib.METHOD_FP64, precond=_lib.PC_BLOCK, rel_tol=1e-8, graph_iters=32)
+    best = dict(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, rel_tol=1e-8, graph_iters=8)
     o_adj = g.opts(**best)
 
     def step():
@@ -91,45 +96,93 @@ def run_batch(a):
         rc2 = g.lib.asend_adjoint_gradient(g.ctx, C.byref(o_adj), C.byref(Lc), None, C.byref(s2))
         return rc, rc2, st
 
-    for _ in range(a.warmup):
+    for _ in range(warmup):
         rc, rc2, st = step()
         assert rc == 0 and rc2 == 0, st
     torch.cuda.synchronize()
+    launches0 = g.kernel_launches
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
         e0.record(stream)
-        for _ in range(a.steps):
+        for _ in range(steps):
             rc, rc2, st = step()
+            assert rc == 0 and rc2 == 0, st
         e1.record(stream)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / a.steps
+    ms = e0.elapsed_time(e1) / steps
+    launches = (g.kernel_launches - launches0) // max(steps, 1)
     value = n_real * n_cases / (ms / 1e3)
-    # plain: FP64 point-Jacobi PCG, one instance and one load case at a time
-    plain = dict(method=_lib.METHOD_FP64, precond=_lib.PC_JACOBI, rel_tol=1e-8, graph_iters=32)
-    t_plain = 0.0
-    it_plain = 0
-    for p in inst:
-        for k in range(n_cases):
-            q = type(p)(p.mesh, p.E, p.nu, p.rho, p.node_sets, p.elem_sets, p.constraints, [p.loads[k]],
-                        ("compliance",))
-            gi = GpuSolver(q)
-            gi.assemble(precision=64)
-            rc, sti = gi.static_solve_device(**plain)
-            t_plain += sti["ms_solve"] + sti["ms_assemble"]
-            it_plain = max(it_plain, sti["iterations"])
-            gi.close()
-    plain_value = n_real * n_cases / (t_plain / 1e3)
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
-           "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f64 operator/dots, f32 block-Jacobi", "data": "synthetic (seeded lognormal fields)",
+    out = {"value": value, "unit": UNIT, "ms_per_step": ms, "steps": steps, "warmup": warmup,
+           "dtype": "f64 (fp32 hi+lo operator values) + f64 dots + f32 multigrid",
+           "data": "synthetic (seeded lognormal fields)",
            "config": {"workload": "batch_uq: 64 uneven hex8 cantilevers nx in [20,120], ny=nz in [4,16], 4 load "
-                                  "cases each (256 right-hand sides), batched block-Jacobi PCG + compliance gradient",
-                      "n_dof_total": n_real, "rhs_per_step": 64 * n_cases},
-           "iterations_max": st["iterations"],
-           "plain_fp64_jacobi_sequential": {"value": plain_value, "ms_total": t_plain, "iterations_max": it_plain},
-           "speedup_vs_plain_fp64": value / plain_value, "clocks": clk.summary(), "gpu_launches": None}
-    print(json.dumps(out))
+                                  "cases each (256 right-hand sides), batched multigrid CG + compliance gradients",
+                      "n_dof_total": n_real, "rhs_per_step": 64 * n_cases, "rel_tol": 1e-8,
+                      "method": "CG + per-instance geometric multigrid, one V-cycle over all instances",
+                      "l2": "stack operator 1.2 GB FP64 + 0.6 GB FP32 > 129 MB L2"},
+           "iterations_max": st["iterations"], "ms_breakdown": {"assemble": st["ms_assemble"], "solve": st["ms_solve"]},
+           "gpu_launches_per_step": launches, "clocks": clk.summary()}
+    if plain:
+        # plain: FP64 point-Jacobi PCG, one instance and one load case at a time
+        jac = dict(method=_lib.METHOD_FP64, precond=_lib.PC_JACOBI, rel_tol=1e-8, graph_iters=32)
+        t_plain = 0.0
+        it_plain = 0
+        for p in inst:
+            for k in range(n_cases):
+                q = type(p)(p.mesh, p.E, p.nu, p.rho, p.node_sets, p.elem_sets, p.constraints, [p.loads[k]],
+                            ("compliance",))
+                gi = GpuSolver(q)
+                gi.assemble(precision=64)
+                rc, sti = gi.static_solve_device(**jac)
+                t_plain += sti["ms_solve"] + sti["ms_assemble"]
+                it_plain = max(it_plain, sti["iterations"])
+                gi.close()
+        plain_value = n_real * n_cases / (t_plain / 1e3)
+        out["plain_fp64_jacobi_sequential"] = {"value": plain_value, "ms_total": t_plain, "iterations_max": it_plain}
+        out["speedup_vs_plain_fp64"] = value / plain_value
+    if accuracy:
+        acc = {}
+        try:
+            rel = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))
+            g.assemble(precision=64)
+            u8, _, _ = g.static_solve(**best)
+            L8, gE8, _, _ = g.adjoint_gradient(**best)
+            tight = dict(best, method=_lib.METHOD_FP64, rel_tol=1e-11, max_iter=400)
+            u11, rc11, st11 = g.static_solve(**tight)
+            L11, gE11, _, _ = g.adjoint_gradient(**tight)
+            acc["full_size_vs_fp64_1e-11"] = {"u_rel": rel(u8, u11), "compliance_rel": abs(L8 - L11) / abs(L11),
+                                              "gradient_rel": rel(gE8, gE11), "rc_1e-11": rc11,
+                                              "rel_residual_1e-11": st11["rel_residual"]}
+            # the smallest instance of the stack against the FP64 oracle's direct LDL^T
+            from oracle import pyoracle as po
+
+            i = int(np.argmin([p.mesh.n_dof for p in inst]))
+            p = inst[i]
+            o = po.Oracle(p)
+            F = np.stack([f + o.penalty_rhs() for f in o.loads()])
+            U, _, _ = o.solve_cases(F, precond=po.PC_DIRECT)
+            a0, e0_ = node_ptr[i], elem_ptr[i]
+            ui = u8[:, 3 * a0:3 * a0 + p.mesh.n_dof]
+            gref = sum(o.adjoint(U[k], lam=U[k])[0] for k in range(n_cases))
+            acc["instance_vs_oracle"] = {"instance": i, "n_dof": p.mesh.n_dof,
+                                         "u_rel": max(rel(ui[k], U[k]) for k in range(n_cases)),
+                                         "gradient_rel": rel(gE8[e0_:e0_ + p.mesh.n_elems], gref)}
+        except Exception as err:  # the measurement above stands on its own
+            acc["error"] = repr(err)[:200]
+        out["accuracy"] = acc
     g.close()
+    return out
+
+
+def run_batch(a):
+    b = batch_measure(a.steps, a.warmup)
+    out = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": b["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": b["dtype"], "data": b["data"], "config": b["config"],
+           **{k: v for k, v in b.items() if k not in ("value", "unit", "ms_per_step", "steps", "warmup", "dtype",
+                                                       "data", "config", "clocks", "gpu_launches_per_step")},
+           "clocks": b["clocks"], "gpu_launches": b["gpu_launches_per_step"] * a.steps}
+    print(json.dumps(out))
 
 
 def run_shell(a):
@@ -324,8 +377,8 @@ def run_profile(a):
     p = configs.block_large(nx=a.nx, ny=a.ny, nz=a.nz)
     g = GpuSolver(p)
     g.assemble(precision=64)
-    rc, st = g.static_solve_device(method=_lib.METHOD_FP64, precond=_lib.PC_MG, rel_tol=1e-8)
-    ms, by = g.time_spmv(precision=32, n_launch=3)
+    rc, st = g.static_solve_device(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, rel_tol=1e-8)
+    ms, by = g.time_spmv(precision=48, n_launch=3)
     print(json.dumps({"rc": rc, "iterations": st["iterations"], "ms_solve": st["ms_solve"], "spmv_ms": ms,
                       "spmv_bytes": by, "launches": g.kernel_launches}))
     g.close()
@@ -366,9 +419,13 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """Per-launch DRAM traffic of the FP32 SpMV from the committed ncu summary."""
-    f = ROOT / "profiles" / "spmv_fp32_block_large.md"
+NCU_SUMMARY = {0: "mg_outer_split_block_large.md", 1: "vc_resid_block_large.md", 2: "vc_post_block_large.md"}
+
+
+def ncu_traffic(kernel: int):
+    """Per-launch DRAM traffic (read + write) of a multigrid-CG kernel at the
+    full size, from the committed ncu summary of that kernel (None if absent)."""
+    f = ROOT / "profiles" / NCU_SUMMARY[kernel]
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
@@ -533,7 +590,9 @@ def run_ours(a):
     stream = torch.cuda.ExternalStream(g.stream, device=torch.device("cuda", local))
     n_dof = g.n_dof
     n_el = p.mesh.n_elems
-    mixed = dict(method=_lib.METHOD_FP64, precond=_lib.PC_MG, rel_tol=1e-8, graph_iters=8)
+    # headline method: FP64-accurate outer product on the FP32 pipes (hi + lo
+    # value pairs), FP64 vectors / dots / residuals, FP32 multigrid V-cycle
+    mixed = dict(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, rel_tol=1e-8, graph_iters=8)
 
     def step_device():
         g.assemble(precision=64)
@@ -641,15 +700,29 @@ def run_ours(a):
     ms_plain = max_over_ranks(ms_plain, world)
     plain_value = replicas_value(n_dof, world, ms_plain)
 
-    # ---- roofline of the dominant kernel (FP32 sliced block-ELL SpMV)
-    ms_spmv, bytes_spmv = g.time_spmv(precision=32, n_launch=50)
-    ms_spmv64, bytes_spmv64 = g.time_spmv(precision=64, n_launch=20)
+    # ---- roofline: the three kernels of every multigrid-CG iteration that
+    # read a full finest-level operator (each launched once per iteration),
+    # timed as they run in the step; the slowest is reported
     peak, peak_kind = measured_peak()
-    achieved = bytes_spmv / (ms_spmv * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": "k_spmv_dot<float> (sliced block-ELL FP32 SpMV)", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"of {peak_kind}",
-            "traffic": ncu_traffic(), "algorithmic_bytes_per_launch": bytes_spmv, "ms_per_launch": ms_spmv,
-            "fp64_spmv": {"ms_per_launch": ms_spmv64, "achieved_GBps": bytes_spmv64 / (ms_spmv64 * 1e-3) / 1e9}}
+    kern = {}
+    names = {0: "k_mg_spmv_dot<float,SplitP> (outer FP64-accurate product, FP32 hi+lo values, + p.Ap)",
+             1: "k_vc_resid (finest-level V-cycle residual, FP32 SBELL SpMV)",
+             2: "k_vc_post (finest-level post-smoothing, FP32 SBELL SpMV + block Jacobi)"}
+    for k in (0, 1, 2):
+        ms_k, by_k = g.time_mg_kernel(k, _lib.METHOD_SPLIT, 30)
+        kern[k] = {"kernel": names[k], "ms_per_launch": ms_k, "algorithmic_bytes_per_launch": by_k,
+                   "achieved_GBps": by_k / (ms_k * 1e-3) / 1e9}
+    ms64, by64 = g.time_mg_kernel(0, _lib.METHOD_FP64, 20)
+    top = max(kern, key=lambda k: kern[k]["ms_per_launch"])
+    achieved = kern[top]["achieved_GBps"]
+    roof = {"bound": "hbm", "kernel": kern[top]["kernel"], "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": f"of {peak_kind}", "traffic": ncu_traffic(top),
+            "algorithmic_bytes_per_launch": kern[top]["algorithmic_bytes_per_launch"],
+            "ms_per_launch": kern[top]["ms_per_launch"],
+            "per_iteration_kernels": [dict(kern[k], frac=kern[k]["achieved_GBps"] / peak,
+                                           traffic=ncu_traffic(k)) for k in (0, 1, 2)],
+            "fp64_outer_product": {"kernel": "k_mg_spmv_dot<double,double> (native FP64 values)",
+                                   "ms_per_launch": ms64, "achieved_GBps": by64 / (ms64 * 1e-3) / 1e9}}
 
     # ---- accuracy at full size: the benchmark's 1e-8 solution and gradient
     # against the same library at 1e-11 (FP64 operator); never fatal
@@ -659,7 +732,7 @@ def run_ours(a):
             g.assemble(precision=64)
             u8, _, _ = g.static_solve(**mixed)
             L8, gE8, _, _ = g.adjoint_gradient(**mixed)
-            tight = dict(mixed, rel_tol=1e-11, max_iter=400)
+            tight = dict(mixed, method=_lib.METHOD_FP64, rel_tol=1e-11, max_iter=400)
             u11, rc11, st11 = g.static_solve(**tight)
             L11, gE11, _, _ = g.adjoint_gradient(**tight)
             rel = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))
@@ -680,11 +753,19 @@ def run_ours(a):
             except Exception as err:
                 accuracy["sample_vs_oracle_error"] = repr(err)[:200]
         clocks = clk.summary()
+        batch = None
+        if not a.no_batch and world == 1:
+            try:
+                batch = batch_measure(steps=3, warmup=2)
+            except Exception as err:  # the headline measurement stands on its own
+                batch = {"error": repr(err)[:300]}
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f64 operator/dots + f32 multigrid", "data": "synthetic (seeded lognormal field)",
+               "vs_baseline": None, "dtype": "f64 (fp32 hi+lo operator values) + f64 dots + f32 multigrid",
+               "data": "synthetic (seeded lognormal field)",
                "config": {"workload": f"block_large {a.nx}x{a.ny}x{a.nz} hex8 static + adjoint",
-                          "n_dof": n_dof, "n_elems": n_el, "rhs_per_step": 1, "method": "CG + geometric multigrid V-cycle (FP32 levels), FP64 operator",
+                          "n_dof": n_dof, "n_elems": n_el, "rhs_per_step": 1,
+                          "method": "CG + geometric multigrid V-cycle (FP32 levels), FP64-accurate split operator",
                           "rel_tol": 1e-8, "l2": "operator 640 MB FP64 + 330 MB FP32 > 129 MB L2 (inputs larger than L2)",
                           "parallelism": f"replicas x{world}"},
                "iterations": iters, "ms_breakdown": {"assemble": stats[-1]["ms_assemble"],
@@ -695,7 +776,7 @@ def run_ours(a):
                                      "iterations": st_plain["iterations"]},
                "speedup_vs_plain_fp64": value / plain_value,
                "roofline": roof, "cpu_baseline": cb, "clocks": clocks, "gpu_launches": launches,
-               "accuracy": accuracy}
+               "accuracy": accuracy, "batch_uq": batch}
         print(json.dumps(out))
     g.close()
     if world > 1:

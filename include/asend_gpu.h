@@ -47,6 +47,10 @@ typedef struct asend_ctx asend_ctx;
 /* solver methods */
 #define ASEND_METHOD_FP64 0   /* plain FP64 PCG (values, SpMV, vectors all FP64)           */
 #define ASEND_METHOD_MIXED 1  /* FP32 SpMV + FP64 vectors/dots + FP64 residual replacement */
+#define ASEND_METHOD_SPLIT 2  /* FP64-accurate SpMV on the FP32 pipes: each FP64 value and
+                                 direction entry held as an FP32 hi + lo pair (same bytes as
+                                 FP64), products in compensated FP32 arithmetic; FP64
+                                 vectors, dots and residuals                               */
 
 /* preconditioners */
 #define ASEND_PC_JACOBI 0     /* point Jacobi                                             */
@@ -144,6 +148,15 @@ int asend_mg_vcycle(asend_ctx* ctx, const float* b, float* z);
  * then runs over all instances at once while step lengths, convergence and
  * stopping are kept per instance and load case. */
 int asend_set_instances(asend_ctx* ctx, int32_t n_inst, const int32_t* node_ptr);
+/* Declares each instance of the stack (after asend_set_instances) a
+ * structured hex8 / brickIM block dims[3i..3i+2] = (nx, ny, nz) in the
+ * numbering of asend_set_block_structure relative to the instance's first
+ * node; instance i's elements are the next nx*ny*nz elements.  Enables
+ * ASEND_PC_MG on the stack: every instance gets its own multigrid hierarchy
+ * and one V-cycle serves all of them, in place of the reference's per-model
+ * block-LDL^T preconditioner (lower_tri_mat_meth.rs:15-241).  Validated
+ * against the connectivity. */
+int asend_set_instance_blocks(asend_ctx* ctx, int32_t n_inst, const int32_t* dims);
 
 /* Node / element sets (model_input.rs:720-860 'sets' blocks).  Returns the
  * set id (>= 0) or a negative error code. */
@@ -260,8 +273,9 @@ int asend_newmark_run(asend_ctx* ctx, const asend_solve_opts* opts, int32_t n_st
                       double* u_final, asend_solve_stats* stats);
 
 /* ---- kernel-level entry points (measurement / tests) ----------------------
- * y = A x with the assembled operator at the given value precision (32/64),
- * host buffers.  Equivalent of SparseMat::vector_multiply
+ * y = A x with the assembled operator at the given value precision (32 =
+ * FP32 values, 64 = FP64, 48 = the split FP32 hi + lo product of
+ * ASEND_METHOD_SPLIT), host buffers.  Equivalent of SparseMat::vector_multiply
  * (list_ent_meth.rs:64-79) plus the penalty product (const_meth.rs:92-103). */
 int asend_apply_operator(asend_ctx* ctx, int32_t precision, const double* x, double* y);
 /* Time n_launch back-to-back operator applications on the library stream with
@@ -269,6 +283,15 @@ int asend_apply_operator(asend_ctx* ctx, int32_t precision, const double* x, dou
  * launch. */
 int asend_time_spmv(asend_ctx* ctx, int32_t precision, int32_t n_launch, double* ms_per_launch,
                     double* bytes_per_launch);
+/* Time n_launch back-to-back launches of one kernel of the multigrid-
+ * preconditioned CG on the assembled operator (building the hierarchy if
+ * needed): kernel 0 = the outer product with its p.Ap reduction in the given
+ * method's value format, 1 = the finest level's V-cycle residual, 2 = its
+ * post-smoothing sweep.  Returns the mean ms per launch and the algorithmic
+ * bytes per launch (values, column indices, gathered and streamed vectors
+ * counted once).  No reference counterpart (measurement). */
+int asend_time_mg_kernel(asend_ctx* ctx, int32_t kernel, int32_t method, int32_t n_launch, double* ms_per_launch,
+                         double* bytes_per_launch);
 /* Number of kernels this library launched since the context was created. */
 int64_t asend_kernel_launches(const asend_ctx* ctx);
 /* The context's CUDA stream (cudaStream_t as void*), so a caller can record
@@ -332,8 +355,8 @@ int asend_dense_sym_eigen(int32_t m, const double* a, double* vals, double* vecs
 int asend_element_matrices(asend_ctx* ctx, int32_t first, int32_t count, double* ke, double* me);
 
 /* y = A x and *energy = x^T A x with the assembled FP64 operator, on DEVICE
- * buffers (x, y: n_dof doubles; energy: one double), without allocating any
- * device memory.  No counterpart in the reference: it exists for callers that
+ * buffers (x, y: n_dof doubles; energy: one double; the three must not
+ * overlap, else ASEND_EINVAL), without allocating any device memory.  No counterpart in the reference: it exists for callers that
  * cannot call cudaMalloc -- applications that give all device memory to their
  * own pool allocator or run under a fixed HBM budget, and optimisation loops
  * that evaluate the energy many times where an allocation could fail or stall.
@@ -342,7 +365,12 @@ int asend_element_matrices(asend_ctx* ctx, int32_t first, int32_t count, double*
  * Limit: 4,194,304 node rows (12,582,912 DOF), 3 DOF per node; larger
  * operators are rejected with ASEND_EINVAL and a message.  The first call on a
  * device looks up the array's device address (a one-time set-up), so make
- * that first call before any stream capture.  The work is enqueued on the
+ * that first call before any stream capture.  With CUDA's lazy module
+ * loading (the default) that first call also loads this part of the library
+ * onto the device, which reserves device memory for the array and its kernel
+ * code; a caller whose pool will take all HBM makes the first call before
+ * the pool does, or sets CUDA_MODULE_LOADING=EAGER.  Later calls allocate
+ * nothing.  The work is enqueued on the
  * context's stream and not synchronised.  All calls share the scratch array:
  * calls that overlap on the GPU (other streams or contexts on the same
  * device) race and must be serialised by the caller. */

@@ -1451,6 +1451,43 @@ int orc_static_solve(orc_model* m, const double* f, double* u, int32_t precond, 
     return status;
 }
 
+// Several load cases against one preconditioner set-up (one factorization
+// for PC_DIRECT): the loop of solve_step over a model's load cases, each as
+// orc_static_solve.  st receives the largest iteration count and residual.
+int orc_static_solve_multi(orc_model* m, int32_t n_rhs, const double* f, double* u, int32_t precond,
+                           int32_t stop_rule, double tol, int32_t max_it, int32_t block_dim, orc_stats* st) {
+    if (!m->assembled) return -1;
+    const int n = m->n_dof;
+    if (st) std::memset(st, 0, sizeof(*st));
+    auto t0 = std::chrono::steady_clock::now();
+    Precond pc;
+    pc.setup(m, precond, block_dim);
+    int status = 0;
+    double relmax = 0.0;
+    for (int r = 0; r < n_rhs; ++r) {
+        std::vector<double> load(f + (size_t)r * n, f + (size_t)(r + 1) * n), zero(n, 0.0);
+        constraint_load(m, zero.data(), load.data());
+        double* ur = u + (size_t)r * n;
+        orc_stats sr;
+        std::memset(&sr, 0, sizeof(sr));
+        if (precond == ORC_PC_DIRECT) {
+            pc.apply(load.data(), ur);
+        } else {
+            std::fill(ur, ur + n, 0.0);
+            status = std::max(status, pcg(m, pc, load.data(), ur, stop_rule, tol, max_it > 0 ? max_it : n, &sr));
+        }
+        relmax = std::max(relmax, true_rel_residual(m, load.data(), ur));
+        if (st) st->iterations = std::max(st->iterations, sr.iterations);
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    if (st) {
+        st->seconds = std::chrono::duration<double>(t1 - t0).count();
+        st->rel_residual = relmax;
+        st->status = status;
+    }
+    return status;
+}
+
 // Static adjoint: model_analysis.rs:1065-1126 (solve_for_adjoint: same
 // operator and solver for lambda = A^-1 dL/du) and :1632-1704 with
 // d_relasticd_d :1379-1457; for a modulus DV on element e the only nonzero

@@ -80,6 +80,10 @@ int orc_surface_traction(const orc_model* m, int32_t n_set, const int32_t* elem_
 int orc_static_solve(orc_model* m, const double* f, double* u, int32_t precond,
                      int32_t stop_rule, double tol, int32_t max_it, int32_t block_dim,
                      orc_stats* st);
+/* All n_rhs load cases f[n_rhs][n_dof] against one preconditioner set-up
+ * (one factorization with ORC_PC_DIRECT); u[n_rhs][n_dof]. */
+int orc_static_solve_multi(orc_model* m, int32_t n_rhs, const double* f, double* u, int32_t precond,
+                           int32_t stop_rule, double tol, int32_t max_it, int32_t block_dim, orc_stats* st);
 
 /* Apply the solve operator (natural numbering): y = A x. */
 int orc_apply_operator(const orc_model* m, const double* x, double* y);

@@ -56,6 +56,8 @@ def load():
             "orc_surface_traction": (C.c_int, [C.c_void_p, C.c_int32, P_i, P_d, C.c_double, P_d, P_d]),
             "orc_static_solve": (C.c_int, [C.c_void_p, P_d, P_d, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                            C.c_int32, C.POINTER(Stats)]),
+            "orc_static_solve_multi": (C.c_int, [C.c_void_p, C.c_int32, P_d, P_d, C.c_int32, C.c_int32, C.c_double,
+                                                 C.c_int32, C.c_int32, C.POINTER(Stats)]),
             "orc_apply_operator": (C.c_int, [C.c_void_p, P_d, P_d]),
             "orc_adjoint_modulus_gradient": (C.c_int, [C.c_void_p, P_d, P_d, P_d, P_d, P_d, C.c_int32, C.c_int32,
                                                        C.c_double, C.c_int32, C.POINTER(Stats)]),
@@ -183,6 +185,15 @@ class Oracle:
         st = Stats()
         rc = self.lib.orc_static_solve(self.m, _p(f), _p(u), precond, stop, tol, max_it, block_dim, C.byref(st))
         return u, rc, st.as_dict()
+
+    def solve_cases(self, F, precond=PC_DIRECT, stop=STOP_RELATIVE, tol=1e-12, max_it=0, block_dim=0):
+        """Every row of F[n_rhs][n_dof] against one preconditioner set-up."""
+        F = np.ascontiguousarray(F, np.float64)
+        U = np.zeros_like(F)
+        st = Stats()
+        rc = self.lib.orc_static_solve_multi(self.m, F.shape[0], _p(F), _p(U), precond, stop, tol, max_it,
+                                             block_dim, C.byref(st))
+        return U, rc, st.as_dict()
 
     def adjoint(self, u, dLdu=None, lam=None, precond=PC_JACOBI, stop=STOP_RELATIVE, tol=1e-10, max_it=0):
         u = np.ascontiguousarray(u, np.float64)

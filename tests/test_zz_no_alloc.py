@@ -34,10 +34,17 @@ def test_operator_energy_noalloc_matches_apply(gpu_lib):
         yd = torch.full_like(xd, float("nan"))
         ed = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
+        free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
         rc = g.lib.asend_operator_energy_noalloc(g.ctx, xd.data_ptr(), yd.data_ptr(), ed.data_ptr())
         assert rc == 0, g.lib.asend_last_error(g.ctx)
         torch.cuda.synchronize()
+        if call > 0:  # the first call may load the module (lazy loading); later calls take no device memory
+            assert torch.cuda.mem_get_info()[0] == free0
+            assert torch.cuda.memory_allocated() == alloc0
         y = yd.cpu().numpy()
         assert np.linalg.norm(y - y_ref) / np.linalg.norm(y_ref) < 1e-11
         assert float(ed.cpu()[0]) == pytest.approx(e_ref, rel=1e-11)
+    # an in-place product (x and y sharing memory) is rejected, not computed wrongly
+    rc = g.lib.asend_operator_energy_noalloc(g.ctx, xd.data_ptr(), xd.data_ptr(), ed.data_ptr())
+    assert rc == -1
     g.close()
