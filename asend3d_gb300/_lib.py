@@ -103,6 +103,10 @@ SIGNATURES = [
     ("asend_material_dv_gradient", c_int, [C.c_void_p, c_int, c_int, c_int, c_int, P_dbl, P_dbl]),
     ("asend_material_dC", c_int, [c_int, c_int, c_dbl, c_dbl, P_dbl]),
     ("asend_time_mg_kernel", c_int, [C.c_void_p, c_int, c_int, c_int, P_dbl, P_dbl]),
+    ("asend_set_orthotropic", c_int, [C.c_void_p, P_dbl]),
+    ("asend_orthotropic_cmat", c_int, [P_dbl, P_dbl]),
+    ("asend_set_damping", c_int, [C.c_void_p, c_dbl, c_dbl, P_dbl]),
+    ("asend_set_lumped_mass", c_int, [C.c_void_p, c_int]),
     ("asend_operator_energy_noalloc", c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("asend_learned_n_params", c_int, []),
     ("asend_learned_init", c_int, [C.c_void_p, C.c_uint64]),

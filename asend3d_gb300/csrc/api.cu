@@ -300,6 +300,39 @@ void build_pattern(Ctx& c) {
     c.pattern_ready = true;
 }
 
+// 6x6 solid stiffness (Voigt 11,22,33,12,13,23, engineering shear) from
+// engineering constants p = E1 E2 E3 nu12 nu13 nu23 G12 G13 G23 by inverting
+// the compliance, as get_solid_stiff (element_properties.rs:648-764) does:
+// S11 = 1/E1, S12 = -nu12/E1, S13 = -nu13/E1, S22 = 1/E2, S23 = -nu23/E2,
+// S33 = 1/E3, S44 = 1/G12, S55 = 1/G13, S66 = 1/G23.  Returns false when the
+// normal block is not positive definite.
+bool orthotropic_cmat(const double* p, double* C) {
+    for (int i = 0; i < 9; ++i)
+        if (!std::isfinite(p[i])) return false;
+    if (!(p[0] > 0 && p[1] > 0 && p[2] > 0 && p[6] > 0 && p[7] > 0 && p[8] > 0)) return false;
+    double S[3][3] = {{1.0 / p[0], -p[3] / p[0], -p[4] / p[0]},
+                      {-p[3] / p[0], 1.0 / p[1], -p[5] / p[1]},
+                      {-p[4] / p[0], -p[5] / p[1], 1.0 / p[2]}};
+    const double c00 = S[1][1] * S[2][2] - S[1][2] * S[2][1];
+    const double c01 = S[1][2] * S[2][0] - S[1][0] * S[2][2];
+    const double c02 = S[1][0] * S[2][1] - S[1][1] * S[2][0];
+    const double det = S[0][0] * c00 + S[0][1] * c01 + S[0][2] * c02;
+    if (!(det > 0.0) || !(S[0][0] > 0.0) || !(S[0][0] * S[1][1] - S[0][1] * S[1][0] > 0.0)) return false;
+    const double inv[3][3] = {{c00 / det, (S[0][2] * S[2][1] - S[0][1] * S[2][2]) / det,
+                               (S[0][1] * S[1][2] - S[0][2] * S[1][1]) / det},
+                              {c01 / det, (S[0][0] * S[2][2] - S[0][2] * S[2][0]) / det,
+                               (S[0][2] * S[1][0] - S[0][0] * S[1][2]) / det},
+                              {c02 / det, (S[0][1] * S[2][0] - S[0][0] * S[2][1]) / det,
+                               (S[0][0] * S[1][1] - S[0][1] * S[1][0]) / det}};
+    for (int i = 0; i < 36; ++i) C[i] = 0.0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) C[6 * i + j] = inv[i][j];
+    C[21] = p[6];
+    C[28] = p[7];
+    C[35] = p[8];
+    return true;
+}
+
 int instance_of_node(const Ctx& c, int node) {
     if (c.n_inst <= 1) return 0;
     return (int)(std::upper_bound(c.inst_node_ptr.begin(), c.inst_node_ptr.end(), node) - c.inst_node_ptr.begin()) - 1;
@@ -653,6 +686,64 @@ int asend_set_modulus(asend_ctx* ctx, const double* E) {
     });
 }
 
+int asend_orthotropic_cmat(const double* props, double* C_out) {
+    if (!props || !C_out) return ASEND_EINVAL;
+    return orthotropic_cmat(props, C_out) ? ASEND_OK : ASEND_EINVAL;
+}
+
+int asend_set_orthotropic(asend_ctx* ctx, const double* props) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.n_el > 0, "set the mesh first");
+        if (!props) {
+            c.ortho.clear();
+            c.d_cmat.release();
+        } else {
+            require(c.type == 8 || c.type == 4,
+                    "orthotropic materials take hex8 / tet4 meshes (elements without condensed internal DOF)");
+            std::vector<double> C((size_t)c.n_el * 36);
+            for (int e = 0; e < c.n_el; ++e)
+                require(orthotropic_cmat(props + (size_t)e * 9, &C[(size_t)e * 36]),
+                        "orthotropic constants give no positive definite stiffness");
+            c.ortho.assign(props, props + (size_t)c.n_el * 9);
+            c.d_cmat.upload(C, c.stream);
+            ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        }
+        c.assembled = c.solved = false;
+        return ASEND_OK;
+    });
+}
+
+int asend_set_damping(asend_ctx* ctx, double rayleigh_cm, double rayleigh_ck, const double* D) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.n_el > 0, "set the mesh first");
+        require(std::isfinite(rayleigh_cm) && std::isfinite(rayleigh_ck) && rayleigh_cm >= 0.0 && rayleigh_ck >= 0.0,
+                "Rayleigh coefficients must be finite and non-negative");
+        require(!(rayleigh_ck != 0.0 || D) || c.type == 8 || c.type == 4,
+                "stiffness-proportional and material damping take hex8 / tet4 meshes (elements without condensed "
+                "internal DOF)");
+        c.ray_cm = rayleigh_cm;
+        c.ray_ck = rayleigh_ck;
+        if (D) {
+            c.dmat.assign(D, D + (size_t)c.n_el * 36);
+            c.d_dmat.upload(c.dmat, c.stream);
+            ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        } else {
+            c.dmat.clear();
+            c.d_dmat.release();
+        }
+        c.assembled = c.solved = false;
+        return ASEND_OK;
+    });
+}
+
+int asend_set_lumped_mass(asend_ctx* ctx, int32_t on) {
+    return guarded(ctx, [&](Ctx& c) {
+        c.lump = on != 0;
+        c.assembled = c.solved = false;
+        return ASEND_OK;
+    });
+}
+
 int asend_add_node_set(asend_ctx* ctx, int32_t n, const int32_t* nodes) {
     return guarded(ctx, [&](Ctx& c) {
         require(n >= 1 && nodes, "empty node set");
@@ -860,8 +951,9 @@ int asend_get_csr(asend_ctx* ctx, int32_t which, int64_t* nnz_out, int64_t* row_
                   double* val) {
     return guarded(ctx, [&](Ctx& c) {
         require(c.assembled, "assemble first");
-        require(which >= 0 && which <= 2, "which must be 0, 1 or 2");
+        require(which >= 0 && which <= 3, "which must be 0, 1, 2 or 3");
         require(which != 1 || c.dynamic, "no mass matrix (static assembly)");
+        require(which != 3 || c.A.d64.n, "no damping matrix (assembly without damping)");
         const Sbell& A = c.A;
         const int b = A.b, b2 = b * b;
         const int64_t nnz = A.nnz_scalar();
@@ -869,7 +961,7 @@ int asend_get_csr(asend_ctx* ctx, int32_t which, int64_t* nnz_out, int64_t* row_
         if (!row_ptr && !col && !val) return ASEND_OK;
         std::vector<double> h;
         if (val) {
-            const DArr<double>& src = (which == 1) ? A.m64 : A.v64;
+            const DArr<double>& src = (which == 1) ? A.m64 : (which == 3) ? A.d64 : A.v64;
             h.resize(src.n);
             ASEND_CUDA(cudaMemcpyAsync(h.data(), src.p, src.n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
             ASEND_CUDA(cudaStreamSynchronize(c.stream));
@@ -1011,6 +1103,12 @@ int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double*
         NvtxRange nvtx_range("asend_adjoint_gradient");
         require(opts != nullptr, "null options");
         require(c.solved, "run a static solve before the adjoint gradient");
+        // the per-element modulus gradient scales an isotropic element; with
+        // orthotropic constants the gradient goes through the strain pairs
+        // (asend_material_dv_gradient)
+        const bool iso = c.ortho.empty();
+        require(iso || !dLdE_out,
+                "per-element modulus gradients need isotropic elements; use asend_material_dv_gradient");
         const size_t n = c.n_dof;
         c.d_gE.alloc(c.n_el);
         DArr<double> part, scal;
@@ -1029,7 +1127,7 @@ int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double*
                 ASEND_CUDA(cudaMemcpyAsync(&v, scal.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
                 ASEND_CUDA(cudaStreamSynchronize(c.stream));
                 L += v;
-                adjoint_contract(c, c.d_x.p + r * n, c.d_x.p + r * n, c.d_gE.p, r > 0);
+                if (iso) adjoint_contract(c, c.d_x.p + r * n, c.d_x.p + r * n, c.d_gE.p, r > 0);
             }
         } else {
             // L = coef * sum_r sum_{node in set} u_r[node, comp]  ('powerNorm', exponent 1)
@@ -1056,7 +1154,7 @@ int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double*
             ASEND_CUDA(cudaEventCreate(&e0));
             ASEND_CUDA(cudaEventCreate(&e1));
             ASEND_CUDA(cudaEventRecord(e0, c.stream));
-            adjoint_contract(c, c.d_lam.p, d_usum.p, c.d_gE.p, false);
+            if (iso) adjoint_contract(c, c.d_lam.p, d_usum.p, c.d_gE.p, false);
             ASEND_CUDA(cudaEventRecord(e1, c.stream));
             ASEND_CUDA(cudaEventSynchronize(e1));
             float mc = 0.f;
@@ -1150,29 +1248,31 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
     });
 }
 
-// dC/dD of an isotropic element (E, nu, G = E / (2 (1 + nu))) for a DV on one
-// component of the reference's compliance S (element_properties.rs:648-764:
-// S00 = 1/E1, S01 = -nu12/E1, S02 = -nu13/E1, S11 = 1/E2, S12 = -nu23/E2,
-// S22 = 1/E3, S33..S55 = 1/G12, 1/G13, 1/G23; C = S^-1): dC = -C dS C.
-static void material_dC(int category, int component, double E, double nu, double* dC) {
+// dC/dD for a DV on one component of the reference's compliance S
+// (element_properties.rs:648-764: S00 = 1/E1, S01 = -nu12/E1, S02 = -nu13/E1,
+// S11 = 1/E2, S12 = -nu23/E2, S22 = 1/E3, S33..S55 = 1/G12, 1/G13, 1/G23;
+// C = S^-1) at engineering constants p = E1 E2 E3 nu12 nu13 nu23 G12 G13 G23:
+// dC = -C dS C.
+static void material_dC_props(int category, int component, const double* p, double* dC) {
     const int k = component - 1;
-    const double G = E / (2.0 * (1.0 + nu));
-    const double la = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), mu = G;
-    double C[36] = {0};
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) C[6 * i + j] = la + (i == j ? 2.0 * mu : 0.0);
-    for (int i = 3; i < 6; ++i) C[7 * i] = mu;
+    double C[36];
+    orthotropic_cmat(p, C);
     double dS[36] = {0};
     if (category == ASEND_DV_MODULUS) {
-        dS[7 * k] = -1.0 / (E * E);
-        if (k == 0) dS[1] = dS[6] = dS[2] = dS[12] = nu / (E * E);
-        if (k == 1) dS[8] = dS[13] = nu / (E * E);
+        const double Ek = p[k];
+        dS[7 * k] = -1.0 / (Ek * Ek);
+        if (k == 0) {
+            dS[1] = dS[6] = p[3] / (Ek * Ek);
+            dS[2] = dS[12] = p[4] / (Ek * Ek);
+        }
+        if (k == 1) dS[8] = dS[13] = p[5] / (Ek * Ek);
     } else if (category == ASEND_DV_SHEAR_MODULUS) {
-        dS[7 * (3 + k)] = -1.0 / (G * G);
+        const double Gk = p[6 + k];
+        dS[7 * (3 + k)] = -1.0 / (Gk * Gk);
     } else {
         const int pr[3][2] = {{0, 1}, {0, 2}, {1, 2}};
         const int a = pr[k][0], b = pr[k][1];
-        dS[6 * a + b] = dS[6 * b + a] = -1.0 / E;
+        dS[6 * a + b] = dS[6 * b + a] = -1.0 / p[a];
     }
     double T[36];
     for (int i = 0; i < 6; ++i)
@@ -1187,6 +1287,19 @@ static void material_dC(int category, int component, double E, double nu, double
             for (int l = 0; l < 6; ++l) s += C[6 * i + l] * T[6 * l + j];
             dC[6 * i + j] = -s;
         }
+}
+
+// The isotropic element (E, nu, G = E / (2 (1 + nu))) as constants.
+static void iso_props(double E, double nu, double* p) {
+    const double G = E / (2.0 * (1.0 + nu));
+    const double q[9] = {E, E, E, nu, nu, nu, G, G, G};
+    std::copy(q, q + 9, p);
+}
+
+static void material_dC(int category, int component, double E, double nu, double* dC) {
+    double p[9];
+    iso_props(E, nu, p);
+    material_dC_props(category, component, p, dC);
 }
 
 int asend_material_dC(int32_t category, int32_t component, double E, double nu, double* dC_out) {
@@ -1228,8 +1341,9 @@ int asend_adjoint_strain_pairs(asend_ctx* ctx, double* pairs_out) {
 // dL/dD for a material design variable over an element set
 // (model_analysis.rs:1692-1700 with d_relasticd_d :1379-1457): the element
 // stiffness C = S^-1 from the compliance S(E1..3, nu12, nu13, nu23,
-// G12, G13, G23) of get_solid_stiff (element_properties.rs:648-764), here
-// isotropic per element (E_e, nu_e, G = E_e / (2 (1 + nu_e))); the DV adds
+// G12, G13, G23) of get_solid_stiff (element_properties.rs:648-764), per
+// element orthotropic (asend_set_orthotropic) or isotropic (E_e, nu_e,
+// G = E_e / (2 (1 + nu_e))); the DV adds
 // coef * D to its component, so dC/dD = -coef C (dS/dE_k | dS/dG_k |
 // dS/dnu_k) C and dL/dD = -sum_e sum_ij (dC/dD)_ij P_e[i][j].
 int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t component, int32_t elem_set,
@@ -1247,7 +1361,8 @@ int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t compone
         for (size_t q = 0; q < set.size(); ++q) {
             const int e = set[q];
             double dC[36];
-            material_dC(category, component, c.E[e], c.nu[e], dC);
+            if (!c.ortho.empty()) material_dC_props(category, component, &c.ortho[(size_t)e * 9], dC);
+            else material_dC(category, component, c.E[e], c.nu[e], dC);
             const double* P = &c.h_pairs[(size_t)e * 36];
             double s = 0.0;
             for (int i = 0; i < 36; ++i) s += dC[i] * P[i];

@@ -69,6 +69,19 @@ void init_tables() {
     g_tables_ready = true;
 }
 
+// Optional element data of the colour assembly: per-element 6x6 stiffness
+// (replacing the isotropic E, nu), material damping matrices, Rayleigh
+// coefficients, the damping coefficient of the Newmark operator and the
+// damping values (nullptr: no damping).
+struct ElemExtra {
+    const double* cmat;
+    const double* dmat;
+    double rcm, rck, cD;
+    double* dvals;
+};
+
+__constant__ int c_voigt[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+
 template <int NN>
 struct ElemTraits;
 template <>
@@ -102,7 +115,7 @@ assemble_colour_kernel(int n_el, const int32_t* __restrict__ el_list, const int3
                        const double* __restrict__ xyz, const double* __restrict__ E,
                        const double* __restrict__ nu, const double* __restrict__ rho,
                        const int32_t* __restrict__ slot_map, T* __restrict__ vals,
-                       double* __restrict__ mvals, double cM) {
+                       double* __restrict__ mvals, double cM, ElemExtra X) {
     constexpr int NIP = ElemTraits<NN>::NIP, NP = ElemTraits<NN>::NP, EB = ElemTraits<NN>::EB;
     __shared__ T s_x[EB][NN][3];
     __shared__ T s_g[EB][NIP][NN][3];
@@ -183,43 +196,78 @@ assemble_colour_kernel(int n_el, const int32_t* __restrict__ el_list, const int3
             m += na * nb * w;
         }
     }
-    const double Ee = E[e], ne = nu[e];
-    const T lam = (T)(Ee * ne / ((1.0 + ne) * (1.0 - 2.0 * ne)));
-    const T mu = (T)(Ee / (2.0 * (1.0 + ne)));
-    const T tr = mu * (S[0][0] + S[1][1] + S[2][2]);
     const T mass = mvals ? m * (T)rho[e] : (T)0;
-    const int32_t slot = slot_map[((size_t)e * NN + a) * NN + b];
-    const int64_t g = slot >> 5, lane = slot & 31;
-    T* vb = vals + (g * 9) * 32 + lane;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            T kij = lam * S[i][j] + mu * S[j][i] + ((i == j) ? tr : (T)0);
-            if (i == j) kij += (T)cM * mass;
-            vb[(i * 3 + j) * 32] += kij;
-        }
-    if (mvals) {
-        double* mb = mvals + (g * 9) * 32 + lane;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) mb[(i * 3 + i) * 32] += (double)mass;
-    }
-    if (a != b) {
-        const int32_t slot2 = slot_map[((size_t)e * NN + b) * NN + a];
-        const int64_t g2 = slot2 >> 5, lane2 = slot2 & 31;
-        T* vt = vals + (g2 * 9) * 32 + lane2;
+    // K_ab: isotropic closed form, or a general 6x6 C contracted with S,
+    // K_ab[i][j] = sum_kl C[v(i,k)][v(j,l)] S[k][l] (v: the Voigt index of a
+    // symmetric index pair), which is B_a^T C B_b integrated
+    T Kab[3][3], Dab[3][3];
+    if (X.cmat) {
+        const double* Ce = X.cmat + (size_t)e * 36;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
-                T kij = lam * S[i][j] + mu * S[j][i] + ((i == j) ? tr : (T)0);
+                T acc = 0;
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+#pragma unroll
+                    for (int l = 0; l < 3; ++l) acc += (T)Ce[6 * c_voigt[i][k] + c_voigt[j][l]] * S[k][l];
+                Kab[i][j] = acc;
+            }
+    } else {
+        const double Ee = E[e], ne = nu[e];
+        const T lam = (T)(Ee * ne / ((1.0 + ne) * (1.0 - 2.0 * ne)));
+        const T mu = (T)(Ee / (2.0 * (1.0 + ne)));
+        const T tr = mu * (S[0][0] + S[1][1] + S[2][2]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) Kab[i][j] = lam * S[i][j] + mu * S[j][i] + ((i == j) ? tr : (T)0);
+    }
+    // damping block (Rayleigh mass / stiffness terms + material B^T D B)
+    if (X.dvals) {
+        const double* De = X.dmat ? X.dmat + (size_t)e * 36 : nullptr;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                T acc = (T)X.rck * Kab[i][j] + ((i == j) ? (T)X.rcm * mass : (T)0);
+                if (De) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+#pragma unroll
+                        for (int l = 0; l < 3; ++l) acc += (T)De[6 * c_voigt[i][k] + c_voigt[j][l]] * S[k][l];
+                }
+                Dab[i][j] = acc;
+            }
+    }
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1 && a == b) break;
+        // pass 0: block (a, b); pass 1: its transpose at (b, a)
+        const int32_t slot = pass ? slot_map[((size_t)e * NN + b) * NN + a] : slot_map[((size_t)e * NN + a) * NN + b];
+        const int64_t g = slot >> 5, lane = slot & 31;
+        T* vb = vals + (g * 9) * 32 + lane;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                T kij = Kab[i][j];
                 if (i == j) kij += (T)cM * mass;
-                vt[(j * 3 + i) * 32] += kij;
+                if (X.dvals) kij += (T)X.cD * Dab[i][j];
+                vb[(pass ? (j * 3 + i) : (i * 3 + j)) * 32] += kij;
             }
         if (mvals) {
-            double* mt = mvals + (g2 * 9) * 32 + lane2;
+            double* mb = mvals + (g * 9) * 32 + lane;
 #pragma unroll
-            for (int i = 0; i < 3; ++i) mt[(i * 3 + i) * 32] += (double)mass;
+            for (int i = 0; i < 3; ++i) mb[(i * 3 + i) * 32] += (double)mass;
+        }
+        if (X.dvals) {
+            double* db = X.dvals + (g * 9) * 32 + lane;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) db[(pass ? (j * 3 + i) : (i * 3 + j)) * 32] += (double)Dab[i][j];
         }
     }
 }
@@ -431,6 +479,44 @@ k_gather_assemble(const int64_t* __restrict__ slice_off, const int32_t* __restri
     }
 }
 
+// Row-sum lumping of the assembled mass (the reference lumps each element's
+// mass by its rows, element_equations.rs:950-971; summed over the elements
+// that is the row sum of the global mass): m := diag(row sums), and the
+// operator's diagonal gains cM times it.
+__global__ void k_lump_mass(int n_rows, const int64_t* __restrict__ slice_off, const uint8_t* __restrict__ row_len,
+                            const uint8_t* __restrict__ diag, double* __restrict__ m64, double* __restrict__ v64,
+                            double cM) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n_rows) return;
+    const int lane = row & 31;
+    const int64_t g0 = slice_off[row >> 5];
+    const int len = row_len[row];
+    double s3[3] = {0, 0, 0};
+    for (int j = 0; j < len; ++j)
+        for (int q = 0; q < 9; ++q) {
+            double* mq = m64 + ((g0 + j) * 9 + q) * 32 + lane;
+            s3[q / 3] += *mq;
+            *mq = 0.0;
+        }
+    const int64_t gd = g0 + diag[row];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        m64[(gd * 9 + 4 * a) * 32 + lane] = s3[a];
+        v64[(gd * 9 + 4 * a) * 32 + lane] += cM * s3[a];
+    }
+}
+
+// d := cm * m (Rayleigh mass-proportional damping of elements whose kernels
+// form no damping block), operator += cD d
+__global__ void k_mass_damping(size_t n, const double* __restrict__ m64, double cm, double cD, double* __restrict__ d64,
+                               double* __restrict__ v64) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double d = cm * m64[i];
+        d64[i] = d;
+        v64[i] += cD * d;
+    }
+}
+
 // FP32 hi / lo copies of the entries the penalty or the unit diagonal changed
 __global__ void k_refresh32(int n, const int64_t* __restrict__ idx, const double* __restrict__ v64,
                             float* __restrict__ v32, float* __restrict__ v32lo) {
@@ -448,7 +534,7 @@ int stream_grid(size_t n) {
 }
 
 template <int NN, typename T>
-void launch_colours(Ctx& c, T* vals, double* mvals) {
+void launch_colours(Ctx& c, T* vals, double* mvals, double cM, const ElemExtra& X) {
     constexpr int EB = ElemTraits<NN>::EB, NP = ElemTraits<NN>::NP;
     const int n_col = (int)c.colour_ptr.size() - 1;
     for (int k = 0; k < n_col; ++k) {
@@ -457,7 +543,7 @@ void launch_colours(Ctx& c, T* vals, double* mvals) {
         const int blocks = (n + EB - 1) / EB;
         assemble_colour_kernel<NN, T><<<blocks, EB * NP, 0, c.stream>>>(
             n, c.d_colour_elems.p + c.colour_ptr[k], c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, c.d_rho.p,
-            c.d_slot_map.p, vals, mvals, c.cM);
+            c.d_slot_map.p, vals, mvals, cM, X);
         ASEND_CUDA(cudaGetLastError());
         ++c.launches;
     }
@@ -602,9 +688,14 @@ void assemble_operator(Ctx& c, int precision) {
     A.v64.alloc(nval);
     A.v32.alloc(nval);
     A.v32lo.alloc(nval);
-    // gather path: FP64 hex8 / brickIM with geometry classes (every value
-    // written once, the penalty scale reduced on the way)
-    const bool gather = precision == 64 && c.cls_ready && c.cls_type == c.type;
+    // damping (Newmark only): a damping value array and its operator term
+    const bool damp = c.dynamic && !c.modal && (c.ray_cm != 0.0 || c.ray_ck != 0.0 || !c.dmat.empty());
+    const bool lump = c.dynamic && !c.modal && c.lump;
+    c.cD = damp ? c.dt * c.gamma * c.cM : 0.0;
+    // gather path: FP64 hex8 / brickIM with geometry classes and isotropic
+    // material, no damping or lumping (every value written once, the penalty
+    // scale reduced on the way)
+    const bool gather = precision == 64 && c.cls_ready && c.cls_type == c.type && c.ortho.empty() && !damp && !lump;
     double* mvals = nullptr;
     if (c.dynamic) {
         A.m64.alloc(nval);
@@ -612,6 +703,23 @@ void assemble_operator(Ctx& c, int precision) {
         mvals = A.m64.p;
     } else {
         A.m64.release();
+    }
+    if (damp) {
+        A.d64.alloc(nval);
+        A.d64.zero(c.stream);
+    } else {
+        A.d64.release();
+    }
+    // lumped mass: elements assemble K (and M apart), the lumped mass enters after
+    const double cM_el = lump ? 0.0 : c.cM;
+    ElemExtra X{};
+    X.cmat = c.ortho.empty() ? nullptr : c.d_cmat.p;
+    if (damp && (c.ray_ck != 0.0 || !c.dmat.empty())) {  // damping blocks formed by the element kernel
+        X.dmat = c.dmat.empty() ? nullptr : c.d_dmat.p;
+        X.rcm = c.ray_cm;
+        X.rck = c.ray_ck;
+        X.cD = c.cD;
+        X.dvals = A.d64.p;
     }
     if (!gather) {
         A.v64.zero(c.stream);
@@ -638,17 +746,29 @@ void assemble_operator(Ctx& c, int precision) {
         ASEND_CUDA(cudaGetLastError());
         ASEND_CUDA(cudaStreamSynchronize(c.stream));  // d_si
     } else {
+        const double cM_save = c.cM;
+        c.cM = cM_el;  // the shell / brickIM kernels read the context's coefficient
         if (c.type == 41) {
             shell_assemble(c, A.v64.p, mvals);  // FP64 element matrices at either precision
         } else if (c.type == 81) {
             brickim_assemble(c, A.v64.p, mvals);  // FP64 condensed element matrices at either precision
         } else if (precision == 64) {
-            if (c.nn == 8) launch_colours<8, double>(c, A.v64.p, mvals);
-            else launch_colours<4, double>(c, A.v64.p, mvals);
+            if (c.nn == 8) launch_colours<8, double>(c, A.v64.p, mvals, cM_el, X);
+            else launch_colours<4, double>(c, A.v64.p, mvals, cM_el, X);
         } else {
-            if (c.nn == 8) launch_colours<8, float>(c, A.v32.p, mvals);
-            else launch_colours<4, float>(c, A.v32.p, mvals);
+            if (c.nn == 8) launch_colours<8, float>(c, A.v32.p, mvals, cM_el, X);
+            else launch_colours<4, float>(c, A.v32.p, mvals, cM_el, X);
             widen_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(nval, A.v32.p, A.v64.p);
+            ++c.launches;
+        }
+        c.cM = cM_save;
+        if (damp && !X.dvals) {  // mass-proportional damping only
+            k_mass_damping<<<stream_grid(nval), 256, 0, c.stream>>>(nval, A.m64.p, c.ray_cm, c.cD, A.d64.p, A.v64.p);
+            ++c.launches;
+        }
+        if (lump) {
+            k_lump_mass<<<(A.n_rows + 127) / 128, 128, 0, c.stream>>>(A.n_rows, A.slice_off.p, A.row_len.p, A.diag.p,
+                                                                      A.m64.p, A.v64.p, c.cM);
             ++c.launches;
         }
         // penalty scale over the element matrix (K [+ cM M]): one per

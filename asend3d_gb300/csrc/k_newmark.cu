@@ -3,14 +3,15 @@
 // Reference (solverSrc/asend_run_job/src/):
 //   Model::solve dynamic loop, model_analysis.rs:591-624: for time = 0, dt, ...
 //     solve_step(time) -> load = f(time) - R(u, v, a) + penalty load
-//     (R = K u + M a [+ D v], element_equations.rs:852-1062), solve
+//     (R = K u + M a + D v, element_equations.rs:852-1062), solve
 //     K_eff du = load, u += du, update_vel_acc (corrector);
 //     then advance_disp (prev := current) and update_vel_acc (predictor).
 //   Node::update_vel_acc node_meth.rs:127-138:
 //     a = c1 (u_prev - u + dt v_prev + c2 a_prev), c1 = 1/(dt^2 (beta - gamma)),
 //     c2 = dt^2 (0.5 + beta - gamma); v = v_prev + dt ((1 - gamma) a_prev + gamma a).
-//   With the operator A = K + c_M M + sf C^T C (c_M = -c1), the step load is
-//     b(t) - A u - M (a - c_M u),  b(t) = amp(t) f0 + sf C^T q.
+//   With the operator A = K + c_M M + c_D D + sf C^T C (c_M = -c1, c_D =
+//   dt gamma c_M, element_equations.rs:977-1005), the step load is
+//     b(t) - A u - M (a - c_M u) - D (v - c_D u),  b(t) = amp(t) f0 + sf C^T q.
 //
 // GB300 design: the step right-hand side is one fused FP64 pass over the
 // operator and mass values (same slots, one column-index read); the
@@ -31,7 +32,8 @@ __global__ void __launch_bounds__(128)
 k_dyn_residual(int n_rows, int n_dof, const int64_t* __restrict__ slice_off, const uint8_t* __restrict__ row_len,
                const int32_t* __restrict__ col, const double* __restrict__ v64, const double* __restrict__ m64,
                double cM, double amp, const double* __restrict__ f0, const double* __restrict__ pen,
-               const double* __restrict__ u, const double* __restrict__ a, double* __restrict__ out) {
+               const double* __restrict__ u, const double* __restrict__ a, double* __restrict__ out,
+               const double* __restrict__ d64, const double* __restrict__ v, double cD) {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= n_rows) return;
     const int lane = row & 31;
@@ -50,6 +52,13 @@ k_dyn_residual(int n_rows, int n_dof, const int64_t* __restrict__ slice_off, con
         for (int r = 0; r < 3; ++r) {
             y[r] += kv[(3 * r) * 32] * u0 + kv[(3 * r + 1) * 32] * u1 + kv[(3 * r + 2) * 32] * u2;
             y[r] += mv[(3 * r) * 32] * w0 + mv[(3 * r + 1) * 32] * w1 + mv[(3 * r + 2) * 32] * w2;
+        }
+        if (d64) {  // + D (v - cD u): the damping force D v without its operator share
+            const double z0 = v[3 * (size_t)c] - cD * u0, z1 = v[3 * (size_t)c + 1] - cD * u1,
+                         z2 = v[3 * (size_t)c + 2] - cD * u2;
+            const double* dv = d64 + (g * 9) * 32 + lane;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) y[r] += dv[(3 * r) * 32] * z0 + dv[(3 * r + 1) * 32] * z1 + dv[(3 * r + 2) * 32] * z2;
         }
     }
 #pragma unroll
@@ -134,7 +143,8 @@ int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* am
     ASEND_CUDA(cudaEventRecord(e0, c.stream));
     for (int s = 0; s < n_steps; ++s) {
         k_dyn_residual<<<g_rows, 128, 0, c.stream>>>(rows, n, c.A.slice_off.p, c.A.row_len.p, c.A.col.p, c.A.v64.p,
-                                                      c.A.m64.p, c.cM, amp[s], d_f0.p, d_pen.p, u.p, a.p, rhs.p);
+                                                      c.A.m64.p, c.cM, amp[s], d_f0.p, d_pen.p, u.p, a.p, rhs.p,
+                                                      c.A.d64.n ? c.A.d64.p : nullptr, v.p, c.cD);
         ASEND_CUDA(cudaGetLastError());
         ++c.launches;
         if (s >= 1 && o.warm_start == 2) {  // extrapolated start (the previous increment at step 1)

@@ -48,6 +48,12 @@ class Problem:
     # design variables: (elem_set, coefficients)
     design_vars: list = field(default_factory=list)
     thickness: np.ndarray | None = None  # per element (shell sections)
+    # orthotropic constants per element [n_el][9] = E1 E2 E3 nu12 nu13 nu23 G12 G13 G23
+    # (solids; replaces E, nu in the stiffness)
+    ortho: np.ndarray | None = None
+    # damping of Newmark runs: (rayleigh_cm, rayleigh_ck, material damping [n_el][36] or None)
+    damping: tuple | None = None
+    lump_mass: bool = False  # row-sum lumped mass in Newmark runs
 
     def add_node_set(self, name, nodes):
         self.node_sets[name] = np.asarray(nodes, dtype=np.int32)
@@ -125,6 +131,17 @@ class GpuSolver:
                                             _ptr(conn, C.c_int32), _ptr(E, C.c_double), _ptr(nu, C.c_double),
                                             None if rho is None else _ptr(rho, C.c_double),
                                             None if thk is None else _ptr(thk, C.c_double)), "set_mesh")
+        if p.ortho is not None:
+            self._ortho = np.ascontiguousarray(p.ortho, dtype=np.float64).reshape(-1, 9)
+            self._check(self.lib.asend_set_orthotropic(self.ctx, _ptr(self._ortho, C.c_double)), "set_orthotropic")
+        if p.damping is not None:
+            cm, ck, dm = p.damping
+            self._dmat = None if dm is None else np.ascontiguousarray(dm, dtype=np.float64).reshape(-1, 36)
+            self._check(self.lib.asend_set_damping(self.ctx, float(cm), float(ck),
+                                                   None if self._dmat is None else _ptr(self._dmat, C.c_double)),
+                        "set_damping")
+        if p.lump_mass:
+            self._check(self.lib.asend_set_lumped_mass(self.ctx, 1), "set_lumped_mass")
         if m.elem_type in (8, 81) and m.conn.shape[0] == m.nx * m.ny * m.nz:
             self._check(self.lib.asend_set_block_structure(self.ctx, m.nx, m.ny, m.nz), "set_block_structure")
         for name, nodes in p.node_sets.items():
@@ -227,12 +244,16 @@ class GpuSolver:
         self._check(self.lib.asend_get_solution(self.ctx, case, _ptr(u, C.c_double)), "get_solution")
         return u
 
-    def adjoint_gradient(self, **kw):
+    def adjoint_gradient(self, want_dLdE=True, **kw):
+        """(L, dL/dE per element or None, status, stats).  want_dLdE=False
+        skips the per-element modulus gradient (orthotropic elements: material
+        DV gradients come from material_dv_gradient)."""
         o = self.opts(**kw)
         L = C.c_double(0.0)
-        g = np.zeros(self.p.mesh.n_elems)
+        g = np.zeros(self.p.mesh.n_elems) if want_dLdE else None
         st = SolveStats()
-        rc = self._check(self.lib.asend_adjoint_gradient(self.ctx, C.byref(o), C.byref(L), _ptr(g, C.c_double),
+        rc = self._check(self.lib.asend_adjoint_gradient(self.ctx, C.byref(o), C.byref(L),
+                                                         _ptr(g, C.c_double) if want_dLdE else None,
                                                          C.byref(st)), "adjoint_gradient")
         return L.value, g, rc, st.as_dict()
 

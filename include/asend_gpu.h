@@ -197,8 +197,10 @@ int asend_get_load_vector(asend_ctx* ctx, int32_t rhs, double* f_out);
  * and keeps M apart (modal analysis; dt, beta, gamma unused). */
 int asend_assemble(asend_ctx* ctx, int32_t precision, int32_t dynamic, double dt, double beta,
                    double gamma);
-/* Assembled operator (K [+ c_M M] + sf C^T C) as scalar CSR in natural DOF
- * numbering with sorted columns.  Pass NULL to query sizes: *nnz_out. */
+/* Assembled matrices as scalar CSR in natural DOF numbering with sorted
+ * columns: which 0 = operator (K [+ c_M M] [+ c_D D] + sf C^T C), 1 = mass,
+ * 2 = operator without the penalty terms, 3 = damping.  Pass NULL to query
+ * sizes: *nnz_out. */
 int asend_get_csr(asend_ctx* ctx, int32_t which, int64_t* nnz_out, int64_t* row_ptr,
                   int32_t* col, double* val);
 /* Element colouring used by the scatter assembly (no two elements of one
@@ -248,13 +250,36 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
  *   asend_material_dv_gradient returns dL/dD for one DV over an element set
  *     (coefficients as asend_add_modulus_design_var), with C = S^-1 from the
  *     reference's compliance form at the element's isotropic E, nu.
- * hex8 and tet4 meshes (elements without condensed internal DOF). */
+ * hex8 and tet4 meshes (elements without condensed internal DOF); elements
+ * with orthotropic constants (asend_set_orthotropic) use their own S. */
 #define ASEND_DV_MODULUS 0
 #define ASEND_DV_SHEAR_MODULUS 1
 #define ASEND_DV_POISSON_RATIO 2
 int asend_adjoint_strain_pairs(asend_ctx* ctx, double* pairs_out);
 int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t component, int32_t elem_set,
                                int32_t n_coef, const double* coefs, double* grad_out);
+/* ---- material model and damping (solids) ----------------------------------
+ * Orthotropic elements (the reference's material 'modulus', 'poissonRatio'
+ * and 'shearModulus' lists, element_properties.rs:648-764): props[n_el][9] =
+ * E1 E2 E3 nu12 nu13 nu23 G12 G13 G23 per element, C = S^-1 from the
+ * compliance form; NULL restores the isotropic E, nu.  hex8 / tet4 meshes.
+ * With orthotropic elements asend_adjoint_gradient takes dLdE_out = NULL and
+ * material DV gradients come from asend_material_dv_gradient. */
+int asend_set_orthotropic(asend_ctx* ctx, const double* props);
+/* The 6 x 6 C (row-major, Voigt 11,22,33,12,13,23, engineering shear) of one
+ * set of constants props[9]; host only. */
+int asend_orthotropic_cmat(const double* props, double* C_out);
+/* Damping of Newmark assemblies (get_rud_dfd0, element_equations.rs:628-850):
+ * D = rayleigh_cm M + rayleigh_ck K + sum_gp B^T D_e B w detJ with the
+ * material damping matrices D[n_el][36] (the reference's material 'damping'
+ * entries, element_properties.rs:1537-1575; may be NULL).  The Newmark
+ * operator gains c_D D with c_D = dt gamma c_M (element_equations.rs:995-1005)
+ * and the step residual D v.  rayleigh_ck and D take hex8 / tet4 meshes. */
+int asend_set_damping(asend_ctx* ctx, double rayleigh_cm, double rayleigh_ck, const double* D);
+/* Row-sum lumped mass in Newmark assemblies (the reference's 'lumpMass: yes',
+ * element_equations.rs:950-971): the mass is diag(row sums of M). */
+int asend_set_lumped_mass(asend_ctx* ctx, int32_t on);
+
 /* dC/dD (row-major 6 x 6, Voigt order) of an isotropic element (E, nu,
  * G = E / (2 (1 + nu))) for a DV of the given category on one component;
  * host only, used by asend_material_dv_gradient. */

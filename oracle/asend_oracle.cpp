@@ -598,9 +598,20 @@ struct orc_model {
     // constraint rows (const_meth.rs:30-90 builds C with one row per set member)
     std::vector<int32_t> c_ptr, c_dof;
     std::vector<double> c_coef, c_rhs;
-    Csr K, M;           // K holds the full solve matrix (K + c_M M when dynamic)
+    Csr K, M;           // K holds the full solve matrix (K + c_M M [+ c_D D] when dynamic)
+    Csr D;              // damping matrix (Rayleigh c_M M + c_K K + material B^T D B)
     bool dynamic = false;
     double cM = 0.0;    // coefficient of M inside K (Newmark)
+    double cD = 0.0;    // coefficient of D inside K (Newmark: dt gamma cM)
+    // per-element 6x6 stiffness (engineering constants through the compliance
+    // form, element_properties.rs:648-764) replacing the isotropic one
+    std::vector<double> cmat;
+    // damping (element_equations.rs:628-850): Rayleigh coefficients and the
+    // materials' 6x6 damping matrices per element (element_properties.rs:1537-1575)
+    double ray_cm = 0.0, ray_ck = 0.0;
+    std::vector<double> dmat;
+    bool lump = false;  // row-sum lumped mass (element_equations.rs:950-971)
+    bool damped() const { return ray_cm != 0.0 || ray_ck != 0.0 || !dmat.empty(); }
     double sf = 0.0;    // penalty scale (model_analysis.rs:255-259)
     bool assembled = false;
     // shell4: physical nodes and connectivity (the assembly view above uses
@@ -633,9 +644,33 @@ void elem_km(const orc_model* m, int e, double* ke, double* me) {
     }
     double xyz[30], C[36];
     elem_xyz(m, e, xyz);
-    iso_cmat(m->E[e], m->nu[e], C);
+    if (!m->cmat.empty()) std::copy(m->cmat.begin() + (size_t)e * 36, m->cmat.begin() + (size_t)(e + 1) * 36, C);
+    else iso_cmat(m->E[e], m->nu[e], C);
     solid_ke(m->ti.type, xyz, C, ke);
     if (me) solid_me(m->ti.type, xyz, m->rho[e], me);
+}
+
+// Element damping matrix (get_rud_dfd0, element_equations.rs:628-850, for
+// elements without internal DOF): ray_cm M_e + ray_ck K_e + sum_gp B^T D B
+// w detJ with the element's material damping matrix D.
+void elem_damp(const orc_model* m, int e, const double* ke, const double* me, double* de) {
+    const int nn = m->ti.nn, tot = 3 * nn;
+    for (int i = 0; i < tot * tot; ++i) de[i] = m->ray_cm * me[i] + m->ray_ck * ke[i];
+    if (m->dmat.empty()) return;
+    double xyz[30], kd[900];
+    elem_xyz(m, e, xyz);
+    solid_ke(m->ti.type, xyz, &m->dmat[(size_t)e * 36], kd);
+    for (int i = 0; i < tot * tot; ++i) de[i] += kd[i];
+}
+
+// Row-sum lumping of an element mass (element_equations.rs:950-971: the
+// inertial residual at unit acceleration of every DOF on the diagonal).
+void lump_rows(int tot, double* me) {
+    for (int i = 0; i < tot; ++i) {
+        double s2 = 0.0;
+        for (int j = 0; j < tot; ++j) s2 += me[i * tot + j];
+        for (int j = 0; j < tot; ++j) me[i * tot + j] = (i == j) ? s2 : 0.0;
+    }
 }
 
 // Node adjacency from element connectivity, sorted; defines the full 3x3-block
@@ -1248,19 +1283,35 @@ int orc_assemble(orc_model* m, int32_t dynamic, double dt, double beta, double g
     build_pattern(m, m->K);
     m->dynamic = dynamic != 0;
     m->cM = 0.0;
+    m->cD = 0.0;
+    const bool damp = dynamic == 1 && m->damped();
+    if ((damp && (m->ray_ck != 0.0 || !m->dmat.empty()) && (m->shell || m->ti.type == 81)) ||
+        (!m->cmat.empty() && m->shell))
+        return -2;  // stiffness / material damping and 6x6 stiffness: elements without internal DOF
+    m->D = Csr();
     if (m->dynamic) {
         m->M = m->K;
         // dynamic == 2: modal analysis, K and M kept apart (model_analysis.rs:783-786
         // assembles the static matrix; the mass enters only as the diagonal D)
         if (dynamic != 2) m->cM = -1.0 / (dt * dt * (beta - gamma));
+        // damping enters with c2 = dt gamma c1 (element_equations.rs:995-1005)
+        if (damp) {
+            m->D = m->K;
+            m->cD = dt * gamma * m->cM;
+        }
     }
     const int nn = m->ti.nn, tot = 3 * nn;
-    std::vector<double> ke(tot * tot), me(tot * tot);
+    std::vector<double> ke(tot * tot), me(tot * tot), mc(tot * tot), de(tot * tot);
     std::vector<int32_t> dofs(tot);
     for (int e = 0; e < m->n_el; ++e) {
         elem_km(m, e, ke.data(), m->dynamic ? me.data() : nullptr);
+        if (damp) {
+            mc = me;  // Rayleigh mass damping uses the consistent mass (get_rud -> get_rum)
+            elem_damp(m, e, ke.data(), mc.data(), de.data());
+        }
+        if (m->dynamic && m->lump) lump_rows(tot, me.data());
         if (m->dynamic)
-            for (int i = 0; i < tot * tot; ++i) ke[i] += m->cM * me[i];
+            for (int i = 0; i < tot * tot; ++i) ke[i] += m->cM * me[i] + (damp ? m->cD * de[i] : 0.0);
         for (int a = 0; a < nn; ++a)
             for (int c = 0; c < 3; ++c) dofs[3 * a + c] = m->conn[(size_t)e * nn + a] * 3 + c;
         for (int i = 0; i < tot; ++i)
@@ -1268,6 +1319,7 @@ int orc_assemble(orc_model* m, int32_t dynamic, double dt, double beta, double g
                 const int64_t k = m->K.find(dofs[i], dofs[j]);
                 m->K.val[k] += ke[i * tot + j];
                 if (m->dynamic) m->M.val[k] += me[i * tot + j];
+                if (damp) m->D.val[k] += de[i * tot + j];
             }
     }
     m->sf = 100000.0 * m->K.max_abs();
@@ -1278,10 +1330,42 @@ int orc_assemble(orc_model* m, int32_t dynamic, double dt, double beta, double g
 int64_t orc_nnz(const orc_model* m) { return (int64_t)m->K.col.size(); }
 double orc_penalty_scale(const orc_model* m) { return m->sf; }
 
+int orc_set_cmat(orc_model* m, const double* C) {
+    if (!C) {
+        m->cmat.clear();
+        return 0;
+    }
+    if (m->shell) return -1;
+    m->cmat.assign(C, C + (size_t)m->n_el * 36);
+    m->assembled = false;
+    return 0;
+}
+
+int orc_set_damping(orc_model* m, double ray_cm, double ray_ck, const double* D) {
+    m->ray_cm = ray_cm;
+    m->ray_ck = ray_ck;
+    if (D) m->dmat.assign(D, D + (size_t)m->n_el * 36);
+    else m->dmat.clear();
+    m->assembled = false;
+    return 0;
+}
+
+int orc_set_lumped_mass(orc_model* m, int32_t on) {
+    m->lump = on != 0;
+    m->assembled = false;
+    return 0;
+}
+
+int orc_orthotropic_cmat(const double* e3, const double* nu3, const double* g3, double* C) {
+    solid_cmat(e3, nu3, g3, C);
+    return 0;
+}
+
 int orc_get_csr(const orc_model* m, int32_t which, int64_t* row_ptr, int32_t* col, double* val) {
     if (!m->assembled) return -1;
-    const Csr& A = (which == 1) ? m->M : m->K;
+    const Csr& A = (which == 1) ? m->M : (which == 3) ? m->D : m->K;
     if (which == 1 && !m->dynamic) return -2;
+    if (which == 3 && m->D.val.empty()) return -2;
     if (row_ptr) std::copy(A.ptr.begin(), A.ptr.end(), row_ptr);
     if (col) std::copy(A.col.begin(), A.col.end(), col);
     if (val) {
@@ -1608,12 +1692,18 @@ int orc_newmark_run(orc_model* m, int32_t n_steps, double dt, double beta, doubl
     pc.setup(m, precond, 0);
     orc_stats st{};
     int status = 0;
+    const bool damp = !m->D.val.empty() && m->cD != 0.0;
     for (int s = 0; s < n_steps; ++s) {
-        // residual R = K u + M a (K here is K + cM*M, so subtract cM*M u)
+        // residual R = K u + M a + D v (K here is K + cM M + cD D, so
+        // subtract cM M u and cD D u)
         std::fill(ku.begin(), ku.end(), 0.0);
         m->K.matvec(u.data(), ku.data());
         for (int i = 0; i < n; ++i) tmp[i] = a[i] - m->cM * u[i];
         m->M.matvec(tmp.data(), ku.data());
+        if (damp) {
+            for (int i = 0; i < n; ++i) tmp[i] = v[i] - m->cD * u[i];
+            m->D.matvec(tmp.data(), ku.data());
+        }
         for (int i = 0; i < n; ++i) load[i] = amp[s] * f_shape[i] - ku[i];
         constraint_load(m, u.data(), load.data());
         if (precond == ORC_PC_DIRECT) {
@@ -1708,6 +1798,7 @@ int orc_newmark_adjoint(orc_model* m, int32_t n_steps, double dt, double beta, d
                         const double* f_shape, const double* amp, int32_t n_obj, const int32_t* obj_dof,
                         const double* obj_w, double* L_out, double* gE) {
     if (!m->assembled || !m->dynamic || m->cM == 0.0 || n_steps < 1) return -1;
+    if (m->cD != 0.0 || m->lump || !m->cmat.empty()) return -2;  // undamped consistent-mass isotropic models
     const int n = m->n_dof;
     std::vector<double> u(n, 0.0), v(n, 0.0), a(n, 0.0), up(n, 0.0), vp(n, 0.0), ap(n, 0.0);
     std::vector<double> load(n), du(n), tmp(n), ku(n);

@@ -60,8 +60,19 @@ int orc_set_constraints(orc_model* m, int32_t n_rows, const int32_t* row_ptr,
  * Sets the penalty scale sf = 1e5 * max|K_ij|. */
 /* dynamic: 0 static, 1 Newmark operator K + cM M (M kept), 2 modal (K and M kept apart). */
 int orc_assemble(orc_model* m, int32_t dynamic, double dt, double beta, double gamma);
+/* Per-element 6x6 solid stiffness C[n_el][36] (Voigt 11,22,33,12,13,23,
+ * engineering shear) in place of the isotropic one; NULL restores it. */
+int orc_set_cmat(orc_model* m, const double* C);
+/* Damping for Newmark assemblies: Rayleigh coefficients (mass, stiffness) and
+ * per-element material damping matrices D[n_el][36] (may be NULL). */
+int orc_set_damping(orc_model* m, double ray_cm, double ray_ck, const double* D);
+/* Row-sum lumped mass in Newmark assemblies (the reference's lumpMass). */
+int orc_set_lumped_mass(orc_model* m, int32_t on);
+/* 6x6 stiffness from engineering constants (E1 E2 E3), (nu12 nu13 nu23),
+ * (G12 G13 G23) by inverting the compliance (element_properties.rs:648-764). */
+int orc_orthotropic_cmat(const double* e3, const double* nu3, const double* g3, double* C);
 int64_t orc_nnz(const orc_model* m);
-/* which: 0 = K, 1 = M, 2 = operator (K [+ c_M M] + sf C^T C) */
+/* which: 0 = K, 1 = M, 2 = operator (K [+ c_M M] + sf C^T C), 3 = damping D */
 int orc_get_csr(const orc_model* m, int32_t which, int64_t* row_ptr, int32_t* col, double* val);
 double orc_penalty_scale(const orc_model* m);
 

@@ -59,6 +59,10 @@ def load():
             "orc_static_solve_multi": (C.c_int, [C.c_void_p, C.c_int32, P_d, P_d, C.c_int32, C.c_int32, C.c_double,
                                                  C.c_int32, C.c_int32, C.POINTER(Stats)]),
             "orc_apply_operator": (C.c_int, [C.c_void_p, P_d, P_d]),
+            "orc_set_cmat": (C.c_int, [C.c_void_p, P_d]),
+            "orc_set_damping": (C.c_int, [C.c_void_p, C.c_double, C.c_double, P_d]),
+            "orc_set_lumped_mass": (C.c_int, [C.c_void_p, C.c_int32]),
+            "orc_orthotropic_cmat": (C.c_int, [P_d, P_d, P_d, P_d]),
             "orc_adjoint_modulus_gradient": (C.c_int, [C.c_void_p, P_d, P_d, P_d, P_d, P_d, C.c_int32, C.c_int32,
                                                        C.c_double, C.c_int32, C.POINTER(Stats)]),
             "orc_adjoint_modulus_component_gradient": (C.c_int, [C.c_void_p, P_d, P_d, C.c_int32, P_d]),
@@ -126,7 +130,20 @@ class Oracle:
             rc = self.lib.orc_set_constraints(self.m, len(rhs), _p(ptr, C.c_int32), _p(dof, C.c_int32), _p(coef),
                                               _p(rhs))
             assert rc == 0
-        self.lib.orc_assemble(self.m, 2 if modal else int(dynamic), dt, beta, gamma)
+        ortho = getattr(problem, "ortho", None)
+        if ortho is not None:
+            self._cmat = np.stack([self.orthotropic_cmat(row) for row in np.asarray(ortho, np.float64).reshape(-1, 9)])
+            assert self.lib.orc_set_cmat(self.m, _p(np.ascontiguousarray(self._cmat))) == 0
+        damping = getattr(problem, "damping", None)
+        if damping is not None:
+            cm, ck, dm = damping
+            self._dmat = None if dm is None else np.ascontiguousarray(dm, np.float64).reshape(-1, 36)
+            self.lib.orc_set_damping(self.m, float(cm), float(ck), None if self._dmat is None else _p(self._dmat))
+        if getattr(problem, "lump_mass", False):
+            self.lib.orc_set_lumped_mass(self.m, 1)
+        rc = self.lib.orc_assemble(self.m, 2 if modal else int(dynamic), dt, beta, gamma)
+        if rc != 0:
+            raise RuntimeError(f"orc_assemble failed ({rc})")
         self.sf = self.lib.orc_penalty_scale(self.m)
 
     def __del__(self):
@@ -185,6 +202,13 @@ class Oracle:
         st = Stats()
         rc = self.lib.orc_static_solve(self.m, _p(f), _p(u), precond, stop, tol, max_it, block_dim, C.byref(st))
         return u, rc, st.as_dict()
+
+    def orthotropic_cmat(self, props):
+        """6x6 C of the constants E1 E2 E3 nu12 nu13 nu23 G12 G13 G23."""
+        p = np.ascontiguousarray(props, np.float64)
+        Cm = np.zeros(36)
+        self.lib.orc_orthotropic_cmat(_p(p[0:3].copy()), _p(p[3:6].copy()), _p(p[6:9].copy()), _p(Cm))
+        return Cm
 
     def solve_cases(self, F, precond=PC_DIRECT, stop=STOP_RELATIVE, tol=1e-12, max_it=0, block_dim=0):
         """Every row of F[n_rhs][n_dof] against one preconditioner set-up."""
