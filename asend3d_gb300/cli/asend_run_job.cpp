@@ -158,6 +158,7 @@ struct Section {
 struct Material {
     double density = 0.0;
     std::vector<double> E, nu, G;
+    std::vector<double> damping;  // 6 x 6 symmetric, empty when none
 };
 struct Model {
     std::vector<int> node_labels, elem_labels;
@@ -239,6 +240,12 @@ Model read_model(const std::string& path) {
                 (h[3] == "E" ? mat.E : h[3] == "nu" ? mat.nu : mat.G) = v;
             } else if (h[2] == "elastic" && h[3] == "stiffness" && !d.empty()) {
                 throw Fail("anisotropic stiffness matrices are not on the GPU path");
+            } else if (h[2] == "damping" && d.size() == 3) {
+                // (row, column, value), 1-based, symmetric (model_input.rs:719-723)
+                if (mat.damping.empty()) mat.damping.assign(36, 0.0);
+                const int i = (int)num(d[0]) - 1, j = (int)num(d[1]) - 1;
+                if (i < 0 || i > 5 || j < 0 || j > 5) throw Fail("damping index out of range 1..6");
+                mat.damping[6 * i + j] = mat.damping[6 * j + i] = num(d[2]);
             }
         }
     }
@@ -456,6 +463,8 @@ struct Runner {
         for (const auto& row : m.conn)
             for (int v : row) conn.push_back(nidx.at(v));
         std::vector<double> E(ne, NAN), nu(ne, NAN), rho(ne, NAN), thk(ne, NAN);
+        std::vector<double> props((size_t)ne * 9, NAN), damp((size_t)ne * 36, 0.0);
+        bool ortho = false, damped = false;
         for (const Section& s : m.sections) {
             if (!m.elem_sets.count(s.elset)) throw Fail("section without a valid elementSet");
             std::string mat_name = s.material;
@@ -469,16 +478,32 @@ struct Runner {
             }
             const Material& mt = m.materials.at(mat_name);
             if (mt.E.empty() || mt.nu.empty()) throw Fail("material " + mat_name + " needs E and nu");
-            if (mt.E[0] != mt.E[1] || mt.E[0] != mt.E[2] || mt.nu[0] != mt.nu[1] || mt.nu[0] != mt.nu[2])
-                throw Fail("orthotropic materials are not on the GPU path");
-            if (!mt.G.empty() && std::fabs(mt.G[0] - mt.E[0] / (2.0 * (1.0 + mt.nu[0]))) > 1e-9 * std::fabs(mt.G[0]))
-                throw Fail("G must equal E / (2 (1 + nu)) on the isotropic GPU path");
+            const double Giso = mt.E[0] / (2.0 * (1.0 + mt.nu[0]));
+            std::vector<double> G = mt.G.empty() ? std::vector<double>(3, Giso) : mt.G;
+            const bool iso = mt.E[0] == mt.E[1] && mt.E[0] == mt.E[2] && mt.nu[0] == mt.nu[1] &&
+                             mt.nu[0] == mt.nu[2] && G[0] == G[1] && G[0] == G[2] &&
+                             std::fabs(G[0] - Giso) <= 1e-9 * std::fabs(G[0]);
+            if (!iso) {  // orthotropic constants through the compliance form (element_properties.rs:648-764)
+                if (s.type != "solid" || mt.G.empty())
+                    throw Fail("orthotropic materials take solid sections with E, nu and G lists");
+                ortho = true;
+            }
+            if (!mt.damping.empty()) {
+                if (s.type != "solid") throw Fail("material damping takes solid sections");
+                damped = true;
+            }
             for (int lab : m.elem_sets.at(s.elset)) {
                 const int e = eidx.at(lab);
                 E[e] = mt.E[0];
                 nu[e] = mt.nu[0];
                 rho[e] = mt.density;
                 thk[e] = t;
+                for (int k = 0; k < 3; ++k) {
+                    props[(size_t)e * 9 + k] = mt.E[k];
+                    props[(size_t)e * 9 + 3 + k] = mt.nu[k];
+                    props[(size_t)e * 9 + 6 + k] = G[k];
+                }
+                if (!mt.damping.empty()) std::copy(mt.damping.begin(), mt.damping.end(), damp.begin() + (size_t)e * 36);
             }
         }
         for (int e = 0; e < ne; ++e)
@@ -488,6 +513,8 @@ struct Runner {
         check(asend_set_mesh(ctx, m.elem_type, n_nodes, m.coords.data(), ne, conn.data(), E.data(), nu.data(),
                              rho.data(), m.elem_type == 41 ? thk.data() : nullptr),
               "set_mesh");
+        if (ortho) check(asend_set_orthotropic(ctx, props.data()), "set_orthotropic");
+        if (damped) check(asend_set_damping(ctx, 0.0, 0.0, damp.data()), "set_damping");
         for (const auto& name : m.node_set_order) {
             std::vector<int32_t> v;
             for (int lab : m.node_sets.at(name)) v.push_back(nidx.at(lab));
@@ -543,13 +570,13 @@ struct Runner {
         for (const char* k : {"thermal", "diffusion", "fluid", "nonlinearGeom"})
             if (solve_kv.count(k) && solve_kv[k].find("yes") != std::string::npos)
                 throw Fail(std::string(k) + " analysis is not on the GPU path");
-        // element_equations.rs:950-971; the GPU path uses the consistent mass
-        if (solve_kv.count("lumpMass") && solve_kv["lumpMass"].find("yes") != std::string::npos)
-            throw Fail("lumped-mass dynamics is not on the GPU path");
         if (solve_kv.count("userUpdate") && solve_kv["userUpdate"].find("yes") != std::string::npos)
             throw Fail("user update hooks are not on the GPU path");
         if (ctx) { asend_destroy(ctx); ctx = nullptr; }
         setup();
+        // lumpMass: row-sum lumped mass in dynamic runs (element_equations.rs:950-971)
+        const bool lump = solve_kv.count("lumpMass") && solve_kv["lumpMass"].find("yes") != std::string::npos;
+        check(asend_set_lumped_mass(ctx, lump ? 1 : 0), "set_lumped_mass");
         const asend_solve_opts o = opts(false);
         asend_solve_stats st{};
         const int n = asend_n_dof(ctx);

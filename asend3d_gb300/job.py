@@ -210,6 +210,12 @@ def read_model(path) -> ModelInput:
                 m.materials[h1][h3] = vals * 3 if len(vals) == 1 else vals
             elif h2 == "elastic" and h3 == "stiffness" and data:
                 raise NotImplementedError("anisotropic stiffness matrices are not on the GPU path")
+            elif h2 == "damping" and len(data) == 3:
+                # (row, column, value), 1-based, symmetric (model_input.rs:719-723)
+                d = m.materials[h1].setdefault("damping", [0.0] * 36)
+                i, j, v = int(data[0]) - 1, int(data[1]) - 1, float(data[2])
+                d[6 * i + j] = v
+                d[6 * j + i] = v
     return m
 
 
@@ -362,6 +368,9 @@ class JobRunner:
         eidx = {lab: i for i, lab in enumerate(m.elem_labels)}
         ne = len(m.elem_labels)
         E, nu, rho, thk = (np.full(ne, np.nan) for _ in range(4))
+        props = np.full((ne, 9), np.nan)  # E1 E2 E3 nu12 nu13 nu23 G12 G13 G23
+        damp = np.zeros((ne, 36))
+        ortho = False
         for sec in m.sections:
             es = sec.get("elementSet")
             if es is None or es not in m.elem_sets:
@@ -379,16 +388,31 @@ class JobRunner:
             else:
                 raise NotImplementedError(f"{sec['type']} sections are not on the GPU path")
             Ev, nv = mat.get("E", [np.nan] * 3), mat.get("nu", [np.nan] * 3)
-            if len(set(Ev)) != 1 or len(set(nv)) != 1:
-                raise NotImplementedError("orthotropic materials are not on the GPU path")
-            if "G" in mat:
-                G = mat["G"]
-                if len(set(G)) != 1 or abs(G[0] - Ev[0] / (2 * (1 + nv[0]))) > 1e-9 * abs(G[0]):
-                    raise NotImplementedError("G must equal E / (2 (1 + nu)) on the isotropic GPU path")
+            G = mat.get("G", [Ev[0] / (2 * (1 + nv[0]))] * 3)
+            iso = (len(set(Ev)) == 1 and len(set(nv)) == 1 and len(set(G)) == 1
+                   and abs(G[0] - Ev[0] / (2 * (1 + nv[0]))) <= 1e-9 * abs(G[0]))
+            if not iso:
+                # orthotropic constants through the compliance form (element_properties.rs:648-764)
+                if sec["type"] != "solid" or "G" not in mat:
+                    raise NotImplementedError("orthotropic materials take solid sections with E, nu and G lists")
+                ortho = True
+            props[els] = list(Ev) + list(nv) + list(G)
+            if "damping" in mat:
+                if sec["type"] != "solid":
+                    raise NotImplementedError("material damping takes solid sections")
+                damp[els] = mat["damping"]
             E[els], nu[els], rho[els], thk[els] = Ev[0], nv[0], mat.get("density", 0.0), t
         if np.isnan(E).any():
             raise ValueError("elements without a section")
         p = Problem(mesh, E, nu, rho, thickness=None if np.isnan(thk).all() else thk)
+        if ortho:
+            if m.elem_type not in (8, 4):
+                raise NotImplementedError("orthotropic materials take hex8 / tet4 meshes on the GPU path")
+            p.ortho = props
+        if np.any(damp):
+            if m.elem_type not in (8, 4):
+                raise NotImplementedError("material damping takes hex8 / tet4 meshes on the GPU path")
+            p.damping = (0.0, 0.0, damp)
         for name, labs in m.node_sets.items():
             p.add_node_set(name, [nidx[v] for v in labs])
         if "all" not in m.node_sets:
@@ -509,11 +533,11 @@ class JobRunner:
         for k in ("thermal", "diffusion", "fluid", "nonlinearGeom"):
             if cmd.get(k):
                 raise NotImplementedError(f"{k} analysis is not on the GPU path")
-        if cmd.get("lumpMass"):  # element_equations.rs:950-971; the GPU path uses the consistent mass
-            raise NotImplementedError("lumped-mass dynamics is not on the GPU path")
         if cmd.get("userUpdate"):
             raise NotImplementedError("user update hooks are not on the GPU path")
         g = self._solver()
+        # lumpMass: row-sum lumped mass in dynamic runs (element_equations.rs:950-971)
+        g._check(g.lib.asend_set_lumped_mass(g.ctx, 1 if cmd.get("lumpMass") else 0), "set_lumped_mass")
         dpn = self.problem.mesh.dpn
         n = self.problem.mesh.n_nodes
         if not cmd.get("dynamic"):

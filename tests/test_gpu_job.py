@@ -95,3 +95,67 @@ def test_cli_matches_python_runner(gpu_lib, tmp_path):
         assert fa.shape == fb.shape, name
         # summation order differs (numpy vs the C++ loop) in reactions and sums
         assert np.allclose(fa, fb, rtol=1e-12, atol=1e-12 * np.abs(fa).max()), name
+
+
+def write_dynamic_job(d):
+    """The cantilever with an orthotropic, materially damped material and a
+    lumped-mass Newmark run under the constant tip load."""
+    m, xmin, xmax = write_cantilever_job(d, etype="brick8", modal=False)
+    model = (d / "model.yaml").read_text()
+    iso = "      E: [1000000.0]\n      nu: 0.0\n      G: 500000.0"
+    assert iso in model
+    model = model.replace(iso, "      E: [1000000.0, 500000.0, 400000.0]\n      nu: [0.2, 0.25, 0.3]\n"
+                               "      G: [300000.0, 250000.0, 200000.0]\n    damping:\n    - [1, 1, 40.0]\n"
+                               "    - [2, 2, 40.0]\n    - [3, 3, 40.0]\n    - [1, 2, 10.0]\n    - [4, 4, 20.0]")
+    (d / "model.yaml").write_text(model)
+    job = ["jobCommands:",
+           "- command: readModelInput", "  fileName: model.yaml",
+           "- command: readConstraints", "  fileName: constraints.yaml",
+           "- command: readLoads", "  fileName: loads.yaml",
+           "- command: solve", "  elastic: yes", "  dynamic: yes", "  timeStep: 0.002", "  simPeriod: 0.08",
+           "  newmarkBeta: 0.25", "  newmarkGamma: 0.5", "  lumpMass: yes", "  solverMethod: iterative",
+           "  convergenceTol: 1.0e-12",
+           "- command: writeNodeResults", f"  fileName: {d / 'nodes.csv'}", "  nodeSet: xMax",
+           "  fields:", "  - displacement"]
+    (d / "job.yaml").write_text("\n".join(job) + "\n")
+    return m, xmin, xmax
+
+
+def test_job_lumped_mass_orthotropic_damped_dynamics(gpu_lib, oracle_lib, tmp_path):
+    """lumpMass, orthotropic constants and material damping from job files:
+    the Python runner against the oracle's Newmark run (1e-8 of the largest
+    displacement), and the C++ runner against the Python runner (1e-12)."""
+    import subprocess
+
+    from asend3d_gb300 import build
+
+    d1, d2 = tmp_path / "py", tmp_path / "cli"
+    d1.mkdir()
+    d2.mkdir()
+    m, xmin, xmax = write_dynamic_job(d1)
+    write_dynamic_job(d2)
+    J.JobRunner(d1 / "job.yaml").run()
+    head, rows = read_csv(d1 / "nodes.csv")
+    props = np.tile([1e6, 5e5, 4e5, 0.2, 0.25, 0.3, 3e5, 2.5e5, 2e5], (m.n_elems, 1))
+    D = np.zeros(36)
+    for i, j, v in ((0, 0, 40.0), (1, 1, 40.0), (2, 2, 40.0), (0, 1, 10.0), (3, 3, 20.0)):
+        D[6 * i + j] = D[6 * j + i] = v
+    p = Problem(m, np.full(m.n_elems, 1e6), np.full(m.n_elems, 0.2), np.full(m.n_elems, 1.0),
+                ortho=props, damping=(0.0, 0.0, np.tile(D, (m.n_elems, 1))), lump_mass=True)
+    p.add_node_set("xMin", xmin)
+    p.add_node_set("xMax", xmax)
+    p.fix_displacement("xMin")
+    p.add_nodal_force("xMax", [0.0, 0.0, -2.0 / len(xmax)])
+    n_steps = 40
+    o = oracle_lib.Oracle(p, dynamic=True, dt=0.002, beta=0.25, gamma=0.5)
+    _, uo, rc, _ = o.newmark(n_steps, 0.002, 0.25, 0.5, o.loads()[0], np.ones(n_steps), -1,
+                             precond=oracle_lib.PC_DIRECT)
+    assert rc == 0
+    uo = uo.reshape(-1, 3)
+    assert np.abs(rows[:, 1:4] - uo[xmax]).max() <= 1e-8 * np.abs(uo).max()
+    build.build()
+    build.build_cli()
+    out = subprocess.run([str(build.CLI), str(d2 / "job.yaml")], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    _, rows2 = read_csv(d2 / "nodes.csv")
+    assert np.allclose(rows2, rows, rtol=1e-12, atol=1e-12 * np.abs(rows).max())

@@ -183,7 +183,7 @@ def test_unsupported_inputs(tmp_path):
     r.model = J.ModelInput()
     with pytest.raises(NotImplementedError, match="thermal"):
         r.cmd_solve(r.cmds[0])
-    for key, msg in (("lumpMass", "lumped-mass"), ("userUpdate", "user update")):
+    for key, msg in (("userUpdate", "user update"),):
         (tmp_path / "j.yaml").write_text(f"jobCommands:\n- command: solve\n  dynamic: yes\n  {key}: yes\n")
         r = J.JobRunner(tmp_path / "j.yaml")
         r.model = J.ModelInput()

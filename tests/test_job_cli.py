@@ -66,11 +66,3 @@ def test_parse_shell_model(cli, tmp_path):
     j = json.loads(out.stdout)
     assert j["elem_type"] == 41 and len(j["conn"]) == m.n_elems and all(len(r) == 4 for r in j["conn"])
     assert j["elem_sets"]["all"] == list(range(m.n_elems))
-
-
-def test_cli_rejects_lumped_mass(cli, tmp_path):
-    write_cantilever_job(tmp_path)
-    (tmp_path / "j2.yaml").write_text("jobCommands:\n- command: readModelInput\n  fileName: model.yaml\n"
-                                      "- command: solve\n  dynamic: yes\n  lumpMass: yes\n")
-    out = subprocess.run([cli, str(tmp_path / "j2.yaml")], capture_output=True, text=True)
-    assert out.returncode == 1 and "lumped-mass dynamics is not on the GPU path" in out.stderr
