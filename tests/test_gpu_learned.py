@@ -113,12 +113,10 @@ def test_vcycle_loss_gradient_matches_finite_differences(gpu_lib):
     """The multigrid objective's gradient (V-cycle forward, adjoint coarse
     correction, block chain, network backward) against differences of the GPU
     loss in the FP32 output biases b3[0..5] (not BF16-rounded).  The loss is
-    a high-degree polynomial in the block scale e^(2 y), so the central
-    difference is Richardson-extrapolated (h and h/2) to cancel its h^2 term.
-    Tolerance 5%: the measured agreement is 3.8% (b3[0]); the gap is not the
-    difference truncation (the extrapolation moves the difference by 1.5%)
-    and is attributed to the FP32 Gauss-Jordan inverse of the penalty-stiffened
-    coarsest operator, whose asymmetry the adjoint correction assumes away."""
+    a high-degree polynomial in the block scale e^(2 y), so the derivative is
+    the linear coefficient of a quartic fitted to eight evaluations around the
+    parameter (single central differences of the FP32 loss moved by several
+    percent between builds).  Tolerance 5%."""
     g = GpuSolver(configs.learned_patch(16, 8, 8))
     g.assemble(64)
     p = _oracle_params(7, last_scale=0.02)
@@ -129,18 +127,23 @@ def test_vcycle_loss_gradient_matches_finite_differences(gpu_lib):
     loss, grad = g.learned_loss_grad()
     assert np.isfinite(loss) and loss > 0
 
-    def central(k, h):
-        pp, pm = p.copy(), p.copy()
-        pp[lo.N_PARAMS - 8 + k] += h
-        pm[lo.N_PARAMS - 8 + k] -= h
-        g.set_learned_params(pp)
-        lp = g.learned_train(0)
-        g.set_learned_params(pm)
-        lm = g.learned_train(0)
-        return (lp - lm) / (float(pp[lo.N_PARAMS - 8 + k]) - float(pm[lo.N_PARAMS - 8 + k]))
+    def fitted_slope(k):
+        # the loss at eight offsets h of the bias, fitted by a quartic in h:
+        # its linear coefficient is the derivative, the fit averages out the
+        # FP32 rounding of the individual loss evaluations
+        hs = np.array([-4e-3, -2e-3, -1e-3, -5e-4, 5e-4, 1e-3, 2e-3, 4e-3])
+        vals = []
+        for h in hs:
+            pp = p.copy()
+            pp[lo.N_PARAMS - 8 + k] += h
+            g.set_learned_params(pp)
+            vals.append(g.learned_train(0))
+        hh = np.array([float(np.float32(p[lo.N_PARAMS - 8 + k]) + np.float32(h)) - float(np.float32(p[lo.N_PARAMS - 8 + k]))
+                       for h in hs])
+        return np.polyfit(hh, np.array(vals) - loss, 4)[-2]
 
     for k in range(6):
-        fd = (4.0 * central(k, 1e-3) - central(k, 2e-3)) / 3.0
+        fd = fitted_slope(k)
         gk = grad[lo.N_PARAMS - 8 + k]
         assert abs(fd - gk) <= 0.05 * max(abs(fd), 1e-3 * abs(loss)), (k, fd, gk)
     g.close()
