@@ -22,6 +22,7 @@ ASEND_EINVAL, ASEND_ECUDA, ASEND_ESTATE = -1, -2, -3
 METHOD_FP64, METHOD_MIXED, METHOD_SPLIT = 0, 1, 2
 PC_JACOBI, PC_BLOCK, PC_LEARNED, PC_MG, PC_MG_LEARNED = 0, 1, 2, 3, 4
 OBJ_DISPLACEMENT, OBJ_COMPLIANCE = 0, 1
+LOAD_BODY_FORCE, LOAD_GRAVITY, LOAD_CENTRIFUGAL = 0, 1, 2
 LEARN_BLOCK, LEARN_MG = 0, 1
 DV_MODULUS, DV_SHEAR_MODULUS, DV_POISSON_RATIO = 0, 1, 2
 
@@ -74,6 +75,8 @@ SIGNATURES = [
     ("asend_add_constraint", c_int, [C.c_void_p, c_int, P_int, P_int, P_dbl, c_dbl]),
     ("asend_add_nodal_force", c_int, [C.c_void_p, c_int, c_int, P_dbl]),
     ("asend_add_surface_traction", c_int, [C.c_void_p, c_int, c_int, P_dbl, c_dbl, P_dbl]),
+    ("asend_add_surface_pressure", c_int, [C.c_void_p, c_int, c_int, P_dbl, c_dbl, c_dbl]),
+    ("asend_add_body_load", c_int, [C.c_void_p, c_int, c_int, c_int, P_dbl, c_dbl, P_dbl, P_dbl]),
     ("asend_add_load_vector", c_int, [C.c_void_p, c_int, P_dbl]),
     ("asend_clear_loads", c_int, [C.c_void_p]),
     ("asend_n_dof", c_int, [C.c_void_p]),

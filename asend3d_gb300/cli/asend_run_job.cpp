@@ -284,6 +284,7 @@ struct Load {
     std::string type, node_set, elem_set;
     double load[6] = {0, 0, 0, 0, 0, 0}, norm_dir[3] = {0, 0, 0}, norm_tol = 1.0;
     double t0 = 0.0, t1 = 1e100;
+    double center[3] = {0, 0, 0}, axis[3] = {0, 0, 1}, omega = 0.0;  // centrifugal
 };
 std::vector<Load> read_loads(const std::string& path) {
     std::vector<Load> out;
@@ -292,7 +293,9 @@ std::vector<Load> read_loads(const std::string& path) {
         const auto& d = r.data;
         const std::string& k = r.h[1];
         if (k == "type" && d.size() == 1) {
-            if (d[0] != "nodalForce" && d[0] != "surfaceTraction") throw Fail(d[0] + " loads are not on the GPU path");
+            if (d[0] != "nodalForce" && d[0] != "surfaceTraction" && d[0] != "surfacePressure" && d[0] != "bodyForce" &&
+                d[0] != "gravitational" && d[0] != "centrifugal")
+                throw Fail(d[0] + " loads are not on the GPU path");
             out.emplace_back();
             out.back().type = d[0];
         } else if (out.empty()) {
@@ -310,6 +313,10 @@ std::vector<Load> read_loads(const std::string& path) {
         } else if (k == "activeTime" && !d.empty()) {
             out.back().t0 = num(d[0]);
             out.back().t1 = d.size() > 1 ? num(d[1]) : 1e100;
+        } else if ((k == "center" || k == "axis") && d.size() == 3) {  // model_input.rs:1103-1112
+            for (int i = 0; i < 3; ++i) (k == "center" ? out.back().center : out.back().axis)[i] = num(d[i]);
+        } else if (k == "angularVelocity" && !d.empty()) {
+            out.back().omega = num(d[0]);
         }
     }
     return out;
@@ -542,9 +549,17 @@ struct Runner {
             if (!(l.t0 <= time && time <= l.t1)) continue;
             if (l.type == "nodalForce") {
                 check(asend_add_nodal_force(ctx, 0, set_id.at(l.node_set), l.load), "add_nodal_force");
-            } else {
+            } else if (l.type == "surfaceTraction") {
                 check(asend_add_surface_traction(ctx, 0, elset_id.at(l.elem_set), l.norm_dir, l.norm_tol, l.load),
                       "add_surface_traction");
+            } else if (l.type == "surfacePressure") {
+                check(asend_add_surface_pressure(ctx, 0, elset_id.at(l.elem_set), l.norm_dir, l.norm_tol, l.load[0]),
+                      "add_surface_pressure");
+            } else {
+                const int kind = l.type == "bodyForce" ? ASEND_LOAD_BODY_FORCE
+                                 : l.type == "gravitational" ? ASEND_LOAD_GRAVITY : ASEND_LOAD_CENTRIFUGAL;
+                check(asend_add_body_load(ctx, 0, elset_id.at(l.elem_set), kind, l.load, l.omega, l.center, l.axis),
+                      "add_body_load");
             }
         }
     }

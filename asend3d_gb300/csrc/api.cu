@@ -809,63 +809,205 @@ int asend_add_nodal_force(asend_ctx* ctx, int32_t rhs, int32_t node_set, const d
 
 // surfaceTraction (element_equations.rs:1970-2043); surface faces are faces
 // owned by one element only (model_prep.rs:510-554).
+// Surface traction (traction given) or pressure (traction = -p n on each
+// loaded face, n its outward unit normal): get_app_load_dfd0,
+// element_equations.rs:1970-2043.
+static void surface_load(Ctx& c, int32_t rhs, int32_t elem_set, const double* norm_dir, double norm_tol_deg,
+                         const double* traction, double pressure) {
+    require(c.type == 8 || c.type == 81 || c.type == 4, "surface loads apply to solid element faces");
+    ensure_case(c, rhs);
+    require(elem_set >= 0 && elem_set < (int)c.elem_sets.size() && norm_dir, "unknown element set");
+    const int nf = (c.nn == 8) ? 6 : 4, fnn = (c.nn == 8) ? 4 : 3;
+    auto face_nodes = [&](int fi) -> const int* { return c.nn == 8 ? kHexFaces[fi] : kTetFaces[fi]; };
+    auto key = [&](int e, int fi) {
+        std::array<int32_t, 4> k{-1, -1, -1, -1};
+        const int* ln = face_nodes(fi);
+        for (int q = 0; q < fnn; ++q) k[q] = c.conn[(size_t)e * c.nn + ln[q]];
+        for (int i = 1; i < fnn; ++i)
+            for (int j = i; j > 0 && k[j - 1] > k[j]; --j) std::swap(k[j - 1], k[j]);
+        return k;
+    };
+    std::vector<std::array<int32_t, 4>> all;
+    all.reserve((size_t)c.n_el * nf);
+    for (int e = 0; e < c.n_el; ++e)
+        for (int fi = 0; fi < nf; ++fi) all.push_back(key(e, fi));
+    std::sort(all.begin(), all.end());
+    const double cos_tol = std::cos(kPi / 180.0 * norm_tol_deg);
+    double el_ld[24], keep[24];
+    for (int e : c.elem_sets[elem_set]) {
+        bool any = false;
+        for (int fi = 0; fi < nf; ++fi) {
+            const auto k = key(e, fi);
+            auto rg = std::equal_range(all.begin(), all.end(), k);
+            if (rg.second - rg.first != 1) continue;
+            const int* ln = face_nodes(fi);
+            double v1[3], v2[3], nr[3];
+            for (int i = 0; i < 3; ++i) {
+                const double* x0 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[0]]];
+                const double* x1 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[1]]];
+                const double* x2 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[2]]];
+                if (fnn == 4) {
+                    const double* x3 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[3]]];
+                    v1[i] = x2[i] - x0[i];
+                    v2[i] = x3[i] - x1[i];
+                } else {
+                    v1[i] = x1[i] - x0[i];
+                    v2[i] = x2[i] - x0[i];
+                }
+            }
+            nr[0] = v1[1] * v2[2] - v1[2] * v2[1];
+            nr[1] = v1[2] * v2[0] - v1[0] * v2[2];
+            nr[2] = v1[0] * v2[1] - v1[1] * v2[0];
+            const double l = std::sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
+            const double dp = (norm_dir[0] * nr[0] + norm_dir[1] * nr[1] + norm_dir[2] * nr[2]) / l;
+            if (!(dp > cos_tol)) continue;
+            double tr[3];
+            for (int i = 0; i < 3; ++i) tr[i] = traction ? traction[i] : -pressure * nr[i] / l;
+            face_load(c, e, ln, fnn, tr, el_ld);
+            std::copy(el_ld, el_ld + 3 * c.nn, keep);  // last loaded face survives
+            any = true;
+        }
+        if (any)
+            for (int i = 0; i < 3 * c.nn; ++i)
+                c.loads[rhs][(size_t)c.conn[(size_t)e * c.nn + i / 3] * 3 + i % 3] += keep[i];
+    }
+}
+
 int asend_add_surface_traction(asend_ctx* ctx, int32_t rhs, int32_t elem_set, const double* norm_dir,
                                double norm_tol_deg, const double* traction) {
     return guarded(ctx, [&](Ctx& c) {
-        require(c.type == 8 || c.type == 81 || c.type == 4, "surface tractions apply to solid element faces");
-        ensure_case(c, rhs);
-        require(elem_set >= 0 && elem_set < (int)c.elem_sets.size() && norm_dir && traction, "unknown element set");
-        const int nf = (c.nn == 8) ? 6 : 4, fnn = (c.nn == 8) ? 4 : 3;
-        auto face_nodes = [&](int fi) -> const int* { return c.nn == 8 ? kHexFaces[fi] : kTetFaces[fi]; };
-        auto key = [&](int e, int fi) {
-            std::array<int32_t, 4> k{-1, -1, -1, -1};
-            const int* ln = face_nodes(fi);
-            for (int q = 0; q < fnn; ++q) k[q] = c.conn[(size_t)e * c.nn + ln[q]];
-            for (int i = 1; i < fnn; ++i)
-                for (int j = i; j > 0 && k[j - 1] > k[j]; --j) std::swap(k[j - 1], k[j]);
-            return k;
-        };
-        std::vector<std::array<int32_t, 4>> all;
-        all.reserve((size_t)c.n_el * nf);
-        for (int e = 0; e < c.n_el; ++e)
-            for (int fi = 0; fi < nf; ++fi) all.push_back(key(e, fi));
-        std::sort(all.begin(), all.end());
-        const double cos_tol = std::cos(kPi / 180.0 * norm_tol_deg);
-        double el_ld[24], keep[24];
-        for (int e : c.elem_sets[elem_set]) {
-            bool any = false;
-            for (int fi = 0; fi < nf; ++fi) {
-                const auto k = key(e, fi);
-                auto rg = std::equal_range(all.begin(), all.end(), k);
-                if (rg.second - rg.first != 1) continue;
-                const int* ln = face_nodes(fi);
-                double v1[3], v2[3], nr[3];
-                for (int i = 0; i < 3; ++i) {
-                    const double* x0 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[0]]];
-                    const double* x1 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[1]]];
-                    const double* x2 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[2]]];
-                    if (fnn == 4) {
-                        const double* x3 = &c.xyz[3 * (size_t)c.conn[(size_t)e * c.nn + ln[3]]];
-                        v1[i] = x2[i] - x0[i];
-                        v2[i] = x3[i] - x1[i];
-                    } else {
-                        v1[i] = x1[i] - x0[i];
-                        v2[i] = x2[i] - x0[i];
-                    }
+        require(traction != nullptr, "null traction");
+        surface_load(c, rhs, elem_set, norm_dir, norm_tol_deg, traction, 0.0);
+        return ASEND_OK;
+    });
+}
+
+int asend_add_surface_pressure(asend_ctx* ctx, int32_t rhs, int32_t elem_set, const double* norm_dir,
+                               double norm_tol_deg, double pressure) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(std::isfinite(pressure), "pressure must be finite");
+        surface_load(c, rhs, elem_set, norm_dir, norm_tol_deg, nullptr, pressure);
+        return ASEND_OK;
+    });
+}
+
+// Integrals of the element's node shape functions, w_a = int N_a dV (shells:
+// t int N_a dA), so that the inertial load of a uniform acceleration acc,
+// M_e acc = rho_e w_a acc on the translational DOF (get_rum_dfd0 with a
+// constant acceleration field, element_equations.rs:420-626), is formed
+// without the mass matrix.  Returns the number of physical nodes; dof[a] is
+// node a's first translational DOF; cent the mean of the node coordinates.
+static int element_node_weights(const Ctx& c, int e, double* w, int64_t* dof, double* cent) {
+    if (c.type == 41) {
+        double x[4][3];
+        for (int a = 0; a < 4; ++a) {
+            const int pn = c.conn[(size_t)e * 8 + 2 * a];  // translational pseudo-node 2 n
+            for (int j = 0; j < 3; ++j) x[a][j] = c.xyz[3 * (size_t)pn + j];
+            dof[a] = (int64_t)(pn / 2) * 6;
+        }
+        const double g = 0.5773502691896257, sg[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+        for (int a = 0; a < 4; ++a) w[a] = 0.0;
+        for (int p = 0; p < 4; ++p) {
+            const double s = sg[p][0] * g, t = sg[p][1] * g;
+            double J[2][2] = {{0, 0}, {0, 0}}, N[4];
+            for (int a = 0; a < 4; ++a) {
+                N[a] = 0.25 * (1 + sg[a][0] * s) * (1 + sg[a][1] * t);
+                const double ds = 0.25 * sg[a][0] * (1 + sg[a][1] * t), dt = 0.25 * sg[a][1] * (1 + sg[a][0] * s);
+                for (int j = 0; j < 2; ++j) {
+                    J[j][0] += x[a][j] * ds;
+                    J[j][1] += x[a][j] * dt;
                 }
-                nr[0] = v1[1] * v2[2] - v1[2] * v2[1];
-                nr[1] = v1[2] * v2[0] - v1[0] * v2[2];
-                nr[2] = v1[0] * v2[1] - v1[1] * v2[0];
-                const double l = std::sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
-                const double dp = (norm_dir[0] * nr[0] + norm_dir[1] * nr[1] + norm_dir[2] * nr[2]) / l;
-                if (!(dp > cos_tol)) continue;
-                face_load(c, e, ln, fnn, traction, el_ld);
-                std::copy(el_ld, el_ld + 3 * c.nn, keep);  // last loaded face survives
-                any = true;
             }
-            if (any)
-                for (int i = 0; i < 3 * c.nn; ++i)
-                    c.loads[rhs][(size_t)c.conn[(size_t)e * c.nn + i / 3] * 3 + i % 3] += keep[i];
+            const double det = std::fabs(J[0][0] * J[1][1] - J[0][1] * J[1][0]);
+            for (int a = 0; a < 4; ++a) w[a] += N[a] * det * c.thk[e];
+        }
+        for (int j = 0; j < 3; ++j) cent[j] = 0.25 * (x[0][j] + x[1][j] + x[2][j] + x[3][j]);
+        return 4;
+    }
+    const int nn = c.nn;
+    double x[8][3];
+    for (int a = 0; a < nn; ++a) {
+        const int nd = c.conn[(size_t)e * nn + a];
+        for (int j = 0; j < 3; ++j) x[a][j] = c.xyz[3 * (size_t)nd + j];
+        dof[a] = (int64_t)nd * 3;
+    }
+    for (int j = 0; j < 3; ++j) {
+        cent[j] = 0.0;
+        for (int a = 0; a < nn; ++a) cent[j] += x[a][j];
+        cent[j] /= nn;
+    }
+    if (nn == 4) {  // linear tet: int N_a = V / 4
+        double v1[3], v2[3], v3[3];
+        for (int j = 0; j < 3; ++j) {
+            v1[j] = x[1][j] - x[0][j];
+            v2[j] = x[2][j] - x[0][j];
+            v3[j] = x[3][j] - x[0][j];
+        }
+        const double det = v1[0] * (v2[1] * v3[2] - v2[2] * v3[1]) - v1[1] * (v2[0] * v3[2] - v2[2] * v3[0]) +
+                           v1[2] * (v2[0] * v3[1] - v2[1] * v3[0]);
+        for (int a = 0; a < 4; ++a) w[a] = std::fabs(det) / 24.0;
+        return 4;
+    }
+    const double g = 0.5773502691896257;
+    const double sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                             {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+    for (int a = 0; a < 8; ++a) w[a] = 0.0;
+    for (int p = 0; p < 8; ++p) {
+        const double s[3] = {(p & 1) ? g : -g, (p & 2) ? g : -g, (p & 4) ? g : -g};
+        double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, N[8];
+        for (int a = 0; a < 8; ++a) {
+            const double f0 = 1 + sg[a][0] * s[0], f1 = 1 + sg[a][1] * s[1], f2 = 1 + sg[a][2] * s[2];
+            N[a] = 0.125 * f0 * f1 * f2;
+            const double dn[3] = {0.125 * sg[a][0] * f1 * f2, 0.125 * sg[a][1] * f0 * f2, 0.125 * sg[a][2] * f0 * f1};
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) J[i][j] += x[a][i] * dn[j];
+        }
+        const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                           J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        for (int a = 0; a < 8; ++a) w[a] += N[a] * det;
+    }
+    return 8;
+}
+
+// Element loads of a uniform acceleration field over an element set
+// (get_app_load_dfd0, element_equations.rs:1875-1968): body force (force per
+// unit volume, unit density), gravity (acceleration, the element's density)
+// and centrifugal (omega^2 times the distance of the element centroid from
+// the axis through center, the element's density).
+int asend_add_body_load(asend_ctx* ctx, int32_t rhs, int32_t elem_set, int32_t kind, const double* vec,
+                        double omega, const double* center, const double* axis) {
+    return guarded(ctx, [&](Ctx& c) {
+        ensure_case(c, rhs);
+        require(elem_set >= 0 && elem_set < (int)c.elem_sets.size(), "unknown element set");
+        require(kind >= ASEND_LOAD_BODY_FORCE && kind <= ASEND_LOAD_CENTRIFUGAL, "unknown body load kind");
+        require(kind == ASEND_LOAD_CENTRIFUGAL ? (center && axis && std::isfinite(omega)) : vec != nullptr,
+                "body load without its data");
+        require(kind == ASEND_LOAD_BODY_FORCE || !c.rho.empty(), "gravity and centrifugal loads need densities");
+        double ax[3] = {0, 0, 0};
+        if (kind == ASEND_LOAD_CENTRIFUGAL) {  // the axis is normalised on input (load_meth.rs:41-51)
+            const double l = std::sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2]);
+            require(l > 0.0, "centrifugal axis of zero length");
+            for (int j = 0; j < 3; ++j) ax[j] = axis[j] / l;
+        }
+        double w[8], cent[3];
+        int64_t dof[8];
+        for (int e : c.elem_sets[elem_set]) {
+            const int na = element_node_weights(c, e, w, dof, cent);
+            double acc[3];
+            double rho = (kind == ASEND_LOAD_BODY_FORCE) ? 1.0 : c.rho[e];
+            if (kind == ASEND_LOAD_CENTRIFUGAL) {
+                double d[3], dp = 0.0;
+                for (int j = 0; j < 3; ++j) {
+                    d[j] = cent[j] - center[j];
+                    dp += ax[j] * d[j];
+                }
+                for (int j = 0; j < 3; ++j) acc[j] = omega * omega * (d[j] - ax[j] * dp);
+            } else {
+                for (int j = 0; j < 3; ++j) acc[j] = vec[j];
+            }
+            for (int a = 0; a < na; ++a)
+                for (int j = 0; j < 3; ++j) c.loads[rhs][(size_t)dof[a] + j] += rho * w[a] * acc[j];
         }
         return ASEND_OK;
     });

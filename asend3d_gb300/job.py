@@ -248,9 +248,11 @@ def read_loads(path) -> list:
         if h[0] != "loads":
             continue
         if h[1] == "type" and len(data) == 1:
-            if data[0] not in ("nodalForce", "surfaceTraction"):
+            if data[0] not in ("nodalForce", "surfaceTraction", "surfacePressure", "bodyForce", "gravitational",
+                               "centrifugal"):
                 raise NotImplementedError(f"{data[0]} loads are not on the GPU path")
-            out.append({"type": data[0], "load": [0.0] * 6, "activeTime": [0.0, 1e100], "normTolerance": 1.0})
+            out.append({"type": data[0], "load": [0.0] * 6, "activeTime": [0.0, 1e100], "normTolerance": 1.0,
+                        "center": [0.0] * 3, "axis": [0.0, 0.0, 1.0], "angularVelocity": 0.0})
         elif not out:
             continue
         elif h[1] == "load" and data:
@@ -264,6 +266,10 @@ def read_loads(path) -> list:
             out[-1]["normTolerance"] = float(data[0])
         elif h[1] == "activeTime" and data:
             out[-1]["activeTime"] = [float(data[0]), float(data[1]) if len(data) > 1 else 1e100]
+        elif h[1] in ("center", "axis") and len(data) == 3:  # model_input.rs:1103-1112
+            out[-1][h[1]] = [float(v) for v in data]
+        elif h[1] == "angularVelocity" and data:
+            out[-1]["angularVelocity"] = float(data[0])
     return out
 
 
@@ -430,11 +436,21 @@ class JobRunner:
         for ld in self.loads:
             if not (ld["activeTime"][0] <= time <= ld["activeTime"][1]):
                 continue
-            if ld["type"] == "nodalForce":
+            t = ld["type"]
+            if t == "nodalForce":
                 p.add_nodal_force(ld["nodeSet"], ld["load"])
-            else:
+            elif t == "surfaceTraction":
                 p.add_surface_traction(ld["elementSet"], tuple(ld["normDir"]), tuple(ld["load"][:3]),
                                        norm_tol=ld["normTolerance"])
+            elif t == "surfacePressure":
+                p.add_surface_pressure(ld["elementSet"], tuple(ld["normDir"]), ld["load"][0],
+                                       norm_tol=ld["normTolerance"])
+            elif t == "bodyForce":
+                p.add_body_force(ld["elementSet"], ld["load"][:3])
+            elif t == "gravitational":
+                p.add_gravity(ld["elementSet"], ld["load"][:3])
+            else:
+                p.add_centrifugal(ld["elementSet"], ld["angularVelocity"], ld["center"], ld["axis"])
 
     def _solver(self, time=0.0):
         from .solver import GpuSolver

@@ -42,7 +42,8 @@ class Problem:
     # constraints: (terms=[(node_set, comp(1-based), coef), ...], rhs)
     constraints: list = field(default_factory=list)
     # loads[case] = list of ("nodalForce", set, load6) | ("surfaceTraction", elset, normDir, normTol, t3)
-    #               | ("vector", f)
+    #               | ("surfacePressure", elset, normDir, normTol, p) | ("bodyForce" | "gravitational", elset, v3)
+    #               | ("centrifugal", elset, omega, center3, axis3) | ("vector", f)
     loads: list = field(default_factory=list)
     objective: tuple = ("compliance",)
     # design variables: (elem_set, coefficients)
@@ -78,6 +79,21 @@ class Problem:
     def add_surface_traction(self, elem_set, normal_dir, traction, norm_tol=1.0, case=0):
         self._case(case).append(("surfaceTraction", elem_set, np.asarray(normal_dir, float), float(norm_tol),
                                  np.asarray(traction, float)))
+
+    def add_surface_pressure(self, elem_set, normal_dir, pressure, norm_tol=1.0, case=0):
+        self._case(case).append(("surfacePressure", elem_set, np.asarray(normal_dir, float), float(norm_tol),
+                                 float(pressure)))
+
+    def add_body_force(self, elem_set, f, case=0):
+        """Force per unit volume (the reference's 'bodyForce')."""
+        self._case(case).append(("bodyForce", elem_set, np.asarray(f, float)))
+
+    def add_gravity(self, elem_set, g, case=0):
+        self._case(case).append(("gravitational", elem_set, np.asarray(g, float)))
+
+    def add_centrifugal(self, elem_set, omega, center, axis, case=0):
+        self._case(case).append(("centrifugal", elem_set, float(omega), np.asarray(center, float),
+                                 np.asarray(axis, float)))
 
     def add_load_vector(self, f, case=0):
         self._case(case).append(("vector", np.asarray(f, float)))
@@ -192,6 +208,24 @@ class GpuSolver:
                     self._check(self.lib.asend_add_surface_traction(self.ctx, case, self.elset_ids[it[1]],
                                                                     _ptr(nd, C.c_double), it[3],
                                                                     _ptr(t, C.c_double)), "add_surface_traction")
+                elif it[0] == "surfacePressure":
+                    nd = np.ascontiguousarray(it[2], dtype=np.float64)
+                    self._check(self.lib.asend_add_surface_pressure(self.ctx, case, self.elset_ids[it[1]],
+                                                                    _ptr(nd, C.c_double), it[3], float(it[4])),
+                                "add_surface_pressure")
+                elif it[0] in ("bodyForce", "gravitational", "centrifugal"):
+                    kind = {"bodyForce": _lib.LOAD_BODY_FORCE, "gravitational": _lib.LOAD_GRAVITY,
+                            "centrifugal": _lib.LOAD_CENTRIFUGAL}[it[0]]
+                    if kind == _lib.LOAD_CENTRIFUGAL:
+                        cen = np.ascontiguousarray(it[3], dtype=np.float64)
+                        ax = np.ascontiguousarray(it[4], dtype=np.float64)
+                        rc = self.lib.asend_add_body_load(self.ctx, case, self.elset_ids[it[1]], kind, None,
+                                                          float(it[2]), _ptr(cen, C.c_double), _ptr(ax, C.c_double))
+                    else:
+                        v = np.ascontiguousarray(it[2], dtype=np.float64)
+                        rc = self.lib.asend_add_body_load(self.ctx, case, self.elset_ids[it[1]], kind,
+                                                          _ptr(v, C.c_double), 0.0, None, None)
+                    self._check(rc, "add_body_load")
                 else:
                     f = np.ascontiguousarray(it[1], dtype=np.float64)
                     self._check(self.lib.asend_add_load_vector(self.ctx, case, _ptr(f, C.c_double)),

@@ -178,6 +178,25 @@ int asend_add_nodal_force(asend_ctx* ctx, int32_t rhs, int32_t node_set, const d
 int asend_add_surface_traction(asend_ctx* ctx, int32_t rhs, int32_t elem_set,
                                const double* norm_dir, double norm_tol_deg,
                                const double* traction);
+/* Surface pressure: each loaded face (selected like asend_add_surface_traction)
+ * carries the traction -pressure * n, n its outward unit normal
+ * (get_app_load_dfd0 'surfacePressure', element_equations.rs:1970-1996). */
+int asend_add_surface_pressure(asend_ctx* ctx, int32_t rhs, int32_t elem_set, const double* norm_dir,
+                               double norm_tol_deg, double pressure);
+/* Element loads of a uniform acceleration field (get_app_load_dfd0,
+ * element_equations.rs:1875-1968; the reference's 'bodyForce',
+ * 'gravitational' and 'centrifugal' load types): for each element of the set,
+ * M_e acc on its translational DOF, with
+ *   ASEND_LOAD_BODY_FORCE: acc = vec (force per unit volume, unit density);
+ *   ASEND_LOAD_GRAVITY:    acc = vec, the element's density;
+ *   ASEND_LOAD_CENTRIFUGAL: acc = omega^2 (r - (r . a) a), r = element
+ *     centroid - center, a = axis normalised; the element's density.
+ * vec is unused by centrifugal loads; omega, center, axis only by them. */
+#define ASEND_LOAD_BODY_FORCE 0
+#define ASEND_LOAD_GRAVITY 1
+#define ASEND_LOAD_CENTRIFUGAL 2
+int asend_add_body_load(asend_ctx* ctx, int32_t rhs, int32_t elem_set, int32_t kind, const double* vec,
+                        double omega, const double* center, const double* axis);
 /* Raw load vector in natural DOF numbering (adds to load case `rhs`). */
 int asend_add_load_vector(asend_ctx* ctx, int32_t rhs, const double* f);
 int asend_clear_loads(asend_ctx* ctx);

@@ -1421,9 +1421,23 @@ int orc_element_mass(int32_t elem_type, const double* xyz, double rho, double th
 // at the face nodes, restricted to the face nodes and scaled so its magnitude
 // is area*|t|.  Only the last loaded face of an element survives (the
 // reference recomputes the element load per face before accumulating).
+int orc_surface_load(const orc_model* m, int32_t n_set, const int32_t* elem_set, const double* norm_dir,
+                     double norm_tol_deg, const double* traction_in, double pressure, double* f);
+
 int orc_surface_traction(const orc_model* m, int32_t n_set, const int32_t* elem_set,
                          const double* norm_dir, double norm_tol_deg, const double* traction,
                          double* f) {
+    return orc_surface_load(m, n_set, elem_set, norm_dir, norm_tol_deg, traction, 0.0, f);
+}
+
+// surfacePressure: the traction -p n of each loaded face (element_equations.rs:1984-1990)
+int orc_surface_pressure(const orc_model* m, int32_t n_set, const int32_t* elem_set, const double* norm_dir,
+                         double norm_tol_deg, double pressure, double* f) {
+    return orc_surface_load(m, n_set, elem_set, norm_dir, norm_tol_deg, nullptr, pressure, f);
+}
+
+int orc_surface_load(const orc_model* m, int32_t n_set, const int32_t* elem_set, const double* norm_dir,
+                     double norm_tol_deg, const double* traction_in, double pressure, double* f) {
     if (m->shell || m->ti.nfaces == 0) return -1;  // solid element faces only (none restated for tet10)
     const TypeInfo& t = m->ti;
     const int nn = t.nn, tot = 3 * nn;
@@ -1473,6 +1487,8 @@ int orc_surface_traction(const orc_model* m, int32_t n_set, const int32_t* elem_
             area *= 0.5;
             const double dp = norm_dir[0] * nrm[0] + norm_dir[1] * nrm[1] + norm_dir[2] * nrm[2];
             if (!(dp > cos_tol)) continue;
+            double traction[3];
+            for (int i = 0; i < 3; ++i) traction[i] = traction_in ? traction_in[i] : -pressure * nrm[i];
             // acceleration = traction at face nodes, zero elsewhere
             double acc[24] = {0};
             for (int q = 0; q < t.face_nn; ++q)
@@ -1498,6 +1514,79 @@ int orc_surface_traction(const orc_model* m, int32_t n_set, const int32_t* elem_
         }
         if (any)
             for (int i = 0; i < tot; ++i) f[m->conn[(size_t)e * nn + i / 3] * 3 + i % 3] += el_ld[i];
+    }
+    return 0;
+}
+
+// Uniform-acceleration element loads, get_app_load_dfd0
+// (element_equations.rs:1875-1968): M_e acc with acc on the translational DOF
+// of every node.  kind 0 bodyForce: unit density, then scaled by
+// |load| vol / |sum of the element's forces| (:1893-1911); kind 1
+// gravitational: the element's density; kind 2 centrifugal: omega^2 times the
+// element centroid's offset from the axis (axis normalised on input,
+// load_meth.rs:41-51), the element's density.
+int orc_body_load(const orc_model* m, int32_t n_set, const int32_t* elem_set, int32_t kind, const double* vec,
+                  double omega, const double* center, const double* axis, double* f) {
+    const int nn = m->ti.nn, tot = 3 * nn;
+    std::vector<double> ke(tot * tot), me(tot * tot);
+    double ax[3] = {0, 0, 0};
+    if (kind == 2) {
+        const double l = std::sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2]);
+        for (int j = 0; j < 3; ++j) ax[j] = axis[j] / l;
+    }
+    for (int s = 0; s < n_set; ++s) {
+        const int e = elem_set[s];
+        double xyz[30];
+        elem_xyz(m, e, xyz);
+        // element mass at its density, or at unit density for body forces
+        if (m->shell) {
+            double x4[12];
+            for (int a = 0; a < 4; ++a)
+                for (int j = 0; j < 3; ++j) x4[3 * a + j] = m->phys_xyz[3 * (size_t)m->conn4[(size_t)e * 4 + a] + j];
+            shell_km(x4, m->E[e], m->nu[e], kind == 0 ? 1.0 : m->rho[e], m->thk[e], ke.data(), me.data());
+        } else {
+            solid_me(m->ti.type, xyz, kind == 0 ? 1.0 : m->rho[e], me.data());
+        }
+        // physical nodes: shells carry translations on pseudo-node 2a
+        const int nphys = m->shell ? 4 : nn;
+        double acc_e[3];
+        if (kind == 2) {
+            double cen[3] = {0, 0, 0}, d[3], dp = 0.0;
+            for (int a = 0; a < nphys; ++a)
+                for (int j = 0; j < 3; ++j) cen[j] += xyz[3 * (m->shell ? 2 * a : a) + j] / nphys;
+            for (int j = 0; j < 3; ++j) {
+                d[j] = cen[j] - center[j];
+                dp += ax[j] * d[j];
+            }
+            for (int j = 0; j < 3; ++j) acc_e[j] = omega * omega * (d[j] - ax[j] * dp);
+        } else {
+            for (int j = 0; j < 3; ++j) acc_e[j] = vec[j];
+        }
+        std::vector<double> acc(tot, 0.0), ld(tot, 0.0);
+        for (int a = 0; a < nphys; ++a)
+            for (int j = 0; j < 3; ++j) acc[3 * (m->shell ? 2 * a : a) + j] = acc_e[j];
+        double tot_f[3] = {0, 0, 0};
+        for (int i = 0; i < tot; ++i) {
+            double v = 0.0;
+            for (int j = 0; j < tot; ++j) v += me[i * tot + j] * acc[j];
+            ld[i] = v;
+            if (!m->shell || (i / 3) % 2 == 0) tot_f[i % 3] += v;
+        }
+        if (kind == 0) {
+            // element volume: the unit-density mass summed over one direction
+            double vol = 0.0;
+            for (int i = 0; i < tot; i += 3)
+                if (!m->shell || (i / 3) % 2 == 0)
+                    for (int j = 0; j < tot; j += 3) vol += me[i * tot + j];
+            double imag = 0.0, vmag = 0.0;
+            for (int j = 0; j < 3; ++j) {
+                imag += vec[j] * vec[j];
+                vmag += tot_f[j] * tot_f[j];
+            }
+            const double sc = (vmag > 0.0) ? std::sqrt(imag) * vol / std::sqrt(vmag) : 0.0;
+            for (double& v : ld) v *= sc;
+        }
+        for (int i = 0; i < tot; ++i) f[(size_t)m->conn[(size_t)e * nn + i / 3] * 3 + i % 3] += ld[i];
     }
     return 0;
 }

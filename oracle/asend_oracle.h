@@ -86,6 +86,12 @@ int orc_element_mass(int32_t elem_type, const double* xyz, double rho, double th
 int orc_surface_traction(const orc_model* m, int32_t n_set, const int32_t* elem_set,
                          const double* norm_dir, double norm_tol_deg, const double* traction,
                          double* f);
+/* surfacePressure: traction -pressure * n on each loaded face. */
+int orc_surface_pressure(const orc_model* m, int32_t n_set, const int32_t* elem_set, const double* norm_dir,
+                         double norm_tol_deg, double pressure, double* f);
+/* bodyForce (kind 0), gravitational (1), centrifugal (2) element loads added to f. */
+int orc_body_load(const orc_model* m, int32_t n_set, const int32_t* elem_set, int32_t kind, const double* vec,
+                  double omega, const double* center, const double* axis, double* f);
 
 /* Static linear solve: (K + sf C^T C) u = f + sf C^T q, x0 = 0. */
 int orc_static_solve(orc_model* m, const double* f, double* u, int32_t precond,

@@ -60,6 +60,8 @@ def load():
                                                  C.c_int32, C.c_int32, C.POINTER(Stats)]),
             "orc_apply_operator": (C.c_int, [C.c_void_p, P_d, P_d]),
             "orc_set_cmat": (C.c_int, [C.c_void_p, P_d]),
+            "orc_surface_pressure": (C.c_int, [C.c_void_p, C.c_int32, P_i, P_d, C.c_double, C.c_double, P_d]),
+            "orc_body_load": (C.c_int, [C.c_void_p, C.c_int32, P_i, C.c_int32, P_d, C.c_double, P_d, P_d, P_d]),
             "orc_set_damping": (C.c_int, [C.c_void_p, C.c_double, C.c_double, P_d]),
             "orc_set_lumped_mass": (C.c_int, [C.c_void_p, C.c_int32]),
             "orc_orthotropic_cmat": (C.c_int, [P_d, P_d, P_d, P_d]),
@@ -168,6 +170,23 @@ class Oracle:
                     nd = np.ascontiguousarray(it[2], np.float64)
                     t = np.ascontiguousarray(it[4], np.float64)
                     self.lib.orc_surface_traction(self.m, len(els), _p(els, C.c_int32), _p(nd), it[3], _p(t), _p(f))
+                elif it[0] == "surfacePressure":
+                    els = np.ascontiguousarray(self.p.elem_sets[it[1]], np.int32)
+                    nd = np.ascontiguousarray(it[2], np.float64)
+                    self.lib.orc_surface_pressure(self.m, len(els), _p(els, C.c_int32), _p(nd), it[3], float(it[4]),
+                                                  _p(f))
+                elif it[0] in ("bodyForce", "gravitational", "centrifugal"):
+                    els = np.ascontiguousarray(self.p.elem_sets[it[1]], np.int32)
+                    kind = ("bodyForce", "gravitational", "centrifugal").index(it[0])
+                    if kind == 2:
+                        cen = np.ascontiguousarray(it[3], np.float64)
+                        ax = np.ascontiguousarray(it[4], np.float64)
+                        self.lib.orc_body_load(self.m, len(els), _p(els, C.c_int32), 2, None, float(it[2]), _p(cen),
+                                               _p(ax), _p(f))
+                    else:
+                        v = np.ascontiguousarray(it[2], np.float64)
+                        self.lib.orc_body_load(self.m, len(els), _p(els, C.c_int32), kind, _p(v), 0.0, None, None,
+                                               _p(f))
                 else:
                     f += it[1]
             out.append(f)

@@ -175,8 +175,8 @@ def test_unsupported_inputs(tmp_path):
     (tmp_path / "m.yaml").write_text("elements:\n- type: beam2\n")
     with pytest.raises(NotImplementedError, match="beam2"):
         J.read_model(tmp_path / "m.yaml")
-    (tmp_path / "l.yaml").write_text("loads:\n- type: gravitational\n")
-    with pytest.raises(NotImplementedError, match="gravitational"):
+    (tmp_path / "l.yaml").write_text("loads:\n- type: bodyHeatGen\n")
+    with pytest.raises(NotImplementedError, match="bodyHeatGen"):
         J.read_loads(tmp_path / "l.yaml")
     (tmp_path / "j.yaml").write_text("jobCommands:\n- command: solve\n  thermal: yes\n")
     r = J.JobRunner(tmp_path / "j.yaml")
