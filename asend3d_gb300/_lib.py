@@ -75,6 +75,9 @@ SIGNATURES = [
     ("asend_add_constraint", c_int, [C.c_void_p, c_int, P_int, P_int, P_dbl, c_dbl]),
     ("asend_add_nodal_force", c_int, [C.c_void_p, c_int, c_int, P_dbl]),
     ("asend_add_surface_traction", c_int, [C.c_void_p, c_int, c_int, P_dbl, c_dbl, P_dbl]),
+    ("asend_newmark_keep_history", c_int, [C.c_void_p, c_int]),
+    ("asend_newmark_step_state", c_int, [C.c_void_p, c_int, P_dbl, P_dbl, P_dbl]),
+    ("asend_newmark_adjoint", c_int, [C.c_void_p, C.c_void_p, c_int, P_int, P_dbl, P_dbl, P_dbl, C.c_void_p]),
     ("asend_add_surface_pressure", c_int, [C.c_void_p, c_int, c_int, P_dbl, c_dbl, c_dbl]),
     ("asend_add_body_load", c_int, [C.c_void_p, c_int, c_int, c_int, P_dbl, c_dbl, P_dbl, P_dbl]),
     ("asend_add_load_vector", c_int, [C.c_void_p, c_int, P_dbl]),

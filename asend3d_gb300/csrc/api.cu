@@ -1335,6 +1335,46 @@ int asend_newmark_run(asend_ctx* ctx, const asend_solve_opts* opts, int32_t n_st
     });
 }
 
+int asend_newmark_keep_history(asend_ctx* ctx, int32_t fields) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(fields == 0 || fields == 1 || fields == 3, "fields must be 0, 1 or 3");
+        c.hist_fields = fields;
+        if (!fields) {
+            c.d_hist.release();
+            c.hist_steps = 0;
+        }
+        return ASEND_OK;
+    });
+}
+
+int asend_newmark_step_state(asend_ctx* ctx, int32_t step, double* u_out, double* v_out, double* a_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.hist_fields > 0 && c.hist_steps > 0, "no stored Newmark history (asend_newmark_keep_history)");
+        require(step >= 1 && step <= c.hist_steps, "step out of range 1..n_steps");
+        require(c.hist_fields == 3 || (!v_out && !a_out), "velocities and accelerations need fields = 3");
+        const size_t n = c.n_dof;
+        const double* h = c.d_hist.p + (size_t)(step - 1) * c.hist_fields * n;
+        if (u_out) ASEND_CUDA(cudaMemcpy(u_out, h, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        if (v_out) ASEND_CUDA(cudaMemcpy(v_out, h + n, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        if (a_out) ASEND_CUDA(cudaMemcpy(a_out, h + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        return ASEND_OK;
+    });
+}
+
+int asend_newmark_adjoint(asend_ctx* ctx, const asend_solve_opts* opts, int32_t n_obj, const int32_t* obj_dof,
+                          const double* obj_w, double* L_out, double* dLdE_out, asend_solve_stats* stats) {
+    return guarded(ctx, [&](Ctx& c) {
+        NvtxRange nvtx_range("asend_newmark_adjoint");
+        require(opts && n_obj >= 1 && obj_dof && obj_w, "bad objective");
+        require(c.assembled && c.dynamic && !c.modal, "assemble with dynamic=1 first");
+        require(c.hist_fields > 0 && c.hist_steps > 0, "run asend_newmark_run with a kept history first");
+        require(!c.A.d64.n && !c.lump && c.ortho.empty() && c.n_inst <= 1,
+                "the transient adjoint takes undamped, consistent-mass, isotropic single models");
+        for (int k = 0; k < n_obj; ++k) require(obj_dof[k] >= 0 && obj_dof[k] < c.n_dof, "objective DOF out of range");
+        return newmark_adjoint(c, *opts, n_obj, obj_dof, obj_w, L_out, dLdE_out, stats);
+    });
+}
+
 int asend_eigen_solve(asend_ctx* ctx, const asend_eigen_opts* opts, double* eig_out, double* freq_out,
                       double* modes_out, double* diag_mass_out, asend_eigen_stats* stats) {
     return guarded(ctx, [&](Ctx& c) {

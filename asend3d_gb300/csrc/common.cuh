@@ -193,6 +193,13 @@ struct Ctx {
     int64_t adj_serial = 0, pairs_serial = -1;
     std::vector<double> h_pairs;   // strain-pair tensors of the last adjoint [n_el][36]
 
+    // Newmark solution history (kept when hist_fields > 0): per step the
+    // displacement (fields = 1) or displacement, velocity and acceleration
+    // (fields = 3), [steps][fields][n_dof]
+    int hist_fields = 0, hist_steps = 0;
+    double hist_dt = 0.0;
+    DArr<double> d_hist;
+
     // timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -267,6 +274,8 @@ int sym_eigen_dense(int m, const double* a, double* vals, double* vecs);
 int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* amp, int probe,
                 double* probe_hist, double* u_final, asend_solve_stats* st);
 void upload_rhs(Ctx& c);
+int newmark_adjoint(Ctx& c, const asend_solve_opts& o, int n_obj, const int32_t* obj_dof, const double* obj_w,
+                    double* L_out, double* gE_out, asend_solve_stats* st);
 void ensure_pinned_scalars(Ctx& c, size_t bytes);
 int instance_of_node(const Ctx& c, int node);
 bool orthotropic_cmat(const double* props9, double* C36);

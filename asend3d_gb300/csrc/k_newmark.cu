@@ -21,6 +21,7 @@
 // extrapolation of the two previous increments.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "common.cuh"
@@ -101,6 +102,53 @@ __global__ void k_extrapolate(int n, double* __restrict__ du, double* __restrict
     du_prev[i] = d;
 }
 
+// y = A x for an FP64 SBELL value array (the mass in the adjoint sweep)
+__global__ void __launch_bounds__(128) k_sbell_apply64(int n_rows, const int64_t* __restrict__ slice_off,
+                                                       const uint8_t* __restrict__ row_len,
+                                                       const int32_t* __restrict__ col, const double* __restrict__ vals,
+                                                       const double* __restrict__ x, double* __restrict__ y) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n_rows) return;
+    const int lane = row & 31;
+    const int64_t g0 = slice_off[row >> 5];
+    const int len = row_len[row];
+    double acc[3] = {0, 0, 0};
+    for (int j = 0; j < len; ++j) {
+        const int64_t g = g0 + j;
+        const int cn = col[g * 32 + lane];
+        const double x0 = x[3 * (size_t)cn], x1 = x[3 * (size_t)cn + 1], x2 = x[3 * (size_t)cn + 2];
+        const double* v = vals + (g * 9) * 32 + lane;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) acc[r] += v[(3 * r) * 32] * x0 + v[(3 * r + 1) * 32] * x1 + v[(3 * r + 2) * 32] * x2;
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) y[3 * (size_t)row + r] = acc[r];
+}
+
+// One step of the reverse Newmark sweep (the adjoint of update_vel_acc and
+// of the coupling to the next step, augmentd_ld_u model_analysis.rs:936-1063
+// and solve_for_adjoint :1065-1126): from the next step's adjoints (mu =
+// M u_adj) form dL/du, dL/dv, dL/da, then v_adj = dL/dv, a_adj = dL/da +
+// dt gamma v_adj and the right-hand side dL/du - d_ad_up a_adj of this step's
+// operator solve.  w: the step's objective weights (dense).
+__global__ void k_adjoint_step(int n, int first, double d_ad_up, double d_ad_vp, double d_ad_ap, double c3, double c4,
+                               double dt_gamma, const double* __restrict__ mu, const double* __restrict__ w,
+                               double* __restrict__ v_adj, double* __restrict__ a_adj, double* __restrict__ rhs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double du = w[i], dv = 0.0, da = 0.0;
+    if (!first) {
+        const double m = mu[i], aa = a_adj[i], vv = v_adj[i];
+        du += -d_ad_up * m + d_ad_up * aa;
+        da = -d_ad_ap * m + d_ad_ap * aa + c3 * vv;
+        dv = -d_ad_vp * m + c4 * aa + vv;
+    }
+    const double vn = dv, an = da + dt_gamma * vn;
+    v_adj[i] = vn;
+    a_adj[i] = an;
+    rhs[i] = du - d_ad_up * an;
+}
+
 __global__ void k_probe(const double* __restrict__ u, int dof, double* __restrict__ hist, int step) {
     if (threadIdx.x == 0 && blockIdx.x == 0) hist[step] = u[dof];
 }
@@ -129,6 +177,12 @@ int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* am
         z->zero(c.stream);
     }
     hist.alloc(std::max(1, n_steps));
+    c.hist_steps = 0;
+    if (c.hist_fields > 0) {
+        c.d_hist.alloc((size_t)n_steps * c.hist_fields * n);
+        c.hist_steps = n_steps;
+        c.hist_dt = dt;
+    }
     hist.zero(c.stream);
     // prep predictor (model_prep.rs:584-590): all zero initial state -> zeros
     const int rows = c.A.n_rows;
@@ -163,6 +217,15 @@ int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* am
         if (rc == ASEND_MAX_ITER) status = rc;
         k_newmark_update<<<g_dof, 256, 0, c.stream>>>(n, dt, gamma, c1, c2, du.p, u.p, v.p, a.p, up.p, vp.p, ap.p);
         ++c.launches;
+        if (c.hist_fields > 0) {  // the corrected state of step s + 1 (the solnTStep fields)
+            double* h = c.d_hist.p + (size_t)s * c.hist_fields * n;
+            ASEND_CUDA(cudaMemcpyAsync(h, up.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+            if (c.hist_fields == 3) {
+                ASEND_CUDA(cudaMemcpyAsync(h + n, vp.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+                ASEND_CUDA(cudaMemcpyAsync(h + 2 * (size_t)n, ap.p, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                           c.stream));
+            }
+        }
         if (probe >= 0) {
             k_probe<<<1, 32, 0, c.stream>>>(u.p, probe, hist.p, s);
             ++c.launches;
@@ -183,6 +246,85 @@ int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* am
         st->rel_residual = relmax;
         st->ms_solve = ms;
         st->n_rhs = 1;
+        st->penalty_scale = c.sf;
+    }
+    return status;
+}
+
+// Reverse Newmark sweep for L = sum_{steps s} sum_k w_k u_s[dof_k] and its
+// per-element modulus gradient (Model::get_obj_gradient's transient branch,
+// model_analysis.rs:1544-1631, with augmentd_ld_u :936-1063): per step from
+// the last, the fused adjoint update, one solve with the step operator
+// (warm-started from the later step's adjoint) and the contraction
+// dL/dE_e -= u_adj_e^T (K_e / E_e) u_s,e with the stored displacement.  Needs
+// the displacement history of the preceding asend_newmark_run.  Undamped,
+// consistent-mass, isotropic models (the oracle's restatement covers these).
+int newmark_adjoint(Ctx& c, const asend_solve_opts& o, int n_obj, const int32_t* obj_dof, const double* obj_w,
+                    double* L_out, double* gE_out, asend_solve_stats* st) {
+    const int n = c.n_dof, N = c.hist_steps, F = c.hist_fields;
+    const double dt = c.hist_dt, beta = c.beta, gamma = c.gamma;
+    const double d_ad_up = 1.0 / (dt * dt * (beta - gamma));
+    const double d_ad_vp = d_ad_up * dt;
+    const double d_ad_ap = d_ad_up * dt * dt * (0.5 + beta - gamma);
+    const double c3 = dt * (1.0 - gamma), c4 = 1.0 / (dt * (beta - gamma));
+    std::vector<double> w(n, 0.0);
+    double L = 0.0;
+    {
+        std::vector<double> us(n);
+        for (int k = 0; k < n_obj; ++k) w[obj_dof[k]] += obj_w[k];
+        // L from the stored displacements at the objective DOFs
+        for (int s = 0; s < N; ++s)
+            for (int k = 0; k < n_obj; ++k) {
+                double v = 0.0;
+                ASEND_CUDA(cudaMemcpyAsync(&v, c.d_hist.p + (size_t)s * F * n + obj_dof[k], sizeof(double),
+                                           cudaMemcpyDeviceToHost, c.stream));
+                ASEND_CUDA(cudaStreamSynchronize(c.stream));
+                L += obj_w[k] * v;
+            }
+    }
+    DArr<double> d_w, mu, v_adj, a_adj, rhs, u_adj, gE;
+    d_w.upload(w, c.stream);
+    for (DArr<double>* z : {&mu, &v_adj, &a_adj, &rhs, &u_adj}) {
+        z->alloc(n);
+        z->zero(c.stream);
+    }
+    gE.alloc(c.n_el);
+    gE.zero(c.stream);
+    const int rows = c.A.n_rows, g_rows = (rows + 127) / 128, g_dof = (n + 255) / 256;
+    int iters = 0, status = 0;
+    double relmax = 0.0;
+    ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
+    for (int s = N - 1; s >= 0; --s) {
+        const bool first = (s == N - 1);
+        if (!first) {
+            k_sbell_apply64<<<g_rows, 128, 0, c.stream>>>(rows, c.A.slice_off.p, c.A.row_len.p, c.A.col.p, c.A.m64.p,
+                                                          u_adj.p, mu.p);
+            ++c.launches;
+        }
+        k_adjoint_step<<<g_dof, 256, 0, c.stream>>>(n, first ? 1 : 0, d_ad_up, d_ad_vp, d_ad_ap, c3, c4, dt * gamma,
+                                                    mu.p, d_w.p, v_adj.p, a_adj.p, rhs.p);
+        ++c.launches;
+        asend_solve_stats ps{};
+        const int rc = pcg_solve(c, o, &ps, !first, rhs.p, u_adj.p, 1);
+        iters += ps.iterations;
+        relmax = std::max(relmax, ps.rel_residual);
+        if (rc == ASEND_NONFINITE) { status = rc; break; }
+        if (rc == ASEND_MAX_ITER) status = rc;
+        adjoint_contract(c, u_adj.p, c.d_hist.p + (size_t)s * F * n, gE.p, true);
+    }
+    ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
+    ASEND_CUDA(cudaEventSynchronize(c.ev1));
+    float ms = 0.f;
+    ASEND_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    if (gE_out) ASEND_CUDA(cudaMemcpy(gE_out, gE.p, sizeof(double) * c.n_el, cudaMemcpyDeviceToHost));
+    if (L_out) *L_out = L;
+    if (st) {
+        std::memset(st, 0, sizeof(*st));
+        st->iterations = iters;
+        st->status = status;
+        st->rel_residual = relmax;
+        st->ms_solve = ms;
+        st->n_rhs = N;
         st->penalty_scale = c.sf;
     }
     return status;

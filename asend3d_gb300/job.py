@@ -349,6 +349,7 @@ class JobRunner:
         self.g = None
         self.solve_cmd: dict = {}
         self.state = None          # {"u", "v", "a"} per node [n, dpn]
+        self.hist = None           # saved solution history {"dir", "steps", "dt"}
         self.modal = None
         self.obj_values = None
         self.obj_gradient = None
@@ -576,11 +577,27 @@ class JobRunner:
             g.assemble(precision=64, dynamic=True, dt=dt, beta=beta, gamma=gamma)
             kw = self._opts(cmd)
             kw["precond"] = _lib.PC_JACOBI if kw["precond"] == _lib.PC_MG else kw["precond"]
+            save = bool(cmd.get("saveSolnHist"))
+            if save and self.model.elem_type not in (8, 4):
+                raise NotImplementedError("solution histories of elements with internal DOF are not written by the "
+                                          "GPU path")
+            g.keep_history(3)  # the last state's velocity and acceleration, and the solnTStep files
             hist, u, rc, st = g.newmark(np.ones(n_steps), **kw)
             if rc not in (_lib.ASEND_OK, _lib.ASEND_MAX_ITER):
                 raise RuntimeError(f"Newmark run failed: {st}")
             _cg_log(st["iterations"], st["rel_residual"])
-            self.state = {"u": u.reshape(n, dpn), "v": None, "a": None, "time": n_steps * dt}
+            _, v, a = g.step_state(n_steps, fields=3)
+            self.state = {"u": u.reshape(n, dpn), "v": v.reshape(n, dpn), "a": a.reshape(n, dpn),
+                          "time": n_steps * dt}
+            if save:  # solnTStep0 (the initial state) .. solnTStep<n_steps> (model_analysis.rs:591-622)
+                from .results_io import write_time_step_soln
+                d = self._out(cmd.get("solnHistDir", cmd.get("fileName", ".")))
+                z = np.zeros((n, dpn))
+                write_time_step_soln(d, 0, z, z, z)
+                for s in range(1, n_steps + 1):
+                    us, vs, as_ = g.step_state(s, fields=3)
+                    write_time_step_soln(d, s, us.reshape(n, dpn), vs.reshape(n, dpn), as_.reshape(n, dpn))
+                self.hist = {"dir": d, "steps": n_steps, "dt": dt}
 
     def cmd_modalAnalysis(self, c):
         from . import _lib
@@ -651,7 +668,7 @@ class JobRunner:
     def cmd_writeNodeResults(self, c):
         from .results_io import write_node_results
         if c.get("timeSteps") or c.get("timeStepTag"):
-            raise NotImplementedError("time-step histories are not written by the GPU path")
+            return self._write_node_history(c)
         if self.state is None:
             raise RuntimeError("writeNodeResults before a solve")
         fields = {}
@@ -667,6 +684,32 @@ class JobRunner:
         labels = self.model.node_sets.get(c.get("nodeSet", "all"), self.model.node_labels)
         write_node_results(self._out(c["fileName"]), labels, fields, time=-1.0,
                            rows=[self.node_index[v] for v in labels])
+
+    def _write_node_history(self, c):
+        """writeNodeResults for saved time steps (model_meth.rs:91-110,
+        model_output.rs:84-130): per step the solnTStep file is read back and
+        written to <name>_timestep<N><ext>, time = N dt."""
+        from .results_io import read_time_step_soln, write_node_results
+        h = self.hist
+        if h is None:
+            raise RuntimeError("writeNodeResults for time steps needs a dynamic solve with saveSolnHist")
+        tag = c.get("timeStepTag")
+        steps = list(range(h["steps"] + 1)) if tag == "all" else [h["steps"]] if tag == "last" else c["timeSteps"]
+        n, dpn = len(self.model.node_labels), self.problem.mesh.dpn
+        labels = self.model.node_sets.get(c.get("nodeSet", "all"), self.model.node_labels)
+        name = c["fileName"]
+        i = name.find(".")
+        root, ext = (name[:i], name[i:]) if i >= 0 else (name, "")
+        for ts in steps:
+            u, v, a, _ = read_time_step_soln(h["dir"], ts, n, dpn)
+            fields = {}
+            for f in c.get("fields", ["displacement"]):
+                if f in ("displacement", "velocity", "acceleration"):
+                    fields[f] = {"displacement": u, "velocity": v, "acceleration": a}[f]
+                else:
+                    raise NotImplementedError(f"node field {f} of a time step is not written by the GPU path")
+            write_node_results(self._out(f"{root}_timestep{ts}{ext}"), labels, fields, time=h["dt"] * ts,
+                               rows=[self.node_index[v_] for v_ in labels])
 
     def _reaction(self):
         """R(u) = K u (element internal forces, model_output.rs:207-216 with

@@ -337,6 +337,35 @@ class GpuSolver:
                          "newmark_run")
         return hist, u, rc, st.as_dict()
 
+    def keep_history(self, fields=1):
+        """Keep the next Newmark run's per-step states on the device (1: u; 3: u, v, a)."""
+        self._check(self.lib.asend_newmark_keep_history(self.ctx, fields), "newmark_keep_history")
+
+    def step_state(self, step, fields=1):
+        """(u, v, a) after step `step` (1-based) of the last run (v, a: None unless fields == 3)."""
+        n = self.n_dof
+        u = np.zeros(n)
+        v = np.zeros(n) if fields == 3 else None
+        a = np.zeros(n) if fields == 3 else None
+        self._check(self.lib.asend_newmark_step_state(self.ctx, step, _ptr(u, C.c_double),
+                                                      None if v is None else _ptr(v, C.c_double),
+                                                      None if a is None else _ptr(a, C.c_double)), "step_state")
+        return u, v, a
+
+    def newmark_adjoint(self, obj_dof, obj_w, **kw):
+        """(L, dL/dE, status, stats) of L = sum over the last run's steps of
+        sum_k w_k u[dof_k]."""
+        o = self.opts(**kw)
+        dofs = np.ascontiguousarray(obj_dof, dtype=np.int32)
+        w = np.ascontiguousarray(obj_w, dtype=np.float64)
+        L = C.c_double(0.0)
+        g = np.zeros(self.p.mesh.n_elems)
+        st = SolveStats()
+        rc = self._check(self.lib.asend_newmark_adjoint(self.ctx, C.byref(o), len(dofs), _ptr(dofs, C.c_int32),
+                                                        _ptr(w, C.c_double), C.byref(L), _ptr(g, C.c_double),
+                                                        C.byref(st)), "newmark_adjoint")
+        return L.value, g, rc, st.as_dict()
+
     def eigen(self, n_modes, shift=0.0, block_size=2, tol=1e-8, max_subspace=0, modes=True, **inner):
         """Frequency job: the n_modes eigenpairs of (K + penalty) x = lambda D x
         nearest to ``shift`` (lowest first), D the row-sum diagonal mass.

@@ -316,6 +316,24 @@ int asend_newmark_run(asend_ctx* ctx, const asend_solve_opts* opts, int32_t n_st
                       const double* amp, int32_t probe_dof, double* probe_hist,
                       double* u_final, asend_solve_stats* stats);
 
+/* Solution history of the next asend_newmark_run, kept on the device:
+ * fields 1 = displacements, 3 = displacements, velocities and accelerations
+ * after every step (the solnTStep fields, write_time_step_soln
+ * model_output.rs:14-82), 0 = none.  n_steps x fields x n_dof doubles. */
+int asend_newmark_keep_history(asend_ctx* ctx, int32_t fields);
+/* State after step `step` (1-based) of the last run; pointers may be NULL
+ * (v_out, a_out need fields = 3). */
+int asend_newmark_step_state(asend_ctx* ctx, int32_t step, double* u_out, double* v_out, double* a_out);
+/* Transient adjoint (Model::get_obj_gradient's time-stepping branch,
+ * model_analysis.rs:1544-1631, augmentd_ld_u :936-1063, solve_for_adjoint
+ * :1065-1126): L = sum over the run's steps of sum_k obj_w[k] u[obj_dof[k]],
+ * and dL/dE per element by the reverse Newmark sweep over the kept
+ * displacement history (one operator solve per step).  Undamped,
+ * consistent-mass, isotropic models; needs asend_newmark_keep_history(>= 1)
+ * before the run. */
+int asend_newmark_adjoint(asend_ctx* ctx, const asend_solve_opts* opts, int32_t n_obj, const int32_t* obj_dof,
+                          const double* obj_w, double* L_out, double* dLdE_out, asend_solve_stats* stats);
+
 /* ---- kernel-level entry points (measurement / tests) ----------------------
  * y = A x with the assembled operator at the given value precision (32 =
  * FP32 values, 64 = FP64, 48 = the split FP32 hi + lo product of
