@@ -21,7 +21,7 @@ ASEND_OK, ASEND_MAX_ITER, ASEND_NONFINITE, ASEND_FALLBACK = 0, 1, 2, 3
 ASEND_EINVAL, ASEND_ECUDA, ASEND_ESTATE = -1, -2, -3
 METHOD_FP64, METHOD_MIXED, METHOD_SPLIT = 0, 1, 2
 PC_JACOBI, PC_BLOCK, PC_LEARNED, PC_MG, PC_MG_LEARNED = 0, 1, 2, 3, 4
-OBJ_DISPLACEMENT, OBJ_COMPLIANCE = 0, 1
+OBJ_DISPLACEMENT, OBJ_COMPLIANCE, OBJ_ELEMENT = 0, 1, 2
 LOAD_BODY_FORCE, LOAD_GRAVITY, LOAD_CENTRIFUGAL = 0, 1, 2
 LEARN_BLOCK, LEARN_MG = 0, 1
 DV_MODULUS, DV_SHEAR_MODULUS, DV_POISSON_RATIO = 0, 1, 2
@@ -93,6 +93,8 @@ SIGNATURES = [
     ("asend_get_solution", c_int, [C.c_void_p, c_int, P_dbl]),
     ("asend_set_objective", c_int, [C.c_void_p, c_int, c_int, c_int, c_dbl]),
     ("asend_adjoint_gradient", c_int, [C.c_void_p, C.POINTER(SolveOpts), P_dbl, P_dbl, C.POINTER(SolveStats)]),
+    ("asend_element_fields", c_int, [C.c_void_p, c_int, P_dbl, P_dbl, P_dbl]),
+    ("asend_set_element_objective", c_int, [C.c_void_p, P_dbl, P_dbl]),
     ("asend_add_modulus_design_var", c_int, [C.c_void_p, c_int, c_int, P_dbl]),
     ("asend_design_var_gradient", c_int, [C.c_void_p, P_dbl, P_dbl]),
     ("asend_newmark_run", c_int, [C.c_void_p, C.POINTER(SolveOpts), c_int, P_dbl, c_int, P_dbl, P_dbl,

@@ -1224,7 +1224,8 @@ int asend_get_solution(asend_ctx* ctx, int32_t rhs, double* u_out) {
 
 int asend_set_objective(asend_ctx* ctx, int32_t kind, int32_t node_set, int32_t comp, double coef) {
     return guarded(ctx, [&](Ctx& c) {
-        require(kind == ASEND_OBJ_DISPLACEMENT || kind == ASEND_OBJ_COMPLIANCE, "unknown objective kind");
+        require(kind == ASEND_OBJ_DISPLACEMENT || kind == ASEND_OBJ_COMPLIANCE, "unknown objective kind "
+                "(element-category terms are set by asend_set_element_objective)");
         if (kind == ASEND_OBJ_DISPLACEMENT) {
             require(node_set >= 0 && node_set < (int)c.node_sets.size(), "unknown node set");
             require(comp >= 1 && comp <= c.udpn, "objective component out of range");
@@ -1233,6 +1234,44 @@ int asend_set_objective(asend_ctx* ctx, int32_t kind, int32_t node_set, int32_t 
         c.obj_set = node_set;
         c.obj_comp = comp;
         c.obj_coef = coef;
+        return ASEND_OK;
+    });
+}
+
+int asend_set_element_objective(asend_ctx* ctx, const double* w_stress, const double* w_strain) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.n_el > 0, "set the mesh first");
+        require(c.type == 8 || c.type == 81 || c.type == 4,
+                "element-category objectives are built for hex8, brickIM and tet4 meshes");
+        const size_t m = (size_t)c.n_el * 6;
+        for (const double* w : {w_stress, w_strain})
+            if (w)
+                for (size_t i = 0; i < m; ++i) require(std::isfinite(w[i]), "non-finite objective weight");
+        std::vector<double> zero;
+        if (!w_stress || !w_strain) zero.assign(m, 0.0);
+        c.d_obj_wa.upload(w_stress ? w_stress : zero.data(), m, c.stream);
+        c.d_obj_wb.upload(w_strain ? w_strain : zero.data(), m, c.stream);
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        c.obj_kind = ASEND_OBJ_ELEMENT;
+        c.obj_set = -1;
+        return ASEND_OK;
+    });
+}
+
+int asend_element_fields(asend_ctx* ctx, int32_t rhs, double* eps_out, double* sig_out, double* vol_out) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.solved, "run a static solve first");
+        require(rhs >= 0 && rhs < c.nrhs, "load case out of range");
+        const size_t m = (size_t)c.n_el;
+        DArr<double> eps, sig, vol;
+        if (eps_out) eps.alloc(m * 6);
+        if (sig_out) sig.alloc(m * 6);
+        if (vol_out) vol.alloc(m);
+        element_fields(c, c.d_x.p + (size_t)rhs * c.n_dof, eps.p, sig.p, vol.p);
+        if (eps_out) ASEND_CUDA(cudaMemcpyAsync(eps_out, eps.p, sizeof(double) * m * 6, cudaMemcpyDeviceToHost, c.stream));
+        if (sig_out) ASEND_CUDA(cudaMemcpyAsync(sig_out, sig.p, sizeof(double) * m * 6, cudaMemcpyDeviceToHost, c.stream));
+        if (vol_out) ASEND_CUDA(cudaMemcpyAsync(vol_out, vol.p, sizeof(double) * m, cudaMemcpyDeviceToHost, c.stream));
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
         return ASEND_OK;
     });
 }
@@ -1272,22 +1311,32 @@ int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double*
                 if (iso) adjoint_contract(c, c.d_x.p + r * n, c.d_x.p + r * n, c.d_gE.p, r > 0);
             }
         } else {
-            // L = coef * sum_r sum_{node in set} u_r[node, comp]  ('powerNorm', exponent 1)
-            const auto& set = c.node_sets[c.obj_set];
-            std::vector<double> dldu(n, 0.0);
-            for (int nd : set) dldu[(size_t)nd * c.udpn + c.obj_comp - 1] += c.obj_coef;
             DArr<double> d_dldu;
             DArr<double>& d_usum = c.d_adj_b;
-            d_dldu.upload(dldu, c.stream);
             d_usum.alloc(n);
             d_usum.zero(c.stream);
-            for (int r = 0; r < c.nrhs; ++r) {
-                device_dot(c, n, d_dldu.p, c.d_x.p + r * n, scal.p, part.p);
-                double v = 0.0;
-                ASEND_CUDA(cudaMemcpyAsync(&v, scal.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-                ASEND_CUDA(cudaStreamSynchronize(c.stream));
-                L += v;
-                device_axpy(c, n, 1.0, c.d_x.p + r * n, d_usum.p);
+            if (c.obj_kind == ASEND_OBJ_ELEMENT) {
+                // element-category term: adjoint load sum_e B_c^T (b_e + C_e a_e)
+                // from the caller's weights; L is evaluated by the caller
+                require(c.nrhs == 1, "element-category objectives take a single load case");
+                d_dldu.alloc(n);
+                d_dldu.zero(c.stream);
+                element_objective_rhs(c, d_dldu.p);
+                device_axpy(c, n, 1.0, c.d_x.p, d_usum.p);
+            } else {
+                // L = coef * sum_r sum_{node in set} u_r[node, comp]  ('powerNorm', exponent 1)
+                const auto& set = c.node_sets[c.obj_set];
+                std::vector<double> dldu(n, 0.0);
+                for (int nd : set) dldu[(size_t)nd * c.udpn + c.obj_comp - 1] += c.obj_coef;
+                d_dldu.upload(dldu, c.stream);
+                for (int r = 0; r < c.nrhs; ++r) {
+                    device_dot(c, n, d_dldu.p, c.d_x.p + r * n, scal.p, part.p);
+                    double v = 0.0;
+                    ASEND_CUDA(cudaMemcpyAsync(&v, scal.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+                    ASEND_CUDA(cudaStreamSynchronize(c.stream));
+                    L += v;
+                    device_axpy(c, n, 1.0, c.d_x.p + r * n, d_usum.p);
+                }
             }
             c.d_lam.alloc(n);
             rc = pcg_solve(c, *opts, &ast, false, d_dldu.p, c.d_lam.p, 1);
@@ -1297,6 +1346,7 @@ int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double*
             ASEND_CUDA(cudaEventCreate(&e1));
             ASEND_CUDA(cudaEventRecord(e0, c.stream));
             if (iso) adjoint_contract(c, c.d_lam.p, d_usum.p, c.d_gE.p, false);
+            if (iso && c.obj_kind == ASEND_OBJ_ELEMENT) element_objective_explicit(c, d_usum.p, c.d_gE.p, nullptr);
             ASEND_CUDA(cudaEventRecord(e1, c.stream));
             ASEND_CUDA(cudaEventSynchronize(e1));
             float mc = 0.f;
@@ -1504,6 +1554,7 @@ static void ensure_pairs(Ctx& c) {
         for (int r = 0; r < c.nrhs; ++r) adjoint_pairs(c, c.d_x.p + r * n, c.d_x.p + r * n, P.p, r > 0);
     } else {
         adjoint_pairs(c, c.d_lam.p, c.d_adj_b.p, P.p, false);
+        if (c.adj_kind == ASEND_OBJ_ELEMENT) element_objective_explicit(c, c.d_adj_b.p, nullptr, P.p);
     }
     c.h_pairs.resize((size_t)c.n_el * 36);
     ASEND_CUDA(cudaMemcpyAsync(c.h_pairs.data(), P.p, sizeof(double) * c.h_pairs.size(), cudaMemcpyDeviceToHost,

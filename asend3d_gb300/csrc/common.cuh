@@ -189,6 +189,9 @@ struct Ctx {
     // adjoint
     DArr<double> d_lam, d_gE;
     DArr<double> d_adj_b;          // second field of the last adjoint contraction (displacement objective)
+    // element-category objective: per-element weights dL/dsigma, dL/deps at
+    // the centroid [n_el][6] each (ASEND_OBJ_ELEMENT)
+    DArr<double> d_obj_wa, d_obj_wb;
     int adj_kind = -1;             // objective of the last adjoint gradient (-1: none)
     int64_t adj_serial = 0, pairs_serial = -1;
     std::vector<double> h_pairs;   // strain-pair tensors of the last adjoint [n_el][36]
@@ -293,6 +296,10 @@ int mg_levels(const Ctx& c);
 double mg_time_kernel(Ctx& c, int kernel, int method, int n_launch, double* bytes);
 int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f, double* d_x,
                  int nrhs);
+// element-category objectives (k_objective.cu)
+void element_fields(Ctx& c, const double* d_u, double* d_eps, double* d_sig, double* d_vol);
+void element_objective_rhs(Ctx& c, double* d_rhs);
+void element_objective_explicit(Ctx& c, const double* d_u, double* d_gE, double* d_P);
 // shell4 elements (k_shell.cu)
 void shell_assemble(Ctx& c, double* vals, double* mvals);
 void shell_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate);

@@ -300,6 +300,30 @@ class GpuSolver:
             rc = self.lib.asend_set_objective(self.ctx, _lib.OBJ_DISPLACEMENT, self.set_ids[set_name], comp, coef)
         self._check(rc, "set_objective")
 
+    def element_fields(self, rhs=0):
+        """Centroid strain and stress [n_el, 6] of load case rhs of the last
+        solve and the element volumes [n_el] (solid meshes)."""
+        n = self.p.mesh.n_elems
+        eps, sig, vol = np.zeros((n, 6)), np.zeros((n, 6)), np.zeros(n)
+        self._check(self.lib.asend_element_fields(self.ctx, rhs, _ptr(eps, C.c_double), _ptr(sig, C.c_double),
+                                                  _ptr(vol, C.c_double)), "element_fields")
+        return eps, sig, vol
+
+    def set_element_objective(self, elems, category, component=0, operator="powerNorm", coef=1.0, exponent=1.0,
+                              targets=None) -> float:
+        """Evaluate an element-category term ('stress', 'strain',
+        'strainEnergy' with powerNorm / ks / volumeIntegral / volumeAverage)
+        on the last solution and select it for the next adjoint_gradient.
+        Returns its value."""
+        from .objective import element_term
+        eps, sig, vol = self.element_fields(0)
+        L, wa, wb = element_term(eps, sig, vol, elems, category, component, operator, coef, exponent, targets)
+        wa = np.ascontiguousarray(wa)
+        wb = np.ascontiguousarray(wb)
+        self._check(self.lib.asend_set_element_objective(self.ctx, _ptr(wa, C.c_double), _ptr(wb, C.c_double)),
+                    "set_element_objective")
+        return L
+
     def strain_pairs(self) -> np.ndarray:
         """[n_el, 6, 6] strain-pair tensors of the last adjoint gradient."""
         P = np.zeros((self.p.mesh.n_elems, 6, 6))

@@ -67,6 +67,9 @@ typedef struct asend_ctx asend_ctx;
 /* objective kinds (reference objective categories, objective_meth.rs:592-942) */
 #define ASEND_OBJ_DISPLACEMENT 0 /* 'displacement' + 'powerNorm' on a node set            */
 #define ASEND_OBJ_COMPLIANCE 1   /* f^T u summed over load cases (self-adjoint)           */
+#define ASEND_OBJ_ELEMENT 2      /* element-category term ('stress', 'strain',
+                                    'strainEnergy' at the centroid) given as
+                                    per-element weights (asend_set_element_objective) */
 
 typedef struct asend_solve_opts {
     int32_t method;       /* ASEND_METHOD_*                                          */
@@ -252,6 +255,28 @@ int asend_set_objective(asend_ctx* ctx, int32_t kind, int32_t node_set, int32_t 
                         double coef);
 int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double* L_out,
                            double* dLdE_out, asend_solve_stats* stats);
+
+/* Element-category objective terms (ObjectiveTerm::get_obj_val
+ * objective_meth.rs:665-720, getd_ld_u :1051-1160, getd_ld_d :1372-1500) on
+ * solid meshes (hex8, brickIM, tet4).
+ *   asend_element_fields: centroid strain eps[n_el][6] and stress
+ *     sig[n_el][6] (Voigt 11,22,33,12,13,23, engineering shear; s_cent of
+ *     get_stress_strain_dfd0, element_soln_fields.rs:1463-1576) of load case
+ *     rhs of the last solve, and the element volumes vol[n_el] (sum_ip w detJ,
+ *     get_volume_dfd0 :1118-1155).  Any output may be NULL.
+ *   asend_set_element_objective: selects ASEND_OBJ_ELEMENT with the weights
+ *     w_stress[e] = dL/dsigma_e and w_strain[e] = dL/deps_e ([n_el][6] each,
+ *     NULL = zeros) that the caller derives from its operator (powerNorm, ks,
+ *     volumeIntegral, volumeAverage) on the fields above.  The next
+ *     asend_adjoint_gradient then solves K lambda = sum_e B_c^T (w_strain_e +
+ *     C_e w_stress_e) for a single load case and returns dLdE = explicit
+ *     w_stress . sigma / E - lambda^T dR/dE (isotropic elements); its L_out
+ *     is 0 (the caller evaluates the operator).  The strain pairs of
+ *     asend_adjoint_strain_pairs then include the explicit material term,
+ *     P_e - w_stress_e eps_e^T, so that asend_material_dv_gradient returns
+ *     the total derivative. */
+int asend_element_fields(asend_ctx* ctx, int32_t rhs, double* eps_out, double* sig_out, double* vol_out);
+int asend_set_element_objective(asend_ctx* ctx, const double* w_stress, const double* w_strain);
 /* Design variables over element sets with per-element coefficients
  * (read_des_var_input model_input.rs:1218-1296; element coefficient lists
  * model_prep.rs:414-442): dL/dD_i = sum_e coef_ie dL/dE_e. */

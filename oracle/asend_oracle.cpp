@@ -2049,4 +2049,141 @@ int orc_adjoint_strain_pairs(const orc_model* m, const double* u, const double* 
     return 0;
 }
 
+// Element-category objective terms (categories stress / strain /
+// strainEnergy) evaluated at the element centroid s_cent, with the operators
+// powerNorm, ks, volumeIntegral and volumeAverage:
+//   values      ObjectiveTerm::get_obj_val, objective_meth.rs:665-720, with
+//               get_stress_strain_dfd0 element_soln_fields.rs:1463-1576 and
+//               get_volume_dfd0 :1118-1155 (sum_ip w detJ);
+//   operators   get_power_norm :329-337, get_ks :390-398,
+//               get_vol_integral :442-449, get_vol_average :504-516;
+//   dL/du       getd_ld_u :1051-1160 (dq/du = b^T B + a^T C B with
+//               a = dq/dsigma, b = dq/deps at the centroid);
+//   dL/dD       getd_ld_d :1372-1500: dq/dD = a^T (dC/dD) eps at fixed u.
+// Targets: one value for all elements, one per element, or none (0; 1 for
+// ks), get_tgt_vec :94-215.  The incompatible modes of brickIM have zero
+// derivatives at the centroid (element_soln_fields.rs:212-227), so its
+// centroid strain is the hex8 one.  Outputs: L; dLdu[n_dof] (may be null);
+// Q[n_el][36] with dL/dD|explicit = sum_e sum_ij (dC/dD)_ij Q_e[i][j] (may be
+// null); dLdE[n_el], the explicit isotropic-modulus term (C = E C1) (may be
+// null).  Elements outside the set get zeros.
+int orc_element_objective(const orc_model* m, const double* u, int32_t n_set, const int32_t* elem_set,
+                          int32_t category, int32_t component, int32_t optr, double coef, double expnt,
+                          int32_t n_tgt, const double* tgt, double* L_out, double* dLdu, double* Q,
+                          double* dLdE) {
+    if (!m->assembled || m->shell || n_set <= 0) return -1;
+    if (category < 0 || category > 2 || optr < 0 || optr > 3) return -1;
+    if (category != 2 && (component < 1 || component > 6)) return -1;
+    if (n_tgt != 0 && n_tgt != 1 && n_tgt != n_set) return -1;
+    const TypeInfo& t = m->ti;
+    const int nn = t.nn, tot = 3 * nn;
+    const int stype = (t.type == 81) ? 8 : t.type;
+    const TypeInfo ts = type_info(stype);
+    const double s_cent[3] = {0.0, 0.0, 0.0};  // hex8 / brickIM / tet4 (element_meth.rs:81-83)
+    std::vector<double> q(n_set), vol(n_set), tg(n_set), eps(6 * (size_t)n_set), sig(6 * (size_t)n_set);
+    std::vector<double> Bc((size_t)n_set * 6 * tot), Cs((size_t)n_set * 36);
+    for (int k = 0; k < n_set; ++k) {
+        const int e = elem_set[k];
+        if (e < 0 || e >= m->n_el) return -1;
+        double xyz[30], nv[10], dndx[30], C[36];
+        elem_xyz(m, e, xyz);
+        ip_data(stype, nn, xyz, s_cent, nv, dndx);
+        double* B = &Bc[(size_t)k * 6 * tot];
+        solid_bmat(nn, dndx, B);
+        if (!m->cmat.empty()) std::copy(m->cmat.begin() + (size_t)e * 36, m->cmat.begin() + (size_t)(e + 1) * 36, C);
+        else iso_cmat(m->E[e], m->nu[e], C);
+        std::copy(C, C + 36, &Cs[(size_t)k * 36]);
+        double* ep = &eps[6 * (size_t)k];
+        double* sp = &sig[6 * (size_t)k];
+        for (int i = 0; i < 6; ++i) {
+            double a = 0.0;
+            for (int c = 0; c < tot; ++c) a += B[i * tot + c] * u[m->conn[(size_t)e * nn + c / 3] * 3 + c % 3];
+            ep[i] = a;
+        }
+        for (int i = 0; i < 6; ++i) {
+            double a = 0.0;
+            for (int j = 0; j < 6; ++j) a += C[6 * i + j] * ep[j];
+            sp[i] = a;
+        }
+        if (category == 0) q[k] = sp[component - 1];
+        else if (category == 1) q[k] = ep[component - 1];
+        else {
+            double se = 0.0;
+            for (int i = 0; i < 6; ++i) se += sp[i] * ep[i];
+            q[k] = 0.5 * se;
+        }
+        double v = 0.0;
+        for (int p = 0; p < ts.nip; ++p) v += ip_data(stype, nn, xyz, ts.ip + 3 * p, nv, dndx) * ts.wt[p];
+        vol[k] = v;
+        tg[k] = (n_tgt == 0) ? (optr == 1 ? 1.0 : 0.0) : (n_tgt == 1 ? tgt[0] : tgt[k]);
+    }
+    // operator value and the per-element weights g_k = dL/dq_k
+    std::vector<double> g(n_set);
+    double L = 0.0;
+    if (optr == 0) {
+        double ps = 0.0;
+        for (int k = 0; k < n_set; ++k) ps += std::pow(q[k] - tg[k], expnt);
+        L = coef * std::pow(ps, 1.0 / expnt);
+        const double f = coef * std::pow(ps, 1.0 / expnt - 1.0);
+        for (int k = 0; k < n_set; ++k) g[k] = f * std::pow(q[k] - tg[k], expnt - 1.0);
+    } else if (optr == 1) {
+        double ps = 0.0;
+        for (int k = 0; k < n_set; ++k) ps += std::exp(expnt * q[k] / tg[k]);
+        L = (coef / expnt) * std::log(ps);
+        for (int k = 0; k < n_set; ++k) g[k] = coef * std::exp(expnt * q[k] / tg[k]) / ps / tg[k];
+    } else {
+        double vi = 0.0, tv = 0.0;
+        for (int k = 0; k < n_set; ++k) {
+            vi += q[k] * vol[k];
+            tv += vol[k];
+        }
+        const double base = (optr == 2) ? vi - tg[0] : vi / tv - tg[0];
+        L = coef * std::pow(base, expnt);
+        const double f = coef * expnt * std::pow(base, expnt - 1.0) / (optr == 2 ? 1.0 : tv);
+        for (int k = 0; k < n_set; ++k) g[k] = f * vol[k];
+    }
+    if (L_out) *L_out = L;
+    if (dLdu) std::fill(dLdu, dLdu + m->n_dof, 0.0);
+    if (Q) std::fill(Q, Q + (size_t)m->n_el * 36, 0.0);
+    if (dLdE) std::fill(dLdE, dLdE + m->n_el, 0.0);
+    for (int k = 0; k < n_set; ++k) {
+        const int e = elem_set[k];
+        const double* ep = &eps[6 * (size_t)k];
+        const double* sp = &sig[6 * (size_t)k];
+        double a[6] = {0}, b[6] = {0};
+        if (category == 0) a[component - 1] = 1.0;
+        else if (category == 1) b[component - 1] = 1.0;
+        else
+            for (int i = 0; i < 6; ++i) {
+                a[i] = 0.5 * ep[i];
+                b[i] = 0.5 * sp[i];
+            }
+        if (dLdu) {
+            // w = b + C^T a (strain-space weight), dL/du_e += g B^T w
+            const double* C = &Cs[(size_t)k * 36];
+            const double* B = &Bc[(size_t)k * 6 * tot];
+            double w[6];
+            for (int j = 0; j < 6; ++j) {
+                double s = b[j];
+                for (int i = 0; i < 6; ++i) s += C[6 * i + j] * a[i];
+                w[j] = g[k] * s;
+            }
+            for (int c = 0; c < tot; ++c) {
+                double s = 0.0;
+                for (int i = 0; i < 6; ++i) s += B[i * tot + c] * w[i];
+                dLdu[m->conn[(size_t)e * nn + c / 3] * 3 + c % 3] += s;
+            }
+        }
+        if (Q)
+            for (int i = 0; i < 6; ++i)
+                for (int j = 0; j < 6; ++j) Q[(size_t)e * 36 + 6 * i + j] += g[k] * a[i] * ep[j];
+        if (dLdE) {
+            double s = 0.0;
+            for (int i = 0; i < 6; ++i) s += a[i] * sp[i];
+            dLdE[e] += g[k] * s / m->E[e];
+        }
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -146,6 +146,17 @@ int orc_adjoint_strain_pairs(const orc_model* m, const double* u, const double* 
 
 int orc_reorder_nodes(const orc_model* m, int32_t block_dim, int32_t* order_out);
 
+/* Element-category objective term at the element centroids (category 0
+ * stress, 1 strain, 2 strainEnergy; component 1-6 for 0/1; optr 0 powerNorm,
+ * 1 ks, 2 volumeIntegral, 3 volumeAverage).  n_tgt 0, 1 or n_set targets.
+ * Outputs L, dLdu[n_dof], Q[n_el][36] (explicit material term: dL/dD =
+ * sum (dC/dD) : Q_e) and dLdE[n_el] (explicit isotropic-modulus term);
+ * any output may be NULL. */
+int orc_element_objective(const orc_model* m, const double* u, int32_t n_set, const int32_t* elem_set,
+                          int32_t category, int32_t component, int32_t optr, double coef, double expnt,
+                          int32_t n_tgt, const double* tgt, double* L_out, double* dLdu, double* Q,
+                          double* dLdE);
+
 #ifdef __cplusplus
 }
 #endif

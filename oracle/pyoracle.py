@@ -75,6 +75,8 @@ def load():
             "orc_adjoint_strain_pairs": (C.c_int, [C.c_void_p, P_d, P_d, P_d]),
             "orc_newmark_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double, P_d, P_d,
                                               C.c_int32, P_i, P_d, P_d, P_d]),
+            "orc_element_objective": (C.c_int, [C.c_void_p, P_d, C.c_int32, P_i, C.c_int32, C.c_int32, C.c_int32,
+                                                C.c_double, C.c_double, C.c_int32, P_d, P_d, P_d, P_d, P_d]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -290,6 +292,28 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"orc_adjoint_strain_pairs failed ({rc})")
         return P
+
+    ELEM_CATEGORIES = {"stress": 0, "strain": 1, "strainEnergy": 2}
+    ELEM_OPERATORS = {"powerNorm": 0, "ks": 1, "volumeIntegral": 2, "volumeAverage": 3}
+
+    def element_objective(self, u, elems, category, component=0, operator="powerNorm", coef=1.0, exponent=1.0,
+                          targets=()):
+        """Element-category objective term at the centroids: returns L,
+        dL/du [n_dof], the explicit material pairs Q [n_el, 6, 6] and the
+        explicit isotropic-modulus term dL/dE [n_el]."""
+        u = np.ascontiguousarray(u, np.float64)
+        el = np.ascontiguousarray(elems, np.int32)
+        tg = np.ascontiguousarray(targets if len(targets) else [0.0], np.float64)
+        L = C.c_double(0.0)
+        dLdu = np.zeros(self.n_dof)
+        Q = np.zeros((self.p.mesh.n_elems, 6, 6))
+        dLdE = np.zeros(self.p.mesh.n_elems)
+        rc = self.lib.orc_element_objective(self.m, _p(u), len(el), _p(el, C.c_int32), self.ELEM_CATEGORIES[category],
+                                            component, self.ELEM_OPERATORS[operator], coef, exponent, len(targets),
+                                            _p(tg), C.byref(L), _p(dLdu), _p(Q), _p(dLdE))
+        if rc != 0:
+            raise RuntimeError(f"orc_element_objective failed ({rc})")
+        return L.value, dLdu, Q, dLdE
 
     def newmark_adjoint(self, n_steps, dt, beta, gamma, f_shape, amp, obj_dof, obj_w):
         """Transient adjoint (construct with dynamic=True): L = sum over steps of

@@ -36,7 +36,15 @@ def beam():
     return p, 3 * tip + 2
 
 
-@pytest.mark.parametrize("beta,gamma", [(0.25, 0.5), (0.3, 0.55)])
+# (beta, gamma) in the reference's convention (beta_standard = gamma - beta,
+# node_meth.rs:127-138): both pairs keep beta_standard >= gamma / 2, the
+# unconditionally stable range; (0.25, 0.55) adds numerical damping.  (0.3,
+# 0.55) has beta_standard = 0.25 < 0.275 and its response grows without bound
+# on the plate's rotational modes.
+PAIRS = [(0.25, 0.5), (0.25, 0.55)]
+
+
+@pytest.mark.parametrize("beta,gamma", PAIRS)
 def test_transient_adjoint_beam(gpu_lib, oracle_lib, beta, gamma):
     p, dof = beam()
     dt, N = 2e-4, 40
@@ -59,7 +67,7 @@ def test_transient_adjoint_beam(gpu_lib, oracle_lib, beta, gamma):
     g.close()
 
 
-@pytest.mark.parametrize("beta,gamma", [(0.25, 0.5), (0.3, 0.55)])
+@pytest.mark.parametrize("beta,gamma", PAIRS)
 def test_transient_adjoint_shell_plate(gpu_lib, oracle_lib, beta, gamma):
     p = configs.shell_plate(n=20)
     dt, N = 2e-6, 150
