@@ -308,6 +308,7 @@ void shell_element_matrices(Ctx& c, int e0, int n, double* ke_host, double* me_h
 void brickim_assemble(Ctx& c, double* vals, double* mvals);
 void brickim_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate);
 void brickim_element_matrices(Ctx& c, int e0, int n, double* ke_host, double* me_host);
+void brickim_pairs(Ctx& c, const double* d_a, const double* d_b, double* d_P, bool accumulate);
 void brickim_element_ke32(Ctx& c, float* d_ke);
 // learned nodal preconditioner blocks (k_learned.cu)
 bool learned_ready(const Ctx& c);

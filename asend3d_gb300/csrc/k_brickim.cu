@@ -245,6 +245,60 @@ k_brick_adjoint(const int32_t* __restrict__ conn, const double* __restrict__ xyz
     }
 }
 
+// Strain-pair tensors with the condensed modes recovered (update_internal,
+// element_equations.rs:19-194): each field's internal DOF are
+// alpha = -Kii^-1 Kie f_e (the element's X), so the full 33-DOF strains give
+// P_e[i][j] = sum_gp w detJ eps_i(a) eps_j(b), the tensor whose contraction
+// with dC/dD is a^T dK~_e/dD b of the condensed matrix K~ = Kee - Kei X
+// (d K~ = [I, -X^T] dK [I; -X]).
+__global__ void __launch_bounds__(kBT)
+k_brick_pairs(const int32_t* __restrict__ conn, const double* __restrict__ xyz, const double* __restrict__ E,
+              const double* __restrict__ nu, const double* __restrict__ av, const double* __restrict__ bv,
+              double* __restrict__ P, int accumulate) {
+    __shared__ BrickSmem S;
+    __shared__ double f[2][kTot];
+    __shared__ double eps[2][8][6];
+    const int e = blockIdx.x, t = threadIdx.x;
+    brick_element(S, e, conn, xyz, E, nu, nullptr);
+    if (t < 2 * kNd) {
+        const int fld = t / kNd, c = t % kNd;
+        const size_t g = 3 * (size_t)conn[8 * (size_t)e + c / 3] + c % 3;
+        f[fld][c] = fld ? bv[g] : av[g];
+    }
+    __syncthreads();
+    if (t < 18) {
+        const int fld = t / 9, i = t % 9;
+        double acc = 0.0;
+        for (int c = 0; c < kNd; ++c) acc += S.X[i][c] * f[fld][c];
+        f[fld][kNd + i] = -acc;
+    }
+    __syncthreads();
+    if (t < 16) {  // strains of both fields at the 8 points
+        const int fld = t / 8, ip = t % 8;
+        double H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int fn = 0; fn < 11; ++fn)
+            for (int i = 0; i < 3; ++i) {
+                const double v = (fn < 8) ? f[fld][3 * fn + i] : f[fld][kNd + 3 * (fn - 8) + i];
+                for (int j = 0; j < 3; ++j) H[i][j] += v * S.dx[ip][fn][j];
+            }
+        double* ep = eps[fld][ip];
+        ep[0] = H[0][0];
+        ep[1] = H[1][1];
+        ep[2] = H[2][2];
+        ep[3] = H[0][1] + H[1][0];
+        ep[4] = H[0][2] + H[2][0];
+        ep[5] = H[1][2] + H[2][1];
+    }
+    __syncthreads();
+    if (t < 36) {
+        const int i = t / 6, j = t % 6;
+        double acc = 0.0;
+        for (int ip = 0; ip < 8; ++ip) acc += eps[0][ip][i] * eps[1][ip][j] * S.det[ip];
+        double* out = P + (size_t)e * 36 + t;
+        *out = accumulate ? *out + acc : acc;
+    }
+}
+
 __global__ void __launch_bounds__(kBT)
 k_brick_export(int e0, const int32_t* __restrict__ conn, const double* __restrict__ xyz, const double* __restrict__ E,
                const double* __restrict__ nu, const double* __restrict__ rho, double* __restrict__ ke,
@@ -293,6 +347,13 @@ void brickim_assemble(Ctx& c, double* vals, double* mvals) {
 void brickim_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate) {
     k_brick_adjoint<<<c.n_el, kBT, 0, c.stream>>>(c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, d_u, d_lam, d_g,
                                                  accumulate ? 1 : 0);
+    ASEND_CUDA(cudaGetLastError());
+    ++c.launches;
+}
+
+void brickim_pairs(Ctx& c, const double* d_a, const double* d_b, double* d_P, bool accumulate) {
+    k_brick_pairs<<<c.n_el, kBT, 0, c.stream>>>(c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, d_a, d_b, d_P,
+                                               accumulate ? 1 : 0);
     ASEND_CUDA(cudaGetLastError());
     ++c.launches;
 }

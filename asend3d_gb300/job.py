@@ -274,6 +274,7 @@ def read_loads(path) -> list:
 
 
 DV_CATEGORIES = ("modulus", "shearModulus", "poissonRatio")
+ELEMENT_CATEGORIES = ("stress", "strain", "strainEnergy")
 
 
 def read_design_vars(path) -> list:
@@ -521,12 +522,20 @@ class JobRunner:
         grad = np.zeros(len(self.dvs))
         opts = self._opts(self.solve_cmd)
         for t in self.objective:
-            if t["category"] != "displacement" or t["operator"] != "powerNorm" or t["exponent"] != 1.0:
-                raise NotImplementedError("gradients of displacement powerNorm terms of exponent 1 only")
+            element_term = t["category"] in ELEMENT_CATEGORIES
+            if not element_term and (t["category"] != "displacement" or t["operator"] != "powerNorm"
+                                     or t["exponent"] != 1.0):
+                raise NotImplementedError("gradients of displacement powerNorm terms of exponent 1 and of "
+                                          "stress / strain / strainEnergy terms only")
             if not (t["activeTime"][0] <= self.state["time"] <= t["activeTime"][1]):
                 continue
-            self.g.set_objective(("displacement", t["nodeSet"], t["component"], t["coefficient"]))
-            _, _, rc, st = self.g.adjoint_gradient(**opts)
+            if element_term:
+                self.g.set_element_objective(self._term_elements(t), t["category"], t["component"], t["operator"],
+                                             t["coefficient"], t["exponent"], t["targets"])
+                _, _, rc, st = self.g.adjoint_gradient(want_dLdE=False, **opts)
+            else:
+                self.g.set_objective(("displacement", t["nodeSet"], t["component"], t["coefficient"]))
+                _, _, rc, st = self.g.adjoint_gradient(**opts)
             if rc not in (_lib.ASEND_OK, _lib.ASEND_MAX_ITER):
                 raise RuntimeError(f"adjoint solve failed: {st}")
             _cg_log(st["iterations"], st["rel_residual"])
@@ -636,6 +645,13 @@ class JobRunner:
         key = {"displacement": "u", "velocity": "v", "acceleration": "a"}[field]
         self.state[key] = (amp / np.abs(mode).max()) * mode
 
+    def _term_elements(self, t):
+        """Element indices of an element-category term's set."""
+        name = t.get("elementSet")
+        if name is None or name not in self.problem.elem_sets:
+            raise ValueError(f"objective terms of category '{t['category']}' need a valid element set")
+        return self.problem.elem_sets[name]
+
     def cmd_calcObjective(self, c):
         if self.state is None:
             raise RuntimeError("calcObjective before a solve")
@@ -643,7 +659,21 @@ class JobRunner:
             raise NotImplementedError("time-integrated objectives of dynamic runs are not on the GPU path")
         vals = []
         fields = {"displacement": "u", "velocity": "v", "acceleration": "a"}
+        cent = None
         for t in self.objective:
+            if t["category"] in ELEMENT_CATEGORIES:
+                # stress / strain / strainEnergy at the element centroids
+                # (objective_meth.rs:665-720) with the term's operator
+                from .objective import element_term
+                if not (t["activeTime"][0] <= self.state["time"] <= t["activeTime"][1]):
+                    vals.append(0.0)
+                    continue
+                if cent is None:
+                    cent = self.g.element_fields(0)
+                L, _, _ = element_term(*cent, self._term_elements(t), t["category"], t["component"], t["operator"],
+                                       t["coefficient"], t["exponent"], t["targets"])
+                vals.append(L)
+                continue
             if t["category"] not in fields or t["operator"] != "powerNorm":
                 raise NotImplementedError(f"objective {t['category']}/{t['operator']} is not on the GPU path")
             arr = self.state[fields[t["category"]]]

@@ -294,8 +294,10 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
  *   asend_material_dv_gradient returns dL/dD for one DV over an element set
  *     (coefficients as asend_add_modulus_design_var), with C = S^-1 from the
  *     reference's compliance form at the element's isotropic E, nu.
- * hex8 and tet4 meshes (elements without condensed internal DOF); elements
- * with orthotropic constants (asend_set_orthotropic) use their own S. */
+ * hex8, tet4 and brickIM meshes: brickIM strains include the condensed
+ * modes recovered per element (alpha = -Kii^-1 Kie f_e for both fields,
+ * update_internal element_equations.rs:19-194); elements with orthotropic
+ * constants (asend_set_orthotropic) use their own S. */
 #define ASEND_DV_MODULUS 0
 #define ASEND_DV_SHEAR_MODULUS 1
 #define ASEND_DV_POISSON_RATIO 2

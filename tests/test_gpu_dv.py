@@ -113,30 +113,50 @@ def test_isotropic_identity_and_poisson_fd(gpu_lib, oracle_lib):
     g.close()
 
 
-def test_brickim_rejected(gpu_lib):
-    m = block_hex8(2, 1, 1, 1.0, 0.5, 0.5)
-    m.elem_type = 81
-    p = Problem(m, np.full(2, 1e9), np.full(2, 0.3))
-    p.add_node_set("xMin", m.nodes_in_range(xr=(-1e-9, 1e-9)))
-    p.fix_displacement("xMin")
-    p.add_elem_set("all", [0, 1])
-    p.add_load_vector(np.ones(m.n_dof))
+def test_brickim_pairs_match_oracle(gpu_lib, oracle_lib):
+    """brickIM: strain pairs with the condensed modes recovered against the
+    oracle's (orc_adjoint_strain_pairs), 1e-8 of the largest entry; the
+    pairs contracted with C_e / E_e reproduce the condensed per-element
+    gradient (1e-10); material DV gradients equal -sum (dC/dD) : P_oracle."""
+    p = beam()
+    p.mesh.elem_type = 81
     g = GpuSolver(p)
     g.assemble(precision=64)
     g.static_solve(**KW)
-    g.adjoint_gradient(**KW)
-    with pytest.raises(AsendError, match="hex8 and tet4"):
-        g.material_dv_gradient("modulus", 1, "all")
+    L, gE, rc, _ = g.adjoint_gradient(**KW)
+    assert rc == 0
+    P = g.strain_pairs()
+    o = oracle_lib.Oracle(p)
+    uo, _, _ = o.solve(o.loads()[0] + o.penalty_rhs(), precond=oracle_lib.PC_DIRECT)
+    tip = p.node_sets["tip"]
+    dLdu = np.zeros(o.n_dof)
+    dLdu[3 * tip + 2] = 1.0 / len(tip)
+    _, lam, _, _ = o.adjoint(uo, dLdu=dLdu, precond=oracle_lib.PC_DIRECT)
+    Po = o.strain_pairs(uo, lam)
+    assert np.abs(P - Po).max() <= 1e-8 * np.abs(Po).max()
+    giso = np.array([-(iso_C(1.0, nu) * P[e]).sum() for e, nu in enumerate(p.nu)])
+    assert np.abs(giso - gE).max() <= 1e-10 * np.abs(gE).max()
+    from test_gpu_job import compliance_dC
+    for cat, k in (("modulus", 1), ("shearModulus", 3), ("poissonRatio", 2)):
+        ref = -sum((compliance_dC(p.E[e], p.nu[e], p.E[e] / (2 * (1 + p.nu[e])), cat, k) * Po[e]).sum()
+                   for e in range(p.mesh.n_elems))
+        assert g.material_dv_gradient(cat, k, "all") == pytest.approx(ref, rel=1e-8)
     g.close()
 
 
-def test_job_gradient_file(gpu_lib, oracle_lib, tmp_path):
-    m, xmin, xmax = write_cantilever_job(tmp_path, etype="brick8", modal=False, dvs=True)
+@pytest.mark.parametrize("etype", ["brick8", "brickIM"])
+def test_job_gradient_file(gpu_lib, oracle_lib, tmp_path, etype):
+    """calcObjGradient through the job runner: the three DVs of the
+    cantilever job against the oracle's strain pairs contracted with the
+    compliance-form dC/dD (1e-7), brickIM with its condensed modes."""
+    from test_gpu_job import compliance_dC
+    m, xmin, xmax = write_cantilever_job(tmp_path, etype=etype, modal=False, dvs=True)
     r = J.JobRunner(tmp_path / "job.yaml").run()
     lines = (tmp_path / "obj_grad.csv").read_text().splitlines()
     assert lines[0] == "designVariable,objGrad" and len(lines) == 4
     grad = [float(ln.split(",")[1]) for ln in lines[1:]]
-    # oracle: modulus component 1 over all elements, coefficient 1
+    if etype == "brickIM":
+        m.elem_type = 81
     p = Problem(m, np.full(m.n_elems, 1e6), np.full(m.n_elems, 0.0), np.full(m.n_elems, 1.0))
     p.add_node_set("xMin", xmin)
     p.add_node_set("xMax", xmax)
@@ -147,7 +167,14 @@ def test_job_gradient_file(gpu_lib, oracle_lib, tmp_path):
     dLdu = np.zeros(o.n_dof)
     dLdu[3 * xmax + 2] = 1.0 / len(xmax)
     _, lam, _, _ = o.adjoint(uo, dLdu=dLdu, precond=oracle_lib.PC_DIRECT)
-    assert grad[0] == pytest.approx(o.component_gradient(uo, lam, 1).sum(), rel=1e-7)
+    Po = o.strain_pairs(uo, lam)
+    if etype == "brick8":
+        assert grad[0] == pytest.approx(o.component_gradient(uo, lam, 1).sum(), rel=1e-7)
+    dvs = [("modulus", 1, np.ones(m.n_elems)), ("shearModulus", 2, np.ones(m.n_elems)),
+           ("poissonRatio", 3, np.array([2.0, 3.0, 4.0, 5.0]))]
+    for k, (cat, comp, cf) in enumerate(dvs):
+        dC = compliance_dC(1e6, 0.0, 5e5, cat, comp)
+        ref = -np.sum(cf[:, None, None] * dC[None] * Po)
+        assert grad[k] == pytest.approx(ref, rel=1e-7, abs=1e-9 * max(abs(g) for g in grad))
     # the bending beam's tip deflection falls as E1 grows
     assert grad[0] > 0  # w < 0, so dw/dE1 > 0
-    assert np.isfinite(grad).all()
