@@ -175,8 +175,9 @@ int element_type(const std::string& t) {
     if (t == "brick8") return 8;
     if (t == "brickIM") return 81;
     if (t == "tet4") return 4;
+    if (t == "tet10") return 10;
     if (t == "shell4") return 41;
-    for (const char* o : {"wedge6", "tet10", "shell3", "beam2", "frcFld", "mass", "fl4", "fl6", "fl8", "fl10"})
+    for (const char* o : {"wedge6", "shell3", "beam2", "frcFld", "mass", "fl4", "fl6", "fl8", "fl10"})
         if (t == o) throw Fail("element type " + t + " is not on the GPU path");
     throw Fail("unrecognized element type: " + t);
 }

@@ -34,6 +34,7 @@ int nodes_per_elem(int type) {
         case 8: return 8;
         case 81: return 8;
         case 4: return 4;
+        case 10: return 10;
         case 41: return 4;
         default: return 0;
     }
@@ -441,7 +442,7 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
                    const double* rho, const double* thickness) {
     return guarded(ctx, [&](Ctx& c) {
         const int nn = nodes_per_elem(elem_type);
-        require(nn > 0, "unsupported element type (supported: 8 hex8, 81 brickIM, 4 tet4, 41 shell4)");
+        require(nn > 0, "unsupported element type (supported: 8 hex8, 81 brickIM, 4 tet4, 10 tet10, 41 shell4)");
         require(n_nodes > 0 && n_elems > 0 && coords && conn && E && nu, "empty or null mesh input");
         for (int64_t k = 0; k < (int64_t)n_elems * nn; ++k)
             require(conn[k] >= 0 && conn[k] < n_nodes, "connectivity refers to a node out of range");
@@ -488,7 +489,7 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         } else {
             c.nn = nn;
             c.udpn = 3;
-            c.nip = (nn == 8) ? 8 : 1;
+            c.nip = (nn == 8) ? 8 : (nn == 10 ? 4 : 1);
             c.n_nodes = n_nodes;
             c.xyz.assign(coords, coords + (size_t)3 * n_nodes);
             c.conn.assign(conn, conn + (size_t)n_elems * nn);
@@ -698,8 +699,8 @@ int asend_set_orthotropic(asend_ctx* ctx, const double* props) {
             c.ortho.clear();
             c.d_cmat.release();
         } else {
-            require(c.type == 8 || c.type == 4,
-                    "orthotropic materials take hex8 / tet4 meshes (elements without condensed internal DOF)");
+            require(c.type == 8 || c.type == 4 || c.type == 10,
+                    "orthotropic materials take hex8 / tet4 / tet10 meshes (elements without condensed internal DOF)");
             std::vector<double> C((size_t)c.n_el * 36);
             for (int e = 0; e < c.n_el; ++e)
                 require(orthotropic_cmat(props + (size_t)e * 9, &C[(size_t)e * 36]),
@@ -718,9 +719,9 @@ int asend_set_damping(asend_ctx* ctx, double rayleigh_cm, double rayleigh_ck, co
         require(c.n_el > 0, "set the mesh first");
         require(std::isfinite(rayleigh_cm) && std::isfinite(rayleigh_ck) && rayleigh_cm >= 0.0 && rayleigh_ck >= 0.0,
                 "Rayleigh coefficients must be finite and non-negative");
-        require(!(rayleigh_ck != 0.0 || D) || c.type == 8 || c.type == 4,
-                "stiffness-proportional and material damping take hex8 / tet4 meshes (elements without condensed "
-                "internal DOF)");
+        require(!(rayleigh_ck != 0.0 || D) || c.type == 8 || c.type == 4 || c.type == 10,
+                "stiffness-proportional and material damping take hex8 / tet4 / tet10 meshes (elements without "
+                "condensed internal DOF)");
         c.ray_cm = rayleigh_cm;
         c.ray_ck = rayleigh_ck;
         if (D) {
@@ -925,7 +926,7 @@ static int element_node_weights(const Ctx& c, int e, double* w, int64_t* dof, do
         return 4;
     }
     const int nn = c.nn;
-    double x[8][3];
+    double x[10][3];
     for (int a = 0; a < nn; ++a) {
         const int nd = c.conn[(size_t)e * nn + a];
         for (int j = 0; j < 3; ++j) x[a][j] = c.xyz[3 * (size_t)nd + j];
@@ -947,6 +948,22 @@ static int element_node_weights(const Ctx& c, int e, double* w, int64_t* dof, do
                            v1[2] * (v2[0] * v3[1] - v2[1] * v3[0]);
         for (int a = 0; a < 4; ++a) w[a] = std::fabs(det) / 24.0;
         return 4;
+    }
+    if (nn == 10) {  // quadratic tet: the 4-point rule, weights 1/24
+        for (int a = 0; a < 10; ++a) w[a] = 0.0;
+        for (int p = 0; p < 4; ++p) {
+            double s[3], N[10], dn[10][3], J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            tet10_point(p, s);
+            tet10_shape(s, N, dn);
+            for (int a = 0; a < 10; ++a)
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) J[i][j] += x[a][i] * dn[a][j];
+            const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                               J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                               J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+            for (int a = 0; a < 10; ++a) w[a] += N[a] * det / 24.0;
+        }
+        return 10;
     }
     const double g = 0.5773502691896257;
     const double sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
@@ -990,8 +1007,8 @@ int asend_add_body_load(asend_ctx* ctx, int32_t rhs, int32_t elem_set, int32_t k
             require(l > 0.0, "centrifugal axis of zero length");
             for (int j = 0; j < 3; ++j) ax[j] = axis[j] / l;
         }
-        double w[8], cent[3];
-        int64_t dof[8];
+        double w[10], cent[3];
+        int64_t dof[10];
         for (int e : c.elem_sets[elem_set]) {
             const int na = element_node_weights(c, e, w, dof, cent);
             double acc[3];
@@ -1241,8 +1258,8 @@ int asend_set_objective(asend_ctx* ctx, int32_t kind, int32_t node_set, int32_t 
 int asend_set_element_objective(asend_ctx* ctx, const double* w_stress, const double* w_strain) {
     return guarded(ctx, [&](Ctx& c) {
         require(c.n_el > 0, "set the mesh first");
-        require(c.type == 8 || c.type == 81 || c.type == 4,
-                "element-category objectives are built for hex8, brickIM and tet4 meshes");
+        require(c.type == 8 || c.type == 81 || c.type == 4 || c.type == 10,
+                "element-category objectives are built for hex8, brickIM, tet4 and tet10 meshes");
         const size_t m = (size_t)c.n_el * 6;
         for (const double* w : {w_stress, w_strain})
             if (w)

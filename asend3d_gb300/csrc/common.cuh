@@ -98,6 +98,42 @@ struct PcgScalars {
 struct MgHierarchy;
 struct LearnedState;
 
+// Quadratic tetrahedron (type 10) at s: corners 0..3, mid-edge nodes 4 (0-1),
+// 5 (1-2), 6 (0-2), 7 (0-3), 8 (1-3), 9 (2-3) (element_soln_fields.rs:229-298).
+__host__ __device__ inline void tet10_shape(const double* s, double* n, double (*dn)[3]) {
+    const double p1 = 1.0 - s[0] - s[1] - s[2];
+    n[0] = p1 * (2.0 * p1 - 1.0);
+    for (int j = 0; j < 3; ++j) dn[0][j] = 1.0 - 4.0 * p1;
+    for (int k = 0; k < 3; ++k) {
+        n[1 + k] = s[k] * (2.0 * s[k] - 1.0);
+        for (int j = 0; j < 3; ++j) dn[1 + k][j] = (j == k) ? 4.0 * s[k] - 1.0 : 0.0;
+    }
+    const int edge0[3] = {4, 6, 7};  // edges (0, k+1): 4 s_k p1
+    for (int k = 0; k < 3; ++k) {
+        const int a = edge0[k];
+        n[a] = 4.0 * s[k] * p1;
+        for (int j = 0; j < 3; ++j) dn[a][j] = (j == k) ? 4.0 * (p1 - s[k]) : -4.0 * s[k];
+    }
+    const int edge[3][3] = {{5, 0, 1}, {8, 0, 2}, {9, 1, 2}};  // edges between corners 1..3: 4 s_i s_j
+    for (int q = 0; q < 3; ++q) {
+        const int a = edge[q][0], i = edge[q][1], k = edge[q][2];
+        n[a] = 4.0 * s[i] * s[k];
+        for (int j = 0; j < 3; ++j) dn[a][j] = (j == i) ? 4.0 * s[k] : (j == k ? 4.0 * s[i] : 0.0);
+    }
+}
+
+// The tet10 rule: four points with R_TET1 ~ (5 - sqrt 5) / 20 on every axis
+// but one, which takes R_TET2 ~ (5 + 3 sqrt 5) / 20, weights 1/24
+// (element_meth.rs:228-262).  The values are the reference's own 16-digit
+// constants (constants.rs:10-11), 2e-14 from the exact roots, so that the
+// element matrices agree with the reference's to rounding.
+constexpr double kRTet1 = 0.1381966011250071;
+constexpr double kRTet2 = 0.585410196624929;
+__host__ __device__ inline void tet10_point(int gp, double* s) {
+    s[0] = s[1] = s[2] = kRTet1;
+    if (gp > 0) s[gp - 1] = kRTet2;
+}
+
 struct Ctx {
     int device = 0;
     // structured-block metadata (multigrid) and its hierarchy

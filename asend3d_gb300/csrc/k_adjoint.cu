@@ -69,6 +69,11 @@ __device__ __forceinline__ double point_strains(int gp, const double (&x)[NN][3]
             dn[a][2] = 0.125 * sg[a][2] * f0 * f1;
         }
         wt = 1.0;
+    } else if constexpr (NN == 10) {
+        double sp[3], nv[10];
+        tet10_point(gp, sp);
+        tet10_shape(sp, nv, dn);
+        wt = 1.0 / 24.0;
     } else {
         const double d[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
 #pragma unroll
@@ -133,7 +138,7 @@ k_adjoint_modulus(int n_el, const int32_t* __restrict__ conn, const double* __re
     const double ne = nu[e];
     const double lam = ne / ((1.0 + ne) * (1.0 - 2.0 * ne));  // C / E
     const double mu = 1.0 / (2.0 * (1.0 + ne));
-    constexpr int NIP = (NN == 8) ? 8 : 1;
+    constexpr int NIP = (NN == 8) ? 8 : (NN == 10 ? 4 : 1);
     double acc = 0.0;
 #pragma unroll
     for (int gp = 0; gp < NIP; ++gp) {
@@ -163,7 +168,7 @@ k_adjoint_pairs(int n_el, const int32_t* __restrict__ conn, const double* __rest
     if (e >= n_el) return;
     double x[NN][3], ua[NN][3], ub[NN][3];
     gather_element<NN>(e, conn, xyz, av, bv, x, ua, ub);
-    constexpr int NIP = (NN == 8) ? 8 : 1;
+    constexpr int NIP = (NN == 8) ? 8 : (NN == 10 ? 4 : 1);
     double acc[36];
 #pragma unroll
     for (int k = 0; k < 36; ++k) acc[k] = 0.0;
@@ -231,6 +236,9 @@ void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g,
     if (c.nn == 8)
         k_adjoint_modulus<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_nu.p, d_a, d_b, d_g,
                                                             accumulate ? 1 : 0);
+    else if (c.nn == 10)
+        k_adjoint_modulus<10><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_nu.p, d_a, d_b, d_g,
+                                                             accumulate ? 1 : 0);
     else
         k_adjoint_modulus<4><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_nu.p, d_a, d_b, d_g,
                                                             accumulate ? 1 : 0);
@@ -243,11 +251,14 @@ void adjoint_pairs(Ctx& c, const double* d_a, const double* d_b, double* d_P, bo
         brickim_pairs(c, d_a, d_b, d_P, accumulate);
         return;
     }
-    if (c.type != 8 && c.type != 4)
-        throw InputError("strain-pair tensors are built for hex8, brickIM and tet4 meshes");
+    if (c.type != 8 && c.type != 4 && c.type != 10)
+        throw InputError("strain-pair tensors are built for hex8, brickIM, tet4 and tet10 meshes");
     const int blocks = (c.n_el + 127) / 128;
     if (c.nn == 8)
         k_adjoint_pairs<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, d_a, d_b, d_P, accumulate ? 1 : 0);
+    else if (c.nn == 10)
+        k_adjoint_pairs<10><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, d_a, d_b, d_P,
+                                                           accumulate ? 1 : 0);
     else
         k_adjoint_pairs<4><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, d_a, d_b, d_P, accumulate ? 1 : 0);
     ASEND_CUDA(cudaGetLastError());

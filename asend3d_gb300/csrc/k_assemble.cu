@@ -33,7 +33,11 @@ __constant__ double c_hex_dn[8][8][3];  // [gp][node][ds_j]
 __constant__ double c_hex_n[8][8];      // [gp][node]
 __constant__ int c_hex_pair[36][2];
 __constant__ int c_tet_pair[10][2];
+__constant__ double c_t10_dn[4][10][3];  // tet10 at its 4 points
+__constant__ double c_t10_n[4][10];
+__constant__ int c_t10_pair[55][2];
 bool g_tables_ready = false;
+
 
 void init_tables() {
     if (g_tables_ready) return;
@@ -66,6 +70,19 @@ void init_tables() {
     ASEND_CUDA(cudaMemcpyToSymbol(c_hex_n, nv, sizeof(nv)));
     ASEND_CUDA(cudaMemcpyToSymbol(c_hex_pair, hp, sizeof(hp)));
     ASEND_CUDA(cudaMemcpyToSymbol(c_tet_pair, tp, sizeof(tp)));
+    double t10dn[4][10][3], t10n[4][10];
+    for (int gp = 0; gp < 4; ++gp) {
+        double sp[3];
+        tet10_point(gp, sp);
+        tet10_shape(sp, t10n[gp], t10dn[gp]);
+    }
+    int t10p[55][2];
+    k = 0;
+    for (int a = 0; a < 10; ++a)
+        for (int b = a; b < 10; ++b) { t10p[k][0] = a; t10p[k][1] = b; ++k; }
+    ASEND_CUDA(cudaMemcpyToSymbol(c_t10_dn, t10dn, sizeof(t10dn)));
+    ASEND_CUDA(cudaMemcpyToSymbol(c_t10_n, t10n, sizeof(t10n)));
+    ASEND_CUDA(cudaMemcpyToSymbol(c_t10_pair, t10p, sizeof(t10p)));
     g_tables_ready = true;
 }
 
@@ -92,6 +109,24 @@ template <>
 struct ElemTraits<4> {
     static constexpr int NIP = 1, NP = 10, EB = 32;
 };
+template <>
+struct ElemTraits<10> {
+    static constexpr int NIP = 4, NP = 55, EB = 8;
+};
+
+template <int NN>
+__device__ __forceinline__ void pair_of(int p, int& a, int& b) {
+    if constexpr (NN == 8) {
+        a = c_hex_pair[p][0];
+        b = c_hex_pair[p][1];
+    } else if constexpr (NN == 10) {
+        a = c_t10_pair[p][0];
+        b = c_t10_pair[p][1];
+    } else {
+        a = c_tet_pair[p][0];
+        b = c_tet_pair[p][1];
+    }
+}
 
 template <int NN, typename T>
 __device__ __forceinline__ void shape_ref(int gp, int a, T& n, T (&dn)[3]) {
@@ -100,6 +135,11 @@ __device__ __forceinline__ void shape_ref(int gp, int a, T& n, T (&dn)[3]) {
         dn[0] = (T)c_hex_dn[gp][a][0];
         dn[1] = (T)c_hex_dn[gp][a][1];
         dn[2] = (T)c_hex_dn[gp][a][2];
+    } else if constexpr (NN == 10) {
+        n = (T)c_t10_n[gp][a];
+        dn[0] = (T)c_t10_dn[gp][a][0];
+        dn[1] = (T)c_t10_dn[gp][a][1];
+        dn[2] = (T)c_t10_dn[gp][a][2];
     } else {
         n = (T)0.25;
         dn[0] = (a == 1) ? (T)1 : (a == 0 ? (T)-1 : (T)0);
@@ -170,15 +210,15 @@ assemble_colour_kernel(int n_el, const int32_t* __restrict__ el_list, const int3
 #pragma unroll
             for (int j = 0; j < 3; ++j) s_g[el][gp][a][j] = dn[0] * Ji[0][j] + dn[1] * Ji[1][j] + dn[2] * Ji[2][j];
         }
-        s_w[el][gp] = det * ((NN == 8) ? (T)1 : (T)(1.0 / 6.0));
+        s_w[el][gp] = det * ((NN == 8) ? (T)1 : (NN == 10 ? (T)(1.0 / 24.0) : (T)(1.0 / 6.0)));
     }
     __syncthreads();
     if (tid >= EB * NP) return;
     const int el = tid / NP, p = tid % NP;
     const int e = s_el[el];
     if (e < 0) return;
-    const int a = (NN == 8) ? c_hex_pair[p][0] : c_tet_pair[p][0];
-    const int b = (NN == 8) ? c_hex_pair[p][1] : c_tet_pair[p][1];
+    int a, b;
+    pair_of<NN>(p, a, b);
     T S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     T m = 0;
 #pragma unroll
@@ -754,9 +794,11 @@ void assemble_operator(Ctx& c, int precision) {
             brickim_assemble(c, A.v64.p, mvals);  // FP64 condensed element matrices at either precision
         } else if (precision == 64) {
             if (c.nn == 8) launch_colours<8, double>(c, A.v64.p, mvals, cM_el, X);
+            else if (c.nn == 10) launch_colours<10, double>(c, A.v64.p, mvals, cM_el, X);
             else launch_colours<4, double>(c, A.v64.p, mvals, cM_el, X);
         } else {
             if (c.nn == 8) launch_colours<8, float>(c, A.v32.p, mvals, cM_el, X);
+            else if (c.nn == 10) launch_colours<10, float>(c, A.v32.p, mvals, cM_el, X);
             else launch_colours<4, float>(c, A.v32.p, mvals, cM_el, X);
             widen_kernel<<<stream_grid(nval), 256, 0, c.stream>>>(nval, A.v32.p, A.v64.p);
             ++c.launches;

@@ -12,13 +12,15 @@
 // so that dL/du = sum_e B_c^T (b_e + C_e a_e) and the explicit material term
 // is dL/dD = sum_e a_e^T (dC_e/dD) eps_e.  B_c is the strain-displacement
 // matrix at the centroid: s = 0 for hex8 and brickIM (whose incompatible
-// modes 1 - s_i^2 have zero slope there, element_soln_fields.rs:212-227) and
-// the constant tet4 gradients.
+// modes 1 - s_i^2 have zero slope there, element_soln_fields.rs:212-227),
+// the constant tet4 gradients, and s = (1/4, 1/4, 1/4) for tet10
+// (element_meth.rs:257-259).
 //
 // GB300 design: one thread per element; node data gathered once and made
 // element-relative in FP64; the adjoint right-hand side is scattered with
 // FP64 atomics (at most 8 elements meet at a node of a block mesh).
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -45,6 +47,10 @@ __device__ __forceinline__ void centroid_gradients(int e, const int32_t* __restr
         for (int a = 0; a < 8; ++a)
 #pragma unroll
             for (int j = 0; j < 3; ++j) dn[a][j] = 0.125 * sg[a][j];
+    } else if constexpr (NN == 10) {
+        const double sc[3] = {0.25, 0.25, 0.25};  // s_cent of tet10 (element_meth.rs:257-259)
+        double nv[10];
+        tet10_shape(sc, nv, dn);
     } else {
         const double d[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
 #pragma unroll
@@ -104,6 +110,23 @@ __device__ __forceinline__ void centroid_gradients(int e, const int32_t* __restr
             v += Jp[0][0] * (Jp[1][1] * Jp[2][2] - Jp[1][2] * Jp[2][1]) +
                  Jp[0][1] * (Jp[1][2] * Jp[2][0] - Jp[1][0] * Jp[2][2]) +
                  Jp[0][2] * (Jp[1][0] * Jp[2][1] - Jp[1][1] * Jp[2][0]);
+        }
+        *vol = v;
+    } else if constexpr (NN == 10) {
+        double v = 0.0;
+#pragma unroll 1
+        for (int gp = 0; gp < 4; ++gp) {
+            double sp[3], nv[10], dp[10][3], Jp[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            tet10_point(gp, sp);
+            tet10_shape(sp, nv, dp);
+            for (int a = 0; a < 10; ++a)
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) Jp[i][j] += x[a][i] * dp[a][j];
+            v += (Jp[0][0] * (Jp[1][1] * Jp[2][2] - Jp[1][2] * Jp[2][1]) +
+                  Jp[0][1] * (Jp[1][2] * Jp[2][0] - Jp[1][0] * Jp[2][2]) +
+                  Jp[0][2] * (Jp[1][0] * Jp[2][1] - Jp[1][1] * Jp[2][0])) / 24.0;
         }
         *vol = v;
     } else {
@@ -266,8 +289,16 @@ k_centroid_explicit(int n_el, const int32_t* __restrict__ conn, const double* __
 }
 
 void check_solid(const Ctx& c) {
-    if (c.type != 8 && c.type != 81 && c.type != 4)
-        throw InputError("element-category objectives are built for hex8, brickIM and tet4 meshes");
+    if (c.type != 8 && c.type != 81 && c.type != 4 && c.type != 10)
+        throw InputError("element-category objectives are built for hex8, brickIM, tet4 and tet10 meshes");
+}
+
+// one launch of a kernel templated on the element's node count
+template <typename F>
+void by_nodes(const Ctx& c, F&& f) {
+    if (c.nn == 8) f(std::integral_constant<int, 8>{});
+    else if (c.nn == 10) f(std::integral_constant<int, 10>{});
+    else f(std::integral_constant<int, 4>{});
 }
 
 const double* cmat_of(const Ctx& c) { return c.ortho.empty() ? nullptr : c.d_cmat.p; }
@@ -277,12 +308,10 @@ const double* cmat_of(const Ctx& c) { return c.ortho.empty() ? nullptr : c.d_cma
 void element_fields(Ctx& c, const double* d_u, double* d_eps, double* d_sig, double* d_vol) {
     check_solid(c);
     const int blocks = (c.n_el + 127) / 128;
-    if (c.nn == 8)
-        k_centroid_fields<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p,
-                                                            cmat_of(c), d_u, d_eps, d_sig, d_vol);
-    else
-        k_centroid_fields<4><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p,
-                                                            cmat_of(c), d_u, d_eps, d_sig, d_vol);
+    by_nodes(c, [&](auto nn) {
+        k_centroid_fields<decltype(nn)::value><<<blocks, 128, 0, c.stream>>>(
+            c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, cmat_of(c), d_u, d_eps, d_sig, d_vol);
+    });
     ASEND_CUDA(cudaGetLastError());
     ++c.launches;
 }
@@ -290,12 +319,10 @@ void element_fields(Ctx& c, const double* d_u, double* d_eps, double* d_sig, dou
 void element_objective_rhs(Ctx& c, double* d_rhs) {
     check_solid(c);
     const int blocks = (c.n_el + 127) / 128;
-    if (c.nn == 8)
-        k_centroid_rhs<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, cmat_of(c),
-                                                         c.d_obj_wa.p, c.d_obj_wb.p, d_rhs);
-    else
-        k_centroid_rhs<4><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, cmat_of(c),
-                                                         c.d_obj_wa.p, c.d_obj_wb.p, d_rhs);
+    by_nodes(c, [&](auto nn) {
+        k_centroid_rhs<decltype(nn)::value><<<blocks, 128, 0, c.stream>>>(
+            c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, cmat_of(c), c.d_obj_wa.p, c.d_obj_wb.p, d_rhs);
+    });
     ASEND_CUDA(cudaGetLastError());
     ++c.launches;
 }
@@ -303,12 +330,10 @@ void element_objective_rhs(Ctx& c, double* d_rhs) {
 void element_objective_explicit(Ctx& c, const double* d_u, double* d_gE, double* d_P) {
     check_solid(c);
     const int blocks = (c.n_el + 127) / 128;
-    if (c.nn == 8)
-        k_centroid_explicit<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p,
-                                                              cmat_of(c), c.d_obj_wa.p, d_u, d_gE, d_P);
-    else
-        k_centroid_explicit<4><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p,
-                                                              cmat_of(c), c.d_obj_wa.p, d_u, d_gE, d_P);
+    by_nodes(c, [&](auto nn) {
+        k_centroid_explicit<decltype(nn)::value><<<blocks, 128, 0, c.stream>>>(
+            c.n_el, c.d_conn.p, c.d_xyz.p, c.d_E.p, c.d_nu.p, cmat_of(c), c.d_obj_wa.p, d_u, d_gE, d_P);
+    });
     ASEND_CUDA(cudaGetLastError());
     ++c.launches;
 }

@@ -40,8 +40,8 @@ from pathlib import Path
 
 import numpy as np
 
-ELEMENT_TYPES = {"brick8": 8, "brickIM": 81, "tet4": 4, "shell4": 41}
-OTHER_ELEMENT_TYPES = ("wedge6", "tet10", "shell3", "beam2", "frcFld", "mass", "fl4", "fl6", "fl8", "fl10")
+ELEMENT_TYPES = {"brick8": 8, "brickIM": 81, "tet4": 4, "tet10": 10, "shell4": 41}
+OTHER_ELEMENT_TYPES = ("wedge6", "shell3", "beam2", "frcFld", "mass", "fl4", "fl6", "fl8", "fl10")
 
 
 # ---------------------------------------------------------------------------
@@ -414,12 +414,12 @@ class JobRunner:
             raise ValueError("elements without a section")
         p = Problem(mesh, E, nu, rho, thickness=None if np.isnan(thk).all() else thk)
         if ortho:
-            if m.elem_type not in (8, 4):
-                raise NotImplementedError("orthotropic materials take hex8 / tet4 meshes on the GPU path")
+            if m.elem_type not in (8, 4, 10):
+                raise NotImplementedError("orthotropic materials take hex8 / tet4 / tet10 meshes on the GPU path")
             p.ortho = props
         if np.any(damp):
-            if m.elem_type not in (8, 4):
-                raise NotImplementedError("material damping takes hex8 / tet4 meshes on the GPU path")
+            if m.elem_type not in (8, 4, 10):
+                raise NotImplementedError("material damping takes hex8 / tet4 / tet10 meshes on the GPU path")
             p.damping = (0.0, 0.0, damp)
         for name, labs in m.node_sets.items():
             p.add_node_set(name, [nidx[v] for v in labs])
@@ -587,7 +587,7 @@ class JobRunner:
             kw = self._opts(cmd)
             kw["precond"] = _lib.PC_JACOBI if kw["precond"] == _lib.PC_MG else kw["precond"]
             save = bool(cmd.get("saveSolnHist"))
-            if save and self.model.elem_type not in (8, 4):
+            if save and self.model.elem_type not in (8, 4, 10):
                 raise NotImplementedError("solution histories of elements with internal DOF are not written by the "
                                           "GPU path")
             g.keep_history(3)  # the last state's velocity and acceleration, and the solnTStep files

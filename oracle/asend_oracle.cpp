@@ -2079,7 +2079,9 @@ int orc_element_objective(const orc_model* m, const double* u, int32_t n_set, co
     const int nn = t.nn, tot = 3 * nn;
     const int stype = (t.type == 81) ? 8 : t.type;
     const TypeInfo ts = type_info(stype);
-    const double s_cent[3] = {0.0, 0.0, 0.0};  // hex8 / brickIM / tet4 (element_meth.rs:81-83)
+    // s_cent: 0 for hex8 / brickIM / tet4 (element_meth.rs:81-83), 1/4 for tet10 (:257-259)
+    const double sc = (t.type == 10) ? 0.25 : 0.0;
+    const double s_cent[3] = {sc, sc, sc};
     std::vector<double> q(n_set), vol(n_set), tg(n_set), eps(6 * (size_t)n_set), sig(6 * (size_t)n_set);
     std::vector<double> Bc((size_t)n_set * 6 * tot), Cs((size_t)n_set * 36);
     for (int k = 0; k < n_set; ++k) {
