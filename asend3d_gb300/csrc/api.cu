@@ -521,6 +521,9 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         c.n_inst = 0;
         c.inst_node_ptr.clear();
         c.inst_dims.clear();
+        c.shell_layered = false;
+        c.d_shell_abd.release();
+        c.d_shell_msec.release();
         c.d_xyz.upload(c.xyz, c.stream);
         c.d_conn.upload(c.conn, c.stream);
         c.d_E.upload(c.E, c.stream);
@@ -690,6 +693,105 @@ int asend_set_modulus(asend_ctx* ctx, const double* E) {
 int asend_orthotropic_cmat(const double* props, double* C_out) {
     if (!props || !C_out) return ASEND_EINVAL;
     return orthotropic_cmat(props, C_out) ? ASEND_OK : ASEND_EINVAL;
+}
+
+// Layered shell section: layers bottom to top from z = -t (1 + z_offset) / 2;
+// each layer's plane-stress stiffness Q = S^-1 (S from E1, E2, nu12, G12) is
+// turned to the section axes as Qbar = Ts Q Te^-1 with the stress and strain
+// rotations of its angle, and integrated through its thickness into A (z^0),
+// B (z^1) and D (z^2); the section mass integrates the layer density the
+// same way (translation 1, coupling +-z, rotation z^2).
+static bool shell_section(int n_lay, const double* L, double z_offset, double* C, double* M) {
+    std::fill(C, C + 81, 0.0);
+    std::fill(M, M + 36, 0.0);
+    double tot = 0.0;
+    for (int k = 0; k < n_lay; ++k) {
+        const double* p = L + 7 * k;
+        for (int i = 0; i < 7; ++i)
+            if (!std::isfinite(p[i])) return false;
+        if (!(p[0] > 0 && p[1] > 0 && p[3] > 0 && p[5] > 0 && p[4] >= 0)) return false;
+        tot += p[5];
+    }
+    double z0 = -0.5 * tot * (1.0 + z_offset);
+    for (int k = 0; k < n_lay; ++k) {
+        const double* p = L + 7 * k;
+        const double E1 = p[0], E2 = p[1], n12 = p[2], G12 = p[3], rho = p[4], th = p[5];
+        const double z1 = z0 + th;
+        // Q = inverse of [[1/E1, -n12/E1, 0], [-n12/E1, 1/E2, 0], [0, 0, 1/G12]]
+        const double det = 1.0 / (E1 * E2) - n12 * n12 / (E1 * E1);
+        if (!(det > 0.0)) return false;
+        double Q[3][3] = {{1.0 / E2 / det, n12 / E1 / det, 0.0}, {n12 / E1 / det, 1.0 / E1 / det, 0.0},
+                          {0.0, 0.0, G12}};
+        const double a = p[6] * (M_PI / 180.0), c = std::cos(a), s = std::sin(a);
+        const double Ts[3][3] = {{c * c, s * s, -2.0 * c * s}, {s * s, c * c, 2.0 * c * s}, {c * s, -s * c, c * c - s * s}};
+        double Te[3][3] = {{c * c, s * s, -c * s}, {s * s, c * c, c * s}, {2.0 * c * s, -2.0 * s * c, c * c - s * s}};
+        // Te^-1 by the adjugate
+        double Ti[3][3];
+        const double dT = Te[0][0] * (Te[1][1] * Te[2][2] - Te[1][2] * Te[2][1]) -
+                          Te[0][1] * (Te[1][0] * Te[2][2] - Te[1][2] * Te[2][0]) +
+                          Te[0][2] * (Te[1][0] * Te[2][1] - Te[1][1] * Te[2][0]);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                const int i1 = (j + 1) % 3, i2 = (j + 2) % 3, j1 = (i + 1) % 3, j2 = (i + 2) % 3;
+                Ti[i][j] = (Te[i1][j1] * Te[i2][j2] - Te[i1][j2] * Te[i2][j1]) / dT;
+            }
+        double Qb[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double acc = 0.0;
+                for (int l = 0; l < 3; ++l)
+                    for (int m = 0; m < 3; ++m) acc += Ts[i][l] * Q[l][m] * Ti[m][j];
+                Qb[i][j] = acc;
+            }
+        const double fa = z1 - z0, fb = 0.5 * (z1 * z1 - z0 * z0), fd = (z1 * z1 * z1 - z0 * z0 * z0) / 3.0;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                C[9 * i + j] += fa * Qb[i][j];
+                C[9 * i + j + 3] += fb * Qb[i][j];
+                C[9 * (i + 3) + j] += fb * Qb[i][j];
+                C[9 * (i + 3) + j + 3] += fd * Qb[i][j];
+            }
+        for (int i = 0; i < 3; ++i) {
+            M[7 * i] += rho * fa;
+            M[7 * (i + 3)] += rho * fd;
+        }
+        // translation-rotation coupling: u with theta_y (+), v with theta_x (-)
+        M[0 * 6 + 4] += rho * fb;
+        M[4 * 6 + 0] += rho * fb;
+        M[1 * 6 + 3] -= rho * fb;
+        M[3 * 6 + 1] -= rho * fb;
+        z0 = z1;
+    }
+    C[60] = C[70] = C[80] = C[20];
+    return true;
+}
+
+int asend_shell_section(int32_t n_layers, const double* layers, double z_offset, double* abd_out,
+                        double* msec_out) {
+    if (n_layers < 1 || !layers || !abd_out || !msec_out || !std::isfinite(z_offset)) return ASEND_EINVAL;
+    return shell_section(n_layers, layers, z_offset, abd_out, msec_out) ? ASEND_OK : ASEND_EINVAL;
+}
+
+int asend_set_shell_sections(asend_ctx* ctx, const double* abd, const double* msec) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.type == 41, "layered sections take shell4 meshes");
+        if (!abd) {
+            c.shell_layered = false;
+            c.d_shell_abd.release();
+            c.d_shell_msec.release();
+        } else {
+            require(msec != nullptr, "layered sections need their section mass");
+            const size_t n = (size_t)c.n_el;
+            for (size_t i = 0; i < n * 81; ++i) require(std::isfinite(abd[i]), "non-finite ABD entry");
+            for (size_t i = 0; i < n * 36; ++i) require(std::isfinite(msec[i]), "non-finite section mass entry");
+            c.d_shell_abd.upload(abd, n * 81, c.stream);
+            c.d_shell_msec.upload(msec, n * 36, c.stream);
+            ASEND_CUDA(cudaStreamSynchronize(c.stream));
+            c.shell_layered = true;
+        }
+        c.assembled = c.solved = false;
+        return ASEND_OK;
+    });
 }
 
 int asend_set_orthotropic(asend_ctx* ctx, const double* props) {
@@ -900,6 +1002,7 @@ int asend_add_surface_pressure(asend_ctx* ctx, int32_t rhs, int32_t elem_set, co
 // node a's first translational DOF; cent the mean of the node coordinates.
 static int element_node_weights(const Ctx& c, int e, double* w, int64_t* dof, double* cent) {
     if (c.type == 41) {
+        if (c.shell_layered) throw InputError("body loads on layered shell sections are not built");
         double x[4][3];
         for (int a = 0; a < 4; ++a) {
             const int pn = c.conn[(size_t)e * 8 + 2 * a];  // translational pseudo-node 2 n
@@ -1304,7 +1407,7 @@ int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double*
         // the per-element modulus gradient scales an isotropic element; with
         // orthotropic constants the gradient goes through the strain pairs
         // (asend_material_dv_gradient)
-        const bool iso = c.ortho.empty();
+        const bool iso = c.ortho.empty() && !c.shell_layered;
         require(iso || !dLdE_out,
                 "per-element modulus gradients need isotropic elements; use asend_material_dv_gradient");
         const size_t n = c.n_dof;

@@ -173,6 +173,10 @@ struct Ctx {
     DArr<int32_t> d_conn;
     DArr<int32_t> d_shell_conn;  // shell4: 4 physical nodes per element
     DArr<double> d_shell_xyz;    // shell4: physical node coordinates
+    // shell4 layered sections: per-element ABD [n_el][81] and section mass
+    // [n_el][36] replacing the isotropic E, nu, t section
+    bool shell_layered = false;
+    DArr<double> d_shell_abd, d_shell_msec;
     bool pattern_ready = false, assembled = false, dynamic = false;
     bool modal = false;  // K and M assembled apart (c_M = 0) for the frequency job
     double dt = 0, beta = 0.25, gamma = 0.5, cM = 0;

@@ -1,5 +1,6 @@
 // k_shell.cu -- shell4 (type 41) element kernels: stiffness with condensed
-// internal DOF, consistent section mass, coloured scatter, adjoint contraction.
+// internal DOF, consistent section mass, coloured scatter, adjoint contraction;
+// isotropic E, nu, t sections or per-element layered ABD and section mass.
 //
 // Reference formulation (solverSrc/asend_run_job/src/):
 //   element_meth.rs:326-370      type 41: 4 nodes x 6 DOF, 8 internal DOF, 2x2 points
@@ -46,7 +47,14 @@ struct ShellSmem {
     double Kii[8][8];
     double X[8][24];              // K_ii^-1 K_in
     double K24[24][24];
-    double msec[6];
+    double msec[36];              // section mass 6 x 6 (u v w thx thy thz)
+};
+
+// Layered sections (per-element ABD [81] and section mass [36]); null
+// pointers: the isotropic E, nu, t section.
+struct ShellSec {
+    const double* abd;
+    const double* msec;
 };
 
 __device__ void shape(double s, double t, double* n, double* ds, double* dt) {
@@ -66,10 +74,13 @@ __device__ void shape(double s, double t, double* n, double* ds, double* dt) {
 // e in shared memory.  All threads of the CTA must call it.
 __device__ void shell_element(ShellSmem& S, int e, const int32_t* __restrict__ conn4, const double* __restrict__ xyz,
                               const double* __restrict__ Ev, const double* __restrict__ nuv,
-                              const double* __restrict__ rhov, const double* __restrict__ thkv) {
+                              const double* __restrict__ rhov, const double* __restrict__ thkv, ShellSec sec) {
     const int t = threadIdx.x;
     if (t < 12) S.xyz[t / 3][t % 3] = xyz[3 * (size_t)conn4[4 * (size_t)e + t / 3] + t % 3];
-    if (t == 12) {
+    if (sec.abd) {
+        for (int q = t; q < 81; q += kST) S.C[q] = sec.abd[(size_t)e * 81 + q];
+        for (int q = t; q < 36; q += kST) S.msec[q] = rhov ? sec.msec[(size_t)e * 36 + q] : 0.0;
+    } else if (t == 12) {
         const double E = Ev[e], nu = nuv[e], h = thkv[e];
         const double G = E / (2.0 * (1.0 + nu)), q = E / (1.0 - nu * nu);
         const double Q[9] = {q, nu * q, 0, nu * q, q, 0, 0, 0, G};
@@ -82,8 +93,9 @@ __device__ void shell_element(ShellSmem& S, int e, const int32_t* __restrict__ c
             }
         S.C[60] = S.C[70] = S.C[80] = S.C[20];
         const double r = rhov ? rhov[e] : 0.0;
-        S.msec[0] = S.msec[1] = S.msec[2] = r * h;
-        S.msec[3] = S.msec[4] = S.msec[5] = r * d;
+        for (int i = 0; i < 36; ++i) S.msec[i] = 0.0;
+        S.msec[0] = S.msec[7] = S.msec[14] = r * h;
+        S.msec[21] = S.msec[28] = S.msec[35] = r * d;
     }
     __syncthreads();
     if (t < 5) {  // points 0..3 and the centroid
@@ -203,22 +215,24 @@ __device__ void shell_element(ShellSmem& S, int e, const int32_t* __restrict__ c
     __syncthreads();
 }
 
-// mass entry between node DOF (a, ca) and (b, cb) (zero unless ca == cb)
+// mass entry between node DOF (a, ca) and (b, cb): the section mass couples
+// the components, the shape functions the nodes
 __device__ __forceinline__ double mass_entry(const ShellSmem& S, int a, int ca, int b, int cb) {
-    if (ca != cb) return 0.0;
+    const double m = S.msec[6 * ca + cb];
+    if (m == 0.0) return 0.0;
     double acc = 0.0;
     for (int ip = 0; ip < 4; ++ip) acc += S.n[ip][a] * S.n[ip][b] * S.det[ip];
-    return S.msec[ca] * acc;
+    return m * acc;
 }
 
 __global__ void __launch_bounds__(kST)
 k_shell_assemble(const int32_t* __restrict__ elems, const int32_t* __restrict__ conn4, const double* __restrict__ xyz,
                  const double* __restrict__ E, const double* __restrict__ nu, const double* __restrict__ rho,
                  const double* __restrict__ thk, const int32_t* __restrict__ slot_map, double* __restrict__ vals,
-                 double* __restrict__ mvals, double cM) {
+                 double* __restrict__ mvals, double cM, ShellSec sec) {
     __shared__ ShellSmem S;
     const int e = elems[blockIdx.x];
-    shell_element(S, e, conn4, xyz, E, nu, mvals ? rho : nullptr, thk);
+    shell_element(S, e, conn4, xyz, E, nu, mvals ? rho : nullptr, thk, sec);
     const int pr = threadIdx.x;  // pseudo-node pair (pa, pb)
     const int pa = pr >> 3, pb = pr & 7;
     const int32_t slot = slot_map[(size_t)e * 64 + pr];
@@ -248,7 +262,7 @@ k_shell_adjoint(const int32_t* __restrict__ conn4, const double* __restrict__ xy
     __shared__ ShellSmem S;
     __shared__ double red[kST];
     const int e = blockIdx.x;
-    shell_element(S, e, conn4, xyz, E, nu, nullptr, thk);
+    shell_element(S, e, conn4, xyz, E, nu, nullptr, thk, ShellSec{nullptr, nullptr});
     double acc = 0.0;
     for (int q = threadIdx.x; q < 24 * 24; q += kST) {
         const int r = q / 24, c = q % 24;
@@ -272,15 +286,19 @@ k_shell_adjoint(const int32_t* __restrict__ conn4, const double* __restrict__ xy
 __global__ void __launch_bounds__(kST)
 k_shell_export(int e0, const int32_t* __restrict__ conn4, const double* __restrict__ xyz, const double* __restrict__ E,
                const double* __restrict__ nu, const double* __restrict__ rho, const double* __restrict__ thk,
-               double* __restrict__ ke, double* __restrict__ me) {
+               double* __restrict__ ke, double* __restrict__ me, ShellSec sec) {
     __shared__ ShellSmem S;
     const int e = e0 + blockIdx.x;
-    shell_element(S, e, conn4, xyz, E, nu, rho, thk);
+    shell_element(S, e, conn4, xyz, E, nu, rho, thk, sec);
     for (int q = threadIdx.x; q < 576; q += kST) {
         const int r = q / 24, c = q % 24;
         ke[(size_t)blockIdx.x * 576 + q] = S.K24[r][c];
         if (me) me[(size_t)blockIdx.x * 576 + q] = mass_entry(S, r / 6, r % 6, c / 6, c % 6);
     }
+}
+
+ShellSec sections_of(const Ctx& c) {
+    return c.shell_layered ? ShellSec{c.d_shell_abd.p, c.d_shell_msec.p} : ShellSec{nullptr, nullptr};
 }
 
 }  // namespace
@@ -292,13 +310,15 @@ void shell_assemble(Ctx& c, double* vals, double* mvals) {
         if (n == 0) continue;
         k_shell_assemble<<<n, kST, 0, c.stream>>>(c.d_colour_elems.p + c.colour_ptr[k], c.d_shell_conn.p,
                                                  c.d_shell_xyz.p, c.d_E.p, c.d_nu.p, c.d_rho.p, c.d_thk.p,
-                                                 c.d_slot_map.p, vals, mvals, c.cM);
+                                                 c.d_slot_map.p, vals, mvals, c.cM, sections_of(c));
         ASEND_CUDA(cudaGetLastError());
         ++c.launches;
     }
 }
 
 void shell_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate) {
+    if (c.shell_layered)
+        throw InputError("layered shell sections have no per-element modulus gradient (K is not proportional to E)");
     k_shell_adjoint<<<c.n_el, kST, 0, c.stream>>>(c.d_shell_conn.p, c.d_shell_xyz.p, c.d_E.p, c.d_nu.p, c.d_thk.p,
                                                  d_u, d_lam, d_g, accumulate ? 1 : 0);
     ASEND_CUDA(cudaGetLastError());
@@ -310,7 +330,7 @@ void shell_element_matrices(Ctx& c, int e0, int n, double* ke_host, double* me_h
     ke.alloc((size_t)n * 576);
     if (me_host) me.alloc((size_t)n * 576);
     k_shell_export<<<n, kST, 0, c.stream>>>(e0, c.d_shell_conn.p, c.d_shell_xyz.p, c.d_E.p, c.d_nu.p, c.d_rho.p,
-                                            c.d_thk.p, ke.p, me_host ? me.p : nullptr);
+                                            c.d_thk.p, ke.p, me_host ? me.p : nullptr, sections_of(c));
     ++c.launches;
     ASEND_CUDA(cudaGetLastError());
     ASEND_CUDA(cudaMemcpyAsync(ke_host, ke.p, sizeof(double) * n * 576, cudaMemcpyDeviceToHost, c.stream));

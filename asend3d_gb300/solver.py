@@ -55,6 +55,9 @@ class Problem:
     # damping of Newmark runs: (rayleigh_cm, rayleigh_ck, material damping [n_el][36] or None)
     damping: tuple | None = None
     lump_mass: bool = False  # row-sum lumped mass in Newmark runs
+    # layered shell4 sections: [(element indices, layers [n, 7] = E1 E2 nu12
+    # G12 density thickness angle[deg], z offset)]; other elements keep E, nu, t
+    shell_sections: list | None = None
 
     def add_node_set(self, name, nodes):
         self.node_sets[name] = np.asarray(nodes, dtype=np.int32)
@@ -158,6 +161,8 @@ class GpuSolver:
                         "set_damping")
         if p.lump_mass:
             self._check(self.lib.asend_set_lumped_mass(self.ctx, 1), "set_lumped_mass")
+        if p.shell_sections:
+            self._set_shell_sections(p, E, nu, rho, thk)
         if m.elem_type in (8, 81) and m.conn.shape[0] == m.nx * m.ny * m.nz:
             self._check(self.lib.asend_set_block_structure(self.ctx, m.nx, m.ny, m.nz), "set_block_structure")
         for name, nodes in p.node_sets.items():
@@ -299,6 +304,31 @@ class GpuSolver:
             _, set_name, comp, coef = objective
             rc = self.lib.asend_set_objective(self.ctx, _lib.OBJ_DISPLACEMENT, self.set_ids[set_name], comp, coef)
         self._check(rc, "set_objective")
+
+    def shell_section(self, layers, z_offset=0.0):
+        """(ABD [81], section mass [36]) of a layered shell section; layers
+        [n, 7] = E1, E2, nu12, G12, density, thickness, angle [deg]."""
+        lay = np.ascontiguousarray(layers, dtype=np.float64).reshape(-1, 7)
+        abd, ms = np.zeros(81), np.zeros(36)
+        rc = self.lib.asend_shell_section(len(lay), _ptr(lay, C.c_double), float(z_offset), _ptr(abd, C.c_double),
+                                          _ptr(ms, C.c_double))
+        if rc != 0:
+            raise AsendError("asend_shell_section: invalid layers")
+        return abd, ms
+
+    def _set_shell_sections(self, p, E, nu, rho, thk):
+        ne = p.mesh.n_elems
+        abd, ms = np.zeros((ne, 81)), np.zeros((ne, 36))
+        r = np.zeros(ne) if rho is None else rho
+        for e in range(ne):  # elements outside the sections: one isotropic layer
+            abd[e], ms[e] = self.shell_section([[E[e], E[e], nu[e], E[e] / (2 * (1 + nu[e])), r[e], thk[e], 0.0]])
+        for els, layers, zoff in p.shell_sections:
+            a, mm = self.shell_section(layers, zoff)
+            abd[np.asarray(els)] = a
+            ms[np.asarray(els)] = mm
+        self._sec = (np.ascontiguousarray(abd), np.ascontiguousarray(ms))
+        self._check(self.lib.asend_set_shell_sections(self.ctx, _ptr(self._sec[0], C.c_double),
+                                                      _ptr(self._sec[1], C.c_double)), "set_shell_sections")
 
     def element_fields(self, rhs=0):
         """Centroid strain and stress [n_el, 6] of load case rhs of the last

@@ -322,6 +322,24 @@ int asend_orthotropic_cmat(const double* props, double* C_out);
  * operator gains c_D D with c_D = dt gamma c_M (element_equations.rs:995-1005)
  * and the step residual D v.  rayleigh_ck and D take hex8 / tet4 meshes. */
 int asend_set_damping(asend_ctx* ctx, double rayleigh_cm, double rayleigh_ck, const double* D);
+/* Layered shell4 sections (the reference's shell section 'layup': layers of
+ * orthotropic material, thickness and angle, and zOffset).
+ *   asend_shell_section (host only): the 9 x 9 ABD of the section
+ *     (get_layer_thk_z element_properties.rs:75-136, get_layer_q :138-222,
+ *     transform_q :581-646, get_abd :766-876: A, B, D from the rotated
+ *     plane-stress layer stiffnesses, transverse shear and drilling = A66)
+ *     and its 6 x 6 section mass (get_shell_mass :1354-1408).  Layer k:
+ *     layers[7k..7k+6] = E1, E2, nu12, G12, density, thickness, angle [deg];
+ *     z_offset -1 / 0 / 1 puts the reference plane on the lower surface /
+ *     mid-plane / upper surface.
+ *   asend_set_shell_sections: per-element abd[n_el][81] and msec[n_el][36]
+ *     replacing the isotropic E, nu, t section of a shell4 mesh (NULL abd:
+ *     back to E, nu, t).  Layered sections have no per-element modulus
+ *     gradient (asend_adjoint_gradient takes dLdE_out = NULL) and no body
+ *     loads. */
+int asend_shell_section(int32_t n_layers, const double* layers, double z_offset, double* abd_out,
+                        double* msec_out);
+int asend_set_shell_sections(asend_ctx* ctx, const double* abd, const double* msec);
 /* Row-sum lumped mass in Newmark assemblies (the reference's 'lumpMass: yes',
  * element_equations.rs:950-971): the mass is diag(row sums of M). */
 int asend_set_lumped_mass(asend_ctx* ctx, int32_t on);

@@ -26,6 +26,7 @@ constexpr double kPi = 3.14159265358979323846;
 constexpr double kRTet1 = 0.1381966011250071;  // constants.rs:10 (R_TET1)
 constexpr double kRTet2 = 0.585410196624929;   // constants.rs:11 (R_TET2)
 constexpr double kR1O24 = 0.041666666666666664; // constants.rs:7 (R_1O24)
+constexpr double kRPi0180 = 0.017453292519943295;  // constants.rs:9 (R_PI_0180)
 
 // ---------------------------------------------------------------------------
 // Element type tables: element_meth.rs:74-448 (initialize_type)
@@ -503,18 +504,98 @@ void shell_bmat(const double* n, const double* dndx /* [10][3] */, double* B /* 
 // QR), and the consistent mass (get_rum_dfd0 :514-581 with the section mass of
 // get_shell_mass_dfd0, element_properties.rs:1354-1408: rho t on the
 // translations, rho t^3/12 on the rotations) over the 24 node DOF.
+// Layered shell section (get_layer_thk_z_dfd0 element_properties.rs:75-136,
+// get_layer_q_dfd0 :138-222, transform_q_dfd0 :581-646, get_abd_dfd0
+// :766-876, get_shell_mass_dfd0 :1354-1408).  Layer k: props[7k..7k+6] =
+// E1, E2, nu12, G12, density, thickness, angle (degrees).  z_offset = 1 puts
+// the reference plane on the upper surface, -1 on the lower one.  Outputs
+// the 9x9 ABD (shear and drilling entries = A66) and the 6x6 section mass.
+void shell_section(int n_lay, const double* props, double z_offset, double* C, double* msec) {
+    for (int i = 0; i < 81; ++i) C[i] = 0.0;
+    for (int i = 0; i < 36; ++i) msec[i] = 0.0;
+    double tot = 0.0;
+    for (int k = 0; k < n_lay; ++k) tot += props[7 * k + 5];
+    double zc = -0.5 * tot * (1.0 + z_offset);
+    for (int k = 0; k < n_lay; ++k) {
+        const double* p = props + 7 * k;
+        const double th = p[5], zmid = 0.5 * (zc + zc + th);
+        zc += th;
+        const double zmin = zmid - 0.5 * th, zmax = zmid + 0.5 * th;
+        // layer Q: inverse of the plane-stress compliance
+        double S[9] = {1.0 / p[0], -p[2] / p[0], 0.0, -p[2] / p[0], 1.0 / p[1], 0.0, 0.0, 0.0, 1.0 / p[3]}, Q[9];
+        det_inv(Q, S, 3);
+        // rotation to the section axes: Qbar = Ts Q Te^-1
+        const double ang = kRPi0180 * p[6];
+        const double c = std::cos(ang), s = std::sin(ang);
+        const double a11 = c, a21 = s, a12 = -s, a22 = c;
+        const double Ts[9] = {a11 * a11, a12 * a12, 2.0 * a11 * a12, a21 * a21, a22 * a22, 2.0 * a22 * a21,
+                              a11 * a21, a12 * a22, a11 * a22 + a12 * a21};
+        double Te[9], Tei[9], QT[9], Qb[9];
+        std::copy(Ts, Ts + 9, Te);
+        Te[2] *= 0.5;
+        Te[5] *= 0.5;
+        Te[6] *= 2.0;
+        Te[7] *= 2.0;
+        det_inv(Tei, Te, 3);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double a = 0.0;
+                for (int l = 0; l < 3; ++l) a += Q[3 * i + l] * Tei[3 * l + j];
+                QT[3 * i + j] = a;
+            }
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double a = 0.0;
+                for (int l = 0; l < 3; ++l) a += Ts[3 * i + l] * QT[3 * l + j];
+                Qb[3 * i + j] = a;
+            }
+        const double fa = zmax - zmin, fb = 0.5 * (zmax * zmax - zmin * zmin),
+                     fd = (zmax * zmax * zmax - zmin * zmin * zmin) / 3.0;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                C[9 * i + j] += fa * Qb[3 * i + j];
+                C[9 * i + j + 3] += fb * Qb[3 * i + j];
+                C[9 * (i + 3) + j + 3] += fd * Qb[3 * i + j];
+            }
+        const double rho = p[4];
+        msec[0] += rho * fa;
+        msec[7] += rho * fa;
+        msec[14] += rho * fa;
+        msec[4] += rho * fb;
+        msec[24] += rho * fb;
+        msec[9] -= rho * fb;
+        msec[19] -= rho * fb;
+        msec[21] += rho * fd;
+        msec[28] += rho * fd;
+        msec[35] += rho * fd;
+    }
+    // the lower triangle mirrors the upper one; shear and drilling = A66
+    for (int i = 1; i < 6; ++i)
+        for (int j = 0; j < i; ++j) C[9 * i + j] = C[9 * j + i];
+    C[60] = C[70] = C[80] = C[20];
+}
+
+void shell_km_sec(const double* xyz, const double* C, const double* msec, double* ke, double* me);
+
 void shell_km(const double* xyz, double E, double nu, double rho, double t, double* ke, double* me) {
-    constexpr int tot = 32, nd = 24;
-    double C[81];
+    double C[81], msec[36] = {0};
     shell_abd(E, nu, t, C);
+    for (int c = 0; c < 3; ++c) {
+        msec[7 * c] = rho * t;
+        msec[7 * (c + 3)] = rho * t * t * t / 12.0;
+    }
+    shell_km_sec(xyz, C, msec, ke, me);
+}
+
+// Shell element matrices from a section: ABD C[81] and section mass msec[36].
+void shell_km_sec(const double* xyz, const double* C, const double* msec, double* ke, double* me) {
+    constexpr int tot = 32, nd = 24;
     std::vector<double> K(tot * tot, 0.0), B(9 * tot), CB(9 * tot);
     if (me) for (int i = 0; i < nd * nd; ++i) me[i] = 0.0;
     double n0[10], ds0[10], dt0[10], jinv0[9];
     shell_shape(0.0, 0.0, n0, ds0, dt0);
     shell_jac(xyz, ds0, dt0, jinv0);  // centroid Jacobian for the non-nodal functions
     const double sp[4][2] = {{-kR1ORt3, -kR1ORt3}, {kR1ORt3, -kR1ORt3}, {-kR1ORt3, kR1ORt3}, {kR1ORt3, kR1ORt3}};
-    const double msec[6] = {rho * t, rho * t, rho * t, rho * t * t * t / 12.0, rho * t * t * t / 12.0,
-                            rho * t * t * t / 12.0};
     for (int ip = 0; ip < 4; ++ip) {
         double n[10], ds[10], dt[10], jinv[9], dndx[30];
         shell_shape(sp[ip][0], sp[ip][1], n, ds, dt);
@@ -539,7 +620,9 @@ void shell_km(const double* xyz, double E, double nu, double rho, double t, doub
         if (me)
             for (int a = 0; a < 4; ++a)
                 for (int b = 0; b < 4; ++b)
-                    for (int c = 0; c < 6; ++c) me[(6 * a + c) * nd + 6 * b + c] += msec[c] * n[a] * n[b] * detj;
+                    for (int c = 0; c < 6; ++c)
+                        for (int d = 0; d < 6; ++d)
+                            me[(6 * a + c) * nd + 6 * b + d] += msec[6 * c + d] * n[a] * n[b] * detj;
     }
     // static condensation of the internal DOF
     double Kii[64];
@@ -618,6 +701,8 @@ struct orc_model {
     // two pseudo-nodes per physical node)
     bool shell = false;
     int n_phys = 0;
+    // layered shell sections per element: ABD [n_el][81], section mass [n_el][36]
+    std::vector<double> shell_abd81, shell_msec36;
     std::vector<double> phys_xyz;
     std::vector<int32_t> conn4;
 };
@@ -639,7 +724,10 @@ void elem_km(const orc_model* m, int e, double* ke, double* me) {
         double xyz[12];
         for (int a = 0; a < 4; ++a)
             for (int j = 0; j < 3; ++j) xyz[3 * a + j] = m->phys_xyz[3 * (size_t)m->conn4[(size_t)e * 4 + a] + j];
-        shell_km(xyz, m->E[e], m->nu[e], m->rho[e], m->thk[e], ke, me);
+        if (!m->shell_abd81.empty())
+            shell_km_sec(xyz, &m->shell_abd81[(size_t)e * 81], &m->shell_msec36[(size_t)e * 36], ke, me);
+        else
+            shell_km(xyz, m->E[e], m->nu[e], m->rho[e], m->thk[e], ke, me);
         return;
     }
     double xyz[30], C[36];
@@ -1341,6 +1429,26 @@ int orc_set_cmat(orc_model* m, const double* C) {
     return 0;
 }
 
+int orc_shell_section(int32_t n_layers, const double* props, double z_offset, double* abd, double* msec) {
+    if (n_layers < 1 || !props || !abd || !msec) return -1;
+    shell_section(n_layers, props, z_offset, abd, msec);
+    return 0;
+}
+
+int orc_set_shell_sections(orc_model* m, const double* abd, const double* msec) {
+    if (!m->shell) return -1;
+    if (!abd) {
+        m->shell_abd81.clear();
+        m->shell_msec36.clear();
+    } else {
+        if (!msec) return -1;
+        m->shell_abd81.assign(abd, abd + (size_t)m->n_el * 81);
+        m->shell_msec36.assign(msec, msec + (size_t)m->n_el * 36);
+    }
+    m->assembled = false;
+    return 0;
+}
+
 int orc_set_damping(orc_model* m, double ray_cm, double ray_ck, const double* D) {
     m->ray_cm = ray_cm;
     m->ray_ck = ray_ck;
@@ -1527,6 +1635,7 @@ int orc_surface_load(const orc_model* m, int32_t n_set, const int32_t* elem_set,
 // load_meth.rs:41-51), the element's density.
 int orc_body_load(const orc_model* m, int32_t n_set, const int32_t* elem_set, int32_t kind, const double* vec,
                   double omega, const double* center, const double* axis, double* f) {
+    if (!m->shell_abd81.empty()) return -2;  // layered sections: not restated
     const int nn = m->ti.nn, tot = 3 * nn;
     std::vector<double> ke(tot * tot), me(tot * tot);
     double ax[3] = {0, 0, 0};
@@ -1671,6 +1780,7 @@ int orc_adjoint_modulus_gradient(orc_model* m, const double* u, const double* dL
                                  int32_t precond, int32_t stop_rule, double tol, int32_t max_it,
                                  orc_stats* st) {
     if (!m->assembled) return -1;
+    if (!m->shell_abd81.empty()) return -2;  // layered sections are not proportional to E
     const int n = m->n_dof;
     std::vector<double> lam(n, 0.0);
     int status = 0;

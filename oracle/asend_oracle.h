@@ -146,6 +146,13 @@ int orc_adjoint_strain_pairs(const orc_model* m, const double* u, const double* 
 
 int orc_reorder_nodes(const orc_model* m, int32_t block_dim, int32_t* order_out);
 
+/* Layered shell section: layer k props[7k..] = E1, E2, nu12, G12, density,
+ * thickness, angle [deg]; z_offset -1 / 0 / 1 = reference plane on the lower
+ * surface / mid-plane / upper surface.  abd[81] (9x9), msec[36] (6x6). */
+int orc_shell_section(int32_t n_layers, const double* props, double z_offset, double* abd, double* msec);
+/* Per-element sections of a shell4 model (NULL abd: back to E, nu, t). */
+int orc_set_shell_sections(orc_model* m, const double* abd, const double* msec);
+
 /* Element-category objective term at the element centroids (category 0
  * stress, 1 strain, 2 strainEnergy; component 1-6 for 0/1; optr 0 powerNorm,
  * 1 ks, 2 volumeIntegral, 3 volumeAverage).  n_tgt 0, 1 or n_set targets.

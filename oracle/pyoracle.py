@@ -75,6 +75,8 @@ def load():
             "orc_adjoint_strain_pairs": (C.c_int, [C.c_void_p, P_d, P_d, P_d]),
             "orc_newmark_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double, P_d, P_d,
                                               C.c_int32, P_i, P_d, P_d, P_d]),
+            "orc_shell_section": (C.c_int, [C.c_int32, P_d, C.c_double, P_d, P_d]),
+            "orc_set_shell_sections": (C.c_int, [C.c_void_p, P_d, P_d]),
             "orc_element_objective": (C.c_int, [C.c_void_p, P_d, C.c_int32, P_i, C.c_int32, C.c_int32, C.c_int32,
                                                 C.c_double, C.c_double, C.c_int32, P_d, P_d, P_d, P_d, P_d]),
         }
@@ -145,6 +147,22 @@ class Oracle:
             self.lib.orc_set_damping(self.m, float(cm), float(ck), None if self._dmat is None else _p(self._dmat))
         if getattr(problem, "lump_mass", False):
             self.lib.orc_set_lumped_mass(self.m, 1)
+        secs = getattr(problem, "shell_sections", None)
+        if secs:
+            # layered sections: (element indices, layer table [n, 7], z offset);
+            # other elements keep their single isotropic layer
+            ne = m.n_elems
+            abd, ms = np.zeros((ne, 81)), np.zeros((ne, 36))
+            for e in range(ne):
+                G = self._E[e] / (2.0 * (1.0 + self._nu[e]))
+                row = [self._E[e], self._E[e], self._nu[e], G, self._rho[e], self._thk[e], 0.0]
+                abd[e], ms[e] = self.shell_section([row], 0.0)
+            for els, props, zoff in secs:
+                a, mm = self.shell_section(props, zoff)
+                abd[np.asarray(els)] = a
+                ms[np.asarray(els)] = mm
+            self._abd, self._msec = np.ascontiguousarray(abd), np.ascontiguousarray(ms)
+            assert self.lib.orc_set_shell_sections(self.m, _p(self._abd), _p(self._msec)) == 0
         rc = self.lib.orc_assemble(self.m, 2 if modal else int(dynamic), dt, beta, gamma)
         if rc != 0:
             raise RuntimeError(f"orc_assemble failed ({rc})")
@@ -292,6 +310,14 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"orc_adjoint_strain_pairs failed ({rc})")
         return P
+
+    def shell_section(self, props, z_offset):
+        """Layered shell section: (ABD [81], section mass [36]) of layers
+        props [n, 7] = E1, E2, nu12, G12, density, thickness, angle [deg]."""
+        pr = np.ascontiguousarray(props, np.float64).reshape(-1, 7)
+        abd, ms = np.zeros(81), np.zeros(36)
+        assert self.lib.orc_shell_section(len(pr), _p(pr), float(z_offset), _p(abd), _p(ms)) == 0
+        return abd, ms
 
     ELEM_CATEGORIES = {"stress": 0, "strain": 1, "strainEnergy": 2}
     ELEM_OPERATORS = {"powerNorm": 0, "ks": 1, "volumeIntegral": 2, "volumeAverage": 3}
