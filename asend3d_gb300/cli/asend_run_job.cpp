@@ -150,10 +150,15 @@ std::vector<Command> read_job(const std::string& path) {
     return cmds;
 }
 
+struct Layer {
+    std::string material;
+    double thickness = 0.0, angle = 0.0;
+};
 struct Section {
     std::string type, material, elset;
-    std::vector<std::pair<std::string, double>> layers;  // (material, thickness)
+    std::vector<Layer> layers;
     double z_offset = 0.0;
+    std::vector<double> orientation;  // xDir, xyVec
 };
 struct Material {
     double density = 0.0;
@@ -170,6 +175,21 @@ struct Model {
     std::vector<Section> sections;
     std::map<std::string, Material> materials;
 };
+
+// Angle [deg] of a shell section's material x axis (orientation xDir,
+// xyVec) from the global x axis, for flat shells in a plane z = const whose
+// local z is +z (correct_orient, element_properties.rs:2052-2150).
+double shell_frame_angle(const Section& s) {
+    if (s.orientation.empty()) return 0.0;
+    const double* x = s.orientation.data();
+    const double* y = x + 3;
+    const double z[3] = {x[1] * y[2] - x[2] * y[1], x[2] * y[0] - x[0] * y[2], x[0] * y[1] - x[1] * y[0]};
+    const double nx = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    const double nz = std::sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
+    if (std::fabs(x[2]) > 1e-12 * nx || z[2] <= 0.0 || std::hypot(z[0], z[1]) > 1e-12 * nz)
+        throw Fail("shell orientations with the local z axis along +z only");
+    return std::atan2(x[1], x[0]) * 180.0 / M_PI;
+}
 
 int element_type(const std::string& t) {
     if (t == "brick8") return 8;
@@ -213,19 +233,24 @@ Model read_model(const std::string& path) {
             }
         } else if (h[0] == "sections") {
             if (h[1] == "type" && d.size() == 1) {
-                m.sections.push_back(Section{d[0], "", "", {}, 0.0});
+                m.sections.push_back(Section{d[0], "", "", {}, 0.0, {}});
             } else if (m.sections.empty()) {
                 continue;
             } else if (h[1] == "material" && d.size() == 1) {
                 m.sections.back().material = d[0];
             } else if (h[1] == "elementSet" && d.size() == 1) {
                 m.sections.back().elset = d[0];
+            } else if (h[1] == "orientation" && d.size() == 6) {
+                for (const auto& x : d) m.sections.back().orientation.push_back(num(x));
             } else if (h[1] == "layup") {
+                auto& lay = m.sections.back().layers;
                 if (h[2] == "zOffset" && d.size() == 1) m.sections.back().z_offset = num(d[0]);
                 else if (h[2] == "layers" && h[3] == "material" && d.size() == 1)
-                    m.sections.back().layers.push_back({d[0], 0.0});
-                else if (h[2] == "layers" && h[3] == "thickness" && d.size() == 1 && !m.sections.back().layers.empty())
-                    m.sections.back().layers.back().second = num(d[0]);
+                    lay.push_back(Layer{d[0], 0.0, 0.0});
+                else if (h[2] == "layers" && h[3] == "thickness" && d.size() == 1 && !lay.empty())
+                    lay.back().thickness = num(d[0]);
+                else if (h[2] == "layers" && h[3] == "angle" && d.size() == 1 && !lay.empty())
+                    lay.back().angle = num(d[0]);
             } else if ((h[1] == "beamProps" || h[1] == "potField" || h[1] == "dampField" || h[1] == "thermField") &&
                        !d.empty()) {
                 throw Fail("section " + h[1] + " is not on the GPU path");
@@ -472,15 +497,49 @@ struct Runner {
             for (int v : row) conn.push_back(nidx.at(v));
         std::vector<double> E(ne, NAN), nu(ne, NAN), rho(ne, NAN), thk(ne, NAN);
         std::vector<double> props((size_t)ne * 9, NAN), damp((size_t)ne * 36, 0.0);
-        bool ortho = false, damped = false;
+        std::vector<double> sec_abd((size_t)ne * 81, 0.0), sec_ms((size_t)ne * 36, 0.0);
+        std::vector<char> has_sec(ne, 0);
+        bool ortho = false, damped = false, layered = false;
         for (const Section& s : m.sections) {
             if (!m.elem_sets.count(s.elset)) throw Fail("section without a valid elementSet");
             std::string mat_name = s.material;
             double t = NAN;
             if (s.type == "shell") {
-                if (s.layers.size() != 1 || s.z_offset != 0.0) throw Fail("shell sections with one centred layer only");
-                mat_name = s.layers[0].first;
-                t = s.layers[0].second;
+                // layup: layers of (material, thickness, angle) about zOffset
+                // (element_properties.rs:75-222, :766-876)
+                if (s.layers.empty()) throw Fail("shell section without layers");
+                const double phi = shell_frame_angle(s);
+                std::vector<double> rows;
+                t = 0.0;
+                for (const Layer& l : s.layers) {
+                    const Material& lm = m.materials.at(l.material);
+                    if (lm.E.empty() || lm.nu.empty()) throw Fail("material " + l.material + " needs E and nu");
+                    if (!lm.damping.empty()) throw Fail("material damping takes solid sections");
+                    const double g12 = lm.G.empty() ? lm.E[0] / (2.0 * (1.0 + lm.nu[0])) : lm.G[0];
+                    const double r[7] = {lm.E[0], lm.E[1], lm.nu[0], g12, lm.density, l.thickness, l.angle + phi};
+                    rows.insert(rows.end(), r, r + 7);
+                    t += l.thickness;
+                }
+                const bool one_iso = s.layers.size() == 1 && s.z_offset == 0.0 && rows[0] == rows[1] &&
+                                     std::fabs(rows[3] - rows[0] / (2.0 * (1.0 + rows[2]))) <= 1e-9 * rows[3];
+                double abd[81], ms[36];
+                if (!one_iso) {
+                    check(asend_shell_section((int)s.layers.size(), rows.data(), s.z_offset, abd, ms), "shell_section");
+                    layered = true;
+                }
+                for (int lab : m.elem_sets.at(s.elset)) {
+                    const int e = eidx.at(lab);
+                    E[e] = rows[0];
+                    nu[e] = rows[2];
+                    rho[e] = rows[4];
+                    thk[e] = t;
+                    if (!one_iso) {
+                        std::copy(abd, abd + 81, sec_abd.begin() + (size_t)e * 81);
+                        std::copy(ms, ms + 36, sec_ms.begin() + (size_t)e * 36);
+                        has_sec[e] = 1;
+                    }
+                }
+                continue;
             } else if (s.type != "solid") {
                 throw Fail(s.type + " sections are not on the GPU path");
             }
@@ -522,6 +581,16 @@ struct Runner {
                              rho.data(), m.elem_type == 41 ? thk.data() : nullptr),
               "set_mesh");
         if (ortho) check(asend_set_orthotropic(ctx, props.data()), "set_orthotropic");
+        if (layered) {
+            // elements outside the layered sections keep one isotropic layer
+            for (int e = 0; e < ne; ++e) {
+                if (has_sec[e]) continue;
+                const double r[7] = {E[e], E[e], nu[e], E[e] / (2.0 * (1.0 + nu[e])), rho[e], thk[e], 0.0};
+                check(asend_shell_section(1, r, 0.0, &sec_abd[(size_t)e * 81], &sec_ms[(size_t)e * 36]),
+                      "shell_section");
+            }
+            check(asend_set_shell_sections(ctx, sec_abd.data(), sec_ms.data()), "set_shell_sections");
+        }
         if (damped) check(asend_set_damping(ctx, 0.0, 0.0, damp.data()), "set_damping");
         for (const auto& name : m.node_set_order) {
             std::vector<int32_t> v;

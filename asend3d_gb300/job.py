@@ -379,6 +379,7 @@ class JobRunner:
         props = np.full((ne, 9), np.nan)  # E1 E2 E3 nu12 nu13 nu23 G12 G13 G23
         damp = np.zeros((ne, 36))
         ortho = False
+        shell_secs = []
         for sec in m.sections:
             es = sec.get("elementSet")
             if es is None or es not in m.elem_sets:
@@ -388,11 +389,28 @@ class JobRunner:
                 mat = m.materials[sec["material"]]
                 t = np.nan
             elif sec["type"] == "shell":
-                if len(sec["layers"]) != 1 or sec.get("zOffset", 0.0) != 0.0:
-                    raise NotImplementedError("shell sections with one centred layer only")
-                lay = sec["layers"][0]
-                mat = m.materials[lay["material"]]
-                t = lay["thickness"]
+                # layup: layers of (material, thickness, angle) about zOffset
+                # (get_layer_thk_z / get_layer_q / get_abd, element_properties.rs:75-222, :766-876)
+                rows = []
+                for lay in sec["layers"]:
+                    lm = m.materials[lay["material"]]
+                    le, ln = lm.get("E", [np.nan] * 3), lm.get("nu", [np.nan] * 3)
+                    lg = lm.get("G", [le[0] / (2 * (1 + ln[0]))] * 3)
+                    if "damping" in lm:
+                        raise NotImplementedError("material damping takes solid sections")
+                    rows.append([le[0], le[1], ln[0], lg[0], lm.get("density", 0.0), lay["thickness"],
+                                 lay.get("angle", 0.0) + self._shell_frame_angle(sec)])
+                if not rows:
+                    raise ValueError(f"shell section without layers: {sec}")
+                mat = m.materials[sec["layers"][0]["material"]]
+                t = float(sum(r[5] for r in rows))
+                r0 = rows[0]
+                one_iso = (len(rows) == 1 and sec.get("zOffset", 0.0) == 0.0 and r0[0] == r0[1]
+                           and abs(r0[3] - r0[0] / (2 * (1 + r0[2]))) <= 1e-9 * abs(r0[3]))
+                if not one_iso:
+                    shell_secs.append((els, rows, sec.get("zOffset", 0.0)))
+                E[els], nu[els], rho[els], thk[els] = r0[0], r0[2], r0[4], t
+                continue
             else:
                 raise NotImplementedError(f"{sec['type']} sections are not on the GPU path")
             Ev, nv = mat.get("E", [np.nan] * 3), mat.get("nu", [np.nan] * 3)
@@ -413,6 +431,8 @@ class JobRunner:
         if np.isnan(E).any():
             raise ValueError("elements without a section")
         p = Problem(mesh, E, nu, rho, thickness=None if np.isnan(thk).all() else thk)
+        if shell_secs:
+            p.shell_sections = shell_secs
         if ortho:
             if m.elem_type not in (8, 4, 10):
                 raise NotImplementedError("orthotropic materials take hex8 / tet4 / tet10 meshes on the GPU path")
@@ -644,6 +664,21 @@ class JobRunner:
             self.state = {"u": np.zeros(shape), "v": np.zeros(shape), "a": np.zeros(shape), "time": 0.0}
         key = {"displacement": "u", "velocity": "v", "acceleration": "a"}[field]
         self.state[key] = (amp / np.abs(mode).max()) * mode
+
+    @staticmethod
+    def _shell_frame_angle(sec):
+        """Angle [deg] of the section's material x axis (orientation xDir,
+        xyVec; correct_orient element_properties.rs:2052-2150) from the
+        global x axis, for flat shells in a plane z = const whose local z is
+        +z; layer angles are measured from that axis."""
+        o = sec.get("orientation")
+        if o is None:
+            return 0.0
+        xd, xy = np.asarray(o[:3], float), np.asarray(o[3:], float)
+        zl = np.cross(xd, xy)
+        if abs(xd[2]) > 1e-12 * np.linalg.norm(xd) or zl[2] <= 0 or np.hypot(zl[0], zl[1]) > 1e-12 * np.linalg.norm(zl):
+            raise NotImplementedError("shell orientations with the local z axis along +z only")
+        return float(np.degrees(np.arctan2(xd[1], xd[0])))
 
     def _term_elements(self, t):
         """Element indices of an element-category term's set."""

@@ -227,3 +227,62 @@ def test_job_element_objective_gradient(gpu_lib, oracle_lib, tmp_path):
     np.testing.assert_allclose(got, vals, rtol=1e-9)
     g = np.array([float(ln.split(",")[1]) for ln in (tmp_path / "obj_grad.csv").read_text().splitlines()[1:]])
     assert np.linalg.norm(g - grads) <= 1e-7 * np.linalg.norm(grads)
+
+
+def write_twoply_job(d):
+    """The reference's compositePlate [+45 / -45] case as job files: one
+    2 x 2 shell4 element, xyMin fully fixed, xMinyMax fixed in x, F = 1 in x
+    on each xMax node."""
+    coords = [(-1.0, -1.0, 0.0), (1.0, -1.0, 0.0), (1.0, 1.0, 0.0), (-1.0, 1.0, 0.0)]
+    lines = ["nodes:"] + [f"- [{i + 1}, {x!r}, {y!r}, {z!r}]" for i, (x, y, z) in enumerate(coords)]
+    lines += ["elements:", "- type: shell4", "  connectivity:", "  - [1, 1, 2, 3, 4]"]
+    lines += ["sets:", "  node:", "    xyMin:", "    - 1", "    xMinyMax:", "    - 4", "    xMax:", "    - 2", "    - 3",
+              "  element:", "    all:", "    - 1"]
+    lines += ["sections:", "- type: shell", "  orientation: [1.0, 0.0, 0.0, 0.0, 1.0, 0.0]", "  layup:",
+              "    zOffset: 0.0", "    layers:",
+              "    - material: cf", "      thickness: 0.05", "      angle: 45.0",
+              "    - material: cf", "      thickness: 0.05", "      angle: -45.0",
+              "  elementSet: all", "materials:", "  cf:", "    density: 1000.0", "    elastic:",
+              "      E: [10000000.0, 1000000.0, 1000000.0]", "      nu: [0.0, 0.0, 0.0]",
+              "      G: [5000000.0, 5000000.0, 5000000.0]"]
+    (d / "model.yaml").write_text("\n".join(lines) + "\n")
+    cons = ["constraints:"]
+    for dof in range(1, 7):
+        cons += ["- type: displacement", "  terms:", "  - nodeSet: xyMin", f"    dof: {dof}", "    coef: 1.0",
+                 "  rhs: 0.0"]
+    cons += ["- type: displacement", "  terms:", "  - nodeSet: xMinyMax", "    dof: 1", "    coef: 1.0", "  rhs: 0.0"]
+    (d / "constraints.yaml").write_text("\n".join(cons) + "\n")
+    (d / "loads.yaml").write_text("loads:\n- type: nodalForce\n  nodeSet: xMax\n  load: [1.0, 0.0, 0.0, 0.0, 0.0, 0.0]\n")
+    job = ["jobCommands:", "- command: readModelInput", "  fileName: model.yaml",
+           "- command: readConstraints", "  fileName: constraints.yaml",
+           "- command: readLoads", "  fileName: loads.yaml",
+           "- command: solve", "  elastic: yes", "  dynamic: no", "  solverMethod: iterative",
+           "  convergenceTol: 1.0e-14", "  maxIterations: 20000",
+           "- command: writeNodeResults", f"  fileName: {d / 'nodes.csv'}", "  nodeSet: xMax",
+           "  fields:", "  - displacement"]
+    (d / "job.yaml").write_text("\n".join(job) + "\n")
+
+
+def test_job_layered_shell_known_answers(gpu_lib, tmp_path):
+    """A layered shell section through the Python runner and the C++ CLI:
+    the compositePlate [+45 / -45] known answers at the (1, 1) corner
+    (examples/testCases/compositePlate/notes.txt; 1e-8, ux 1e-5)."""
+    import subprocess
+
+    from asend3d_gb300 import build
+    build.build_cli()
+    for runner in ("python", "cli"):
+        d = tmp_path / runner
+        d.mkdir()
+        write_twoply_job(d)
+        if runner == "python":
+            J.JobRunner(d / "job.yaml").run()
+        else:
+            out = subprocess.run([str(build.CLI), str(d / "job.yaml")], capture_output=True, text=True)
+            assert out.returncode == 0, out.stderr
+        head, rows = read_csv(d / "nodes.csv")
+        corner = rows[rows[:, 0] == 3][0]
+        assert corner[1] == pytest.approx(4.651452282161358e-06, rel=1e-5), runner
+        assert corner[2] == pytest.approx(2.6514522821613584e-06, rel=1e-8), runner
+        assert corner[3] == pytest.approx(-1.79253112033e-04, rel=1e-8), runner
+        assert corner[4] == pytest.approx(-8.96265560167775e-05, rel=1e-8), runner

@@ -249,11 +249,16 @@ def test_shell_job_problem(tmp_path):
     assert p.mesh.elem_type == 41 and p.mesh.dpn == 6
     np.testing.assert_array_equal(p.thickness, np.full(m.n_elems, 0.004))
     assert np.all(p.E == 70e9) and np.all(p.rho == 2700.0)
-    for kw, msg in ((dict(layers=2), "one centred layer"), (dict(z_offset=0.001), "one centred layer")):
-        d = tmp_path / f"bad{len(msg)}{kw.get('layers', 1)}"
+    assert p.shell_sections is None  # one centred isotropic layer: the E, nu, t section
+    # several layers or an offset: a layered section per element set
+    for kw in (dict(layers=2), dict(z_offset=-1.0)):
+        d = tmp_path / f"lay{kw.get('layers', 1)}"
         d.mkdir()
         write_shell_job(d, **kw)
         rb = J.JobRunner(d / "job.yaml")
         rb.cmd_readModelInput(rb.cmds[0])
-        with pytest.raises(NotImplementedError, match=msg):
-            rb._problem()
+        pb = rb._problem()
+        (els, rows, zoff), = pb.shell_sections
+        assert len(els) == m.n_elems and len(rows) == kw.get("layers", 1) and zoff == kw.get("z_offset", 0.0)
+        assert rows[0][:6] == [70e9, 70e9, 0.33, 70e9 / 2.66, 2700.0, 0.004]
+        np.testing.assert_allclose(pb.thickness, 0.004 * kw.get("layers", 1))
