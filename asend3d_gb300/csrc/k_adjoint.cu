@@ -186,6 +186,47 @@ k_adjoint_pairs(int n_el, const int32_t* __restrict__ conn, const double* __rest
     for (int k = 0; k < 36; ++k) out[k] = accumulate ? out[k] + acc[k] : acc[k];
 }
 
+// The same contraction for hex8 meshes kept as geometry classes (K_e = E_e K^):
+// g_e = -a_e^T K^_cls b_e, one thread per element, 576 FP64 FMA against the
+// class matrix (read through L1; a structured block has one class, so a warp
+// reads each entry once) in place of the Gauss-point integration.
+__global__ void __launch_bounds__(128)
+k_adjoint_cls(int n_el, const int32_t* __restrict__ conn, const int32_t* __restrict__ cls_of,
+              const double* __restrict__ cls_ke, const double* __restrict__ av, const double* __restrict__ bv,
+              double* __restrict__ g, int accumulate) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_el) return;
+    int nd[8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) nd[a] = conn[(size_t)e * 8 + a];
+    double ua[24], ub[24];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            ua[3 * a + j] = av[3 * (size_t)nd[a] + j];
+            ub[3 * a + j] = bv[3 * (size_t)nd[a] + j];
+        }
+    // element-relative: K^ annihilates a rigid translation
+#pragma unroll
+    for (int a = 7; a >= 0; --a)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            ua[3 * a + j] -= ua[j];
+            ub[3 * a + j] -= ub[j];
+        }
+    const double* K = cls_ke + (size_t)cls_of[e] * 576;
+    double acc = 0.0;
+#pragma unroll
+    for (int r = 3; r < 24; ++r) {
+        double s = 0.0;
+#pragma unroll
+        for (int q = 3; q < 24; ++q) s = fma(__ldg(K + r * 24 + q), ub[q], s);
+        acc = fma(ua[r], s, acc);
+    }
+    g[e] = accumulate ? g[e] - acc : -acc;
+}
+
 __global__ void k_dot_partial(size_t n, const double* __restrict__ a, const double* __restrict__ b,
                               double* __restrict__ part) {
     __shared__ double sm[32];
@@ -233,7 +274,10 @@ void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g,
         return;
     }
     const int blocks = (c.n_el + 127) / 128;
-    if (c.nn == 8)
+    if (c.type == 8 && c.cls_ready && c.cls_type == 8 && c.ortho.empty())
+        k_adjoint_cls<<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_cls_of.p, c.cls_ke.p, d_a, d_b, d_g,
+                                                    accumulate ? 1 : 0);
+    else if (c.nn == 8)
         k_adjoint_modulus<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, c.d_nu.p, d_a, d_b, d_g,
                                                             accumulate ? 1 : 0);
     else if (c.nn == 10)

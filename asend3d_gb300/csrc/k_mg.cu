@@ -50,7 +50,6 @@ struct MgBlk {
     int node0 = 0, el0 = 0;       // first node / element in the level numbering
     MgAxis ax[3];                 // maps from the finer level's block (levels >= 1)
     int ox[3] = {0, 0, 0}, ol[3] = {0, 0, 0};  // offsets into the level's packed xs / lo, w
-    int t1_0 = 0, t2_0 = 0;       // offsets (nodes) of the restriction intermediates
     double h[3] = {0, 0, 0};      // cell spacing per axis
     bool done = false;            // coarse enough: identity maps below this level
     int n_nodes() const { return (nx + 1) * (ny + 1) * (nz + 1); }
@@ -63,15 +62,14 @@ struct BlkDev {
     int nx, ny, nz, node0, el0;
     int fnx, fny, fnz, fnode0, fel0;
     int ox0, ox1, ox2, ol0, ol1, ol2;
-    int t1_0, t2_0, dense0, pad;
+    int dense0, pad;
 };
 
 struct MgLevel {
     int n_nodes = 0, n_el = 0, n_dof = 0;  // totals (level 0 of a batch includes padding nodes)
-    int n_t1 = 0, n_t2 = 0;       // restriction intermediate sizes (nodes)
     std::vector<MgBlk> blk;
     DArr<BlkDev> d_blk;
-    DArr<int32_t> pre_node, pre_el, pre_t1, pre_t2;  // per-block starts (+ total)
+    DArr<int32_t> pre_node, pre_el;  // per-block starts (+ total)
     DArr<int32_t> d_xs, d_lo;     // packed per block and axis
     DArr<float> d_w;
     Sbell own;                    // pattern + FP32 values (levels >= 1)
@@ -82,7 +80,6 @@ struct MgLevel {
     std::vector<float> h_pen;     // lumped penalty per DOF (in units of sf)
     DArr<float> pen;
     DArr<float> binv, b, r, x4, y4;
-    DArr<float> t1, t2;           // restriction intermediates (after the z and y passes)
     DArr<float> pow_vec;          // last power-iteration vector (warm start)
     bool pow_warm = false;
     int pow_steps = 0;            // steps of the last estimate
@@ -95,6 +92,8 @@ struct MgHierarchy {
     int n_blk = 1;
     std::vector<int32_t> h_dense0;  // offset of each block's dense matrix (floats)
     DArr<double> blk_sf;          // penalty scale per block (instance)
+    DArr<float> child;            // projected class matrices of the first coarsening [n_cls][27][576]
+    bool child_ready = false;
     // captured outer iterations, reused while the launch arguments match
     std::vector<std::pair<std::vector<uint8_t>, cudaGraphExec_t>> graphs;
     ~MgHierarchy() {
@@ -120,6 +119,9 @@ using namespace pcg;
 
 constexpr int kT = 128;
 inline int grid_of(int n) { return (n + kT - 1) / kT; }
+// classes up to which the first coarsening uses projected class matrices
+// (27 x 576 floats each, 62 KB)
+constexpr int kMaxChildClasses = 512;
 
 __device__ __forceinline__ int nid(int i, int j, int k, int ny, int nz) { return (i * (ny + 1) + j) * (nz + 1) + k; }
 
@@ -273,6 +275,90 @@ k_coarsen(LevelView cv, const int32_t* __restrict__ pre_el, const float* __restr
             for (int a = 0; a < 8; ++a) acc = fmaf(Q[ch][a][b], T[ch][(3 * a + c1) * 24 + col], acc);
         coarse_ke[(size_t)C * 576 + q] = acc;
     }
+}
+
+// First coarsening of a level-0 block made of geometry classes: with
+// K_e = E_e K^_cls, the coarse matrix K_C = sum_ch E_ch (Q_ch x I3)^T K^ (Q_ch x I3)
+// is linear in the children's moduli, and the projected class matrix depends
+// only on the child's place in its coarse element.  Per axis a child is one
+// of three cases (coarse cell of width 1; width 2, first or second half), so
+// 27 projected matrices per class, built once per hierarchy in FP64 from the
+// FP64 class matrices (CTA = (case, class)).
+__global__ void __launch_bounds__(256) k_child_mats(const double* __restrict__ cls_ke, float* __restrict__ out) {
+    __shared__ double K[576];
+    __shared__ double T[576];
+    __shared__ double Q[8][8];
+    const int tc = blockIdx.x, cls = blockIdx.y, t = threadIdx.x;
+    int w[3], o[3];
+    for (int ax = 0, v = tc; ax < 3; ++ax, v /= 3) {
+        const int s = v % 3;
+        w[ax] = s == 0 ? 1 : 2;
+        o[ax] = s == 2 ? 1 : 0;
+    }
+    for (int q = t; q < 576; q += blockDim.x) K[q] = cls_ke[(size_t)cls * 576 + q];
+    if (t < 64) {
+        const int a = t >> 3, b = t & 7;
+        double q = 1.0;
+        for (int ax = 0; ax < 3; ++ax) {
+            const double xi = (double)(o[ax] + c_corner[a][ax]) / w[ax];
+            q *= c_corner[b][ax] ? xi : 1.0 - xi;
+        }
+        Q[a][b] = q;
+    }
+    __syncthreads();
+    for (int q = t; q < 576; q += blockDim.x) {  // T = K (Q x I3)
+        const int row = q / 24, col = q % 24, b = col / 3, c2 = col % 3;
+        double acc = 0.0;
+        for (int a = 0; a < 8; ++a) acc += K[row * 24 + 3 * a + c2] * Q[a][b];
+        T[q] = acc;
+    }
+    __syncthreads();
+    for (int q = t; q < 576; q += blockDim.x) {  // (Q x I3)^T T
+        const int row = q / 24, col = q % 24, b = row / 3, c1 = row % 3;
+        double acc = 0.0;
+        for (int a = 0; a < 8; ++a) acc += Q[a][b] * T[(3 * a + c1) * 24 + col];
+        out[((size_t)cls * 27 + tc) * 576 + q] = (float)acc;
+    }
+}
+
+// K_C = sum_ch E_ch B[cls_ch][case_ch]: one CTA of 144 threads per coarse
+// element, four consecutive entries per thread.
+__global__ void __launch_bounds__(144) k_coarsen_lin(LevelView cv, const int32_t* __restrict__ pre_el,
+                                                     const double* __restrict__ E, const int32_t* __restrict__ cls_of,
+                                                     const float* __restrict__ child, float* __restrict__ coarse_ke) {
+    __shared__ float ew[8];
+    __shared__ int bi[8];
+    __shared__ int nch_s;
+    const int t = threadIdx.x, C = blockIdx.x;
+    if (t < 8) {
+        const BlkDev& d = cv.blk[find_blk(pre_el, cv.n_blk, C)];
+        const int Cl = C - d.el0;
+        const int ci = Cl / (d.ny * d.nz), cj = (Cl / d.nz) % d.ny, ck = Cl % d.nz;
+        const int s0 = cv.xs[d.ox0 + ci], w0 = cv.xs[d.ox0 + ci + 1] - s0;
+        const int s1 = cv.xs[d.ox1 + cj], w1 = cv.xs[d.ox1 + cj + 1] - s1;
+        const int s2 = cv.xs[d.ox2 + ck], w2 = cv.xs[d.ox2 + ck + 1] - s2;
+        const int nch = w0 * w1 * w2;
+        if (t == 0) nch_s = nch;
+        if (t < nch) {
+            const int o0 = t / (w1 * w2), o1 = (t / w2) % w1, o2 = t % w2;
+            const int e = d.fel0 + ((s0 + o0) * d.fny + (s1 + o1)) * d.fnz + (s2 + o2);
+            const int tc = (w0 == 1 ? 0 : 1 + o0) + 3 * (w1 == 1 ? 0 : 1 + o1) + 9 * (w2 == 1 ? 0 : 1 + o2);
+            ew[t] = (float)E[e];
+            bi[t] = cls_of[e] * 27 + tc;
+        }
+    }
+    __syncthreads();
+    const int nch = nch_s;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int ch = 0; ch < nch; ++ch) {
+        const float4 b = reinterpret_cast<const float4*>(child + (size_t)bi[ch] * 576)[t];
+        const float e = ew[ch];
+        acc.x = fmaf(e, b.x, acc.x);
+        acc.y = fmaf(e, b.y, acc.y);
+        acc.z = fmaf(e, b.z, acc.z);
+        acc.w = fmaf(e, b.w, acc.w);
+    }
+    reinterpret_cast<float4*>(coarse_ke + (size_t)C * 576)[t] = acc;
 }
 
 // Coloured scatter of stored element matrices into a level's FP32 values.
@@ -453,6 +539,37 @@ __device__ __forceinline__ void sb_row(const SbView& A, int row, const float4* _
     }
 }
 
+// The share of row `row`'s product held by lane t of its T lanes (block
+// columns t, t + T, ...); the T lanes of a row are consecutive threads of one
+// warp and are summed by xor shuffles, which every lane of the warp executes.
+template <int T>
+__device__ __forceinline__ void sb_row_part(const SbView& A, int row, int t, const float4* __restrict__ x,
+                                            float (&y)[3]) {
+    y[0] = y[1] = y[2] = 0.f;
+    const int lane = row & 31;
+    const int64_t g0 = A.slice_off[row >> 5];
+    const int len = A.row_len[row];
+    for (int j = t; j < len; j += T) {
+        const int64_t g = g0 + j;
+        const int c = A.col[g * 32 + lane];
+        const float* v = A.v + (g * 9) * 32 + lane;
+        float m[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) m[q] = v[q * 32];
+        const float4 p = x[c];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) y[a] = fmaf(m[a * 3], p.x, fmaf(m[a * 3 + 1], p.y, fmaf(m[a * 3 + 2], p.z, y[a])));
+    }
+}
+
+template <int T>
+__device__ __forceinline__ void sum_lanes(float (&y)[3]) {
+#pragma unroll
+    for (int o = T / 2; o >= 1; o >>= 1)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) y[a] += __shfl_xor_sync(0xffffffffu, y[a], o);
+}
+
 __global__ void k_vc_smooth0(int n, const float* __restrict__ binv, const float* __restrict__ b, float4* __restrict__ x,
                              const Control* ctl) {
     if (ctl && ctl->all_done) return;
@@ -473,6 +590,43 @@ __global__ void __launch_bounds__(kT) k_vc_resid(SbView A, const float* __restri
     sb_row(A, row, x, y);
 #pragma unroll
     for (int a = 0; a < 3; ++a) r[3 * row + a] = b[3 * row + a] - y[a];
+}
+
+// Coarse-level variants with T lanes per row: a coarse level has too few
+// rows to fill the GPU with one thread each, and a row's 27 block columns
+// then form a long chain of dependent loads; T lanes split the chain.
+template <int T>
+__global__ void __launch_bounds__(kT) k_vc_resid_t(SbView A, const float* __restrict__ b, const float4* __restrict__ x,
+                                                   float* __restrict__ r, const Control* ctl) {
+    if (ctl && ctl->all_done) return;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = gt / T, t = gt % T;
+    const bool ok = row < A.n_rows;
+    float y[3] = {0.f, 0.f, 0.f};
+    if (ok) sb_row_part<T>(A, row, t, x, y);
+    sum_lanes<T>(y);
+    if (!ok || t != 0) return;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) r[3 * row + a] = b[3 * row + a] - y[a];
+}
+
+template <int T>
+__global__ void __launch_bounds__(kT) k_vc_post_t(SbView A, const float* __restrict__ binv, const float* __restrict__ b,
+                                                  const float4* __restrict__ x, float4* __restrict__ y4,
+                                                  const Control* ctl) {
+    if (ctl && ctl->all_done) return;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = gt / T, t = gt % T;
+    const bool ok = row < A.n_rows;
+    float y[3] = {0.f, 0.f, 0.f};
+    if (ok) sb_row_part<T>(A, row, t, x, y);
+    sum_lanes<T>(y);
+    if (!ok || t != 0) return;
+    const float d0 = b[3 * row] - y[0], d1 = b[3 * row + 1] - y[1], d2 = b[3 * row + 2] - y[2];
+    const float* B = binv + 9 * (size_t)row;
+    const float4 xv = x[row];
+    y4[row] = make_float4(xv.x + B[0] * d0 + B[1] * d1 + B[2] * d2, xv.y + B[3] * d0 + B[4] * d1 + B[5] * d2,
+                          xv.z + B[6] * d0 + B[7] * d1 + B[8] * d2, 0.f);
 }
 
 __global__ void __launch_bounds__(kT) k_vc_post(SbView A, const float* __restrict__ binv, const float* __restrict__ b,
@@ -744,60 +898,58 @@ __global__ void __launch_bounds__(1024) k_vc_dense(LevelView cv, const float* __
     }
 }
 
-// Separable trilinear restriction, one axis per pass (z, then y, then x),
-// over every block at once: out[o] = sum_f w(f, m) in[f] along axis AX, m the
-// output index on that axis.  Per block the output dims are
-//   AX = 2: (fnx+1) x (fny+1) x (nz+1) at t1_0, input the fine level at fnode0;
-//   AX = 1: (fnx+1) x (ny+1)  x (nz+1) at t2_0, input t1 at t1_0;
-//   AX = 0: (nx+1)  x (ny+1)  x (nz+1) at node0, input t2 at t2_0.
-// The last (x) pass writes the coarse right-hand side and, fused, the coarse
-// level's first smoothing sweep x4 = B^-1 b.
-template <int AX>
-__global__ void k_vc_restrict_axis(LevelView cv, const int32_t* __restrict__ pre_out, int n_out,
-                                   const float* __restrict__ in, float* __restrict__ out,
-                                   const float* __restrict__ binv, float4* __restrict__ x4, const Control* ctl) {
+// Trilinear restriction R = P^T over every block at once, one coarse node per
+// thread: b_c[m] = sum over the fine nodes f of w_x w_y w_z r_f, where along
+// each axis the fine nodes between xs[m-1] and xs[m+1] contribute with the
+// prolongation weight of m (1 - w on the node's lower coarse neighbour, w on
+// the upper one).  The coarse level's first smoothing sweep x4 = B^-1 b is
+// fused in (binv non-null).
+__device__ __forceinline__ int axis_taps(const int32_t* __restrict__ xs, const int32_t* __restrict__ lo,
+                                         const float* __restrict__ w, int m, int n_c, int (&f)[3], float (&wf)[3]) {
+    const int f_lo = xs[max(m - 1, 0)], f_hi = xs[min(m + 1, n_c)];
+    int k = 0;
+    for (int q = f_lo; q <= f_hi && k < 3; ++q) {
+        const float v = (lo[q] == m) ? 1.f - w[q] : ((lo[q] + 1 == m) ? w[q] : 0.f);
+        if (v == 0.f) continue;
+        f[k] = q;
+        wf[k] = v;
+        ++k;
+    }
+    return k;
+}
+
+__global__ void __launch_bounds__(kT) k_vc_restrict(LevelView cv, const int32_t* __restrict__ pre_node, int n_out,
+                                                    const float* __restrict__ in, float* __restrict__ out,
+                                                    const float* __restrict__ binv, float4* __restrict__ x4,
+                                                    const Control* ctl) {
     if (ctl && ctl->all_done) return;
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= n_out) return;
-    const BlkDev& d = cv.blk[find_blk(pre_out, cv.n_blk, o)];
-    int d0, d1, d2, in_n, n_c, in0, o0;
-    const int32_t *xs, *lo;
-    const float* w;
-    if (AX == 2) {
-        d0 = d.fnx + 1; d1 = d.fny + 1; d2 = d.nz + 1; in_n = d.fnz + 1; n_c = d.nz;
-        in0 = d.fnode0; o0 = d.t1_0;
-        xs = cv.xs + d.ox2; lo = cv.lo + d.ol2; w = cv.w + d.ol2;
-    } else if (AX == 1) {
-        d0 = d.fnx + 1; d1 = d.ny + 1; d2 = d.nz + 1; in_n = d.fny + 1; n_c = d.ny;
-        in0 = d.t1_0; o0 = d.t2_0;
-        xs = cv.xs + d.ox1; lo = cv.lo + d.ol1; w = cv.w + d.ol1;
-    } else {
-        d0 = d.nx + 1; d1 = d.ny + 1; d2 = d.nz + 1; in_n = d.fnx + 1; n_c = d.nx;
-        in0 = d.t2_0; o0 = d.node0;
-        xs = cv.xs + d.ox0; lo = cv.lo + d.ol0; w = cv.w + d.ol0;
-    }
-    (void)d0;
-    const int ol = o - o0;
-    const int i0 = ol / (d1 * d2), i1 = (ol / d2) % d1, i2 = ol % d2;
-    const int m = (AX == 0) ? i0 : (AX == 1) ? i1 : i2;
-    const int f_lo = xs[max(m - 1, 0)], f_hi = xs[min(m + 1, n_c)];
+    const BlkDev& d = cv.blk[find_blk(pre_node, cv.n_blk, o)];
+    const int ol = o - d.node0;
+    const int i0 = ol / ((d.ny + 1) * (d.nz + 1)), i1 = (ol / (d.nz + 1)) % (d.ny + 1), i2 = ol % (d.nz + 1);
+    int fx[3], fy[3], fz[3];
+    float wx[3], wy[3], wz[3];
+    const int nx = axis_taps(cv.xs + d.ox0, cv.lo + d.ol0, cv.w + d.ol0, i0, d.nx, fx, wx);
+    const int ny = axis_taps(cv.xs + d.ox1, cv.lo + d.ol1, cv.w + d.ol1, i1, d.ny, fy, wy);
+    const int nz = axis_taps(cv.xs + d.ox2, cv.lo + d.ol2, cv.w + d.ol2, i2, d.nz, fz, wz);
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    for (int f = f_lo; f <= f_hi; ++f) {
-        const float wf = (lo[f] == m) ? 1.f - w[f] : ((lo[f] + 1 == m) ? w[f] : 0.f);
-        if (wf == 0.f) continue;
-        int src;
-        if (AX == 0) src = (f * d1 + i1) * d2 + i2;
-        else if (AX == 1) src = (i0 * in_n + f) * d2 + i2;
-        else src = (i0 * d1 + i1) * in_n + f;
-        src += in0;
-        s0 = fmaf(wf, in[3 * (size_t)src], s0);
-        s1 = fmaf(wf, in[3 * (size_t)src + 1], s1);
-        s2 = fmaf(wf, in[3 * (size_t)src + 2], s2);
-    }
+    for (int a = 0; a < nx; ++a)
+        for (int b = 0; b < ny; ++b) {
+            const float wab = wx[a] * wy[b];
+            const int base = d.fnode0 + (fx[a] * (d.fny + 1) + fy[b]) * (d.fnz + 1);
+            for (int c = 0; c < nz; ++c) {
+                const float ww = wab * wz[c];
+                const size_t src = 3 * (size_t)(base + fz[c]);
+                s0 = fmaf(ww, in[src], s0);
+                s1 = fmaf(ww, in[src + 1], s1);
+                s2 = fmaf(ww, in[src + 2], s2);
+            }
+        }
     out[3 * (size_t)o] = s0;
     out[3 * (size_t)o + 1] = s1;
     out[3 * (size_t)o + 2] = s2;
-    if (AX == 0 && binv) {
+    if (binv) {
         const float* B = binv + 9 * (size_t)o;
         x4[o] = make_float4(B[0] * s0 + B[1] * s1 + B[2] * s2, B[3] * s0 + B[4] * s1 + B[5] * s2,
                             B[6] * s0 + B[7] * s1 + B[8] * s2, 0.f);
@@ -1147,7 +1299,7 @@ void level_tables(Ctx& c, MgHierarchy& H, int l) {
     const MgLevel* F = l > 0 ? H.L[l - 1].get() : nullptr;
     const int nb = (int)L.blk.size();
     std::vector<BlkDev> dv(nb);
-    std::vector<int32_t> pn(nb + 1), pe(nb + 1), p1(nb + 1), p2(nb + 1);
+    std::vector<int32_t> pn(nb + 1), pe(nb + 1);
     for (int b = 0; b < nb; ++b) {
         const MgBlk& B = L.blk[b];
         BlkDev& d = dv[b];
@@ -1171,23 +1323,15 @@ void level_tables(Ctx& c, MgHierarchy& H, int l) {
         d.ol0 = B.ol[0];
         d.ol1 = B.ol[1];
         d.ol2 = B.ol[2];
-        d.t1_0 = B.t1_0;
-        d.t2_0 = B.t2_0;
         d.dense0 = (l + 1 == (int)H.L.size() && !H.h_dense0.empty()) ? H.h_dense0[b] : 0;
         pn[b] = B.node0;
         pe[b] = B.el0;
-        p1[b] = B.t1_0;
-        p2[b] = B.t2_0;
     }
     pn[nb] = L.n_nodes;
     pe[nb] = L.n_el;
-    p1[nb] = L.n_t1;
-    p2[nb] = L.n_t2;
     L.d_blk.upload(dv, c.stream);
     L.pre_node.upload(pn, c.stream);
     L.pre_el.upload(pe, c.stream);
-    L.pre_t1.upload(p1, c.stream);
-    L.pre_t2.upload(p2, c.stream);
 }
 
 LevelView view_of(const MgLevel& L) {
@@ -1297,7 +1441,7 @@ void build_hierarchy(Ctx& c) {
         auto L = std::make_unique<MgLevel>();
         std::vector<int32_t> xs, lo;
         std::vector<float> w;
-        int node0 = 0, el0 = 0, t1 = 0, t2 = 0;
+        int node0 = 0, el0 = 0;
         for (int b = 0; b < nb; ++b) {
             const MgBlk& P = F.blk[b];
             MgBlk B;
@@ -1314,12 +1458,8 @@ void build_hierarchy(Ctx& c) {
             B.nz = B.ax[2].n_c;
             B.node0 = node0;
             B.el0 = el0;
-            B.t1_0 = t1;
-            B.t2_0 = t2;
             node0 += B.n_nodes();
             el0 += B.n_el();
-            t1 += (P.nx + 1) * (P.ny + 1) * (B.nz + 1);
-            t2 += (P.nx + 1) * (B.ny + 1) * (B.nz + 1);
             for (int ax = 0; ax < 3; ++ax) {
                 B.ox[ax] = (int)xs.size();
                 B.ol[ax] = (int)lo.size();
@@ -1332,8 +1472,6 @@ void build_hierarchy(Ctx& c) {
         L->n_nodes = node0;
         L->n_el = el0;
         L->n_dof = 3 * node0;
-        L->n_t1 = t1;
-        L->n_t2 = t2;
         L->d_xs.upload(xs, c.stream);
         L->d_lo.upload(lo, c.stream);
         L->d_w.upload(w, c.stream);
@@ -1366,8 +1504,6 @@ void build_hierarchy(Ctx& c) {
         }
         level_pattern(c, *L);
         L->Ke.alloc((size_t)L->n_el * 576);
-        L->t1.alloc((size_t)3 * std::max(t1, 1));
-        L->t2.alloc((size_t)3 * std::max(t2, 1));
         H->L.push_back(std::move(L));
     }
     for (auto& Lp : H->L) {
@@ -1477,8 +1613,18 @@ void setup_values(Ctx& c) {
                 fine_ke = F.Ke.p;
             }
         }
-        k_coarsen<<<L.n_el, 512, 0, c.stream>>>(view_of(L), L.pre_el.p, fine_ke, cls_ke, cls_of, c.d_xyz.p,
-                                                c.d_conn.p, c.d_E.p, c.d_nu.p, L.Ke.p);
+        if (l == 1 && cls_ke && c.n_cls <= kMaxChildClasses) {
+            if (!H.child_ready) {
+                H.child.alloc((size_t)c.n_cls * 27 * 576);
+                k_child_mats<<<dim3(27, c.n_cls), 256, 0, c.stream>>>(c.cls_ke.p, H.child.p);
+                ++c.launches;
+                H.child_ready = true;
+            }
+            k_coarsen_lin<<<L.n_el, 144, 0, c.stream>>>(view_of(L), L.pre_el.p, c.d_E.p, cls_of, H.child.p, L.Ke.p);
+        } else {
+            k_coarsen<<<L.n_el, 512, 0, c.stream>>>(view_of(L), L.pre_el.p, fine_ke, cls_ke, cls_of, c.d_xyz.p,
+                                                    c.d_conn.p, c.d_E.p, c.d_nu.p, L.Ke.p);
+        }
         L.own.v32.zero(c.stream);
         for (size_t k = 0; k + 1 < L.colour_ptr.size(); ++k) {
             const int n = L.colour_ptr[k + 1] - L.colour_ptr[k];
@@ -1514,14 +1660,9 @@ void restrict_to(Ctx& c, int l, const Control* ctl) {
     MgLevel& L = *H.L[l];
     MgLevel& C = *H.L[l + 1];
     const bool last = (l + 2 == (int)H.L.size());  // the coarsest level is solved directly: no sweep
-    const LevelView cv = view_of(C);
-    k_vc_restrict_axis<2><<<grid_of(C.n_t1), kT, 0, c.stream>>>(cv, C.pre_t1.p, C.n_t1, L.r.p, C.t1.p, nullptr,
-                                                                 nullptr, ctl);
-    k_vc_restrict_axis<1><<<grid_of(C.n_t2), kT, 0, c.stream>>>(cv, C.pre_t2.p, C.n_t2, C.t1.p, C.t2.p, nullptr,
-                                                                 nullptr, ctl);
-    k_vc_restrict_axis<0><<<grid_of(C.n_nodes), kT, 0, c.stream>>>(cv, C.pre_node.p, C.n_nodes, C.t2.p, C.b.p,
-                                                                    last ? nullptr : C.binv.p,
-                                                                    reinterpret_cast<float4*>(C.x4.p), ctl);
+    k_vc_restrict<<<grid_of(C.n_nodes), kT, 0, c.stream>>>(view_of(C), C.pre_node.p, C.n_nodes, L.r.p, C.b.p,
+                                                           last ? nullptr : C.binv.p,
+                                                           reinterpret_cast<float4*>(C.x4.p), ctl);
 }
 
 void coarsest_solve(Ctx& c, const Control* ctl) {
@@ -1541,6 +1682,45 @@ void prolong_from(Ctx& c, int l, const Control* ctl) {
 
 // One V(1,1) cycle on level 0's b.  With fused0, the caller has already
 // written level 0's first sweep x4 = B^-1 b (fused into the PCG update).
+// Lanes per row of a level's products: one per row while the rows alone
+// fill the GPU (about 152 SMs x 1024 threads), else the smallest power of two
+// up to 16 that does.
+int lanes_for(int n_rows) {
+    constexpr int kFill = 152 * 1024;
+    int t = 1;
+    while (t < 16 && (int64_t)n_rows * t < kFill) t *= 2;
+    return t;
+}
+
+void level_resid(Ctx& c, MgLevel& L, const Control* ctl) {
+    const int t = lanes_for(L.n_nodes);
+    const SbView A = sbview(L);
+    const float4* x = reinterpret_cast<const float4*>(L.x4.p);
+    const int g = (int)(((int64_t)L.n_nodes * t + kT - 1) / kT);
+    switch (t) {
+        case 1: k_vc_resid<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(A, L.b.p, x, L.r.p, ctl); break;
+        case 2: k_vc_resid_t<2><<<g, kT, 0, c.stream>>>(A, L.b.p, x, L.r.p, ctl); break;
+        case 4: k_vc_resid_t<4><<<g, kT, 0, c.stream>>>(A, L.b.p, x, L.r.p, ctl); break;
+        case 8: k_vc_resid_t<8><<<g, kT, 0, c.stream>>>(A, L.b.p, x, L.r.p, ctl); break;
+        default: k_vc_resid_t<16><<<g, kT, 0, c.stream>>>(A, L.b.p, x, L.r.p, ctl); break;
+    }
+}
+
+void level_post(Ctx& c, MgLevel& L, const Control* ctl) {
+    const int t = lanes_for(L.n_nodes);
+    const SbView A = sbview(L);
+    const float4* x = reinterpret_cast<const float4*>(L.x4.p);
+    float4* y = reinterpret_cast<float4*>(L.y4.p);
+    const int g = (int)(((int64_t)L.n_nodes * t + kT - 1) / kT);
+    switch (t) {
+        case 1: k_vc_post<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(A, L.binv.p, L.b.p, x, y, ctl); break;
+        case 2: k_vc_post_t<2><<<g, kT, 0, c.stream>>>(A, L.binv.p, L.b.p, x, y, ctl); break;
+        case 4: k_vc_post_t<4><<<g, kT, 0, c.stream>>>(A, L.binv.p, L.b.p, x, y, ctl); break;
+        case 8: k_vc_post_t<8><<<g, kT, 0, c.stream>>>(A, L.binv.p, L.b.p, x, y, ctl); break;
+        default: k_vc_post_t<16><<<g, kT, 0, c.stream>>>(A, L.binv.p, L.b.p, x, y, ctl); break;
+    }
+}
+
 void vcycle(Ctx& c, const Control* ctl, bool fused0) {
     MgHierarchy& H = *c.mg;
     const int nl = (int)H.L.size();
@@ -1550,22 +1730,17 @@ void vcycle(Ctx& c, const Control* ctl, bool fused0) {
                                                               reinterpret_cast<float4*>(L.x4.p), ctl);
     }
     for (int l = 0; l < nl - 1; ++l) {
-        MgLevel& L = *H.L[l];
-        k_vc_resid<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(sbview(L), L.b.p, reinterpret_cast<float4*>(L.x4.p), L.r.p,
-                                                            ctl);
+        level_resid(c, *H.L[l], ctl);
         restrict_to(c, l, ctl);
     }
     coarsest_solve(c, ctl);
     for (int l = nl - 2; l >= 0; --l) {
-        MgLevel& L = *H.L[l];
         prolong_from(c, l, ctl);
-        k_vc_post<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(sbview(L), L.binv.p, L.b.p,
-                                                           reinterpret_cast<const float4*>(L.x4.p),
-                                                           reinterpret_cast<float4*>(L.y4.p), ctl);
+        level_post(c, *H.L[l], ctl);
     }
 }
 
-int vcycle_launches(const MgHierarchy& H) { return 6 * ((int)H.L.size() - 1) + 1; }
+int vcycle_launches(const MgHierarchy& H) { return 4 * ((int)H.L.size() - 1) + 1; }
 
 // L0.x4 = P C R (L0.r): the coarse-grid correction of one V-cycle alone
 // (restriction of level 0's r, the V-cycle of the coarser levels, and the
