@@ -122,6 +122,9 @@ inline int grid_of(int n) { return (n + kT - 1) / kT; }
 // classes up to which the first coarsening uses projected class matrices
 // (27 x 576 floats each, 62 KB)
 constexpr int kMaxChildClasses = 512;
+// dynamic shared memory of the blocked coarsest inverse (227 KB per CTA less
+// the 4 KB panel inverse and static data)
+constexpr size_t kGjSmem = 220 * 1024;
 
 __device__ __forceinline__ int nid(int i, int j, int k, int ny, int nz) { return (i * (ny + 1) + j) * (nz + 1) + k; }
 
@@ -489,6 +492,133 @@ __global__ void __launch_bounds__(1024) k_gauss_jordan(LevelView cv, float* __re
         for (int q = threadIdx.x; q < n * n; q += blockDim.x) Ag[q] = dyn[q];
 }
 
+// Blocked Gauss-Jordan inverse in shared memory (row stride ld, a multiple
+// of 4), 32-column panels: for panel P (rows / columns k0..k0+kb)
+//   D = A_PP^-1 (warp 0, in registers, lane = row), R = D A_P,rest (row
+//   panel), A_rest,rest -= A_rest,P R, A_rest,P = -A_rest,P D, A_PP = D,
+// which is the unblocked in-place elimination regrouped, so a panel costs
+// four CTA barriers instead of 2 kb, and the trailing update runs as 2 x 4
+// register tiles.  No pivoting: the coarse operators are SPD.
+__device__ __forceinline__ void gj_panel_inverse(float* __restrict__ A, int ld, int k0, int kb, float* __restrict__ D) {
+    const int lane = threadIdx.x & 31;
+    float d[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) d[j] = (lane < kb && j < kb) ? A[(size_t)(k0 + lane) * ld + k0 + j] : (lane == j ? 1.f : 0.f);
+#pragma unroll
+    for (int p = 0; p < 32; ++p) {
+        const float piv = __shfl_sync(0xffffffffu, d[p], p);
+        const float inv = 1.f / piv;
+        const float cp = d[p];  // this row's entry in column p
+        if (lane == p) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) d[j] = (j == p) ? inv : d[j] * inv;
+        }
+        // row p (already scaled) from lane p, entry by entry; lane p keeps its row
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float rpj = __shfl_sync(0xffffffffu, d[j], p);
+            if (lane != p) d[j] = (j == p) ? -cp * inv : fmaf(-cp, rpj, d[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 32; ++j) D[lane * 32 + j] = d[j];
+}
+
+__global__ void __launch_bounds__(1024) k_gauss_jordan_blk(LevelView cv, float* __restrict__ Dall, int ld) {
+    extern __shared__ float dyn[];
+    __shared__ float D[32 * 32];
+    const BlkDev& dv = cv.blk[blockIdx.x];
+    const int n = 3 * (dv.nx + 1) * (dv.ny + 1) * (dv.nz + 1);
+    float* Ag = Dall + dv.dense0;
+    float* A = dyn;
+    const int t = threadIdx.x, nt = blockDim.x;
+    for (int q = t; q < n * ld; q += nt) {
+        const int i = q / ld, j = q % ld;
+        A[q] = (j < n) ? Ag[(size_t)i * n + j] : 0.f;
+    }
+    __syncthreads();
+    for (int k0 = 0; k0 < n; k0 += 32) {
+        const int kb = min(32, n - k0);
+        if (t < 32) gj_panel_inverse(A, ld, k0, kb, D);
+        __syncthreads();
+        // row panel: A_P,j = D A_P,j for the columns j outside the panel
+        for (int j = t; j < n; j += nt) {
+            if (j >= k0 && j < k0 + kb) continue;
+            float a[32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) a[q] = (q < kb) ? A[(size_t)(k0 + q) * ld + j] : 0.f;
+#pragma unroll 4
+            for (int p = 0; p < kb; ++p) {
+                float s = 0.f;
+#pragma unroll
+                for (int q = 0; q < 32; ++q) s = fmaf(D[p * 32 + q], a[q], s);
+                A[(size_t)(k0 + p) * ld + j] = s;
+            }
+        }
+        __syncthreads();
+        // trailing block: A_ij -= sum_q A_iq R_qj, rows and columns outside
+        // the panel, 2 x 4 tiles (columns in float4 groups; ld % 4 == 0)
+        const int ncg = ld / 4, nrg = (n + 1) / 2;
+        for (int tile = t; tile < nrg * ncg; tile += nt) {
+            const int i0 = 2 * (tile / ncg), j0 = 4 * (tile % ncg);
+            if (j0 >= n) continue;
+            const bool r0 = (i0 < k0 || i0 >= k0 + kb), r1 = (i0 + 1 < n) && (i0 + 1 < k0 || i0 + 1 >= k0 + kb);
+            if (!r0 && !r1) continue;
+            float4 acc0 = *reinterpret_cast<const float4*>(A + (size_t)i0 * ld + j0);
+            float4 acc1 = (i0 + 1 < n) ? *reinterpret_cast<const float4*>(A + (size_t)(i0 + 1) * ld + j0)
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int q = 0; q < kb; ++q) {
+                const float4 rq = *reinterpret_cast<const float4*>(A + (size_t)(k0 + q) * ld + j0);
+                const float a0 = A[(size_t)i0 * ld + k0 + q];
+                const float a1 = (i0 + 1 < n) ? A[(size_t)(i0 + 1) * ld + k0 + q] : 0.f;
+                acc0.x = fmaf(-a0, rq.x, acc0.x); acc0.y = fmaf(-a0, rq.y, acc0.y);
+                acc0.z = fmaf(-a0, rq.z, acc0.z); acc0.w = fmaf(-a0, rq.w, acc0.w);
+                acc1.x = fmaf(-a1, rq.x, acc1.x); acc1.y = fmaf(-a1, rq.y, acc1.y);
+                acc1.z = fmaf(-a1, rq.z, acc1.z); acc1.w = fmaf(-a1, rq.w, acc1.w);
+            }
+            // columns of the panel keep their old values here (they are
+            // rewritten below); columns beyond n stay zero
+            float* o0 = A + (size_t)i0 * ld + j0;
+            float* o1 = A + (size_t)(i0 + 1) * ld + j0;
+            const float v0[4] = {acc0.x, acc0.y, acc0.z, acc0.w}, v1[4] = {acc1.x, acc1.y, acc1.z, acc1.w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int j = j0 + c;
+                if (j >= n || (j >= k0 && j < k0 + kb)) continue;
+                if (r0) o0[c] = v0[c];
+                if (r1) o1[c] = v1[c];
+            }
+        }
+        __syncthreads();
+        // column panel A_i,P = -A_i,P D for the rows outside the panel; the
+        // diagonal block becomes D
+        for (int i = t; i < n; i += nt) {
+            float* Ar = A + (size_t)i * ld + k0;
+            if (i >= k0 && i < k0 + kb) {
+                const int p = i - k0;
+                for (int q = 0; q < kb; ++q) Ar[q] = D[p * 32 + q];
+                continue;
+            }
+            float a[32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) a[q] = (q < kb) ? Ar[q] : 0.f;
+#pragma unroll 4
+            for (int p = 0; p < kb; ++p) {
+                float s = 0.f;
+#pragma unroll
+                for (int q = 0; q < 32; ++q) s = fmaf(a[q], D[q * 32 + p], s);
+                Ar[p] = -s;
+            }
+        }
+        __syncthreads();
+    }
+    // symmetrise (the exact inverse is symmetric) and store
+    for (int q = t; q < n * n; q += nt) {
+        const int i = q / n, j = q % n;
+        Ag[q] = 0.5f * (A[(size_t)i * ld + j] + A[(size_t)j * ld + i]);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // V-cycle kernels (all FP32; x4/y4 node-padded float4)
 // ---------------------------------------------------------------------------
@@ -784,7 +914,8 @@ __global__ void __launch_bounds__(kT) k_pow_step(SbView A, const float* __restri
     if (!last) return;
     __threadfence();
     double s[1] = {0.0};
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s[0] += ((volatile double*)part)[b];
+#pragma unroll 4
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s[0] += __ldcg(part + b);
     block_sum<1>(s, sm);
     if (threadIdx.x == 0) nrm[k + 1] = (float)sqrt(s[0]);
 }
@@ -1643,11 +1774,15 @@ void setup_values(Ctx& c) {
     MgLevel& Lc = *H.L.back();
     k_dense_build<<<Lc.n_nodes, 128, 0, c.stream>>>(Lc.n_nodes, Lc.A->slice_off.p, Lc.A->row_len.p, Lc.A->col.p,
                                                     Lc.A->v32.p, view_of(Lc), Lc.pre_node.p, H.dense.p);
-    const size_t gj_smem = sizeof(float) * (size_t)H.n_coarse * H.n_coarse;
-    const bool in_smem = H.n_coarse <= 234;
-    if (in_smem)
-        ASEND_CUDA(cudaFuncSetAttribute(k_gauss_jordan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gj_smem));
-    k_gauss_jordan<<<H.n_blk, 1024, in_smem ? gj_smem : 0, c.stream>>>(view_of(Lc), H.dense.p, in_smem ? 1 : 0);
+    const int ld = (H.n_coarse + 3) & ~3;
+    const size_t blk_smem = sizeof(float) * (size_t)H.n_coarse * ld;
+    if (blk_smem <= kGjSmem) {  // blocked elimination in shared memory
+        ASEND_CUDA(cudaFuncSetAttribute(k_gauss_jordan_blk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)blk_smem));
+        k_gauss_jordan_blk<<<H.n_blk, 1024, blk_smem, c.stream>>>(view_of(Lc), H.dense.p, ld);
+    } else {  // larger coarsest blocks: column-by-column elimination in global memory
+        k_gauss_jordan<<<H.n_blk, 1024, 0, c.stream>>>(view_of(Lc), H.dense.p, 0);
+    }
     c.launches += 2;
     ASEND_CUDA(cudaGetLastError());
     H.epoch = c.assembly_epoch;

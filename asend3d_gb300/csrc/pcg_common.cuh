@@ -313,10 +313,13 @@ __device__ __forceinline__ bool last_block_reduce(const PcgArgs& A, double (&val
     double acc[NR * NV];
 #pragma unroll
     for (int q = 0; q < NR * NV; ++q) acc[q] = 0.0;
+    // L2 reads (ld.global.cg: no stale L1 line after the fence) that may all
+    // be in flight together, unlike volatile loads, which issue one by one
+#pragma unroll 4
     for (int b = b0 + threadIdx.x; b < b0 + nb; b += blockDim.x) {
-        const volatile double* pp = A.partials + (size_t)b * (kMaxRhs * 3);
+        const double* pp = A.partials + (size_t)b * (kMaxRhs * 3);
 #pragma unroll
-        for (int q = 0; q < NR * NV; ++q) acc[q] += pp[q];
+        for (int q = 0; q < NR * NV; ++q) acc[q] += __ldcg(pp + q);
     }
     __syncthreads();
     block_sum<NR * NV>(acc, sm);

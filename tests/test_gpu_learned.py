@@ -115,8 +115,10 @@ def test_vcycle_loss_gradient_matches_finite_differences(gpu_lib):
     loss in the FP32 output biases b3[0..5] (not BF16-rounded).  The loss is
     a high-degree polynomial in the block scale e^(2 y), so the derivative is
     the linear coefficient of a quartic fitted to eight evaluations around the
-    parameter (single central differences of the FP32 loss moved by several
-    percent between builds).  Tolerance 5%."""
+    parameter over offsets up to 8e-3 (single central differences of the FP32
+    loss moved by several percent between builds, and so did fits over
+    offsets up to 4e-3 when the V-cycle's summation order changed).
+    Tolerance 5%."""
     g = GpuSolver(configs.learned_patch(16, 8, 8))
     g.assemble(64)
     p = _oracle_params(7, last_scale=0.02)
@@ -131,7 +133,7 @@ def test_vcycle_loss_gradient_matches_finite_differences(gpu_lib):
         # the loss at eight offsets h of the bias, fitted by a quartic in h:
         # its linear coefficient is the derivative, the fit averages out the
         # FP32 rounding of the individual loss evaluations
-        hs = np.array([-4e-3, -2e-3, -1e-3, -5e-4, 5e-4, 1e-3, 2e-3, 4e-3])
+        hs = np.array([-8e-3, -4e-3, -2e-3, -1e-3, 1e-3, 2e-3, 4e-3, 8e-3])
         vals = []
         for h in hs:
             pp = p.copy()
