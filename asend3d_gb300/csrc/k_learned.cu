@@ -415,8 +415,9 @@ __global__ void __launch_bounds__(kLT) k_block_grad(int n, const int64_t* slice_
 // ---------------------------------------------------------------------------
 constexpr int kBT = 128;                       // nodes per tile = threads per CTA
 constexpr int kPad = kH + 1;                   // padded row (floats)
-constexpr int kPerThread = (kNParam + kBT - 1) / kBT;
-constexpr size_t kBwdSmem = sizeof(float) * ((size_t)kBT * (17 + 4 * kPad + 9) + (kNW1 + kNW2 + kNW3) + 2 * kH + kO);
+constexpr size_t kBwdSmem =
+    sizeof(float) * ((size_t)kBT * (17 + 4 * kPad + 9) + (kNW1 + kNW2 + kNW3) + 2 * kH + kO + kNParam);
+static_assert(kBwdSmem <= 227 * 1024, "backward tile exceeds the shared-memory limit");
 
 __global__ void __launch_bounds__(kBT) k_mlp_backward(int n, const __nv_bfloat16* __restrict__ feat,
                                                       const __nv_bfloat16* __restrict__ wbf,
@@ -431,6 +432,7 @@ __global__ void __launch_bounds__(kBT) k_mlp_backward(int n, const __nv_bfloat16
     float* sdy = sd1 + kBT * kPad;       // [kBT][9]
     float* sw = sdy + kBT * 9;           // W1 W2 W3 (float copies of the BF16 weights)
     float* sb = sw + kNW1 + kNW2 + kNW3; // b1 b2 b3
+    float* sacc = sb + 2 * kH + kO;      // [kNParam] this CTA's gradient sums; entry q belongs to thread q % kBT
     const int t = threadIdx.x;
     for (int q = t; q < kNW1 + kNW2 + kNW3; q += kBT) sw[q] = __bfloat162float(wbf[q]);
     for (int q = t; q < kH; q += kBT) {
@@ -441,9 +443,7 @@ __global__ void __launch_bounds__(kBT) k_mlp_backward(int n, const __nv_bfloat16
     const float* W1 = sw;
     const float* W2 = sw + kNW1;
     const float* W3 = sw + kNW1 + kNW2;
-    float acc[kPerThread];
-#pragma unroll
-    for (int i = 0; i < kPerThread; ++i) acc[i] = 0.f;
+    for (int q = t; q < kNParam; q += kBT) sacc[q] = 0.f;
     const int tiles = (n + kBT - 1) / kBT;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         __syncthreads();  // previous tile's gradient sums are done with the rows
@@ -487,10 +487,10 @@ __global__ void __launch_bounds__(kBT) k_mlp_backward(int n, const __nv_bfloat16
             d1[j] = a1[j] > 0.f ? s : 0.f;
         }
         __syncthreads();
-#pragma unroll
-        for (int i = 0; i < kPerThread; ++i) {
-            const int q = t + i * kBT;
-            if (q >= kNParam) break;
+        // Kept rolled: fully unrolled over the 46 parameters a thread owns, the 128-row sums
+        // below made the compiler's optimiser run for minutes.
+#pragma unroll 1
+        for (int q = t; q < kNParam; q += kBT) {
             const float* lhs;  // per-node factor (stride ls), rhs per-node factor (stride rs)
             const float* rhs = nullptr;
             int ls, rs = 0;
@@ -515,14 +515,10 @@ __global__ void __launch_bounds__(kBT) k_mlp_backward(int n, const __nv_bfloat16
             } else {
                 for (int r = 0; r < kBT; ++r) s += lhs[r * ls];
             }
-            acc[i] += s;
+            sacc[q] += s;
         }
     }
-#pragma unroll
-    for (int i = 0; i < kPerThread; ++i) {
-        const int q = t + i * kBT;
-        if (q < kNParam) part[(size_t)blockIdx.x * kNParam + q] = acc[i];
-    }
+    for (int q = t; q < kNParam; q += kBT) part[(size_t)blockIdx.x * kNParam + q] = sacc[q];
 }
 
 __global__ void k_grad_reduce(int n_part, const float* __restrict__ part, float* __restrict__ grad) {

@@ -781,10 +781,6 @@ __global__ void __launch_bounds__(kT) k_vc_post(SbView A, const float* __restric
 // w = A q, t = w - A M w and v = t - A P C R t (C: coarse V-cycle,
 // R = P^T), the loss ||q||^2 has dL/dM_n = -2 (v_n b_n^T + w_n r2_n^T).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float4 f4of(const float* a, int row) {
-    return make_float4(a[3 * row], a[3 * row + 1], a[3 * row + 2], 0.f);
-}
-
 // q = b - A z, r2 = b - A x2; loss += ||q||^2
 __global__ void __launch_bounds__(kT) k_vl_resid(SbView A, const float* __restrict__ b, const float4* __restrict__ z,
                                                  const float4* __restrict__ x2, float4* __restrict__ q,

@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="omit the nested batch_uq block of the default line")
     ap.add_argument("--cpu-sample-nx", type=int, default=40)
+    ap.add_argument("--no-size-series", action="store_true",
+                    help="reference arm: skip the one-off 40/60/80-cell size series")
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu: one assembly, one multigrid solve, three FP32 SpMV launches")
     ap.add_argument("--workload", default="block_large",
@@ -554,6 +556,28 @@ def sample_accuracy(nx: int, kw: dict) -> dict:
             "u_rel": rel(u[0], ur), "compliance_rel": abs(L - f @ ur) / abs(f @ ur), "gradient_rel": rel(gE, gr)}
 
 
+def size_series(nxs=(40, 60, 80), target_dof: int = 1_013_643) -> dict:
+    """The CPU port on one core per block size (the sizes run concurrently,
+    one process each), and a power-law fit rate = c * n_dof^k through them.
+    The port's per-DOF rate falls with size (its LDL^T blocks grow with the
+    cross-section and its PCG iteration count grows), so the fixed-size
+    sample overstates what one core does on the 200x40x40 block; the fit's
+    value there is an extrapolation, labelled as one."""
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(len(nxs)) as pool:
+        res = pool.map(_cpu_sample, [(nx, 100) for nx in nxs])
+    pts = [{"cells": f"{nx}x{nx // 5}x{nx // 5}", "n_dof": r[0], "s": r[1], "iterations": r[2],
+            "dof_solves_per_s_per_core": r[0] / r[1]} for nx, r in zip(nxs, res)]
+    x = np.log([q["n_dof"] for q in pts])
+    y = np.log([q["dof_solves_per_s_per_core"] for q in pts])
+    k, c = np.polyfit(x, y, 1)
+    return {"points": pts, "fit": f"rate = {np.exp(c):.4g} * n_dof^{k:.3f} per core",
+            "exponent": float(k), "target_n_dof": target_dof,
+            "extrapolated_dof_solves_per_s_per_core": float(np.exp(c) * target_dof ** k)}
+
+
 def run_reference(a):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -568,12 +592,18 @@ def run_reference(a):
         vals.append(cb["value"])
     wall = time.perf_counter() - t0
     v = statistics.mean(vals)
+    series = None
+    if not a.no_size_series:
+        series = size_series(target_dof=3 * (a.nx + 1) * (a.ny + 1) * (a.nz + 1))
+        series["extrapolated_dof_solves_per_s_all_cores"] = (series["extrapolated_dof_solves_per_s_per_core"]
+                                                             * procs)
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
            "warmup": a.warmup, "ms_per_step": 1000 * wall / a.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": f"block_large sample {cb['sample']}"},
            "cpu_baseline": {**cb, "value": v},
-           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "size_series": series}
     print(json.dumps(out))
 
 

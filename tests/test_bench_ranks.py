@@ -60,7 +60,7 @@ def test_single_rank_is_identity():
 def test_reference_arm_prints_on_rank0_only(tmp_path):
     env = dict(os.environ, MASTER_ADDR="127.0.0.1", WORLD_SIZE="2", LOCAL_RANK="0")
     args = [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "0",
-            "--cpu-sample-nx", "10"]
+            "--cpu-sample-nx", "10", "--no-size-series"]
     r1 = subprocess.run(args, env=dict(env, RANK="1"), capture_output=True, text=True, timeout=300)
     assert r1.returncode == 0 and r1.stdout.strip() == ""
     r0 = subprocess.run(args, env=dict(env, RANK="0"), capture_output=True, text=True, timeout=300)
@@ -68,3 +68,16 @@ def test_reference_arm_prints_on_rank0_only(tmp_path):
     line = json.loads(r0.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_reference_size_series_fit():
+    """The size series' power-law fit passes through its own points and
+    extrapolates with the fitted exponent."""
+    import bench
+    ser = bench.size_series(nxs=(10, 15, 20), target_dof=10_000)
+    pts = ser["points"]
+    assert [q["cells"] for q in pts] == ["10x2x2", "15x3x3", "20x4x4"]
+    assert all(q["dof_solves_per_s_per_core"] > 0 for q in pts)
+    k = ser["exponent"]
+    c = pts[-1]["dof_solves_per_s_per_core"] / pts[-1]["n_dof"] ** k
+    assert ser["extrapolated_dof_solves_per_s_per_core"] == pytest.approx(c * 10_000 ** k, rel=0.5)
