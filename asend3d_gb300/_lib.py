@@ -21,6 +21,10 @@ ASEND_OK, ASEND_MAX_ITER, ASEND_NONFINITE, ASEND_FALLBACK = 0, 1, 2, 3
 ASEND_EINVAL, ASEND_ECUDA, ASEND_ESTATE = -1, -2, -3
 METHOD_FP64, METHOD_MIXED, METHOD_SPLIT = 0, 1, 2
 PC_JACOBI, PC_BLOCK, PC_LEARNED, PC_MG, PC_MG_LEARNED = 0, 1, 2, 3, 4
+# shapes of the multigrid CG's split outer product (bit-identical results)
+(PRODUCT_DEFAULT, PRODUCT_REGISTERS, PRODUCT_STAGED_2x3, PRODUCT_STAGED_3x2, PRODUCT_STAGED_2x2,
+ PRODUCT_STAGED_4x2) = range(6)
+PRODUCT_VARIANTS = (PRODUCT_REGISTERS, PRODUCT_STAGED_2x3, PRODUCT_STAGED_3x2, PRODUCT_STAGED_2x2, PRODUCT_STAGED_4x2)
 OBJ_DISPLACEMENT, OBJ_COMPLIANCE, OBJ_ELEMENT = 0, 1, 2
 LOAD_BODY_FORCE, LOAD_GRAVITY, LOAD_CENTRIFUGAL = 0, 1, 2
 LEARN_BLOCK, LEARN_MG = 0, 1
@@ -66,6 +70,8 @@ SIGNATURES = [
     ("asend_set_block_structure", c_int, [C.c_void_p, c_int, c_int, c_int]),
     ("asend_mg_levels", c_int, [C.c_void_p]),
     ("asend_mg_set_damping", c_int, [C.c_void_p, c_dbl]),
+    ("asend_set_product_variant", c_int, [C.c_void_p, c_int]),
+    ("asend_mg_set_fused_tail", c_int, [C.c_void_p, c_int]),
     ("asend_mg_level_info", c_int, [C.c_void_p, c_int, P_int, P_dbl, P_dbl, P_dbl]),
     ("asend_mg_vcycle", c_int, [C.c_void_p, P_flt, P_flt]),
     ("asend_set_instances", c_int, [C.c_void_p, c_int, P_int]),

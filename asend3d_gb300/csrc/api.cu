@@ -656,6 +656,23 @@ int asend_mg_set_damping(asend_ctx* ctx, double factor) {
     });
 }
 
+int asend_set_product_variant(asend_ctx* ctx, int32_t variant) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(variant >= ASEND_PRODUCT_DEFAULT && variant <= ASEND_PRODUCT_STAGED_4x2,
+                "unknown product variant");
+        c.product_variant = variant;
+        return ASEND_OK;
+    });
+}
+
+int asend_mg_set_fused_tail(asend_ctx* ctx, int32_t enable) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(enable == 0 || enable == 1, "enable must be 0 or 1");
+        c.mg_tail = enable != 0;
+        return ASEND_OK;
+    });
+}
+
 int asend_mg_levels(const asend_ctx* ctx) {
     const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
     return c ? mg_levels(*c) : ASEND_EINVAL;

@@ -140,6 +140,8 @@ struct Ctx {
     int bx = 0, by = 0, bz = 0;
     std::shared_ptr<MgHierarchy> mg;
     float mg_damping = 1.5f;  // smoother omega = mg_damping / lambda_max(D^-1 A)
+    int product_variant = 0;  // split outer product: ASEND_PRODUCT_* (0 = the default shape)
+    bool mg_tail = true;      // multigrid: fuse the V-cycle's smallest levels into one launch
     std::shared_ptr<LearnedState> learned;  // learned nodal preconditioner blocks
     int64_t assembly_epoch = 0;
     cudaStream_t stream = nullptr;
@@ -218,6 +220,7 @@ struct Ctx {
     DArr<double> d_f, d_x, d_r;        // rhs incl. penalty, solution, residual
     DArr<float> d_p32, d_ap32;         // mixed: padded direction, A p
     DArr<double> d_p64, d_ap64;        // fp64: padded direction, A p
+    DArr<float4> d_xpair;              // split multigrid CG: correction of x as node-padded FP32 pairs
     DArr<double> d_dinv;               // point Jacobi inverse diagonal (n_dof)
     DArr<float> d_binv;                // nodal block inverse (n_nodes * b*b)
     DArr<double> d_partials;           // block partial sums

@@ -108,6 +108,7 @@ struct MgHierarchy {
     DArr<unsigned int> pow_bound; // ||D^-1 A||_inf per level (float bits)
     DArr<float> pow_omega;        // damping in use per level
     bool safe_damping = false;    // omega from the guaranteed bound (after a failed solve)
+    int tail = 0;                 // first level of the fused coarse tail (0: none)
     DArr<float> vl_q, vl_mw, vl_t4, vl_r2, vl_w;  // learned-smoother training vectors
 };
 
@@ -965,12 +966,8 @@ __global__ void k_scale_blocks(int n, float* __restrict__ binv, const float* __r
 // x_f[i] += sum_I w_iI y_c[I] over the fine level's nodes (a fine node outside
 // every block -- padding between instances -- is left alone); cv describes
 // the coarse level, pre_fnode the fine blocks' first nodes.
-__global__ void k_vc_prolong(LevelView cv, const int32_t* __restrict__ pre_fnode, int n_fine,
-                             const float4* __restrict__ yc, float4* __restrict__ xf, const Control* ctl) {
-    if (ctl && ctl->all_done) return;
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= n_fine) return;
-    const BlkDev& d = cv.blk[find_blk(pre_fnode, cv.n_blk, f)];
+__device__ __forceinline__ void prolong_row(const LevelView& cv, const BlkDev& d, int f, const float4* __restrict__ yc,
+                                            float4* __restrict__ xf) {
     const int fl = f - d.fnode0;
     if (fl >= (d.fnx + 1) * (d.fny + 1) * (d.fnz + 1)) return;
     const int i = fl / ((d.fny + 1) * (d.fnz + 1)), j = (fl / (d.fnz + 1)) % (d.fny + 1), k = fl % (d.fnz + 1);
@@ -1000,14 +997,20 @@ __global__ void k_vc_prolong(LevelView cv, const int32_t* __restrict__ pre_fnode
     xf[f] = acc;
 }
 
+__global__ void k_vc_prolong(LevelView cv, const int32_t* __restrict__ pre_fnode, int n_fine,
+                             const float4* __restrict__ yc, float4* __restrict__ xf, const Control* ctl) {
+    if (ctl && ctl->all_done) return;
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_fine) return;
+    prolong_row(cv, cv.blk[find_blk(pre_fnode, cv.n_blk, f)], f, yc, xf);
+}
+
 // Coarsest solve y = A_b^-1 b per block (CTA = block): one warp per row,
 // lanes stride the row (coalesced), shuffle reduction.  y is node-padded.
-__global__ void __launch_bounds__(1024) k_vc_dense(LevelView cv, const float* __restrict__ ainv,
-                                                   const float* __restrict__ b, float* __restrict__ y4,
-                                                   const Control* ctl) {
-    if (ctl && ctl->all_done) return;
-    __shared__ float sb[1024];
-    const BlkDev& d = cv.blk[blockIdx.x];
+// sb: shared staging of the block's b (at least n floats); the CTA's threads
+// all call this (it synchronises them).
+__device__ __forceinline__ void dense_block(const BlkDev& d, const float* __restrict__ ainv, const float* __restrict__ b,
+                                            float* __restrict__ y4, float* sb) {
     const int n = 3 * (d.nx + 1) * (d.ny + 1) * (d.nz + 1);
     const float* bb = b + 3 * (size_t)d.node0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) sb[i] = bb[i];
@@ -1015,14 +1018,36 @@ __global__ void __launch_bounds__(1024) k_vc_dense(LevelView cv, const float* __
     const float* Ab = ainv + d.dense0;
     float* yb = y4 + 4 * (size_t)d.node0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    // eight loads per lane issued together (a 256-wide row in one pass): the
+    // row's loads overlap instead of waiting on each other
     for (int row = warp; row < n; row += nw) {
         const float* ar = Ab + (size_t)row * n;
         float acc = 0.f;
-        for (int j = lane; j < n; j += 32) acc = fmaf(ar[j], sb[j], acc);
+        for (int j0 = 0; j0 < n; j0 += 256) {
+            float a[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int j = j0 + lane + 32 * t;
+                a[t] = j < n ? ar[j] : 0.f;
+            }
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int j = j0 + lane + 32 * t;
+                if (j < n) acc = fmaf(a[t], sb[j], acc);
+            }
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) yb[4 * (row / 3) + row % 3] = acc;
     }
+}
+
+__global__ void __launch_bounds__(1024) k_vc_dense(LevelView cv, const float* __restrict__ ainv,
+                                                   const float* __restrict__ b, float* __restrict__ y4,
+                                                   const Control* ctl) {
+    if (ctl && ctl->all_done) return;
+    __shared__ float sb[1024];
+    dense_block(cv.blk[blockIdx.x], ainv, b, y4, sb);
 }
 
 // Trilinear restriction R = P^T over every block at once, one coarse node per
@@ -1031,46 +1056,66 @@ __global__ void __launch_bounds__(1024) k_vc_dense(LevelView cv, const float* __
 // prolongation weight of m (1 - w on the node's lower coarse neighbour, w on
 // the upper one).  The coarse level's first smoothing sweep x4 = B^-1 b is
 // fused in (binv non-null).
-__device__ __forceinline__ int axis_taps(const int32_t* __restrict__ xs, const int32_t* __restrict__ lo,
-                                         const float* __restrict__ w, int m, int n_c, int (&f)[3], float (&wf)[3]) {
-    const int f_lo = xs[max(m - 1, 0)], f_hi = xs[min(m + 1, n_c)];
-    int k = 0;
-    for (int q = f_lo; q <= f_hi && k < 3; ++q) {
-        const float v = (lo[q] == m) ? 1.f - w[q] : ((lo[q] + 1 == m) ? w[q] : 0.f);
-        if (v == 0.f) continue;
-        f[k] = q;
-        wf[k] = v;
-        ++k;
-    }
-    return k;
+// The taps of coarse node m on one axis: fine nodes xs[m] - 1, xs[m] and
+// xs[m] + 1, each present when it lies strictly between xs[m - 1] and
+// xs[m + 1] (coarse spacing is one or two fine cells, so no other fine node
+// has a non-zero weight); weights w[xs[m] - 1], 1 and 1 - w[xs[m] + 1], the
+// prolongation weights of m.  Fixed slots keep the taps in registers and let
+// the 27 loads of a coarse node issue together.
+struct Taps {
+    int f[3];
+    float w[3];
+    bool on[3];
+};
+__device__ __forceinline__ Taps axis_taps(const int32_t* __restrict__ xs, const float* __restrict__ w, int m,
+                                          int n_c) {
+    Taps t;
+    const int x = xs[m];
+    t.on[0] = m > 0 && x - 1 > xs[m - 1];
+    t.on[1] = true;
+    t.on[2] = m < n_c && x + 1 < xs[m + 1];
+    t.f[0] = t.on[0] ? x - 1 : x;  // an absent tap points at x: every address formed stays in range
+    t.f[1] = x;
+    t.f[2] = t.on[2] ? x + 1 : x;
+    t.w[0] = t.on[0] ? w[x - 1] : 0.f;
+    t.w[1] = 1.f;
+    t.w[2] = t.on[2] ? 1.f - w[x + 1] : 0.f;
+    return t;
 }
 
-__global__ void __launch_bounds__(kT) k_vc_restrict(LevelView cv, const int32_t* __restrict__ pre_node, int n_out,
-                                                    const float* __restrict__ in, float* __restrict__ out,
-                                                    const float* __restrict__ binv, float4* __restrict__ x4,
-                                                    const Control* ctl) {
-    if (ctl && ctl->all_done) return;
-    const int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= n_out) return;
-    const BlkDev& d = cv.blk[find_blk(pre_node, cv.n_blk, o)];
+__device__ __forceinline__ void restrict_row(const LevelView& cv, const BlkDev& d, int o, const float* __restrict__ in,
+                                             float* __restrict__ out, const float* __restrict__ binv,
+                                             float4* __restrict__ x4) {
     const int ol = o - d.node0;
     const int i0 = ol / ((d.ny + 1) * (d.nz + 1)), i1 = (ol / (d.nz + 1)) % (d.ny + 1), i2 = ol % (d.nz + 1);
-    int fx[3], fy[3], fz[3];
-    float wx[3], wy[3], wz[3];
-    const int nx = axis_taps(cv.xs + d.ox0, cv.lo + d.ol0, cv.w + d.ol0, i0, d.nx, fx, wx);
-    const int ny = axis_taps(cv.xs + d.ox1, cv.lo + d.ol1, cv.w + d.ol1, i1, d.ny, fy, wy);
-    const int nz = axis_taps(cv.xs + d.ox2, cv.lo + d.ol2, cv.w + d.ol2, i2, d.nz, fz, wz);
+    const Taps tx = axis_taps(cv.xs + d.ox0, cv.w + d.ol0, i0, d.nx);
+    const Taps ty = axis_taps(cv.xs + d.ox1, cv.w + d.ol1, i1, d.ny);
+    const Taps tz = axis_taps(cv.xs + d.ox2, cv.w + d.ol2, i2, d.nz);
+    float v[3][3][3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const bool on = tx.on[a] && ty.on[b] && tz.on[c];
+                const size_t src = 3 * (size_t)(d.fnode0 + (tx.f[a] * (d.fny + 1) + ty.f[b]) * (d.fnz + 1) + tz.f[c]);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) v[a][b][c][q] = on ? in[src + q] : 0.f;
+            }
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    for (int a = 0; a < nx; ++a)
-        for (int b = 0; b < ny; ++b) {
-            const float wab = wx[a] * wy[b];
-            const int base = d.fnode0 + (fx[a] * (d.fny + 1) + fy[b]) * (d.fnz + 1);
-            for (int c = 0; c < nz; ++c) {
-                const float ww = wab * wz[c];
-                const size_t src = 3 * (size_t)(base + fz[c]);
-                s0 = fmaf(ww, in[src], s0);
-                s1 = fmaf(ww, in[src + 1], s1);
-                s2 = fmaf(ww, in[src + 2], s2);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const float wab = tx.w[a] * ty.w[b];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                if (!(tx.on[a] && ty.on[b] && tz.on[c])) continue;
+                const float ww = wab * tz.w[c];
+                s0 = fmaf(ww, v[a][b][c][0], s0);
+                s1 = fmaf(ww, v[a][b][c][1], s1);
+                s2 = fmaf(ww, v[a][b][c][2], s2);
             }
         }
     out[3 * (size_t)o] = s0;
@@ -1083,12 +1128,121 @@ __global__ void __launch_bounds__(kT) k_vc_restrict(LevelView cv, const int32_t*
     }
 }
 
+__global__ void __launch_bounds__(kT) k_vc_restrict(LevelView cv, const int32_t* __restrict__ pre_node, int n_out,
+                                                    const float* __restrict__ in, float* __restrict__ out,
+                                                    const float* __restrict__ binv, float4* __restrict__ x4,
+                                                    const Control* ctl) {
+    if (ctl && ctl->all_done) return;
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n_out) return;
+    restrict_row(cv, cv.blk[find_blk(pre_node, cv.n_blk, o)], o, in, out, binv, x4);
+}
+
+// ---------------------------------------------------------------------------
+// Fused coarse tail of the V-cycle.  Below a size threshold every level of an
+// instance fits one CTA, and an instance's rows couple only to its own rows
+// on every level (the stacked operator is block diagonal), so one CTA per
+// block runs the tail's residuals, restrictions, the coarsest dense solve,
+// prolongations and post-smoothing in sequence with CTA barriers between the
+// steps, in place of a dozen small grid-wide launches whose latency, not
+// their few hundred kilobytes, set their time.  Per row the arithmetic and
+// its order are those of the separate kernels (same lanes per row).
+// ---------------------------------------------------------------------------
+constexpr int kMaxTail = 8;       // levels a fused tail may hold
+constexpr int kTailNodes = 512;   // largest block (nodes) of a level in the tail
+constexpr int kTailThreads = 1024;
+
+struct TailLevel {
+    SbView A;
+    LevelView V;   // blocks of this level (with their finer blocks' maps)
+    const float* binv;
+    float* b;
+    float* r;
+    float4* x4;
+    float4* y4;
+    int lanes;     // lanes per row of this level's products (as the separate kernels)
+};
+struct TailArgs {
+    int n_lev;     // levels lt .. nl - 1; the last one is solved by its dense inverse
+    TailLevel L[kMaxTail];
+    const float* ainv;
+};
+
+// r = b - A x (post == false) or y = x + B^-1 (b - A x) (post == true) over
+// the rows [row0, row0 + nn) of one block, T lanes per row.
+template <int T>
+__device__ __forceinline__ void tail_rows(const TailLevel& L, int row0, int nn, bool post) {
+    const int tot = nn * T;
+    const float4* x = L.x4;
+    for (int base = 0; base < tot; base += blockDim.x) {  // same trip count in every thread
+        const int gt = base + threadIdx.x;
+        const int row = row0 + gt / T, t = gt % T;
+        const bool ok = gt < tot;
+        float y[3] = {0.f, 0.f, 0.f};
+        if (ok) sb_row_part<T>(L.A, row, t, x, y);
+        sum_lanes<T>(y);
+        if (!ok || t != 0) continue;
+        if (!post) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) L.r[3 * row + a] = L.b[3 * row + a] - y[a];
+        } else {
+            const float d0 = L.b[3 * row] - y[0], d1 = L.b[3 * row + 1] - y[1], d2 = L.b[3 * row + 2] - y[2];
+            const float* B = L.binv + 9 * (size_t)row;
+            const float4 xv = x[row];
+            L.y4[row] = make_float4(xv.x + B[0] * d0 + B[1] * d1 + B[2] * d2, xv.y + B[3] * d0 + B[4] * d1 + B[5] * d2,
+                                    xv.z + B[6] * d0 + B[7] * d1 + B[8] * d2, 0.f);
+        }
+    }
+}
+__device__ __forceinline__ void tail_level_rows(const TailLevel& L, int row0, int nn, bool post) {
+    switch (L.lanes) {
+        case 1: tail_rows<1>(L, row0, nn, post); break;
+        case 2: tail_rows<2>(L, row0, nn, post); break;
+        case 4: tail_rows<4>(L, row0, nn, post); break;
+        case 8: tail_rows<8>(L, row0, nn, post); break;
+        default: tail_rows<16>(L, row0, nn, post); break;
+    }
+}
+
+__global__ void __launch_bounds__(kTailThreads) k_vc_tail(TailArgs ta, const Control* ctl) {
+    if (ctl && ctl->all_done) return;
+    __shared__ float sb[1024];
+    const int b = blockIdx.x;
+    const int nl = ta.n_lev;
+    auto nodes = [](const BlkDev& d) { return (d.nx + 1) * (d.ny + 1) * (d.nz + 1); };
+    for (int l = 0; l + 1 < nl; ++l) {
+        const BlkDev& d = ta.L[l].V.blk[b];
+        tail_level_rows(ta.L[l], d.node0, nodes(d), false);
+        __syncthreads();
+        const TailLevel& C = ta.L[l + 1];
+        const BlkDev& dc = C.V.blk[b];
+        const bool last = (l + 2 == nl);  // the coarsest level takes no smoothing sweep
+        for (int q = threadIdx.x; q < nodes(dc); q += blockDim.x)
+            restrict_row(C.V, dc, dc.node0 + q, ta.L[l].r, C.b, last ? nullptr : C.binv, C.x4);
+        __syncthreads();
+    }
+    dense_block(ta.L[nl - 1].V.blk[b], ta.ainv, ta.L[nl - 1].b, reinterpret_cast<float*>(ta.L[nl - 1].y4), sb);
+    __syncthreads();
+    for (int l = nl - 2; l >= 0; --l) {
+        const TailLevel& C = ta.L[l + 1];
+        const BlkDev& dc = C.V.blk[b];
+        const int nf = (dc.fnx + 1) * (dc.fny + 1) * (dc.fnz + 1);
+        for (int q = threadIdx.x; q < nf; q += blockDim.x) prolong_row(C.V, dc, dc.fnode0 + q, C.y4, ta.L[l].x4);
+        __syncthreads();
+        const BlkDev& d = ta.L[l].V.blk[b];
+        tail_level_rows(ta.L[l], d.node0, nodes(d), true);
+        __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // multigrid-preconditioned flexible CG kernels (one right-hand side; every
 // instance of a batched stack at once, with its own scalars and tickets)
 // ---------------------------------------------------------------------------
 struct MgPcg {
     PcgArgs a;            // outer operator, x, r, p, ap, partials, sc, ctl (nrhs = 1)
+    float4* xp;           // split method: the correction e of x since its last true residual,
+                          // node-padded FP32 pairs (hi float4, lo float4)
     float* b0;            // V-cycle input (level-0 rhs, FP32 r)
     const float4* z;      // V-cycle output (level-0 y4)
     const float* binv0;   // level-0 smoother blocks: the first sweep
@@ -1151,6 +1305,271 @@ __global__ void __launch_bounds__(kThreads) k_mg_spmv_dot(MgPcg M) {
         RhsScalars& s = S[0];
         s.pAp = tot[0][0];
         s.alpha = s.rz / s.pAp;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Split method, vector side: the correction e of x (node-padded), r and A p
+// (natural layout) are FP32 pairs and every per-row update and dot product is
+// pair arithmetic on the FP32 pipes; FP64 is left to the per-CTA reductions
+// (one value per thread), the scalars, and the true residuals (x64 += e, then
+// r = f - A64 x64), formed two or three times per solve.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ F2 ld_pair(const float2* v, size_t i) {
+    const float2 q = v[i];
+    return {q.x, q.y};
+}
+__device__ __forceinline__ void st_pair(float2* v, size_t i, F2 a) { v[i] = make_float2(a.h, a.l); }
+__device__ __forceinline__ void ld_pad_pair(const void* p, size_t node, F2 (&v)[3]) {
+    const float4 h = reinterpret_cast<const float4*>(p)[2 * node];
+    const float4 l = reinterpret_cast<const float4*>(p)[2 * node + 1];
+    v[0] = {h.x, l.x};
+    v[1] = {h.y, l.y};
+    v[2] = {h.z, l.z};
+}
+__device__ __forceinline__ void st_pad_pair(void* p, size_t node, const F2 (&v)[3]) {
+    reinterpret_cast<float4*>(p)[2 * node] = make_float4(v[0].h, v[1].h, v[2].h, 0.f);
+    reinterpret_cast<float4*>(p)[2 * node + 1] = make_float4(v[0].l, v[1].l, v[2].l, 0.f);
+}
+
+// Store A p of this row (pairs) and return p . A p over the row's 3 DOF.
+__device__ __forceinline__ double pair_ap_dot(const PcgArgs& A, int row, const F2 (&y)[3]) {
+    F2 pv[3];
+    ld_pad_pair(A.p, row, pv);
+    float2* ap = reinterpret_cast<float2*>(A.ap);
+    F2 acc{0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        st_pair(ap, 3 * (size_t)row + q, y[q]);
+        acc = f2_add(acc, f2_mul(pv[q], y[q]));
+    }
+    return f2_dbl(acc);
+}
+
+__device__ __forceinline__ void set_alpha(RhsScalars& s, double pAp) {
+    s.pAp = pAp;
+    s.alpha = s.rz / s.pAp;
+    const F2 a = f2_of(s.alpha);
+    s.alpha2[0] = a.h;
+    s.alpha2[1] = a.l;
+}
+
+// The register-fed split product with the pair epilogue.
+__global__ void __launch_bounds__(kThreads) k_mg_spmv_dot_pair(MgPcg M) {
+    const PcgArgs& A = M.a;
+    RhsScalars* Sc = A.sc + cta_instance(A) * kMaxRhs;
+    if (cta_done<1>(A, Sc)) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    double d[1][1] = {{0.0}};
+    if (row < A.n_rows) {
+        float Sm[1][3], Cc[1][3];
+        spmv_row_split_sc<1>(row, A, A.p, Sm, Cc);
+        const F2 y[3] = {two_sum(Sm[0][0], Cc[0][0]), two_sum(Sm[0][1], Cc[0][1]), two_sum(Sm[0][2], Cc[0][2])};
+        d[0][0] = pair_ap_dot(A, row, y);
+    }
+    double tot[1][1];
+    if (last_block_reduce<1, 1>(A, d, 0, tot) && threadIdx.x == 0) set_alpha(Sc[0], tot[0][0]);
+}
+
+// The split method iterates on x = x64 + e: x64 (FP64) changes only when a
+// true residual is formed, and the correction e gathered since then is an
+// FP32 pair.  Folding e into x64 there (and at the end) keeps the stored
+// solution in FP64, so the pairs' 48-bit rounding of e stays far below the
+// solve's tolerance (x itself as a pair left a noise floor near 1e-9).
+__global__ void k_zero_pairs(int n, float4* __restrict__ e) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 2 * n) e[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// x64 += e, e = 0 for the instances whose true residual is formed next (all
+// rows when all is set)
+__global__ void __launch_bounds__(kThreads) k_fold_pairs(MgPcg M, int all) {
+    const PcgArgs& A = M.a;
+    const RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (!all && !S[0].replace) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= A.n_rows) return;
+    F2 e[3];
+    ld_pad_pair(M.xp, row, e);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) A.x[3 * (size_t)row + q] += f2_dbl(e[q]);
+    const F2 z[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    st_pad_pair(M.xp, row, z);
+}
+
+// e += alpha p, r -= alpha A p, b0 = r (FP32), |r|^2, and the level-0 first
+// smoothing sweep.
+__global__ void __launch_bounds__(kThreads) k_mg_update_xr_pair(MgPcg M) {
+    const PcgArgs& A = M.a;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (cta_done<1>(A, S)) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    double d[1][1] = {{0.0}};
+    if (row < A.n_rows) {
+        const F2 alpha{S[0].alpha2[0], S[0].alpha2[1]};
+        F2 pv[3], xv[3];
+        ld_pad_pair(A.p, row, pv);
+        ld_pad_pair(M.xp, row, xv);
+        const float2* ap = reinterpret_cast<const float2*>(A.ap);
+        float2* r = reinterpret_cast<float2*>(A.r);
+        F2 acc{0.f, 0.f};
+        float rf[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const size_t o = 3 * (size_t)row + q;
+            xv[q] = f2_add(xv[q], f2_mul(alpha, pv[q]));
+            const F2 rv = f2_add(ld_pair(r, o), f2_neg(f2_mul(alpha, ld_pair(ap, o))));
+            st_pair(r, o, rv);
+            M.b0[o] = rv.h;
+            rf[q] = rv.h;
+            acc = f2_add(acc, f2_mul(rv, rv));
+        }
+        st_pad_pair(M.xp, row, xv);
+        const float* B = M.binv0 + 9 * (size_t)row;
+        M.x40[row] = make_float4(B[0] * rf[0] + B[1] * rf[1] + B[2] * rf[2], B[3] * rf[0] + B[4] * rf[1] + B[5] * rf[2],
+                                 B[6] * rf[0] + B[7] * rf[1] + B[8] * rf[2], 0.f);
+        d[0][0] = f2_dbl(acc);
+    }
+    double tot[1][1];
+    if (last_block_reduce<1, 1>(A, d, 1, tot) && threadIdx.x == 0) {
+        RhsScalars& s = S[0];
+        s.rr = tot[0][0];
+        s.iter += 1;
+        if (!isfinite(s.rr)) {
+            s.nonfinite = 1;
+            s.done = 1;
+        } else if (s.rr <= s.target) {
+            s.done = 1;
+            s.restart = 1;  // this iteration's p update is skipped
+        }
+        if (s.done) retire_instance(A);
+    }
+}
+
+// r . z and (mode 0) A p . z in pairs, beta (Polak-Ribiere); mode 1: rz
+// after a true-residual evaluation, and p = z on a restart.
+__global__ void __launch_bounds__(kThreads) k_mg_rz_pair(MgPcg M, int mode) {
+    const PcgArgs& A = M.a;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (mode == 0 && cta_done<1>(A, S)) return;
+    if (mode == 1 && !S[0].refresh) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    double d[1][2] = {{0.0, 0.0}};
+    if (row < A.n_rows) {
+        const float4 z = M.z[row];
+        const float zz[3] = {z.x, z.y, z.z};
+        const float2* r = reinterpret_cast<const float2*>(A.r);
+        const float2* ap = reinterpret_cast<const float2*>(A.ap);
+        F2 a0{0.f, 0.f}, a1{0.f, 0.f};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const size_t o = 3 * (size_t)row + q;
+            a0 = f2_add(a0, f2_mul_f(ld_pair(r, o), zz[q]));
+            if (mode == 0) a1 = f2_add(a1, f2_mul_f(ld_pair(ap, o), zz[q]));
+        }
+        d[0][0] = f2_dbl(a0);
+        d[0][1] = f2_dbl(a1);
+        if (mode == 1 && S[0].restart) {
+            const F2 pz[3] = {{zz[0], 0.f}, {zz[1], 0.f}, {zz[2], 0.f}};
+            st_pad_pair(A.p, row, pz);
+        }
+    }
+    double tot[1][2];
+    if (last_block_reduce<1, 2>(A, d, 2, tot) && threadIdx.x == 0) {
+        RhsScalars& s = S[0];
+        if (mode == 0) {
+            s.beta = -s.alpha * tot[0][1] / s.rz;
+            const F2 b = f2_of(s.beta);
+            s.beta2[0] = b.h;
+            s.beta2[1] = b.l;
+        }
+        s.rz = tot[0][0];
+        if (mode == 1) {
+            s.refresh = 0;
+            s.restart = 0;
+        }
+        if (!isfinite(s.rz)) {
+            s.nonfinite = 1;
+            if (!s.done) {
+                s.done = 1;
+                if (mode == 0) retire_instance(A);
+            }
+            s.finished = 1;
+        }
+    }
+}
+
+// p = z + beta p in pairs
+__global__ void __launch_bounds__(kThreads) k_mg_update_p_pair(MgPcg M) {
+    const PcgArgs& A = M.a;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (cta_done<1>(A, S)) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= A.n_rows) return;
+    const F2 beta{S[0].beta2[0], S[0].beta2[1]};
+    const float4 z = M.z[row];
+    F2 pv[3];
+    ld_pad_pair(A.p, row, pv);
+    pv[0] = f2_add(f2_mul(beta, pv[0]), F2{z.x, 0.f});
+    pv[1] = f2_add(f2_mul(beta, pv[1]), F2{z.y, 0.f});
+    pv[2] = f2_add(f2_mul(beta, pv[2]), F2{z.z, 0.f});
+    st_pad_pair(A.p, row, pv);
+}
+
+// The split product with its values and columns staged through shared memory
+// by bulk copies (spmv_row_split_staged): same rows per CTA, same results and
+// the same pair epilogue and p.Ap reduction as k_mg_spmv_dot_pair.  A warp whose
+// copies time out makes its rows' contribution NaN, which the solve reports
+// as a non-finite breakdown.
+template <int G, int S>
+__global__ void __launch_bounds__(kThreads) k_mg_spmv_dot_staged(MgPcg M) {
+    extern __shared__ __align__(128) unsigned char st_smem[];
+    const PcgArgs& A = M.a;
+    RhsScalars* Sc = A.sc + cta_instance(A) * kMaxRhs;
+    if (cta_done<1>(A, Sc)) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    F2 y[3];
+    const bool ok = spmv_row_split_staged<G, S>(A, A.p, st_smem, y);
+    double d[1][1] = {{0.0}};
+    if (row < A.n_rows) d[0][0] = pair_ap_dot(A, row, y);
+    if (!ok) d[0][0] = __longlong_as_double(0x7ff8000000000000ll);
+    double tot[1][1];
+    if (last_block_reduce<1, 1>(A, d, 0, tot) && threadIdx.x == 0) set_alpha(Sc[0], tot[0][0]);
+}
+
+// Launch of the split outer product in one of its shapes (ASEND_PRODUCT_*):
+// register-fed, or staged with G groups per stage and S stages per warp.
+template <int G, int S>
+void launch_staged(const MgPcg& M, int grid, cudaStream_t st) {
+    k_mg_spmv_dot_staged<G, S><<<grid, kThreads, SplitStage<G, S>::smem(kThreads), st>>>(M);
+}
+
+// Opt the staged shapes into their dynamic shared memory (above the 48 KB
+// default) on the current device; called outside stream capture.
+template <int G, int S>
+void staged_attr() {
+    ASEND_CUDA(cudaFuncSetAttribute(k_mg_spmv_dot_staged<G, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    SplitStage<G, S>::smem(kThreads)));
+}
+void product_attrs() {
+    static bool done[64] = {};
+    int dev = 0;
+    ASEND_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && done[dev]) return;
+    staged_attr<2, 3>();
+    staged_attr<3, 2>();
+    staged_attr<2, 2>();
+    staged_attr<4, 2>();
+    if (dev >= 0 && dev < 64) done[dev] = true;
+}
+
+void launch_split_product(const Ctx& c, const MgPcg& M, int grid) {
+    switch (c.product_variant) {
+        case ASEND_PRODUCT_REGISTERS: k_mg_spmv_dot_pair<<<grid, kThreads, 0, c.stream>>>(M); break;
+        case ASEND_PRODUCT_STAGED_3x2: launch_staged<3, 2>(M, grid, c.stream); break;
+        case ASEND_PRODUCT_STAGED_2x2: launch_staged<2, 2>(M, grid, c.stream); break;
+        case ASEND_PRODUCT_STAGED_4x2: launch_staged<4, 2>(M, grid, c.stream); break;
+        default: launch_staged<2, 3>(M, grid, c.stream); break;  // ASEND_PRODUCT_DEFAULT, ASEND_PRODUCT_STAGED_2x3
     }
 }
 
@@ -1260,6 +1679,7 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_p(MgPcg M) {
 // (init = 1: also |f|^2, the target and fresh recurrence state) or for the
 // instances whose replace flag is set (init = 0).  Marks them for the rz /
 // direction refresh that follows the next V-cycle.
+template <bool PAIR_R>
 __global__ void __launch_bounds__(kThreads) k_mg_residual(MgPcg M, int init, double tol2) {
     const PcgArgs& A = M.a;
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
@@ -1283,7 +1703,8 @@ __global__ void __launch_bounds__(kThreads) k_mg_residual(MgPcg M, int init, dou
         for (int a = 0; a < 3; ++a) {
             const size_t o = 3 * (size_t)row + a;
             const double rv = A.f[o] - y[a];
-            A.r[o] = rv;
+            if constexpr (PAIR_R) st_pair(reinterpret_cast<float2*>(A.r), o, f2_of(rv));  // split method
+            else A.r[o] = rv;
             M.b0[o] = (float)rv;
             d[0][0] += rv * rv;
             d[0][1] += A.f[o] * A.f[o];
@@ -1657,6 +2078,19 @@ void build_hierarchy(Ctx& c) {
     if (dense_tot > (size_t)INT32_MAX) throw InputError("multigrid coarsest blocks too large");
     H->dense.alloc(dense_tot);
     for (int l = 0; l < (int)H->L.size(); ++l) level_tables(c, *H, l);
+    // fused tail: the deepest levels whose every block has <= kTailNodes
+    // nodes, if there are at least two (one besides the coarsest)
+    {
+        const int nl = (int)H->L.size();
+        int lt = nl;
+        for (int l = nl - 1; l >= 1; --l) {
+            int mx = 0;
+            for (const MgBlk& B : H->L[l]->blk) mx = std::max(mx, B.n_nodes());
+            if (mx > kTailNodes) break;
+            lt = l;
+        }
+        H->tail = (nl - lt >= 2 && nl - lt <= kMaxTail) ? lt : 0;
+    }
     ASEND_CUDA(cudaStreamSynchronize(c.stream));
     c.mg = H;
 }
@@ -1852,26 +2286,58 @@ void level_post(Ctx& c, MgLevel& L, const Control* ctl) {
     }
 }
 
+// First level of the fused coarse tail in use (nl - 1: no tail, the
+// coarsest level alone is solved by its own launch).
+int tail_level(const Ctx& c) {
+    const MgHierarchy& H = *c.mg;
+    const int nl = (int)H.L.size();
+    return (c.mg_tail && H.tail > 0) ? H.tail : nl - 1;
+}
+
+// Levels lt .. nl - 1 in one launch of k_vc_tail (one CTA per block).
+void launch_tail(Ctx& c, int lt, const Control* ctl) {
+    MgHierarchy& H = *c.mg;
+    TailArgs ta;
+    std::memset(&ta, 0, sizeof(ta));
+    ta.n_lev = (int)H.L.size() - lt;
+    for (int i = 0; i < ta.n_lev; ++i) {
+        MgLevel& L = *H.L[lt + i];
+        TailLevel& T = ta.L[i];
+        T.A = sbview(L);
+        T.V = view_of(L);
+        T.binv = L.binv.p;
+        T.b = L.b.p;
+        T.r = L.r.p;
+        T.x4 = reinterpret_cast<float4*>(L.x4.p);
+        T.y4 = reinterpret_cast<float4*>(L.y4.p);
+        T.lanes = lanes_for(L.n_nodes);
+    }
+    ta.ainv = H.dense.p;
+    k_vc_tail<<<H.n_blk, kTailThreads, 0, c.stream>>>(ta, ctl);
+}
+
 void vcycle(Ctx& c, const Control* ctl, bool fused0) {
     MgHierarchy& H = *c.mg;
     const int nl = (int)H.L.size();
+    const int lt = tail_level(c);
     if (!fused0 && nl > 1) {
         MgLevel& L = *H.L[0];
         k_vc_smooth0<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(L.n_nodes, L.binv.p, L.b.p,
                                                               reinterpret_cast<float4*>(L.x4.p), ctl);
     }
-    for (int l = 0; l < nl - 1; ++l) {
+    for (int l = 0; l < lt; ++l) {
         level_resid(c, *H.L[l], ctl);
         restrict_to(c, l, ctl);
     }
-    coarsest_solve(c, ctl);
-    for (int l = nl - 2; l >= 0; --l) {
+    if (lt < nl - 1) launch_tail(c, lt, ctl);
+    else coarsest_solve(c, ctl);
+    for (int l = lt - 1; l >= 0; --l) {
         prolong_from(c, l, ctl);
         level_post(c, *H.L[l], ctl);
     }
 }
 
-int vcycle_launches(const MgHierarchy& H) { return 4 * ((int)H.L.size() - 1) + 1; }
+int vcycle_launches(const Ctx& c) { return 4 * tail_level(c) + 1; }
 
 // L0.x4 = P C R (L0.r): the coarse-grid correction of one V-cycle alone
 // (restriction of level 0's r, the V-cycle of the coarser levels, and the
@@ -1908,6 +2374,7 @@ void mg_invalidate_values(Ctx& c) {
 }
 
 void mg_prepare(Ctx& c) {
+    product_attrs();
     if (!c.mg) build_hierarchy(c);
     if (c.mg->epoch != c.assembly_epoch) {
         setup_values(c);
@@ -1941,7 +2408,7 @@ void mg_apply(Ctx& c, const float* d_b, float* d_z4) {
     ASEND_CUDA(cudaMemcpyAsync(L0.b.p, d_b, sizeof(float) * c.n_dof, cudaMemcpyDeviceToDevice, c.stream));
     vcycle(c, nullptr, false);
     ASEND_CUDA(cudaMemcpyAsync(d_z4, L0.y4.p, sizeof(float) * 4 * c.n_nodes, cudaMemcpyDeviceToDevice, c.stream));
-    c.launches += vcycle_launches(*c.mg);
+    c.launches += vcycle_launches(c);
 }
 
 int mg_levels(const Ctx& c) { return c.mg ? (int)c.mg->L.size() : 0; }
@@ -1992,7 +2459,7 @@ double mg_time_kernel(Ctx& c, int kernel, int method, int n_launch, double* byte
     auto launch = [&]() {
         if (kernel == 0) {
             if (method == ASEND_METHOD_MIXED) k_mg_spmv_dot<float, float><<<grid, kThreads, 0, c.stream>>>(M);
-            else if (method == ASEND_METHOD_SPLIT) k_mg_spmv_dot<float, SplitP><<<grid, kThreads, 0, c.stream>>>(M);
+            else if (method == ASEND_METHOD_SPLIT) launch_split_product(c, M, grid);
             else k_mg_spmv_dot<double, double><<<grid, kThreads, 0, c.stream>>>(M);
         } else if (kernel == 1) {
             k_vc_resid<<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(sbview(L0), L0.b.p, reinterpret_cast<float4*>(L0.x4.p),
@@ -2054,7 +2521,7 @@ void mg_vcycle_host(Ctx& c, const float* b, float* z) {
     if (H.L.size() < 2) throw InputError("multigrid hierarchy has a single level");
     ASEND_CUDA(cudaMemcpyAsync(L0.b.p, b, sizeof(float) * c.n_dof, cudaMemcpyHostToDevice, c.stream));
     vcycle(c, nullptr, false);
-    c.launches += vcycle_launches(H);
+    c.launches += vcycle_launches(c);
     std::vector<float> y4((size_t)4 * c.n_nodes);
     ASEND_CUDA(cudaMemcpyAsync(y4.data(), L0.y4.p, sizeof(float) * y4.size(), cudaMemcpyDeviceToHost, c.stream));
     ASEND_CUDA(cudaStreamSynchronize(c.stream));
@@ -2078,7 +2545,7 @@ void mg_stationary_residual(Ctx& c, float* r_host, int k, bool learned_smoother)
         ASEND_CUDA(cudaMemcpyAsync(L0.b.p, H.vl_w.p, sizeof(float) * c.n_dof, cudaMemcpyDeviceToDevice, c.stream));
         vcycle(c, nullptr, false);
         k_vl_rstep<<<g, kT, 0, c.stream>>>(sbview(L0), reinterpret_cast<const float4*>(L0.y4.p), H.vl_w.p);
-        c.launches += vcycle_launches(H) + 1;
+        c.launches += vcycle_launches(c) + 1;
     }
     ASEND_CUDA(cudaMemcpyAsync(r_host, H.vl_w.p, sizeof(float) * c.n_dof, cudaMemcpyDeviceToHost, c.stream));
     ASEND_CUDA(cudaStreamSynchronize(c.stream));
@@ -2115,7 +2582,7 @@ void mg_learned_loss_grad(Ctx& c, const float* samples, int n_samples, float* gb
         coarse_correction(c);  // L0.x4 = P C R t
         k_vl_grad<<<g, kT, 0, c.stream>>>(sbview(L0), t4, reinterpret_cast<const float4*>(L0.x4.p), b, H.vl_w.p,
                                          H.vl_r2.p, gblk);
-        c.launches += vcycle_launches(H) + 4;
+        c.launches += vcycle_launches(c) + 4;
     }
     ASEND_CUDA(cudaGetLastError());
 }
@@ -2162,6 +2629,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         c.d_p64.alloc(std::max(c.d_p64.n, (size_t)kMaxRhs * 4 * n));
         c.d_ap64.alloc(std::max(c.d_ap64.n, (size_t)kMaxRhs * nd));
     }
+    if (split) c.d_xpair.alloc(std::max(c.d_xpair.n, (size_t)2 * n));
     // one scalar set per instance (slot 0 of kMaxRhs), persistent so the
     // captured iteration graphs stay valid across solves
     const int NI = c.n_inst > 1 ? c.n_inst : 1;
@@ -2210,19 +2678,30 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         M.binv0 = L0.binv.p;
         M.x40 = reinterpret_cast<float4*>(L0.x4.p);
         M.n_inst = NI;
+        if (split) {  // the split method's correction e (FP32 pairs) starts at zero
+            M.xp = c.d_xpair.p;
+            k_zero_pairs<<<(2 * n + kThreads - 1) / kThreads, kThreads, 0, c.stream>>>(n, M.xp);
+            ++c.launches;
+        }
         ASEND_CUDA(cudaMemsetAsync(d_sc, 0, sc_need, c.stream));
         ASEND_CUDA(cudaMemsetAsync(d_ctl, 0, sizeof(Control), c.stream));
         auto launch_residual = [&](int init) {
-            k_mg_residual<<<grid, kThreads, 0, c.stream>>>(M, init, o.rel_tol * o.rel_tol);
-            ++c.launches;
+            if (split) {  // x64 += e first (the instances being replaced), then r = f - A64 x64
+                k_fold_pairs<<<grid, kThreads, 0, c.stream>>>(M, init);
+                k_mg_residual<true><<<grid, kThreads, 0, c.stream>>>(M, init, o.rel_tol * o.rel_tol);
+                c.launches += 2;
+            } else {
+                k_mg_residual<false><<<grid, kThreads, 0, c.stream>>>(M, init, o.rel_tol * o.rel_tol);
+                ++c.launches;
+            }
         };
         auto launch_iteration = [&]() {
             if (mixed) {
                 k_mg_spmv_dot<float, float><<<grid, kThreads, 0, c.stream>>>(M);
                 k_mg_update_xr<float><<<grid, kThreads, 0, c.stream>>>(M);
             } else if (split) {
-                k_mg_spmv_dot<float, SplitP><<<grid, kThreads, 0, c.stream>>>(M);
-                k_mg_update_xr<SplitP><<<grid, kThreads, 0, c.stream>>>(M);
+                launch_split_product(c, M, grid);
+                k_mg_update_xr_pair<<<grid, kThreads, 0, c.stream>>>(M);
             } else {
                 k_mg_spmv_dot<double, double><<<grid, kThreads, 0, c.stream>>>(M);
                 k_mg_update_xr<double><<<grid, kThreads, 0, c.stream>>>(M);
@@ -2232,8 +2711,8 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
                 k_mg_rz<float><<<grid, kThreads, 0, c.stream>>>(M, 0);
                 k_mg_update_p<float><<<grid, kThreads, 0, c.stream>>>(M);
             } else if (split) {
-                k_mg_rz<SplitP><<<grid, kThreads, 0, c.stream>>>(M, 0);
-                k_mg_update_p<SplitP><<<grid, kThreads, 0, c.stream>>>(M);
+                k_mg_rz_pair<<<grid, kThreads, 0, c.stream>>>(M, 0);
+                k_mg_update_p_pair<<<grid, kThreads, 0, c.stream>>>(M);
             } else {
                 k_mg_rz<double><<<grid, kThreads, 0, c.stream>>>(M, 0);
                 k_mg_update_p<double><<<grid, kThreads, 0, c.stream>>>(M);
@@ -2244,18 +2723,20 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         auto launch_start = [&]() {
             vcycle(c, nullptr, false);
             if (mixed) k_mg_rz<float><<<grid, kThreads, 0, c.stream>>>(M, 1);
-            else if (split) k_mg_rz<SplitP><<<grid, kThreads, 0, c.stream>>>(M, 1);
+            else if (split) k_mg_rz_pair<<<grid, kThreads, 0, c.stream>>>(M, 1);
             else k_mg_rz<double><<<grid, kThreads, 0, c.stream>>>(M, 1);
-            c.launches += vcycle_launches(H) + 2;
+            c.launches += vcycle_launches(c) + 2;
         };
         launch_residual(1);
         launch_start();
         ASEND_CUDA(cudaGetLastError());
         // G iterations as one graph, kept with the hierarchy and reused while
         // the launch arguments are the same (they fully define the graph)
-        std::vector<uint8_t> key(sizeof(MgPcg) + 2 * sizeof(int));
+        // (with everything else that changes the captured sequence: the
+        // method, the chunk length, the product shape and the tail switch)
+        std::vector<uint8_t> key(sizeof(MgPcg) + 4 * sizeof(int));
         std::memcpy(key.data(), &M, sizeof(MgPcg));
-        const int extra[2] = {o.method, G};
+        const int extra[4] = {o.method, G, c.product_variant, c.mg_tail ? 1 : 0};
         std::memcpy(key.data() + sizeof(MgPcg), extra, sizeof(extra));
         cudaGraphExec_t exec = nullptr;
         for (auto& g : H.graphs)
@@ -2274,7 +2755,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
             }
             H.graphs.emplace_back(key, exec);
         }
-        const int per_iter = 4 + vcycle_launches(H);
+        const int per_iter = 4 + vcycle_launches(c);
         const size_t sc_bytes = sizeof(RhsScalars) * NI * kMaxRhs;
         int since_repl = 0;
         for (;;) {
@@ -2312,6 +2793,10 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
             ASEND_CUDA(cudaGraphLaunch(exec, c.stream));
             c.launches += (int64_t)per_iter * G + 1;
             since_repl += G;
+        }
+        if (split) {  // the solution: x64 + e
+            k_fold_pairs<<<grid, kThreads, 0, c.stream>>>(M, 1);
+            ++c.launches;
         }
         ASEND_CUDA(cudaMemcpyAsync(h, d_sc, sc_bytes, cudaMemcpyDeviceToHost, c.stream));
         ASEND_CUDA(cudaStreamSynchronize(c.stream));

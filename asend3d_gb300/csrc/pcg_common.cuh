@@ -17,6 +17,7 @@ struct RhsScalars {
     int32_t restart;  // done by convergence: that iteration's p update was skipped
     int32_t refresh;  // multigrid CG: rz (and p when restarting) to be re-formed after a V-cycle
     int32_t pad2;
+    float alpha2[2], beta2[2];  // alpha and beta as FP32 pairs (the split method's vector updates)
 };
 struct Control {
     int32_t all_done;
@@ -140,11 +141,52 @@ __device__ __forceinline__ void split_term(float h, float l, float xh, float xl,
     C = __fmaf_rn(l, xh, C);
 }
 
-// FP64-accurate row product from FP32 hi / lo values and a split direction.
+// ---------------------------------------------------------------------------
+// FP32 pairs (double-float): a value v = h + l with |l| <= ulp(h) / 2, a
+// 48-bit significand carried by two FP32 numbers.  The arithmetic below is
+// built from error-free transformations -- Knuth's TwoSum, Dekker's
+// Fast2Sum and the FMA-exact product -- so it runs on the FP32 pipes, which
+// on this GPU issue many times faster than its FP64 pipe.  The intrinsics
+// keep the compiler from contracting or reassociating the steps.
+// ---------------------------------------------------------------------------
+struct F2 {
+    float h, l;
+};
+__device__ __forceinline__ F2 fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ F2 two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp))};
+}
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+    const F2 s = two_sum(a.h, b.h);
+    return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ F2 f2_neg(F2 a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+    const float p = __fmul_rn(a.h, b.h);
+    const float e = __fmaf_rn(a.h, b.h, -p);
+    return fast_two_sum(p, __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e)));
+}
+__device__ __forceinline__ F2 f2_mul_f(F2 a, float b) {  // pair times an FP32 number
+    const float p = __fmul_rn(a.h, b);
+    const float e = __fmaf_rn(a.h, b, -p);
+    return fast_two_sum(p, __fmaf_rn(a.l, b, e));
+}
+__device__ __forceinline__ F2 f2_of(double v) {  // FP64 -> pair (FP64 pipe: conversions)
+    const float h = (float)v;
+    return {h, (float)(v - (double)h)};
+}
+__device__ __forceinline__ double f2_dbl(F2 a) { return (double)a.h + (double)a.l; }
+
+// FP64-accurate row product from FP32 hi / lo values and a split direction:
+// the running sums S and their compensations Cc (y = S + Cc).
 template <int NR>
-__device__ __forceinline__ void spmv_row_split(int row, const PcgArgs& A, const void* __restrict__ p,
-                                               double (&y)[NR][3]) {
-    float S[NR][3], Cc[NR][3];
+__device__ __forceinline__ void spmv_row_split_sc(int row, const PcgArgs& A, const void* __restrict__ p,
+                                                  float (&S)[NR][3], float (&Cc)[NR][3]) {
 #pragma unroll
     for (int k = 0; k < NR; ++k)
 #pragma unroll
@@ -206,6 +248,13 @@ __device__ __forceinline__ void spmv_row_split(int row, const PcgArgs& A, const 
             }
         }
     }
+}
+
+template <int NR>
+__device__ __forceinline__ void spmv_row_split(int row, const PcgArgs& A, const void* __restrict__ p,
+                                               double (&y)[NR][3]) {
+    float S[NR][3], Cc[NR][3];
+    spmv_row_split_sc<NR>(row, A, p, S, Cc);
 #pragma unroll
     for (int k = 0; k < NR; ++k)
 #pragma unroll
@@ -266,6 +315,162 @@ __device__ __forceinline__ void spmv_row(int row, const PcgArgs& A, const TV* __
         }
     }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Staged split product.  A warp owns one slice (32 rows); the slice's block
+// column groups -- 288 FP32 hi values, 288 lo values and 32 column indices
+// each, contiguous in HBM group after group -- stream through a ring of
+// shared-memory stages that cp.async.bulk copies fill and that complete on
+// one mbarrier per stage.  The bytes in flight per SM are then set by the
+// ring depth (warps x stages x stage bytes) instead of by how many loads the
+// resident warps' registers can hold, which left the register-fed product
+// latency-bound near half of the HBM bandwidth.  The arithmetic and its
+// order per row are those of spmv_row_split (bit-identical results).
+// ---------------------------------------------------------------------------
+template <int G, int S>
+struct SplitStage {
+    static constexpr int kVal = 9 * 32;                            // floats per group and value part
+    static constexpr int kStage = G * (2 * kVal * 4 + 32 * 4);     // bytes per stage
+    static constexpr int kWarp = S * kStage;                       // ring bytes per warp
+    static constexpr int kBar = 128;                               // mbarrier area (16 x 8 B max)
+    static constexpr int smem(int threads) { return kBar + (threads / 32) * kWarp; }
+    static_assert((kThreads / 32) * S <= kBar / 8, "one mbarrier per warp and stage must fit the barrier area");
+    static_assert(kStage % 16 == 0 && (G * kVal * 4) % 16 == 0, "bulk copies need 16-byte aligned stages");
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false after kSpinLimit polls (each poll may suspend the
+// thread for a hardware-chosen interval), so a copy that never lands ends
+// the kernel with an error instead of a hang.
+constexpr int kSpinLimit = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (int i = 0; i < kSpinLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// global -> shared bulk copy (16-byte aligned addresses, size a multiple of
+// 16) completing on bar; the executing CTA's shared::cta address is a valid
+// shared::cluster address
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// y = A p (FP64-accurate, split values and direction) for this thread's row;
+// the CTA's rows are 32-row slices, one per warp.  Returns false in every
+// lane of a warp whose copies did not land within the wait limit (y is then
+// incomplete).  smem: SplitStage<G, S>::smem(blockDim.x) bytes, 16-aligned.
+template <int G, int S>
+__device__ __forceinline__ bool spmv_row_split_staged(const PcgArgs& A, const void* __restrict__ p,
+                                                      unsigned char* smem, F2 (&y)[3]) {
+    using St = SplitStage<G, S>;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sl = row >> 5;
+    float Sm[3] = {0.f, 0.f, 0.f}, Cc[3] = {0.f, 0.f, 0.f};
+    y[0] = y[1] = y[2] = F2{0.f, 0.f};
+    if ((sl << 5) >= A.n_rows) return true;  // warp-uniform: no slice for this warp
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + warp * S;
+    unsigned char* ring = smem + St::kBar + warp * St::kWarp;
+    const int64_t g0 = A.slice_off[sl];
+    const int ng = (int)(A.slice_off[sl + 1] - g0);
+    const int len = row < A.n_rows ? A.row_len[row] : 0;
+    const int nst = (ng + G - 1) / G;
+    const float4* P = reinterpret_cast<const float4*>(p);
+    auto issue = [&](int k) {  // lane 0 only
+        const int s = k % S;
+        const int cnt = min(G, ng - k * G);
+        const int64_t gk = g0 + (int64_t)k * G;
+        unsigned char* st = ring + s * St::kStage;
+        mbar_expect_tx(bars + s, (uint32_t)cnt * (2 * St::kVal * 4 + 32 * 4));
+        bulk_g2s(st, A.v32 + gk * St::kVal, cnt * St::kVal * 4, bars + s);
+        bulk_g2s(st + G * St::kVal * 4, A.v32lo + gk * St::kVal, cnt * St::kVal * 4, bars + s);
+        bulk_g2s(st + 2 * G * St::kVal * 4, A.col + gk * 32, cnt * 32 * 4, bars + s);
+    };
+    if (lane == 0) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) mbar_init(bars + s, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fence_async_shared();
+        for (int k = 0; k < min(S, nst); ++k) issue(k);
+    }
+    __syncwarp();
+    int k = 0;
+    bool ok = true;
+    for (; k < nst; ++k) {
+        const int s = k % S;
+        const bool landed = __all_sync(0xffffffffu, mbar_wait(bars + s, (uint32_t)((k / S) & 1)));
+        if (!landed) {
+            ok = false;
+            break;
+        }
+        const float* hv = reinterpret_cast<const float*>(ring + s * St::kStage);
+        const float* lv = hv + G * St::kVal;
+        const int* cv = reinterpret_cast<const int*>(lv + G * St::kVal);
+        const int cnt = min(G, ng - k * G);
+        float4 xh[G], xl[G];
+#pragma unroll
+        for (int u = 0; u < G; ++u) {
+            if (u < cnt && k * G + u < len) {
+                const int c = cv[u * 32 + lane];
+                xh[u] = P[2 * (size_t)c];
+                xl[u] = P[2 * (size_t)c + 1];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < G; ++u) {
+            if (u < cnt && k * G + u < len) {
+                const float* h = hv + u * St::kVal + lane;
+                const float* l = lv + u * St::kVal + lane;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    split_term(h[(3 * a) * 32], l[(3 * a) * 32], xh[u].x, xl[u].x, Sm[a], Cc[a]);
+                    split_term(h[(3 * a + 1) * 32], l[(3 * a + 1) * 32], xh[u].y, xl[u].y, Sm[a], Cc[a]);
+                    split_term(h[(3 * a + 2) * 32], l[(3 * a + 2) * 32], xh[u].z, xl[u].z, Sm[a], Cc[a]);
+                }
+            }
+        }
+        __syncwarp();  // every lane is done reading stage s before it is refilled
+        if (lane == 0 && k + S < nst) {
+            fence_async_shared();
+            issue(k + S);
+        }
+    }
+    if (!ok) {
+        // stages k .. min(nst, k + S) - 1 may still be in flight: wait for them
+        // (bounded) before the CTA can leave and its shared memory be reused
+        if (lane == 0)
+            for (int q = k; q < min(nst, k + S); ++q) mbar_wait(bars + q % S, (uint32_t)((q / S) & 1));
+        __syncwarp();
+        return false;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) y[a] = two_sum(Sm[a], Cc[a]);
+    return true;
 }
 
 // Preconditioner application z = M^-1 r for one node.

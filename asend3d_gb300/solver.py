@@ -258,9 +258,12 @@ class GpuSolver:
         self._check(self.lib.asend_get_load_vector(self.ctx, case, _ptr(f, C.c_double)), "get_load_vector")
         return f
 
-    @staticmethod
-    def opts(method=_lib.METHOD_MIXED, precond=_lib.PC_JACOBI, rel_tol=1e-8, max_iter=0, graph_iters=16,
-             warm_start=0, replace_every=0) -> SolveOpts:
+    def opts(self, method=_lib.METHOD_MIXED, precond=_lib.PC_JACOBI, rel_tol=1e-8, max_iter=0, graph_iters=16,
+             warm_start=0, replace_every=0, product=None) -> SolveOpts:
+        """Solve options; `product` (an autotuned _lib.PRODUCT_* shape of the
+        split outer product) is a context setting and is installed here."""
+        if product is not None:
+            self.set_product_variant(product)
         return SolveOpts(method, precond, rel_tol, max_iter, graph_iters, warm_start, replace_every)
 
     def static_solve(self, u0=None, **kw):
@@ -493,6 +496,16 @@ class GpuSolver:
     def mg_set_damping(self, factor):
         """Multigrid smoother omega = factor / lambda_max(D^-1 A) (default 1.5)."""
         self._check(self.lib.asend_mg_set_damping(self.ctx, factor), "mg_set_damping")
+
+    def set_product_variant(self, variant):
+        """Shape of the multigrid CG's split outer product (_lib.PRODUCT_*):
+        register-fed or staged through shared memory; results are identical."""
+        self._check(self.lib.asend_set_product_variant(self.ctx, int(variant)), "set_product_variant")
+
+    def mg_set_fused_tail(self, enable=True):
+        """Multigrid: the smallest levels as one fused launch (default) or one
+        launch per level and step; same arithmetic."""
+        self._check(self.lib.asend_mg_set_fused_tail(self.ctx, int(bool(enable))), "mg_set_fused_tail")
 
     @property
     def mg_levels(self) -> int:

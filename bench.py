@@ -38,6 +38,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 # the headline metric, verbatim; each line's config.workload says what was run
+# kernel of each shape of the split outer product (asend_set_product_variant)
+PRODUCT_KERNEL = {1: "k_mg_spmv_dot_pair", 2: "k_mg_spmv_dot_staged<2,3>", 3: "k_mg_spmv_dot_staged<3,2>",
+                  4: "k_mg_spmv_dot_staged<2,2>", 5: "k_mg_spmv_dot_staged<4,2>"}
 METRIC = "DOF-solves/sec at 1e-8 rel. residual, learned+batched vs plain PCG, 1 GB300; HBM GB/s"
 UNIT = "DOF-solves/s"
 
@@ -89,6 +92,10 @@ def batch_measure(steps: int, warmup: int, plain: bool = True, accuracy: bool = 
     n_cases = len(prob.loads)
     best = dict(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, rel_tol=1e-8, graph_iters=8)
     o_adj = g.opts(**best)
+    from asend3d_gb300 import autotune
+
+    g.assemble(precision=64)
+    shape, _ = autotune.tune_product(g)
 
     def step():
         g.assemble(precision=64)
@@ -122,7 +129,7 @@ def batch_measure(steps: int, warmup: int, plain: bool = True, accuracy: bool = 
                       "n_dof_total": n_real, "rhs_per_step": 64 * n_cases, "rel_tol": 1e-8,
                       "method": "CG + per-instance geometric multigrid, one V-cycle over all instances",
                       "l2": "stack operator 1.2 GB FP64 + 0.6 GB FP32 > 129 MB L2"},
-           "iterations_max": st["iterations"], "ms_breakdown": {"assemble": st["ms_assemble"], "solve": st["ms_solve"]},
+           "iterations_max": st["iterations"], "product_shape": PRODUCT_KERNEL[shape], "ms_breakdown": {"assemble": st["ms_assemble"], "solve": st["ms_solve"]},
            "gpu_launches_per_step": launches, "clocks": clk.summary()}
     if plain:
         # plain: FP64 point-Jacobi PCG, one instance and one load case at a time
@@ -647,6 +654,13 @@ def run_ours(a):
         rc = g.lib.asend_adjoint_gradient(g.ctx, C.byref(o_adj), C.byref(Lc), None, C.byref(st))
         return Lc.value, rc, st
 
+    # ---- the split product's shape, tuned on this operator (bit-identical
+    # results; the kernel alone is timed per shape)
+    from asend3d_gb300 import autotune
+
+    g.assemble(precision=64)
+    shape, shape_ms = autotune.tune_product(g)
+
     # ---- warm-up
     for _ in range(a.warmup):
         rc, st = step_device()
@@ -742,7 +756,7 @@ def run_ours(a):
     # timed as they run in the step; the slowest is reported
     peak, peak_kind = measured_peak()
     kern = {}
-    names = {0: "k_mg_spmv_dot<float,SplitP> (outer FP64-accurate product, FP32 hi+lo values, + p.Ap)",
+    names = {0: f"{PRODUCT_KERNEL[shape]} (outer FP64-accurate product, FP32 hi+lo values, + p.Ap)",
              1: "k_vc_resid (finest-level V-cycle residual, FP32 SBELL SpMV)",
              2: "k_vc_post (finest-level post-smoothing, FP32 SBELL SpMV + block Jacobi)"}
     for k in (0, 1, 2):
@@ -759,7 +773,8 @@ def run_ours(a):
             "per_iteration_kernels": [dict(kern[k], frac=kern[k]["achieved_GBps"] / peak,
                                            traffic=ncu_traffic(k)) for k in (0, 1, 2)],
             "fp64_outer_product": {"kernel": "k_mg_spmv_dot<double,double> (native FP64 values)",
-                                   "ms_per_launch": ms64, "achieved_GBps": by64 / (ms64 * 1e-3) / 1e9}}
+                                   "ms_per_launch": ms64, "achieved_GBps": by64 / (ms64 * 1e-3) / 1e9},
+            "product_shapes_ms_per_launch": {PRODUCT_KERNEL[v]: t for v, t in shape_ms.items()}}
 
     # ---- accuracy at full size: the benchmark's 1e-8 solution and gradient
     # against the same library at 1e-11 (FP64 operator); never fatal

@@ -130,6 +130,29 @@ int asend_mg_levels(const asend_ctx* ctx);
  * power-iteration estimate of the largest eigenvalue of D^-1 A on each level
  * (D = nodal diagonal blocks).  Default 1.5; factor in (0, 2). */
 int asend_mg_set_damping(asend_ctx* ctx, double factor);
+/* Shape of the multigrid CG's outer split product (ASEND_METHOD_SPLIT), a
+ * kernel variant picked at run time (e.g. by an autotuner): the values and
+ * column indices are fed through registers, or staged through shared memory
+ * by bulk copies with G block-column groups per stage and S stages per warp.
+ * Every shape gives bit-identical results.  No counterpart in the reference
+ * (it has no GPU kernels): it tunes the kernel that replaces the products of
+ * SparseMat::vector_multiply (list_ent_meth.rs:64-79) inside
+ * conj_grad_sparse (matrix_functions.rs:285-362). */
+#define ASEND_PRODUCT_DEFAULT 0
+#define ASEND_PRODUCT_REGISTERS 1
+#define ASEND_PRODUCT_STAGED_2x3 2
+#define ASEND_PRODUCT_STAGED_3x2 3
+#define ASEND_PRODUCT_STAGED_2x2 4
+#define ASEND_PRODUCT_STAGED_4x2 5
+int asend_set_product_variant(asend_ctx* ctx, int32_t variant);
+/* Multigrid V-cycle: run the deepest levels whose every block has at most
+ * 512 nodes (one block per instance), the coarsest dense solve included, as
+ * one fused launch with one CTA per block (enable = 1, the default), or as
+ * one launch per level and step (enable = 0).  Same arithmetic either way.
+ * No counterpart in the reference (it has no multigrid); a tuning and
+ * diagnostic switch of the preconditioner that replaces the reference's
+ * block-LDL^T (lower_tri_mat_meth.rs:15-241). */
+int asend_mg_set_fused_tail(asend_ctx* ctx, int32_t enable);
 /* Level diagnostics after a multigrid solve: dims[3] = (nx, ny, nz) of the
  * level's cells, the power-iteration estimate and the guaranteed bound
  * ||D^-1 A||_inf of lambda_max(D^-1 A), and the smoother damping in use (the

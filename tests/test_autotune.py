@@ -11,16 +11,24 @@ from asend3d_gb300 import _lib, autotune
 class FakeSolver:
     """static_solve_device returns scripted (rc, ms, iterations) per precond."""
 
-    def __init__(self, table, structured=True):
+    def __init__(self, table, structured=True, product_ms=None):
         n = 4 if structured else 3
         self.p = SimpleNamespace(mesh=SimpleNamespace(elem_type=8, nx=n, ny=2, nz=2, n_elems=16))
         self.n_dof = 135
         self.n_cases = 1
         self.table = table
+        self.product_ms = product_ms or {v: 20.0 for v in _lib.PRODUCT_VARIANTS}
+        self.variant = _lib.PRODUCT_DEFAULT
         self.calls = []
 
+    def set_product_variant(self, v):
+        self.variant = v
+
     def static_solve_device(self, **o):
-        self.calls.append(o)
+        self.calls.append(dict(o, product=self.variant))
+        if o["method"] == _lib.METHOD_SPLIT:  # None: that shape's solve hits its cap
+            ms = self.product_ms[self.variant]
+            return (_lib.ASEND_MAX_ITER if ms is None else _lib.ASEND_OK), {"ms_solve": ms or 0.0, "iterations": 10}
         rc, ms, it = self.table[(o["precond"], o["graph_iters"])]
         return rc, {"ms_solve": ms, "iterations": it}
 
@@ -41,7 +49,22 @@ def test_picks_fastest_converged():
     s = FakeSolver(table())
     best, trials = autotune.tune(s)
     assert best == {"method": _lib.METHOD_FP64, "precond": _lib.PC_MG, "graph_iters": 8}
-    assert len(trials) == 12 and all(c["rel_tol"] == 1e-8 for c in s.calls)
+    assert len(trials) == 12 + len(_lib.PRODUCT_VARIANTS) and all(c["rel_tol"] == 1e-8 for c in s.calls)
+    assert s.variant == _lib.PRODUCT_DEFAULT  # restored after the trials
+
+
+def test_picks_product_shape():
+    """The split multigrid CG's outer-product shapes are candidates of their
+    own; each trial runs with its shape installed."""
+    ms = {v: 5.0 + v for v in _lib.PRODUCT_VARIANTS}
+    ms[_lib.PRODUCT_STAGED_3x2] = 0.5
+    s = FakeSolver(table(), product_ms=ms)
+    best, trials = autotune.tune(s, repeats=1)
+    assert best == {"method": _lib.METHOD_SPLIT, "precond": _lib.PC_MG, "graph_iters": 8,
+                    "product": _lib.PRODUCT_STAGED_3x2}
+    split_calls = [c for c in s.calls if c["method"] == _lib.METHOD_SPLIT]
+    assert [c["product"] for c in split_calls] == list(_lib.PRODUCT_VARIANTS)
+    assert all("product" not in t or t["method"] == _lib.METHOD_SPLIT for t in trials)
 
 
 def test_failed_candidates_are_dropped():
@@ -66,7 +89,8 @@ def test_give_up_stops_repeats_of_slow_candidates():
 
 
 def test_nothing_converges_raises():
-    s = FakeSolver(table(fail=[(pc, g) for pc in (0, 1, 3) for g in autotune.DEFAULT_GRAPH_ITERS]))
+    s = FakeSolver(table(fail=[(pc, g) for pc in (0, 1, 3) for g in autotune.DEFAULT_GRAPH_ITERS]),
+                   product_ms={v: None for v in _lib.PRODUCT_VARIANTS})
     with pytest.raises(RuntimeError, match="no candidate"):
         autotune.tune(s)
 

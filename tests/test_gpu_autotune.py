@@ -13,7 +13,7 @@ def test_tune_cantilever(gpu_lib):
     g = GpuSolver(configs.cantilever_small())
     g.assemble(precision=64)
     best, trials = autotune.tune(g, rel_tol=1e-8, repeats=1)
-    assert len(trials) == 12 and best in autotune.default_candidates(True)
+    assert len(trials) == len(autotune.default_candidates(True)) and best in autotune.default_candidates(True)
     ok = [t for t in trials if t["ms"] is not None]
     assert min(t["ms"] for t in ok) == [t for t in ok if all(t[k] == best[k] for k in best)][0]["ms"]
     rc, st = g.static_solve_device(rel_tol=1e-8, **best)

@@ -67,3 +67,56 @@ def test_mg_kernel_timing_entry(gpu_lib):
         ms, by = g.time_mg_kernel(k, _lib.METHOD_SPLIT, 3)
         assert ms > 0 and by > 0
     g.close()
+
+
+def _solve_with_each_product_shape(g, **kw):
+    """Solve + compliance gradient with every product shape (fused V-cycle
+    tail on), and with the register-fed shape and the tail off (one launch
+    per coarse level and step)."""
+    out = {}
+    runs = [(v, True) for v in _lib.PRODUCT_VARIANTS] + [(_lib.PRODUCT_REGISTERS, False)]
+    for v, tail in runs:
+        g.set_product_variant(v)
+        g.mg_set_fused_tail(tail)
+        u, rc, st = g.static_solve(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, **kw)
+        assert rc == 0, (v, tail, st)
+        L, gE, rc2, _ = g.adjoint_gradient(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, **kw)
+        assert rc2 == 0, (v, tail)
+        out[(v, tail)] = (u, st["iterations"], L, gE)
+    g.set_product_variant(_lib.PRODUCT_DEFAULT)
+    g.mg_set_fused_tail(True)
+    return out
+
+
+def _assert_identical(out):
+    u0, it0, L0, g0 = out[(_lib.PRODUCT_REGISTERS, False)]
+    for k, (u, it, L, gE) in out.items():
+        np.testing.assert_array_equal(u, u0, err_msg=f"shape, tail {k}")
+        assert it == it0 and L == L0, k
+        np.testing.assert_array_equal(gE, g0, err_msg=f"shape, tail {k}")
+
+
+def test_product_shapes_bit_identical_single_block(gpu_lib):
+    """Every shape of the multigrid CG's outer split product -- register-fed,
+    or staged through shared memory by bulk copies with 2-4 groups per stage
+    and 2-3 stages per warp -- and the fused V-cycle tail against one launch
+    per coarse level give the same bits: solution, iteration count,
+    compliance and its gradient.  40x8x8 block: slices with ragged row
+    lengths, stage counts that do not divide the slice lengths."""
+    p = configs.block_large(nx=40, ny=8, nz=8, seed=5)
+    g = GpuSolver(p)
+    g.assemble(precision=64)
+    _assert_identical(_solve_with_each_product_shape(g, rel_tol=1e-10))
+    g.close()
+
+
+def test_product_shapes_bit_identical_batched(gpu_lib):
+    """The same on a stacked batch of three uneven instances with 4 load
+    cases each (instances start on CTA boundaries; some warps of a CTA own
+    no slice at the end of the stack)."""
+    prob, node_ptr, elem_ptr, inst = configs.batch_uq(which=[3, 10, 17])
+    dims = [(q.mesh.nx, q.mesh.ny, q.mesh.nz) for q in inst]
+    g = GpuSolver(prob, instances=node_ptr, blocks=dims)
+    g.assemble(precision=64)
+    _assert_identical(_solve_with_each_product_shape(g, rel_tol=1e-10))
+    g.close()
