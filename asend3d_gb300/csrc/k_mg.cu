@@ -120,6 +120,10 @@ using namespace pcg;
 
 constexpr int kT = 128;
 inline int grid_of(int n) { return (n + kT - 1) / kT; }
+// Grid of the split method's CG kernels on a single instance: grid-stride
+// loops over 4 CTAs per SM (152 SMs) instead of one CTA per 128 rows, so the
+// last-CTA reductions sum 608 partials, not thousands.
+constexpr int kPersistCtas = 152 * 4;
 // classes up to which the first coarsening uses projected class matrices
 // (27 x 576 floats each, 62 KB)
 constexpr int kMaxChildClasses = 512;
@@ -1151,6 +1155,7 @@ __global__ void __launch_bounds__(kT) k_vc_restrict(LevelView cv, const int32_t*
 constexpr int kMaxTail = 8;       // levels a fused tail may hold
 constexpr int kTailNodes = 512;   // largest block (nodes) of a level in the tail
 constexpr int kTailThreads = 1024;
+constexpr int kTailMinBlocks = 16;  // instances a stack needs before its tail is fused
 
 struct TailLevel {
     SbView A;
@@ -1359,13 +1364,12 @@ __global__ void __launch_bounds__(kThreads) k_mg_spmv_dot_pair(MgPcg M) {
     const PcgArgs& A = M.a;
     RhsScalars* Sc = A.sc + cta_instance(A) * kMaxRhs;
     if (cta_done<1>(A, Sc)) return;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
     double d[1][1] = {{0.0}};
-    if (row < A.n_rows) {
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n_rows; row += gridDim.x * blockDim.x) {
         float Sm[1][3], Cc[1][3];
         spmv_row_split_sc<1>(row, A, A.p, Sm, Cc);
         const F2 y[3] = {two_sum(Sm[0][0], Cc[0][0]), two_sum(Sm[0][1], Cc[0][1]), two_sum(Sm[0][2], Cc[0][2])};
-        d[0][0] = pair_ap_dot(A, row, y);
+        d[0][0] += pair_ap_dot(A, row, y);
     }
     double tot[1][1];
     if (last_block_reduce<1, 1>(A, d, 0, tot) && threadIdx.x == 0) set_alpha(Sc[0], tot[0][0]);
@@ -1387,14 +1391,14 @@ __global__ void __launch_bounds__(kThreads) k_fold_pairs(MgPcg M, int all) {
     const PcgArgs& A = M.a;
     const RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (!all && !S[0].replace) return;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= A.n_rows) return;
-    F2 e[3];
-    ld_pad_pair(M.xp, row, e);
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n_rows; row += gridDim.x * blockDim.x) {
+        F2 e[3];
+        ld_pad_pair(M.xp, row, e);
 #pragma unroll
-    for (int q = 0; q < 3; ++q) A.x[3 * (size_t)row + q] += f2_dbl(e[q]);
-    const F2 z[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    st_pad_pair(M.xp, row, z);
+        for (int q = 0; q < 3; ++q) A.x[3 * (size_t)row + q] += f2_dbl(e[q]);
+        const F2 z[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        st_pad_pair(M.xp, row, z);
+    }
 }
 
 // e += alpha p, r -= alpha A p, b0 = r (FP32), |r|^2, and the level-0 first
@@ -1403,10 +1407,9 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_xr_pair(MgPcg M) {
     const PcgArgs& A = M.a;
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (cta_done<1>(A, S)) return;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
     double d[1][1] = {{0.0}};
-    if (row < A.n_rows) {
-        const F2 alpha{S[0].alpha2[0], S[0].alpha2[1]};
+    const F2 alpha{S[0].alpha2[0], S[0].alpha2[1]};
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n_rows; row += gridDim.x * blockDim.x) {
         F2 pv[3], xv[3];
         ld_pad_pair(A.p, row, pv);
         ld_pad_pair(M.xp, row, xv);
@@ -1428,7 +1431,7 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_xr_pair(MgPcg M) {
         const float* B = M.binv0 + 9 * (size_t)row;
         M.x40[row] = make_float4(B[0] * rf[0] + B[1] * rf[1] + B[2] * rf[2], B[3] * rf[0] + B[4] * rf[1] + B[5] * rf[2],
                                  B[6] * rf[0] + B[7] * rf[1] + B[8] * rf[2], 0.f);
-        d[0][0] = f2_dbl(acc);
+        d[0][0] += f2_dbl(acc);
     }
     double tot[1][1];
     if (last_block_reduce<1, 1>(A, d, 1, tot) && threadIdx.x == 0) {
@@ -1453,9 +1456,9 @@ __global__ void __launch_bounds__(kThreads) k_mg_rz_pair(MgPcg M, int mode) {
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (mode == 0 && cta_done<1>(A, S)) return;
     if (mode == 1 && !S[0].refresh) return;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
     double d[1][2] = {{0.0, 0.0}};
-    if (row < A.n_rows) {
+    const bool restart = mode == 1 && S[0].restart;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n_rows; row += gridDim.x * blockDim.x) {
         const float4 z = M.z[row];
         const float zz[3] = {z.x, z.y, z.z};
         const float2* r = reinterpret_cast<const float2*>(A.r);
@@ -1467,9 +1470,9 @@ __global__ void __launch_bounds__(kThreads) k_mg_rz_pair(MgPcg M, int mode) {
             a0 = f2_add(a0, f2_mul_f(ld_pair(r, o), zz[q]));
             if (mode == 0) a1 = f2_add(a1, f2_mul_f(ld_pair(ap, o), zz[q]));
         }
-        d[0][0] = f2_dbl(a0);
-        d[0][1] = f2_dbl(a1);
-        if (mode == 1 && S[0].restart) {
+        d[0][0] += f2_dbl(a0);
+        d[0][1] += f2_dbl(a1);
+        if (restart) {
             const F2 pz[3] = {{zz[0], 0.f}, {zz[1], 0.f}, {zz[2], 0.f}};
             st_pad_pair(A.p, row, pz);
         }
@@ -1504,16 +1507,16 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_p_pair(MgPcg M) {
     const PcgArgs& A = M.a;
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (cta_done<1>(A, S)) return;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= A.n_rows) return;
     const F2 beta{S[0].beta2[0], S[0].beta2[1]};
-    const float4 z = M.z[row];
-    F2 pv[3];
-    ld_pad_pair(A.p, row, pv);
-    pv[0] = f2_add(f2_mul(beta, pv[0]), F2{z.x, 0.f});
-    pv[1] = f2_add(f2_mul(beta, pv[1]), F2{z.y, 0.f});
-    pv[2] = f2_add(f2_mul(beta, pv[2]), F2{z.z, 0.f});
-    st_pad_pair(A.p, row, pv);
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n_rows; row += gridDim.x * blockDim.x) {
+        const float4 z = M.z[row];
+        F2 pv[3];
+        ld_pad_pair(A.p, row, pv);
+        pv[0] = f2_add(f2_mul(beta, pv[0]), F2{z.x, 0.f});
+        pv[1] = f2_add(f2_mul(beta, pv[1]), F2{z.y, 0.f});
+        pv[2] = f2_add(f2_mul(beta, pv[2]), F2{z.z, 0.f});
+        st_pad_pair(A.p, row, pv);
+    }
 }
 
 // The split product with its values and columns staged through shared memory
@@ -1527,11 +1530,9 @@ __global__ void __launch_bounds__(kThreads) k_mg_spmv_dot_staged(MgPcg M) {
     const PcgArgs& A = M.a;
     RhsScalars* Sc = A.sc + cta_instance(A) * kMaxRhs;
     if (cta_done<1>(A, Sc)) return;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    F2 y[3];
-    const bool ok = spmv_row_split_staged<G, S>(A, A.p, st_smem, y);
     double d[1][1] = {{0.0}};
-    if (row < A.n_rows) d[0][0] = pair_ap_dot(A, row, y);
+    const bool ok = split_staged_slices<G, S>(A, A.p, st_smem,
+                                              [&](int row, const F2 (&y)[3]) { d[0][0] += pair_ap_dot(A, row, y); });
     if (!ok) d[0][0] = __longlong_as_double(0x7ff8000000000000ll);
     double tot[1][1];
     if (last_block_reduce<1, 1>(A, d, 0, tot) && threadIdx.x == 0) set_alpha(Sc[0], tot[0][0]);
@@ -1684,10 +1685,9 @@ __global__ void __launch_bounds__(kThreads) k_mg_residual(MgPcg M, int init, dou
     const PcgArgs& A = M.a;
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (!init && !S[0].replace) return;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = row & 31;
     double d[1][2] = {{0.0, 0.0}};
-    if (row < A.n_rows) {
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n_rows; row += gridDim.x * blockDim.x) {
+        const int lane = row & 31;
         double y[3] = {0, 0, 0};
         const int64_t g0 = A.slice_off[row >> 5];
         const int len = A.row_len[row];
@@ -2089,7 +2089,9 @@ void build_hierarchy(Ctx& c) {
             if (mx > kTailNodes) break;
             lt = l;
         }
-        H->tail = (nl - lt >= 2 && nl - lt <= kMaxTail) ? lt : 0;
+        // only for stacks of many instances: one CTA cannot carry a lone
+        // block's small levels as fast as the grid-wide launches do
+        H->tail = (H->n_blk >= kTailMinBlocks && nl - lt >= 2 && nl - lt <= kMaxTail) ? lt : 0;
     }
     ASEND_CUDA(cudaStreamSynchronize(c.stream));
     c.mg = H;
@@ -2423,7 +2425,7 @@ double mg_time_kernel(Ctx& c, int kernel, int method, int n_launch, double* byte
     MgHierarchy& H = *c.mg;
     MgLevel& L0 = *H.L[0];
     const int n = c.A.n_rows, nd = c.n_dof;
-    const int grid = grid_of(n);
+    const int grid = (method == ASEND_METHOD_SPLIT && kernel == 0) ? std::min(grid_of(n), kPersistCtas) : grid_of(n);
     const double blocks = (double)(c.A.nnz_scalar() / 9);
     if (kernel != 0 && H.L.size() < 2) throw InputError("multigrid hierarchy has a single level");
     DArr<RhsScalars> sc;
@@ -2633,6 +2635,8 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
     // one scalar set per instance (slot 0 of kMaxRhs), persistent so the
     // captured iteration graphs stay valid across solves
     const int NI = c.n_inst > 1 ? c.n_inst : 1;
+    // a batched stack keeps one CTA per 128 rows (its reductions are per instance)
+    const int grid_cg = (split && NI == 1) ? std::min(grid, kPersistCtas) : grid;
     const size_t sc_need = sizeof(RhsScalars) * NI * kMaxRhs, tk_need = sizeof(uint32_t) * NI * 4;
     if (c.pcg_sc.n < sc_need) c.pcg_sc.alloc(sc_need);
     if (c.pcg_ctl.n < sizeof(Control)) c.pcg_ctl.alloc(sizeof(Control));
@@ -2687,8 +2691,8 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         ASEND_CUDA(cudaMemsetAsync(d_ctl, 0, sizeof(Control), c.stream));
         auto launch_residual = [&](int init) {
             if (split) {  // x64 += e first (the instances being replaced), then r = f - A64 x64
-                k_fold_pairs<<<grid, kThreads, 0, c.stream>>>(M, init);
-                k_mg_residual<true><<<grid, kThreads, 0, c.stream>>>(M, init, o.rel_tol * o.rel_tol);
+                k_fold_pairs<<<grid_cg, kThreads, 0, c.stream>>>(M, init);
+                k_mg_residual<true><<<grid_cg, kThreads, 0, c.stream>>>(M, init, o.rel_tol * o.rel_tol);
                 c.launches += 2;
             } else {
                 k_mg_residual<false><<<grid, kThreads, 0, c.stream>>>(M, init, o.rel_tol * o.rel_tol);
@@ -2700,8 +2704,8 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
                 k_mg_spmv_dot<float, float><<<grid, kThreads, 0, c.stream>>>(M);
                 k_mg_update_xr<float><<<grid, kThreads, 0, c.stream>>>(M);
             } else if (split) {
-                launch_split_product(c, M, grid);
-                k_mg_update_xr_pair<<<grid, kThreads, 0, c.stream>>>(M);
+                launch_split_product(c, M, grid_cg);
+                k_mg_update_xr_pair<<<grid_cg, kThreads, 0, c.stream>>>(M);
             } else {
                 k_mg_spmv_dot<double, double><<<grid, kThreads, 0, c.stream>>>(M);
                 k_mg_update_xr<double><<<grid, kThreads, 0, c.stream>>>(M);
@@ -2711,8 +2715,8 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
                 k_mg_rz<float><<<grid, kThreads, 0, c.stream>>>(M, 0);
                 k_mg_update_p<float><<<grid, kThreads, 0, c.stream>>>(M);
             } else if (split) {
-                k_mg_rz_pair<<<grid, kThreads, 0, c.stream>>>(M, 0);
-                k_mg_update_p_pair<<<grid, kThreads, 0, c.stream>>>(M);
+                k_mg_rz_pair<<<grid_cg, kThreads, 0, c.stream>>>(M, 0);
+                k_mg_update_p_pair<<<grid_cg, kThreads, 0, c.stream>>>(M);
             } else {
                 k_mg_rz<double><<<grid, kThreads, 0, c.stream>>>(M, 0);
                 k_mg_update_p<double><<<grid, kThreads, 0, c.stream>>>(M);
@@ -2723,7 +2727,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         auto launch_start = [&]() {
             vcycle(c, nullptr, false);
             if (mixed) k_mg_rz<float><<<grid, kThreads, 0, c.stream>>>(M, 1);
-            else if (split) k_mg_rz_pair<<<grid, kThreads, 0, c.stream>>>(M, 1);
+            else if (split) k_mg_rz_pair<<<grid_cg, kThreads, 0, c.stream>>>(M, 1);
             else k_mg_rz<double><<<grid, kThreads, 0, c.stream>>>(M, 1);
             c.launches += vcycle_launches(c) + 2;
         };
@@ -2795,7 +2799,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
             since_repl += G;
         }
         if (split) {  // the solution: x64 + e
-            k_fold_pairs<<<grid, kThreads, 0, c.stream>>>(M, 1);
+            k_fold_pairs<<<grid_cg, kThreads, 0, c.stream>>>(M, 1);
             ++c.launches;
         }
         ASEND_CUDA(cudaMemcpyAsync(h, d_sc, sc_bytes, cudaMemcpyDeviceToHost, c.stream));

@@ -380,97 +380,126 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 }
 __device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// y = A p (FP64-accurate, split values and direction) for this thread's row;
-// the CTA's rows are 32-row slices, one per warp.  Returns false in every
-// lane of a warp whose copies did not land within the wait limit (y is then
-// incomplete).  smem: SplitStage<G, S>::smem(blockDim.x) bytes, 16-aligned.
-template <int G, int S>
-__device__ __forceinline__ bool spmv_row_split_staged(const PcgArgs& A, const void* __restrict__ p,
-                                                      unsigned char* smem, F2 (&y)[3]) {
+// Persistent staged split product.  Warp w of CTA b owns the slices
+// b * W + w + j * (gridDim.x * W), j = 0, 1, ... (W warps per CTA), so thread
+// t of CTA b meets the rows b * blockDim.x + t + j * gridDim.x * blockDim.x,
+// as a grid-stride loop over rows does.  The warp's groups, slice after
+// slice, form one stream of stages: lane 0 keeps S stages in flight across
+// slice boundaries, every lane consumes them in order.  After each slice
+// the lane's row (if any) is handed to epi(row, y) with y = A p as FP32
+// pairs.  Returns false in every lane of a warp whose copies did not land
+// within the wait limit (the remaining slices are then skipped).
+// smem: SplitStage<G, S>::smem(blockDim.x) bytes, 16-aligned.
+template <int G, int S, typename Epi>
+__device__ __forceinline__ bool split_staged_slices(const PcgArgs& A, const void* __restrict__ p, unsigned char* smem,
+                                                    Epi&& epi) {
     using St = SplitStage<G, S>;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    const int sl = row >> 5;
-    float Sm[3] = {0.f, 0.f, 0.f}, Cc[3] = {0.f, 0.f, 0.f};
-    y[0] = y[1] = y[2] = F2{0.f, 0.f};
-    if ((sl << 5) >= A.n_rows) return true;  // warp-uniform: no slice for this warp
+    const int wpc = blockDim.x >> 5;
+    const int n_sl = (A.n_rows + 31) >> 5;
+    const int sl0 = blockIdx.x * wpc + warp, sl_step = gridDim.x * wpc;
+    if (sl0 >= n_sl) return true;  // warp-uniform: no slice for this warp
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + warp * S;
     unsigned char* ring = smem + St::kBar + warp * St::kWarp;
-    const int64_t g0 = A.slice_off[sl];
-    const int ng = (int)(A.slice_off[sl + 1] - g0);
-    const int len = row < A.n_rows ? A.row_len[row] : 0;
-    const int nst = (ng + G - 1) / G;
     const float4* P = reinterpret_cast<const float4*>(p);
-    auto issue = [&](int k) {  // lane 0 only
-        const int s = k % S;
-        const int cnt = min(G, ng - k * G);
-        const int64_t gk = g0 + (int64_t)k * G;
+    // producer cursor (lane 0): slice pj, its first group pg0 and group count
+    // png, next stage pk within it; issued = stages issued so far
+    int psl = sl0, pk = 0, issued = 0;
+    int64_t pg0 = 0;
+    int png = 0;
+    auto load_slice = [&](int sl) {
+        pg0 = A.slice_off[sl];
+        png = (int)(A.slice_off[sl + 1] - pg0);
+    };
+    auto issue_next = [&]() {  // lane 0: the next stage of the stream, if any
+        if (psl >= n_sl) return;
+        const int s = issued % S;
+        const int cnt = min(G, png - pk * G);
+        const int64_t gk = pg0 + (int64_t)pk * G;
         unsigned char* st = ring + s * St::kStage;
         mbar_expect_tx(bars + s, (uint32_t)cnt * (2 * St::kVal * 4 + 32 * 4));
         bulk_g2s(st, A.v32 + gk * St::kVal, cnt * St::kVal * 4, bars + s);
         bulk_g2s(st + G * St::kVal * 4, A.v32lo + gk * St::kVal, cnt * St::kVal * 4, bars + s);
         bulk_g2s(st + 2 * G * St::kVal * 4, A.col + gk * 32, cnt * 32 * 4, bars + s);
+        ++issued;
+        if (++pk * G >= png) {  // next slice of this warp
+            pk = 0;
+            psl += sl_step;
+            if (psl < n_sl) load_slice(psl);
+        }
     };
     if (lane == 0) {
 #pragma unroll
         for (int s = 0; s < S; ++s) mbar_init(bars + s, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         fence_async_shared();
-        for (int k = 0; k < min(S, nst); ++k) issue(k);
+        load_slice(psl);
+        for (int s = 0; s < S; ++s) issue_next();
     }
     __syncwarp();
-    int k = 0;
+    int used = 0;  // stages consumed
     bool ok = true;
-    for (; k < nst; ++k) {
-        const int s = k % S;
-        const bool landed = __all_sync(0xffffffffu, mbar_wait(bars + s, (uint32_t)((k / S) & 1)));
-        if (!landed) {
-            ok = false;
-            break;
-        }
-        const float* hv = reinterpret_cast<const float*>(ring + s * St::kStage);
-        const float* lv = hv + G * St::kVal;
-        const int* cv = reinterpret_cast<const int*>(lv + G * St::kVal);
-        const int cnt = min(G, ng - k * G);
-        float4 xh[G], xl[G];
-#pragma unroll
-        for (int u = 0; u < G; ++u) {
-            if (u < cnt && k * G + u < len) {
-                const int c = cv[u * 32 + lane];
-                xh[u] = P[2 * (size_t)c];
-                xl[u] = P[2 * (size_t)c + 1];
+    for (int sl = sl0; sl < n_sl && ok; sl += sl_step) {
+        const int row = sl * 32 + lane;
+        const int64_t g0 = A.slice_off[sl];
+        const int ng = (int)(A.slice_off[sl + 1] - g0);
+        const int len = row < A.n_rows ? A.row_len[row] : 0;
+        const int nst = (ng + G - 1) / G;
+        float Sm[3] = {0.f, 0.f, 0.f}, Cc[3] = {0.f, 0.f, 0.f};
+        for (int k = 0; k < nst; ++k) {
+            const int s = used % S;
+            if (!__all_sync(0xffffffffu, mbar_wait(bars + s, (uint32_t)((used / S) & 1)))) {
+                ok = false;
+                break;
             }
-        }
+            const float* hv = reinterpret_cast<const float*>(ring + s * St::kStage);
+            const float* lv = hv + G * St::kVal;
+            const int* cv = reinterpret_cast<const int*>(lv + G * St::kVal);
+            const int cnt = min(G, ng - k * G);
+            float4 xh[G], xl[G];
 #pragma unroll
-        for (int u = 0; u < G; ++u) {
-            if (u < cnt && k * G + u < len) {
-                const float* h = hv + u * St::kVal + lane;
-                const float* l = lv + u * St::kVal + lane;
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    split_term(h[(3 * a) * 32], l[(3 * a) * 32], xh[u].x, xl[u].x, Sm[a], Cc[a]);
-                    split_term(h[(3 * a + 1) * 32], l[(3 * a + 1) * 32], xh[u].y, xl[u].y, Sm[a], Cc[a]);
-                    split_term(h[(3 * a + 2) * 32], l[(3 * a + 2) * 32], xh[u].z, xl[u].z, Sm[a], Cc[a]);
+            for (int u = 0; u < G; ++u) {
+                if (u < cnt && k * G + u < len) {
+                    const int c = cv[u * 32 + lane];
+                    xh[u] = P[2 * (size_t)c];
+                    xl[u] = P[2 * (size_t)c + 1];
                 }
             }
+#pragma unroll
+            for (int u = 0; u < G; ++u) {
+                if (u < cnt && k * G + u < len) {
+                    const float* h = hv + u * St::kVal + lane;
+                    const float* l = lv + u * St::kVal + lane;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        split_term(h[(3 * a) * 32], l[(3 * a) * 32], xh[u].x, xl[u].x, Sm[a], Cc[a]);
+                        split_term(h[(3 * a + 1) * 32], l[(3 * a + 1) * 32], xh[u].y, xl[u].y, Sm[a], Cc[a]);
+                        split_term(h[(3 * a + 2) * 32], l[(3 * a + 2) * 32], xh[u].z, xl[u].z, Sm[a], Cc[a]);
+                    }
+                }
+            }
+            ++used;
+            __syncwarp();  // every lane is done reading stage s before it is refilled
+            if (lane == 0) {
+                fence_async_shared();
+                issue_next();
+            }
         }
-        __syncwarp();  // every lane is done reading stage s before it is refilled
-        if (lane == 0 && k + S < nst) {
-            fence_async_shared();
-            issue(k + S);
+        if (!ok) break;
+        if (row < A.n_rows) {
+            const F2 y[3] = {two_sum(Sm[0], Cc[0]), two_sum(Sm[1], Cc[1]), two_sum(Sm[2], Cc[2])};
+            epi(row, y);
         }
     }
     if (!ok) {
-        // stages k .. min(nst, k + S) - 1 may still be in flight: wait for them
+        // stages used .. issued - 1 may still be in flight: wait for them
         // (bounded) before the CTA can leave and its shared memory be reused
+        const int upto = __shfl_sync(0xffffffffu, issued, 0);
         if (lane == 0)
-            for (int q = k; q < min(nst, k + S); ++q) mbar_wait(bars + q % S, (uint32_t)((q / S) & 1));
+            for (int q = used; q < upto; ++q) mbar_wait(bars + q % S, (uint32_t)((q / S) & 1));
         __syncwarp();
-        return false;
     }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) y[a] = two_sum(Sm[a], Cc[a]);
-    return true;
+    return ok;
 }
 
 // Preconditioner application z = M^-1 r for one node.

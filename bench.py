@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="omit the nested batch_uq block of the default line")
     ap.add_argument("--cpu-sample-nx", type=int, default=40)
+    ap.add_argument("--product", type=int, default=0,
+                    help="--profile: shape of the split outer product (asend_set_product_variant; 0 = tune)")
     ap.add_argument("--no-size-series", action="store_true",
                     help="reference arm: skip the one-off 40/60/80-cell size series")
     ap.add_argument("--profile", action="store_true",
@@ -386,6 +388,13 @@ def run_profile(a):
     p = configs.block_large(nx=a.nx, ny=a.ny, nz=a.nz)
     g = GpuSolver(p)
     kw = dict(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, rel_tol=1e-8, graph_iters=8)
+    g.assemble(precision=64)
+    if a.product:
+        g.set_product_variant(a.product)
+    else:
+        from asend3d_gb300 import autotune
+
+        autotune.tune_product(g)
     # two benchmark steps (assembly + multigrid solve + compliance gradient):
     # the first warms the caches and graphs, the second is the one to read
     out = []

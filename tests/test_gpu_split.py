@@ -120,3 +120,30 @@ def test_product_shapes_bit_identical_batched(gpu_lib):
     g.assemble(precision=64)
     _assert_identical(_solve_with_each_product_shape(g, rel_tol=1e-10))
     g.close()
+
+
+def test_fused_tail_bit_identical_on_many_instances(gpu_lib):
+    """A stack of the sweep's 16 smallest instances (enough blocks for the
+    V-cycle's fused coarse tail, one CTA per instance): solution, iterations,
+    compliance and gradient equal those of one launch per level and step, and
+    the fused run launches fewer kernels."""
+    sizes = sorted(range(64), key=lambda k: np.prod([d + 1 for d in configs.batch_dims(k, 7)]))
+    prob, node_ptr, elem_ptr, inst = configs.batch_uq(which=sorted(sizes[:16]))
+    dims = [(q.mesh.nx, q.mesh.ny, q.mesh.nz) for q in inst]
+    g = GpuSolver(prob, instances=node_ptr, blocks=dims)
+    g.assemble(precision=64)
+    out, launches = {}, {}
+    for tail in (False, True):
+        g.mg_set_fused_tail(tail)
+        n0 = g.kernel_launches
+        u, rc, st = g.static_solve(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, rel_tol=1e-10)
+        assert rc == 0, st
+        L, gE, rc2, _ = g.adjoint_gradient(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, rel_tol=1e-10)
+        assert rc2 == 0
+        launches[tail] = g.kernel_launches - n0
+        out[tail] = (u, st["iterations"], L, gE)
+    np.testing.assert_array_equal(out[True][0], out[False][0])
+    assert out[True][1] == out[False][1] and out[True][2] == out[False][2]
+    np.testing.assert_array_equal(out[True][3], out[False][3])
+    assert launches[True] < launches[False]
+    g.close()
