@@ -72,6 +72,7 @@ SIGNATURES = [
     ("asend_mg_set_damping", c_int, [C.c_void_p, c_dbl]),
     ("asend_set_product_variant", c_int, [C.c_void_p, c_int]),
     ("asend_mg_set_fused_tail", c_int, [C.c_void_p, c_int]),
+    ("asend_set_launch_overlap", c_int, [C.c_void_p, c_int]),
     ("asend_mg_level_info", c_int, [C.c_void_p, c_int, P_int, P_dbl, P_dbl, P_dbl]),
     ("asend_mg_vcycle", c_int, [C.c_void_p, P_flt, P_flt]),
     ("asend_set_instances", c_int, [C.c_void_p, c_int, P_int]),

@@ -673,6 +673,14 @@ int asend_mg_set_fused_tail(asend_ctx* ctx, int32_t enable) {
     });
 }
 
+int asend_set_launch_overlap(asend_ctx* ctx, int32_t enable) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(enable == 0 || enable == 1, "enable must be 0 or 1");
+        c.pdl = enable != 0;
+        return ASEND_OK;
+    });
+}
+
 int asend_mg_levels(const asend_ctx* ctx) {
     const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
     return c ? mg_levels(*c) : ASEND_EINVAL;

@@ -29,6 +29,7 @@
 #include <cstring>
 #include <cmath>
 #include <memory>
+#include <utility>
 
 #include "pcg_common.cuh"
 
@@ -124,6 +125,28 @@ inline int grid_of(int n) { return (n + kT - 1) / kT; }
 // loops over 4 CTAs per SM (152 SMs) instead of one CTA per 128 rows, so the
 // last-CTA reductions sum 608 partials, not thousands.
 constexpr int kPersistCtas = 152 * 4;
+
+// Launch on the context's stream, with programmatic dependent launch when the
+// context allows it (the kernel then starts while its predecessor drains and
+// waits for it in pdl_begin(); every kernel launched here calls it first).
+template <typename... KArgs, typename... Args>
+void launch_k(const Ctx& c, void (*k)(KArgs...), int grid, int block, size_t smem, Args&&... args) {
+    if (!c.pdl) {
+        k<<<grid, block, smem, c.stream>>>(std::forward<Args>(args)...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = c.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    ASEND_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...));
+}
 // classes up to which the first coarsening uses projected class matrices
 // (27 x 576 floats each, 62 KB)
 constexpr int kMaxChildClasses = 512;
@@ -707,6 +730,7 @@ __device__ __forceinline__ void sum_lanes(float (&y)[3]) {
 
 __global__ void k_vc_smooth0(int n, const float* __restrict__ binv, const float* __restrict__ b, float4* __restrict__ x,
                              const Control* ctl) {
+    pdl_begin();
     if (ctl && ctl->all_done) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= n) return;
@@ -718,6 +742,7 @@ __global__ void k_vc_smooth0(int n, const float* __restrict__ binv, const float*
 
 __global__ void __launch_bounds__(kT) k_vc_resid(SbView A, const float* __restrict__ b, const float4* __restrict__ x,
                                                  float* __restrict__ r, const Control* ctl) {
+    pdl_begin();
     if (ctl && ctl->all_done) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= A.n_rows) return;
@@ -727,12 +752,160 @@ __global__ void __launch_bounds__(kT) k_vc_resid(SbView A, const float* __restri
     for (int a = 0; a < 3; ++a) r[3 * row + a] = b[3 * row + a] - y[a];
 }
 
+// ---------------------------------------------------------------------------
+// Staged FP32 level products (the finest level's residual and post-smoothing
+// sweep).  As the split outer product: warp w of CTA b owns the slices
+// b * W + w + j * gridDim.x * W, and the slices' FP32 values and column
+// indices stream through a per-warp ring of shared-memory stages filled by
+// cp.async.bulk and completed on mbarriers; the gathered x stays a plain
+// load.  Per row the products are summed in the order of sb_row.
+// ---------------------------------------------------------------------------
+template <int G, int S>
+struct F32Stage {
+    static constexpr int kVal = 9 * 32;                      // floats per group
+    static constexpr int kStage = G * (kVal * 4 + 32 * 4);   // bytes per stage
+    static constexpr int kWarp = S * kStage;
+    static constexpr int kBar = 128;
+    static constexpr int smem(int threads) { return kBar + (threads / 32) * kWarp; }
+    static_assert((kT / 32) * S <= kBar / 8, "one mbarrier per warp and stage must fit the barrier area");
+    static_assert(kStage % 16 == 0 && (G * kVal * 4) % 16 == 0, "bulk copies need 16-byte aligned stages");
+};
+constexpr int kVcG = 4, kVcS = 2;  // stage shape of the finest level's products
+
+template <int G, int S, typename Epi>
+__device__ __forceinline__ bool f32_staged_slices(const SbView& A, const float4* __restrict__ x, unsigned char* smem,
+                                                  Epi&& epi) {
+    using St = F32Stage<G, S>;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wpc = blockDim.x >> 5;
+    const int n_sl = (A.n_rows + 31) >> 5;
+    const int sl0 = blockIdx.x * wpc + warp, sl_step = gridDim.x * wpc;
+    if (sl0 >= n_sl) return true;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + warp * S;
+    unsigned char* ring = smem + St::kBar + warp * St::kWarp;
+    int psl = sl0, pk = 0, issued = 0;
+    int64_t pg0 = 0;
+    int png = 0;
+    auto load_slice = [&](int sl) {
+        pg0 = A.slice_off[sl];
+        png = (int)(A.slice_off[sl + 1] - pg0);
+    };
+    auto issue_next = [&]() {  // lane 0
+        if (psl >= n_sl) return;
+        const int s = issued % S;
+        const int cnt = min(G, png - pk * G);
+        const int64_t gk = pg0 + (int64_t)pk * G;
+        unsigned char* st = ring + s * St::kStage;
+        mbar_expect_tx(bars + s, (uint32_t)cnt * (St::kVal * 4 + 32 * 4));
+        bulk_g2s(st, A.v + gk * St::kVal, cnt * St::kVal * 4, bars + s);
+        bulk_g2s(st + G * St::kVal * 4, A.col + gk * 32, cnt * 32 * 4, bars + s);
+        ++issued;
+        if (++pk * G >= png) {
+            pk = 0;
+            psl += sl_step;
+            if (psl < n_sl) load_slice(psl);
+        }
+    };
+    if (lane == 0) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) mbar_init(bars + s, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fence_async_shared();
+        load_slice(psl);
+        for (int s = 0; s < S; ++s) issue_next();
+    }
+    __syncwarp();
+    int used = 0;
+    bool ok = true;
+    for (int sl = sl0; sl < n_sl && ok; sl += sl_step) {
+        const int row = sl * 32 + lane;
+        const int64_t g0 = A.slice_off[sl];
+        const int ng = (int)(A.slice_off[sl + 1] - g0);
+        const int len = row < A.n_rows ? A.row_len[row] : 0;
+        const int nst = (ng + G - 1) / G;
+        float y[3] = {0.f, 0.f, 0.f};
+        for (int k = 0; k < nst; ++k) {
+            const int s = used % S;
+            if (!__all_sync(0xffffffffu, mbar_wait(bars + s, (uint32_t)((used / S) & 1)))) {
+                ok = false;
+                break;
+            }
+            const float* hv = reinterpret_cast<const float*>(ring + s * St::kStage);
+            const int* cv = reinterpret_cast<const int*>(hv + G * St::kVal);
+            const int cnt = min(G, ng - k * G);
+            float4 p[G];
+#pragma unroll
+            for (int u = 0; u < G; ++u)
+                if (u < cnt && k * G + u < len) p[u] = x[cv[u * 32 + lane]];
+#pragma unroll
+            for (int u = 0; u < G; ++u) {
+                if (u < cnt && k * G + u < len) {
+                    const float* m = hv + u * St::kVal + lane;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a)
+                        y[a] = fmaf(m[(a * 3) * 32], p[u].x,
+                                    fmaf(m[(a * 3 + 1) * 32], p[u].y, fmaf(m[(a * 3 + 2) * 32], p[u].z, y[a])));
+                }
+            }
+            ++used;
+            __syncwarp();
+            if (lane == 0) {
+                fence_async_shared();
+                issue_next();
+            }
+        }
+        if (!ok) break;
+        if (row < A.n_rows) epi(row, y);
+    }
+    if (!ok) {
+        const int upto = __shfl_sync(0xffffffffu, issued, 0);
+        if (lane == 0)
+            for (int q = used; q < upto; ++q) mbar_wait(bars + q % S, (uint32_t)((q / S) & 1));
+        __syncwarp();
+        // poison this warp's first row: the V-cycle output turns non-finite
+        // and the solve reports it
+        const int row = sl0 * 32 + lane;
+        if (row < A.n_rows) epi(row, {__int_as_float(0x7fc00000), 0.f, 0.f});
+    }
+    return ok;
+}
+
+// r = b - A x over the level's rows (staged)
+__global__ void __launch_bounds__(kT) k_vc_resid_staged(SbView A, const float* __restrict__ b,
+                                                        const float4* __restrict__ x, float* __restrict__ r,
+                                                        const Control* ctl) {
+    pdl_begin();
+    if (ctl && ctl->all_done) return;
+    extern __shared__ __align__(128) unsigned char vc_smem[];
+    f32_staged_slices<kVcG, kVcS>(A, x, vc_smem, [&](int row, const float (&y)[3]) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) r[3 * row + a] = b[3 * row + a] - y[a];
+    });
+}
+
+// y4 = x + B^-1 (b - A x) over the level's rows (staged)
+__global__ void __launch_bounds__(kT) k_vc_post_staged(SbView A, const float* __restrict__ binv,
+                                                       const float* __restrict__ b, const float4* __restrict__ x,
+                                                       float4* __restrict__ y4, const Control* ctl) {
+    pdl_begin();
+    if (ctl && ctl->all_done) return;
+    extern __shared__ __align__(128) unsigned char vc_smem[];
+    f32_staged_slices<kVcG, kVcS>(A, x, vc_smem, [&](int row, const float (&y)[3]) {
+        const float d0 = b[3 * row] - y[0], d1 = b[3 * row + 1] - y[1], d2 = b[3 * row + 2] - y[2];
+        const float* B = binv + 9 * (size_t)row;
+        const float4 xv = x[row];
+        y4[row] = make_float4(xv.x + B[0] * d0 + B[1] * d1 + B[2] * d2, xv.y + B[3] * d0 + B[4] * d1 + B[5] * d2,
+                              xv.z + B[6] * d0 + B[7] * d1 + B[8] * d2, 0.f);
+    });
+}
+
 // Coarse-level variants with T lanes per row: a coarse level has too few
 // rows to fill the GPU with one thread each, and a row's 27 block columns
 // then form a long chain of dependent loads; T lanes split the chain.
 template <int T>
 __global__ void __launch_bounds__(kT) k_vc_resid_t(SbView A, const float* __restrict__ b, const float4* __restrict__ x,
                                                    float* __restrict__ r, const Control* ctl) {
+    pdl_begin();
     if (ctl && ctl->all_done) return;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = gt / T, t = gt % T;
@@ -749,6 +922,7 @@ template <int T>
 __global__ void __launch_bounds__(kT) k_vc_post_t(SbView A, const float* __restrict__ binv, const float* __restrict__ b,
                                                   const float4* __restrict__ x, float4* __restrict__ y4,
                                                   const Control* ctl) {
+    pdl_begin();
     if (ctl && ctl->all_done) return;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = gt / T, t = gt % T;
@@ -767,6 +941,7 @@ __global__ void __launch_bounds__(kT) k_vc_post_t(SbView A, const float* __restr
 __global__ void __launch_bounds__(kT) k_vc_post(SbView A, const float* __restrict__ binv, const float* __restrict__ b,
                                                 const float4* __restrict__ x, float4* __restrict__ y4,
                                                 const Control* ctl) {
+    pdl_begin();
     if (ctl && ctl->all_done) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= A.n_rows) return;
@@ -1003,6 +1178,7 @@ __device__ __forceinline__ void prolong_row(const LevelView& cv, const BlkDev& d
 
 __global__ void k_vc_prolong(LevelView cv, const int32_t* __restrict__ pre_fnode, int n_fine,
                              const float4* __restrict__ yc, float4* __restrict__ xf, const Control* ctl) {
+    pdl_begin();
     if (ctl && ctl->all_done) return;
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_fine) return;
@@ -1049,6 +1225,7 @@ __device__ __forceinline__ void dense_block(const BlkDev& d, const float* __rest
 __global__ void __launch_bounds__(1024) k_vc_dense(LevelView cv, const float* __restrict__ ainv,
                                                    const float* __restrict__ b, float* __restrict__ y4,
                                                    const Control* ctl) {
+    pdl_begin();
     if (ctl && ctl->all_done) return;
     __shared__ float sb[1024];
     dense_block(cv.blk[blockIdx.x], ainv, b, y4, sb);
@@ -1136,6 +1313,7 @@ __global__ void __launch_bounds__(kT) k_vc_restrict(LevelView cv, const int32_t*
                                                     const float* __restrict__ in, float* __restrict__ out,
                                                     const float* __restrict__ binv, float4* __restrict__ x4,
                                                     const Control* ctl) {
+    pdl_begin();
     if (ctl && ctl->all_done) return;
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= n_out) return;
@@ -1210,6 +1388,7 @@ __device__ __forceinline__ void tail_level_rows(const TailLevel& L, int row0, in
 }
 
 __global__ void __launch_bounds__(kTailThreads) k_vc_tail(TailArgs ta, const Control* ctl) {
+    pdl_begin();
     if (ctl && ctl->all_done) return;
     __shared__ float sb[1024];
     const int b = blockIdx.x;
@@ -1265,6 +1444,7 @@ __device__ __forceinline__ void retire_instance(const PcgArgs& A) {
 // First kernel of a captured chunk of iterations: count the instances not
 // done (all_done when none is left).
 __global__ void k_mg_count_active(MgPcg M) {
+    pdl_begin();
     const PcgArgs& A = M.a;
     int n = 0;
     for (int i = threadIdx.x; i < M.n_inst; i += blockDim.x) n += A.sc[(size_t)i * kMaxRhs].done ? 0 : 1;
@@ -1337,8 +1517,9 @@ __device__ __forceinline__ void st_pad_pair(void* p, size_t node, const F2 (&v)[
     reinterpret_cast<float4*>(p)[2 * node + 1] = make_float4(v[0].l, v[1].l, v[2].l, 0.f);
 }
 
-// Store A p of this row (pairs) and return p . A p over the row's 3 DOF.
-__device__ __forceinline__ double pair_ap_dot(const PcgArgs& A, int row, const F2 (&y)[3]) {
+// Store A p of this row (pairs) and return p . A p over the row's 3 DOF (a
+// pair: a thread sums its rows in pairs and converts to FP64 once).
+__device__ __forceinline__ F2 pair_ap_dot(const PcgArgs& A, int row, const F2 (&y)[3]) {
     F2 pv[3];
     ld_pad_pair(A.p, row, pv);
     float2* ap = reinterpret_cast<float2*>(A.ap);
@@ -1348,7 +1529,7 @@ __device__ __forceinline__ double pair_ap_dot(const PcgArgs& A, int row, const F
         st_pair(ap, 3 * (size_t)row + q, y[q]);
         acc = f2_add(acc, f2_mul(pv[q], y[q]));
     }
-    return f2_dbl(acc);
+    return acc;
 }
 
 __device__ __forceinline__ void set_alpha(RhsScalars& s, double pAp) {
@@ -1361,16 +1542,18 @@ __device__ __forceinline__ void set_alpha(RhsScalars& s, double pAp) {
 
 // The register-fed split product with the pair epilogue.
 __global__ void __launch_bounds__(kThreads) k_mg_spmv_dot_pair(MgPcg M) {
+    pdl_begin();
     const PcgArgs& A = M.a;
     RhsScalars* Sc = A.sc + cta_instance(A) * kMaxRhs;
     if (cta_done<1>(A, Sc)) return;
-    double d[1][1] = {{0.0}};
+    F2 acc{0.f, 0.f};
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n_rows; row += gridDim.x * blockDim.x) {
         float Sm[1][3], Cc[1][3];
         spmv_row_split_sc<1>(row, A, A.p, Sm, Cc);
         const F2 y[3] = {two_sum(Sm[0][0], Cc[0][0]), two_sum(Sm[0][1], Cc[0][1]), two_sum(Sm[0][2], Cc[0][2])};
-        d[0][0] += pair_ap_dot(A, row, y);
+        acc = f2_add(acc, pair_ap_dot(A, row, y));
     }
+    double d[1][1] = {{f2_dbl(acc)}};
     double tot[1][1];
     if (last_block_reduce<1, 1>(A, d, 0, tot) && threadIdx.x == 0) set_alpha(Sc[0], tot[0][0]);
 }
@@ -1388,6 +1571,7 @@ __global__ void k_zero_pairs(int n, float4* __restrict__ e) {
 // x64 += e, e = 0 for the instances whose true residual is formed next (all
 // rows when all is set)
 __global__ void __launch_bounds__(kThreads) k_fold_pairs(MgPcg M, int all) {
+    pdl_begin();
     const PcgArgs& A = M.a;
     const RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (!all && !S[0].replace) return;
@@ -1404,10 +1588,11 @@ __global__ void __launch_bounds__(kThreads) k_fold_pairs(MgPcg M, int all) {
 // e += alpha p, r -= alpha A p, b0 = r (FP32), |r|^2, and the level-0 first
 // smoothing sweep.
 __global__ void __launch_bounds__(kThreads) k_mg_update_xr_pair(MgPcg M) {
+    pdl_begin();
     const PcgArgs& A = M.a;
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (cta_done<1>(A, S)) return;
-    double d[1][1] = {{0.0}};
+    F2 rr{0.f, 0.f};
     const F2 alpha{S[0].alpha2[0], S[0].alpha2[1]};
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n_rows; row += gridDim.x * blockDim.x) {
         F2 pv[3], xv[3];
@@ -1415,7 +1600,6 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_xr_pair(MgPcg M) {
         ld_pad_pair(M.xp, row, xv);
         const float2* ap = reinterpret_cast<const float2*>(A.ap);
         float2* r = reinterpret_cast<float2*>(A.r);
-        F2 acc{0.f, 0.f};
         float rf[3];
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
@@ -1425,14 +1609,14 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_xr_pair(MgPcg M) {
             st_pair(r, o, rv);
             M.b0[o] = rv.h;
             rf[q] = rv.h;
-            acc = f2_add(acc, f2_mul(rv, rv));
+            rr = f2_add(rr, f2_mul(rv, rv));
         }
         st_pad_pair(M.xp, row, xv);
         const float* B = M.binv0 + 9 * (size_t)row;
         M.x40[row] = make_float4(B[0] * rf[0] + B[1] * rf[1] + B[2] * rf[2], B[3] * rf[0] + B[4] * rf[1] + B[5] * rf[2],
                                  B[6] * rf[0] + B[7] * rf[1] + B[8] * rf[2], 0.f);
-        d[0][0] += f2_dbl(acc);
     }
+    double d[1][1] = {{f2_dbl(rr)}};
     double tot[1][1];
     if (last_block_reduce<1, 1>(A, d, 1, tot) && threadIdx.x == 0) {
         RhsScalars& s = S[0];
@@ -1452,31 +1636,30 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_xr_pair(MgPcg M) {
 // r . z and (mode 0) A p . z in pairs, beta (Polak-Ribiere); mode 1: rz
 // after a true-residual evaluation, and p = z on a restart.
 __global__ void __launch_bounds__(kThreads) k_mg_rz_pair(MgPcg M, int mode) {
+    pdl_begin();
     const PcgArgs& A = M.a;
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (mode == 0 && cta_done<1>(A, S)) return;
     if (mode == 1 && !S[0].refresh) return;
-    double d[1][2] = {{0.0, 0.0}};
     const bool restart = mode == 1 && S[0].restart;
+    F2 a0{0.f, 0.f}, a1{0.f, 0.f};
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n_rows; row += gridDim.x * blockDim.x) {
         const float4 z = M.z[row];
         const float zz[3] = {z.x, z.y, z.z};
         const float2* r = reinterpret_cast<const float2*>(A.r);
         const float2* ap = reinterpret_cast<const float2*>(A.ap);
-        F2 a0{0.f, 0.f}, a1{0.f, 0.f};
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             const size_t o = 3 * (size_t)row + q;
             a0 = f2_add(a0, f2_mul_f(ld_pair(r, o), zz[q]));
             if (mode == 0) a1 = f2_add(a1, f2_mul_f(ld_pair(ap, o), zz[q]));
         }
-        d[0][0] += f2_dbl(a0);
-        d[0][1] += f2_dbl(a1);
         if (restart) {
             const F2 pz[3] = {{zz[0], 0.f}, {zz[1], 0.f}, {zz[2], 0.f}};
             st_pad_pair(A.p, row, pz);
         }
     }
+    double d[1][2] = {{f2_dbl(a0), f2_dbl(a1)}};
     double tot[1][2];
     if (last_block_reduce<1, 2>(A, d, 2, tot) && threadIdx.x == 0) {
         RhsScalars& s = S[0];
@@ -1504,6 +1687,7 @@ __global__ void __launch_bounds__(kThreads) k_mg_rz_pair(MgPcg M, int mode) {
 
 // p = z + beta p in pairs
 __global__ void __launch_bounds__(kThreads) k_mg_update_p_pair(MgPcg M) {
+    pdl_begin();
     const PcgArgs& A = M.a;
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (cta_done<1>(A, S)) return;
@@ -1526,13 +1710,15 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_p_pair(MgPcg M) {
 // as a non-finite breakdown.
 template <int G, int S>
 __global__ void __launch_bounds__(kThreads) k_mg_spmv_dot_staged(MgPcg M) {
+    pdl_begin();
     extern __shared__ __align__(128) unsigned char st_smem[];
     const PcgArgs& A = M.a;
     RhsScalars* Sc = A.sc + cta_instance(A) * kMaxRhs;
     if (cta_done<1>(A, Sc)) return;
-    double d[1][1] = {{0.0}};
-    const bool ok = split_staged_slices<G, S>(A, A.p, st_smem,
-                                              [&](int row, const F2 (&y)[3]) { d[0][0] += pair_ap_dot(A, row, y); });
+    F2 acc{0.f, 0.f};
+    const bool ok = split_staged_slices<G, S>(
+        A, A.p, st_smem, [&](int row, const F2 (&y)[3]) { acc = f2_add(acc, pair_ap_dot(A, row, y)); });
+    double d[1][1] = {{f2_dbl(acc)}};
     if (!ok) d[0][0] = __longlong_as_double(0x7ff8000000000000ll);
     double tot[1][1];
     if (last_block_reduce<1, 1>(A, d, 0, tot) && threadIdx.x == 0) set_alpha(Sc[0], tot[0][0]);
@@ -1541,8 +1727,8 @@ __global__ void __launch_bounds__(kThreads) k_mg_spmv_dot_staged(MgPcg M) {
 // Launch of the split outer product in one of its shapes (ASEND_PRODUCT_*):
 // register-fed, or staged with G groups per stage and S stages per warp.
 template <int G, int S>
-void launch_staged(const MgPcg& M, int grid, cudaStream_t st) {
-    k_mg_spmv_dot_staged<G, S><<<grid, kThreads, SplitStage<G, S>::smem(kThreads), st>>>(M);
+void launch_staged(const Ctx& c, const MgPcg& M, int grid) {
+    launch_k(c, k_mg_spmv_dot_staged<G, S>, grid, kThreads, SplitStage<G, S>::smem(kThreads), M);
 }
 
 // Opt the staged shapes into their dynamic shared memory (above the 48 KB
@@ -1566,11 +1752,11 @@ void product_attrs() {
 
 void launch_split_product(const Ctx& c, const MgPcg& M, int grid) {
     switch (c.product_variant) {
-        case ASEND_PRODUCT_REGISTERS: k_mg_spmv_dot_pair<<<grid, kThreads, 0, c.stream>>>(M); break;
-        case ASEND_PRODUCT_STAGED_3x2: launch_staged<3, 2>(M, grid, c.stream); break;
-        case ASEND_PRODUCT_STAGED_2x2: launch_staged<2, 2>(M, grid, c.stream); break;
-        case ASEND_PRODUCT_STAGED_4x2: launch_staged<4, 2>(M, grid, c.stream); break;
-        default: launch_staged<2, 3>(M, grid, c.stream); break;  // ASEND_PRODUCT_DEFAULT, ASEND_PRODUCT_STAGED_2x3
+        case ASEND_PRODUCT_REGISTERS: launch_k(c, k_mg_spmv_dot_pair, grid, kThreads, 0, M); break;
+        case ASEND_PRODUCT_STAGED_3x2: launch_staged<3, 2>(c, M, grid); break;
+        case ASEND_PRODUCT_STAGED_2x2: launch_staged<2, 2>(c, M, grid); break;
+        case ASEND_PRODUCT_STAGED_4x2: launch_staged<4, 2>(c, M, grid); break;
+        default: launch_staged<2, 3>(c, M, grid); break;  // ASEND_PRODUCT_DEFAULT, ASEND_PRODUCT_STAGED_2x3
     }
 }
 
@@ -1682,6 +1868,7 @@ __global__ void __launch_bounds__(kThreads) k_mg_update_p(MgPcg M) {
 // direction refresh that follows the next V-cycle.
 template <bool PAIR_R>
 __global__ void __launch_bounds__(kThreads) k_mg_residual(MgPcg M, int init, double tol2) {
+    pdl_begin();
     const PcgArgs& A = M.a;
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
     if (!init && !S[0].replace) return;
@@ -2227,7 +2414,7 @@ void restrict_to(Ctx& c, int l, const Control* ctl) {
     MgLevel& L = *H.L[l];
     MgLevel& C = *H.L[l + 1];
     const bool last = (l + 2 == (int)H.L.size());  // the coarsest level is solved directly: no sweep
-    k_vc_restrict<<<grid_of(C.n_nodes), kT, 0, c.stream>>>(view_of(C), C.pre_node.p, C.n_nodes, L.r.p, C.b.p,
+    launch_k(c, k_vc_restrict, grid_of(C.n_nodes), kT, 0, view_of(C), C.pre_node.p, C.n_nodes, L.r.p, C.b.p,
                                                            last ? nullptr : C.binv.p,
                                                            reinterpret_cast<float4*>(C.x4.p), ctl);
 }
@@ -2235,14 +2422,14 @@ void restrict_to(Ctx& c, int l, const Control* ctl) {
 void coarsest_solve(Ctx& c, const Control* ctl) {
     MgHierarchy& H = *c.mg;
     MgLevel& Lc = *H.L.back();
-    k_vc_dense<<<H.n_blk, 1024, 0, c.stream>>>(view_of(Lc), H.dense.p, Lc.b.p, Lc.y4.p, ctl);
+    launch_k(c, k_vc_dense, H.n_blk, 1024, 0, view_of(Lc), H.dense.p, Lc.b.p, Lc.y4.p, ctl);
 }
 
 void prolong_from(Ctx& c, int l, const Control* ctl) {
     MgHierarchy& H = *c.mg;
     MgLevel& L = *H.L[l];
     MgLevel& C = *H.L[l + 1];
-    k_vc_prolong<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(view_of(C), L.pre_node.p, L.n_nodes,
+    launch_k(c, k_vc_prolong, grid_of(L.n_nodes), kT, 0, view_of(C), L.pre_node.p, L.n_nodes,
                                                           reinterpret_cast<const float4*>(C.y4.p),
                                                           reinterpret_cast<float4*>(L.x4.p), ctl);
 }
@@ -2265,12 +2452,21 @@ void level_resid(Ctx& c, MgLevel& L, const Control* ctl) {
     const float4* x = reinterpret_cast<const float4*>(L.x4.p);
     const int g = (int)(((int64_t)L.n_nodes * t + kT - 1) / kT);
     switch (t) {
-        case 1: k_vc_resid<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(A, L.b.p, x, L.r.p, ctl); break;
-        case 2: k_vc_resid_t<2><<<g, kT, 0, c.stream>>>(A, L.b.p, x, L.r.p, ctl); break;
-        case 4: k_vc_resid_t<4><<<g, kT, 0, c.stream>>>(A, L.b.p, x, L.r.p, ctl); break;
-        case 8: k_vc_resid_t<8><<<g, kT, 0, c.stream>>>(A, L.b.p, x, L.r.p, ctl); break;
-        default: k_vc_resid_t<16><<<g, kT, 0, c.stream>>>(A, L.b.p, x, L.r.p, ctl); break;
+        case 1:
+            launch_k(c, k_vc_resid_staged, std::min(grid_of(L.n_nodes), kPersistCtas), kT,
+                     (size_t)F32Stage<kVcG, kVcS>::smem(kT), A, L.b.p, x, L.r.p, ctl);
+            break;
+        case 2: launch_k(c, k_vc_resid_t<2>, g, kT, 0, A, L.b.p, x, L.r.p, ctl); break;
+        case 4: launch_k(c, k_vc_resid_t<4>, g, kT, 0, A, L.b.p, x, L.r.p, ctl); break;
+        case 8: launch_k(c, k_vc_resid_t<8>, g, kT, 0, A, L.b.p, x, L.r.p, ctl); break;
+        default: launch_k(c, k_vc_resid_t<16>, g, kT, 0, A, L.b.p, x, L.r.p, ctl); break;
     }
+}
+
+void level_post(Ctx& c, MgLevel& L, const Control* ctl);
+void level_resid_or_post(Ctx& c, MgLevel& L, bool post, const Control* ctl) {
+    if (post) level_post(c, L, ctl);
+    else level_resid(c, L, ctl);
 }
 
 void level_post(Ctx& c, MgLevel& L, const Control* ctl) {
@@ -2280,11 +2476,14 @@ void level_post(Ctx& c, MgLevel& L, const Control* ctl) {
     float4* y = reinterpret_cast<float4*>(L.y4.p);
     const int g = (int)(((int64_t)L.n_nodes * t + kT - 1) / kT);
     switch (t) {
-        case 1: k_vc_post<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(A, L.binv.p, L.b.p, x, y, ctl); break;
-        case 2: k_vc_post_t<2><<<g, kT, 0, c.stream>>>(A, L.binv.p, L.b.p, x, y, ctl); break;
-        case 4: k_vc_post_t<4><<<g, kT, 0, c.stream>>>(A, L.binv.p, L.b.p, x, y, ctl); break;
-        case 8: k_vc_post_t<8><<<g, kT, 0, c.stream>>>(A, L.binv.p, L.b.p, x, y, ctl); break;
-        default: k_vc_post_t<16><<<g, kT, 0, c.stream>>>(A, L.binv.p, L.b.p, x, y, ctl); break;
+        case 1:
+            launch_k(c, k_vc_post_staged, std::min(grid_of(L.n_nodes), kPersistCtas), kT,
+                     (size_t)F32Stage<kVcG, kVcS>::smem(kT), A, L.binv.p, L.b.p, x, y, ctl);
+            break;
+        case 2: launch_k(c, k_vc_post_t<2>, g, kT, 0, A, L.binv.p, L.b.p, x, y, ctl); break;
+        case 4: launch_k(c, k_vc_post_t<4>, g, kT, 0, A, L.binv.p, L.b.p, x, y, ctl); break;
+        case 8: launch_k(c, k_vc_post_t<8>, g, kT, 0, A, L.binv.p, L.b.p, x, y, ctl); break;
+        default: launch_k(c, k_vc_post_t<16>, g, kT, 0, A, L.binv.p, L.b.p, x, y, ctl); break;
     }
 }
 
@@ -2315,7 +2514,7 @@ void launch_tail(Ctx& c, int lt, const Control* ctl) {
         T.lanes = lanes_for(L.n_nodes);
     }
     ta.ainv = H.dense.p;
-    k_vc_tail<<<H.n_blk, kTailThreads, 0, c.stream>>>(ta, ctl);
+    launch_k(c, k_vc_tail, H.n_blk, kTailThreads, 0, ta, ctl);
 }
 
 void vcycle(Ctx& c, const Control* ctl, bool fused0) {
@@ -2324,7 +2523,7 @@ void vcycle(Ctx& c, const Control* ctl, bool fused0) {
     const int lt = tail_level(c);
     if (!fused0 && nl > 1) {
         MgLevel& L = *H.L[0];
-        k_vc_smooth0<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(L.n_nodes, L.binv.p, L.b.p,
+        launch_k(c, k_vc_smooth0, grid_of(L.n_nodes), kT, 0, L.n_nodes, L.binv.p, L.b.p,
                                                               reinterpret_cast<float4*>(L.x4.p), ctl);
     }
     for (int l = 0; l < lt; ++l) {
@@ -2351,7 +2550,7 @@ void coarse_correction(Ctx& c) {
     for (int l = 0; l < nl - 1; ++l) {
         MgLevel& L = *H.L[l];
         if (l > 0)
-            k_vc_resid<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(sbview(L), L.b.p, reinterpret_cast<float4*>(L.x4.p),
+            launch_k(c, k_vc_resid, grid_of(L.n_nodes), kT, 0, sbview(L), L.b.p, reinterpret_cast<float4*>(L.x4.p),
                                                                 L.r.p, nullptr);
         restrict_to(c, l, nullptr);
     }
@@ -2361,7 +2560,7 @@ void coarse_correction(Ctx& c) {
         MgLevel& L = *H.L[l];
         prolong_from(c, l, nullptr);
         if (l > 0)
-            k_vc_post<<<grid_of(L.n_nodes), kT, 0, c.stream>>>(sbview(L), L.binv.p, L.b.p,
+            launch_k(c, k_vc_post, grid_of(L.n_nodes), kT, 0, sbview(L), L.binv.p, L.b.p,
                                                                reinterpret_cast<const float4*>(L.x4.p),
                                                                reinterpret_cast<float4*>(L.y4.p), nullptr);
     }
@@ -2463,13 +2662,8 @@ double mg_time_kernel(Ctx& c, int kernel, int method, int n_launch, double* byte
             if (method == ASEND_METHOD_MIXED) k_mg_spmv_dot<float, float><<<grid, kThreads, 0, c.stream>>>(M);
             else if (method == ASEND_METHOD_SPLIT) launch_split_product(c, M, grid);
             else k_mg_spmv_dot<double, double><<<grid, kThreads, 0, c.stream>>>(M);
-        } else if (kernel == 1) {
-            k_vc_resid<<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(sbview(L0), L0.b.p, reinterpret_cast<float4*>(L0.x4.p),
-                                                                 L0.r.p, nullptr);
-        } else {
-            k_vc_post<<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(sbview(L0), L0.binv.p, L0.b.p,
-                                                                reinterpret_cast<const float4*>(L0.x4.p),
-                                                                reinterpret_cast<float4*>(L0.y4.p), nullptr);
+        } else {  // the finest level's products as the V-cycle runs them
+            level_resid_or_post(c, L0, kernel == 2, nullptr);
         }
     };
     const double ps = (method == ASEND_METHOD_MIXED) ? 4.0 : 8.0;  // bytes per value / direction entry
@@ -2691,11 +2885,12 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         ASEND_CUDA(cudaMemsetAsync(d_ctl, 0, sizeof(Control), c.stream));
         auto launch_residual = [&](int init) {
             if (split) {  // x64 += e first (the instances being replaced), then r = f - A64 x64
-                k_fold_pairs<<<grid_cg, kThreads, 0, c.stream>>>(M, init);
-                k_mg_residual<true><<<grid_cg, kThreads, 0, c.stream>>>(M, init, o.rel_tol * o.rel_tol);
+                launch_k(c, k_fold_pairs, grid_cg, kThreads, 0, M, init);
+                // FP64-pipe bound: all 4 warps of every row tile in flight
+                launch_k(c, k_mg_residual<true>, grid, kThreads, 0, M, init, o.rel_tol * o.rel_tol);
                 c.launches += 2;
             } else {
-                k_mg_residual<false><<<grid, kThreads, 0, c.stream>>>(M, init, o.rel_tol * o.rel_tol);
+                launch_k(c, k_mg_residual<false>, grid, kThreads, 0, M, init, o.rel_tol * o.rel_tol);
                 ++c.launches;
             }
         };
@@ -2705,7 +2900,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
                 k_mg_update_xr<float><<<grid, kThreads, 0, c.stream>>>(M);
             } else if (split) {
                 launch_split_product(c, M, grid_cg);
-                k_mg_update_xr_pair<<<grid_cg, kThreads, 0, c.stream>>>(M);
+                launch_k(c, k_mg_update_xr_pair, grid_cg, kThreads, 0, M);
             } else {
                 k_mg_spmv_dot<double, double><<<grid, kThreads, 0, c.stream>>>(M);
                 k_mg_update_xr<double><<<grid, kThreads, 0, c.stream>>>(M);
@@ -2715,8 +2910,8 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
                 k_mg_rz<float><<<grid, kThreads, 0, c.stream>>>(M, 0);
                 k_mg_update_p<float><<<grid, kThreads, 0, c.stream>>>(M);
             } else if (split) {
-                k_mg_rz_pair<<<grid_cg, kThreads, 0, c.stream>>>(M, 0);
-                k_mg_update_p_pair<<<grid_cg, kThreads, 0, c.stream>>>(M);
+                launch_k(c, k_mg_rz_pair, grid_cg, kThreads, 0, M, 0);
+                launch_k(c, k_mg_update_p_pair, grid_cg, kThreads, 0, M);
             } else {
                 k_mg_rz<double><<<grid, kThreads, 0, c.stream>>>(M, 0);
                 k_mg_update_p<double><<<grid, kThreads, 0, c.stream>>>(M);
@@ -2727,7 +2922,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         auto launch_start = [&]() {
             vcycle(c, nullptr, false);
             if (mixed) k_mg_rz<float><<<grid, kThreads, 0, c.stream>>>(M, 1);
-            else if (split) k_mg_rz_pair<<<grid_cg, kThreads, 0, c.stream>>>(M, 1);
+            else if (split) launch_k(c, k_mg_rz_pair, grid_cg, kThreads, 0, M, 1);
             else k_mg_rz<double><<<grid, kThreads, 0, c.stream>>>(M, 1);
             c.launches += vcycle_launches(c) + 2;
         };
@@ -2737,10 +2932,11 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         // G iterations as one graph, kept with the hierarchy and reused while
         // the launch arguments are the same (they fully define the graph)
         // (with everything else that changes the captured sequence: the
-        // method, the chunk length, the product shape and the tail switch)
+        // method, the chunk length, the product shape, the tail switch and
+        // the launch overlap)
         std::vector<uint8_t> key(sizeof(MgPcg) + 4 * sizeof(int));
         std::memcpy(key.data(), &M, sizeof(MgPcg));
-        const int extra[4] = {o.method, G, c.product_variant, c.mg_tail ? 1 : 0};
+        const int extra[4] = {o.method, G, c.product_variant, (c.mg_tail ? 1 : 0) | (c.pdl ? 2 : 0)};
         std::memcpy(key.data() + sizeof(MgPcg), extra, sizeof(extra));
         cudaGraphExec_t exec = nullptr;
         for (auto& g : H.graphs)
@@ -2748,7 +2944,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         if (!exec) {
             cudaGraph_t graph;
             ASEND_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-            k_mg_count_active<<<1, 32, 0, c.stream>>>(M);
+            launch_k(c, k_mg_count_active, 1, 32, 0, M);
             for (int i = 0; i < G; ++i) launch_iteration();
             ASEND_CUDA(cudaStreamEndCapture(c.stream, &graph));
             ASEND_CUDA(cudaGraphInstantiate(&exec, graph, 0));
@@ -2799,7 +2995,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
             since_repl += G;
         }
         if (split) {  // the solution: x64 + e
-            k_fold_pairs<<<grid_cg, kThreads, 0, c.stream>>>(M, 1);
+            launch_k(c, k_fold_pairs, grid_cg, kThreads, 0, M, 1);
             ++c.launches;
         }
         ASEND_CUDA(cudaMemcpyAsync(h, d_sc, sc_bytes, cudaMemcpyDeviceToHost, c.stream));

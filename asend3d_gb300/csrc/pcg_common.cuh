@@ -502,6 +502,17 @@ __device__ __forceinline__ bool split_staged_slices(const PcgArgs& A, const void
     return ok;
 }
 
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream-serialization attribute may start while its predecessor in the
+// stream drains.  It first waits for the predecessor's completion and memory
+// (griddepcontrol.wait; a no-op without the attribute), then lets its own
+// successor launch early (griddepcontrol.launch_dependents), so only the
+// launch and CTA set-up overlap; every read and write comes after the wait.
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Preconditioner application z = M^-1 r for one node.
 template <int PC>
 __device__ __forceinline__ void precond(const PcgArgs& A, int row, const double (&r)[3], double (&z)[3]) {

@@ -507,6 +507,11 @@ class GpuSolver:
         launch per level and step; same arithmetic."""
         self._check(self.lib.asend_mg_set_fused_tail(self.ctx, int(bool(enable))), "mg_set_fused_tail")
 
+    def set_launch_overlap(self, enable=True):
+        """Programmatic dependent launch between the multigrid CG's kernels
+        (default on); same results either way."""
+        self._check(self.lib.asend_set_launch_overlap(self.ctx, int(bool(enable))), "set_launch_overlap")
+
     @property
     def mg_levels(self) -> int:
         return int(self.lib.asend_mg_levels(self.ctx))

@@ -153,6 +153,13 @@ int asend_set_product_variant(asend_ctx* ctx, int32_t variant);
  * diagnostic switch of the preconditioner that replaces the reference's
  * block-LDL^T (lower_tri_mat_meth.rs:15-241). */
 int asend_mg_set_fused_tail(asend_ctx* ctx, int32_t enable);
+/* Multigrid CG: launch each V-cycle and CG kernel with programmatic
+ * dependent launch (enable = 1), so that its launch and CTA set-up overlap
+ * the end of the kernel before it; every such kernel waits for its
+ * predecessor before reading or writing anything, so results do not change.
+ * enable = 0 (the default) serialises the launches: on GB300 the overlapped
+ * solve measured slower.  No counterpart in the reference (no GPU code). */
+int asend_set_launch_overlap(asend_ctx* ctx, int32_t enable);
 /* Level diagnostics after a multigrid solve: dims[3] = (nx, ny, nz) of the
  * level's cells, the power-iteration estimate and the guaranteed bound
  * ||D^-1 A||_inf of lambda_max(D^-1 A), and the smoother damping in use (the

@@ -71,13 +71,14 @@ def test_mg_kernel_timing_entry(gpu_lib):
 
 def _solve_with_each_product_shape(g, **kw):
     """Solve + compliance gradient with every product shape (fused V-cycle
-    tail on), and with the register-fed shape and the tail off (one launch
-    per coarse level and step)."""
+    tail on, overlapped launches), and with the register-fed shape, the tail
+    off (one launch per coarse level and step) and fully serialised launches."""
     out = {}
     runs = [(v, True) for v in _lib.PRODUCT_VARIANTS] + [(_lib.PRODUCT_REGISTERS, False)]
     for v, tail in runs:
         g.set_product_variant(v)
         g.mg_set_fused_tail(tail)
+        g.set_launch_overlap(tail)  # the serialised launches ride with the unfused tail
         u, rc, st = g.static_solve(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, **kw)
         assert rc == 0, (v, tail, st)
         L, gE, rc2, _ = g.adjoint_gradient(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, **kw)
@@ -85,6 +86,7 @@ def _solve_with_each_product_shape(g, **kw):
         out[(v, tail)] = (u, st["iterations"], L, gE)
     g.set_product_variant(_lib.PRODUCT_DEFAULT)
     g.mg_set_fused_tail(True)
+    g.set_launch_overlap(True)
     return out
 
 
