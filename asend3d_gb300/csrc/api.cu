@@ -1204,7 +1204,7 @@ int asend_assemble(asend_ctx* ctx, int32_t precision, int32_t dynamic, double dt
     return guarded(ctx, [&](Ctx& c) {
         NvtxRange nvtx_range("asend_assemble");
         require(c.n_el > 0, "set the mesh first");
-        require(precision == 32 || precision == 64, "precision must be 32 or 64");
+        require(precision == 32 || precision == 48 || precision == 64, "precision must be 32, 48 or 64");
         require(dynamic >= 0 && dynamic <= 2, "dynamic must be 0, 1 or 2");
         if (dynamic == 1) require(dt > 0.0 && beta != gamma, "Newmark needs dt > 0 and beta != gamma");
         if (dynamic) for (double r : c.rho) require(r > 0.0, "dynamic / modal assembly needs positive densities");
@@ -1248,6 +1248,7 @@ int asend_get_csr(asend_ctx* ctx, int32_t which, int64_t* nnz_out, int64_t* row_
         if (!row_ptr && !col && !val) return ASEND_OK;
         std::vector<double> h;
         if (val) {
+            if (which != 1 && which != 3) ensure_v64(c);
             const DArr<double>& src = (which == 1) ? A.m64 : (which == 3) ? A.d64 : A.v64;
             h.resize(src.n);
             ASEND_CUDA(cudaMemcpyAsync(h.data(), src.p, src.n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));

@@ -197,6 +197,9 @@ struct Ctx {
     bool lump = false;              // row-sum lumped mass in Newmark assemblies
     double sf = 0;
     int assembled_precision = 64;
+    // A split-only assembly (precision 48) writes the operator's FP32 hi / lo
+    // values and leaves the FP64 copy stale until ensure_v64() rebuilds it.
+    bool v64_valid = true;
     float last_assemble_ms = 0.f;
 
     // ---- pattern / assembly
@@ -208,6 +211,8 @@ struct Ctx {
     DArr<int32_t> d_cls_of;          // class of each element
     DArr<double> cls_ke, cls_me;     // [n_cls][(3 nn)^2] stiffness, [n_cls][nn nn] mass (FP64)
     DArr<float> cls_ke32;            // FP32 copy of cls_ke (multigrid coarsening)
+    DArr<float2> cls_ke2;            // cls_ke as FP32 pairs (split-only assembly)
+    DArr<float2> d_E2;               // element moduli as FP32 pairs (split-only assembly)
     DArr<int32_t> d_gat_ptr, d_gat;  // per value slot: contributing (element, a, b) entries
     bool cls_ready = false;
     DArr<int32_t> d_slot_map;  // [n_el * nn * nn] slot of block (a, b)
@@ -223,6 +228,7 @@ struct Ctx {
     DArr<float> d_p32, d_ap32;         // mixed: padded direction, A p
     DArr<double> d_p64, d_ap64;        // fp64: padded direction, A p
     DArr<float4> d_xpair;              // split multigrid CG: correction of x as node-padded FP32 pairs
+    DArr<float4> d_xtrip;              // split multigrid CG on a split-only operator: x as 3 FP32 parts
     DArr<double> d_dinv;               // point Jacobi inverse diagonal (n_dof)
     DArr<float> d_binv;                // nodal block inverse (n_nodes * b*b)
     DArr<double> d_partials;           // block partial sums
@@ -306,6 +312,10 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double* smem /* [32*K]
 
 // host-side helpers implemented in the .cu files
 void assemble_operator(Ctx& c, int precision);
+// Rebuild the FP64 operator values from the hi / lo pairs after a split-only
+// assembly (no-op otherwise); every path that reads A.v64 calls it first.
+void ensure_v64(Ctx& c);
+cudaError_t ensure_v64_rc(Ctx& c);  // the same, returning the launch status instead of throwing
 void build_classes(Ctx& c, const std::vector<int32_t>& slot_map);
 void build_pattern(Ctx& c);
 void apply_operator_device(Ctx& c, int precision, const double* d_x, double* d_y);

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "pcg_common.cuh"
 
 namespace asend {
 namespace {
@@ -519,6 +520,111 @@ k_gather_assemble(const int64_t* __restrict__ slice_off, const int32_t* __restri
     }
 }
 
+// ---------------------------------------------------------------------------
+// Split-only gather assembly (precision 48, statics): the same sums
+// K_slot = sum E_e Khat_class(e)[a, b] as k_gather_assemble, in FP32 pairs
+// (E_e and Khat as pairs, FMA-exact products, TwoSum accumulation) on the
+// FP32 pipes, written as the hi / lo values only.  On this GPU the FP64 gather
+// was bound by its FP64 sums and conversions, not by its writes.  The largest
+// |value| per instance (the penalty scale) is compared exactly on the pairs
+// and converted to FP64 once per thread.
+// ---------------------------------------------------------------------------
+__global__ void k_pairs_of(size_t n, const double* __restrict__ v, float2* __restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const pcg::F2 a = pcg::f2_of(v[i]);
+        out[i] = make_float2(a.h, a.l);
+    }
+}
+
+__device__ __forceinline__ bool pair_abs_greater(pcg::F2 a, pcg::F2 b) {  // |a| > |b| for normalised pairs
+    const float ah = fabsf(a.h), bh = fabsf(b.h);
+    if (ah != bh) return ah > bh;
+    return copysignf(1.f, a.h) * a.l > copysignf(1.f, b.h) * b.l;
+}
+
+__global__ void __launch_bounds__(256)
+k_gather_assemble_pair(const int64_t* __restrict__ slice_off, const int32_t* __restrict__ gat_ptr,
+                       const int32_t* __restrict__ gat, const int32_t* __restrict__ cls_of,
+                       const float2* __restrict__ cls_ke2, const float2* __restrict__ E2, float* __restrict__ v32,
+                       float* __restrict__ v32lo, const int32_t* __restrict__ slice_inst,
+                       unsigned long long* __restrict__ max_out) {
+    __shared__ double s_max[8];
+    const int sl = blockIdx.x, lane = threadIdx.x & 31, jj = threadIdx.x >> 5;
+    const int64_t g0 = slice_off[sl];
+    const int W = (int)(slice_off[sl + 1] - g0);
+    pcg::F2 mx{0.f, 0.f};
+    for (int j = jj; j < W; j += 8) {
+        const int64_t g = g0 + j;
+        const int64_t slot = g * 32 + lane;
+        pcg::F2 k[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) k[q] = {0.f, 0.f};
+        const int q0 = gat_ptr[slot], q1 = gat_ptr[slot + 1];
+        for (int base = q0; base < q1; base += 8) {
+            int ent[8], cl[8];
+            float2 Ee[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) ent[u] = (base + u < q1) ? gat[base + u] : -1;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                cl[u] = 0;
+                Ee[u] = make_float2(0.f, 0.f);
+                if (ent[u] >= 0) {
+                    const int e = ent[u] >> 6;
+                    cl[u] = cls_of[e];
+                    Ee[u] = E2[e];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (ent[u] < 0) continue;
+                const int a = (ent[u] >> 3) & 7, b = ent[u] & 7;
+                const float2* K = cls_ke2 + (size_t)cl[u] * 576 + (3 * a) * 24 + 3 * b;
+                const pcg::F2 E{Ee[u].x, Ee[u].y};
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int c2 = 0; c2 < 3; ++c2) {
+                        const float2 kv = K[i * 24 + c2];
+                        k[i * 3 + c2] = pcg::f2_add(k[i * 3 + c2], pcg::f2_mul(E, pcg::F2{kv.x, kv.y}));
+                    }
+            }
+        }
+        float* wb = v32 + (g * 9) * 32 + lane;
+        float* lb = v32lo + (g * 9) * 32 + lane;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            wb[q * 32] = k[q].h;
+            lb[q * 32] = k[q].l;
+            if (pair_abs_greater(k[q], mx)) mx = k[q];
+        }
+    }
+    double m = fabs(pcg::f2_dbl(mx));
+    m = warp_max(m);
+    if (lane == 0) s_max[jj] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t = fmax(t, s_max[w]);
+        atomicMax(&max_out[slice_inst ? slice_inst[sl] : 0], (unsigned long long)__double_as_longlong(t));
+    }
+}
+
+// FP64 values at the listed slots from their pairs (the penalty and unit
+// slots, before the FP64 penalty update of a split-only assembly)
+__global__ void k_slots_to64(int n, const int64_t* __restrict__ idx, const float* __restrict__ v32,
+                             const float* __restrict__ v32lo, double* __restrict__ v64) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) v64[idx[k]] = (double)v32[idx[k]] + (double)v32lo[idx[k]];
+}
+
+// every FP64 value from its pair
+__global__ void k_pairs_to64(size_t n, const float* __restrict__ v32, const float* __restrict__ v32lo,
+                             double* __restrict__ v64) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        v64[i] = (double)v32[i] + (double)v32lo[i];
+}
+
 // Row-sum lumping of the assembled mass (the reference lumps each element's
 // mass by its rows, element_equations.rs:950-971; summed over the elements
 // that is the row sum of the global mass): m := diag(row sums), and the
@@ -605,6 +711,7 @@ void build_classes(Ctx& c, const std::vector<int32_t>& slot_map) {
     c.cls_ke.release();
     c.cls_me.release();
     c.cls_ke32.release();
+    c.cls_ke2.release();
     c.d_cls_of.release();
     c.d_gat_ptr.release();
     c.d_gat.release();
@@ -735,7 +842,12 @@ void assemble_operator(Ctx& c, int precision) {
     // gather path: FP64 hex8 / brickIM with geometry classes and isotropic
     // material, no damping or lumping (every value written once, the penalty
     // scale reduced on the way)
-    const bool gather = precision == 64 && c.cls_ready && c.cls_type == c.type && c.ortho.empty() && !damp && !lump;
+    const bool gather_ok = c.cls_ready && c.cls_type == c.type && c.ortho.empty() && !damp && !lump;
+    // split-only (precision 48): statics on the class gather; anything else
+    // takes the FP64 assembly
+    const bool split_only = precision == 48 && gather_ok && !c.dynamic;
+    if (precision == 48 && !split_only) precision = 64;
+    const bool gather = precision == 64 && gather_ok;
     double* mvals = nullptr;
     if (c.dynamic) {
         A.m64.alloc(nval);
@@ -761,7 +873,7 @@ void assemble_operator(Ctx& c, int precision) {
         X.cD = c.cD;
         X.dvals = A.d64.p;
     }
-    if (!gather) {
+    if (!gather && !split_only) {  // the scatter paths accumulate into zeroed values
         A.v64.zero(c.stream);
         A.v32.zero(c.stream);
     }
@@ -770,7 +882,37 @@ void assemble_operator(Ctx& c, int precision) {
     c.d_max_partial.alloc(ni);
     c.d_max_partial.zero(c.stream);
     unsigned long long* dmax = reinterpret_cast<unsigned long long*>(c.d_max_partial.p);
-    if (gather) {
+    if (split_only) {
+        const int32_t* slice_inst = nullptr;
+        DArr<int32_t> d_si;
+        if (ni > 1) {
+            std::vector<int32_t> si(A.n_slices);
+            for (int s2 = 0; s2 < A.n_slices; ++s2) si[s2] = instance_of_node(c, s2 * kSlice);
+            d_si.upload(si, c.stream);
+            slice_inst = d_si.p;
+        }
+        const size_t n_cls_vals = (size_t)c.n_cls * 576;
+        if (c.cls_ke2.n != n_cls_vals) {
+            c.cls_ke2.alloc(n_cls_vals);
+            k_pairs_of<<<stream_grid(n_cls_vals), 256, 0, c.stream>>>(n_cls_vals, c.cls_ke.p, c.cls_ke2.p);
+            ++c.launches;
+        }
+        c.d_E2.alloc(c.n_el);
+        k_pairs_of<<<stream_grid(c.n_el), 256, 0, c.stream>>>((size_t)c.n_el, c.d_E.p, c.d_E2.p);
+        k_gather_assemble_pair<<<A.n_slices, 256, 0, c.stream>>>(A.slice_off.p, c.d_gat_ptr.p, c.d_gat.p,
+                                                                 c.d_cls_of.p, c.cls_ke2.p, c.d_E2.p, A.v32.p,
+                                                                 A.v32lo.p, slice_inst, dmax);
+        c.launches += 2;
+        ASEND_CUDA(cudaGetLastError());
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));  // d_si
+        // the FP64 penalty / unit updates below work on FP64 values at their slots
+        const int np0 = (int)c.d_pen_idx.n, nu0 = (int)c.d_unit_idx.n;
+        if (np0 > 0)
+            k_slots_to64<<<(np0 + 255) / 256, 256, 0, c.stream>>>(np0, c.d_pen_idx.p, A.v32.p, A.v32lo.p, A.v64.p);
+        if (nu0 > 0)
+            k_slots_to64<<<(nu0 + 255) / 256, 256, 0, c.stream>>>(nu0, c.d_unit_idx.p, A.v32.p, A.v32lo.p, A.v64.p);
+        c.launches += (np0 > 0) + (nu0 > 0);
+    } else if (gather) {
         const int32_t* slice_inst = nullptr;
         DArr<int32_t> d_si;
         if (ni > 1) {
@@ -864,7 +1006,7 @@ void assemble_operator(Ctx& c, int precision) {
         unit_kernel<<<(nunit + 255) / 256, 256, 0, c.stream>>>(nunit, c.d_unit_idx.p, A.v64.p);
         ++c.launches;
     }
-    if (gather) {  // FP32 copies of the entries changed after the gather
+    if (gather || split_only) {  // FP32 copies of the entries changed after the gather
         if (npen > 0)
             k_refresh32<<<(npen + 255) / 256, 256, 0, c.stream>>>(npen, c.d_pen_idx.p, A.v64.p, A.v32.p, A.v32lo.p);
         if (nunit > 0)
@@ -881,8 +1023,21 @@ void assemble_operator(Ctx& c, int precision) {
     float ms = 0.f;
     ASEND_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
     c.assembled_precision = precision;
+    c.v64_valid = !split_only;
     ++c.assembly_epoch;
     c.last_assemble_ms = ms;
 }
+
+cudaError_t ensure_v64_rc(Ctx& c) {
+    if (c.v64_valid) return cudaSuccess;
+    const size_t nval = (size_t)c.A.n_groups * 9 * kSlice;
+    k_pairs_to64<<<stream_grid(nval), 256, 0, c.stream>>>(nval, c.A.v32.p, c.A.v32lo.p, c.A.v64.p);
+    ++c.launches;
+    const cudaError_t rc = cudaGetLastError();
+    if (rc == cudaSuccess) c.v64_valid = true;
+    return rc;
+}
+
+void ensure_v64(Ctx& c) { ASEND_CUDA(ensure_v64_rc(c)); }
 
 }  // namespace asend

@@ -315,6 +315,7 @@ int sym_eigen_dense(int m, const double* a_in, double* vals, double* vecs) {
 
 int eigen_solve(Ctx& c, const asend_eigen_opts& eo, double* eig_out, double* freq_out, double* modes_out,
                 double* diag_mass_out, asend_eigen_stats* st) {
+    ensure_v64(c);
     const int n = c.n_dof, rows = c.A.n_rows;
     const int nm = eo.n_modes;
     const int b = eo.block_size > 0 ? eo.block_size : 2;

@@ -684,6 +684,7 @@ int learned_n_outputs() { return kO; }
 
 // features for the current assembly
 void learned_features(Ctx& c) {
+    ensure_v64(c);
     ensure_buffers(c);
     LearnedState& L = state(c);
     if (L.feat_epoch == c.assembly_epoch) return;

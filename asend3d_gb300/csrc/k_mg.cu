@@ -1427,6 +1427,8 @@ struct MgPcg {
     PcgArgs a;            // outer operator, x, r, p, ap, partials, sc, ctl (nrhs = 1)
     float4* xp;           // split method: the correction e of x since its last true residual,
                           // node-padded FP32 pairs (hi float4, lo float4)
+    float4* xt;           // split method on a split-only operator: x as three node-padded FP32
+                          // parts (hi, lo, remainder) for the true residual (else nullptr)
     float* b0;            // V-cycle input (level-0 rhs, FP32 r)
     const float4* z;      // V-cycle output (level-0 y4)
     const float* binv0;   // level-0 smoother blocks: the first sweep
@@ -1578,10 +1580,113 @@ __global__ void __launch_bounds__(kThreads) k_fold_pairs(MgPcg M, int all) {
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n_rows; row += gridDim.x * blockDim.x) {
         F2 e[3];
         ld_pad_pair(M.xp, row, e);
+        float t[3][3];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) A.x[3 * (size_t)row + q] += f2_dbl(e[q]);
+        for (int q = 0; q < 3; ++q) {
+            const double xv = A.x[3 * (size_t)row + q] + f2_dbl(e[q]);
+            A.x[3 * (size_t)row + q] = xv;
+            if (M.xt) {  // x = hi + lo + remainder, each FP32
+                const float h = (float)xv;
+                const double r1 = xv - (double)h;
+                const float l = (float)r1;
+                t[0][q] = h;
+                t[1][q] = l;
+                t[2][q] = (float)(r1 - (double)l);
+            }
+        }
         const F2 z[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
         st_pad_pair(M.xp, row, z);
+        if (M.xt)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) M.xt[3 * (size_t)row + k] = make_float4(t[k][0], t[k][1], t[k][2], 0.f);
+    }
+}
+
+// One term (h + l)(xh + xl + xr) of a true residual, added to a three-level
+// sum (S, C, D): S the leading sum, C the next order, D the rest.  The
+// products h xh, h xl and l xh are split exactly (FMA) and every rounding
+// error of S and C goes one level down, so only D rounds, at 2^-24 of a
+// 2^-48-sized quantity: the sum keeps about 70 bits, where the CG product's
+// two levels keep 48 (enough for a search direction, not for f - A x, whose
+// terms are 10^4 times |f| on a point-loaded cantilever).
+__device__ __forceinline__ void res_term(float h, float l, float xh, float xl, float xr, float& S, float& C,
+                                         float& D) {
+    const float p1 = __fmul_rn(h, xh), e1 = __fmaf_rn(h, xh, -p1);
+    const float p2 = __fmul_rn(h, xl), e2 = __fmaf_rn(h, xl, -p2);
+    const float p3 = __fmul_rn(l, xh), e3 = __fmaf_rn(l, xh, -p3);
+    const F2 s0 = two_sum(S, p1);
+    S = s0.h;
+    const F2 c1 = two_sum(C, s0.l);
+    const F2 c2 = two_sum(c1.h, e1);
+    const F2 c3 = two_sum(c2.h, p2);
+    const F2 c4 = two_sum(c3.h, p3);
+    C = c4.h;
+    D = __fadd_rn(D, __fadd_rn(__fadd_rn(c1.l, c2.l), __fadd_rn(c3.l, c4.l)));
+    D = __fadd_rn(D, __fadd_rn(e2, e3));
+    D = __fmaf_rn(h, xr, __fmaf_rn(l, xl, D));
+}
+
+// True residual r = f - A x from the operator's hi / lo values (split-only
+// assembly: no FP64 values) and the three FP32 parts of x written by the
+// fold, each term by res_term.
+__global__ void __launch_bounds__(kThreads) k_mg_residual_split(MgPcg M, int init, double tol2) {
+    pdl_begin();
+    const PcgArgs& A = M.a;
+    RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
+    if (!init && !S[0].replace) return;
+    F2 rr{0.f, 0.f};
+    double ff = 0.0;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n_rows; row += gridDim.x * blockDim.x) {
+        const int lane = row & 31;
+        float Sm[3] = {0.f, 0.f, 0.f}, Cc[3] = {0.f, 0.f, 0.f}, Dd[3] = {0.f, 0.f, 0.f};
+        const int64_t g0 = A.slice_off[row >> 5];
+        const int len = A.row_len[row];
+        for (int j = 0; j < len; ++j) {
+            const int64_t g = g0 + j;
+            const int c = A.col[g * 32 + lane];
+            const float4 xh = M.xt[3 * (size_t)c], xl = M.xt[3 * (size_t)c + 1], xr = M.xt[3 * (size_t)c + 2];
+            const float* hv = A.v32 + (g * 9) * 32 + lane;
+            const float* lv = A.v32lo + (g * 9) * 32 + lane;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                res_term(hv[(3 * a) * 32], lv[(3 * a) * 32], xh.x, xl.x, xr.x, Sm[a], Cc[a], Dd[a]);
+                res_term(hv[(3 * a + 1) * 32], lv[(3 * a + 1) * 32], xh.y, xl.y, xr.y, Sm[a], Cc[a], Dd[a]);
+                res_term(hv[(3 * a + 2) * 32], lv[(3 * a + 2) * 32], xh.z, xl.z, xr.z, Sm[a], Cc[a], Dd[a]);
+            }
+        }
+        float2* r = reinterpret_cast<float2*>(A.r);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const size_t o = 3 * (size_t)row + a;
+            const double f = A.f[o];
+            // f - (S + C + D): the leading cancellation against f is exact in
+            // the pairs' TwoSum; C and D enter below it
+            const F2 y = f2_add(two_sum(Sm[a], Cc[a]), F2{Dd[a], 0.f});
+            const F2 rv = f2_add(f2_of(f), f2_neg(y));
+            st_pair(r, o, rv);
+            M.b0[o] = rv.h;
+            rr = f2_add(rr, f2_mul(rv, rv));
+            if (init) ff += f * f;
+        }
+    }
+    double d[1][2] = {{f2_dbl(rr), ff}};
+    double tot[1][2];
+    if (last_block_reduce<1, 2>(A, d, 3, tot) && threadIdx.x == 0) {
+        RhsScalars& s = S[0];
+        s.rr = tot[0][0];
+        s.rr_last_true = tot[0][0];
+        if (init) {
+            s.bb = tot[0][1];
+            s.target = tol2 * s.bb;
+            s.iter = 0;
+            s.beta = 0.0;
+            s.restart = 1;
+        }
+        s.replace = 0;
+        s.refresh = 1;
+        s.nonfinite = isfinite(s.rr) ? 0 : 1;
+        s.finished = (s.rr <= s.target) || s.nonfinite;
+        s.done = s.finished;
     }
 }
 
@@ -2320,6 +2425,17 @@ void damp_smoother(Ctx& c, int l) {
 
 // per-assembly values: Galerkin element matrices, level operators, penalty,
 // smoother blocks, coarsest inverses
+// Level-0 smoother blocks (undamped D_n^-1) from the FP64 values, or from the
+// FP32 values after a split-only assembly (the smoother is FP32 either way).
+void level0_smoother_blocks(Ctx& c, MgLevel& L0) {
+    if (c.v64_valid)
+        k_smoother_blocks<double><<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(L0.n_nodes, c.A.slice_off.p, c.A.diag.p,
+                                                                            c.A.v64.p, 1.f, L0.binv.p);
+    else
+        k_smoother_blocks<float><<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(L0.n_nodes, c.A.slice_off.p, c.A.diag.p,
+                                                                           c.A.v32.p, 1.f, L0.binv.p);
+}
+
 void setup_values(Ctx& c) {
     MgHierarchy& H = *c.mg;
     const int n_lev = (int)H.L.size();
@@ -2337,8 +2453,7 @@ void setup_values(Ctx& c) {
     }
     {
         MgLevel& L0 = *H.L[0];
-        k_smoother_blocks<double><<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(L0.n_nodes, c.A.slice_off.p, c.A.diag.p,
-                                                                            c.A.v64.p, 1.f, L0.binv.p);
+        level0_smoother_blocks(c, L0);
         ++c.launches;
         if (n_lev > 1) damp_smoother(c, 0);
     }
@@ -2594,8 +2709,7 @@ void mg_select_smoother(Ctx& c, bool learned) {
         learned_blocks(c, L0.binv.p, true);
         H.l0_learned = true;
     } else if (H.l0_learned) {
-        k_smoother_blocks<double><<<grid_of(L0.n_nodes), kT, 0, c.stream>>>(L0.n_nodes, c.A.slice_off.p, c.A.diag.p,
-                                                                            c.A.v64.p, 1.f, L0.binv.p);
+        level0_smoother_blocks(c, L0);
         ++c.launches;
         damp_smoother(c, 0);
         H.l0_learned = false;
@@ -2619,6 +2733,7 @@ int mg_levels(const Ctx& c) { return c.mg ? (int)c.mg->L.size() : 0; }
 // level-0 V-cycle residual; 2: level-0 post-smoothing) and its algorithmic
 // bytes per launch.  Scratch scalars keep the kernels from exiting early.
 double mg_time_kernel(Ctx& c, int kernel, int method, int n_launch, double* bytes) {
+    ensure_v64(c);
     mg_prepare(c);
     mg_select_smoother(c, false);
     MgHierarchy& H = *c.mg;
@@ -2806,14 +2921,16 @@ int pcg_solve_mg(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool 
 namespace {
 int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool warm, const double* d_f,
                       double* d_x, int nrhs_all) {
+    const bool mixed = o.method == ASEND_METHOD_MIXED;
+    const bool split = o.method == ASEND_METHOD_SPLIT;
+    if (!split) ensure_v64(c);  // the split method runs on the hi / lo values alone
+    const bool split_only = split && !c.v64_valid;  // the true residual from the pairs too
     mg_prepare(c);
     mg_select_smoother(c, o.precond == ASEND_PC_MG_LEARNED);
     MgHierarchy& H = *c.mg;
     const int n = c.A.n_rows, nd = c.n_dof;
     const int max_it = o.max_iter > 0 ? o.max_iter : nd;
     const int G = o.graph_iters > 0 ? o.graph_iters : 8;
-    const bool mixed = o.method == ASEND_METHOD_MIXED;
-    const bool split = o.method == ASEND_METHOD_SPLIT;
     if (!warm) ASEND_CUDA(cudaMemsetAsync(d_x, 0, (size_t)nrhs_all * nd * sizeof(double), c.stream));
     c.d_r.alloc(std::max(c.d_r.n, (size_t)nrhs_all * nd));
     const int grid = grid_of(n);
@@ -2826,6 +2943,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         c.d_ap64.alloc(std::max(c.d_ap64.n, (size_t)kMaxRhs * nd));
     }
     if (split) c.d_xpair.alloc(std::max(c.d_xpair.n, (size_t)2 * n));
+    if (split_only) c.d_xtrip.alloc(std::max(c.d_xtrip.n, (size_t)3 * n));
     // one scalar set per instance (slot 0 of kMaxRhs), persistent so the
     // captured iteration graphs stay valid across solves
     const int NI = c.n_inst > 1 ? c.n_inst : 1;
@@ -2878,6 +2996,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         M.n_inst = NI;
         if (split) {  // the split method's correction e (FP32 pairs) starts at zero
             M.xp = c.d_xpair.p;
+            M.xt = split_only ? c.d_xtrip.p : nullptr;
             k_zero_pairs<<<(2 * n + kThreads - 1) / kThreads, kThreads, 0, c.stream>>>(n, M.xp);
             ++c.launches;
         }
@@ -2886,8 +3005,10 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
         auto launch_residual = [&](int init) {
             if (split) {  // x64 += e first (the instances being replaced), then r = f - A64 x64
                 launch_k(c, k_fold_pairs, grid_cg, kThreads, 0, M, init);
-                // FP64-pipe bound: all 4 warps of every row tile in flight
-                launch_k(c, k_mg_residual<true>, grid, kThreads, 0, M, init, o.rel_tol * o.rel_tol);
+                if (split_only)
+                    launch_k(c, k_mg_residual_split, grid, kThreads, 0, M, init, o.rel_tol * o.rel_tol);
+                else  // FP64-pipe bound: all 4 warps of every row tile in flight
+                    launch_k(c, k_mg_residual<true>, grid, kThreads, 0, M, init, o.rel_tol * o.rel_tol);
                 c.launches += 2;
             } else {
                 launch_k(c, k_mg_residual<false>, grid, kThreads, 0, M, init, o.rel_tol * o.rel_tol);

@@ -157,6 +157,7 @@ __global__ void k_probe(const double* __restrict__ u, int dof, double* __restric
 
 int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* amp, int probe, double* probe_hist,
                 double* u_final, asend_solve_stats* st) {
+    ensure_v64(c);
     const int n = c.n_dof;
     const double dt = c.dt, beta = c.beta, gamma = c.gamma;
     const double c1 = 1.0 / (dt * dt * (beta - gamma));

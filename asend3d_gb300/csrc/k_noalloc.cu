@@ -143,6 +143,11 @@ extern "C" int asend_operator_energy_noalloc(asend_ctx* ctx, const double* d_x, 
         return ASEND_ECUDA;
     }
     const int blocks = (c->A.n_rows + kNaThreads - 1) / kNaThreads;
+    rc = ensure_v64_rc(*c);  // after a split-only assembly: the FP64 values from the pairs (no allocation)
+    if (rc != cudaSuccess) {
+        c->err = cudaGetErrorString(rc);
+        return ASEND_ECUDA;
+    }
     k_energy_noalloc<<<blocks, kNaThreads, 0, c->stream>>>(c->A.n_rows, c->A.slice_off.p, c->A.row_len.p,
                                                             c->A.col.p, c->A.v64.p, d_x, d_y, d_energy, sc);
     rc = cudaGetLastError();

@@ -380,6 +380,7 @@ struct Launcher {
 // Device-side y = A x (natural layout), value precision 32, 64 or 48 (the
 // split FP32 hi + lo product, FP64-accurate).
 void apply_operator_device(Ctx& c, int precision, const double* d_x, double* d_y) {
+    ensure_v64(c);
     PcgArgs a{};
     a.n_rows = c.A.n_rows;
     a.nrhs = 1;
@@ -429,6 +430,7 @@ void apply_operator_device(Ctx& c, int precision, const double* d_x, double* d_y
 // algorithmic bytes: values + column indices + one read of the direction +
 // one write of A p.
 double time_spmv(Ctx& c, int precision, int n_launch, double* bytes) {
+    ensure_v64(c);
     const int n = c.A.n_rows;
     PcgArgs a{};
     a.n_rows = n;
@@ -480,8 +482,9 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
     if (!(o.rel_tol > 0.0)) throw InputError("rel_tol must be positive");
     if (o.precond == ASEND_PC_MG || o.precond == ASEND_PC_MG_LEARNED) {
         if (o.precond == ASEND_PC_MG_LEARNED && !learned_ready(c)) throw InputError("no learned weights");
-        return pcg_solve_mg(c, o, st, warm, d_f, d_x, nrhs_all);
+        return pcg_solve_mg(c, o, st, warm, d_f, d_x, nrhs_all);  // keeps a split-only operator as pairs
     }
+    ensure_v64(c);
     int pc = o.precond;
     bool use_learned = false;
     if (pc == ASEND_PC_LEARNED) {

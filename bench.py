@@ -96,11 +96,11 @@ def batch_measure(steps: int, warmup: int, plain: bool = True, accuracy: bool = 
     o_adj = g.opts(**best)
     from asend3d_gb300 import autotune
 
-    g.assemble(precision=64)
+    g.assemble(precision=48)
     shape, _ = autotune.tune_product(g)
 
     def step():
-        g.assemble(precision=64)
+        g.assemble(precision=48)
         rc, st = g.static_solve_device(**best)
         Lc = C.c_double(0)
         s2 = _lib.SolveStats()
@@ -124,7 +124,7 @@ def batch_measure(steps: int, warmup: int, plain: bool = True, accuracy: bool = 
     launches = (g.kernel_launches - launches0) // max(steps, 1)
     value = n_real * n_cases / (ms / 1e3)
     out = {"value": value, "unit": UNIT, "ms_per_step": ms, "steps": steps, "warmup": warmup,
-           "dtype": "f64 (fp32 hi+lo operator values) + f64 dots + f32 multigrid",
+           "dtype": "fp32-pair operator values and CG vectors (FP64-accurate), f64 x / reductions / true residual, f32 multigrid",
            "data": "synthetic (seeded lognormal fields)",
            "config": {"workload": "batch_uq: 64 uneven hex8 cantilevers nx in [20,120], ny=nz in [4,16], 4 load "
                                   "cases each (256 right-hand sides), batched multigrid CG + compliance gradients",
@@ -155,9 +155,10 @@ def batch_measure(steps: int, warmup: int, plain: bool = True, accuracy: bool = 
         acc = {}
         try:
             rel = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))
-            g.assemble(precision=64)
+            g.assemble(precision=48)  # the benchmark's operator and solve
             u8, _, _ = g.static_solve(**best)
             L8, gE8, _, _ = g.adjoint_gradient(**best)
+            g.assemble(precision=64)  # the FP64 reference
             tight = dict(best, method=_lib.METHOD_FP64, rel_tol=1e-11, max_iter=400)
             u11, rc11, st11 = g.static_solve(**tight)
             L11, gE11, _, _ = g.adjoint_gradient(**tight)
@@ -388,7 +389,7 @@ def run_profile(a):
     p = configs.block_large(nx=a.nx, ny=a.ny, nz=a.nz)
     g = GpuSolver(p)
     kw = dict(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, rel_tol=1e-8, graph_iters=8)
-    g.assemble(precision=64)
+    g.assemble(precision=48)
     if a.product:
         g.set_product_variant(a.product)
     else:
@@ -400,7 +401,7 @@ def run_profile(a):
     out = []
     for _ in range(2):
         n0 = g.kernel_launches
-        g.assemble(precision=64)
+        g.assemble(precision=48)
         rc, st = g.static_solve_device(**kw)
         L, _, rc2, st2 = g.adjoint_gradient(want_dLdE=False, **kw)
         out.append({"rc": rc, "rc_adjoint": rc2, "iterations": st["iterations"], "ms_solve": st["ms_solve"],
@@ -648,7 +649,7 @@ def run_ours(a):
     mixed = dict(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, rel_tol=1e-8, graph_iters=8)
 
     def step_device():
-        g.assemble(precision=64)
+        g.assemble(precision=48)
         rc, st = g.static_solve_device(**mixed)
         L, rc2, st2 = adjoint_nocopy()
         return rc, st
@@ -667,7 +668,7 @@ def run_ours(a):
     # results; the kernel alone is timed per shape)
     from asend3d_gb300 import autotune
 
-    g.assemble(precision=64)
+    g.assemble(precision=48)
     shape, shape_ms = autotune.tune_product(g)
 
     # ---- warm-up
@@ -709,7 +710,7 @@ def run_ours(a):
         g.lib.asend_set_modulus(g.ctx, C.cast(E_h.data_ptr(), P))
         g.lib.asend_clear_loads(g.ctx)
         g.lib.asend_add_load_vector(g.ctx, 0, C.cast(f_h.data_ptr(), P))
-        g.lib.asend_assemble(g.ctx, 64, 0, 0.0, 0.25, 0.5)
+        g.lib.asend_assemble(g.ctx, 48, 0, 0.0, 0.25, 0.5)
         st = _lib.SolveStats()
         rc = g.lib.asend_static_solve(g.ctx, C.byref(o_e2e), C.cast(u_h.data_ptr(), P), C.byref(st))
         Lc = C.c_double(0)
@@ -790,9 +791,10 @@ def run_ours(a):
     accuracy = {}
     if rank == 0:
         try:
-            g.assemble(precision=64)
+            g.assemble(precision=48)  # the benchmark's operator and solve
             u8, _, _ = g.static_solve(**mixed)
             L8, gE8, _, _ = g.adjoint_gradient(**mixed)
+            g.assemble(precision=64)  # the FP64 reference
             tight = dict(mixed, method=_lib.METHOD_FP64, rel_tol=1e-11, max_iter=400)
             u11, rc11, st11 = g.static_solve(**tight)
             L11, gE11, _, _ = g.adjoint_gradient(**tight)
@@ -822,7 +824,7 @@ def run_ours(a):
                 batch = {"error": repr(err)[:300]}
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f64 (fp32 hi+lo operator values) + f64 dots + f32 multigrid",
+               "vs_baseline": None, "dtype": "fp32-pair operator values and CG vectors (FP64-accurate), f64 x / reductions / true residual, f32 multigrid",
                "data": "synthetic (seeded lognormal field)",
                "config": {"workload": f"block_large {a.nx}x{a.ny}x{a.nz} hex8 static + adjoint",
                           "n_dof": n_dof, "n_elems": n_el, "rhs_per_step": 1,

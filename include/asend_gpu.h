@@ -243,7 +243,12 @@ int asend_get_load_vector(asend_ctx* ctx, int32_t rhs, double* f_out);
  *      model_prep.rs:556-618, 881-952; element loop model_analysis.rs:179-201;
  *      element kernels element_equations.rs:206-418 / 852-1062) ------------
  * precision: 64 = FP64 element integration (FP32 copy made by rounding),
- *            32 = FP32 element integration (FP64 copy made by widening).
+ *            32 = FP32 element integration (FP64 copy made by widening),
+ *            48 = FP64-accurate values as FP32 hi + lo pairs only, summed in
+ *                 FP32-pair arithmetic (static hex8 / brickIM meshes on the
+ *                 geometry-class gather; otherwise as 64): the operator for
+ *                 ASEND_METHOD_SPLIT solves.  The FP64 copy is rebuilt from
+ *                 the pairs by the first call that needs it.
  * dynamic = 1 assembles K + c_M M with c_M = -1/(dt^2 (beta - gamma)) and
  * keeps M (Newmark, element_equations.rs:977-988); dynamic = 2 assembles K
  * and keeps M apart (modal analysis; dt, beta, gamma unused). */

@@ -149,3 +149,46 @@ def test_fused_tail_bit_identical_on_many_instances(gpu_lib):
     np.testing.assert_array_equal(out[True][3], out[False][3])
     assert launches[True] < launches[False]
     g.close()
+
+
+def test_split_only_assembly(gpu_lib):
+    """precision 48: the operator's hi / lo values summed in FP32 pairs, with
+    no FP64 copy.  The split multigrid solve on it (true residuals from the
+    pairs) reaches 1e-10 and its solution, compliance and gradient match the
+    solve on the FP64 assembly; the FP64 copy rebuilt on demand (CSR export,
+    an FP64 solve) equals the FP64 assembly's values to 1e-13 of max|K| on
+    every slot without a penalty term, and to 2^-46 of the value on the
+    penalty slots (K + sf C^T C with sf = 1e5 max|K|, held as a 48-bit pair
+    in either assembly)."""
+    p = configs.block_large(nx=40, ny=8, nz=8, seed=5)
+    g = GpuSolver(p)
+    kw = dict(method=_lib.METHOD_SPLIT, precond=_lib.PC_MG, rel_tol=1e-10)
+    g.assemble(precision=64)
+    rp0, c0, v0 = g.csr(which=0)
+    rp2, c2, w0 = g.csr(which=2)
+    u64, rc, st = g.static_solve(**kw)
+    assert rc == 0
+    L64, g64, _, _ = g.adjoint_gradient(**kw)
+    g.assemble(precision=48)
+    u48, rc, st48 = g.static_solve(**kw)
+    assert rc == 0 and st48["rel_residual"] <= 1e-10, st48
+    L48, g48, rc2, _ = g.adjoint_gradient(**kw)
+    assert rc2 == 0
+    assert rel(u48, u64) < 1e-9
+    assert L48 == pytest.approx(L64, rel=1e-9)
+    assert rel(g48, g64) < 1e-8
+    kmax = np.abs(w0).max()
+    rp2b, c2b, w48 = g.csr(which=2)  # rebuilds the FP64 values from the pairs
+    np.testing.assert_array_equal(rp2b, rp2)
+    np.testing.assert_array_equal(c2b, c2)
+    rp0b, c0b, v48 = g.csr(which=0)
+    np.testing.assert_array_equal(c0b, c0)
+    np.testing.assert_array_equal(c0, c2)
+    pen = v0 != w0  # slots holding K + sf C^T C: a pair carries K there only to 2^-48 of sf
+    assert pen.any() and not pen.all()
+    assert np.abs(w48 - w0)[~pen].max() <= 1e-13 * kmax
+    assert np.all(np.abs(v48 - v0)[pen] <= 2.0 ** -46 * np.abs(v0)[pen])
+    # an FP64 solve after a split-only assembly runs on the rebuilt values
+    uf, rcf, _ = g.static_solve(method=_lib.METHOD_FP64, precond=_lib.PC_MG, rel_tol=1e-10)
+    assert rcf == 0 and rel(uf, u64) < 1e-9
+    g.close()
