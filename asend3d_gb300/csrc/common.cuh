@@ -339,7 +339,7 @@ int instance_of_node(const Ctx& c, int node);
 bool orthotropic_cmat(const double* props9, double* C36);
 double row_penalty_scale(const Ctx& c, int row);
 // multigrid (k_mg.cu)
-void mg_prepare(Ctx& c);
+void mg_prepare(Ctx& c, bool learned = false);  // learned: the finest smoother comes from the learned model
 void mg_invalidate_values(Ctx& c);
 void mg_level_info(Ctx& c, int level, int32_t* dims, double* lam_est, double* lam_bound, double* omega);
 void mg_vcycle_host(Ctx& c, const float* b, float* z);

@@ -103,6 +103,7 @@ struct MgHierarchy {
     int64_t epoch = -1;
     float omega = 0.6f;           // damping used when the eigenvalue estimate fails
     bool l0_learned = false;      // finest-level smoother blocks come from the learned model
+    bool l0_damped = false;       // finest-level eigenvalue-damped blocks are current
     DArr<float> pow_nrm;          // power-iteration norms per level [levels][kPowSteps + 1]
     DArr<uint32_t> pow_ticket;    // last-CTA tickets per level and step
     DArr<double> pow_part;        // per-CTA partial sums
@@ -2436,7 +2437,10 @@ void level0_smoother_blocks(Ctx& c, MgLevel& L0) {
                                                                            c.A.v32.p, 1.f, L0.binv.p);
 }
 
-void setup_values(Ctx& c) {
+// Per-assembly multigrid values.  skip_l0: the solve takes its finest-level
+// smoother blocks from the learned model, so the finest level's eigenvalue
+// estimate (its power iteration, the largest of the set-up) is not made.
+void setup_values(Ctx& c, bool skip_l0) {
     MgHierarchy& H = *c.mg;
     const int n_lev = (int)H.L.size();
     H.pow_nrm.alloc((size_t)n_lev * (kPowSteps + 1));
@@ -2451,12 +2455,13 @@ void setup_values(Ctx& c) {
         if (c.n_inst > 1 && (int)c.sf_inst.size() == H.n_blk) sf = c.sf_inst;
         H.blk_sf.upload(sf, c.stream);
     }
-    {
+    if (!skip_l0) {
         MgLevel& L0 = *H.L[0];
         level0_smoother_blocks(c, L0);
         ++c.launches;
         if (n_lev > 1) damp_smoother(c, 0);
     }
+    H.l0_damped = !skip_l0;
     for (size_t l = 1; l < H.L.size(); ++l) {
         MgLevel& L = *H.L[l];
         MgLevel& F = *H.L[l - 1];
@@ -2689,11 +2694,11 @@ void mg_invalidate_values(Ctx& c) {
     if (c.mg) c.mg->epoch = -1;
 }
 
-void mg_prepare(Ctx& c) {
+void mg_prepare(Ctx& c, bool learned) {
     product_attrs();
     if (!c.mg) build_hierarchy(c);
     if (c.mg->epoch != c.assembly_epoch) {
-        setup_values(c);
+        setup_values(c, learned);
         c.mg->l0_learned = false;
     }
 }
@@ -2708,11 +2713,12 @@ void mg_select_smoother(Ctx& c, bool learned) {
     if (learned) {
         learned_blocks(c, L0.binv.p, true);
         H.l0_learned = true;
-    } else if (H.l0_learned) {
+    } else if (H.l0_learned || !H.l0_damped) {
         level0_smoother_blocks(c, L0);
         ++c.launches;
-        damp_smoother(c, 0);
+        if (H.L.size() > 1) damp_smoother(c, 0);
         H.l0_learned = false;
+        H.l0_damped = true;
     }
 }
 
@@ -2925,7 +2931,7 @@ int pcg_solve_mg_once(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, 
     const bool split = o.method == ASEND_METHOD_SPLIT;
     if (!split) ensure_v64(c);  // the split method runs on the hi / lo values alone
     const bool split_only = split && !c.v64_valid;  // the true residual from the pairs too
-    mg_prepare(c);
+    mg_prepare(c, o.precond == ASEND_PC_MG_LEARNED);
     mg_select_smoother(c, o.precond == ASEND_PC_MG_LEARNED);
     MgHierarchy& H = *c.mg;
     const int n = c.A.n_rows, nd = c.n_dof;

@@ -50,13 +50,10 @@ def train_on_fresh_fields(solver: GpuSolver, n_fields: int, seed: int = 100, ite
     if iters is None:
         iters = MG_ITERS if objective == _lib.LEARN_MG else BLOCK_ITERS
     if init_seed is not None:
-        solver.learned_init(init_seed)
         if objective == _lib.LEARN_MG:
-            # start from the damped smoother M = 0.5 D^-1 (zero output is the
-            # undamped block Jacobi, not a smoother on stiff grids)
-            w = solver.learned_params()
-            w[-8:-5] = 0.5 * np.log(0.5)
-            solver.set_learned_params(w)
+            solver.set_learned_params(initial_weights(solver, init_seed))
+        else:
+            solver.learned_init(init_seed)
     solver.learned_set_objective(objective)
     log = TrainLog()
     t0 = time.perf_counter()
@@ -72,6 +69,43 @@ def train_on_fresh_fields(solver: GpuSolver, n_fields: int, seed: int = 100, ite
     log.seconds = time.perf_counter() - t0
     log.fields = n_fields
     return log
+
+
+def initial_weights(solver: GpuSolver, init_seed: int = 0) -> np.ndarray:
+    """The weights multigrid-smoother training starts from: the network's
+    initialisation with the output bias set so that every block is the damped
+    smoother 0.5 D^-1 (zero output would be the undamped block Jacobi, not a
+    smoother on stiff grids).  The untrained network of a comparison."""
+    solver.learned_init(init_seed)
+    w = solver.learned_params()
+    w[-8:-5] = 0.5 * np.log(0.5)
+    return w
+
+
+def timed_eval(solver: GpuSolver, seeds, runs, rel_tol=1e-8, sigma_log=0.5, corr_abs=0.1, median=70e9,
+               max_iter=0) -> dict:
+    """For each held-out field seed and each run (name, method, precond,
+    weights or None): install the weights, re-assemble (FP64) and solve.
+    Returns {name: [{iterations, ms_solve, ms_total, status, rel_residual}]};
+    ms_solve is the library's device time of the iterations, ms_total the
+    host wall time of assembly, preconditioner set-up (eigenvalue estimates
+    or network inference) and solve together."""
+    m = solver.p.mesh
+    out = {r[0]: [] for r in runs}
+    for s in seeds:
+        solver.set_modulus(lognormal_modulus(m, median, sigma_log, corr_abs / m.lx, s))
+        for name, method, pc, weights in runs:
+            if weights is not None:
+                solver.set_learned_params(weights)
+            t0 = time.perf_counter()
+            solver.assemble(64)
+            rc, st = solver.static_solve_device(method=method, precond=pc, rel_tol=rel_tol, max_iter=max_iter,
+                                                graph_iters=8)
+            t1 = time.perf_counter()
+            out[name].append({"iterations": int(st["iterations"]), "ms_solve": float(st["ms_solve"]),
+                              "ms_total": 1e3 * (t1 - t0), "status": int(rc),
+                              "rel_residual": float(st["rel_residual"])})
+    return out
 
 
 def patch_solver(nx=32, ny=16, nz=16, full=(128, 64, 64), device=0) -> GpuSolver:

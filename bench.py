@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--nz", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="omit the nested batch_uq block of the default line")
+    ap.add_argument("--no-learned", action="store_true", help="omit the nested learned block of the default line")
     ap.add_argument("--cpu-sample-nx", type=int, default=40)
     ap.add_argument("--product", type=int, default=0,
                     help="--profile: shape of the split outer product (asend_set_product_variant; 0 = tune)")
@@ -69,6 +70,54 @@ def parse():
                          "shell_plate (200x200 shell4 plate, 2000 Newmark steps) or modal (10 lowest "
                          "eigenpairs of the 200x40x40 block)")
     return ap.parse_args()
+
+
+def learned_measure(n_train: int = 2000, n_eval: int = 2) -> dict:
+    """The learned preconditioner at its configuration's scale: the network
+    (16 -> 64 -> 64 -> 8 per node, BF16 weights, FP32 accumulation) trained on
+    the GPU by the library's own kernels on n_train fresh seeded lognormal
+    fields (sigma_log 0.5, correlation 0.05 of the bar) of a 16x8x8 patch with
+    the element size of the 128x64x64 grid, then evaluated on n_eval held-out
+    fields of the 128x64x64 grid (1.6 M DOF) to 1e-8: plain FP64 point-Jacobi
+    PCG, the multigrid CG with eigenvalue-damped finest smoothing, and the
+    same multigrid CG with network-predicted finest smoother blocks, untrained
+    and trained.  ms_total is assembly + preconditioner set-up + solve."""
+    from asend3d_gb300 import _lib, configs
+    from asend3d_gb300 import learned as LN
+    from asend3d_gb300.solver import GpuSolver
+
+    tr = GpuSolver(configs.learned_patch(16, 8, 8))
+    w0 = LN.initial_weights(tr, 0)
+    log = LN.train_on_fresh_fields(tr, n_fields=n_train, seed=1000)
+    w = tr.learned_params()
+    tr.close()
+    ev = GpuSolver(configs.learned_patch(128, 64, 64))
+    runs = [("plain_fp64_jacobi", _lib.METHOD_FP64, _lib.PC_JACOBI, None),
+            ("mg_eigen_damped", _lib.METHOD_SPLIT, _lib.PC_MG, None),
+            ("mg_learned_untrained", _lib.METHOD_SPLIT, _lib.PC_MG_LEARNED, w0),
+            ("mg_learned", _lib.METHOD_SPLIT, _lib.PC_MG_LEARNED, w)]
+    seeds = [95001 + k for k in range(n_eval)]
+    ev.set_learned_params(w)
+    LN.timed_eval(ev, seeds[:1], runs[1:])  # warm-up: hierarchy, graphs
+    t = LN.timed_eval(ev, seeds, runs, max_iter=20000)
+    n_dof = ev.n_dof
+    ev.close()
+    out = {"config": {"workload": "learned: 128x64x64 hex8 grid, lognormal E (median 70 GPa, sigma_log 0.5, "
+                                  "correlation 0.05 of the bar), held-out fields, rel_tol 1e-8",
+                      "n_dof": n_dof, "train_fields": n_train, "train_patch": "16x8x8 (same element size)",
+                      "train_seconds": log.seconds, "eval_fields": n_eval}}
+    for name, rows in t.items():
+        out[name] = {"iterations": [r["iterations"] for r in rows], "ms_total": [r["ms_total"] for r in rows],
+                     "ms_solve": [r["ms_solve"] for r in rows], "status": [r["status"] for r in rows],
+                     "rel_residual": [r["rel_residual"] for r in rows]}
+    mean = lambda k, f: float(np.mean(out[k][f]))
+    out["gain_trained_vs_untrained"] = {"iterations": mean("mg_learned_untrained", "iterations") /
+                                        mean("mg_learned", "iterations"),
+                                        "wall": mean("mg_learned_untrained", "ms_total") / mean("mg_learned", "ms_total")}
+    out["speedup_vs_plain_fp64_jacobi"] = mean("plain_fp64_jacobi", "ms_total") / mean("mg_learned", "ms_total")
+    out["vs_eigen_damped"] = {"iterations": mean("mg_eigen_damped", "iterations") / mean("mg_learned", "iterations"),
+                              "wall": mean("mg_eigen_damped", "ms_total") / mean("mg_learned", "ms_total")}
+    return out
 
 
 def batch_measure(steps: int, warmup: int, plain: bool = True, accuracy: bool = True) -> dict:
@@ -822,6 +871,12 @@ def run_ours(a):
                 batch = batch_measure(steps=3, warmup=2)
             except Exception as err:  # the headline measurement stands on its own
                 batch = {"error": repr(err)[:300]}
+        learned = None
+        if not a.no_learned and world == 1:
+            try:
+                learned = learned_measure()
+            except Exception as err:  # the headline measurement stands on its own
+                learned = {"error": repr(err)[:300]}
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "fp32-pair operator values and CG vectors (FP64-accurate), f64 x / reductions / true residual, f32 multigrid",
@@ -839,7 +894,7 @@ def run_ours(a):
                                      "iterations": st_plain["iterations"]},
                "speedup_vs_plain_fp64": value / plain_value,
                "roofline": roof, "cpu_baseline": cb, "clocks": clocks, "gpu_launches": launches,
-               "accuracy": accuracy, "batch_uq": batch}
+               "accuracy": accuracy, "batch_uq": batch, "learned": learned}
         print(json.dumps(out))
     g.close()
     if world > 1:

@@ -15,7 +15,8 @@ import pytest
 import scipy.sparse as sp
 
 from asend3d_gb300 import _lib, configs
-from asend3d_gb300.learned import BLOCK, LEARNED, MG, MG_LEARNED, PLAIN, evaluate, train_on_fresh_fields
+from asend3d_gb300.learned import (BLOCK, LEARNED, MG, MG_LEARNED, PLAIN, evaluate, initial_weights, timed_eval,
+                                   train_on_fresh_fields)
 from asend3d_gb300.solver import GpuSolver
 from oracle import learned_oracle as lo
 
@@ -153,17 +154,23 @@ def test_vcycle_loss_gradient_matches_finite_differences(gpu_lib):
 
 def test_training_gains(gpu_lib):
     """Train on fresh fields of a patch, evaluate on held-out fields of a
-    larger mesh with the same element size.  Shown: the block objective's
-    loss falls over training; the trained multigrid smoother converges to 1e-8 in at most 10% more
-    iterations than the eigenvalue-damped block-Jacobi smoother and in more
-    than 10x fewer than the plain Jacobi PCG; the learned PCG blocks converge
-    with the Jacobi fallback untouched.  The iteration counts are printed: on
-    these fields the trained smoother ties the eigenvalue-damped one and the
-    learned PCG blocks do not beat point Jacobi."""
+    larger mesh with the same element size.  Asserted: the multigrid CG with
+    the trained network's finest-level smoother blocks converges to 1e-8 on
+    every held-out field within 10% of the iterations of the same solver with
+    the eigenvalue-damped smoother (whose finest power iteration it replaces)
+    and of the untrained network (0.5 D^-1 blocks), and in more than 10x fewer
+    iterations and less wall time than the plain Jacobi PCG; the learned PCG
+    blocks converge with the Jacobi fallback as the judge.  Not asserted,
+    because it does not hold on these fields: a gain of the trained network
+    over the untrained one -- a fixed 0.5 D^-1 block smoother is already as
+    good as the eigenvalue-damped one here (the bench's learned block shows
+    the same at 1.6 M DOF after 2,000 training fields).  The numbers are
+    printed."""
     tr = GpuSolver(configs.learned_patch(16, 8, 8))
     # multigrid objective: its samples are residuals left by stationary
     # V-cycles with the current smoother, so the loss tracks the contraction
     # of the smoother's slowest modes and need not fall as training proceeds
+    w0 = initial_weights(tr, 0)
     log = train_on_fresh_fields(tr, n_fields=80, seed=1000)
     assert np.all(np.isfinite(log.losses))
     w_mg = tr.learned_params()
@@ -172,18 +179,27 @@ def test_training_gains(gpu_lib):
     w_blk = tr.learned_params()
     tr.close()
     ev = GpuSolver(configs.learned_patch(32, 16, 16))
+    seeds = [90001, 90002]
     ev.set_learned_params(w_blk)
-    res = evaluate(ev, seeds=[90001, 90002], methods=[PLAIN, BLOCK, LEARNED])
-    ev.set_learned_params(w_mg)
-    res.update(evaluate(ev, seeds=[90001, 90002], methods=[MG, MG_LEARNED]))
-    ev.close()
+    res = evaluate(ev, seeds=seeds, methods=[PLAIN, BLOCK, LEARNED])
     for k, v in res.items():
         assert all(r[2] == _lib.ASEND_OK for r in v), (k, v)
         assert all(r[3] <= 1e-8 for r in v), (k, v)
+    t = timed_eval(ev, seeds, [("mg", _lib.METHOD_SPLIT, _lib.PC_MG, None),
+                               ("mg_learned_untrained", _lib.METHOD_SPLIT, _lib.PC_MG_LEARNED, w0),
+                               ("mg_learned", _lib.METHOD_SPLIT, _lib.PC_MG_LEARNED, w_mg)])
+    ev.close()
+    for k, v in t.items():
+        assert all(r["status"] == _lib.ASEND_OK and r["rel_residual"] <= 1e-8 for r in v), (k, v)
     it = {k: np.array([r[0] for r in v]) for k, v in res.items()}
-    print({k: v.tolist() for k, v in it.items()})
+    it.update({k: np.array([r["iterations"] for r in v]) for k, v in t.items()})
+    ms = {k: np.array([r["ms_total"] for r in v]) for k, v in t.items()}
+    print({k: v.tolist() for k, v in it.items()}, {k: np.round(v, 2).tolist() for k, v in ms.items()})
     assert np.all(it["mg_learned"] <= 1.1 * it["mg"])
+    assert np.all(it["mg_learned"] <= 1.1 * it["mg_learned_untrained"])
     assert np.all(10 * it["mg_learned"] < it["jacobi"])
+    ms_jacobi = np.array([r[1] for r in res["jacobi"]])
+    assert np.all(ms["mg_learned"] < ms_jacobi)
 
 
 def test_fallback_without_weights_and_on_nonfinite_blocks(gpu_lib):
