@@ -142,6 +142,8 @@ struct Ctx {
     float mg_damping = 1.5f;  // smoother omega = mg_damping / lambda_max(D^-1 A)
     int product_variant = 0;  // split outer product: ASEND_PRODUCT_* (0 = the default shape)
     bool mg_tail = true;      // multigrid: fuse the V-cycle's smallest levels into one launch
+    bool time_solves = true;  // record CUDA events around each PCG solve (off inside Newmark runs)
+    int64_t dinv_epoch = -1;  // assembly whose point-Jacobi diagonal d_dinv holds
     bool pdl = false;         // multigrid CG: programmatic dependent launch between its kernels
                               // (off: measured slower on GB300, 12.3 vs 11.3 ms per solve)
     std::shared_ptr<LearnedState> learned;  // learned nodal preconditioner blocks

@@ -196,6 +196,12 @@ int newmark_run(Ctx& c, const asend_solve_opts& o, int n_steps, const double* am
     ASEND_CUDA(cudaEventCreate(&e0));
     ASEND_CUDA(cudaEventCreate(&e1));
     ASEND_CUDA(cudaEventRecord(e0, c.stream));
+    struct TimeSolves {  // per-solve event timing off for the run (restored on every exit)
+        Ctx& c;
+        bool saved;
+        ~TimeSolves() { c.time_solves = saved; }
+    } time_guard{c, c.time_solves};
+    c.time_solves = false;
     for (int s = 0; s < n_steps; ++s) {
         k_dyn_residual<<<g_rows, 128, 0, c.stream>>>(rows, n, c.A.slice_off.p, c.A.row_len.p, c.A.col.p, c.A.v64.p,
                                                       c.A.m64.p, c.cM, amp[s], d_f0.p, d_pen.p, u.p, a.p, rhs.p,
@@ -295,6 +301,12 @@ int newmark_adjoint(Ctx& c, const asend_solve_opts& o, int n_obj, const int32_t*
     int iters = 0, status = 0;
     double relmax = 0.0;
     ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
+    struct TimeSolves {  // per-solve event timing off for the sweep (restored on every exit)
+        Ctx& c;
+        bool saved;
+        ~TimeSolves() { c.time_solves = saved; }
+    } time_guard{c, c.time_solves};
+    c.time_solves = false;
     for (int s = N - 1; s >= 0; --s) {
         const bool first = (s == N - 1);
         if (!first) {

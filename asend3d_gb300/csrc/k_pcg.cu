@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(kThreads) k_update_p(PcgArgs A) {
 template <typename TP, int NR, int PC>
 __global__ void __launch_bounds__(kThreads) k_residual(PcgArgs A, int mode, double tol2) {
     RhsScalars* S = A.sc + cta_instance(A) * kMaxRhs;
-    if (mode == 1 && A.cta_inst) {  // nothing to replace in this instance
+    if (mode == 1) {  // nothing to replace in this instance (the same answer in all its CTAs)
         bool any = false;
 #pragma unroll
         for (int k = 0; k < NR; ++k) any |= (S[k].replace != 0);
@@ -259,6 +259,21 @@ __global__ void __launch_bounds__(kThreads) k_residual(PcgArgs A, int mode, doub
             all &= s.done;
         }
         if (!A.cta_inst) A.ctl->all_done = all;
+    }
+}
+
+// Device-side replacement request, captured at the end of each graph chunk:
+// every right-hand side whose recurrence converged (or, mixed method, dropped
+// far below its last true residual: both set done) but that is not finished
+// gets its true residual formed by the k_residual(mode 1) that follows, with
+// no host round trip.
+__global__ void k_mark_replace(RhsScalars* sc, int n_slots, int nr) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_slots || q % kMaxRhs >= nr) return;
+    RhsScalars& s = sc[q];
+    if (s.done && !s.finished && !s.nonfinite) {
+        s.replace = 1;
+        s.n_repl += 1;
     }
 }
 
@@ -372,6 +387,11 @@ struct Launcher {
         else if (method == ASEND_METHOD_SPLIT) dispatch_nr<SplitP>(false, mode, tol2);
         else dispatch_nr<double>(false, mode, tol2);
         c.launches += 1;
+    }
+    // end of a graph chunk: replacement requests and the true residuals they ask for
+    void chunk_tail(int n_slots) {
+        k_mark_replace<<<(n_slots + 127) / 128, 128, 0, c.stream>>>(a.sc, n_slots, nr);
+        residual(1, 0.0);
     }
 };
 
@@ -517,8 +537,12 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
     c.d_partials.alloc((size_t)grid * kMaxRhs * 3);
     // preconditioner
     if (pc == ASEND_PC_JACOBI) {
-        c.d_dinv.alloc(nd);
-        k_jacobi<<<grid, kThreads, 0, c.stream>>>(n, c.A.slice_off.p, c.A.diag.p, c.A.v64.p, c.d_dinv.p);
+        if (c.dinv_epoch != c.assembly_epoch || c.d_dinv.n != (size_t)nd) {  // once per assembly
+            c.d_dinv.alloc(nd);
+            k_jacobi<<<grid, kThreads, 0, c.stream>>>(n, c.A.slice_off.p, c.A.diag.p, c.A.v64.p, c.d_dinv.p);
+            ++c.launches;
+            c.dinv_epoch = c.assembly_epoch;
+        }
     } else {
         c.d_binv.alloc((size_t)9 * n);
         if (use_learned) {
@@ -528,7 +552,6 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
             ++c.launches;
         }
     }
-    if (pc == ASEND_PC_JACOBI) ++c.launches;
     const bool mixed = o.method == ASEND_METHOD_MIXED;
     if (mixed) {
         c.d_p32.alloc((size_t)kMaxRhs * 4 * n);
@@ -553,7 +576,7 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
     const size_t sc_bytes = sizeof(RhsScalars) * NI * kMaxRhs;
     int iters_max = 0, repl_total = 0, status = 0;
     double relres_max = 0.0;
-    ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
+    if (c.time_solves) ASEND_CUDA(cudaEventRecord(c.ev0, c.stream));
     for (int r0 = 0; r0 < nrhs_all; r0 += kMaxRhs) {
         const int nr = std::min(kMaxRhs, nrhs_all - r0);
         Launcher L{c, PcgArgs{}, o.method, pc, nr};
@@ -601,14 +624,25 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
             cudaGraph_t graph;
             ASEND_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
             for (int i = 0; i < G; ++i) L.iteration();
+            L.chunk_tail(NI * kMaxRhs);
             ASEND_CUDA(cudaStreamEndCapture(c.stream, &graph));
             ASEND_CUDA(cudaGraphInstantiate(&c.graph, graph, 0));
             ASEND_CUDA(cudaGraphDestroy(graph));
             c.graph_key = key;
         }
         cudaGraphExec_t exec = c.graph;
+        // One host check per graph chunk: the chunk ends with the device-side
+        // replacement of converged recurrences, so a typical solve (or a
+        // Newmark step) is the initial residual, one chunk and one check.
         int since_repl = 0;
+        bool chunk = true;
         for (;;) {
+            if (chunk) {
+                ASEND_CUDA(cudaGraphLaunch(exec, c.stream));
+                c.launches += 3 * G + 2;
+                since_repl += G;
+            }
+            chunk = true;
             ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc_p, sc_bytes, cudaMemcpyDeviceToHost, c.stream));
             ASEND_CUDA(cudaStreamSynchronize(c.stream));
             bool all_finished = true, any_replace = false, any_nonfinite = false;
@@ -620,10 +654,7 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
                 if (s.nonfinite) { any_nonfinite = true; continue; }
                 if (s.finished) continue;
                 all_finished = false;
-                const bool conv = s.done != 0;
-                const bool drop = mixed && s.rr < 1e-4 * s.rr_last_true;
-                const bool periodic = o.replace_every > 0 && since_repl >= o.replace_every;
-                if (conv || drop || periodic) {
+                if (o.replace_every > 0 && since_repl >= o.replace_every) {  // periodic, on request
                     s.replace = 1;
                     any_replace = true;
                 }
@@ -636,29 +667,28 @@ int pcg_solve(Ctx& c, const asend_solve_opts& o, asend_solve_stats* st, bool war
                 L.residual(1, 0.0);
                 ++repl_total;
                 since_repl = 0;
-                continue;  // re-check (a replaced RHS may now be finished)
+                chunk = false;  // re-check (a replaced RHS may now be finished)
             }
-            ASEND_CUDA(cudaGraphLaunch(exec, c.stream));
-            c.launches += 3 * G;
-            since_repl += G;
         }
-        ASEND_CUDA(cudaMemcpyAsync(h_sc, d_sc_p, sc_bytes, cudaMemcpyDeviceToHost, c.stream));
-        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        // h_sc holds the scalars read at the loop's last check
         for (int q = 0; q < NI * kMaxRhs; ++q) {
             if (q % kMaxRhs >= nr) continue;
             const RhsScalars& s = h_sc[q];
             iters_max = std::max(iters_max, (int)s.iter);
+            repl_total += s.n_repl;
             if (s.bb == 0.0) continue;  // empty load case of this instance
             relres_max = std::max(relres_max, std::sqrt(s.rr_last_true / s.bb));
             if (s.nonfinite) status = ASEND_NONFINITE;
             else if (!s.finished) status = std::max(status, (int)ASEND_MAX_ITER);
         }
     }
-    ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
-    ASEND_CUDA(cudaEventSynchronize(c.ev1));
-    ASEND_CUDA(cudaGetLastError());
     float ms = 0.f;
-    ASEND_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    if (c.time_solves) {  // (a Newmark run times its whole loop instead)
+        ASEND_CUDA(cudaEventRecord(c.ev1, c.stream));
+        ASEND_CUDA(cudaEventSynchronize(c.ev1));
+        ASEND_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    }
+    ASEND_CUDA(cudaGetLastError());
     c.last_method = o.method;
     if (st) {
         st->iterations = iters_max;

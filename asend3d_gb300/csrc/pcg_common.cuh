@@ -16,7 +16,7 @@ struct RhsScalars {
     int32_t iter, done, finished, replace, nonfinite;
     int32_t restart;  // done by convergence: that iteration's p update was skipped
     int32_t refresh;  // multigrid CG: rz (and p when restarting) to be re-formed after a V-cycle
-    int32_t pad2;
+    int32_t n_repl;   // true-residual replacements made on the device (Jacobi / block PCG)
     float alpha2[2], beta2[2];  // alpha and beta as FP32 pairs (the split method's vector updates)
 };
 struct Control {
