@@ -2566,8 +2566,12 @@ int lanes_for(int n_rows) {
     return t;
 }
 
+// Levels with at least this many node rows run the staged (bulk-copy) row
+// products, one row per lane; smaller ones split each row over T lanes.
+constexpr int kStagedRows = 8192;
+
 void level_resid(Ctx& c, MgLevel& L, const Control* ctl) {
-    const int t = lanes_for(L.n_nodes);
+    const int t = L.n_nodes >= kStagedRows ? 1 : lanes_for(L.n_nodes);
     const SbView A = sbview(L);
     const float4* x = reinterpret_cast<const float4*>(L.x4.p);
     const int g = (int)(((int64_t)L.n_nodes * t + kT - 1) / kT);
@@ -2590,7 +2594,7 @@ void level_resid_or_post(Ctx& c, MgLevel& L, bool post, const Control* ctl) {
 }
 
 void level_post(Ctx& c, MgLevel& L, const Control* ctl) {
-    const int t = lanes_for(L.n_nodes);
+    const int t = L.n_nodes >= kStagedRows ? 1 : lanes_for(L.n_nodes);
     const SbView A = sbview(L);
     const float4* x = reinterpret_cast<const float4*>(L.x4.p);
     float4* y = reinterpret_cast<float4*>(L.y4.p);
