@@ -36,6 +36,7 @@ int nodes_per_elem(int type) {
         case 4: return 4;
         case 10: return 10;
         case 41: return 4;
+        case 2: return 2;
         default: return 0;
     }
 }
@@ -442,7 +443,8 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
                    const double* rho, const double* thickness) {
     return guarded(ctx, [&](Ctx& c) {
         const int nn = nodes_per_elem(elem_type);
-        require(nn > 0, "unsupported element type (supported: 8 hex8, 81 brickIM, 4 tet4, 10 tet10, 41 shell4)");
+        require(nn > 0,
+                "unsupported element type (supported: 8 hex8, 81 brickIM, 4 tet4, 10 tet10, 41 shell4, 2 beam2)");
         require(n_nodes > 0 && n_elems > 0 && coords && conn && E && nu, "empty or null mesh input");
         for (int64_t k = 0; k < (int64_t)n_elems * nn; ++k)
             require(conn[k] >= 0 && conn[k] < n_nodes, "connectivity refers to a node out of range");
@@ -450,7 +452,15 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
             require(std::isfinite(E[e]) && E[e] > 0.0, "element modulus must be positive and finite");
             require(nu[e] > -1.0 && nu[e] < 0.5, "Poisson ratio out of range (-1, 0.5)");
         }
-        const bool shell = elem_type == 41;
+        const bool shell = elem_type == 41, beam = elem_type == 2;
+        if (beam) {
+            require(n_nodes <= (1 << 29), "too many beam nodes");
+            for (int e = 0; e < n_elems; ++e) {
+                const double* x0 = coords + 3 * (size_t)conn[2 * (size_t)e];
+                const double* x1 = coords + 3 * (size_t)conn[2 * (size_t)e + 1];
+                require(x0[0] != x1[0] || x0[1] != x1[1] || x0[2] != x1[2], "beam2 element of zero length");
+            }
+        }
         if (shell) {
             require(n_nodes <= (1 << 29), "too many shell nodes");
             require(thickness != nullptr, "shell4 elements need a thickness per element");
@@ -466,22 +476,24 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         c.dpn = 3;
         c.n_unodes = n_nodes;
         c.n_el = n_elems;
-        if (shell) {
-            // two internal 3-DOF nodes per shell node: DOF 6 n + c stays the caller's numbering
-            c.nn = 8;
+        if (shell || beam) {
+            // two internal 3-DOF nodes per shell / beam node: DOF 6 n + c stays
+            // the caller's numbering
+            const int np = shell ? 4 : 2;  // physical nodes per element
+            c.nn = 2 * np;
             c.udpn = 6;
-            c.nip = 4;
+            c.nip = shell ? 4 : 2;
             c.n_nodes = 2 * n_nodes;
             c.xyz.resize((size_t)6 * n_nodes);
             for (int i = 0; i < n_nodes; ++i)
                 for (int j = 0; j < 3; ++j)
                     c.xyz[6 * (size_t)i + j] = c.xyz[6 * (size_t)i + 3 + j] = coords[3 * (size_t)i + j];
-            c.conn.resize((size_t)n_elems * 8);
-            for (size_t k = 0; k < (size_t)n_elems * 4; ++k) {
+            c.conn.resize((size_t)n_elems * 2 * np);
+            for (size_t k = 0; k < (size_t)n_elems * np; ++k) {
                 c.conn[2 * k] = 2 * conn[k];
                 c.conn[2 * k + 1] = 2 * conn[k] + 1;
             }
-            std::vector<int32_t> c4(conn, conn + (size_t)n_elems * 4);
+            std::vector<int32_t> c4(conn, conn + (size_t)n_elems * np);
             std::vector<double> x3(coords, coords + (size_t)3 * n_nodes);
             c.d_shell_conn.upload(c4, c.stream);
             c.d_shell_xyz.upload(x3, c.stream);
@@ -524,6 +536,8 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         c.shell_layered = false;
         c.d_shell_abd.release();
         c.d_shell_msec.release();
+        c.beam_sec.clear();
+        c.d_beam_sec.release();
         c.d_xyz.upload(c.xyz, c.stream);
         c.d_conn.upload(c.conn, c.stream);
         c.d_E.upload(c.E, c.stream);
@@ -572,7 +586,7 @@ int asend_set_block_structure(asend_ctx* ctx, int32_t nx, int32_t ny, int32_t nz
 int asend_set_instances(asend_ctx* ctx, int32_t n_inst, const int32_t* node_ptr) {
     return guarded(ctx, [&](Ctx& c) {
         require(c.n_nodes > 0, "set the mesh first");
-        require(c.type != 41, "batched instances take solid meshes");
+        require(c.type != 41 && c.type != 2, "batched instances take solid meshes");
         require(n_inst >= 1 && node_ptr, "need at least one instance");
         require(node_ptr[0] == 0 && node_ptr[n_inst] == c.n_nodes, "node_ptr must span all nodes");
         for (int i = 0; i < n_inst; ++i) {
@@ -819,6 +833,36 @@ int asend_set_shell_sections(asend_ctx* ctx, const double* abd, const double* ms
     });
 }
 
+int asend_set_beam_sections(asend_ctx* ctx, const double* sections) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.type == 2, "beam sections take beam2 meshes");
+        require(sections != nullptr, "null section table");
+        for (int e = 0; e < c.n_el; ++e) {
+            const double* s = sections + (size_t)e * 10;
+            for (int k = 0; k < 10; ++k) require(std::isfinite(s[k]), "beam section values must be finite");
+            require(s[0] > 0.0 && s[3] > 0.0 && s[4] > 0.0 && s[6] > 0.0,
+                    "beam section: area, I3, I4 and J must be positive");
+            // the frame: v must not lie along the element axis
+            const int n0 = c.conn[(size_t)e * 4], n1 = c.conn[(size_t)e * 4 + 2];
+            double d[3], cr[3];
+            for (int j = 0; j < 3; ++j) d[j] = c.xyz[3 * (size_t)n1 + j] - c.xyz[3 * (size_t)n0 + j];
+            const double* v = s + 7;
+            cr[0] = d[1] * v[2] - d[2] * v[1];
+            cr[1] = d[2] * v[0] - d[0] * v[2];
+            cr[2] = d[0] * v[1] - d[1] * v[0];
+            const double nc = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+            const double nd = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            const double nv = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            require(nc > 1e-9 * nd * nv, "beam section direction v lies along the element axis");
+        }
+        c.beam_sec.assign(sections, sections + (size_t)c.n_el * 10);
+        c.d_beam_sec.upload(c.beam_sec, c.stream);
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        c.assembled = c.solved = false;
+        return ASEND_OK;
+    });
+}
+
 int asend_set_orthotropic(asend_ctx* ctx, const double* props) {
     return guarded(ctx, [&](Ctx& c) {
         require(c.n_el > 0, "set the mesh first");
@@ -1026,6 +1070,24 @@ int asend_add_surface_pressure(asend_ctx* ctx, int32_t rhs, int32_t elem_set, co
 // without the mass matrix.  Returns the number of physical nodes; dof[a] is
 // node a's first translational DOF; cent the mean of the node coordinates.
 static int element_node_weights(const Ctx& c, int e, double* w, int64_t* dof, double* cent) {
+    if (c.type == 2) {  // beam2: rho A L / 2 per node on the translations
+        require(c.beam_sec.size() == (size_t)c.n_el * 10, "beam2 meshes need asend_set_beam_sections");
+        const double* s = &c.beam_sec[(size_t)e * 10];
+        require(s[1] == 0.0 && s[2] == 0.0,
+                "body loads on beam sections with first moments (I1, I2 != 0) are not built");
+        double x[2][3], l2 = 0.0;
+        for (int a = 0; a < 2; ++a) {
+            const int pn = c.conn[(size_t)e * 4 + 2 * a];
+            for (int j = 0; j < 3; ++j) x[a][j] = c.xyz[3 * (size_t)pn + j];
+            dof[a] = (int64_t)(pn / 2) * 6;
+        }
+        for (int j = 0; j < 3; ++j) {
+            l2 += (x[1][j] - x[0][j]) * (x[1][j] - x[0][j]);
+            cent[j] = 0.5 * (x[0][j] + x[1][j]);
+        }
+        w[0] = w[1] = 0.5 * s[0] * std::sqrt(l2);
+        return 2;
+    }
     if (c.type == 41) {
         if (c.shell_layered) throw InputError("body loads on layered shell sections are not built");
         double x[4][3];
@@ -1755,9 +1817,11 @@ int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t compone
 
 int asend_element_matrices(asend_ctx* ctx, int32_t first, int32_t count, double* ke, double* me) {
     return guarded(ctx, [&](Ctx& c) {
-        require(c.type == 41 || c.type == 81, "element matrix export is available for shell4 and brickIM meshes");
+        require(c.type == 41 || c.type == 81 || c.type == 2,
+                "element matrix export is available for shell4, brickIM and beam2 meshes");
         require(first >= 0 && count > 0 && (int64_t)first + count <= c.n_el && ke, "bad element range");
         if (c.type == 41) shell_element_matrices(c, first, count, ke, me);
+        else if (c.type == 2) beam_element_matrices(c, first, count, ke, me);
         else brickim_element_matrices(c, first, count, ke, me);
         return ASEND_OK;
     });

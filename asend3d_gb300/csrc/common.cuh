@@ -177,8 +177,11 @@ struct Ctx {
     // ---- device mesh
     DArr<double> d_xyz, d_E, d_nu, d_rho, d_thk;
     DArr<int32_t> d_conn;
-    DArr<int32_t> d_shell_conn;  // shell4: 4 physical nodes per element
-    DArr<double> d_shell_xyz;    // shell4: physical node coordinates
+    DArr<int32_t> d_shell_conn;  // shell4 / beam2: physical nodes per element (4 / 2)
+    DArr<double> d_shell_xyz;    // shell4 / beam2: physical node coordinates
+    // beam2 sections [n_el][10]: area, I1..I5, polar moment J, xy-plane direction
+    std::vector<double> beam_sec;
+    DArr<double> d_beam_sec;
     // shell4 layered sections: per-element ABD [n_el][81] and section mass
     // [n_el][36] replacing the isotropic E, nu, t section
     bool shell_layered = false;
@@ -361,6 +364,10 @@ void element_objective_explicit(Ctx& c, const double* d_u, double* d_gE, double*
 void shell_assemble(Ctx& c, double* vals, double* mvals);
 void shell_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate);
 void shell_element_matrices(Ctx& c, int e0, int n, double* ke_host, double* me_host);
+// beam2 elements (k_beam.cu)
+void beam_assemble(Ctx& c, double* vals, double* mvals);
+void beam_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate);
+void beam_element_matrices(Ctx& c, int e0, int n, double* ke_host, double* me_host);
 // brickIM elements (k_brickim.cu)
 void brickim_assemble(Ctx& c, double* vals, double* mvals);
 void brickim_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate);

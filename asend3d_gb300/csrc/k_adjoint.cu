@@ -269,6 +269,10 @@ void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g,
         shell_adjoint(c, d_b, d_a, d_g, accumulate);
         return;
     }
+    if (c.type == 2) {
+        beam_adjoint(c, d_b, d_a, d_g, accumulate);
+        return;
+    }
     if (c.type == 81) {
         brickim_adjoint(c, d_b, d_a, d_g, accumulate);
         return;

@@ -932,6 +932,8 @@ void assemble_operator(Ctx& c, int precision) {
         c.cM = cM_el;  // the shell / brickIM kernels read the context's coefficient
         if (c.type == 41) {
             shell_assemble(c, A.v64.p, mvals);  // FP64 element matrices at either precision
+        } else if (c.type == 2) {
+            beam_assemble(c, A.v64.p, mvals);  // FP64 element matrices at either precision
         } else if (c.type == 81) {
             brickim_assemble(c, A.v64.p, mvals);  // FP64 condensed element matrices at either precision
         } else if (precision == 64) {

@@ -41,8 +41,8 @@ class BlockMesh:
 
     @property
     def dpn(self) -> int:
-        """DOF per node: 6 for shells (u v w thx thy thz), else 3."""
-        return 6 if self.elem_type == 41 else 3
+        """DOF per node: 6 for shells and beams (u v w thx thy thz), else 3."""
+        return 6 if self.elem_type in (41, 2) else 3
 
     @property
     def n_dof(self) -> int:
@@ -182,3 +182,14 @@ def plate_quad4(nx: int, ny: int, lx: float, ly: float) -> BlockMesh:
     conn = np.stack([nid(i, j), nid(i + 1, j), nid(i + 1, j + 1), nid(i, j + 1)], axis=1).astype(np.int32)
     return BlockMesh(nx, ny, 0, lx, ly, 0.0, coords, conn, elem_type=41)
 
+
+def line_beam2(n: int, length: float, direction=(1.0, 0.0, 0.0), origin=(0.0, 0.0, 0.0)) -> BlockMesh:
+    """Straight line of n beam2 elements (type 2) of total length ``length``
+    from ``origin`` along ``direction``: node i at origin + i/n * length * d,
+    element i = (i, i+1).  ny = nz = 0."""
+    d = np.asarray(direction, np.float64)
+    d = d / np.linalg.norm(d)
+    t = np.linspace(0.0, length, n + 1)
+    coords = np.asarray(origin, np.float64)[None, :] + t[:, None] * d[None, :]
+    conn = np.stack([np.arange(n), np.arange(1, n + 1)], axis=1).astype(np.int32)
+    return BlockMesh(n, 0, 0, float(length), 0.0, 0.0, coords, conn, elem_type=2)

@@ -58,6 +58,10 @@ class Problem:
     # layered shell4 sections: [(element indices, layers [n, 7] = E1 E2 nu12
     # G12 density thickness angle[deg], z offset)]; other elements keep E, nu, t
     shell_sections: list | None = None
+    # beam2 sections [n_el][10] (or one row for every element): area, I1..I5
+    # (int z, int y, int z^2, int y^2, int yz dA in the section axes), polar
+    # moment J, and the vector v fixing the section's xy plane
+    beam_sections: np.ndarray | None = None
 
     def add_node_set(self, name, nodes):
         self.node_sets[name] = np.asarray(nodes, dtype=np.int32)
@@ -163,6 +167,11 @@ class GpuSolver:
             self._check(self.lib.asend_set_lumped_mass(self.ctx, 1), "set_lumped_mass")
         if p.shell_sections:
             self._set_shell_sections(p, E, nu, rho, thk)
+        if p.beam_sections is not None:
+            self._bsec = np.ascontiguousarray(np.broadcast_to(np.asarray(p.beam_sections, np.float64),
+                                                              (m.n_elems, 10)))
+            self._check(self.lib.asend_set_beam_sections(self.ctx, _ptr(self._bsec, C.c_double)),
+                        "set_beam_sections")
         if m.elem_type in (8, 81) and m.conn.shape[0] == m.nx * m.ny * m.nz:
             self._check(self.lib.asend_set_block_structure(self.ctx, m.nx, m.ny, m.nz), "set_block_structure")
         for name, nodes in p.node_sets.items():
@@ -481,10 +490,12 @@ class GpuSolver:
         return ms.value, by.value
 
     def element_matrices(self, first=0, count=None, mass=True):
-        """shell4 / brickIM element stiffness (and mass) matrices [count][24][24]."""
+        """shell4 / brickIM element stiffness (and mass) matrices [count][24][24]
+        ([count][12][12] for beam2)."""
         n = self.p.mesh.n_elems - first if count is None else count
-        ke = np.zeros((n, 24, 24))
-        me = np.zeros((n, 24, 24)) if mass else None
+        d = 12 if self.p.mesh.elem_type == 2 else 24
+        ke = np.zeros((n, d, d))
+        me = np.zeros((n, d, d)) if mass else None
         self._check(self.lib.asend_element_matrices(self.ctx, first, n, _ptr(ke, C.c_double),
                                                     None if me is None else _ptr(me, C.c_double)), "element_matrices")
         return ke, me

@@ -107,9 +107,11 @@ const char* asend_version(void);
  * thickness per element for shells (else NULL).  shell4 (41): 4 nodes per
  * element, 6 DOF per node (u v w thx thy thz), one isotropic layer centred
  * on the element plane; elements must be flat in a plane z = const (their
- * frame is then the global one).  Shell meshes take nodal forces/moments,
- * constraints and objectives on all 6 components; surface tractions,
- * multigrid and batched instances take solid meshes. */
+ * frame is then the global one).  beam2 (2): 2 nodes per element, 6 DOF per
+ * node, sections from asend_set_beam_sections (thickness may be NULL).
+ * Shell and beam meshes take nodal forces/moments, constraints and objectives
+ * on all 6 components; surface tractions, multigrid and batched instances
+ * take solid meshes. */
 int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const double* coords,
                    int32_t n_elems, const int32_t* conn, const double* E, const double* nu,
                    const double* rho, const double* thickness);
@@ -375,6 +377,24 @@ int asend_set_damping(asend_ctx* ctx, double rayleigh_cm, double rayleigh_ck, co
 int asend_shell_section(int32_t n_layers, const double* layers, double z_offset, double* abd_out,
                         double* msec_out);
 int asend_set_shell_sections(asend_ctx* ctx, const double* abd, const double* msec);
+/* beam2 sections (the reference's beam section: area, areaMoment[5],
+ * polarMoment, orientation; Section in section_meth.rs, stiffness
+ * get_beam_stiff_dfd0 element_properties.rs:878-1017, mass
+ * get_beam_mass_dfd0 :1410-1500), required before assembling a beam2 mesh.
+ * sections[n_el][10] = area A, I1 = int z dA, I2 = int y dA, I3 = int z^2 dA,
+ * I4 = int y^2 dA, I5 = int yz dA, polar moment J, and a direction v (3)
+ * fixing the section's xy plane.  Element frame: e1 along the element
+ * (node 1 -> node 2; the reference takes x from the section orientation and
+ * needs it along the element), e3 = e1 x v / |e1 x v|, e2 = e3 x e1.
+ * Section stiffness with the element's E and G = E / (2 (1 + nu)):
+ * EA, GA, GA, GJ, E I3, E I4 on the diagonal of (axial strain, the two
+ * transverse shears, twist, the two curvatures), couplings E I1, -E I2, -G I1,
+ * G I2, -E I5; section mass rho (A, A, A, J, I3, I4) with couplings rho I1,
+ * -rho I1, -rho I2, rho I2, rho I5, as the reference writes them.  A, I3, I4,
+ * J > 0 and v off the element axis are required (EINVAL otherwise).  K_e is
+ * proportional to E_e, so asend_adjoint_gradient gives per-element modulus
+ * gradients; body loads need I1 = I2 = 0; damping takes rayleigh_cm only. */
+int asend_set_beam_sections(asend_ctx* ctx, const double* sections);
 /* Row-sum lumped mass in Newmark assemblies (the reference's 'lumpMass: yes',
  * element_equations.rs:950-971): the mass is diag(row sums of M). */
 int asend_set_lumped_mass(asend_ctx* ctx, int32_t on);
@@ -489,11 +509,12 @@ int asend_eigen_solve(asend_ctx* ctx, const asend_eigen_opts* opts, double* eig_
  * vals[m], vecs[k*m + i] = component i of eigenvector k (may be NULL). */
 int asend_dense_sym_eigen(int32_t m, const double* a, double* vals, double* vecs);
 
-/* shell4 / brickIM element matrices of elements [first, first + count): ke
- * (and me when not NULL) [count][24][24] in node-major DOF order (shell4:
- * u v w thx thy thz per node; brickIM: u v w per node), stiffness after
- * condensing the internal DOF (element_equations.rs:19-57: 8 for shell4, 9
- * for brickIM), consistent mass over the node DOF (:420-626). */
+/* shell4 / brickIM / beam2 element matrices of elements [first, first +
+ * count): ke (and me when not NULL) [count][24][24] ([count][12][12] for
+ * beam2) in node-major DOF order (shell4, beam2: u v w thx thy thz per node;
+ * brickIM: u v w per node), stiffness after condensing the internal DOF
+ * (element_equations.rs:19-57: 8 for shell4, 9 for brickIM, 2 for beam2),
+ * consistent mass over the node DOF (:420-626). */
 int asend_element_matrices(asend_ctx* ctx, int32_t first, int32_t count, double* ke, double* me);
 
 /* y = A x and *energy = x^T A x with the assembled FP64 operator, on DEVICE

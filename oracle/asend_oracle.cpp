@@ -70,6 +70,10 @@ TypeInfo type_info(int type) {
         // pseudo-node 2a, its rotations 2a+1, so DOF 6a + c keeps the
         // reference's node-major numbering (element_meth.rs:424-431)
         t.nn = 8; t.dpn = 3; t.nip = 4; t.nfaces = 0; t.face_nn = 0;
+    } else if (type == 2) {
+        // beam2 as 4 pseudo-nodes of 3 DOF, node a's translations on 2a and
+        // rotations on 2a+1, as for shell4; the 2 internal DOF are condensed
+        t.nn = 4; t.dpn = 3; t.nip = 2; t.nfaces = 0; t.face_nn = 0;
     } else if (type == 10) {
         // tet10: 4 points (R_TET1 x3 with R_TET2 in turn on each axis after
         // the first), weights 1/24 (element_meth.rs:228-262); face loads are
@@ -642,6 +646,161 @@ void shell_km_sec(const double* xyz, const double* C, const double* msec, double
 }
 
 // ---------------------------------------------------------------------------
+// beam2 (type 2): 2 nodes x 6 DOF (u1 u2 u3 th1 th2 th3) + 2 internal DOF, a
+// transverse bubble 1 - s^2 on the section-frame u2 and u3 (dof_table entries
+// (2,1), (2,2)); 2 Gauss points +-1/sqrt(3), weight 1 (element_meth.rs:371-396).
+// Shape functions (element_soln_fields.rs:364-379): N1 = (1-s)/2,
+// N2 = (1+s)/2, N3 = 1 - s^2.  The reference stores the bubble's derivative
+// -2s in node 1's slot (d_nds[0]; node 3's is d_nds[6]), which leaves the
+// internal block without stiffness and node 1's axial derivative wrong; here
+// the derivative goes to the bubble.  Jacobian (:415-421): [x1_s 0 0; x2_s 1 0;
+// x3_s 0 +-1] in the section frame, so d/dx = (2/L) d/ds and detJ = L/2 when
+// the frame's first axis is the element axis.  Section deformation
+// (:1313-1321): [u1', u2' - th3, u3' + th2, th1', th2', th3'].  Section
+// stiffness get_beam_stiff_dfd0 (element_properties.rs:878-1017), section
+// mass get_beam_mass_dfd0 (:1410-1500); M uses the node DOF only
+// (element_equations.rs:420-626, nd_dof = num_nds * dof_per_nd).
+// sec[10] = area, area moments I1..I5 (int z, int y, int z^2, int y^2, int yz
+// over the section, y and z along e2 and e3), polar moment J, and v (3), the
+// direction fixing the xy plane; frame rows e1 = element axis,
+// e3 = e1 x v / |e1 x v|, e2 = e3 x e1 (Section::set_orientation,
+// section_meth.rs:21-50, with the element axis as x).
+// ---------------------------------------------------------------------------
+bool beam_frame(const double* xyz, const double* v, double* R, double* L) {
+    double d[3], l2 = 0.0;
+    for (int j = 0; j < 3; ++j) {
+        d[j] = xyz[3 + j] - xyz[j];
+        l2 += d[j] * d[j];
+    }
+    if (!(l2 > 0.0)) return false;
+    *L = std::sqrt(l2);
+    double e1[3] = {d[0] / *L, d[1] / *L, d[2] / *L};
+    double e3[3] = {e1[1] * v[2] - e1[2] * v[1], e1[2] * v[0] - e1[0] * v[2], e1[0] * v[1] - e1[1] * v[0]};
+    const double n3 = std::sqrt(e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2]);
+    const double nv = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (!(n3 > 1e-9 * nv)) return false;
+    for (int j = 0; j < 3; ++j) e3[j] /= n3;
+    const double e2[3] = {e3[1] * e1[2] - e3[2] * e1[1], e3[2] * e1[0] - e3[0] * e1[2], e3[0] * e1[1] - e3[1] * e1[0]};
+    for (int j = 0; j < 3; ++j) {
+        R[j] = e1[j];
+        R[3 + j] = e2[j];
+        R[6 + j] = e3[j];
+    }
+    return true;
+}
+
+// 6x6 section stiffness (element_properties.rs:921-1010, no stiffness-matrix
+// override): isotropic E, G = E / (2 (1 + nu)).
+void beam_cmat(double E, double nu, const double* sec, double* C) {
+    const double G = E / (2.0 * (1.0 + nu));
+    for (int i = 0; i < 36; ++i) C[i] = 0.0;
+    C[0] = E * sec[0];
+    C[4] = E * sec[1];
+    C[5] = -E * sec[2];
+    C[7] = G * sec[0];
+    C[9] = -G * sec[1];
+    C[14] = G * sec[0];
+    C[15] = G * sec[2];
+    C[21] = G * sec[6];
+    C[28] = E * sec[3];
+    C[29] = -E * sec[5];
+    C[35] = E * sec[4];
+    for (int i = 1; i < 6; ++i)
+        for (int j = 0; j < i; ++j) C[6 * i + j] = C[6 * j + i];
+}
+
+// 6x6 section mass (element_properties.rs:1440-1497, no mass-matrix override)
+void beam_msec(double rho, const double* sec, double* M) {
+    for (int i = 0; i < 36; ++i) M[i] = 0.0;
+    M[0] = M[7] = M[14] = rho * sec[0];
+    M[4] = rho * sec[1];
+    M[9] = -rho * sec[1];
+    M[5] = -rho * sec[2];
+    M[15] = rho * sec[2];
+    M[21] = rho * sec[6];
+    M[28] = rho * sec[3];
+    M[29] = rho * sec[5];
+    M[35] = rho * sec[4];
+    for (int i = 1; i < 6; ++i)
+        for (int j = 0; j < i; ++j) M[6 * i + j] = M[6 * j + i];
+}
+
+// Element stiffness ke[12][12] (internal DOF condensed, condense_mat
+// element_equations.rs:19-57) and consistent mass me[12][12] (may be null) in
+// global DOF 6 a + c.  The rows of B are built in global components through
+// the frame, as get_inst_disp_dfd0 (element_soln_fields.rs:650-690) maps a
+// global DOF to section-frame displacements; the internal DOF are section-frame
+// amplitudes.  Returns false for a zero-length element or v along the axis.
+bool beam_km(const double* xyz, double E, double nu, double rho, const double* sec, double* ke, double* me) {
+    double R[9], L;
+    if (!beam_frame(xyz, sec + 7, R, &L)) return false;
+    constexpr int tot = 14, nd = 12;
+    double C[36], K[tot * tot] = {0.0};
+    beam_cmat(E, nu, sec, C);
+    const double a = 0.5 * L;  // detJ
+    const double sp[2] = {-kR1ORt3, kR1ORt3};
+    for (int ip = 0; ip < 2; ++ip) {
+        const double s = sp[ip];
+        const double N[2] = {0.5 * (1.0 - s), 0.5 * (1.0 + s)}, dN[2] = {-0.5 / a, 0.5 / a};
+        double B[6][tot] = {{0.0}};
+        for (int k = 0; k < 2; ++k)
+            for (int c = 0; c < 3; ++c) {
+                const int ct = 6 * k + c, cr = 6 * k + 3 + c;
+                B[0][ct] += dN[k] * R[c];
+                B[1][ct] += dN[k] * R[3 + c];
+                B[2][ct] += dN[k] * R[6 + c];
+                B[1][cr] -= N[k] * R[6 + c];  // - th3
+                B[2][cr] += N[k] * R[3 + c];  // + th2
+                B[3][cr] += dN[k] * R[c];
+                B[4][cr] += dN[k] * R[3 + c];
+                B[5][cr] += dN[k] * R[6 + c];
+            }
+        B[1][12] = -2.0 * s / a;  // bubble on u2
+        B[2][13] = -2.0 * s / a;  // bubble on u3
+        double CB[6][tot];
+        for (int i = 0; i < 6; ++i)
+            for (int c = 0; c < tot; ++c) {
+                double acc = 0.0;
+                for (int k = 0; k < 6; ++k) acc += C[6 * i + k] * B[k][c];
+                CB[i][c] = acc * a;  // weight 1
+            }
+        for (int r = 0; r < tot; ++r)
+            for (int c = 0; c < tot; ++c) {
+                double acc = 0.0;
+                for (int k = 0; k < 6; ++k) acc += B[k][r] * CB[k][c];
+                K[r * tot + c] += acc;
+            }
+        if (me) {
+            if (ip == 0)
+                for (int i = 0; i < nd * nd; ++i) me[i] = 0.0;
+            double Ms[36], RM[36];
+            beam_msec(rho, sec, Ms);
+            // Rb^T Ms Rb with Rb = diag(R, R)
+            auto rb = [&](int p, int q) { return (p / 3 == q / 3) ? R[3 * (p % 3) + q % 3] : 0.0; };
+            for (int c = 0; c < 6; ++c)
+                for (int d = 0; d < 6; ++d) {
+                    double acc = 0.0;
+                    for (int p = 0; p < 6; ++p)
+                        for (int q = 0; q < 6; ++q) acc += rb(p, c) * Ms[6 * p + q] * rb(q, d);
+                    RM[6 * c + d] = acc;
+                }
+            for (int k = 0; k < 2; ++k)
+                for (int l = 0; l < 2; ++l)
+                    for (int c = 0; c < 6; ++c)
+                        for (int d = 0; d < 6; ++d) me[(6 * k + c) * nd + 6 * l + d] += N[k] * N[l] * a * RM[6 * c + d];
+        }
+    }
+    double Kii[4] = {K[12 * tot + 12], K[12 * tot + 13], K[13 * tot + 12], K[13 * tot + 13]};
+    givens_factor(Kii, 2);
+    for (int r = 0; r < nd; ++r) {
+        double rhs[2] = {K[12 * tot + r], K[13 * tot + r]}, x[2];
+        givens_solve(x, Kii, rhs, 2);
+        for (int c = 0; c < nd; ++c) ke[c * nd + r] = K[c * tot + r] - (K[c * tot + 12] * x[0] + K[c * tot + 13] * x[1]);
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
 // Sparse matrix with a fixed pattern (sorted columns) and element-order
 // accumulation.  The reference keeps row linked lists and add_entry appends or
 // accumulates (list_ent_meth.rs:6-18); every (i,j) sum is accumulated in
@@ -705,6 +864,12 @@ struct orc_model {
     std::vector<double> shell_abd81, shell_msec36;
     std::vector<double> phys_xyz;
     std::vector<int32_t> conn4;
+    // beam2: the same two-pseudo-node view; 2 physical nodes per element and
+    // the section table [n_el][10] (beam_km)
+    bool beam = false;
+    std::vector<int32_t> conn2;
+    std::vector<double> beam_sec;
+    bool structural() const { return shell || beam; }
 };
 
 namespace {
@@ -720,6 +885,13 @@ void elem_xyz(const orc_model* m, int e, double* xyz) {
 // Element stiffness (and mass when me != null) in the assembly view's DOF
 // order: solids from the isotropic C, shells from the shell4 routine.
 void elem_km(const orc_model* m, int e, double* ke, double* me) {
+    if (m->beam) {
+        double xyz[6];
+        for (int a = 0; a < 2; ++a)
+            for (int j = 0; j < 3; ++j) xyz[3 * a + j] = m->phys_xyz[3 * (size_t)m->conn2[(size_t)e * 2 + a] + j];
+        beam_km(xyz, m->E[e], m->nu[e], m->rho[e], &m->beam_sec[(size_t)e * 10], ke, me);
+        return;
+    }
     if (m->shell) {
         double xyz[12];
         for (int a = 0; a < 4; ++a)
@@ -1306,7 +1478,8 @@ extern "C" {
 orc_model* orc_create(int32_t elem_type, int32_t n_nodes, const double* coords, int32_t n_elems,
                       const int32_t* conn, const double* E, const double* nu, const double* rho,
                       const double* thickness) {
-    if (elem_type != 8 && elem_type != 81 && elem_type != 4 && elem_type != 10 && elem_type != 41) return nullptr;
+    if (elem_type != 8 && elem_type != 81 && elem_type != 4 && elem_type != 10 && elem_type != 41 && elem_type != 2)
+        return nullptr;
     auto* m = new orc_model();
     m->ti = type_info(elem_type);
     m->n_el = n_elems;
@@ -1329,6 +1502,20 @@ orc_model* orc_create(int32_t elem_type, int32_t n_nodes, const double* coords, 
             for (int j = 0; j < 3; ++j) m->xyz[6 * (size_t)i + j] = m->xyz[6 * (size_t)i + 3 + j] = coords[3 * (size_t)i + j];
         m->conn.resize((size_t)n_elems * 8);
         for (size_t k = 0; k < (size_t)n_elems * 4; ++k) {
+            m->conn[2 * k] = 2 * conn[k];
+            m->conn[2 * k + 1] = 2 * conn[k] + 1;
+        }
+    } else if (elem_type == 2) {
+        m->beam = true;
+        m->n_phys = n_nodes;
+        m->phys_xyz.assign(coords, coords + (size_t)3 * n_nodes);
+        m->conn2.assign(conn, conn + (size_t)n_elems * 2);
+        m->n_nodes = 2 * n_nodes;
+        m->xyz.resize((size_t)6 * n_nodes);
+        for (int i = 0; i < n_nodes; ++i)
+            for (int j = 0; j < 3; ++j) m->xyz[6 * (size_t)i + j] = m->xyz[6 * (size_t)i + 3 + j] = coords[3 * (size_t)i + j];
+        m->conn.resize((size_t)n_elems * 4);
+        for (size_t k = 0; k < (size_t)n_elems * 2; ++k) {
             m->conn[2 * k] = 2 * conn[k];
             m->conn[2 * k + 1] = 2 * conn[k] + 1;
         }
@@ -1368,13 +1555,22 @@ int orc_set_constraints(orc_model* m, int32_t n_rows, const int32_t* row_ptr, co
 // c1 = -1/(dt^2 (beta - gamma)) at :977-988) -> add_entry per element DOF pair
 // (:1040-1059).  Penalty scale: model_analysis.rs:255-259 over that matrix.
 int orc_assemble(orc_model* m, int32_t dynamic, double dt, double beta, double gamma) {
+    if (m->beam) {  // beam2 needs its sections, with valid frames
+        if (m->beam_sec.size() != (size_t)m->n_el * 10) return -3;
+        for (int e = 0; e < m->n_el; ++e) {
+            double xyz[6], R[9], L;
+            for (int a = 0; a < 2; ++a)
+                for (int j = 0; j < 3; ++j) xyz[3 * a + j] = m->phys_xyz[3 * (size_t)m->conn2[(size_t)e * 2 + a] + j];
+            if (!beam_frame(xyz, &m->beam_sec[(size_t)e * 10 + 7], R, &L)) return -3;
+        }
+    }
     build_pattern(m, m->K);
     m->dynamic = dynamic != 0;
     m->cM = 0.0;
     m->cD = 0.0;
     const bool damp = dynamic == 1 && m->damped();
-    if ((damp && (m->ray_ck != 0.0 || !m->dmat.empty()) && (m->shell || m->ti.type == 81)) ||
-        (!m->cmat.empty() && m->shell))
+    if ((damp && (m->ray_ck != 0.0 || !m->dmat.empty()) && (m->structural() || m->ti.type == 81)) ||
+        (!m->cmat.empty() && m->structural()))
         return -2;  // stiffness / material damping and 6x6 stiffness: elements without internal DOF
     m->D = Csr();
     if (m->dynamic) {
@@ -1423,7 +1619,7 @@ int orc_set_cmat(orc_model* m, const double* C) {
         m->cmat.clear();
         return 0;
     }
-    if (m->shell) return -1;
+    if (m->structural()) return -1;
     m->cmat.assign(C, C + (size_t)m->n_el * 36);
     m->assembled = false;
     return 0;
@@ -1447,6 +1643,19 @@ int orc_set_shell_sections(orc_model* m, const double* abd, const double* msec) 
     }
     m->assembled = false;
     return 0;
+}
+
+int orc_set_beam_sections(orc_model* m, const double* sec) {
+    if (!m->beam || !sec) return -1;
+    m->beam_sec.assign(sec, sec + (size_t)m->n_el * 10);
+    m->assembled = false;
+    return 0;
+}
+
+int orc_beam_element(const double* xyz, double E, double nu, double rho, const double* sec, double* ke,
+                     double* me) {
+    if (!xyz || !sec || !ke) return -1;
+    return beam_km(xyz, E, nu, rho, sec, ke, me) ? 0 : -2;
 }
 
 int orc_set_damping(orc_model* m, double ray_cm, double ray_ck, const double* D) {
@@ -1648,7 +1857,13 @@ int orc_body_load(const orc_model* m, int32_t n_set, const int32_t* elem_set, in
         double xyz[30];
         elem_xyz(m, e, xyz);
         // element mass at its density, or at unit density for body forces
-        if (m->shell) {
+        if (m->beam) {
+            double x2[6];
+            for (int a = 0; a < 2; ++a)
+                for (int j = 0; j < 3; ++j) x2[3 * a + j] = m->phys_xyz[3 * (size_t)m->conn2[(size_t)e * 2 + a] + j];
+            beam_km(x2, m->E[e], m->nu[e], kind == 0 ? 1.0 : m->rho[e], &m->beam_sec[(size_t)e * 10], ke.data(),
+                    me.data());
+        } else if (m->shell) {
             double x4[12];
             for (int a = 0; a < 4; ++a)
                 for (int j = 0; j < 3; ++j) x4[3 * a + j] = m->phys_xyz[3 * (size_t)m->conn4[(size_t)e * 4 + a] + j];
@@ -1657,12 +1872,12 @@ int orc_body_load(const orc_model* m, int32_t n_set, const int32_t* elem_set, in
             solid_me(m->ti.type, xyz, kind == 0 ? 1.0 : m->rho[e], me.data());
         }
         // physical nodes: shells carry translations on pseudo-node 2a
-        const int nphys = m->shell ? 4 : nn;
+        const int nphys = m->shell ? 4 : (m->beam ? 2 : nn);
         double acc_e[3];
         if (kind == 2) {
             double cen[3] = {0, 0, 0}, d[3], dp = 0.0;
             for (int a = 0; a < nphys; ++a)
-                for (int j = 0; j < 3; ++j) cen[j] += xyz[3 * (m->shell ? 2 * a : a) + j] / nphys;
+                for (int j = 0; j < 3; ++j) cen[j] += xyz[3 * (m->structural() ? 2 * a : a) + j] / nphys;
             for (int j = 0; j < 3; ++j) {
                 d[j] = cen[j] - center[j];
                 dp += ax[j] * d[j];
@@ -1673,19 +1888,19 @@ int orc_body_load(const orc_model* m, int32_t n_set, const int32_t* elem_set, in
         }
         std::vector<double> acc(tot, 0.0), ld(tot, 0.0);
         for (int a = 0; a < nphys; ++a)
-            for (int j = 0; j < 3; ++j) acc[3 * (m->shell ? 2 * a : a) + j] = acc_e[j];
+            for (int j = 0; j < 3; ++j) acc[3 * (m->structural() ? 2 * a : a) + j] = acc_e[j];
         double tot_f[3] = {0, 0, 0};
         for (int i = 0; i < tot; ++i) {
             double v = 0.0;
             for (int j = 0; j < tot; ++j) v += me[i * tot + j] * acc[j];
             ld[i] = v;
-            if (!m->shell || (i / 3) % 2 == 0) tot_f[i % 3] += v;
+            if (!m->structural() || (i / 3) % 2 == 0) tot_f[i % 3] += v;
         }
         if (kind == 0) {
             // element volume: the unit-density mass summed over one direction
             double vol = 0.0;
             for (int i = 0; i < tot; i += 3)
-                if (!m->shell || (i / 3) % 2 == 0)
+                if (!m->structural() || (i / 3) % 2 == 0)
                     for (int j = 0; j < tot; j += 3) vol += me[i * tot + j];
             double imag = 0.0, vmag = 0.0;
             for (int j = 0; j < 3; ++j) {
@@ -1818,7 +2033,7 @@ int orc_adjoint_modulus_gradient(orc_model* m, const double* u, const double* dL
 // inverse of :724-760).
 int orc_adjoint_modulus_component_gradient(orc_model* m, const double* u, const double* lambda,
                                            int32_t component, double* gD) {
-    if (component < 1 || component > 3 || m->shell || m->ti.type == 81) return -1;
+    if (component < 1 || component > 3 || m->structural() || m->ti.type == 81) return -1;
     const int k = component - 1;
     const TypeInfo& t = m->ti;
     const int nn = t.nn, tot = 3 * nn;
@@ -2091,7 +2306,7 @@ int orc_newmark_adjoint(orc_model* m, int32_t n_steps, double dt, double beta, d
 // contracted with (lambda_e, u_e) equals the full dK/dD contracted with the
 // recovered (lambda, u).  Solid types (8, 81, 4, 10); P[n_el][36].
 int orc_adjoint_strain_pairs(const orc_model* m, const double* u, const double* lam, double* P) {
-    if (!m->assembled || m->shell) return -1;
+    if (!m->assembled || m->structural()) return -1;
     const TypeInfo& t = m->ti;
     const int nn = t.nn;
     for (int e = 0; e < m->n_el; ++e) {
@@ -2181,7 +2396,7 @@ int orc_element_objective(const orc_model* m, const double* u, int32_t n_set, co
                           int32_t category, int32_t component, int32_t optr, double coef, double expnt,
                           int32_t n_tgt, const double* tgt, double* L_out, double* dLdu, double* Q,
                           double* dLdE) {
-    if (!m->assembled || m->shell || n_set <= 0) return -1;
+    if (!m->assembled || m->structural() || n_set <= 0) return -1;
     if (category < 0 || category > 2 || optr < 0 || optr > 3) return -1;
     if (category != 2 && (component < 1 || component > 6)) return -1;
     if (n_tgt != 0 && n_tgt != 1 && n_tgt != n_set) return -1;

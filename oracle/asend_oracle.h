@@ -7,7 +7,8 @@
  *
  * It restates, in plain single-threaded C++ and FP64 (as the reference runs),
  * the reference's CPU algorithms for:
- *   - element integration (hex8 type 8, tet4 type 4, shell4 type 41),
+ *   - element integration (hex8 type 8, brickIM 81, tet4 4, tet10 10,
+ *     shell4 41, beam2 2),
  *   - row-list sparse assembly, penalty constraints,
  *   - the block-LDL^T preconditioned CG and the direct skyline LDL^T,
  *   - the spatial node reordering that defines the preconditioner blocks,
@@ -42,9 +43,10 @@ enum { ORC_PC_NONE = 0, ORC_PC_JACOBI = 1, ORC_PC_BLOCK_LDL = 2, ORC_PC_DIRECT =
 /* stopping rules */
 enum { ORC_STOP_REFERENCE = 0, ORC_STOP_RELATIVE = 1 };
 
-/* Mesh of one element type (8 hex8, 4 tet4, 41 shell4).  coords[n_nodes*3],
- * conn[n_elems*nodes_per_elem] (0-based), per-element isotropic E, nu, rho.
- * For shell4, thickness[n_elems] gives the section thickness (else NULL). */
+/* Mesh of one element type (8 hex8, 81 brickIM, 4 tet4, 10 tet10, 41 shell4,
+ * 2 beam2).  coords[n_nodes*3], conn[n_elems*nodes_per_elem] (0-based),
+ * per-element isotropic E, nu, rho.  For shell4, thickness[n_elems] gives the
+ * section thickness (else NULL); beam2 takes orc_set_beam_sections. */
 orc_model* orc_create(int32_t elem_type, int32_t n_nodes, const double* coords,
                       int32_t n_elems, const int32_t* conn, const double* E,
                       const double* nu, const double* rho, const double* thickness);
@@ -152,6 +154,17 @@ int orc_reorder_nodes(const orc_model* m, int32_t block_dim, int32_t* order_out)
 int orc_shell_section(int32_t n_layers, const double* props, double z_offset, double* abd, double* msec);
 /* Per-element sections of a shell4 model (NULL abd: back to E, nu, t). */
 int orc_set_shell_sections(orc_model* m, const double* abd, const double* msec);
+
+/* beam2 (type 2) sections, sec[n_el][10] = area, I1..I5 (int z, int y,
+ * int z^2, int y^2, int yz over the section), polar moment J, and the
+ * direction v (3) that fixes the section's xy plane (the element axis is x).
+ * Required before orc_assemble of a beam2 model. */
+int orc_set_beam_sections(orc_model* m, const double* sec);
+/* One beam2 element: xyz[2][3], ke[12][12] (internal DOF condensed), me
+ * [12][12] (may be NULL), global DOF 6 a + c.  -2: zero length or v along
+ * the axis. */
+int orc_beam_element(const double* xyz, double E, double nu, double rho, const double* sec, double* ke,
+                     double* me);
 
 /* Element-category objective term at the element centroids (category 0
  * stress, 1 strain, 2 strainEnergy; component 1-6 for 0/1; optr 0 powerNorm,

@@ -77,6 +77,8 @@ def load():
                                               C.c_int32, P_i, P_d, P_d, P_d]),
             "orc_shell_section": (C.c_int, [C.c_int32, P_d, C.c_double, P_d, P_d]),
             "orc_set_shell_sections": (C.c_int, [C.c_void_p, P_d, P_d]),
+            "orc_set_beam_sections": (C.c_int, [C.c_void_p, P_d]),
+            "orc_beam_element": (C.c_int, [P_d, C.c_double, C.c_double, C.c_double, P_d, P_d, P_d]),
             "orc_element_objective": (C.c_int, [C.c_void_p, P_d, C.c_int32, P_i, C.c_int32, C.c_int32, C.c_int32,
                                                 C.c_double, C.c_double, C.c_int32, P_d, P_d, P_d, P_d, P_d]),
         }
@@ -129,7 +131,7 @@ class Oracle:
         if not self.m:
             raise RuntimeError("orc_create failed")
         self.n_dof = self.lib.orc_n_dof(self.m)
-        self.dpn = 6 if m.elem_type == 41 else 3
+        self.dpn = 6 if m.elem_type in (41, 2) else 3
         ptr, dof, coef, rhs = constraint_rows(problem, self.dpn)
         self._c = (ptr, dof, coef, rhs)
         if len(rhs):
@@ -147,6 +149,10 @@ class Oracle:
             self.lib.orc_set_damping(self.m, float(cm), float(ck), None if self._dmat is None else _p(self._dmat))
         if getattr(problem, "lump_mass", False):
             self.lib.orc_set_lumped_mass(self.m, 1)
+        bsec = getattr(problem, "beam_sections", None)
+        if bsec is not None:
+            self._bsec = np.ascontiguousarray(np.broadcast_to(np.asarray(bsec, np.float64), (m.n_elems, 10)))
+            assert self.lib.orc_set_beam_sections(self.m, _p(self._bsec)) == 0
         secs = getattr(problem, "shell_sections", None)
         if secs:
             # layered sections: (element indices, layer table [n, 7], z offset);
@@ -370,3 +376,15 @@ def element_stiffness(elem_type, xyz, E, nu):
     rc = lib.orc_element_stiffness(elem_type, _p(xyz), E, nu, 0.0, _p(ke))
     assert rc == 0
     return ke.reshape(n, n)
+
+
+def beam_element(xyz, E, nu, rho, sec):
+    """beam2 element stiffness and mass [12][12] (global DOF 6 a + c)."""
+    lib = load()
+    xyz = np.ascontiguousarray(xyz, np.float64).ravel()
+    sec = np.ascontiguousarray(sec, np.float64)
+    ke, me = np.zeros(144), np.zeros(144)
+    rc = lib.orc_beam_element(_p(xyz), float(E), float(nu), float(rho), _p(sec), _p(ke), _p(me))
+    if rc != 0:
+        raise ValueError(f"orc_beam_element failed ({rc})")
+    return ke.reshape(12, 12), me.reshape(12, 12)
