@@ -159,6 +159,9 @@ struct Section {
     std::vector<Layer> layers;
     double z_offset = 0.0;
     std::vector<double> orientation;  // xDir, xyVec
+    // beamProps (model_input.rs:561-596): area, I[5], J
+    double area = 0.0, J = 0.0;
+    std::vector<double> I;
 };
 struct Material {
     double density = 0.0;
@@ -197,7 +200,8 @@ int element_type(const std::string& t) {
     if (t == "tet4") return 4;
     if (t == "tet10") return 10;
     if (t == "shell4") return 41;
-    for (const char* o : {"wedge6", "shell3", "beam2", "frcFld", "mass", "fl4", "fl6", "fl8", "fl10"})
+    if (t == "beam2") return 2;
+    for (const char* o : {"wedge6", "shell3", "frcFld", "mass", "fl4", "fl6", "fl8", "fl10"})
         if (t == o) throw Fail("element type " + t + " is not on the GPU path");
     throw Fail("unrecognized element type: " + t);
 }
@@ -233,7 +237,7 @@ Model read_model(const std::string& path) {
             }
         } else if (h[0] == "sections") {
             if (h[1] == "type" && d.size() == 1) {
-                m.sections.push_back(Section{d[0], "", "", {}, 0.0, {}});
+                m.sections.push_back(Section{d[0], "", "", {}, 0.0, {}, 0.0, 0.0, {}});
             } else if (m.sections.empty()) {
                 continue;
             } else if (h[1] == "material" && d.size() == 1) {
@@ -251,8 +255,17 @@ Model read_model(const std::string& path) {
                     lay.back().thickness = num(d[0]);
                 else if (h[2] == "layers" && h[3] == "angle" && d.size() == 1 && !lay.empty())
                     lay.back().angle = num(d[0]);
-            } else if ((h[1] == "beamProps" || h[1] == "potField" || h[1] == "dampField" || h[1] == "thermField") &&
-                       !d.empty()) {
+            } else if (h[1] == "beamProps" && !d.empty()) {
+                // J is read from its one value (the reference indexes data[1] there)
+                Section& s = m.sections.back();
+                if (h[2] == "area" && d.size() == 1) s.area = num(d[0]);
+                else if (h[2] == "I" && d.size() == 5) {
+                    s.I.clear();
+                    for (const auto& x : d) s.I.push_back(num(x));
+                } else if (h[2] == "J" && d.size() == 1) s.J = num(d[0]);
+                else if (h[2] == "stiffness" || h[2] == "mass" || h[2] == "damping" || h[2] == "expLoadCoef")
+                    throw Fail("beam section " + h[2] + " entries are not on the GPU path");
+            } else if ((h[1] == "potField" || h[1] == "dampField" || h[1] == "thermField") && !d.empty()) {
                 throw Fail("section " + h[1] + " is not on the GPU path");
             }
         } else if (h[0] == "materials" && !h[1].empty()) {
@@ -491,7 +504,7 @@ struct Runner {
         for (size_t i = 0; i < m.elem_labels.size(); ++i) eidx[m.elem_labels[i]] = (int)i;
         const int ne = (int)m.elem_labels.size();
         n_nodes = (int)m.node_labels.size();
-        dpn = m.elem_type == 41 ? 6 : 3;
+        dpn = (m.elem_type == 41 || m.elem_type == 2) ? 6 : 3;
         std::vector<int32_t> conn;
         for (const auto& row : m.conn)
             for (int v : row) conn.push_back(nidx.at(v));
@@ -499,6 +512,7 @@ struct Runner {
         std::vector<double> props((size_t)ne * 9, NAN), damp((size_t)ne * 36, 0.0);
         std::vector<double> sec_abd((size_t)ne * 81, 0.0), sec_ms((size_t)ne * 36, 0.0);
         std::vector<char> has_sec(ne, 0);
+        std::vector<double> beam((size_t)ne * 10, NAN);  // area, I1..I5, J, xy-plane direction
         bool ortho = false, damped = false, layered = false;
         for (const Section& s : m.sections) {
             if (!m.elem_sets.count(s.elset)) throw Fail("section without a valid elementSet");
@@ -540,6 +554,37 @@ struct Runner {
                     }
                 }
                 continue;
+            } else if (s.type == "beam") {
+                // The reference's element frame is the section orientation
+                // (default the global axes, section.rs:150) and it
+                // differentiates along xDir, so xDir must lie along the
+                // element; the GPU element takes x from the element.  An
+                // opposite xDir is the same frame turned half a turn about y:
+                // I1 = int z and I5 = int yz change sign.
+                std::vector<double> ori = s.orientation;
+                if (ori.empty()) ori = {1.0, 0.0, 0.0, 0.0, 1.0, 0.0};
+                const double xn = std::sqrt(ori[0] * ori[0] + ori[1] * ori[1] + ori[2] * ori[2]);
+                for (int lab : m.elem_sets.at(s.elset)) {
+                    const int e = eidx.at(lab);
+                    const int n0 = nidx.at(m.conn[e][0]), n1 = nidx.at(m.conn[e][1]);
+                    double ax[3], an = 0.0, c = 0.0;
+                    for (int j = 0; j < 3; ++j) {
+                        ax[j] = m.coords[3 * (size_t)n1 + j] - m.coords[3 * (size_t)n0 + j];
+                        an += ax[j] * ax[j];
+                    }
+                    an = std::sqrt(an);
+                    for (int j = 0; j < 3; ++j) c += ax[j] * ori[j] / (an * xn);
+                    if (std::fabs(c) < 1.0 - 1e-9)
+                        throw Fail("beam sections whose orientation x direction is not along the element");
+                    double im[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+                    for (size_t k = 0; k < s.I.size() && k < 5; ++k) im[k] = s.I[k];
+                    if (c < 0.0) {
+                        im[0] = -im[0];
+                        im[4] = -im[4];
+                    }
+                    const double row[10] = {s.area, im[0], im[1], im[2], im[3], im[4], s.J, ori[3], ori[4], ori[5]};
+                    std::copy(row, row + 10, beam.begin() + (size_t)e * 10);
+                }
             } else if (s.type != "solid") {
                 throw Fail(s.type + " sections are not on the GPU path");
             }
@@ -580,6 +625,11 @@ struct Runner {
         check(asend_set_mesh(ctx, m.elem_type, n_nodes, m.coords.data(), ne, conn.data(), E.data(), nu.data(),
                              rho.data(), m.elem_type == 41 ? thk.data() : nullptr),
               "set_mesh");
+        if (m.elem_type == 2) {
+            for (double v : beam)
+                if (std::isnan(v)) throw Fail("beam2 elements need a beam section");
+            check(asend_set_beam_sections(ctx, beam.data()), "set_beam_sections");
+        }
         if (ortho) check(asend_set_orthotropic(ctx, props.data()), "set_orthotropic");
         if (layered) {
             // elements outside the layered sections keep one isotropic layer

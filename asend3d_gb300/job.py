@@ -40,8 +40,8 @@ from pathlib import Path
 
 import numpy as np
 
-ELEMENT_TYPES = {"brick8": 8, "brickIM": 81, "tet4": 4, "tet10": 10, "shell4": 41}
-OTHER_ELEMENT_TYPES = ("wedge6", "shell3", "beam2", "frcFld", "mass", "fl4", "fl6", "fl8", "fl10")
+ELEMENT_TYPES = {"brick8": 8, "brickIM": 81, "tet4": 4, "tet10": 10, "shell4": 41, "beam2": 2}
+OTHER_ELEMENT_TYPES = ("wedge6", "shell3", "frcFld", "mass", "fl4", "fl6", "fl8", "fl10")
 
 
 # ---------------------------------------------------------------------------
@@ -198,7 +198,18 @@ def read_model(path) -> ModelInput:
                     m.sections[-1]["layers"].append({"material": data[0]})
                 elif h2 == "layers" and h3 in ("thickness", "angle") and len(data) == 1:
                     m.sections[-1]["layers"][-1][h3] = float(data[0])
-            elif h1 in ("beamProps", "potField", "dampField", "thermField") and data:
+            elif h1 == "beamProps" and data:
+                # model_input.rs:561-596 (J is read from its one value; the
+                # reference indexes data[1] there)
+                if h2 == "area" and len(data) == 1:
+                    m.sections[-1]["area"] = float(data[0])
+                elif h2 == "I" and len(data) == 5:
+                    m.sections[-1]["I"] = [float(v) for v in data]
+                elif h2 == "J" and len(data) == 1:
+                    m.sections[-1]["J"] = float(data[0])
+                elif h2 in ("stiffness", "mass", "damping", "expLoadCoef"):
+                    raise NotImplementedError(f"beam section {h2} entries are not on the GPU path")
+            elif h1 in ("potField", "dampField", "thermField") and data:
                 raise NotImplementedError(f"section {h1} is not on the GPU path")
         elif h0 == "materials" and h1 != "":
             if h2 == "" and key_line:
@@ -380,6 +391,7 @@ class JobRunner:
         damp = np.zeros((ne, 36))
         ortho = False
         shell_secs = []
+        beam = np.full((ne, 10), np.nan)  # area, I1..I5, J, xy-plane direction
         for sec in m.sections:
             es = sec.get("elementSet")
             if es is None or es not in m.elem_sets:
@@ -411,6 +423,13 @@ class JobRunner:
                     shell_secs.append((els, rows, sec.get("zOffset", 0.0)))
                 E[els], nu[els], rho[els], thk[els] = r0[0], r0[2], r0[4], t
                 continue
+            elif sec["type"] == "beam":
+                mat = m.materials[sec["material"]]
+                if "damping" in mat:
+                    raise NotImplementedError("material damping takes solid sections")
+                for e in els:
+                    beam[e] = self._beam_row(sec, coords[conn[e, 1]] - coords[conn[e, 0]])
+                t = np.nan
             else:
                 raise NotImplementedError(f"{sec['type']} sections are not on the GPU path")
             Ev, nv = mat.get("E", [np.nan] * 3), mat.get("nu", [np.nan] * 3)
@@ -433,6 +452,10 @@ class JobRunner:
         p = Problem(mesh, E, nu, rho, thickness=None if np.isnan(thk).all() else thk)
         if shell_secs:
             p.shell_sections = shell_secs
+        if m.elem_type == 2:
+            if np.isnan(beam).any():
+                raise ValueError("beam2 elements need a beam section")
+            p.beam_sections = beam
         if ortho:
             if m.elem_type not in (8, 4, 10):
                 raise NotImplementedError("orthotropic materials take hex8 / tet4 / tet10 meshes on the GPU path")
@@ -664,6 +687,27 @@ class JobRunner:
             self.state = {"u": np.zeros(shape), "v": np.zeros(shape), "a": np.zeros(shape), "time": 0.0}
         key = {"displacement": "u", "velocity": "v", "acceleration": "a"}[field]
         self.state[key] = (amp / np.abs(mode).max()) * mode
+
+    @staticmethod
+    def _beam_row(sec, axis):
+        """The section table row of one beam2 element.  The reference takes the
+        element frame from the section orientation (xDir, xyVec; default the
+        global axes, section.rs:150) and differentiates along xDir, so a beam
+        is only consistent there when xDir lies along the element; the GPU
+        element takes x from the element itself.  An xDir opposite to the
+        element gives the same frame turned half a turn about y: the odd
+        moments I1 = int z and I5 = int yz change sign."""
+        ori = sec.get("orientation", [1.0, 0.0, 0.0, 0.0, 1.0, 0.0])
+        x = np.asarray(ori[:3], float)
+        x = x / np.linalg.norm(x)
+        a = np.asarray(axis, float) / np.linalg.norm(axis)
+        c = float(x @ a)
+        if abs(c) < 1.0 - 1e-9:
+            raise NotImplementedError("beam sections whose orientation x direction is not along the element")
+        im = list(sec.get("I", [0.0] * 5))
+        if c < 0.0:
+            im[0], im[4] = -im[0], -im[4]
+        return [sec.get("area", 0.0), *im, sec.get("J", 0.0), *ori[3:6]]
 
     @staticmethod
     def _shell_frame_angle(sec):

@@ -14,7 +14,7 @@ from asend3d_gb300 import job as J
 from asend3d_gb300.solver import Problem
 
 from eigen_cases import dense_reference, genuine_pairs
-from test_job import write_cantilever_job
+from test_job import write_beam_job, write_cantilever_job
 
 pytestmark = pytest.mark.gpu
 
@@ -286,3 +286,33 @@ def test_job_layered_shell_known_answers(gpu_lib, tmp_path):
         assert corner[2] == pytest.approx(2.6514522821613584e-06, rel=1e-8), runner
         assert corner[3] == pytest.approx(-1.79253112033e-04, rel=1e-8), runner
         assert corner[4] == pytest.approx(-8.96265560167775e-05, rel=1e-8), runner
+
+
+def test_beam_job_runners(gpu_lib, tmp_path):
+    """The beam2 cantilever job (hexBeam / shellBeam known answer, tip w = 8 at
+    the pin's 1e-3) through the Python runner and the C++ CLI (same values to
+    1e-12), and with every element numbered against the section's x direction
+    (same tip to 1e-8)."""
+    import subprocess
+
+    from asend3d_gb300 import build
+    build.build()
+    build.build_cli()
+    d1, d2, d3 = tmp_path / "py", tmp_path / "cli", tmp_path / "rev"
+    for d in (d1, d2, d3):
+        d.mkdir()
+    write_beam_job(d1)
+    write_beam_job(d2)
+    write_beam_job(d3, reverse=True)
+    J.JobRunner(d1 / "job.yaml").run()
+    J.JobRunner(d3 / "job.yaml").run()
+    out = subprocess.run([str(build.CLI), str(d2 / "job.yaml")], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    _, r1 = read_csv(d1 / "nodes.csv")
+    _, r2 = read_csv(d2 / "nodes.csv")
+    _, r3 = read_csv(d3 / "nodes.csv")
+    np.testing.assert_allclose(r1, r2, rtol=1e-12, atol=1e-12 * np.abs(r1).max())
+    np.testing.assert_allclose(r3[:, 1:4], r1[:, 1:4], rtol=1e-8, atol=1e-8 * np.abs(r1).max())
+    assert r1[0, 3] == pytest.approx(8.0, rel=1e-3)
+    w = float((d1 / "obj.csv").read_text().splitlines()[1].split(",")[1])
+    assert w == pytest.approx(r1[0, 3], rel=1e-12)

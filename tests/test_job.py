@@ -172,8 +172,8 @@ def test_design_var_reader(tmp_path):
 
 
 def test_unsupported_inputs(tmp_path):
-    (tmp_path / "m.yaml").write_text("elements:\n- type: beam2\n")
-    with pytest.raises(NotImplementedError, match="beam2"):
+    (tmp_path / "m.yaml").write_text("elements:\n- type: shell3\n")
+    with pytest.raises(NotImplementedError, match="shell3"):
         J.read_model(tmp_path / "m.yaml")
     (tmp_path / "l.yaml").write_text("loads:\n- type: bodyHeatGen\n")
     with pytest.raises(NotImplementedError, match="bodyHeatGen"):
@@ -262,3 +262,75 @@ def test_shell_job_problem(tmp_path):
         assert len(els) == m.n_elems and len(rows) == kw.get("layers", 1) and zoff == kw.get("z_offset", 0.0)
         assert rows[0][:6] == [70e9, 70e9, 0.33, 70e9 / 2.66, 2700.0, 0.004]
         np.testing.assert_allclose(pb.thickness, 0.004 * kw.get("layers", 1))
+
+
+def write_beam_job(d: Path, n=20, reverse=False, x_dir=(1.0, 0.0, 0.0), moments=(0.0, 0.0)):
+    """The hexBeam / shellBeam cantilever as a line of beam2 elements (L = 10,
+    b = 1, h = 0.1, E = 1e6, nu = 0), clamped at x = 0, Fz = 2 at the tip;
+    ``reverse`` numbers every element from its outer node to its inner one."""
+    from asend3d_gb300.mesh import line_beam2
+    m = line_beam2(n, 10.0)
+    if reverse:
+        m.conn = m.conn[:, ::-1].copy()
+    lines = ["nodes:"] + [f"- [{i}, {float(x)!r}, {float(y)!r}, {float(z)!r}]" for i, (x, y, z) in enumerate(m.coords)]
+    lines += ["elements:", "- type: beam2", "  connectivity:"]
+    lines += ["  - [" + ", ".join(str(v) for v in [e, *row]) + "]" for e, row in enumerate(m.conn)]
+    lines += ["sets:", "  node:", "    root:", "    - 0", "    tip:", f"    - {n}"]
+    lines += ["  element:", "    all:", f"    - [0, {n}]"]
+    lines += ["sections:", "- type: beam", "  material: mat1", "  elementSet: all",
+              "  orientation: [" + ", ".join(repr(float(v)) for v in (*x_dir, 0.0, 1.0, 0.0)) + "]",
+              "  beamProps:", "    area: 0.1",
+              f"    I: [{moments[0]!r}, 0.0, {1.0 * 0.1**3 / 12!r}, {0.1 * 1.0**3 / 12!r}, {moments[1]!r}]",
+              "    J: 0.00028",
+              "materials:", "  mat1:", "    density: 1.0", "    elastic:", "      E: [1000000.0]", "      nu: 0.0"]
+    (d / "model.yaml").write_text("\n".join(lines) + "\n")
+    cons = ["constraints:"]
+    for dof in range(1, 7):
+        cons += ["- type: displacement", "  terms:", "  - nodeSet: root", f"    dof: {dof}", "    coef: 1.0",
+                 "  rhs: 0.0"]
+    (d / "constraints.yaml").write_text("\n".join(cons) + "\n")
+    (d / "loads.yaml").write_text("loads:\n- type: nodalForce\n  nodeSet: tip\n  load: [0.0, 0.0, 2.0, 0.0, 0.0, 0.0]\n")
+    (d / "objective.yaml").write_text("objectiveTerms:\n- category: displacement\n  operator: powerNorm\n"
+                                      "  nodeSet: tip\n  component: 3\n  coefficient: 1.0\n  exponent: 1.0\n")
+    job = ["jobCommands:",
+           "- command: readModelInput", "  fileName: model.yaml",
+           "- command: readConstraints", "  fileName: constraints.yaml",
+           "- command: readLoads", "  fileName: loads.yaml",
+           "- command: readObjectiveInput", "  fileName: objective.yaml",
+           "- command: solve", "  elastic: yes", "  dynamic: no", "  solverMethod: iterative",
+           "  convergenceTol: 1.0e-12", "  maxIterations: 400000",
+           "- command: calcObjective",
+           "- command: writeNodeResults", f"  fileName: {d / 'nodes.csv'}", "  nodeSet: tip",
+           "  fields:", "  - displacement",
+           "- command: writeObjective", f"  fileName: {d / 'obj.csv'}"]
+    (d / "job.yaml").write_text("\n".join(job) + "\n")
+    return m
+
+
+def test_beam_job_problem(tmp_path):
+    """beamProps and orientation reach the section table; an element numbered
+    against the section's x direction flips the odd moments I1 and I5."""
+    write_beam_job(tmp_path, moments=(1e-3, 2e-5))
+    r = J.JobRunner(tmp_path / "job.yaml")
+    r.cmd_readModelInput(r.cmds[0])
+    sec = r.model.sections[0]
+    assert sec["area"] == 0.1 and sec["J"] == 0.00028 and len(sec["I"]) == 5
+    p = r._problem()
+    assert p.mesh.elem_type == 2 and p.mesh.dpn == 6
+    assert p.beam_sections.shape == (20, 10)
+    np.testing.assert_allclose(p.beam_sections[0], [0.1, 1e-3, 0.0, 0.1**3 / 12, 0.1 / 12, 2e-5, 0.00028, 0, 1, 0])
+    d = tmp_path / "rev"
+    d.mkdir()
+    write_beam_job(d, reverse=True, moments=(1e-3, 2e-5))
+    rb = J.JobRunner(d / "job.yaml")
+    rb.cmd_readModelInput(rb.cmds[0])
+    pb = rb._problem()
+    np.testing.assert_allclose(pb.beam_sections[:, [1, 5]], np.tile([-1e-3, -2e-5], (20, 1)))
+    # a section x direction across the element is not a consistent beam
+    d2 = tmp_path / "skew"
+    d2.mkdir()
+    write_beam_job(d2, x_dir=(1.0, 1.0, 0.0))
+    rs = J.JobRunner(d2 / "job.yaml")
+    rs.cmd_readModelInput(rs.cmds[0])
+    with pytest.raises(NotImplementedError, match="along the element"):
+        rs._problem()

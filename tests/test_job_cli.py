@@ -45,10 +45,10 @@ def test_parse_matches_python_readers(cli, tmp_path):
 
 
 def test_cli_errors(cli, tmp_path):
-    (tmp_path / "m.yaml").write_text("elements:\n- type: beam2\n")
+    (tmp_path / "m.yaml").write_text("elements:\n- type: shell3\n")
     (tmp_path / "job.yaml").write_text("jobCommands:\n- command: readModelInput\n  fileName: m.yaml\n")
     out = subprocess.run([cli, "--parse", str(tmp_path / "job.yaml")], capture_output=True, text=True)
-    assert out.returncode == 1 and "beam2 is not on the GPU path" in out.stderr
+    assert out.returncode == 1 and "shell3 is not on the GPU path" in out.stderr
     (tmp_path / "m.yaml").write_text("nodes:\n- [0, 0.0, 0.0, 0.0]\n")
     (tmp_path / "job.yaml").write_text("jobCommands:\n- command: readModelInput\n  fileName: m.yaml\n"
                                        "- command: buildMesh\n")
