@@ -837,7 +837,10 @@ def run_ours(a):
 
     # ---- accuracy at full size: the benchmark's 1e-8 solution and gradient
     # against the same library at 1e-11 (FP64 operator); never fatal
-    accuracy = {}
+    accuracy = {"reference_parity": "unpinned at solver precision: the oracle restates the reference's "
+                                    "algorithm in C++ and is tied to the reference by its analytic known answers "
+                                    "(rtol 1e-3 to 2e-2; singleHex 2e-5), finite differences and self-consistency; "
+                                    "the reference (Rust) cannot be built here"}
     if rank == 0:
         try:
             g.assemble(precision=48)  # the benchmark's operator and solve
