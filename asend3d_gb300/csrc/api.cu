@@ -1802,7 +1802,8 @@ int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t compone
         for (size_t q = 0; q < set.size(); ++q) {
             const int e = set[q];
             double dC[36];
-            if (!c.ortho.empty()) material_dC_props(category, component, &c.ortho[(size_t)e * 9], dC);
+            if (c.type == 2) beam_section_dC(category, component, &c.beam_sec[(size_t)e * 10], dC);
+            else if (!c.ortho.empty()) material_dC_props(category, component, &c.ortho[(size_t)e * 9], dC);
             else material_dC(category, component, c.E[e], c.nu[e], dC);
             const double* P = &c.h_pairs[(size_t)e * 36];
             double s = 0.0;

@@ -295,12 +295,16 @@ void adjoint_contract(Ctx& c, const double* d_a, const double* d_b, double* d_g,
 }
 
 void adjoint_pairs(Ctx& c, const double* d_a, const double* d_b, double* d_P, bool accumulate) {
+    if (c.type == 2) {
+        beam_pairs(c, d_a, d_b, d_P, accumulate);
+        return;
+    }
     if (c.type == 81) {
         brickim_pairs(c, d_a, d_b, d_P, accumulate);
         return;
     }
     if (c.type != 8 && c.type != 4 && c.type != 10)
-        throw InputError("strain-pair tensors are built for hex8, brickIM, tet4 and tet10 meshes");
+        throw InputError("strain-pair tensors are built for hex8, brickIM, tet4, tet10 and beam2 meshes");
     const int blocks = (c.n_el + 127) / 128;
     if (c.nn == 8)
         k_adjoint_pairs<8><<<blocks, 128, 0, c.stream>>>(c.n_el, c.d_conn.p, c.d_xyz.p, d_a, d_b, d_P, accumulate ? 1 : 0);

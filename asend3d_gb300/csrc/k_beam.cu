@@ -16,6 +16,9 @@
 //                                  and the first-moment / product couplings)
 //   element_properties.rs:1410-1500 section mass
 //   element_equations.rs:206-418, :19-57, :420-626  K, condensation, M (node DOF)
+//   model_analysis.rs:1379-1457     d_relasticd_d: section-strain pairs for material
+//                                  DVs (E1 and G1..G3 enter the section stiffness
+//                                  separately; nu does not)
 // Frame: rows e1 = element axis, e3 = e1 x v / |e1 x v|, e2 = e3 x e1 (the
 // section orientation of section_meth.rs:21-50 with the element axis as x).
 //
@@ -43,8 +46,11 @@ struct BeamLocal {
 };
 
 // Frame and condensed section-frame stiffness of element e (sec[10] = area,
-// I1..I5, J, v).  Returns false on a degenerate frame (rejected on the host).
-__device__ bool beam_local(BeamLocal& B, const double* x0, const double* x1, double E, double nu, const double* sec) {
+// I1..I5, J, v); kfull (may be null) receives the uncondensed 14 x 14
+// section-frame stiffness.  Returns false on a degenerate frame (rejected on
+// the host).
+__device__ bool beam_local(BeamLocal& B, const double* x0, const double* x1, double E, double nu, const double* sec,
+                           double* kfull = nullptr) {
     double d[3] = {x1[0] - x0[0], x1[1] - x0[1], x1[2] - x0[2]};
     const double L = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     if (!(L > 0.0)) return false;
@@ -116,6 +122,9 @@ __device__ bool beam_local(BeamLocal& B, const double* x0, const double* x1, dou
             }
         }
     }
+    if (kfull)
+        for (int i = 0; i < 14; ++i)
+            for (int j = 0; j < 14; ++j) kfull[14 * i + j] = K[i][j];
     // condense the bubbles: K_nn - K_ni K_ii^-1 K_in (2 x 2 inverse)
     const double det = K[12][12] * K[13][13] - K[12][13] * K[13][12];
     const double i00 = K[13][13] / det, i01 = -K[12][13] / det, i10 = -K[13][12] / det, i11 = K[12][12] / det;
@@ -256,6 +265,74 @@ k_beam_adjoint(int n_el, const int32_t* __restrict__ conn2, const double* __rest
     g[e] = accumulate ? g[e] + v : v;
 }
 
+// node DOF of element e in the section frame: f_loc[6 k + 3 t + p] = R f_glob
+__device__ void beam_to_local(const BeamLocal& B, const double* f, int n0, int n1, double* fl) {
+    for (int k = 0; k < 2; ++k) {
+        const size_t base = 6 * (size_t)(k ? n1 : n0);
+        for (int t3 = 0; t3 < 2; ++t3)
+            for (int p = 0; p < 3; ++p) {
+                double acc = 0.0;
+                for (int c = 0; c < 3; ++c) acc += B.R[3 * p + c] * f[base + 3 * t3 + c];
+                fl[6 * k + 3 * t3 + p] = acc;
+            }
+    }
+}
+
+// Section-strain pairs P_e[36] = sum_ip detJ eps(a) eps(b)^T with the bubble
+// amplitudes recovered (alpha = -K_ii^-1 K_in f, update_internal
+// element_equations.rs:147-194), so that a^T (dK_e/dD) b = sum (dC/dD) : P_e
+// for any section-stiffness parameter D (d_relasticd_d,
+// model_analysis.rs:1379-1457).
+__global__ void __launch_bounds__(kBT)
+k_beam_pairs(int n_el, const int32_t* __restrict__ conn2, const double* __restrict__ xyz,
+             const double* __restrict__ E, const double* __restrict__ nu, const double* __restrict__ sec,
+             const double* __restrict__ fa, const double* __restrict__ fb, double* __restrict__ P, int accumulate) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_el) return;
+    BeamLocal B;
+    double K[196];
+    const int n0 = conn2[2 * (size_t)e], n1 = conn2[2 * (size_t)e + 1];
+    double acc[36];
+    for (int i = 0; i < 36; ++i) acc[i] = 0.0;
+    if (beam_local(B, xyz + 3 * (size_t)n0, xyz + 3 * (size_t)n1, E[e], nu[e], sec + 10 * (size_t)e, K)) {
+        double la[14], lb[14];
+        beam_to_local(B, fa, n0, n1, la);
+        beam_to_local(B, fb, n0, n1, lb);
+        const double det = K[14 * 12 + 12] * K[14 * 13 + 13] - K[14 * 12 + 13] * K[14 * 13 + 12];
+        for (double* f : {la, lb}) {
+            double r0 = 0.0, r1 = 0.0;
+            for (int c = 0; c < 12; ++c) {
+                r0 += K[14 * 12 + c] * f[c];
+                r1 += K[14 * 13 + c] * f[c];
+            }
+            f[12] = -(K[14 * 13 + 13] * r0 - K[14 * 12 + 13] * r1) / det;
+            f[13] = -(-K[14 * 13 + 12] * r0 + K[14 * 12 + 12] * r1) / det;
+        }
+        const double a = B.a;
+        for (int ip = 0; ip < 2; ++ip) {
+            const double s = ip ? kG : -kG;
+            const double N0 = 0.5 * (1.0 - s), N1 = 0.5 * (1.0 + s), d0 = -0.5 / a, d1 = 0.5 / a, db = -2.0 * s / a;
+            double ea[6], eb[6];
+            const double* fs[2] = {la, lb};
+            double* es[2] = {ea, eb};
+            for (int q = 0; q < 2; ++q) {
+                const double* f = fs[q];
+                double* ev = es[q];
+                ev[0] = d0 * f[0] + d1 * f[6];
+                ev[1] = d0 * f[1] + d1 * f[7] - (N0 * f[5] + N1 * f[11]) + db * f[12];
+                ev[2] = d0 * f[2] + d1 * f[8] + (N0 * f[4] + N1 * f[10]) + db * f[13];
+                ev[3] = d0 * f[3] + d1 * f[9];
+                ev[4] = d0 * f[4] + d1 * f[10];
+                ev[5] = d0 * f[5] + d1 * f[11];
+            }
+            for (int i = 0; i < 6; ++i)
+                for (int j = 0; j < 6; ++j) acc[6 * i + j] += ea[i] * eb[j] * a;
+        }
+    }
+    double* Pe = P + 36 * (size_t)e;
+    for (int i = 0; i < 36; ++i) Pe[i] = accumulate ? Pe[i] + acc[i] : acc[i];
+}
+
 // element matrices (checks): ke/me [count][12][12], global DOF 6 a + c
 __global__ void __launch_bounds__(kBT)
 k_beam_export(int e0, int n, const int32_t* __restrict__ conn2, const double* __restrict__ xyz,
@@ -311,6 +388,36 @@ void beam_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, b
                                                                    accumulate ? 1 : 0);
     ASEND_CUDA(cudaGetLastError());
     ++c.launches;
+}
+
+void beam_pairs(Ctx& c, const double* d_a, const double* d_b, double* d_P, bool accumulate) {
+    require_sections(c);
+    k_beam_pairs<<<(c.n_el + kBT - 1) / kBT, kBT, 0, c.stream>>>(c.n_el, c.d_shell_conn.p, c.d_shell_xyz.p, c.d_E.p,
+                                                                 c.d_nu.p, c.d_beam_sec.p, d_a, d_b, d_P,
+                                                                 accumulate ? 1 : 0);
+    ASEND_CUDA(cudaGetLastError());
+    ++c.launches;
+}
+
+void beam_section_dC(int category, int component, const double* sec, double* dC) {
+    for (int i = 0; i < 36; ++i) dC[i] = 0.0;
+    auto set = [&](int i, int j, double v) { dC[6 * i + j] = dC[6 * j + i] = v; };
+    if (category == ASEND_DV_MODULUS && component == 1) {  // E1: EA, E I1, -E I2, E I3, -E I5, E I4
+        set(0, 0, sec[0]);
+        set(0, 4, sec[1]);
+        set(0, 5, -sec[2]);
+        set(4, 4, sec[3]);
+        set(4, 5, -sec[5]);
+        set(5, 5, sec[4]);
+    } else if (category == ASEND_DV_SHEAR_MODULUS && component == 1) {  // G1: GA, -G I1, GJ
+        set(1, 1, sec[0]);
+        set(1, 3, -sec[1]);
+        set(3, 3, sec[6]);
+    } else if (category == ASEND_DV_SHEAR_MODULUS && component == 2) {  // G2: GA of the second shear
+        set(2, 2, sec[0]);
+    } else if (category == ASEND_DV_SHEAR_MODULUS && component == 3) {  // G3: G I2
+        set(2, 3, sec[2]);
+    }
 }
 
 void beam_element_matrices(Ctx& c, int e0, int n, double* ke_host, double* me_host) {

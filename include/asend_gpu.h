@@ -334,7 +334,13 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
  * hex8, tet4 and brickIM meshes: brickIM strains include the condensed
  * modes recovered per element (alpha = -Kii^-1 Kie f_e for both fields,
  * update_internal element_equations.rs:19-194); elements with orthotropic
- * constants (asend_set_orthotropic) use their own S. */
+ * constants (asend_set_orthotropic) use their own S.  beam2 meshes: the pairs
+ * are of the section strains (axial, two shears, twist, two curvatures) with
+ * the bubbles recovered, and the DVs act on the section stiffness as the
+ * reference's get_beam_stiff_dfd0 does: modulus component 1 scales the E
+ * entries, shearModulus components 1 / 2 / 3 the G entries of the first
+ * shear and twist / the second shear / the I2 coupling, the other
+ * components and poissonRatio give zero. */
 #define ASEND_DV_MODULUS 0
 #define ASEND_DV_SHEAR_MODULUS 1
 #define ASEND_DV_POISSON_RATIO 2

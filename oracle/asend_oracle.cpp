@@ -731,32 +731,36 @@ void beam_msec(double rho, const double* sec, double* M) {
 // the frame, as get_inst_disp_dfd0 (element_soln_fields.rs:650-690) maps a
 // global DOF to section-frame displacements; the internal DOF are section-frame
 // amplitudes.  Returns false for a zero-length element or v along the axis.
-bool beam_km(const double* xyz, double E, double nu, double rho, const double* sec, double* ke, double* me) {
-    double R[9], L;
-    if (!beam_frame(xyz, sec + 7, R, &L)) return false;
-    constexpr int tot = 14, nd = 12;
-    double C[36], K[tot * tot] = {0.0};
-    beam_cmat(E, nu, sec, C);
-    const double a = 0.5 * L;  // detJ
+// Section-strain rows B[6][14] at s: global node DOF 6 k + c, then the two
+// section-frame bubble amplitudes.
+void beam_bmat(const double* R, double a, double s, double B[6][14]) {
+    const double N[2] = {0.5 * (1.0 - s), 0.5 * (1.0 + s)}, dN[2] = {-0.5 / a, 0.5 / a};
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 14; ++j) B[i][j] = 0.0;
+    for (int k = 0; k < 2; ++k)
+        for (int c = 0; c < 3; ++c) {
+            const int ct = 6 * k + c, cr = 6 * k + 3 + c;
+            B[0][ct] += dN[k] * R[c];
+            B[1][ct] += dN[k] * R[3 + c];
+            B[2][ct] += dN[k] * R[6 + c];
+            B[1][cr] -= N[k] * R[6 + c];  // - th3
+            B[2][cr] += N[k] * R[3 + c];  // + th2
+            B[3][cr] += dN[k] * R[c];
+            B[4][cr] += dN[k] * R[3 + c];
+            B[5][cr] += dN[k] * R[6 + c];
+        }
+    B[1][12] = -2.0 * s / a;  // bubble on u2
+    B[2][13] = -2.0 * s / a;  // bubble on u3
+}
+
+// Uncondensed stiffness K[14][14] of a beam2 element with section stiffness C.
+void beam_kfull(const double* R, double a, const double* C, double* K) {
+    constexpr int tot = 14;
+    for (int i = 0; i < tot * tot; ++i) K[i] = 0.0;
     const double sp[2] = {-kR1ORt3, kR1ORt3};
     for (int ip = 0; ip < 2; ++ip) {
-        const double s = sp[ip];
-        const double N[2] = {0.5 * (1.0 - s), 0.5 * (1.0 + s)}, dN[2] = {-0.5 / a, 0.5 / a};
-        double B[6][tot] = {{0.0}};
-        for (int k = 0; k < 2; ++k)
-            for (int c = 0; c < 3; ++c) {
-                const int ct = 6 * k + c, cr = 6 * k + 3 + c;
-                B[0][ct] += dN[k] * R[c];
-                B[1][ct] += dN[k] * R[3 + c];
-                B[2][ct] += dN[k] * R[6 + c];
-                B[1][cr] -= N[k] * R[6 + c];  // - th3
-                B[2][cr] += N[k] * R[3 + c];  // + th2
-                B[3][cr] += dN[k] * R[c];
-                B[4][cr] += dN[k] * R[3 + c];
-                B[5][cr] += dN[k] * R[6 + c];
-            }
-        B[1][12] = -2.0 * s / a;  // bubble on u2
-        B[2][13] = -2.0 * s / a;  // bubble on u3
+        double B[6][tot];
+        beam_bmat(R, a, sp[ip], B);
         double CB[6][tot];
         for (int i = 0; i < 6; ++i)
             for (int c = 0; c < tot; ++c) {
@@ -770,20 +774,34 @@ bool beam_km(const double* xyz, double E, double nu, double rho, const double* s
                 for (int k = 0; k < 6; ++k) acc += B[k][r] * CB[k][c];
                 K[r * tot + c] += acc;
             }
-        if (me) {
-            if (ip == 0)
-                for (int i = 0; i < nd * nd; ++i) me[i] = 0.0;
-            double Ms[36], RM[36];
-            beam_msec(rho, sec, Ms);
-            // Rb^T Ms Rb with Rb = diag(R, R)
-            auto rb = [&](int p, int q) { return (p / 3 == q / 3) ? R[3 * (p % 3) + q % 3] : 0.0; };
-            for (int c = 0; c < 6; ++c)
-                for (int d = 0; d < 6; ++d) {
-                    double acc = 0.0;
-                    for (int p = 0; p < 6; ++p)
-                        for (int q = 0; q < 6; ++q) acc += rb(p, c) * Ms[6 * p + q] * rb(q, d);
-                    RM[6 * c + d] = acc;
-                }
+    }
+}
+
+bool beam_km(const double* xyz, double E, double nu, double rho, const double* sec, double* ke, double* me) {
+    double R[9], L;
+    if (!beam_frame(xyz, sec + 7, R, &L)) return false;
+    constexpr int tot = 14, nd = 12;
+    double C[36], K[tot * tot];
+    beam_cmat(E, nu, sec, C);
+    const double a = 0.5 * L;  // detJ
+    beam_kfull(R, a, C, K);
+    if (me) {
+        for (int i = 0; i < nd * nd; ++i) me[i] = 0.0;
+        double Ms[36], RM[36];
+        beam_msec(rho, sec, Ms);
+        // Rb^T Ms Rb with Rb = diag(R, R)
+        auto rb = [&](int p, int q) { return (p / 3 == q / 3) ? R[3 * (p % 3) + q % 3] : 0.0; };
+        for (int c = 0; c < 6; ++c)
+            for (int d = 0; d < 6; ++d) {
+                double acc = 0.0;
+                for (int p = 0; p < 6; ++p)
+                    for (int q = 0; q < 6; ++q) acc += rb(p, c) * Ms[6 * p + q] * rb(q, d);
+                RM[6 * c + d] = acc;
+            }
+        const double sp[2] = {-kR1ORt3, kR1ORt3};
+        for (int ip = 0; ip < 2; ++ip) {
+            const double s = sp[ip];
+            const double N[2] = {0.5 * (1.0 - s), 0.5 * (1.0 + s)};
             for (int k = 0; k < 2; ++k)
                 for (int l = 0; l < 2; ++l)
                     for (int c = 0; c < 6; ++c)
@@ -796,6 +814,51 @@ bool beam_km(const double* xyz, double E, double nu, double rho, const double* s
         double rhs[2] = {K[12 * tot + r], K[13 * tot + r]}, x[2];
         givens_solve(x, Kii, rhs, 2);
         for (int c = 0; c < nd; ++c) ke[c * nd + r] = K[c * tot + r] - (K[c * tot + 12] * x[0] + K[c * tot + 13] * x[1]);
+    }
+    return true;
+}
+
+// Section-strain pairs P[36] = sum_ip detJ eps(lambda) eps(u)^T of one beam2
+// element with its bubble amplitudes recovered from the node values
+// (alpha = -K_ii^-1 K_in f, update_internal element_equations.rs:147-194), so
+// that lambda^T (dK_e/dD) u = sum_ij (dC/dD)_ij P_ij for any section-stiffness
+// parameter D (d_relasticd_d, model_analysis.rs:1379-1457).
+bool beam_pairs(const double* xyz, double E, double nu, const double* sec, const double* ue, const double* le,
+                double* P) {
+    double R[9], L;
+    if (!beam_frame(xyz, sec + 7, R, &L)) return false;
+    constexpr int tot = 14;
+    double C[36], K[tot * tot];
+    beam_cmat(E, nu, sec, C);
+    const double a = 0.5 * L;
+    beam_kfull(R, a, C, K);
+    double Kii[4] = {K[12 * tot + 12], K[12 * tot + 13], K[13 * tot + 12], K[13 * tot + 13]};
+    givens_factor(Kii, 2);
+    double uf[tot], lf[tot];
+    for (int c = 0; c < 12; ++c) {
+        uf[c] = ue[c];
+        lf[c] = le[c];
+    }
+    for (double* f : {uf, lf}) {
+        double rhs[2] = {0.0, 0.0}, x[2];
+        for (int i = 0; i < 2; ++i)
+            for (int c = 0; c < 12; ++c) rhs[i] += K[(12 + i) * tot + c] * f[c];
+        givens_solve(x, Kii, rhs, 2);
+        f[12] = -x[0];
+        f[13] = -x[1];
+    }
+    for (int i = 0; i < 36; ++i) P[i] = 0.0;
+    const double sp[2] = {-kR1ORt3, kR1ORt3};
+    for (int ip = 0; ip < 2; ++ip) {
+        double B[6][tot], eu[6] = {0}, el[6] = {0};
+        beam_bmat(R, a, sp[ip], B);
+        for (int q = 0; q < 6; ++q)
+            for (int c = 0; c < tot; ++c) {
+                eu[q] += B[q][c] * uf[c];
+                el[q] += B[q][c] * lf[c];
+            }
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) P[6 * i + j] += el[i] * eu[j] * a;
     }
     return true;
 }
@@ -1658,6 +1721,35 @@ int orc_beam_element(const double* xyz, double E, double nu, double rho, const d
     return beam_km(xyz, E, nu, rho, sec, ke, me) ? 0 : -2;
 }
 
+// dC/dD of the beam section stiffness (get_beam_stiff_dfd0,
+// element_properties.rs:921-1010) for a unit change of one material DV:
+// category 0 modulus (component 1: E1 in EA, E I1, -E I2, E I3, -E I5, E I4;
+// components 2, 3 do not enter), 1 shearModulus (component 1: G1 in GA of the
+// first shear, -G I1, G J; 2: G2 in GA of the second shear; 3: G3 in G I2),
+// 2 poissonRatio (does not enter).
+int orc_beam_section_dC(int32_t category, int32_t component, const double* sec, double* dC) {
+    if (category < 0 || category > 2 || component < 1 || component > 3 || !sec || !dC) return -1;
+    for (int i = 0; i < 36; ++i) dC[i] = 0.0;
+    auto set = [&](int i, int j, double v) { dC[6 * i + j] = dC[6 * j + i] = v; };
+    if (category == 0 && component == 1) {
+        set(0, 0, sec[0]);
+        set(0, 4, sec[1]);
+        set(0, 5, -sec[2]);
+        set(4, 4, sec[3]);
+        set(4, 5, -sec[5]);
+        set(5, 5, sec[4]);
+    } else if (category == 1 && component == 1) {
+        set(1, 1, sec[0]);
+        set(1, 3, -sec[1]);
+        set(3, 3, sec[6]);
+    } else if (category == 1 && component == 2) {
+        set(2, 2, sec[0]);
+    } else if (category == 1 && component == 3) {
+        set(2, 3, sec[2]);
+    }
+    return 0;
+}
+
 int orc_set_damping(orc_model* m, double ray_cm, double ray_ck, const double* D) {
     m->ray_cm = ray_cm;
     m->ray_ck = ray_ck;
@@ -2306,7 +2398,22 @@ int orc_newmark_adjoint(orc_model* m, int32_t n_steps, double dt, double beta, d
 // contracted with (lambda_e, u_e) equals the full dK/dD contracted with the
 // recovered (lambda, u).  Solid types (8, 81, 4, 10); P[n_el][36].
 int orc_adjoint_strain_pairs(const orc_model* m, const double* u, const double* lam, double* P) {
-    if (!m->assembled || m->structural()) return -1;
+    if (!m->assembled || m->shell) return -1;
+    if (m->beam) {  // section strains of beam2 (beam_pairs)
+        for (int e = 0; e < m->n_el; ++e) {
+            double xyz[6], ue[12], le[12];
+            for (int a = 0; a < 2; ++a) {
+                const int nd = m->conn2[(size_t)e * 2 + a];
+                for (int j = 0; j < 3; ++j) xyz[3 * a + j] = m->phys_xyz[3 * (size_t)nd + j];
+                for (int c = 0; c < 6; ++c) {
+                    ue[6 * a + c] = u[6 * (size_t)nd + c];
+                    le[6 * a + c] = lam[6 * (size_t)nd + c];
+                }
+            }
+            beam_pairs(xyz, m->E[e], m->nu[e], &m->beam_sec[(size_t)e * 10], ue, le, P + (size_t)e * 36);
+        }
+        return 0;
+    }
     const TypeInfo& t = m->ti;
     const int nn = t.nn;
     for (int e = 0; e < m->n_el; ++e) {

@@ -143,7 +143,8 @@ int orc_newmark_adjoint(orc_model* m, int32_t n_steps, double dt, double beta, d
                         const double* obj_w, double* L_out, double* gE);
 
 /* Strain-pair tensors P[n_el][36] = sum_gp w detJ eps(lambda_e) eps(u_e)^T of
- * solid elements (brickIM with its condensed modes recovered). */
+ * solid elements (brickIM with its condensed modes recovered) and of beam2
+ * section strains (bubbles recovered). */
 int orc_adjoint_strain_pairs(const orc_model* m, const double* u, const double* lam, double* P);
 
 int orc_reorder_nodes(const orc_model* m, int32_t block_dim, int32_t* order_out);
@@ -165,6 +166,9 @@ int orc_set_beam_sections(orc_model* m, const double* sec);
  * the axis. */
 int orc_beam_element(const double* xyz, double E, double nu, double rho, const double* sec, double* ke,
                      double* me);
+/* dC[36] of the beam section stiffness per unit change of a material DV
+ * (category 0 modulus, 1 shearModulus, 2 poissonRatio; component 1-3). */
+int orc_beam_section_dC(int32_t category, int32_t component, const double* sec, double* dC);
 
 /* Element-category objective term at the element centroids (category 0
  * stress, 1 strain, 2 strainEnergy; component 1-6 for 0/1; optr 0 powerNorm,

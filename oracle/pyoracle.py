@@ -79,6 +79,7 @@ def load():
             "orc_set_shell_sections": (C.c_int, [C.c_void_p, P_d, P_d]),
             "orc_set_beam_sections": (C.c_int, [C.c_void_p, P_d]),
             "orc_beam_element": (C.c_int, [P_d, C.c_double, C.c_double, C.c_double, P_d, P_d, P_d]),
+            "orc_beam_section_dC": (C.c_int, [C.c_int32, C.c_int32, P_d, P_d]),
             "orc_element_objective": (C.c_int, [C.c_void_p, P_d, C.c_int32, P_i, C.c_int32, C.c_int32, C.c_int32,
                                                 C.c_double, C.c_double, C.c_int32, P_d, P_d, P_d, P_d, P_d]),
         }
@@ -388,3 +389,12 @@ def beam_element(xyz, E, nu, rho, sec):
     if rc != 0:
         raise ValueError(f"orc_beam_element failed ({rc})")
     return ke.reshape(12, 12), me.reshape(12, 12)
+
+
+def beam_section_dC(category, component, sec):
+    """dC[6][6] of the beam section stiffness per unit change of a material DV."""
+    lib = load()
+    sec = np.ascontiguousarray(sec, np.float64)
+    dC = np.zeros(36)
+    assert lib.orc_beam_section_dC(int(category), int(component), _p(sec), _p(dC)) == 0
+    return dC.reshape(6, 6)

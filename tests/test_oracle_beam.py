@@ -185,3 +185,41 @@ def test_first_frequency_pin(oracle_lib):
     assert f1 == pytest.approx(pin["value"], rel=pin["rtol"])
     # beam theory: (1.8751^2 / (2 pi L^2)) sqrt(E I / (rho A)) (shear and rotary inertia: < 1e-4 here)
     assert f1 == pytest.approx(1.8751040687**2 / (2 * np.pi * L**2) * np.sqrt(E0 * IZZ / A), rel=2e-4)
+
+
+def _tip_w(oracle_lib, E, nu, n=20):
+    p = cantilever(n)
+    p.E = np.full(n, E)
+    p.nu = np.full(n, nu)
+    return tip_solution(oracle_lib, p)[0][2]
+
+
+def test_material_dv_pairs(oracle_lib):
+    """Section-strain pairs of beam2 (bubbles recovered): the isotropic modulus
+    gradient is -(C / E) : P per element (1e-10), and the reference's separate
+    modulus (E with G held) and shearModulus (G with E held) DVs match central
+    differences of the oracle (E and nu moved together to hold G or E; 1e-5)."""
+    n = 20
+    p = cantilever(n)
+    t, u, o = tip_solution(oracle_lib, p)
+    dldu = np.zeros(o.n_dof)
+    dldu[6 * n + 2] = 1.0
+    g, lam, rc, _ = o.adjoint(u, dLdu=dldu, precond=oracle_lib.PC_DIRECT)
+    assert rc == 0
+    P = o.strain_pairs(u, lam)
+    sec = p.beam_sections[0]
+    dE = oracle_lib.beam_section_dC(0, 1, sec)
+    dG = sum(oracle_lib.beam_section_dC(1, k, sec) for k in (1, 2, 3))
+    G0 = E0 / 2.0
+    for e in range(n):
+        assert -np.sum((dE * E0 + dG * G0) / E0 * P[e]) == pytest.approx(g[e], rel=1e-10)
+    assert np.all(oracle_lib.beam_section_dC(2, 1, sec) == 0.0)
+    g_E = -sum(np.sum(dE * P[e]) for e in range(n))
+    g_G = -sum(np.sum(dG * P[e]) for e in range(n))
+    h = 1e-3
+    # E with G held: nu' = E' / (2 G) - 1
+    wE = [_tip_w(oracle_lib, E0 * (1 + s * h), E0 * (1 + s * h) / (2 * G0) - 1.0) for s in (1, -1)]
+    assert g_E == pytest.approx((wE[0] - wE[1]) / (2 * h * E0), rel=1e-5)
+    # G with E held: nu' = E / (2 G') - 1
+    wG = [_tip_w(oracle_lib, E0, E0 / (2 * G0 * (1 + s * h)) - 1.0) for s in (1, -1)]
+    assert g_G == pytest.approx((wG[0] - wG[1]) / (2 * h * G0), rel=1e-5)
