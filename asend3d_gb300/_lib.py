@@ -104,6 +104,7 @@ SIGNATURES = [
     ("asend_shell_section", c_int, [c_int, P_dbl, c_dbl, P_dbl, P_dbl]),
     ("asend_set_shell_sections", c_int, [C.c_void_p, P_dbl, P_dbl]),
     ("asend_set_beam_sections", c_int, [C.c_void_p, P_dbl]),
+    ("asend_set_beam_section_matrices", c_int, [C.c_void_p, P_dbl, P_dbl]),
     ("asend_set_element_objective", c_int, [C.c_void_p, P_dbl, P_dbl]),
     ("asend_add_modulus_design_var", c_int, [C.c_void_p, c_int, c_int, P_dbl]),
     ("asend_design_var_gradient", c_int, [C.c_void_p, P_dbl, P_dbl]),

@@ -159,9 +159,10 @@ struct Section {
     std::vector<Layer> layers;
     double z_offset = 0.0;
     std::vector<double> orientation;  // xDir, xyVec
-    // beamProps (model_input.rs:561-596): area, I[5], J
+    // beamProps (model_input.rs:561-596): area, I[5], J, given stiffness / mass
+    // matrices (symmetric, section_meth.rs:61-71; empty when not given)
     double area = 0.0, J = 0.0;
-    std::vector<double> I;
+    std::vector<double> I, stiffness, mass;
 };
 struct Material {
     double density = 0.0;
@@ -237,7 +238,7 @@ Model read_model(const std::string& path) {
             }
         } else if (h[0] == "sections") {
             if (h[1] == "type" && d.size() == 1) {
-                m.sections.push_back(Section{d[0], "", "", {}, 0.0, {}, 0.0, 0.0, {}});
+                m.sections.push_back(Section{d[0], "", "", {}, 0.0, {}, 0.0, 0.0, {}, {}, {}});
             } else if (m.sections.empty()) {
                 continue;
             } else if (h[1] == "material" && d.size() == 1) {
@@ -263,7 +264,13 @@ Model read_model(const std::string& path) {
                     s.I.clear();
                     for (const auto& x : d) s.I.push_back(num(x));
                 } else if (h[2] == "J" && d.size() == 1) s.J = num(d[0]);
-                else if (h[2] == "stiffness" || h[2] == "mass" || h[2] == "damping" || h[2] == "expLoadCoef")
+                else if ((h[2] == "stiffness" || h[2] == "mass") && d.size() == 3) {
+                    std::vector<double>& mat = h[2] == "stiffness" ? s.stiffness : s.mass;
+                    if (mat.empty()) mat.assign(36, 0.0);
+                    const int r = (int)num(d[0]) - 1, c = (int)num(d[1]) - 1;
+                    if (r < 0 || r > 5 || c < 0 || c > 5) throw Fail("beam section matrix index out of range");
+                    mat[6 * r + c] = mat[6 * c + r] = num(d[2]);
+                } else if (h[2] == "damping" || h[2] == "expLoadCoef")
                     throw Fail("beam section " + h[2] + " entries are not on the GPU path");
             } else if ((h[1] == "potField" || h[1] == "dampField" || h[1] == "thermField") && !d.empty()) {
                 throw Fail("section " + h[1] + " is not on the GPU path");
@@ -513,6 +520,8 @@ struct Runner {
         std::vector<double> sec_abd((size_t)ne * 81, 0.0), sec_ms((size_t)ne * 36, 0.0);
         std::vector<char> has_sec(ne, 0);
         std::vector<double> beam((size_t)ne * 10, NAN);  // area, I1..I5, J, xy-plane direction
+        std::vector<double> beam_c((size_t)ne * 36, 0.0), beam_m((size_t)ne * 36, 0.0);  // given matrices
+        bool beam_given = false;
         bool ortho = false, damped = false, layered = false;
         for (const Section& s : m.sections) {
             if (!m.elem_sets.count(s.elset)) throw Fail("section without a valid elementSet");
@@ -584,6 +593,18 @@ struct Runner {
                     }
                     const double row[10] = {s.area, im[0], im[1], im[2], im[3], im[4], s.J, ori[3], ori[4], ori[5]};
                     std::copy(row, row + 10, beam.begin() + (size_t)e * 10);
+                    // given matrices; against x: the half turn about y flips strains 2 and 5
+                    // and velocities 1, 3, 4, 6
+                    const double ts[6] = {1, -1, 1, 1, -1, 1}, tm[6] = {-1, 1, -1, -1, 1, -1};
+                    for (int i = 0; i < 6; ++i)
+                        for (int j = 0; j < 6; ++j) {
+                            if (!s.stiffness.empty())
+                                beam_c[(size_t)e * 36 + 6 * i + j] =
+                                    s.stiffness[6 * i + j] * (c < 0.0 ? ts[i] * ts[j] : 1.0);
+                            if (!s.mass.empty())
+                                beam_m[(size_t)e * 36 + 6 * i + j] = s.mass[6 * i + j] * (c < 0.0 ? tm[i] * tm[j] : 1.0);
+                        }
+                    beam_given = beam_given || !s.stiffness.empty() || !s.mass.empty();
                 }
             } else if (s.type != "solid") {
                 throw Fail(s.type + " sections are not on the GPU path");
@@ -629,6 +650,8 @@ struct Runner {
             for (double v : beam)
                 if (std::isnan(v)) throw Fail("beam2 elements need a beam section");
             check(asend_set_beam_sections(ctx, beam.data()), "set_beam_sections");
+            if (beam_given)
+                check(asend_set_beam_section_matrices(ctx, beam_c.data(), beam_m.data()), "set_beam_section_matrices");
         }
         if (ortho) check(asend_set_orthotropic(ctx, props.data()), "set_orthotropic");
         if (layered) {

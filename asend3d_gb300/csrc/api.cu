@@ -537,6 +537,7 @@ int asend_set_mesh(asend_ctx* ctx, int32_t elem_type, int32_t n_nodes, const dou
         c.d_shell_abd.release();
         c.d_shell_msec.release();
         c.beam_sec.clear();
+        c.beam_cm.clear();
         c.d_beam_sec.release();
         c.d_xyz.upload(c.xyz, c.stream);
         c.d_conn.upload(c.conn, c.stream);
@@ -856,7 +857,31 @@ int asend_set_beam_sections(asend_ctx* ctx, const double* sections) {
             require(nc > 1e-9 * nd * nv, "beam section direction v lies along the element axis");
         }
         c.beam_sec.assign(sections, sections + (size_t)c.n_el * 10);
-        c.d_beam_sec.upload(c.beam_sec, c.stream);
+        c.d_beam_sec.upload(beam_device_table(c), c.stream);
+        ASEND_CUDA(cudaStreamSynchronize(c.stream));
+        c.assembled = c.solved = false;
+        return ASEND_OK;
+    });
+}
+
+int asend_set_beam_section_matrices(asend_ctx* ctx, const double* stiffness, const double* mass) {
+    return guarded(ctx, [&](Ctx& c) {
+        require(c.type == 2, "beam section matrices take beam2 meshes");
+        require(c.beam_sec.size() == (size_t)c.n_el * 10, "set the beam sections first");
+        if (!stiffness && !mass) {
+            c.beam_cm.clear();
+        } else {
+            c.beam_cm.assign((size_t)c.n_el * 72, 0.0);
+            for (int e = 0; e < c.n_el; ++e)
+                for (int k = 0; k < 36; ++k) {
+                    const double cv = stiffness ? stiffness[(size_t)e * 36 + k] : 0.0;
+                    const double mv = mass ? mass[(size_t)e * 36 + k] : 0.0;
+                    require(std::isfinite(cv) && std::isfinite(mv), "beam section matrices must be finite");
+                    c.beam_cm[(size_t)e * 72 + k] = cv;
+                    c.beam_cm[(size_t)e * 72 + 36 + k] = mv;
+                }
+        }
+        c.d_beam_sec.upload(beam_device_table(c), c.stream);
         ASEND_CUDA(cudaStreamSynchronize(c.stream));
         c.assembled = c.solved = false;
         return ASEND_OK;
@@ -1075,6 +1100,8 @@ static int element_node_weights(const Ctx& c, int e, double* w, int64_t* dof, do
         const double* s = &c.beam_sec[(size_t)e * 10];
         require(s[1] == 0.0 && s[2] == 0.0,
                 "body loads on beam sections with first moments (I1, I2 != 0) are not built");
+        require(c.beam_cm.empty() || !(c.beam_cm[(size_t)e * 72 + 36] > 0.0),
+                "body loads on beam sections with a given mass matrix are not built");
         double x[2][3], l2 = 0.0;
         for (int a = 0; a < 2; ++a) {
             const int pn = c.conn[(size_t)e * 4 + 2 * a];
@@ -1495,7 +1522,7 @@ int asend_adjoint_gradient(asend_ctx* ctx, const asend_solve_opts* opts, double*
         // the per-element modulus gradient scales an isotropic element; with
         // orthotropic constants the gradient goes through the strain pairs
         // (asend_material_dv_gradient)
-        const bool iso = c.ortho.empty() && !c.shell_layered;
+        const bool iso = c.ortho.empty() && !c.shell_layered && !c.beam_given_stiffness();
         require(iso || !dLdE_out,
                 "per-element modulus gradients need isotropic elements; use asend_material_dv_gradient");
         const size_t n = c.n_dof;
@@ -1802,7 +1829,9 @@ int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t compone
         for (size_t q = 0; q < set.size(); ++q) {
             const int e = set[q];
             double dC[36];
-            if (c.type == 2) beam_section_dC(category, component, &c.beam_sec[(size_t)e * 10], dC);
+            if (c.type == 2 && !c.beam_cm.empty() && c.beam_cm[(size_t)e * 72] > 0.0)
+                std::fill(dC, dC + 36, 0.0);  // a given section stiffness: no E or G in it
+            else if (c.type == 2) beam_section_dC(category, component, &c.beam_sec[(size_t)e * 10], dC);
             else if (!c.ortho.empty()) material_dC_props(category, component, &c.ortho[(size_t)e * 9], dC);
             else material_dC(category, component, c.E[e], c.nu[e], dC);
             const double* P = &c.h_pairs[(size_t)e * 36];

@@ -179,9 +179,16 @@ struct Ctx {
     DArr<int32_t> d_conn;
     DArr<int32_t> d_shell_conn;  // shell4 / beam2: physical nodes per element (4 / 2)
     DArr<double> d_shell_xyz;    // shell4 / beam2: physical node coordinates
-    // beam2 sections [n_el][10]: area, I1..I5, polar moment J, xy-plane direction
-    std::vector<double> beam_sec;
+    // beam2 sections [n_el][10]: area, I1..I5, polar moment J, xy-plane direction;
+    // optional given section stiffness and mass matrices [n_el][72] (C then M,
+    // entry [0] <= 0: computed); the device table joins both per element
+    std::vector<double> beam_sec, beam_cm;
     DArr<double> d_beam_sec;
+    bool beam_given_stiffness() const {
+        for (size_t e = 0; e < beam_cm.size() / 72; ++e)
+            if (beam_cm[e * 72] > 0.0) return true;
+        return false;
+    }
     // shell4 layered sections: per-element ABD [n_el][81] and section mass
     // [n_el][36] replacing the isotropic E, nu, t section
     bool shell_layered = false;
@@ -369,6 +376,7 @@ void beam_assemble(Ctx& c, double* vals, double* mvals);
 void beam_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate);
 void beam_element_matrices(Ctx& c, int e0, int n, double* ke_host, double* me_host);
 void beam_pairs(Ctx& c, const double* d_a, const double* d_b, double* d_P, bool accumulate);
+std::vector<double> beam_device_table(const Ctx& c);
 // dC[36] of the beam section stiffness per unit change of a material DV
 void beam_section_dC(int category, int component, const double* sec, double* dC);
 // brickIM elements (k_brickim.cu)

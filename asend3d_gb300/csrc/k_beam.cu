@@ -38,6 +38,10 @@ namespace {
 
 constexpr int kBT = 128;
 constexpr double kG = 0.57735026918962576451;  // 1/sqrt(3)
+// device section table per element: area, I1..I5, J, v (3), then the section
+// stiffness and mass given as matrices (6 x 6 each; entry [0] <= 0: computed
+// from the area and moments), as the reference's beamProps stiffness / mass
+constexpr int kSecC = 10, kSecM = 46, kSecStride = 82;
 
 struct BeamLocal {
     double R[9];        // rows e1 e2 e3
@@ -83,6 +87,9 @@ __device__ bool beam_local(BeamLocal& B, const double* x0, const double* x1, dou
     C[28] = E * sec[3];
     C[29] = C[34] = -E * sec[5];
     C[35] = E * sec[4];
+    if (sec[kSecC] > 0.0)  // a given matrix (upper triangle, mirrored)
+        for (int i = 0; i < 6; ++i)
+            for (int j = i; j < 6; ++j) C[6 * i + j] = C[6 * j + i] = sec[kSecC + 6 * i + j];
     // Section-frame strain rows at a point, as (column, coefficient) lists:
     // node DOF 6k + c (c < 3 translation, c >= 3 rotation), bubbles 12 / 13.
     double K[14][14];
@@ -143,6 +150,7 @@ __device__ double beam_msec(const double* sec, double rho, int p, int q) {
         p = q;
         q = t;
     }
+    if (sec[kSecM] > 0.0) return sec[kSecM + 6 * p + q];  // a given matrix (upper triangle)
     switch (6 * p + q) {
         case 0: case 7: case 14: return rho * sec[0];
         case 4: return rho * sec[1];
@@ -205,7 +213,7 @@ k_beam_assemble(int n, const int32_t* __restrict__ elems, const int32_t* __restr
     if (t >= n) return;
     const int e = elems[t];
     BeamLocal B;
-    const double* se = sec + 10 * (size_t)e;
+    const double* se = sec + kSecStride * (size_t)e;
     if (!beam_local(B, xyz + 3 * (size_t)conn2[2 * (size_t)e], xyz + 3 * (size_t)conn2[2 * (size_t)e + 1], E[e], nu[e],
                     se))
         return;  // frames are validated on the host before assembly
@@ -239,7 +247,7 @@ k_beam_adjoint(int n_el, const int32_t* __restrict__ conn2, const double* __rest
     BeamLocal B;
     const int n0 = conn2[2 * (size_t)e], n1 = conn2[2 * (size_t)e + 1];
     double v = 0.0;
-    if (beam_local(B, xyz + 3 * (size_t)n0, xyz + 3 * (size_t)n1, E[e], nu[e], sec + 10 * (size_t)e)) {
+    if (beam_local(B, xyz + 3 * (size_t)n0, xyz + 3 * (size_t)n1, E[e], nu[e], sec + kSecStride * (size_t)e)) {
         double ul[12], ll[12];
         for (int k = 0; k < 2; ++k) {
             const size_t base = 6 * (size_t)(k ? n1 : n0);
@@ -294,7 +302,7 @@ k_beam_pairs(int n_el, const int32_t* __restrict__ conn2, const double* __restri
     const int n0 = conn2[2 * (size_t)e], n1 = conn2[2 * (size_t)e + 1];
     double acc[36];
     for (int i = 0; i < 36; ++i) acc[i] = 0.0;
-    if (beam_local(B, xyz + 3 * (size_t)n0, xyz + 3 * (size_t)n1, E[e], nu[e], sec + 10 * (size_t)e, K)) {
+    if (beam_local(B, xyz + 3 * (size_t)n0, xyz + 3 * (size_t)n1, E[e], nu[e], sec + kSecStride * (size_t)e, K)) {
         double la[14], lb[14];
         beam_to_local(B, fa, n0, n1, la);
         beam_to_local(B, fb, n0, n1, lb);
@@ -342,7 +350,7 @@ k_beam_export(int e0, int n, const int32_t* __restrict__ conn2, const double* __
     if (t >= n) return;
     const int e = e0 + t;
     BeamLocal B;
-    const double* se = sec + 10 * (size_t)e;
+    const double* se = sec + kSecStride * (size_t)e;
     double* ko = ke + (size_t)t * 144;
     double* mo = me ? me + (size_t)t * 144 : nullptr;
     if (!beam_local(B, xyz + 3 * (size_t)conn2[2 * (size_t)e], xyz + 3 * (size_t)conn2[2 * (size_t)e + 1], E[e], nu[e],
@@ -361,7 +369,7 @@ k_beam_export(int e0, int n, const int32_t* __restrict__ conn2, const double* __
 }
 
 void require_sections(const Ctx& c) {
-    if (c.d_beam_sec.n != (size_t)c.n_el * 10)
+    if (c.d_beam_sec.n != (size_t)c.n_el * kSecStride)
         throw InputError("beam2 meshes need asend_set_beam_sections before assembly");
 }
 
@@ -397,6 +405,18 @@ void beam_pairs(Ctx& c, const double* d_a, const double* d_b, double* d_P, bool 
                                                                  accumulate ? 1 : 0);
     ASEND_CUDA(cudaGetLastError());
     ++c.launches;
+}
+
+std::vector<double> beam_device_table(const Ctx& c) {
+    std::vector<double> t((size_t)c.n_el * kSecStride, 0.0);
+    for (int e = 0; e < c.n_el; ++e) {
+        std::copy(c.beam_sec.begin() + (size_t)e * 10, c.beam_sec.begin() + (size_t)e * 10 + 10,
+                  t.begin() + (size_t)e * kSecStride);
+        if (!c.beam_cm.empty())
+            std::copy(c.beam_cm.begin() + (size_t)e * 72, c.beam_cm.begin() + (size_t)e * 72 + 72,
+                      t.begin() + (size_t)e * kSecStride + kSecC);
+    }
+    return t;
 }
 
 void beam_section_dC(int category, int component, const double* sec, double* dC) {

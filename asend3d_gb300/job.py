@@ -207,7 +207,12 @@ def read_model(path) -> ModelInput:
                     m.sections[-1]["I"] = [float(v) for v in data]
                 elif h2 == "J" and len(data) == 1:
                     m.sections[-1]["J"] = float(data[0])
-                elif h2 in ("stiffness", "mass", "damping", "expLoadCoef"):
+                elif h2 in ("stiffness", "mass") and len(data) == 3:
+                    # (row, column, value), 1-based, symmetric (section_meth.rs:61-71)
+                    mat = m.sections[-1].setdefault(h2, [0.0] * 36)
+                    r, c = int(data[0]) - 1, int(data[1]) - 1
+                    mat[6 * r + c] = mat[6 * c + r] = float(data[2])
+                elif h2 in ("damping", "expLoadCoef"):
                     raise NotImplementedError(f"beam section {h2} entries are not on the GPU path")
             elif h1 in ("potField", "dampField", "thermField") and data:
                 raise NotImplementedError(f"section {h1} is not on the GPU path")
@@ -392,6 +397,7 @@ class JobRunner:
         ortho = False
         shell_secs = []
         beam = np.full((ne, 10), np.nan)  # area, I1..I5, J, xy-plane direction
+        beam_cm = np.zeros((ne, 72))      # given section stiffness, mass (section_meth.rs:61-71)
         for sec in m.sections:
             es = sec.get("elementSet")
             if es is None or es not in m.elem_sets:
@@ -428,7 +434,13 @@ class JobRunner:
                 if "damping" in mat:
                     raise NotImplementedError("material damping takes solid sections")
                 for e in els:
-                    beam[e] = self._beam_row(sec, coords[conn[e, 1]] - coords[conn[e, 0]])
+                    beam[e], flip = self._beam_row(sec, coords[conn[e, 1]] - coords[conn[e, 0]])
+                    cm = np.asarray(sec.get("stiffness", [0.0] * 36), float).reshape(6, 6)
+                    mm = np.asarray(sec.get("mass", [0.0] * 36), float).reshape(6, 6)
+                    if flip:  # the half turn about y: strains (1,-1,1,1,-1,1), velocities (-1,1,-1,-1,1,-1)
+                        ts, tm = np.array([1, -1, 1, 1, -1, 1.0]), np.array([-1, 1, -1, -1, 1, -1.0])
+                        cm, mm = cm * np.outer(ts, ts), mm * np.outer(tm, tm)
+                    beam_cm[e, :36], beam_cm[e, 36:] = cm.ravel(), mm.ravel()
                 t = np.nan
             else:
                 raise NotImplementedError(f"{sec['type']} sections are not on the GPU path")
@@ -456,6 +468,8 @@ class JobRunner:
             if np.isnan(beam).any():
                 raise ValueError("beam2 elements need a beam section")
             p.beam_sections = beam
+            if np.any(beam_cm[:, 0] > 0.0) or np.any(beam_cm[:, 36] > 0.0):
+                p.beam_section_matrices = (beam_cm[:, :36].copy(), beam_cm[:, 36:].copy())
         if ortho:
             if m.elem_type not in (8, 4, 10):
                 raise NotImplementedError("orthotropic materials take hex8 / tet4 / tet10 meshes on the GPU path")
@@ -696,7 +710,9 @@ class JobRunner:
         is only consistent there when xDir lies along the element; the GPU
         element takes x from the element itself.  An xDir opposite to the
         element gives the same frame turned half a turn about y: the odd
-        moments I1 = int z and I5 = int yz change sign."""
+        moments I1 = int z and I5 = int yz change sign, and so do the given
+        matrices' entries that couple an odd number of the flipped strains
+        or velocities.  Returns (row, flipped)."""
         ori = sec.get("orientation", [1.0, 0.0, 0.0, 0.0, 1.0, 0.0])
         x = np.asarray(ori[:3], float)
         x = x / np.linalg.norm(x)
@@ -707,7 +723,7 @@ class JobRunner:
         im = list(sec.get("I", [0.0] * 5))
         if c < 0.0:
             im[0], im[4] = -im[0], -im[4]
-        return [sec.get("area", 0.0), *im, sec.get("J", 0.0), *ori[3:6]]
+        return [sec.get("area", 0.0), *im, sec.get("J", 0.0), *ori[3:6]], c < 0.0
 
     @staticmethod
     def _shell_frame_angle(sec):

@@ -62,6 +62,9 @@ class Problem:
     # (int z, int y, int z^2, int y^2, int yz dA in the section axes), polar
     # moment J, and the vector v fixing the section's xy plane
     beam_sections: np.ndarray | None = None
+    # given beam section matrices (stiffness [n_el][36] or None, mass [n_el][36]
+    # or None); an element whose [0] entry is <= 0 keeps the computed one
+    beam_section_matrices: tuple | None = None
 
     def add_node_set(self, name, nodes):
         self.node_sets[name] = np.asarray(nodes, dtype=np.int32)
@@ -172,6 +175,14 @@ class GpuSolver:
                                                               (m.n_elems, 10)))
             self._check(self.lib.asend_set_beam_sections(self.ctx, _ptr(self._bsec, C.c_double)),
                         "set_beam_sections")
+            if p.beam_section_matrices is not None:
+                cs, ms = (None if x is None else np.ascontiguousarray(np.broadcast_to(np.asarray(x, np.float64),
+                                                                                      (m.n_elems, 36)))
+                          for x in p.beam_section_matrices)
+                self._bcm = (cs, ms)
+                self._check(self.lib.asend_set_beam_section_matrices(
+                    self.ctx, None if cs is None else _ptr(cs, C.c_double),
+                    None if ms is None else _ptr(ms, C.c_double)), "set_beam_section_matrices")
         if m.elem_type in (8, 81) and m.conn.shape[0] == m.nx * m.ny * m.nz:
             self._check(self.lib.asend_set_block_structure(self.ctx, m.nx, m.ny, m.nz), "set_block_structure")
         for name, nodes in p.node_sets.items():

@@ -401,6 +401,16 @@ int asend_set_shell_sections(asend_ctx* ctx, const double* abd, const double* ms
  * proportional to E_e, so asend_adjoint_gradient gives per-element modulus
  * gradients; body loads need I1 = I2 = 0; damping takes rayleigh_cm only. */
 int asend_set_beam_sections(asend_ctx* ctx, const double* sections);
+/* Given beam section matrices (the reference's beamProps stiffness / mass
+ * entries, section_meth.rs:61-71, used in place of the area and moments when
+ * their [0] entry is positive, element_properties.rs:896-920, :1430-1440):
+ * stiffness[n_el][36] and mass[n_el][36] in the section axes and the section
+ * deformation order, symmetric (the upper triangle is read); an element whose
+ * [0] entry is <= 0 keeps the computed matrix; either pointer may be NULL,
+ * both NULL clears them.  After asend_set_beam_sections.  A given stiffness is
+ * not proportional to E: asend_adjoint_gradient then takes dLdE_out = NULL and
+ * material DVs give zero on those elements; a given mass takes no body loads. */
+int asend_set_beam_section_matrices(asend_ctx* ctx, const double* stiffness, const double* mass);
 /* Row-sum lumped mass in Newmark assemblies (the reference's 'lumpMass: yes',
  * element_equations.rs:950-971): the mass is diag(row sums of M). */
 int asend_set_lumped_mass(asend_ctx* ctx, int32_t on);

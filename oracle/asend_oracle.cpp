@@ -777,18 +777,30 @@ void beam_kfull(const double* R, double a, const double* C, double* K) {
     }
 }
 
-bool beam_km(const double* xyz, double E, double nu, double rho, const double* sec, double* ke, double* me) {
+// Given section matrices ov[72] (stiffness then mass, each used when its [0]
+// entry is positive, element_properties.rs:896-920, :1430-1440; symmetric by
+// construction, section_meth.rs:61-71) replace the computed ones.
+void beam_given(const double* ov, double* C, double* M) {
+    if (!ov) return;
+    if (C && ov[0] > 0.0) std::copy(ov, ov + 36, C);
+    if (M && ov[36] > 0.0) std::copy(ov + 36, ov + 72, M);
+}
+
+bool beam_km(const double* xyz, double E, double nu, double rho, const double* sec, double* ke, double* me,
+             const double* ov = nullptr) {
     double R[9], L;
     if (!beam_frame(xyz, sec + 7, R, &L)) return false;
     constexpr int tot = 14, nd = 12;
     double C[36], K[tot * tot];
     beam_cmat(E, nu, sec, C);
+    beam_given(ov, C, nullptr);
     const double a = 0.5 * L;  // detJ
     beam_kfull(R, a, C, K);
     if (me) {
         for (int i = 0; i < nd * nd; ++i) me[i] = 0.0;
         double Ms[36], RM[36];
         beam_msec(rho, sec, Ms);
+        beam_given(ov, nullptr, Ms);
         // Rb^T Ms Rb with Rb = diag(R, R)
         auto rb = [&](int p, int q) { return (p / 3 == q / 3) ? R[3 * (p % 3) + q % 3] : 0.0; };
         for (int c = 0; c < 6; ++c)
@@ -824,12 +836,13 @@ bool beam_km(const double* xyz, double E, double nu, double rho, const double* s
 // that lambda^T (dK_e/dD) u = sum_ij (dC/dD)_ij P_ij for any section-stiffness
 // parameter D (d_relasticd_d, model_analysis.rs:1379-1457).
 bool beam_pairs(const double* xyz, double E, double nu, const double* sec, const double* ue, const double* le,
-                double* P) {
+                double* P, const double* ov = nullptr) {
     double R[9], L;
     if (!beam_frame(xyz, sec + 7, R, &L)) return false;
     constexpr int tot = 14;
     double C[36], K[tot * tot];
     beam_cmat(E, nu, sec, C);
+    beam_given(ov, C, nullptr);
     const double a = 0.5 * L;
     beam_kfull(R, a, C, K);
     double Kii[4] = {K[12 * tot + 12], K[12 * tot + 13], K[13 * tot + 12], K[13 * tot + 13]};
@@ -932,6 +945,8 @@ struct orc_model {
     bool beam = false;
     std::vector<int32_t> conn2;
     std::vector<double> beam_sec;
+    std::vector<double> beam_cm;  // given section matrices [n_el][72] (may be empty)
+    const double* beam_ov(int e) const { return beam_cm.empty() ? nullptr : &beam_cm[(size_t)e * 72]; }
     bool structural() const { return shell || beam; }
 };
 
@@ -952,7 +967,7 @@ void elem_km(const orc_model* m, int e, double* ke, double* me) {
         double xyz[6];
         for (int a = 0; a < 2; ++a)
             for (int j = 0; j < 3; ++j) xyz[3 * a + j] = m->phys_xyz[3 * (size_t)m->conn2[(size_t)e * 2 + a] + j];
-        beam_km(xyz, m->E[e], m->nu[e], m->rho[e], &m->beam_sec[(size_t)e * 10], ke, me);
+        beam_km(xyz, m->E[e], m->nu[e], m->rho[e], &m->beam_sec[(size_t)e * 10], ke, me, m->beam_ov(e));
         return;
     }
     if (m->shell) {
@@ -1721,6 +1736,28 @@ int orc_beam_element(const double* xyz, double E, double nu, double rho, const d
     return beam_km(xyz, E, nu, rho, sec, ke, me) ? 0 : -2;
 }
 
+int orc_beam_element_given(const double* xyz, double E, double nu, double rho, const double* sec,
+                           const double* given, double* ke, double* me) {
+    if (!xyz || !sec || !ke) return -1;
+    return beam_km(xyz, E, nu, rho, sec, ke, me, given) ? 0 : -2;
+}
+
+int orc_set_beam_section_matrices(orc_model* m, const double* stiffness, const double* mass) {
+    if (!m->beam) return -1;
+    if (!stiffness && !mass) {
+        m->beam_cm.clear();
+    } else {
+        m->beam_cm.assign((size_t)m->n_el * 72, 0.0);
+        for (int e = 0; e < m->n_el; ++e)
+            for (int k = 0; k < 36; ++k) {
+                if (stiffness) m->beam_cm[(size_t)e * 72 + k] = stiffness[(size_t)e * 36 + k];
+                if (mass) m->beam_cm[(size_t)e * 72 + 36 + k] = mass[(size_t)e * 36 + k];
+            }
+    }
+    m->assembled = false;
+    return 0;
+}
+
 // dC/dD of the beam section stiffness (get_beam_stiff_dfd0,
 // element_properties.rs:921-1010) for a unit change of one material DV:
 // category 0 modulus (component 1: E1 in EA, E I1, -E I2, E I3, -E I5, E I4;
@@ -1954,7 +1991,7 @@ int orc_body_load(const orc_model* m, int32_t n_set, const int32_t* elem_set, in
             for (int a = 0; a < 2; ++a)
                 for (int j = 0; j < 3; ++j) x2[3 * a + j] = m->phys_xyz[3 * (size_t)m->conn2[(size_t)e * 2 + a] + j];
             beam_km(x2, m->E[e], m->nu[e], kind == 0 ? 1.0 : m->rho[e], &m->beam_sec[(size_t)e * 10], ke.data(),
-                    me.data());
+                    me.data(), m->beam_ov(e));
         } else if (m->shell) {
             double x4[12];
             for (int a = 0; a < 4; ++a)
@@ -2088,6 +2125,8 @@ int orc_adjoint_modulus_gradient(orc_model* m, const double* u, const double* dL
                                  orc_stats* st) {
     if (!m->assembled) return -1;
     if (!m->shell_abd81.empty()) return -2;  // layered sections are not proportional to E
+    for (size_t e = 0; e < m->beam_cm.size() / 72; ++e)
+        if (m->beam_cm[e * 72] > 0.0) return -2;  // nor are given beam section stiffnesses
     const int n = m->n_dof;
     std::vector<double> lam(n, 0.0);
     int status = 0;
@@ -2410,7 +2449,8 @@ int orc_adjoint_strain_pairs(const orc_model* m, const double* u, const double* 
                     le[6 * a + c] = lam[6 * (size_t)nd + c];
                 }
             }
-            beam_pairs(xyz, m->E[e], m->nu[e], &m->beam_sec[(size_t)e * 10], ue, le, P + (size_t)e * 36);
+            beam_pairs(xyz, m->E[e], m->nu[e], &m->beam_sec[(size_t)e * 10], ue, le, P + (size_t)e * 36,
+                       m->beam_ov(e));
         }
         return 0;
     }

@@ -166,6 +166,13 @@ int orc_set_beam_sections(orc_model* m, const double* sec);
  * the axis. */
 int orc_beam_element(const double* xyz, double E, double nu, double rho, const double* sec, double* ke,
                      double* me);
+/* As orc_beam_element with given section matrices given[72] (stiffness then
+ * mass, each used when its [0] entry is positive; may be NULL). */
+int orc_beam_element_given(const double* xyz, double E, double nu, double rho, const double* sec,
+                           const double* given, double* ke, double* me);
+/* Given beam section matrices of a beam2 model, stiffness[n_el][36] and
+ * mass[n_el][36] (either may be NULL; both NULL clears them). */
+int orc_set_beam_section_matrices(orc_model* m, const double* stiffness, const double* mass);
 /* dC[36] of the beam section stiffness per unit change of a material DV
  * (category 0 modulus, 1 shearModulus, 2 poissonRatio; component 1-3). */
 int orc_beam_section_dC(int32_t category, int32_t component, const double* sec, double* dC);

@@ -80,6 +80,8 @@ def load():
             "orc_set_beam_sections": (C.c_int, [C.c_void_p, P_d]),
             "orc_beam_element": (C.c_int, [P_d, C.c_double, C.c_double, C.c_double, P_d, P_d, P_d]),
             "orc_beam_section_dC": (C.c_int, [C.c_int32, C.c_int32, P_d, P_d]),
+            "orc_beam_element_given": (C.c_int, [P_d, C.c_double, C.c_double, C.c_double, P_d, P_d, P_d, P_d]),
+            "orc_set_beam_section_matrices": (C.c_int, [C.c_void_p, P_d, P_d]),
             "orc_element_objective": (C.c_int, [C.c_void_p, P_d, C.c_int32, P_i, C.c_int32, C.c_int32, C.c_int32,
                                                 C.c_double, C.c_double, C.c_int32, P_d, P_d, P_d, P_d, P_d]),
         }
@@ -154,6 +156,13 @@ class Oracle:
         if bsec is not None:
             self._bsec = np.ascontiguousarray(np.broadcast_to(np.asarray(bsec, np.float64), (m.n_elems, 10)))
             assert self.lib.orc_set_beam_sections(self.m, _p(self._bsec)) == 0
+            given = getattr(problem, "beam_section_matrices", None)
+            if given is not None:
+                self._bcm = [None if x is None else np.ascontiguousarray(
+                    np.broadcast_to(np.asarray(x, np.float64), (m.n_elems, 36))) for x in given]
+                assert self.lib.orc_set_beam_section_matrices(
+                    self.m, None if self._bcm[0] is None else _p(self._bcm[0]),
+                    None if self._bcm[1] is None else _p(self._bcm[1])) == 0
         secs = getattr(problem, "shell_sections", None)
         if secs:
             # layered sections: (element indices, layer table [n, 7], z offset);
@@ -379,13 +388,19 @@ def element_stiffness(elem_type, xyz, E, nu):
     return ke.reshape(n, n)
 
 
-def beam_element(xyz, E, nu, rho, sec):
-    """beam2 element stiffness and mass [12][12] (global DOF 6 a + c)."""
+def beam_element(xyz, E, nu, rho, sec, given=None):
+    """beam2 element stiffness and mass [12][12] (global DOF 6 a + c);
+    ``given`` [72]: section stiffness then mass matrices (each used when its
+    [0] entry is positive)."""
     lib = load()
     xyz = np.ascontiguousarray(xyz, np.float64).ravel()
     sec = np.ascontiguousarray(sec, np.float64)
     ke, me = np.zeros(144), np.zeros(144)
-    rc = lib.orc_beam_element(_p(xyz), float(E), float(nu), float(rho), _p(sec), _p(ke), _p(me))
+    if given is None:
+        rc = lib.orc_beam_element(_p(xyz), float(E), float(nu), float(rho), _p(sec), _p(ke), _p(me))
+    else:
+        gv = np.ascontiguousarray(given, np.float64)
+        rc = lib.orc_beam_element_given(_p(xyz), float(E), float(nu), float(rho), _p(sec), _p(gv), _p(ke), _p(me))
     if rc != 0:
         raise ValueError(f"orc_beam_element failed ({rc})")
     return ke.reshape(12, 12), me.reshape(12, 12)

@@ -224,3 +224,68 @@ def test_beam_material_dvs(gpu_lib, oracle_lib):
         g.material_dv_gradient("shearModulus", k, "all") for k in (1, 2, 3))
     assert tot == pytest.approx(gE.sum(), rel=1e-9)
     g.close()
+
+
+def test_beam_newmark_lumped_damped(gpu_lib, oracle_lib):
+    """Newmark on a beam line with row-sum lumped mass and mass-proportional
+    Rayleigh damping (the forms beam2 takes) against the oracle (1e-6)."""
+    p = cantilever(20, rho=1.0)
+    p.lump_mass = True
+    p.damping = (0.3, 0.0, None)
+    dt, beta, gamma, n = 0.05, 0.25, 0.5, 40
+    amp = np.sin(np.linspace(0.0, np.pi, n))
+    probe = 6 * 20 + 2
+    g = GpuSolver(p)
+    g.assemble(dynamic=True, dt=dt, beta=beta, gamma=gamma)
+    hist, u, rc, st = g.newmark(amp, probe_dof=probe, method=_lib.METHOD_FP64, rel_tol=1e-8, max_iter=400000)
+    assert rc == _lib.ASEND_OK
+    o = oracle_lib.Oracle(p, dynamic=True, dt=dt, beta=beta, gamma=gamma)
+    href, uref, rc2, _ = o.newmark(n, dt, beta, gamma, o.loads()[0], amp, probe, precond=oracle_lib.PC_DIRECT)
+    assert rc2 == 0
+    assert rel(hist, href) < 1e-6
+    assert rel(u, uref) < 1e-6
+    g.close()
+
+
+def test_beam_given_section_matrices(gpu_lib, oracle_lib):
+    """beamProps stiffness / mass given as matrices on half of a bent line's
+    elements (the other half computed): element matrices (1e-11), the static
+    solve against the oracle (1e-6), the modulus adjoint refused, material DVs
+    zero on the given-stiffness elements."""
+    from test_oracle_beam import _section_matrices
+    p = random_frame_problem(seed=9)
+    ne = p.mesh.n_elems
+    rng = np.random.default_rng(4)
+    Cg, Mg = np.zeros((ne, 36)), np.zeros((ne, 36))
+    for e in range(0, ne, 2):
+        C, M = _section_matrices(p.E[e], p.nu[e], p.rho[e], p.beam_sections[e])
+        S = np.diag(rng.uniform(0.8, 1.25, 6))  # a different, still positive-definite section
+        Cg[e], Mg[e] = (S @ C @ S).ravel(), (S @ M @ S).ravel()
+    p.beam_section_matrices = (Cg, Mg)
+    p.add_node_set("root", np.array([0], np.int32))
+    p.add_node_set("tip", np.array([ne], np.int32))
+    p.add_elem_set("all", np.arange(ne, dtype=np.int32))
+    p.fix_displacement("root", comps=(1, 2, 3, 4, 5, 6))
+    p.add_nodal_force("tip", [1e3, -2e3, 5e2, 40.0, -10.0, 25.0])
+    g = GpuSolver(p)
+    ke, me = g.element_matrices()
+    m = p.mesh
+    for e in range(ne):
+        given = np.concatenate([Cg[e], Mg[e]])
+        ko, mo = oracle_lib.beam_element(m.coords[m.conn[e]], p.E[e], p.nu[e], p.rho[e], p.beam_sections[e], given)
+        assert np.abs(ke[e] - ko).max() <= 1e-11 * np.abs(ko).max(), e
+        assert np.abs(me[e] - mo).max() <= 1e-11 * np.abs(mo).max(), e
+    g.assemble(precision=64)
+    u, rc, st = g.static_solve(**FP64)
+    assert rc == _lib.ASEND_OK, st
+    o = oracle_lib.Oracle(p)
+    uo, _, _ = o.solve(o.loads()[0] + o.penalty_rhs(), precond=oracle_lib.PC_DIRECT)
+    assert rel(u[0], uo) < 1e-6
+    with pytest.raises(AsendError, match="isotropic"):
+        g.adjoint_gradient(**FP64)
+    g.adjoint_gradient(want_dLdE=False, **FP64)
+    P = g.strain_pairs()
+    mod = g.material_dv_gradient("modulus", 1, "all")
+    ref = -sum(np.sum(oracle_lib.beam_section_dC(0, 1, p.beam_sections[e]) * P[e]) for e in range(1, ne, 2))
+    assert mod == pytest.approx(ref, rel=1e-12)
+    g.close()

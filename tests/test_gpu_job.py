@@ -316,3 +316,37 @@ def test_beam_job_runners(gpu_lib, tmp_path):
     assert r1[0, 3] == pytest.approx(8.0, rel=1e-3)
     w = float((d1 / "obj.csv").read_text().splitlines()[1].split(",")[1])
     assert w == pytest.approx(r1[0, 3], rel=1e-12)
+
+
+def test_beam_job_given_matrices(gpu_lib, tmp_path):
+    """A beam job whose section stiffness is given as beamProps entries (with
+    an axial-bending coupling): the Python runner and the CLI agree (1e-12),
+    and the same job with every element numbered against the orientation's x
+    direction (the given matrix turned into its frame) gives the same tip
+    (1e-8); with the given diagonal equal to the computed one the tip is the
+    pin's 8 (1e-3)."""
+    import subprocess
+
+    from asend3d_gb300 import build
+    build.build()
+    build.build_cli()
+    given = [("stiffness", 1, 1, 1e5), ("stiffness", 2, 2, 5e4), ("stiffness", 3, 3, 5e4),
+             ("stiffness", 4, 4, 140.0), ("stiffness", 5, 5, 1e6 * 0.1**3 / 12), ("stiffness", 6, 6, 1e6 * 0.1 / 12)]
+    coupled = given + [("stiffness", 1, 5, 3.0)]
+    dirs = {k: tmp_path / k for k in ("plain", "py", "cli", "rev")}
+    for d in dirs.values():
+        d.mkdir()
+    write_beam_job(dirs["plain"], given=given)
+    write_beam_job(dirs["py"], given=coupled)
+    write_beam_job(dirs["cli"], given=coupled)
+    write_beam_job(dirs["rev"], reverse=True, given=coupled)
+    for k in ("plain", "py", "rev"):
+        J.JobRunner(dirs[k] / "job.yaml").run()
+    out = subprocess.run([str(build.CLI), str(dirs["cli"] / "job.yaml")], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    rows = {k: read_csv(dirs[k] / "nodes.csv")[1] for k in dirs}
+    assert rows["plain"][0, 3] == pytest.approx(8.0, rel=1e-3)
+    np.testing.assert_allclose(rows["py"], rows["cli"], rtol=1e-12, atol=1e-12 * np.abs(rows["py"]).max())
+    np.testing.assert_allclose(rows["rev"][:, 1:4], rows["py"][:, 1:4], rtol=1e-8,
+                               atol=1e-8 * np.abs(rows["py"]).max())
+    assert abs(rows["py"][0, 1]) > 1e-9  # the coupling moves the tip axially

@@ -264,7 +264,7 @@ def test_shell_job_problem(tmp_path):
         np.testing.assert_allclose(pb.thickness, 0.004 * kw.get("layers", 1))
 
 
-def write_beam_job(d: Path, n=20, reverse=False, x_dir=(1.0, 0.0, 0.0), moments=(0.0, 0.0)):
+def write_beam_job(d: Path, n=20, reverse=False, x_dir=(1.0, 0.0, 0.0), moments=(0.0, 0.0), given=()):
     """The hexBeam / shellBeam cantilever as a line of beam2 elements (L = 10,
     b = 1, h = 0.1, E = 1e6, nu = 0), clamped at x = 0, Fz = 2 at the tip;
     ``reverse`` numbers every element from its outer node to its inner one."""
@@ -281,7 +281,7 @@ def write_beam_job(d: Path, n=20, reverse=False, x_dir=(1.0, 0.0, 0.0), moments=
               "  orientation: [" + ", ".join(repr(float(v)) for v in (*x_dir, 0.0, 1.0, 0.0)) + "]",
               "  beamProps:", "    area: 0.1",
               f"    I: [{moments[0]!r}, 0.0, {1.0 * 0.1**3 / 12!r}, {0.1 * 1.0**3 / 12!r}, {moments[1]!r}]",
-              "    J: 0.00028",
+              "    J: 0.00028"] + [f"    {kind}: [{r}, {c}, {v!r}]" for kind, r, c, v in given] + [
               "materials:", "  mat1:", "    density: 1.0", "    elastic:", "      E: [1000000.0]", "      nu: 0.0"]
     (d / "model.yaml").write_text("\n".join(lines) + "\n")
     cons = ["constraints:"]
@@ -334,3 +334,29 @@ def test_beam_job_problem(tmp_path):
     rs.cmd_readModelInput(rs.cmds[0])
     with pytest.raises(NotImplementedError, match="along the element"):
         rs._problem()
+
+
+def test_beam_job_given_matrices(tmp_path):
+    """beamProps stiffness / mass entries (1-based, symmetric) become given
+    section matrices; an element against the orientation's x direction gets
+    them in its own frame (the half turn about y flips the couplings of an odd
+    number of flipped components)."""
+    given = [("stiffness", 1, 1, 1e5), ("stiffness", 1, 5, 3.0), ("stiffness", 5, 5, 90.0),
+             ("mass", 1, 1, 0.1), ("mass", 2, 4, 0.002)]
+    write_beam_job(tmp_path, n=4, given=given)
+    r = J.JobRunner(tmp_path / "job.yaml")
+    r.cmd_readModelInput(r.cmds[0])
+    st = np.array(r.model.sections[0]["stiffness"]).reshape(6, 6)
+    assert st[0, 0] == 1e5 and st[0, 4] == st[4, 0] == 3.0 and st[4, 4] == 90.0
+    p = r._problem()
+    C, M = p.beam_section_matrices
+    np.testing.assert_array_equal(C[0].reshape(6, 6), st)
+    assert M[0].reshape(6, 6)[1, 3] == M[0].reshape(6, 6)[3, 1] == 0.002
+    d = tmp_path / "rev"
+    d.mkdir()
+    write_beam_job(d, n=4, reverse=True, given=given)
+    rb = J.JobRunner(d / "job.yaml")
+    rb.cmd_readModelInput(rb.cmds[0])
+    Cr, Mr = rb._problem().beam_section_matrices
+    assert Cr[0].reshape(6, 6)[0, 4] == -3.0 and Cr[0].reshape(6, 6)[4, 4] == 90.0
+    assert Mr[0].reshape(6, 6)[1, 3] == -0.002 and Mr[0].reshape(6, 6)[0, 0] == 0.1

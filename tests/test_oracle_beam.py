@@ -223,3 +223,46 @@ def test_material_dv_pairs(oracle_lib):
     # G with E held: nu' = E / (2 G') - 1
     wG = [_tip_w(oracle_lib, E0, E0 / (2 * G0 * (1 + s * h)) - 1.0) for s in (1, -1)]
     assert g_G == pytest.approx((wG[0] - wG[1]) / (2 * h * G0), rel=1e-5)
+
+
+def _section_matrices(E, nu, rho, sec):
+    """The computed section stiffness and mass (element_properties.rs:921-1010,
+    :1440-1497) written out, for the given-matrix checks."""
+    G = E / (2 * (1 + nu))
+    A_, i1, i2, i3, i4, i5, J_ = sec[:7]
+    C = np.zeros((6, 6))
+    C[0, 0], C[0, 4], C[0, 5] = E * A_, E * i1, -E * i2
+    C[1, 1], C[1, 3], C[2, 2], C[2, 3], C[3, 3] = G * A_, -G * i1, G * A_, G * i2, G * J_
+    C[4, 4], C[4, 5], C[5, 5] = E * i3, -E * i5, E * i4
+    M = np.zeros((6, 6))
+    M[0, 0] = M[1, 1] = M[2, 2] = rho * A_
+    M[0, 4], M[1, 3], M[0, 5], M[2, 3] = rho * i1, -rho * i1, -rho * i2, rho * i2
+    M[3, 3], M[4, 4], M[4, 5], M[5, 5] = rho * J_, rho * i3, rho * i5, rho * i4
+    return np.triu(C) + np.triu(C, 1).T, np.triu(M) + np.triu(M, 1).T
+
+
+def test_given_section_matrices(oracle_lib):
+    """beamProps stiffness / mass given as matrices: the computed ones given
+    back reproduce the element (1e-14), a stiffer given bending entry acts as
+    a larger moment of inertia (1e-9), and the modulus adjoint refuses them."""
+    sec = np.array([0.3, 0.01, -0.02, 2e-3, 3e-3, 4e-4, 5e-3, 0.3, -1.0, 0.5])
+    xyz = np.array([[0.1, 0.2, -0.3], [1.1, -0.4, 0.5]])
+    C, M = _section_matrices(2e11, 0.3, 7800.0, sec)
+    k0, m0 = oracle_lib.beam_element(xyz, 2e11, 0.3, 7800.0, sec)
+    k1, m1 = oracle_lib.beam_element(xyz, 2e11, 0.3, 7800.0, sec, given=np.concatenate([C.ravel(), M.ravel()]))
+    assert np.abs(k1 - k0).max() <= 1e-14 * np.abs(k0).max()
+    assert np.abs(m1 - m0).max() <= 1e-14 * np.abs(m0).max()
+    # given stiffness with E I3 doubled == a section with I3 doubled
+    n = 20
+    p = cantilever(n)
+    Cg, _ = _section_matrices(E0, 0.0, 0.0, section())
+    Cg[4, 4] *= 2.0
+    p.beam_section_matrices = (Cg.ravel(), None)
+    q = cantilever(n)
+    q.beam_sections = q.beam_sections.copy()
+    q.beam_sections[:, 3] *= 2.0
+    t1, u1, o1 = tip_solution(oracle_lib, p)
+    t2, _, _ = tip_solution(oracle_lib, q)
+    assert t1[2] == pytest.approx(t2[2], rel=1e-9)
+    _, _, rc, _ = o1.adjoint(u1, dLdu=np.ones(o1.n_dof), precond=oracle_lib.PC_DIRECT)
+    assert rc == -2
