@@ -29,6 +29,7 @@ OBJ_DISPLACEMENT, OBJ_COMPLIANCE, OBJ_ELEMENT = 0, 1, 2
 LOAD_BODY_FORCE, LOAD_GRAVITY, LOAD_CENTRIFUGAL = 0, 1, 2
 LEARN_BLOCK, LEARN_MG = 0, 1
 DV_MODULUS, DV_SHEAR_MODULUS, DV_POISSON_RATIO = 0, 1, 2
+DV_AREA, DV_AREA_MOMENT, DV_POLAR_MOMENT = 3, 4, 5  # beam2 sections
 
 
 class SolveOpts(C.Structure):

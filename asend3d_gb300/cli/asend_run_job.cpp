@@ -420,7 +420,8 @@ std::vector<DesignVar> read_design_vars(const std::string& path) {
         const auto& d = r.data;
         const std::string& k = r.h[1];
         if (k == "category" && d.size() == 1) {
-            if (d[0] != "modulus" && d[0] != "shearModulus" && d[0] != "poissonRatio")
+            if (d[0] != "modulus" && d[0] != "shearModulus" && d[0] != "poissonRatio" && d[0] != "area" &&
+                d[0] != "areaMoment" && d[0] != "polarMoment")
                 throw Fail("design variable category " + d[0] + " is not on the GPU path");
             out.emplace_back();
             out.back().category = d[0];
@@ -823,8 +824,12 @@ struct Runner {
             for (size_t i = 0; i < dvs.size(); ++i) {
                 const DesignVar& dv = dvs[i];
                 if (!(dv.t0 <= time && time <= dv.t1)) continue;
-                const int cat = dv.category == "modulus" ? ASEND_DV_MODULUS
-                                : dv.category == "shearModulus" ? ASEND_DV_SHEAR_MODULUS : ASEND_DV_POISSON_RATIO;
+                const int cat = dv.category == "modulus"        ? ASEND_DV_MODULUS
+                                : dv.category == "shearModulus" ? ASEND_DV_SHEAR_MODULUS
+                                : dv.category == "area"         ? ASEND_DV_AREA
+                                : dv.category == "areaMoment"   ? ASEND_DV_AREA_MOMENT
+                                : dv.category == "polarMoment"  ? ASEND_DV_POLAR_MOMENT
+                                                                : ASEND_DV_POISSON_RATIO;
                 double g = 0.0;
                 check(asend_material_dv_gradient(ctx, cat, dv.component, elset_id.at(dv.elem_set), (int)dv.coefs.size(),
                                                  dv.coefs.empty() ? nullptr : dv.coefs.data(), &g),

@@ -1817,8 +1817,10 @@ int asend_adjoint_strain_pairs(asend_ctx* ctx, double* pairs_out) {
 int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t component, int32_t elem_set,
                                int32_t n_coef, const double* coefs, double* grad_out) {
     return guarded(ctx, [&](Ctx& c) {
-        require(category >= ASEND_DV_MODULUS && category <= ASEND_DV_POISSON_RATIO, "unknown DV category");
-        require(component >= 1 && component <= 3, "component must be 1, 2 or 3");
+        require(category >= ASEND_DV_MODULUS && category <= ASEND_DV_POLAR_MOMENT, "unknown DV category");
+        require(category <= ASEND_DV_POISSON_RATIO || c.type == 2, "area / areaMoment / polarMoment DVs take beam2 meshes");
+        if (category == ASEND_DV_AREA_MOMENT) require(component >= 1 && component <= 5, "areaMoment component must be 1-5");
+        else if (category <= ASEND_DV_POISSON_RATIO) require(component >= 1 && component <= 3, "component must be 1, 2 or 3");
         require(elem_set >= 0 && elem_set < (int)c.elem_sets.size(), "unknown element set");
         require(grad_out, "null output");
         const auto& set = c.elem_sets[elem_set];
@@ -1831,7 +1833,7 @@ int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t compone
             double dC[36];
             if (c.type == 2 && !c.beam_cm.empty() && c.beam_cm[(size_t)e * 72] > 0.0)
                 std::fill(dC, dC + 36, 0.0);  // a given section stiffness: no E or G in it
-            else if (c.type == 2) beam_section_dC(category, component, &c.beam_sec[(size_t)e * 10], dC);
+            else if (c.type == 2) beam_section_dC(category, component, &c.beam_sec[(size_t)e * 10], c.E[e], c.nu[e], dC);
             else if (!c.ortho.empty()) material_dC_props(category, component, &c.ortho[(size_t)e * 9], dC);
             else material_dC(category, component, c.E[e], c.nu[e], dC);
             const double* P = &c.h_pairs[(size_t)e * 36];

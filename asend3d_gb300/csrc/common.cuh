@@ -378,7 +378,7 @@ void beam_element_matrices(Ctx& c, int e0, int n, double* ke_host, double* me_ho
 void beam_pairs(Ctx& c, const double* d_a, const double* d_b, double* d_P, bool accumulate);
 std::vector<double> beam_device_table(const Ctx& c);
 // dC[36] of the beam section stiffness per unit change of a material DV
-void beam_section_dC(int category, int component, const double* sec, double* dC);
+void beam_section_dC(int category, int component, const double* sec, double E, double nu, double* dC);
 // brickIM elements (k_brickim.cu)
 void brickim_assemble(Ctx& c, double* vals, double* mvals);
 void brickim_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate);

@@ -419,9 +419,36 @@ std::vector<double> beam_device_table(const Ctx& c) {
     return t;
 }
 
-void beam_section_dC(int category, int component, const double* sec, double* dC) {
+void beam_section_dC(int category, int component, const double* sec, double E, double nu, double* dC) {
     for (int i = 0; i < 36; ++i) dC[i] = 0.0;
     auto set = [&](int i, int j, double v) { dC[6 * i + j] = dC[6 * j + i] = v; };
+    const double G = E / (2.0 * (1.0 + nu));
+    if (category == ASEND_DV_AREA) {  // EA, GA, GA
+        set(0, 0, E);
+        set(1, 1, G);
+        set(2, 2, G);
+        return;
+    }
+    if (category == ASEND_DV_AREA_MOMENT) {
+        if (component == 1) {  // E I1, -G I1
+            set(0, 4, E);
+            set(1, 3, -G);
+        } else if (component == 2) {  // -E I2, G I2
+            set(0, 5, -E);
+            set(2, 3, G);
+        } else if (component == 3) {
+            set(4, 4, E);
+        } else if (component == 4) {
+            set(5, 5, E);
+        } else if (component == 5) {
+            set(4, 5, -E);
+        }
+        return;
+    }
+    if (category == ASEND_DV_POLAR_MOMENT) {  // GJ
+        set(3, 3, G);
+        return;
+    }
     if (category == ASEND_DV_MODULUS && component == 1) {  // E1: EA, E I1, -E I2, E I3, -E I5, E I4
         set(0, 0, sec[0]);
         set(0, 4, sec[1]);

@@ -289,7 +289,7 @@ def read_loads(path) -> list:
     return out
 
 
-DV_CATEGORIES = ("modulus", "shearModulus", "poissonRatio")
+DV_CATEGORIES = ("modulus", "shearModulus", "poissonRatio", "area", "areaMoment", "polarMoment")
 ELEMENT_CATEGORIES = ("stress", "strain", "strainEnergy")
 
 
@@ -562,8 +562,10 @@ class JobRunner:
         for dv in read_design_vars(self._path(c["fileName"])):
             if dv["category"] not in DV_CATEGORIES:
                 raise NotImplementedError(f"design variable category {dv['category']} is not on the GPU path")
-            if not isinstance(dv["component"], int) or not 1 <= dv["component"] <= 3 or "elementSet" not in dv:
-                raise ValueError(f"design variable needs an element set and a component 1-3: {dv}")
+            top = {"area": 5, "polarMoment": 5, "areaMoment": 5}.get(dv["category"], 3)
+            low = 0 if dv["category"] in ("area", "polarMoment") else 1  # the reference ignores their component
+            if not isinstance(dv["component"], int) or not low <= dv["component"] <= top or "elementSet" not in dv:
+                raise ValueError(f"design variable needs an element set and a component {low}-{top}: {dv}")
             self.dvs.append(dv)
 
     def cmd_calcObjGradient(self, c):

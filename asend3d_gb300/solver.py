@@ -388,7 +388,8 @@ class GpuSolver:
         'poissonRatio' or the _lib.DV_* code) over an element set, from the
         last adjoint gradient."""
         cat = {"modulus": _lib.DV_MODULUS, "shearModulus": _lib.DV_SHEAR_MODULUS,
-               "poissonRatio": _lib.DV_POISSON_RATIO}.get(category, category)
+               "poissonRatio": _lib.DV_POISSON_RATIO, "area": _lib.DV_AREA, "areaMoment": _lib.DV_AREA_MOMENT,
+               "polarMoment": _lib.DV_POLAR_MOMENT}.get(category, category)
         cf = np.ascontiguousarray(np.atleast_1d(coefs), dtype=np.float64)
         out = C.c_double(0.0)
         self._check(self.lib.asend_material_dv_gradient(self.ctx, cat, component, self.elset_ids[elem_set], len(cf),

@@ -344,6 +344,13 @@ int asend_design_var_gradient(asend_ctx* ctx, const double* dLdE, double* dLdD_o
 #define ASEND_DV_MODULUS 0
 #define ASEND_DV_SHEAR_MODULUS 1
 #define ASEND_DV_POISSON_RATIO 2
+/* beam2 section DVs (get_beam_stiff_dfd0's area, areaMoment and polarMoment
+ * categories): area (component ignored), areaMoment component 1-5 (I1..I5),
+ * polarMoment (component ignored); dC/dD with the element's E and
+ * G = E / (2 (1 + nu)). */
+#define ASEND_DV_AREA 3
+#define ASEND_DV_AREA_MOMENT 4
+#define ASEND_DV_POLAR_MOMENT 5
 int asend_adjoint_strain_pairs(asend_ctx* ctx, double* pairs_out);
 int asend_material_dv_gradient(asend_ctx* ctx, int32_t category, int32_t component, int32_t elem_set,
                                int32_t n_coef, const double* coefs, double* grad_out);

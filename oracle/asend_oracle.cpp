@@ -1764,10 +1764,33 @@ int orc_set_beam_section_matrices(orc_model* m, const double* stiffness, const d
 // components 2, 3 do not enter), 1 shearModulus (component 1: G1 in GA of the
 // first shear, -G I1, G J; 2: G2 in GA of the second shear; 3: G3 in G I2),
 // 2 poissonRatio (does not enter).
-int orc_beam_section_dC(int32_t category, int32_t component, const double* sec, double* dC) {
-    if (category < 0 || category > 2 || component < 1 || component > 3 || !sec || !dC) return -1;
+// Categories 3 area (EA, GA, GA), 4 areaMoment component 1-5 (the entries of
+// I1..I5), 5 polarMoment (GJ), with the element's E and G = E / (2 (1 + nu)).
+int orc_beam_section_dC(int32_t category, int32_t component, double E, double nu, const double* sec, double* dC) {
+    if (category < 0 || category > 5 || !sec || !dC) return -1;
+    if (category <= 2 && (component < 1 || component > 3)) return -1;
+    if (category == 4 && (component < 1 || component > 5)) return -1;
     for (int i = 0; i < 36; ++i) dC[i] = 0.0;
     auto set = [&](int i, int j, double v) { dC[6 * i + j] = dC[6 * j + i] = v; };
+    const double G = E / (2.0 * (1.0 + nu));
+    if (category == 3) {
+        set(0, 0, E);
+        set(1, 1, G);
+        set(2, 2, G);
+        return 0;
+    }
+    if (category == 4) {
+        const int ij[5][2][2] = {{{0, 4}, {1, 3}}, {{0, 5}, {2, 3}}, {{4, 4}, {-1, -1}}, {{5, 5}, {-1, -1}},
+                                 {{4, 5}, {-1, -1}}};
+        const double v[5][2] = {{E, -G}, {-E, G}, {E, 0.0}, {E, 0.0}, {-E, 0.0}};
+        for (int t = 0; t < 2; ++t)
+            if (ij[component - 1][t][0] >= 0) set(ij[component - 1][t][0], ij[component - 1][t][1], v[component - 1][t]);
+        return 0;
+    }
+    if (category == 5) {
+        set(3, 3, G);
+        return 0;
+    }
     if (category == 0 && component == 1) {
         set(0, 0, sec[0]);
         set(0, 4, sec[1]);

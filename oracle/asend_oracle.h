@@ -173,9 +173,10 @@ int orc_beam_element_given(const double* xyz, double E, double nu, double rho, c
 /* Given beam section matrices of a beam2 model, stiffness[n_el][36] and
  * mass[n_el][36] (either may be NULL; both NULL clears them). */
 int orc_set_beam_section_matrices(orc_model* m, const double* stiffness, const double* mass);
-/* dC[36] of the beam section stiffness per unit change of a material DV
- * (category 0 modulus, 1 shearModulus, 2 poissonRatio; component 1-3). */
-int orc_beam_section_dC(int32_t category, int32_t component, const double* sec, double* dC);
+/* dC[36] of the beam section stiffness per unit change of a DV (category 0
+ * modulus, 1 shearModulus, 2 poissonRatio: component 1-3; 3 area, 4
+ * areaMoment component 1-5, 5 polarMoment, with the element's E and nu). */
+int orc_beam_section_dC(int32_t category, int32_t component, double E, double nu, const double* sec, double* dC);
 
 /* Element-category objective term at the element centroids (category 0
  * stress, 1 strain, 2 strainEnergy; component 1-6 for 0/1; optr 0 powerNorm,

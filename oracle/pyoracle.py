@@ -79,7 +79,7 @@ def load():
             "orc_set_shell_sections": (C.c_int, [C.c_void_p, P_d, P_d]),
             "orc_set_beam_sections": (C.c_int, [C.c_void_p, P_d]),
             "orc_beam_element": (C.c_int, [P_d, C.c_double, C.c_double, C.c_double, P_d, P_d, P_d]),
-            "orc_beam_section_dC": (C.c_int, [C.c_int32, C.c_int32, P_d, P_d]),
+            "orc_beam_section_dC": (C.c_int, [C.c_int32, C.c_int32, C.c_double, C.c_double, P_d, P_d]),
             "orc_beam_element_given": (C.c_int, [P_d, C.c_double, C.c_double, C.c_double, P_d, P_d, P_d, P_d]),
             "orc_set_beam_section_matrices": (C.c_int, [C.c_void_p, P_d, P_d]),
             "orc_element_objective": (C.c_int, [C.c_void_p, P_d, C.c_int32, P_i, C.c_int32, C.c_int32, C.c_int32,
@@ -406,10 +406,12 @@ def beam_element(xyz, E, nu, rho, sec, given=None):
     return ke.reshape(12, 12), me.reshape(12, 12)
 
 
-def beam_section_dC(category, component, sec):
-    """dC[6][6] of the beam section stiffness per unit change of a material DV."""
+def beam_section_dC(category, component, sec, E=1.0, nu=0.0):
+    """dC[6][6] of the beam section stiffness per unit change of a DV
+    (0 modulus, 1 shearModulus, 2 poissonRatio, 3 area, 4 areaMoment,
+    5 polarMoment; the last three at the element's E and nu)."""
     lib = load()
     sec = np.ascontiguousarray(sec, np.float64)
     dC = np.zeros(36)
-    assert lib.orc_beam_section_dC(int(category), int(component), _p(sec), _p(dC)) == 0
+    assert lib.orc_beam_section_dC(int(category), int(component), float(E), float(nu), _p(sec), _p(dC)) == 0
     return dC.reshape(6, 6)

@@ -193,7 +193,7 @@ def test_beam_material_dvs(gpu_lib, oracle_lib):
     oracle (1e-6 relative, the solves' floor), and the reference's separate
     material DVs on a beam: modulus component 1 (E in EA, EI), shearModulus
     components 1-3 (G in GA, GJ; GA; G I2), poissonRatio (absent from a beam
-    section: zero)."""
+    section: zero), and the section DVs area, areaMoment and polarMoment."""
     n = 20
     p = cantilever(n)
     p.add_elem_set("all", np.arange(n, dtype=np.int32))
@@ -214,8 +214,10 @@ def test_beam_material_dvs(gpu_lib, oracle_lib):
     assert rel(P, Po) < 1e-6
     sec = p.beam_sections[0]
     for cat, comp, name in ((0, 1, "modulus"), (1, 1, "shearModulus"), (1, 2, "shearModulus"),
-                            (1, 3, "shearModulus"), (0, 2, "modulus")):
-        ref = -sum(np.sum(oracle_lib.beam_section_dC(cat, comp, sec) * Po[e]) for e in range(n))
+                            (1, 3, "shearModulus"), (0, 2, "modulus"), (3, 0, "area"), (4, 3, "areaMoment"),
+                            (4, 4, "areaMoment"), (5, 0, "polarMoment")):
+        ref = -sum(np.sum(oracle_lib.beam_section_dC(cat, comp, sec, E=p.E[e], nu=p.nu[e]) * Po[e])
+                   for e in range(n))
         got = g.material_dv_gradient(name, comp, "all")
         assert got == pytest.approx(ref, rel=1e-6, abs=1e-12 * abs(gE).max()), (name, comp)
     assert g.material_dv_gradient("poissonRatio", 1, "all") == 0.0

@@ -266,3 +266,34 @@ def test_given_section_matrices(oracle_lib):
     assert t1[2] == pytest.approx(t2[2], rel=1e-9)
     _, _, rc, _ = o1.adjoint(u1, dLdu=np.ones(o1.n_dof), precond=oracle_lib.PC_DIRECT)
     assert rc == -2
+
+
+def test_section_dvs_against_differences(oracle_lib):
+    """The reference's beam section DVs (area, areaMoment, polarMoment) through
+    the section-strain pairs, against central differences of the oracle on
+    L = tip w + tip twist under a tip force and torque (step 1e-3; 1e-4: the
+    penalty scale follows max|K|, which moves with A, a 1e-5 effect that the
+    adjoint, like the reference's, leaves out)."""
+    n = 20
+    F = (0.0, 0.0, 2.0, 0.3, 0.0, 0.0)
+
+    def objective(scale_col=None, h=0.0):
+        p = cantilever(n, F=F)
+        if scale_col is not None:
+            p.beam_sections = p.beam_sections.copy()
+            p.beam_sections[:, scale_col] *= 1.0 + h
+        t, u, o = tip_solution(oracle_lib, p)
+        return t[2] + t[3], u, o, p
+
+    L0, u, o, p = objective()
+    dldu = np.zeros(o.n_dof)
+    dldu[6 * n + 2] = dldu[6 * n + 3] = 1.0
+    lam, _, _ = o.solve(dldu, precond=oracle_lib.PC_DIRECT)
+    P = o.strain_pairs(u, lam)
+    sec = p.beam_sections[0]
+    for cat, comp, col in ((3, 0, 0), (4, 3, 3), (5, 0, 6)):
+        dC = oracle_lib.beam_section_dC(cat, comp, sec, E=E0, nu=0.0)
+        g = -sum(np.sum(dC * P[e]) for e in range(n))
+        h = 1e-3
+        fd = (objective(col, h)[0] - objective(col, -h)[0]) / (2 * h * sec[col])
+        assert g == pytest.approx(fd, rel=1e-4), (cat, comp)
