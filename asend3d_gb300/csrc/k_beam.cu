@@ -391,6 +391,9 @@ void beam_assemble(Ctx& c, double* vals, double* mvals) {
 
 void beam_adjoint(Ctx& c, const double* d_u, const double* d_lam, double* d_g, bool accumulate) {
     require_sections(c);
+    if (c.beam_given_stiffness())
+        throw InputError("given beam section stiffness matrices have no per-element modulus gradient "
+                         "(K is not proportional to E)");
     k_beam_adjoint<<<(c.n_el + kBT - 1) / kBT, kBT, 0, c.stream>>>(c.n_el, c.d_shell_conn.p, c.d_shell_xyz.p, c.d_E.p,
                                                                    c.d_nu.p, c.d_beam_sec.p, d_u, d_lam, d_g,
                                                                    accumulate ? 1 : 0);

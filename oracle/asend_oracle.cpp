@@ -2367,6 +2367,9 @@ int orc_newmark_adjoint(orc_model* m, int32_t n_steps, double dt, double beta, d
                         const double* obj_w, double* L_out, double* gE) {
     if (!m->assembled || !m->dynamic || m->cM == 0.0 || n_steps < 1) return -1;
     if (m->cD != 0.0 || m->lump || !m->cmat.empty()) return -2;  // undamped consistent-mass isotropic models
+    if (!m->shell_abd81.empty()) return -2;                        // K proportional to E only
+    for (size_t e = 0; e < m->beam_cm.size() / 72; ++e)
+        if (m->beam_cm[e * 72] > 0.0) return -2;
     const int n = m->n_dof;
     std::vector<double> u(n, 0.0), v(n, 0.0), a(n, 0.0), up(n, 0.0), vp(n, 0.0), ap(n, 0.0);
     std::vector<double> load(n), du(n), tmp(n), ku(n);
